@@ -1,0 +1,83 @@
+// Shared helpers of libffs_reml: status/error plumbing, warp reductions and the
+// bf16 hi/lo split used by the tensor-core projection.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/ffs_reml.h"
+
+namespace ffsk {
+
+// Records a message for ffs_last_error() on the calling host thread.
+void set_error(const char* fmt, ...);
+void clear_error();
+
+// Returns FFS_ERR_CUDA (with the CUDA message recorded) if a launch failed.
+int check_launch(const char* what);
+
+#define FFS_REQUIRE(cond, ...)                 \
+  do {                                         \
+    if (!(cond)) {                             \
+      ::ffsk::set_error(__VA_ARGS__);           \
+      return FFS_ERR_INVALID;                  \
+    }                                          \
+  } while (0)
+
+#define FFS_CUDA(call)                                                        \
+  do {                                                                        \
+    cudaError_t _e = (call);                                                  \
+    if (_e != cudaSuccess) {                                                  \
+      ::ffsk::set_error("%s: %s", #call, cudaGetErrorString(_e));              \
+      return FFS_ERR_CUDA;                                                    \
+    }                                                                         \
+  } while (0)
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// x ~ hi + lo with hi = bf16(x), lo = bf16(x - hi): about 16 significant bits.
+__device__ __forceinline__ void split_bf16(float x, uint16_t& hi, uint16_t& lo) {
+  __nv_bfloat16 h = __float2bfloat16_rn(x);
+  float r = __fsub_rn(x, __bfloat162float(h));
+  __nv_bfloat16 l = __float2bfloat16_rn(r);
+  hi = __bfloat16_as_ushort(h);
+  lo = __bfloat16_as_ushort(l);
+}
+
+// float32 lambda in the reference's operation order, no contraction:
+// (a+b)*(1+a*b) / ((1+b*b) + (2*a)*b)
+__device__ __forceinline__ float lambda_f32(float a, float b) {
+  float num = __fmul_rn(__fadd_rn(a, b), __fadd_rn(1.0f, __fmul_rn(a, b)));
+  float den = __fadd_rn(__fadd_rn(1.0f, __fmul_rn(b, b)), __fmul_rn(__fmul_rn(2.0f, a), b));
+  return __fdiv_rn(num, den);
+}
+
+__device__ __forceinline__ double lambda_f64(double a, double b) {
+  double num = __dmul_rn(__dadd_rn(a, b), __dadd_rn(1.0, __dmul_rn(a, b)));
+  double den = __dadd_rn(__dadd_rn(1.0, __dmul_rn(b, b)), __dmul_rn(__dmul_rn(2.0, a), b));
+  return __ddiv_rn(num, den);
+}
+
+// The per-voxel output lambda: (b+a)*(1+a*b) / (((1+(2a)b) + b*b) + 1e-10), float32.
+__device__ __forceinline__ float lambda_out_f32(float a, float b) {
+  float num = __fmul_rn(__fadd_rn(b, a), __fadd_rn(1.0f, __fmul_rn(a, b)));
+  float den = __fadd_rn(__fadd_rn(__fadd_rn(1.0f, __fmul_rn(__fmul_rn(2.0f, a), b)), __fmul_rn(b, b)),
+                        1e-10f);
+  return __fdiv_rn(num, den);
+}
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace ffsk

@@ -1,0 +1,378 @@
+// K1: FP64 factorisation of the REML grid, one CTA per (a, b) pair.
+//
+// The ARMA(1,1) correlation of a run, R_ij = rho(|tau_i - tau_j|) with
+// rho(0) = 1, rho(k) = lambda a^(k-1), becomes tridiagonal after the AR filter
+// z_t = y_t - c_t y_{t-1}, c_t = a^(tau_t - tau_{t-1}) (c = 0 at a run start):
+//   T_tt      = 1 + c_t^2 - 2 c_t rho(g_t)      (1 at a run start)
+//   T_t,t-1   = rho(g_t) - c_t                  (g_t = tau_t - tau_{t-1})
+// and every other entry is zero, censoring gaps included. Its LDL' factor
+// (unit bidiagonal L~ with sub-diagonal m_t, diagonal D_t) gives the Cholesky
+// factor of R exactly: chol(R) = A^-1 L~ D^1/2, A the unit bidiagonal AR filter.
+// So diag(chol(R)) = sqrt(D_t) and log|R| = 2 sum log(sqrt(D_t) + 1e-10), the
+// same quantity fastfuncstuff/glm/whiten.py:219-223 takes from a dense
+// Cholesky, at O(T) cost instead of O(T^3).
+//
+// The design-dependent part follows fastfuncstuff/glm/arma.py:1459-1506:
+// X_w = L^-1 X, Cholesky of X_w'X_w (QR when it is not positive definite),
+// Q = X_w L_xtx^-T, logdet = 2 sum log(|diag| + 1e-10). On top of that the
+// kernel emits U = L^-T Q (the projection that lets the search skip the
+// whitening GEMM) and G = U L_xtx^-1 (the GLS solve), and the per-pair GLS
+// constants of fastfuncstuff/glm/arma.py:4853-4905.
+#include "common.cuh"
+
+namespace ffsk {
+
+namespace {
+
+struct PairScratch {
+  double* cm;  // [T][4]  c, m, D, 1/sqrt(D)
+  double* Xw;  // [K][T]  whitened design, later U = L^-T Q
+  double* Qm;  // [K][T]  Q
+  double* Lx;  // [K][K]  Cholesky factor of X_w'X_w (lower, row-major)
+  double* Li;  // [K][K]  its inverse
+  double* A;   // [K][K]  (X_w'X_w)^-1
+  double* S;   // [K][K]  scratch for the task block
+};
+
+__host__ __device__ inline size_t pair_doubles(int T, int K) {
+  return (size_t)4 * T + (size_t)2 * K * T + (size_t)4 * K * K;
+}
+
+__device__ PairScratch scratch_of(double* work, int p, int T, int K) {
+  PairScratch s;
+  double* w = work + (size_t)p * pair_doubles(T, K);
+  s.cm = w;
+  s.Xw = s.cm + 4 * T;
+  s.Qm = s.Xw + (size_t)K * T;
+  s.Lx = s.Qm + (size_t)K * T;
+  s.Li = s.Lx + (size_t)K * K;
+  s.A = s.Li + (size_t)K * K;
+  s.S = s.A + (size_t)K * K;
+  return s;
+}
+
+__device__ double block_sum(double v, double* red) {
+  v = warp_sum_d(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < 32) {
+    t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+    t = warp_sum_d(t);
+    if (threadIdx.x == 0) red[0] = t;
+  }
+  __syncthreads();
+  return red[0];
+}
+
+// In-place right-looking Cholesky of the leading n x n block of M (row stride
+// ld, lower triangle used). Returns false if a pivot is not positive
+// (LAPACK potrf's failure test).
+__device__ bool block_cholesky(double* M, int n, int ld, int* flag) {
+  if (threadIdx.x == 0) *flag = 0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      double d = M[k * ld + k];
+      if (!(d > 0.0)) *flag = 1;
+      M[k * ld + k] = d > 0.0 ? sqrt(d) : 1.0;
+    }
+    __syncthreads();
+    if (*flag) return false;
+    const double dk = M[k * ld + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) M[i * ld + k] /= dk;
+    __syncthreads();
+    const int m = n - k - 1;
+    for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+      const int i = k + 1 + idx / m, j = k + 1 + idx % m;
+      if (j <= i) M[i * ld + j] -= M[i * ld + k] * M[j * ld + k];
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// Li = L^-1 for lower-triangular L (n x n, row stride ld); column-parallel.
+__device__ void block_tri_inverse(const double* L, double* Li, int n, int ld) {
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    for (int i = 0; i < c; ++i) Li[i * ld + c] = 0.0;
+    for (int i = c; i < n; ++i) {
+      double s = (i == c) ? 1.0 : 0.0;
+      for (int k = c; k < i; ++k) s -= L[i * ld + k] * Li[k * ld + c];
+      const double d = L[i * ld + i];
+      Li[i * ld + c] = d != 0.0 ? s / d : 0.0;
+    }
+  }
+  __syncthreads();
+}
+
+struct BuildArgs {
+  ffs_grid_desc d;
+  ffs_grid_out o;
+};
+
+__global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
+  const ffs_grid_desc& d = args.d;
+  const ffs_grid_out& o = args.o;
+  const int p = blockIdx.x;
+  const int T = d.T, K = d.K;
+  PairScratch s = scratch_of(o.work, p, T, K);
+
+  __shared__ double red[32];
+  __shared__ double run_ld[64];
+  __shared__ int flag, bad_r;
+
+  const float af = d.a[p], bf = d.b[p];
+  const double a = (double)af;
+  const double lam = d.lambda_fp32 ? (double)lambda_f32(af, bf) : lambda_f64(a, (double)bf);
+  if (threadIdx.x == 0) bad_r = 0;
+  __syncthreads();
+
+  // ---- 1. per-run LDL' of the AR-filtered tridiagonal correlation
+  double ld_local = 0.0;
+  for (int r = threadIdx.x; r < d.n_runs; r += blockDim.x) {
+    const int t0 = d.run_start[r], t1 = d.run_start[r + 1];
+    double Dprev = 1.0, ld = 0.0;
+    for (int t = t0; t < t1; ++t) {
+      double c = 0.0, m = 0.0, D = 1.0;
+      if (t > t0) {
+        const int gap = d.tau[t] - d.tau[t - 1];
+        c = pow(a, (double)gap);
+        const double rho = lam * pow(a, (double)(gap - 1));
+        const double Ttt = 1.0 + c * c - 2.0 * c * rho;
+        const double Toff = rho - c;
+        m = Toff / Dprev;
+        D = Ttt - m * Toff;
+      }
+      if (!(D > 0.0)) {
+        bad_r = 1;
+        D = 1.0;
+      }
+      const double sD = sqrt(D);
+      const double rsD = 1.0 / sD;
+      ld += 2.0 * log(sD + 1e-10);
+      double* cm = s.cm + 4 * t;
+      cm[0] = c; cm[1] = m; cm[2] = D; cm[3] = rsD;
+      reinterpret_cast<float4*>(o.coef)[(size_t)p * T + t] =
+          make_float4((float)c, (float)m, (float)(1.0 / D), (float)rsD);
+      Dprev = D;
+    }
+    if (r < 64) run_ld[r] = ld; else ld_local += ld;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ld = 0.0;
+    for (int r = 0; r < min(d.n_runs, 64); ++r) ld += run_ld[r];
+    red[1] = ld;
+  }
+  __syncthreads();
+  {
+    // runs beyond 64 (rare) are summed through a block reduction
+    const double extra = block_sum(ld_local, red + 2);
+    if (threadIdx.x == 0) o.logdet_R[p] = red[1] + extra;
+  }
+
+  // ---- 2. X_w = L^-1 X, one column per thread
+  for (int j = threadIdx.x; j < K; j += blockDim.x) {
+    double xp = 0.0, vp = 0.0;
+    for (int t = 0; t < T; ++t) {
+      const double* cm = s.cm + 4 * t;
+      const double x = (double)d.X[(size_t)t * K + j];
+      const double z = x - cm[0] * xp;
+      const double v = z - cm[1] * vp;
+      s.Xw[(size_t)j * T + t] = v * cm[3];
+      xp = x;
+      vp = v;
+    }
+  }
+  __syncthreads();
+
+  // ---- 3. X_w'X_w (full symmetric) into Lx, and the fp32 copy
+  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
+    const int i = idx / K, j = idx % K;
+    if (j > i) continue;
+    const double* xi = s.Xw + (size_t)i * T;
+    const double* xj = s.Xw + (size_t)j * T;
+    double acc = 0.0;
+    for (int t = 0; t < T; ++t) acc += xi[t] * xj[t];
+    s.Lx[i * K + j] = acc;
+    s.Lx[j * K + i] = acc;
+    o.XtX[(size_t)p * K * K + i * K + j] = (float)acc;
+    o.XtX[(size_t)p * K * K + j * K + i] = (float)acc;
+  }
+  __syncthreads();
+
+  // ---- 4. Cholesky of X_w'X_w, QR (modified Gram-Schmidt, twice) otherwise
+  int info = 0;
+  if (!block_cholesky(s.Lx, K, K, &flag)) {
+    info = 1;
+    // Q and R from X_w; Lx := R' (lower), so that X_w'X_w = Lx Lx'.
+    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) s.Lx[idx] = 0.0;
+    __syncthreads();
+    for (int j = 0; j < K; ++j) {
+      double* q = s.Qm + (size_t)j * T;
+      for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] = s.Xw[(size_t)j * T + t];
+      __syncthreads();
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int i = 0; i < j; ++i) {
+          const double* qi = s.Qm + (size_t)i * T;
+          double part = 0.0;
+          for (int t = threadIdx.x; t < T; t += blockDim.x) part += qi[t] * q[t];
+          const double rij = block_sum(part, red);
+          for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] -= rij * qi[t];
+          if (threadIdx.x == 0) s.Lx[j * K + i] += rij;
+          __syncthreads();
+        }
+      }
+      double part = 0.0;
+      for (int t = threadIdx.x; t < T; t += blockDim.x) part += q[t] * q[t];
+      const double nrm = sqrt(block_sum(part, red));
+      const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+      for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] *= inv;
+      if (threadIdx.x == 0) s.Lx[j * K + j] = nrm;
+      __syncthreads();
+    }
+  }
+  if (bad_r) info = 2;
+  __syncthreads();
+
+  if (threadIdx.x == 0) {
+    double ld = 0.0;
+    for (int j = 0; j < K; ++j) ld += 2.0 * log(fabs(s.Lx[j * K + j]) + 1e-10);
+    o.logdet_XtX[p] = ld;
+    o.info[p] = info;
+  }
+
+  // ---- 5. Q = X_w Lx^-T (row by row forward substitution)
+  if (info != 1) {
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+      for (int j = 0; j < K; ++j) {
+        double acc = s.Xw[(size_t)j * T + t];
+        for (int i = 0; i < j; ++i) acc -= s.Lx[j * K + i] * s.Qm[(size_t)i * T + t];
+        s.Qm[(size_t)j * T + t] = acc / s.Lx[j * K + j];
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- 6. U = L^-T Q = A' L~^-T D^-1/2 Q (backward recursions), into Xw's slot
+  for (int j = threadIdx.x; j < K; j += blockDim.x) {
+    const double* q = s.Qm + (size_t)j * T;
+    double* u = s.Xw + (size_t)j * T;
+    double xn = 0.0, mn = 0.0, cn = 0.0;  // x_{t+1}, m_{t+1}, c_{t+1}
+    for (int t = T - 1; t >= 0; --t) {
+      const double* cm = s.cm + 4 * t;
+      const double x = q[t] * cm[3] - mn * xn;
+      const double ut = x - cn * xn;
+      u[t] = ut;
+      const float uf = (float)ut;
+      o.U[((size_t)p * K + j) * T + t] = uf;
+      if (o.U_hi) {
+        uint16_t hi, lo;
+        split_bf16(uf, hi, lo);
+        const size_t row = ((size_t)p * K + j) * d.ld_u;
+        o.U_hi[row + t] = hi;
+        o.U_lo[row + t] = lo;
+      }
+      xn = x;
+      mn = cm[1];
+      cn = cm[0];
+    }
+    if (o.U_hi) {
+      const size_t row = ((size_t)p * K + j) * d.ld_u;
+      for (int t = T; t < d.ld_u; ++t) {
+        o.U_hi[row + t] = 0;
+        o.U_lo[row + t] = 0;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- 7. Lx^-1, A = Lx^-T Lx^-1, diag(A)
+  block_tri_inverse(s.Lx, s.Li, K, K);
+  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
+    const int i = idx / K, j = idx % K;
+    double acc = 0.0;
+    for (int k = max(i, j); k < K; ++k) acc += s.Li[k * K + i] * s.Li[k * K + j];
+    s.A[i * K + j] = acc;
+    if (i == j) o.Adiag[(size_t)p * K + j] = (float)acc;
+  }
+  __syncthreads();
+
+  // ---- 8. G = U Lx^-1: row t of G solves g Lx = u_t; Gsum = G' 1 (FP64)
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    for (int j = 0; j < K; ++j) {
+      double acc = 0.0;
+      for (int i = j; i < K; ++i) acc += s.Xw[(size_t)i * T + t] * s.Li[i * K + j];
+      o.G[((size_t)p * K + j) * T + t] = (float)acc;
+      s.Qm[(size_t)j * T + t] = acc;  // Q is no longer needed: keep G in FP64
+    }
+  }
+  __syncthreads();
+  if (o.Gsum) {
+    for (int j = threadIdx.x; j < K; j += blockDim.x) {
+      double acc = 0.0;
+      for (int t = 0; t < T; ++t) acc += s.Qm[(size_t)j * T + t];
+      o.Gsum[(size_t)p * K + j] = (float)acc;
+    }
+  }
+
+  // ---- 9. task-column F matrix inv(A_task + 1e-8 I) and GLT variances c A c'
+  const int nt = d.n_task;
+  if (nt > 0 && o.Ftask) {
+    for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
+      const int i = idx / nt, j = idx % nt;
+      s.S[i * nt + j] = s.A[d.task_idx[i] * K + d.task_idx[j]] + (i == j ? 1e-8 : 0.0);
+    }
+    __syncthreads();
+    block_cholesky(s.S, nt, nt, &flag);
+    // Li (free now) holds the inverse factor; Ftask = Li' Li
+    block_tri_inverse(s.S, s.Li, nt, nt);
+    for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
+      const int i = idx / nt, j = idx % nt;
+      double acc = 0.0;
+      for (int k = max(i, j); k < nt; ++k) acc += s.Li[k * nt + i] * s.Li[k * nt + j];
+      o.Ftask[(size_t)p * nt * nt + idx] = (float)acc;
+    }
+  }
+  if (d.n_glt > 0 && o.glt_var) {
+    for (int c = 0; c < d.n_glt; ++c) {
+      const float* gc = d.glt + (size_t)c * K;
+      double part = 0.0;
+      for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x)
+        part += (double)gc[idx / K] * s.A[idx] * (double)gc[idx % K];
+      const double v = block_sum(part, red);
+      if (threadIdx.x == 0) o.glt_var[(size_t)p * d.n_glt + c] = (float)v;
+    }
+  }
+}
+
+}  // namespace
+
+}  // namespace ffsk
+
+extern "C" size_t ffs_grid_work_bytes(int T, int K, int P) {
+  return sizeof(double) * ffsk::pair_doubles(T, K) * (size_t)P;
+}
+
+extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream) {
+  using namespace ffsk;
+  clear_error();
+  FFS_REQUIRE(d && o, "ffs_grid_build: null descriptor");
+  FFS_REQUIRE(d->T > 0 && d->K > 0 && d->P > 0 && d->n_runs > 0,
+              "ffs_grid_build: T=%d K=%d P=%d n_runs=%d must be positive", d->T, d->K, d->P,
+              d->n_runs);
+  FFS_REQUIRE(d->K <= d->T, "ffs_grid_build: K=%d exceeds T=%d", d->K, d->T);
+  FFS_REQUIRE(d->n_task >= 0 && d->n_task <= d->K, "ffs_grid_build: bad n_task=%d", d->n_task);
+  FFS_REQUIRE(!o->U_hi || (d->ld_u >= d->T && d->ld_u % 8 == 0),
+              "ffs_grid_build: ld_u=%d must be >= T and a multiple of 8", d->ld_u);
+  FFS_REQUIRE(d->run_start && d->tau && d->a && d->b && d->X, "ffs_grid_build: null input");
+  FFS_REQUIRE(o->coef && o->logdet_R && o->logdet_XtX && o->U && o->G && o->Adiag && o->XtX &&
+                  o->info && o->work,
+              "ffs_grid_build: null output");
+  BuildArgs args{*d, *o};
+  grid_build_kernel<<<d->P, 256, 0, (cudaStream_t)stream>>>(args);
+  return check_launch("grid_build_kernel");
+}

@@ -1,0 +1,312 @@
+// Projection GEMM on the 5th-generation tensor cores.
+//
+//   proj[p][v] = sum_{j<K} ( sum_t Y_r[v][t] U[p*K + j][t] )^2
+//
+// is the ||Q'Y_w||^2 term of the REML criterion (fastfuncstuff/glm/arma.py:
+// 1992-1995) for every voxel and every pair at once, since Q'L^-1 y = U'y with
+// U = L^-T Q. Operands are bf16 hi/lo splits of Y_r (voxel-major) and U, so the
+// contraction runs as three tcgen05.mma products per k-step (hi*hi, hi*lo,
+// lo*hi) accumulating in fp32 in tensor memory; dropping lo*lo leaves a
+// relative error near 2^-17 per product.
+//
+// CTA tile: 128 voxels x N columns (g whole pairs, N = roundup16(g*K) <= 256).
+// Warp 0 issues TMA loads (128B-swizzled boxes of 64 k-elements), warp 1 owns
+// TMEM and issues the MMAs from one thread, warps 2-5 square and sum each
+// pair's K columns straight out of TMEM and store proj. Nothing but proj
+// returns to global memory. All mbarrier waits are bounded: on expiry a flag is
+// raised and the CTA winds down instead of spinning.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "common.cuh"
+
+namespace ffsk {
+namespace {
+
+constexpr int BM = 128;         // voxels per tile (TMEM lanes)
+constexpr int BK = 64;          // k elements per stage (one 128-byte swizzle row)
+constexpr int STAGES = 2;
+constexpr int A_TILE = BM * BK * 2;  // bytes of one A box (hi or lo)
+constexpr uint32_t WAIT_LIMIT = 1u << 22;
+
+struct TcParams {
+  int V, K, P, ld;     // ld: padded k extent (multiple of BK)
+  int g, N;            // pairs per column tile, MMA N
+  int n_col_tiles;
+  float* proj;
+  int* flag;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// Bounded parity wait; returns false if the limit expired.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 bytes (stride byte offset 1024), descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)1 << 46;              // version
+  d |= (uint64_t)2 << 61;              // SWIZZLE_128B
+  return d;
+}
+
+// kind::f16 instruction descriptor: fp32 accumulator, bf16 A and B, both
+// K-major, M = 128.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__global__ void __launch_bounds__(192, 1)
+    project_tc_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
+                      const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
+                      TcParams prm) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int b_tile = prm.N * BK * 2;
+  const int stage_bytes = 2 * A_TILE + 2 * b_tile;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
+  uint64_t* empty = full + STAGES;
+  uint64_t* done = empty + STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  __shared__ int abort_cta;
+
+  // a CTA that finds an earlier CTA's wait expired does nothing
+  if (*reinterpret_cast<volatile int*>(prm.flag) != 0) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int col_tile = blockIdx.x, vox_tile = blockIdx.y;
+  const int p_first = col_tile * prm.g;
+  const int v0 = vox_tile * BM;
+  const int nk = prm.ld / BK;
+
+  if (threadIdx.x == 0) {
+    abort_cta = 0;
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES && !mbar_wait(empty + s, ((kb / STAGES) - 1) & 1)) {
+        atomicExch(prm.flag, 1);
+        abort_cta = 1;
+        break;
+      }
+      uint8_t* st = smem + s * stage_bytes;
+      mbar_expect_tx(full + s, (uint32_t)stage_bytes);
+      const int k0 = kb * BK;
+      tma_load_2d(st, &ta_hi, full + s, k0, v0);
+      tma_load_2d(st + A_TILE, &ta_lo, full + s, k0, v0);
+      tma_load_2d(st + 2 * A_TILE, &tb_hi, full + s, k0, p_first * prm.K);
+      tma_load_2d(st + 2 * A_TILE + b_tile, &tb_lo, full + s, k0, p_first * prm.K);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
+    const uint32_t idesc = idesc_bf16(BM, prm.N);
+    bool ok = true;
+    for (int kb = 0; kb < nk && ok; ++kb) {
+      const int s = kb % STAGES;
+      if (!mbar_wait(full + s, (kb / STAGES) & 1)) {
+        atomicExch(prm.flag, 2);
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      uint8_t* st = smem + s * stage_bytes;
+      const uint64_t a_hi = sdesc(smem_u32(st));
+      const uint64_t a_lo = sdesc(smem_u32(st + A_TILE));
+      const uint64_t b_hi = sdesc(smem_u32(st + 2 * A_TILE));
+      const uint64_t b_lo = sdesc(smem_u32(st + 2 * A_TILE + b_tile));
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk) {
+        const uint64_t off = (uint64_t)((kk * 32) >> 4);  // 16 bf16 = 32 bytes along k
+        const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
+        mma_bf16(tmem, a_hi + off, b_hi + off, idesc, acc0);
+        mma_bf16(tmem, a_hi + off, b_lo + off, idesc, 1u);
+        mma_bf16(tmem, a_lo + off, b_hi + off, idesc, 1u);
+      }
+      mma_commit(empty + s);
+    }
+    mma_commit(done);
+  } else if (warp >= 2) {
+    // ---- epilogue: square and sum each pair's K columns from TMEM
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int row = q * 32 + lane;
+    const int v = v0 + row;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
+    if (!ok && lane == 0) atomicExch(prm.flag, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+      const int ncols = prm.g * prm.K;
+      int j = 0, pl = 0;
+      float run = 0.f;
+      for (int c0 = 0; c0 < prm.N; c0 += 16) {
+        uint32_t r[16];
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+              "=r"(r[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          if (c0 + i < ncols) {
+            const float x = __uint_as_float(r[i]);
+            run = fmaf(x, x, run);
+            if (++j == prm.K) {
+              const int p = p_first + pl;
+              if (p < prm.P && v < prm.V) prm.proj[(size_t)p * prm.V + v] = run;
+              run = 0.f;
+              j = 0;
+              ++pl;
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+int make_map(CUtensorMap* m, const void* base, int inner, int rows, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return FFS_ERR_CUDA;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)inner * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d) for a %d x %d bf16 operand", (int)r, rows, inner);
+    return FFS_ERR_CUDA;
+  }
+  return FFS_OK;
+}
+
+}  // namespace
+}  // namespace ffsk
+
+using namespace ffsk;
+
+extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
+  clear_error();
+  FFS_REQUIRE(a && a->V > 0 && a->T > 0 && a->K > 0 && a->P > 0, "ffs_reml_project_tc: bad sizes");
+  FFS_REQUIRE(a->yr_hi && a->yr_lo && a->u_hi && a->u_lo && a->proj && a->flag,
+              "ffs_reml_project_tc: null buffer");
+  FFS_REQUIRE(a->ld_y == a->ld_u && a->ld_y % BK == 0 && a->ld_y >= a->T,
+              "ffs_reml_project_tc: ld_y=%d and ld_u=%d must be equal multiples of %d", a->ld_y, a->ld_u, BK);
+  if (a->K > 256) {
+    set_error("ffs_reml_project_tc: K=%d exceeds one 256-column MMA tile", a->K);
+    return FFS_ERR_UNSUPPORTED;
+  }
+  for (const void* ptr : {(const void*)a->yr_hi, (const void*)a->yr_lo, (const void*)a->u_hi, (const void*)a->u_lo})
+    FFS_REQUIRE(((uintptr_t)ptr & 15) == 0, "ffs_reml_project_tc: operands must be 16-byte aligned");
+  TcParams prm;
+  prm.V = a->V;
+  prm.K = a->K;
+  prm.P = a->P;
+  prm.ld = a->ld_y;
+  prm.g = 256 / a->K;
+  if (prm.g > a->P) prm.g = a->P;
+  prm.N = ((prm.g * a->K) + 15) / 16 * 16;
+  prm.n_col_tiles = ceil_div(a->P, prm.g);
+  prm.proj = a->proj;
+  prm.flag = a->flag;
+  CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;
+  int st;
+  if ((st = make_map(&ta_hi, a->yr_hi, a->ld_y, a->V, BM))) return st;
+  if ((st = make_map(&ta_lo, a->yr_lo, a->ld_y, a->V, BM))) return st;
+  if ((st = make_map(&tb_hi, a->u_hi, a->ld_u, a->P * a->K, prm.N))) return st;
+  if ((st = make_map(&tb_lo, a->u_lo, a->ld_u, a->P * a->K, prm.N))) return st;
+  const int stage_bytes = 2 * A_TILE + 2 * prm.N * BK * 2;
+  const size_t smem = (size_t)STAGES * stage_bytes + 1024 + 64;
+  FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_project_tc: tile needs %zu bytes of shared memory", smem);
+  FFS_CUDA(cudaFuncSetAttribute(project_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid(prm.n_col_tiles, ceil_div(a->V, BM));
+  project_tc_kernel<<<grid, 192, smem, (cudaStream_t)stream>>>(ta_hi, ta_lo, tb_hi, tb_lo, prm);
+  return check_launch("project_tc_kernel");
+}

@@ -1,0 +1,369 @@
+// Search-side kernels of the REML grid search:
+//   prep     per-voxel std scaling + residualisation against the design
+//   surface  y'R^-1 y by the O(T) recurrence for every (voxel, pair) and the
+//            REML criterion, relative to the pair (0, 0)
+//   select   exhaustive argmin or AFNI's hierarchical descent
+//   group    counting sort of voxels by their chosen pair
+//   project  (CUDA-core form) ||U'y||^2 for every (voxel, pair)
+#include "common.cuh"
+
+namespace ffsk {
+
+namespace {
+
+// ------------------------------------------------------------------------ prep
+// 8 warps, 32 voxels per CTA (4 per warp). The residualised rows are staged in
+// shared memory and written out time-major in coalesced 128-byte rows.
+constexpr int PREP_VOX = 32;
+
+__global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
+  extern __shared__ float sm[];  // [PREP_VOX][ld_s]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int T = a.T, K = a.K;
+  const int v0 = blockIdx.x * PREP_VOX;
+  for (int k = 0; k < PREP_VOX / 8; ++k) {
+    const int lv = wid * (PREP_VOX / 8) + k;
+    const int v = v0 + lv;
+    if (v >= a.V) break;  // warp-uniform
+    float* row = sm + (size_t)lv * ld_s;
+    const float* y = a.Y + (size_t)v * T;
+    // mean and (N-1) variance, two passes for accuracy
+    float s = 0.f;
+    for (int t = lane; t < T; t += 32) {
+      const float x = y[t];
+      row[t] = x;
+      s += x;
+    }
+    const float mean = warp_sum(s) / (float)T;
+    float q = 0.f;
+    for (int t = lane; t < T; t += 32) {
+      const float dlt = row[t] - mean;
+      q += dlt * dlt;
+    }
+    q = warp_sum(q);
+    float sc = 1.0f;
+    if (a.do_scale) {
+      sc = T > 1 ? sqrtf(q / (float)(T - 1)) : 0.f;
+      sc = fmaxf(sc, 1e-8f);
+    }
+    // centring is one subtraction per sample, rounded relative to its (small)
+    // result; the criterion ignores the constant when it lies in span(X)
+    const float m = a.center ? mean : 0.f;
+    for (int t = lane; t < T; t += 32) row[t] = __fdiv_rn(__fsub_rn(row[t], m), sc);
+    __syncwarp();
+    // residualise: row -= Q0 (Q0' row)
+    for (int j = 0; j < K; ++j) {
+      const float* qj = a.Q0 + (size_t)j * T;
+      float c = 0.f;
+      for (int t = lane; t < T; t += 32) c += qj[t] * row[t];
+      c = warp_sum(c);
+      for (int t = lane; t < T; t += 32) row[t] -= c * qj[t];
+      __syncwarp();
+    }
+    if (lane == 0) a.scale[v] = sc;
+    if (a.yr_hi) {
+      uint16_t* hi = a.yr_hi + (size_t)v * a.ld_y;
+      uint16_t* lo = a.yr_lo + (size_t)v * a.ld_y;
+      for (int t = lane; t < a.ld_y; t += 32) {
+        uint16_t h = 0, l = 0;
+        if (t < T) split_bf16(row[t], h, l);
+        hi[t] = h;
+        lo[t] = l;
+      }
+    }
+  }
+  __syncthreads();
+  // time-major store: warp w writes rows t = w, w+8, ...; lane = voxel
+  const int nv = min(PREP_VOX, a.V - v0);
+  for (int t = wid; t < T; t += 8) {
+    if (lane < nv) a.yr_t[(size_t)t * a.V + v0 + lane] = sm[(size_t)lane * ld_s + t];
+  }
+}
+
+// --------------------------------------------------------------------- surface
+// One thread per voxel, one CTA per (voxel tile, chunk of pairs sharing a).
+// For each pair g of the chunk: v_t = z_t - m_t v_{t-1}, s += v_t^2 / D_t.
+constexpr int SURF_G = 16;
+constexpr int SURF_THREADS = 128;
+
+__global__ void __launch_bounds__(SURF_THREADS) surface_kernel(ffs_surface_args a) {
+  extern __shared__ float2 cf[];  // [T][SURF_G] (m, 1/D)
+  float* cs = reinterpret_cast<float*>(cf + (size_t)a.T * SURF_G);  // [T] c_t
+  const int chunk = blockIdx.y;
+  const int c0 = a.chunk_start[chunk], c1 = a.chunk_start[chunk + 1];
+  const int ng = c1 - c0;
+  const int T = a.T;
+  const float4* coef = reinterpret_cast<const float4*>(a.coef);
+  for (int idx = threadIdx.x; idx < T * SURF_G; idx += blockDim.x) {
+    const int t = idx / SURF_G, g = idx % SURF_G;
+    float2 val = make_float2(0.f, 0.f);
+    if (g < ng) {
+      const float4 q = coef[(size_t)a.chunk_pairs[c0 + g] * T + t];
+      val = make_float2(q.y, q.z);
+    }
+    cf[idx] = val;
+  }
+  for (int t = threadIdx.x; t < T; t += blockDim.x)
+    cs[t] = coef[(size_t)a.chunk_pairs[c0] * T + t].x;
+  __syncthreads();
+
+  const int v = blockIdx.x * SURF_THREADS + threadIdx.x;
+  if (v >= a.V) return;
+  float vv[SURF_G], sb[SURF_G], st[SURF_G];
+#pragma unroll
+  for (int g = 0; g < SURF_G; ++g) vv[g] = sb[g] = st[g] = 0.f;
+  float yy_b = 0.f, yy = 0.f, yp = 0.f;
+  const float* yc = a.yr_t + v;
+  for (int t0 = 0; t0 < T; t0 += 32) {
+    const int t1 = min(T, t0 + 32);
+    for (int t = t0; t < t1; ++t) {
+      const float y = yc[(size_t)t * a.V];
+      const float z = fmaf(-cs[t], yp, y);
+      yp = y;
+      yy_b = fmaf(y, y, yy_b);
+      const float2* row = cf + (size_t)t * SURF_G;
+#pragma unroll
+      for (int g = 0; g < SURF_G; ++g) {
+        const float2 q = row[g];
+        vv[g] = fmaf(-q.x, vv[g], z);
+        sb[g] = fmaf(vv[g] * q.y, vv[g], sb[g]);
+      }
+    }
+#pragma unroll
+    for (int g = 0; g < SURF_G; ++g) {
+      st[g] += sb[g];
+      sb[g] = 0.f;
+    }
+    yy += yy_b;
+    yy_b = 0.f;
+  }
+  const int Tk = a.T - a.K;
+  const double c_p0 = a.logdet_R[a.p0] + a.logdet_XtX[a.p0];
+  const float rss0 = fmaxf(yy - a.proj[(size_t)a.p0 * a.V + v], 0.f);
+  const float den = rss0 + 1e-10f;
+  for (int g = 0; g < ng; ++g) {
+    const int p = a.chunk_pairs[c0 + g];
+    const float rss = fmaxf(st[g] - a.proj[(size_t)p * a.V + v], 0.f);
+    const float dc = (float)((a.logdet_R[p] + a.logdet_XtX[p]) - c_p0);
+    const float dv = dc + (float)Tk * log1pf((rss - rss0) / den);
+    a.surf[(size_t)p * a.V + v] = dv;
+  }
+  if (chunk == 0) a.crit0[v] = c_p0 + (double)Tk * log((double)rss0 + 1e-10);
+}
+
+// ---------------------------------------------------------------------- select
+__global__ void select_kernel(ffs_select_args a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.V) return;
+  const float* s = a.surf + v;
+  const size_t V = (size_t)a.V;
+  int best = a.lattice[a.za * a.n_b + a.zb];
+  float bl;
+  if (!a.hierarchical) {
+    bl = INFINITY;
+    for (int p = 0; p < a.P; ++p) {
+      const float d = s[(size_t)p * V];
+      if (d < bl) {
+        bl = d;
+        best = p;
+      }
+    }
+  } else {
+    // AFNI power-of-2 descent from (0, 0) on the (a, b) lattice
+    auto at = [&](int ai, int bi) -> float {
+      const int p = a.lattice[ai * a.n_b + bi];
+      return p < 0 ? INFINITY : s[(size_t)p * V];
+    };
+    int ba = a.za, bb = a.zb;
+    bl = at(ba, bb);
+    for (int lev = a.ltop; lev >= 0; --lev) {
+      const int step = 1 << lev;
+      float mn = INFINITY;
+      int sa = -1, sb = -1;
+      if (lev == a.ltop) {
+        for (int bi = 0; bi < a.n_b; bi += step)
+          for (int ai = 0; ai < a.n_a; ai += step) {
+            const float d = at(ai, bi);
+            if (sa < 0 || d < mn) {
+              mn = d;
+              sa = ai;
+              sb = bi;
+            }
+          }
+      } else {
+        for (int ob = -1; ob <= 1; ++ob) {
+          const int bi = min(max(bb + ob * step, 0), a.n_b - 1);
+          for (int oa = -1; oa <= 1; ++oa) {
+            const int ai = min(max(ba + oa * step, 0), a.n_a - 1);
+            const float d = at(ai, bi);
+            if (sa < 0 || d < mn) {
+              mn = d;
+              sa = ai;
+              sb = bi;
+            }
+          }
+        }
+      }
+      if (mn < bl) {
+        bl = mn;
+        ba = sa;
+        bb = sb;
+      }
+    }
+    best = a.lattice[ba * a.n_b + bb];
+  }
+  a.best[v] = best;
+  a.best_crit[v] = (float)(a.crit0[v] + (double)bl);
+}
+
+// ----------------------------------------------------------------------- group
+__global__ void group_hist(int V, const int* best, int* cnt) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < V) atomicAdd(cnt + best[v], 1);
+}
+
+__global__ void group_scan(int P, int* cnt) {
+  // single CTA exclusive scan of cnt[0..P) in place; cnt[P] = total
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < P; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int x = i < P ? cnt[i] : 0;
+    // block inclusive scan by warps
+    int incl = x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    __shared__ int wsum[32];
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      int w = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    const int before = (wid > 0 ? wsum[wid - 1] : 0) + carry;
+    if (i < P) cnt[i] = before + incl - x;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = before + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cnt[P] = carry;
+}
+
+__global__ void group_scatter(int V, const int* best, int* cursor, int* order) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < V) order[atomicAdd(cursor + best[v], 1)] = v;
+}
+
+// --------------------------------------------------------- projection (CUDA cores)
+// proj[p][v] = sum_j (sum_t U[p][j][t] y_t)^2 with y time-major. CTA = 128
+// voxels x one pair; U columns are staged through shared memory 16 at a time.
+constexpr int PJ_COLS = 16;
+constexpr int PJ_TT = 128;
+
+__global__ void __launch_bounds__(128) project_simt_kernel(ffs_project_args a) {
+  __shared__ float us[PJ_COLS][PJ_TT];
+  const int p = blockIdx.y;
+  const int v = blockIdx.x * 128 + threadIdx.x;
+  const int T = a.T, K = a.K;
+  float total = 0.f;
+  for (int c0 = 0; c0 < K; c0 += PJ_COLS) {
+    const int nc = min(PJ_COLS, K - c0);
+    float acc[PJ_COLS];
+#pragma unroll
+    for (int j = 0; j < PJ_COLS; ++j) acc[j] = 0.f;
+    for (int t0 = 0; t0 < T; t0 += PJ_TT) {
+      const int nt = min(PJ_TT, T - t0);
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < PJ_COLS * PJ_TT; idx += 128) {
+        const int j = idx / PJ_TT, t = idx % PJ_TT;
+        us[j][t] = (j < nc && t < nt) ? a.U[((size_t)p * K + c0 + j) * T + t0 + t] : 0.f;
+      }
+      __syncthreads();
+      if (v < a.V) {
+        const float* yc = a.yr_t + (size_t)t0 * a.V + v;
+        for (int t = 0; t < nt; ++t) {
+          const float y = yc[(size_t)t * a.V];
+#pragma unroll
+          for (int j = 0; j < PJ_COLS; ++j) acc[j] = fmaf(us[j][t], y, acc[j]);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < PJ_COLS; ++j) total = fmaf(acc[j], acc[j], total);
+  }
+  if (v < a.V) a.proj[(size_t)p * a.V + v] = total;
+}
+
+}  // namespace
+
+}  // namespace ffsk
+
+using namespace ffsk;
+
+extern "C" int ffs_reml_prep(const ffs_prep_args* a, void* stream) {
+  clear_error();
+  FFS_REQUIRE(a && a->V > 0 && a->T > 1 && a->K >= 0, "ffs_reml_prep: bad sizes");
+  FFS_REQUIRE(a->Y && a->scale && a->yr_t && (a->K == 0 || a->Q0), "ffs_reml_prep: null buffer");
+  FFS_REQUIRE(!a->yr_hi || (a->yr_lo && a->ld_y >= a->T && a->ld_y % 8 == 0),
+              "ffs_reml_prep: ld_y=%d must be >= T and a multiple of 8", a->ld_y);
+  const int ld_s = a->T + ((a->T & 1) ? 2 : 1);  // odd stride: conflict-free transposed reads
+  const size_t smem = sizeof(float) * PREP_VOX * ld_s;
+  FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_prep: T=%d too long for one tile", a->T);
+  FFS_CUDA(cudaFuncSetAttribute(prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  prep_kernel<<<ceil_div(a->V, PREP_VOX), 256, smem, (cudaStream_t)stream>>>(*a, ld_s);
+  return check_launch("prep_kernel");
+}
+
+extern "C" int ffs_reml_surface(const ffs_surface_args* a, void* stream) {
+  clear_error();
+  FFS_REQUIRE(a && a->V > 0 && a->T > 0 && a->P > 0 && a->n_chunks > 0, "ffs_reml_surface: bad sizes");
+  FFS_REQUIRE(a->p0 >= 0 && a->p0 < a->P, "ffs_reml_surface: p0=%d out of range", a->p0);
+  FFS_REQUIRE(a->yr_t && a->coef && a->logdet_R && a->logdet_XtX && a->proj && a->chunk_start &&
+                  a->chunk_pairs && a->surf && a->crit0,
+              "ffs_reml_surface: null buffer");
+  const size_t smem = (sizeof(float2) * SURF_G + sizeof(float)) * (size_t)a->T;
+  FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_surface: T=%d too long", a->T);
+  FFS_CUDA(cudaFuncSetAttribute(surface_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid(ceil_div(a->V, SURF_THREADS), a->n_chunks);
+  surface_kernel<<<grid, SURF_THREADS, smem, (cudaStream_t)stream>>>(*a);
+  return check_launch("surface_kernel");
+}
+
+extern "C" int ffs_reml_select(const ffs_select_args* a, void* stream) {
+  clear_error();
+  FFS_REQUIRE(a && a->V > 0 && a->P > 0, "ffs_reml_select: bad sizes");
+  FFS_REQUIRE(a->surf && a->crit0 && a->lattice && a->best && a->best_crit, "ffs_reml_select: null buffer");
+  FFS_REQUIRE(a->za >= 0 && a->za < a->n_a && a->zb >= 0 && a->zb < a->n_b,
+              "ffs_reml_select: (0,0) index outside the lattice");
+  select_kernel<<<ceil_div(a->V, 256), 256, 0, (cudaStream_t)stream>>>(*a);
+  return check_launch("select_kernel");
+}
+
+extern "C" int ffs_reml_group(int V, int P, const int* best, int* work, int* order, void* stream) {
+  clear_error();
+  FFS_REQUIRE(V > 0 && P > 0 && best && work && order, "ffs_reml_group: bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  FFS_CUDA(cudaMemsetAsync(work, 0, sizeof(int) * (P + 1), st));
+  group_hist<<<ceil_div(V, 256), 256, 0, st>>>(V, best, work);
+  group_scan<<<1, 1024, 0, st>>>(P, work);
+  group_scatter<<<ceil_div(V, 256), 256, 0, st>>>(V, best, work, order);
+  return check_launch("group kernels");
+}
+
+extern "C" int ffs_reml_project_simt(const ffs_project_args* a, void* stream) {
+  clear_error();
+  FFS_REQUIRE(a && a->V > 0 && a->T > 0 && a->K > 0 && a->P > 0, "ffs_reml_project_simt: bad sizes");
+  FFS_REQUIRE(a->yr_t && a->U && a->proj, "ffs_reml_project_simt: null buffer");
+  dim3 grid(ceil_div(a->V, 128), a->P);
+  project_simt_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(*a);
+  return check_launch("project_simt_kernel");
+}

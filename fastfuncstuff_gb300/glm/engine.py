@@ -1,0 +1,281 @@
+"""Device-side orchestration of the REML kernels (libffs_reml.so).
+
+Every function here works on CUDA tensors, allocates its outputs through
+torch's caching allocator, and launches the library's kernels on torch's
+current stream. Nothing synchronises the device and nothing leaves the GPU, so
+a whole fit can be captured in a CUDA graph (see ``RemlPlan``).
+
+Layouts (V voxels, T time points, K design columns, P pairs):
+  Y        [V][T] fp32 voxel-major data
+  yr_t     [T][V] fp32 residualised, scaled data (time-major, for the O(T)
+           recurrences)
+  yr_hi/lo [V][ld] bf16 bits of the same (the projection GEMM's A operand)
+  U_hi/lo  [P*K][ld] bf16 bits of U = L^-T Q (the GEMM's B operand)
+  proj     [P][V], surf [P][V]
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .grid import RemlGrid, RunLayout
+
+LD_ALIGN = 64  # k extent of one tcgen05 pipeline stage
+
+
+def _p(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def padded_ld(T: int) -> int:
+    return (T + LD_ALIGN - 1) // LD_ALIGN * LD_ALIGN
+
+
+def require_cuda(device) -> torch.device:
+    device = torch.device(device) if device is not None else torch.device("cuda")
+    if device.type != "cuda":
+        raise ValueError(f"fastfuncstuff_gb300 runs on a CUDA device only (got {device})")
+    if not torch.cuda.is_available():
+        raise RuntimeError("fastfuncstuff_gb300 needs a CUDA GPU; none is available")
+    _lib.load()
+    return device
+
+
+@dataclass
+class GridFactors:
+    """Per-pair FP64-derived factors written by ``ffs_grid_build``."""
+
+    grid: RemlGrid
+    T: int
+    K: int
+    ld: int
+    coef: torch.Tensor
+    logdet_R: torch.Tensor
+    logdet_XtX: torch.Tensor
+    U: torch.Tensor
+    U_hi: torch.Tensor | None
+    U_lo: torch.Tensor | None
+    G: torch.Tensor
+    Adiag: torch.Tensor
+    XtX: torch.Tensor
+    info: torch.Tensor
+    Ftask: torch.Tensor | None
+    glt_var: torch.Tensor | None
+    a: torch.Tensor
+    b: torch.Tensor
+    chunk_start: torch.Tensor
+    chunk_pairs: torch.Tensor
+    lattice: torch.Tensor
+    task_idx: torch.Tensor | None
+    glt: torch.Tensor | None
+    Gsum: torch.Tensor | None = None
+    center: bool = False
+
+    @property
+    def P(self) -> int:
+        return self.grid.P
+
+
+def constant_in_span(X: np.ndarray, tol: float = 1e-6) -> bool:
+    """True when the constant series lies in the column span of X (FP64 least squares)."""
+    Xd = np.asarray(X, dtype=np.float64)
+    ones = np.ones(Xd.shape[0])
+    coef, *_ = np.linalg.lstsq(Xd, ones, rcond=None)
+    return float(np.linalg.norm(Xd @ coef - ones)) <= tol * np.sqrt(Xd.shape[0])
+
+
+def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_indices=None,
+                  glt: np.ndarray | None = None, with_tc: bool = True) -> GridFactors:
+    """Run the FP64 grid build for design ``X`` (T, K) on its device.
+
+    lambda is always evaluated in float64 from the float32 (a, b) values (the
+    FP64 fit's value); the fit's mode only decides the validity filter and the
+    reported per-voxel lambda.
+    """
+    dev = X.device
+    T, K = X.shape
+    P = grid.P
+    ld = padded_ld(T)
+    f32 = dict(device=dev, dtype=torch.float32)
+    Xc = X.to(**f32).contiguous()
+    a = torch.from_numpy(grid.a).to(dev)
+    b = torch.from_numpy(grid.b).to(dev)
+    run_start = torch.from_numpy(layout.run_start).to(dev)
+    tau = torch.from_numpy(layout.tau).to(dev)
+    task_idx = None
+    if task_indices is not None and len(task_indices) > 0:
+        task_idx = torch.as_tensor(list(task_indices), dtype=torch.int32, device=dev)
+    glt_t = None if glt is None else torch.as_tensor(np.asarray(glt, np.float32), device=dev).reshape(-1, K)
+    nt = 0 if task_idx is None else task_idx.numel()
+    ng = 0 if glt_t is None else glt_t.shape[0]
+    lib = _lib.load()
+    work = torch.empty(int(lib.ffs_grid_work_bytes(T, K, P)) // 8 + 1, dtype=torch.float64, device=dev)
+    f = GridFactors(
+        grid=grid, T=T, K=K, ld=ld,
+        coef=torch.empty(P, T, 4, **f32),
+        logdet_R=torch.empty(P, dtype=torch.float64, device=dev),
+        logdet_XtX=torch.empty(P, dtype=torch.float64, device=dev),
+        U=torch.empty(P, K, T, **f32),
+        U_hi=torch.empty(P * K, ld, dtype=torch.int16, device=dev) if with_tc else None,
+        U_lo=torch.empty(P * K, ld, dtype=torch.int16, device=dev) if with_tc else None,
+        G=torch.empty(P, K, T, **f32),
+        Adiag=torch.empty(P, K, **f32),
+        XtX=torch.empty(P, K, K, **f32),
+        info=torch.empty(P, dtype=torch.int32, device=dev),
+        Ftask=torch.empty(P, nt, nt, **f32) if nt else None,
+        glt_var=torch.empty(P, ng, **f32) if ng else None,
+        a=a, b=b,
+        chunk_start=torch.from_numpy(grid.chunk_start).to(dev),
+        chunk_pairs=torch.from_numpy(grid.chunk_pairs).to(dev),
+        lattice=torch.from_numpy(grid.lattice.reshape(-1).copy()).to(dev),
+        task_idx=task_idx, glt=glt_t,
+        Gsum=torch.empty(P, K, **f32),
+        center=constant_in_span(X.detach().cpu().numpy()),
+    )
+    d = _lib.GridDesc(T=T, K=K, P=P, n_runs=layout.n_runs, run_start=_p(run_start), tau=_p(tau),
+                      a=_p(a), b=_p(b), X=_p(Xc), lambda_fp32=0, ld_u=ld,
+                      n_task=nt, task_idx=_p(task_idx), n_glt=ng, glt=_p(glt_t))
+    o = _lib.GridOut(coef=_p(f.coef), logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), U=_p(f.U),
+                     U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
+                     info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=_p(f.Gsum),
+                     work=_p(work))
+    _lib.check(lib.ffs_grid_build(C.byref(d), C.byref(o), _stream()), "ffs_grid_build")
+    f._keep = (Xc, run_start, tau, work)  # inputs must outlive the launch
+    return f
+
+
+@dataclass
+class SearchOut:
+    best: torch.Tensor        # [V] int32 pair index
+    best_crit: torch.Tensor   # [V] float32 criterion (scaled-data likelihood)
+    scale: torch.Tensor       # [V] float32 per-voxel std
+    surf: torch.Tensor | None = None   # [P][V] criterion relative to (0,0)
+    crit0: torch.Tensor | None = None  # [V] float64 criterion at (0,0)
+
+
+def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projector: str = "tc",
+           do_scale: bool = True, keep_surface: bool = False) -> SearchOut:
+    """REML grid search of every voxel of ``Y`` (V, T) against the factors ``f``.
+
+    ``projector`` picks the projection kernel: "tc" (tcgen05 split-bf16 GEMM) or
+    "simt" (fp32 CUDA cores).
+    """
+    lib = _lib.load()
+    dev = Y.device
+    V, T = Y.shape
+    K, P, ld = f.K, f.P, f.ld
+    st = _stream()
+    Y = Y.to(dtype=torch.float32).contiguous()
+    scale = torch.empty(V, dtype=torch.float32, device=dev)
+    yr_t = torch.empty(T, V, dtype=torch.float32, device=dev)
+    use_tc = projector == "tc"
+    if use_tc and f.U_hi is None:
+        raise ValueError("the factors were built without the tensor-core operands")
+    yr_hi = torch.empty(V, ld, dtype=torch.int16, device=dev) if use_tc else None
+    yr_lo = torch.empty(V, ld, dtype=torch.int16, device=dev) if use_tc else None
+    q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T])
+    pa = _lib.PrepArgs(V=V, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=int(f.center), ld_y=ld,
+                       scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo))
+    _lib.check(lib.ffs_reml_prep(C.byref(pa), st), "ffs_reml_prep")
+
+    proj = torch.empty(P, V, dtype=torch.float32, device=dev)
+    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    ja = _lib.ProjectArgs(V=V, T=T, K=K, P=P, ld_y=ld, ld_u=ld, yr_hi=_p(yr_hi), yr_lo=_p(yr_lo),
+                          u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yr_t=_p(yr_t), U=_p(f.U), proj=_p(proj),
+                          flag=_p(flag))
+    if use_tc:
+        _lib.check(lib.ffs_reml_project_tc(C.byref(ja), st), "ffs_reml_project_tc")
+    elif projector == "simt":
+        _lib.check(lib.ffs_reml_project_simt(C.byref(ja), st), "ffs_reml_project_simt")
+    else:
+        raise ValueError(f"unknown projector {projector!r}")
+
+    surf = torch.empty(P, V, dtype=torch.float32, device=dev)
+    crit0 = torch.empty(V, dtype=torch.float64, device=dev)
+    sa = _lib.SurfaceArgs(V=V, T=T, K=K, P=P, p0=f.grid.p0, yr_t=_p(yr_t), coef=_p(f.coef),
+                          logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), proj=_p(proj),
+                          chunk_start=_p(f.chunk_start), n_chunks=f.chunk_start.numel() - 1,
+                          chunk_pairs=_p(f.chunk_pairs), surf=_p(surf), crit0=_p(crit0))
+    _lib.check(lib.ffs_reml_surface(C.byref(sa), st), "ffs_reml_surface")
+
+    best = torch.empty(V, dtype=torch.int32, device=dev)
+    best_crit = torch.empty(V, dtype=torch.float32, device=dev)
+    g = f.grid
+    se = _lib.SelectArgs(V=V, P=P, surf=_p(surf), crit0=_p(crit0), hierarchical=int(hierarchical),
+                         n_a=len(g.a_axis), n_b=len(g.b_axis), ltop=g.ltop, za=g.za, zb=g.zb,
+                         lattice=_p(f.lattice), best=_p(best), best_crit=_p(best_crit))
+    _lib.check(lib.ffs_reml_select(C.byref(se), st), "ffs_reml_select")
+    out = SearchOut(best=best, best_crit=best_crit, scale=scale)
+    out._flag = flag
+    if keep_surface:
+        out.surf, out.crit0 = surf, crit0
+    return out
+
+
+@dataclass
+class GlsOut:
+    betas: torch.Tensor   # [V][K] (unscaled)
+    tstats: torch.Tensor  # [V][K]
+    sigma2: torch.Tensor
+    fstats: torch.Tensor
+    r2: torch.Tensor
+    lam: torch.Tensor
+    cbeta: torch.Tensor | None = None
+    ct: torch.Tensor | None = None
+    resid: torch.Tensor | None = None
+    resid_w: torch.Tensor | None = None
+    pred: torch.Tensor | None = None
+    ljung_box: torch.Tensor | None = None
+
+
+def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors, X: torch.Tensor, *,
+        want_residuals: bool = False, want_predicted: bool = False, lj=None) -> GlsOut:
+    """GLS refit of every voxel at its pair ``best`` (indices into ``f``)."""
+    lib = _lib.load()
+    dev = Y.device
+    V, T = Y.shape
+    K, P = f.K, f.P
+    st = _stream()
+    Y = Y.to(dtype=torch.float32).contiguous()
+    order = torch.empty(V, dtype=torch.int32, device=dev)
+    work = torch.empty(P + 1, dtype=torch.int32, device=dev)
+    _lib.check(lib.ffs_reml_group(V, P, _p(best), _p(work), _p(order), st), "ffs_reml_group")
+    Xt = X.to(device=dev, dtype=torch.float32).t().contiguous()
+    f32 = dict(device=dev, dtype=torch.float32)
+    ng = 0 if f.glt is None else f.glt.shape[0]
+    o = GlsOut(betas=torch.empty(V, K, **f32), tstats=torch.empty(V, K, **f32), sigma2=torch.empty(V, **f32),
+               fstats=torch.empty(V, **f32), r2=torch.empty(V, **f32), lam=torch.empty(V, **f32),
+               cbeta=torch.empty(V, ng, **f32) if ng else None, ct=torch.empty(V, ng, **f32) if ng else None,
+               resid=torch.empty(V, T, **f32) if want_residuals else None,
+               resid_w=torch.empty(V, T, **f32) if want_residuals else None,
+               pred=torch.empty(V, T, **f32) if want_predicted else None)
+    nt = 0 if f.task_idx is None else f.task_idx.numel()
+    ga = _lib.GlsArgs(V=V, T=T, K=K, dof=max(1, T - K), center=int(f.center), Gsum=_p(f.Gsum), Y=_p(Y),
+                      scale=_p(scale), Xt=_p(Xt), best=_p(best),
+                      order=_p(order), coef=_p(f.coef), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
+                      a=_p(f.a), b=_p(f.b), lambda_fp32=int(f.grid.lambda_fp32), n_task=nt,
+                      task_idx=_p(f.task_idx), Ftask=_p(f.Ftask), n_glt=ng, glt=_p(f.glt),
+                      glt_var=_p(f.glt_var), betas=_p(o.betas), tstats=_p(o.tstats), sigma2=_p(o.sigma2),
+                      fstats=_p(o.fstats), r2=_p(o.r2), lam=_p(o.lam), cbeta=_p(o.cbeta), ct=_p(o.ct),
+                      resid=_p(o.resid), resid_w=_p(o.resid_w), pred=_p(o.pred))
+    if lj is not None and lj[0] > 0:
+        h, ptau, w, _ = lj
+        ptau_d = None if ptau is None else torch.from_numpy(ptau).to(dev)
+        w_d = torch.from_numpy(w).to(dev)
+        o.ljung_box = torch.empty(V, **f32)
+        _lib.check(lib.ffs_reml_gls_ex(C.byref(ga), h, _p(ptau_d), _p(w_d), _p(o.ljung_box), st),
+                   "ffs_reml_gls_ex")
+        o._keep = (ptau_d, w_d)
+    else:
+        _lib.check(lib.ffs_reml_gls(C.byref(ga), st), "ffs_reml_gls")
+    o._keep2 = (Y, order, work, Xt)
+    return o

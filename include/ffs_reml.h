@@ -1,0 +1,263 @@
+/*
+ * ffs_reml.h -- C ABI of the GB300 ARMA(1,1) REML voxelwise GLM library
+ * (libffs_reml.so).
+ *
+ * Every entry point takes plain device pointers and sizes, launches on the
+ * caller's CUDA stream (cudaStream_t passed as void*), allocates nothing and
+ * never synchronises the device. Buffers are owned by the caller; their layouts
+ * are stated below. Each call returns an ffs_status; on failure a message for
+ * the calling thread is available from ffs_last_error().
+ *
+ * The reference is Python (fastfuncstuff/glm/arma.py, fastfuncstuff/glm/whiten.py);
+ * each entry point names the reference function whose work it replaces. The
+ * Python package fastfuncstuff_gb300 binds these through ctypes and exposes the
+ * reference's own API (fit_glm_arma11, fit_glm_arma11_grouped, ...).
+ *
+ * Notation: V voxels, T retained time points, K design columns, P valid (a,b)
+ * pairs, R runs. "time-major" = [T][V] (voxel index fastest), "voxel-major" =
+ * [V][T].
+ */
+#ifndef FFS_REML_H
+#define FFS_REML_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  FFS_OK = 0,
+  FFS_ERR_INVALID = 1,     /* bad argument or shape (Python: ValueError)          */
+  FFS_ERR_CUDA = 2,        /* CUDA runtime error                                  */
+  FFS_ERR_UNSUPPORTED = 3, /* shape outside what the kernels were built for       */
+  FFS_ERR_WORKSPACE = 4,   /* workspace smaller than required (Python: MemoryError)*/
+  FFS_ERR_TIMEOUT = 5      /* a bounded device-side wait expired                  */
+} ffs_status;
+
+/* Library version, (major << 16) | minor. */
+int ffs_version(void);
+
+/* Static description of a status code. */
+const char* ffs_status_string(int status);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* ffs_last_error(void);
+
+/* ------------------------------------------------------------------------ grid
+ * Replaces fastfuncstuff/glm/whiten.py:197-271 (arma11_whiteners) and
+ * fastfuncstuff/glm/arma.py:1371-1531 (precompute_reml_grid), plus the
+ * per-group GLS constants of fastfuncstuff/glm/arma.py:4853-4905.
+ *
+ * For each valid pair p (a_p, b_p) the ARMA(1,1) correlation of every run is
+ * factorised exactly in FP64 through its AR-filtered tridiagonal form
+ * (R = A^-1 L~ D L~^T A^-T, so the Cholesky factor is A^-1 L~ D^1/2), giving:
+ *   coef[p][t]   = (c_t, m_t, 1/D_t, 1/sqrt(D_t)) as float4:
+ *                  z_t = y_t - c_t y_{t-1};  v_t = z_t - m_t v_{t-1};
+ *                  (L^-1 y)_t = v_t / sqrt(D_t);  y'R^-1 y = sum v_t^2 / D_t.
+ *                  c_t = m_t = 0 at every run start.
+ *   logdet_R[p]  = 2 sum_t log(sqrt(D_t) + 1e-10)          (FP64)
+ *   logdet_XtX[p]= 2 sum_j log(|L_xtx,jj| + 1e-10)          (FP64)
+ *   U[p]         = L^-T Q, Q = X_w L_xtx^-T, stored [P][K][T] fp32:
+ *                  ||Q' L^-1 y||^2 = ||U' y||^2 for any series y.
+ *   U_hi/U_lo    = the same as a bf16 split (U ~ hi + lo), rows p*K+j of
+ *                  length ld_u (>= T, multiple of 8, zero padded): the B
+ *                  operand of the projection GEMM.
+ *   G[p]         = U L_xtx^-1 = R^-1 X (X'R^-1 X)^-1, [P][K][T] fp32:
+ *                  GLS betas b = G' y.
+ *   Adiag[p][K]  = diag((X_w'X_w)^-1);  XtX[p][K][K] = X_w'X_w (fp32).
+ *   Ftask[p]     = inv(A_task + 1e-8 I) for the task-column F statistic
+ *                  (fastfuncstuff/glm/arma.py:4891-4898), A = (X_w'X_w)^-1.
+ *   glt_var[p][c]= c A c' for each single-row GLT c (arma.py:5455-5466).
+ *   info[p]      = 0 Cholesky of X_w'X_w, 1 QR fallback used (the design is
+ *                  rank deficient at this pair), 2 a pivot of R's factor was
+ *                  not positive.
+ */
+typedef struct {
+  int T, K, P, n_runs;
+  const int* run_start; /* device [n_runs + 1], run_start[n_runs] == T           */
+  const int* tau;       /* device [T], within-run time index (censoring gaps)    */
+  const float* a;       /* device [P]                                            */
+  const float* b;       /* device [P]                                            */
+  const float* X;       /* device [T][K] row-major design                        */
+  int lambda_fp32;      /* 1: lambda in float32 op order (float32 fits),
+                           0: in float64 (use_double fits)                        */
+  int ld_u;             /* row length of U_hi / U_lo (>= T, multiple of 8)       */
+  int n_task;           /* task columns for the F statistic (0: full model)      */
+  const int* task_idx;  /* device [n_task]                                       */
+  int n_glt;            /* single-row GLT contrasts                              */
+  const float* glt;     /* device [n_glt][K]                                     */
+} ffs_grid_desc;
+
+typedef struct {
+  float* coef;          /* [P][T][4]                                              */
+  double* logdet_R;     /* [P]                                                    */
+  double* logdet_XtX;   /* [P]                                                    */
+  float* U;             /* [P][K][T]                                              */
+  uint16_t* U_hi;       /* [P*K][ld_u] bf16 bits (may be NULL)                    */
+  uint16_t* U_lo;       /* [P*K][ld_u] bf16 bits (may be NULL)                    */
+  float* G;             /* [P][K][T]                                              */
+  float* Adiag;         /* [P][K]                                                 */
+  float* XtX;           /* [P][K][K]                                              */
+  int* info;            /* [P]                                                    */
+  float* Ftask;         /* [P][n_task][n_task] inv(A_task + 1e-8 I), or NULL      */
+  float* glt_var;       /* [P][n_glt] c A c', or NULL                             */
+  float* Gsum;          /* [P][K] G' 1: the betas of the constant series          */
+  double* work;         /* scratch, ffs_grid_work_bytes() bytes                   */
+} ffs_grid_out;
+
+size_t ffs_grid_work_bytes(int T, int K, int P);
+int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
+
+/* ---------------------------------------------------------------- search data
+ * Replaces the per-voxel scaling of fastfuncstuff/glm/arma.py:3952-3954,
+ * 4685-4686 and _residualize_reml_search_data (arma.py:1554-1571).
+ *   scale[v] = max(std(Y[v]) (N-1 divisor), 1e-8);
+ *   Y_r[v]   = Y[v]/scale[v] - Q0 Q0' (Y[v]/scale[v]), Q0 an orthonormal basis
+ *              of the design's columns (U of the pair (0,0) is that basis).
+ * Outputs Y_r time-major fp32 and, when yr_hi/yr_lo are given, voxel-major bf16
+ * hi/lo splits with row length ld_y (>= T, multiple of 8, zero padded).
+ * With do_scale == 0 the data are used as given (scale = 1). With center != 0
+ * (only valid when the constant series lies in the design's span) each voxel's
+ * mean is subtracted first: the criterion is unchanged, and the float32
+ * residualisation no longer rounds against a large baseline.
+ */
+typedef struct {
+  int V, T, K;
+  const float* Y;       /* device [V][T] voxel-major input                       */
+  const float* Q0;      /* device [K][T]: orthonormal basis of the design columns*/
+  int do_scale;
+  int center;
+  int ld_y;
+  float* scale;         /* [V]                                                    */
+  float* yr_t;          /* [T][V] time-major residualised data                    */
+  uint16_t* yr_hi;      /* [V][ld_y] bf16 bits or NULL                            */
+  uint16_t* yr_lo;      /* [V][ld_y] bf16 bits or NULL                            */
+} ffs_prep_args;
+
+int ffs_reml_prep(const ffs_prep_args* a, void* stream);
+
+/* ------------------------------------------------------------------ projection
+ * The ||Q'Y_w||^2 term of fastfuncstuff/glm/arma.py:1992-1995 for every voxel
+ * and pair: proj[p][v] = sum_j (sum_t U[p][j][t] Y_r[v][t])^2.
+ * ffs_reml_project_tc runs it as a TMA-fed tcgen05 GEMM in split bf16
+ * (hi*hi + hi*lo + lo*hi, fp32 accumulation in TMEM) with the square-and-sum
+ * epilogue on chip. ffs_reml_project_simt is the CUDA-core form of the same
+ * contraction (fp32), used for small or per-voxel-window problems.
+ */
+typedef struct {
+  int V, T, K, P;
+  int ld_y, ld_u;
+  const uint16_t* yr_hi; const uint16_t* yr_lo;   /* [V][ld_y]  */
+  const uint16_t* u_hi;  const uint16_t* u_lo;    /* [P*K][ld_u] */
+  const float* yr_t;    /* [T][V] (simt form)                                    */
+  const float* U;       /* [P][K][T] (simt form)                                 */
+  float* proj;          /* [P][V]                                                 */
+  int* flag;            /* device int, 0 on entry; set non-zero if a bounded
+                           device-side wait expired (tc form)                    */
+} ffs_project_args;
+
+int ffs_reml_project_tc(const ffs_project_args* a, void* stream);
+int ffs_reml_project_simt(const ffs_project_args* a, void* stream);
+
+/* --------------------------------------------------------------------- surface
+ * The REML criterion of every voxel at every pair
+ * (fastfuncstuff/glm/arma.py:1983-2002):
+ *   crit = logdet_R + logdet_XtX + (T-K) log(RSS + 1e-10),
+ *   RSS  = y'R^-1 y - proj, y'R^-1 y by the O(T) recurrence of coef.
+ * The criterion is formed relative to the pair (0,0) (index p0) so that the
+ * float32 arithmetic resolves differences between neighbouring pairs:
+ *   d[p][v] = (const_p - const_p0) + (T-K) log1p((RSS_p - RSS_p0)/(RSS_p0+1e-10))
+ * and crit = crit0[v] + d[p][v], crit0 = const_p0 + (T-K) log(RSS_p0 + 1e-10)
+ * evaluated in FP64. Pairs are walked in chunks that share a (work list below).
+ */
+typedef struct {
+  int V, T, K, P;
+  int p0;                 /* index of the pair (0, 0)                             */
+  const float* yr_t;      /* [T][V]                                               */
+  const float* coef;      /* [P][T][4]                                            */
+  const double* logdet_R; const double* logdet_XtX;  /* [P]                      */
+  const float* proj;      /* [P][V]                                               */
+  const int* chunk_start; /* device [n_chunks+1]: pairs of chunk c are           */
+  int n_chunks;           /*   chunk_pairs[chunk_start[c] .. chunk_start[c+1])   */
+  const int* chunk_pairs; /*   all pairs of a chunk share one a                  */
+  float* surf;            /* [P][V] d[p][v]                                       */
+  double* crit0;          /* [V]                                                  */
+} ffs_surface_args;
+
+int ffs_reml_surface(const ffs_surface_args* a, void* stream);
+
+/* ---------------------------------------------------------------------- select
+ * Exhaustive global argmin (fastfuncstuff/glm/arma.py:2004-2009: strict '<',
+ * the first pair in list order wins ties) or AFNI's power-of-2 hierarchical
+ * descent from (0,0) on the lattice (select_arma_params_hierarchical_from_surface,
+ * fastfuncstuff/glm/arma.py:2224-2322).
+ * lattice[ai*n_b + bi] = pair index or -1 for a filtered point.
+ */
+typedef struct {
+  int V, P;
+  const float* surf;      /* [P][V]                                               */
+  const double* crit0;    /* [V]                                                  */
+  int hierarchical;       /* 0 exhaustive, 1 hierarchical                         */
+  int n_a, n_b, ltop, za, zb;
+  const int* lattice;     /* device [n_a*n_b]                                     */
+  int* best;              /* [V] pair index                                       */
+  float* best_crit;       /* [V] crit0 + d (float32, the reported likelihood)     */
+} ffs_select_args;
+
+int ffs_reml_select(const ffs_select_args* a, void* stream);
+
+/* ---------------------------------------------------------------------- GLS
+ * The GLS refit at each voxel's chosen pair (fastfuncstuff/glm/arma.py:4784-5590):
+ * betas by G' y with one refinement step on the unwhitened residual, sigma2 from
+ * the whitened residual (float64-style blocked accumulation), t, F (full model
+ * or task columns), R^2 (unwhitened), GLT contrasts, lambda, and optional
+ * residuals / whitened residuals / predicted series, all unscaled by scale[v].
+ * Voxels are processed in the order of `order` (sorted by pair) so that a
+ * warp reads one pair's matrices.
+ */
+typedef struct {
+  int V, T, K;
+  int dof;
+  int center;             /* subtract the voxel mean first and add its betas
+                             (mean/scale * Gsum) back; constant must be in span(X)*/
+  const float* Gsum;      /* [P][K] (used with center)                            */
+  const float* Y;         /* [V][T] voxel-major input data (unscaled)             */
+  const float* scale;     /* [V]                                                  */
+  const float* Xt;        /* [K][T] the design, transposed                        */
+  const int* best;        /* [V] pair per voxel                                   */
+  const int* order;       /* [V] voxel permutation (grouped by pair) or NULL      */
+  const float* coef; const float* G; const float* Adiag; const float* XtX;
+  const float* a; const float* b;                    /* [P] grid values          */
+  int lambda_fp32;        /* output lambda in float32 (1) or float64 rounded (0)  */
+  int n_task; const int* task_idx;                   /* task columns (device)    */
+  const float* Ftask;     /* [P][n_task][n_task] inv(A_task + 1e-8 I), or NULL    */
+  int n_glt; const float* glt;                       /* [n_glt][K]                */
+  const float* glt_var;   /* [P][n_glt] c A c'                                    */
+  float* betas;           /* [V][K] every column; task selection is the caller's  */
+  float* tstats;          /* [V][K]                                               */
+  float* sigma2; float* fstats; float* r2; float* lam;   /* [V]                  */
+  float* cbeta; float* ct;                           /* [V][n_glt] or NULL        */
+  float* resid; float* resid_w; float* pred;         /* [V][T] or NULL            */
+} ffs_gls_args;
+
+int ffs_reml_gls(const ffs_gls_args* a, void* stream);
+
+/* ffs_reml_gls plus the Ljung-Box statistic of each voxel's whitened residual
+ * (fastfuncstuff/glm/arma.py:6058-6141, AFNI ljung_box_uneven): lj_h is the
+ * resolved max lag (<= T/2), lj_tau the pseudo-time of every retained point
+ * (NULL: plain index lags), lj_w[k] = 1/n_k for bins with n_k > 1 else 0. */
+int ffs_reml_gls_ex(const ffs_gls_args* a, int lj_h, const int* lj_tau, const float* lj_w,
+                    float* ljung_box, void* stream);
+
+/* Counting sort of voxels by pair: order[] lists voxel ids grouped by best[].
+ * Replaces the torch.unique / sort grouping of fastfuncstuff/glm/arma.py:4794-4811.
+ * work: int[P + 1]. */
+int ffs_reml_group(int V, int P, const int* best, int* work, int* order, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFS_REML_H */

@@ -1,0 +1,252 @@
+"""CUDA path against the FP64 oracle and the reference's golden fixtures (GB300 only).
+
+Parity bars (written where they are used):
+* selected pair: identical to the FP64 oracle on >= 99.9% of voxels, and every
+  disagreement within 1e-6 (relative) of the optimal criterion on the oracle's
+  FP64 surface;
+* betas and t: within 1e-4 relative (per voxel, max-norm) of the FP64 oracle;
+* grid factors (FP64 on the GPU): logdets within 1e-9 relative of the reference.
+"""
+
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from fastfuncstuff_gb300 import synth
+from fastfuncstuff_gb300.glm import engine
+from fastfuncstuff_gb300.glm import grid as G
+from fastfuncstuff_gb300.glm.arma import fit_glm_arma11, fit_glm_arma11_grouped, precompute_reml_grid
+from oracle import reml as o
+from tests.conftest import load_golden
+from tests.test_oracle_golden import case_kwargs
+
+pytestmark = pytest.mark.gpu
+
+DEV = torch.device("cuda:0")
+
+# tolerances (see module docstring)
+# projection kernel of the full-fit tests: "tc" (tcgen05, the default) or "simt"
+PROJ = os.environ.get("FFS_TEST_PROJECTOR", "tc")
+ARGMIN_AGREE = 0.999
+CRIT_GAP_REL = 1e-6
+BETA_REL = 1e-4
+
+
+def rel_maxnorm(got, want):
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    num = np.abs(got - want).max(axis=-1)
+    den = np.maximum(np.abs(want).max(axis=-1), 1e-12)
+    return num / den
+
+
+def check_selection(idx_gpu, idx_ref, surf64):
+    """>= 99.9% identical; the rest within CRIT_GAP_REL of the optimum on the FP64 surface."""
+    idx_gpu = np.asarray(idx_gpu)
+    idx_ref = np.asarray(idx_ref)
+    agree = float((idx_gpu == idx_ref).mean())
+    bad = np.nonzero(idx_gpu != idx_ref)[0]
+    if bad.size:
+        v = bad
+        c_gpu = surf64[v, idx_gpu[v]]
+        c_ref = surf64[v, idx_ref[v]]
+        gap = np.abs(c_gpu - c_ref) / np.maximum(np.abs(c_ref), 1.0)
+        assert gap.max() <= CRIT_GAP_REL, (agree, gap.max())
+    assert agree >= ARGMIN_AGREE or bad.size <= 1, agree
+    return agree
+
+
+def _index(params, grid):
+    return grid.index_of(np.asarray(params[:, 0], np.float32), np.asarray(params[:, 1], np.float32))
+
+
+# ------------------------------------------------------------------ grid build
+
+
+def test_grid_factors_match_reference_precompute():
+    d = load_golden("grid")
+    X = torch.from_numpy(d["X"])
+    T = X.shape[0]
+    f = precompute_reml_grid(X, T, d["a_grid"], d["b_grid"], DEV, run_starts=d["run_starts"], use_double=True)
+    torch.cuda.synchronize()
+    pairs = np.stack([f.grid.a, f.grid.b], 1).astype(np.float64)
+    np.testing.assert_array_equal(pairs, d["pairs"])
+    np.testing.assert_allclose(f.logdet_R.cpu().numpy(), d["logdet_R"], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(f.logdet_XtX.cpu().numpy(), d["logdet_XtX"], rtol=1e-9, atol=1e-9)
+    assert int(f.info.cpu().abs().sum()) == 0
+    # the recurrence coefficients whiten exactly like the dense L^-1
+    coef = f.coef.cpu().numpy().astype(np.float64)
+    Xd = d["X"].astype(np.float64)
+    for p in range(f.P):
+        c, m, _, rs = coef[p, :, 0], coef[p, :, 1], coef[p, :, 2], coef[p, :, 3]
+        xw = np.zeros_like(Xd)
+        xp = np.zeros(Xd.shape[1])
+        vp = np.zeros(Xd.shape[1])
+        for t in range(T):
+            z = Xd[t] - c[t] * xp
+            v = z - m[t] * vp
+            xw[t] = v * rs[t]
+            xp, vp = Xd[t], v
+        np.testing.assert_allclose(xw, d["X_w"][p], rtol=2e-6, atol=2e-6)
+    # U = L^-T Q and G = R^-1 X (X'R^-1 X)^-1 against the dense FP64 restatement
+    og = o.valid_grid(d["a_grid"], d["b_grid"], np.float64)
+    pre = o.precompute_reml_grid(Xd, og, run_starts=d["run_starts"])
+    U = f.U.cpu().numpy()
+    Gm = f.G.cpu().numpy()
+    for p in range(0, f.P, 5):
+        Li = pre.whiteners[p].dense()
+        U_ref = Li.T @ pre.Q[p]
+        np.testing.assert_allclose(U[p].T, U_ref, rtol=1e-5, atol=1e-6)
+        A = np.linalg.inv(pre.X_w[p].T @ pre.X_w[p])
+        G_ref = Li.T @ pre.X_w[p] @ A
+        np.testing.assert_allclose(Gm[p].T, G_ref, rtol=1e-4, atol=1e-5)
+
+
+# --------------------------------------------------------- projection kernels
+
+
+@pytest.mark.parametrize("K,T,V", [(20, 400, 1000), (8, 200, 777), (18, 855, 300), (130, 600, 260)])
+def test_tensor_core_projection_matches_simt(K, T, V):
+    rng = np.random.default_rng(K)
+    X = rng.standard_normal((T, K)).astype(np.float32)
+    Y = rng.standard_normal((V, T)).astype(np.float32)
+    g = torch.linspace(-0.8, 0.8, 9)
+    f = precompute_reml_grid(torch.from_numpy(X), T, g, g, DEV, run_starts=[0, T // 2])
+    Yd = torch.from_numpy(Y).to(DEV)
+    outs = {}
+    for proj in ("tc", "simt"):
+        so = engine.search(Yd, f, hierarchical=False, projector=proj, keep_surface=True)
+        torch.cuda.synchronize()
+        assert int(so._flag.item()) == 0
+        outs[proj] = so
+    s_tc = outs["tc"].surf.cpu().numpy()
+    s_si = outs["simt"].surf.cpu().numpy()
+    # criterion differences agree to well below one grid step
+    assert np.abs(s_tc - s_si).max() < 5e-3, np.abs(s_tc - s_si).max()
+    np.testing.assert_array_equal(outs["tc"].best.cpu().numpy()[:50] >= 0, True)
+
+
+# ------------------------------------------------------------- full fits
+
+
+@pytest.mark.parametrize("case", ["single", "multirun", "censored", "baseline"])
+@pytest.mark.parametrize("exhaustive", [True, False])
+def test_fit_matches_fp64_oracle(case, exhaustive):
+    projector = PROJ
+    d = load_golden(case)
+    kw = case_kwargs(d)
+    ref = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, fp64_scaled=True,
+                           force_exhaustive_search=exhaustive, save_profile_likelihoods=True, **kw)
+    gkw = dict(kw)
+    if "glt_matrices" in gkw:
+        gkw["glt_labels"] = ["c0"]
+    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=projector,
+                         force_exhaustive_search=exhaustive, want_r2_partial=True, **gkw)
+    grid = G.make_grid(d["a_grid"], d["b_grid"])
+    idx = _index(got.arma_params.numpy(), grid)
+    check_selection(idx, ref.arma_index, ref.reml_lklhd_surface)
+    same = idx == ref.arma_index
+    assert rel_maxnorm(got.betas.numpy()[same], ref.betas[same]).max() <= BETA_REL
+    assert rel_maxnorm(got.tstats.numpy()[same], ref.tstats[same]).max() <= BETA_REL
+    np.testing.assert_allclose(got.sigma2.numpy()[same], ref.sigma2[same], rtol=1e-4)
+    np.testing.assert_allclose(got.fstats.numpy()[same], ref.fstats[same], rtol=2e-4, atol=1e-4)
+    np.testing.assert_allclose(got.r2.numpy()[same], ref.r2[same], atol=2e-5)
+    np.testing.assert_allclose(got.reml_likelihood.numpy()[same], ref.reml_likelihood[same], rtol=1e-5,
+                               atol=2e-3)
+    lam = o.arma_lambda_output_f32(got.arma_params[:, 0].numpy(), got.arma_params[:, 1].numpy())
+    np.testing.assert_array_equal(got.arma_lambda.numpy(), lam)
+    if kw.get("want_ljung_box"):
+        np.testing.assert_allclose(got.ljung_box.numpy()[same], ref.ljung_box[same], rtol=2e-3, atol=1e-3)
+        assert got.ljung_box_dof == ref.ljung_box_dof
+    if "glt_matrices" in kw:
+        assert rel_maxnorm(got.contrast_betas.numpy()[same], ref.contrast_betas[same]).max() <= BETA_REL
+        assert rel_maxnorm(got.contrast_tstats.numpy()[same], ref.contrast_tstats[same]).max() <= BETA_REL
+    if kw.get("want_residuals"):
+        np.testing.assert_allclose(got.residuals.numpy()[same], ref.residuals[same], rtol=1e-4, atol=2e-4)
+        np.testing.assert_allclose(got.residuals_whitened.numpy()[same], ref.residuals_whitened[same],
+                                   rtol=1e-4, atol=2e-4)
+    np.testing.assert_allclose(got.r2_partial.numpy()[same], ref.r2_partial[same], atol=1e-4)
+
+
+def test_reference_float32_selection_agrees():
+    """The reference's own float32 run (golden) selects what the GPU selects."""
+    for case in ("single", "multirun", "censored", "baseline"):
+        d = load_golden(case)
+        kw = case_kwargs(d)
+        if "glt_matrices" in kw:
+            kw["glt_labels"] = ["c0"]
+        got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, projector=PROJ, verbose=False, force_exhaustive_search=True, **kw)
+        agree = (got.arma_params.numpy() == d["f32_exh__arma_params"]).all(1).mean()
+        assert agree >= 0.98, (case, agree)
+
+
+def test_use_double_semantics_match_fp64_reference():
+    d = load_golden("single")
+    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, a_grid=d["a_grid"], b_grid=d["b_grid"], device=DEV, projector=PROJ,
+                         verbose=False, use_double=True, force_exhaustive_search=True)
+    assert got.betas.dtype == torch.float64
+    np.testing.assert_array_equal(got.arma_params.numpy(), d["f64_exh__arma_params"])
+    np.testing.assert_allclose(got.reml_likelihood.numpy(), d["f64_exh__reml_likelihood"], rtol=1e-5, atol=2e-3)
+    assert rel_maxnorm(got.betas.numpy(), d["f64_exh__betas"]).max() <= BETA_REL
+
+
+def test_grouped_matches_reference():
+    d = load_golden("grouped")
+    designs = {h: d[f"X{h}"] for h in range(3)}
+    got = fit_glm_arma11_grouped(d["Y"], designs, d["gid"], tr=2.0, a_grid=d["a_grid"], b_grid=d["b_grid"],
+                                 device=DEV, projector=PROJ, force_exhaustive_search=True)
+    grid = G.make_grid(d["a_grid"], d["b_grid"])
+    ref_idx = _index(d["f64_exh__arma_params"], grid)
+    idx = _index(got.arma_params.numpy(), grid)
+    agree = (idx == ref_idx).mean()
+    assert agree >= 0.99, agree
+    same = idx == ref_idx
+    assert rel_maxnorm(got.betas.numpy()[same], d["f64_exh__betas"][same]).max() <= BETA_REL
+
+
+def test_precomputed_params_path():
+    d = load_golden("multirun")
+    kw = case_kwargs(d)
+    kw["glt_labels"] = ["c0"]
+    first = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, projector=PROJ, verbose=False, **kw)
+    again = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, projector=PROJ, verbose=False,
+                           precomputed_arma_params=first.arma_params, **kw)
+    np.testing.assert_array_equal(again.arma_params.numpy(), first.arma_params.numpy())
+    assert rel_maxnorm(again.betas.numpy(), first.betas.numpy()).max() <= 1e-5
+    np.testing.assert_allclose(again.sigma2.numpy(), first.sigma2.numpy(), rtol=1e-5)
+
+
+def test_edge_cases_constant_and_pure_signal_voxels():
+    d = load_golden("single")
+    Y = d["Y"][:40].copy()
+    Y[0] = 0.0                                 # all-zero voxel
+    Y[1] = 7.5                                 # constant voxel
+    Y[2] = d["X"] @ np.arange(d["X"].shape[1], dtype=np.float32)  # exactly in the design span
+    got = fit_glm_arma11(Y, d["X"], tr=2.0, a_grid=d["a_grid"], b_grid=d["b_grid"], device=DEV, projector=PROJ, verbose=False)
+    for name in ("betas", "tstats", "sigma2", "fstats", "r2", "reml_likelihood"):
+        assert torch.isfinite(getattr(got, name)).all(), name
+    assert float(got.r2[0]) == 0.0
+
+
+# ----------------------------------------------------- workload-size parity
+
+
+def test_workload0_subset_parity_exhaustive_and_hierarchical():
+    w = synth.workload(0, V=1500)
+    g = torch.linspace(-0.8, 0.8, 33)
+    og = o.valid_grid(g.numpy(), g.numpy(), np.float64)
+    surf = o.criterion_surface(w.X, w.Y, og, scaled=True)
+    for exhaustive in (True, False):
+        got = fit_glm_arma11(w.Y, w.X, tr=2.0, a_grid=g, b_grid=g, device=DEV, projector=PROJ, verbose=False,
+                             force_exhaustive_search=exhaustive)
+        if exhaustive:
+            ref_idx = np.argmin(surf, axis=1)
+        else:
+            ref_idx, _ = o.select_hierarchical_from_surface(surf, og)
+        idx = _index(got.arma_params.numpy(), G.make_grid(g, g))
+        agree = check_selection(idx, ref_idx, surf)
+        print(f"workload0 exhaustive={exhaustive}: agreement {agree:.5f}")

@@ -1,0 +1,145 @@
+"""Host-side logic of the product path, checked on the CPU against the oracle."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from fastfuncstuff_gb300 import synth
+from fastfuncstuff_gb300.glm import grid as G
+from fastfuncstuff_gb300.glm.arma import fit_glm_arma11, fit_glm_arma11_grouped
+from oracle import reml as o
+from tests.conftest import load_golden
+
+
+@pytest.mark.parametrize("use_double", [False, True])
+@pytest.mark.parametrize(
+    "grids",
+    [
+        (torch.linspace(-0.8, 0.8, 33), torch.linspace(-0.8, 0.8, 33)),
+        (torch.linspace(0.0, 0.8, 9), torch.linspace(-0.8, 0.8, 17)),
+        (torch.linspace(-0.8, 0.8, 17), torch.linspace(-0.8, 0.8, 17)),
+        (torch.tensor([0.1, 0.3, 0.5]), torch.tensor([-0.2, 0.2])),  # zero inserted
+        (torch.linspace(-0.95, 0.95, 39), torch.linspace(-0.95, 0.95, 39)),
+    ],
+)
+def test_grid_matches_oracle(grids, use_double):
+    a, b = grids
+    g = G.make_grid(a, b, use_double=use_double)
+    og = o.valid_grid(a.numpy(), b.numpy(), np.float64 if use_double else np.float32)
+    np.testing.assert_array_equal(g.a, og.a)
+    np.testing.assert_array_equal(g.b, og.b)
+    np.testing.assert_array_equal(g.a_axis, og.a_axis)
+    assert g.a[g.p0] == 0 and g.b[g.p0] == 0
+    assert g.ltop == o._ltop(len(og.a_axis), len(og.b_axis))
+    # lattice round trip and chunks that share a
+    for p in range(g.P):
+        ai = np.searchsorted(g.a_axis, g.a[p])
+        bi = np.searchsorted(g.b_axis, g.b[p])
+        assert g.lattice[ai, bi] == p
+    for c in range(len(g.chunk_start) - 1):
+        s, e = g.chunk_start[c], g.chunk_start[c + 1]
+        assert 0 < e - s <= G.SURFACE_CHUNK
+        assert len(set(g.a[s:e].tolist())) == 1
+    assert g.chunk_start[-1] == g.P
+
+
+def test_grid_counts_and_default():
+    assert G.estimate_valid_grid_pairs(torch.linspace(-0.8, 0.8, 33), torch.linspace(-0.8, 0.8, 33)) == 561
+    a, b = G.get_default_arma_grids()
+    assert G.make_grid(a, b).P == G.estimate_valid_grid_pairs(a, b)
+    assert 100 < G.make_grid(a, b).P < 153
+
+
+def test_index_of_pairs():
+    g = G.make_grid(torch.linspace(-0.8, 0.8, 17), torch.linspace(-0.8, 0.8, 17))
+    idx = g.index_of(g.a, g.b)
+    np.testing.assert_array_equal(idx, np.arange(g.P))
+    assert g.index_of(np.array([0.05], np.float32), np.array([0.0], np.float32))[0] == -1
+
+
+def test_grid_of_pairs_rejects_invalid():
+    with pytest.raises(ValueError, match="Invalid ARMA"):
+        G.grid_of_pairs(np.array([0.5], np.float32), np.array([-0.7], np.float32))  # lambda < 0
+    with pytest.raises(ValueError):
+        G.grid_of_pairs(np.array([1.0], np.float32), np.array([0.0], np.float32))
+
+
+def test_run_layout_and_censoring():
+    lay = G.run_layout(10, [0, 5])
+    assert lay.run_start.tolist() == [0, 5, 10]
+    assert lay.tau.tolist() == [0, 1, 2, 3, 4, 0, 1, 2, 3, 4]
+    starts, tau = G.build_censor_run_info([0, 5], 10, [0, 1, 3, 4, 5, 6, 8, 9])
+    assert starts == [0, 4] and tau.tolist() == [0, 1, 3, 4, 0, 1, 3, 4]
+    lay = G.run_layout(8, starts, tau)
+    assert lay.run_start.tolist() == [0, 4, 8] and lay.tau.tolist() == [0, 1, 3, 4, 0, 1, 3, 4]
+    with pytest.raises(ValueError):
+        G.run_layout(4, None, np.array([0, 2, 2, 3]))
+    assert G.run_bounds(10, [4]) == [(0, 4), (4, 10)]
+
+
+@pytest.mark.parametrize("case", ["multirun", "censored", "single"])
+def test_ljung_box_plan_matches_oracle_binning(case):
+    d = load_golden(case)
+    T, K = d["X"].shape
+    rs = d["run_starts"] if "run_starts" in d else None
+    tau = d["tau"] if "tau" in d else None
+    h, ptau, w, dof = G.ljung_box_plan(T, K, rs, tau)
+    starts = sorted(set(np.asarray(rs).tolist())) if rs is not None else [0]
+    mins = min(b - a for a, b in zip(starts, starts[1:] + [T])) if len(starts) > 1 else T
+    assert h == o.resolve_ljung_box_lag(T, o.ljung_box_max_lag(T, K, mins))
+    assert dof == max(1, h - 2)
+    # the weighted statistic from the plan equals the oracle's on random residuals
+    r = np.random.default_rng(0).standard_normal((3, T))
+    want = o.ljung_box(r, o.ljung_box_max_lag(T, K, mins), o.build_ljung_box_tau(T, rs, tau))
+    got = []
+    for row in r:
+        s0 = (row**2).sum()
+        bins = np.zeros(h + 1)
+        for k in range(1, h + 1):
+            for t in range(T - k):
+                dj = (ptau[t + k] - ptau[t]) if ptau is not None else k
+                if 0 < dj <= h:
+                    bins[dj] += row[t] * row[t + k]
+        got.append(T * (T + 2.0) * ((bins / s0) ** 2 * w).sum())
+    np.testing.assert_allclose(got, want, rtol=1e-6)  # float32 1/n_k weights
+
+
+def test_fit_argument_errors_raise_before_gpu():
+    with pytest.raises(ValueError, match="2D or 4D"):
+        fit_glm_arma11(np.zeros((2, 3, 10), np.float32), np.ones((10, 2)), tr=2.0)
+    with pytest.raises(ValueError, match="Timepoints mismatch"):
+        fit_glm_arma11(np.zeros((2, 10), np.float32), np.ones((9, 2)), tr=2.0)
+    with pytest.raises(NotImplementedError):
+        fit_glm_arma11(np.zeros((2, 10), np.float32), np.ones((10, 2)), tr=2.0, want_ols=True)
+
+
+def test_grouped_argument_errors():
+    Y = np.zeros((4, 10), np.float32)
+    with pytest.raises(KeyError):
+        fit_glm_arma11_grouped(Y, {0: np.ones((10, 2))}, [0, 0, 1, 1], tr=2.0)
+    with pytest.raises(ValueError):
+        fit_glm_arma11_grouped(Y, {0: np.ones((10, 2)), 1: np.ones((10, 3))}, [0, 0, 1, 1], tr=2.0)
+
+
+def test_synthetic_workloads_are_seeded_and_shaped():
+    w0 = synth.workload(0, V=300)
+    w0b = synth.workload(0, V=300)
+    np.testing.assert_array_equal(w0.Y, w0b.Y)
+    assert w0.Y.shape == (300, 200) and w0.X.shape == (200, 8)
+    w1 = synth.workload(1, V=500)
+    assert w1.Y.shape == (500, 400) and w1.X.shape == (400, 20) and w1.run_starts == [0, 200]
+    w2 = synth.workload(2, V=400)
+    assert w2.Y.shape == (400, 855) and len(w2.designs) == 20
+    assert all(d.shape == (855, 18) for d in w2.designs.values())
+    assert w2.run_starts == [0, 171, 380, 608] and w2.tau.shape == (855,)
+    w3 = synth.workload(3, V=200)
+    assert w3.Y.shape == (200, 600) and w3.X.shape == (600, 130)
+    assert np.linalg.matrix_rank(w3.X.astype(np.float64)) == 130
+    # the noise follows y_t = a y_{t-1} + e_t + b e_{t-1}: lag-1 autocorrelation ~ lambda
+    rng = np.random.default_rng(5)
+    n = synth.arma_noise(rng, 4000, np.full(4, 0.6), np.full(4, 0.2))
+    r1 = (n[:, 1:] * n[:, :-1]).mean(1)
+    lam = (0.6 + 0.2) * (1 + 0.12) / (1 + 0.04 + 0.24)
+    np.testing.assert_allclose(r1, lam, atol=0.06)

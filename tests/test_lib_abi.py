@@ -1,0 +1,95 @@
+"""The C ABI library builds, loads and exports what include/ffs_reml.h declares.
+
+No kernel is launched here: these run on the CPU-only container. The ctypes
+structures are checked field by field against the header, compiled by gcc.
+"""
+
+from __future__ import annotations
+
+import re
+import shutil
+import subprocess
+
+import pytest
+
+from fastfuncstuff_gb300 import _lib
+from fastfuncstuff_gb300 import build as B
+from tests.conftest import ROOT
+
+HEADER = ROOT / "include" / "ffs_reml.h"
+
+STRUCTS = {
+    "ffs_grid_desc": _lib.GridDesc,
+    "ffs_grid_out": _lib.GridOut,
+    "ffs_prep_args": _lib.PrepArgs,
+    "ffs_project_args": _lib.ProjectArgs,
+    "ffs_surface_args": _lib.SurfaceArgs,
+    "ffs_select_args": _lib.SelectArgs,
+    "ffs_gls_args": _lib.GlsArgs,
+}
+
+
+def declared_functions() -> list[str]:
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(ffs_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_the_entry_points():
+    names = declared_functions()
+    for n in ("ffs_grid_build", "ffs_reml_prep", "ffs_reml_project_tc", "ffs_reml_surface",
+              "ffs_reml_select", "ffs_reml_gls", "ffs_last_error"):
+        assert n in names
+    assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
+
+
+def test_library_builds_loads_and_exports_every_symbol():
+    path = B.build()
+    assert path.exists()
+    lib = _lib.load()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    assert lib.ffs_version() >> 16 == 1
+    assert lib.ffs_status_string(1).decode() == "invalid argument"
+    assert lib.ffs_last_error().decode() == ""
+    # a host-only entry point: workspace sizing
+    assert lib.ffs_grid_work_bytes(400, 20, 561) == 8 * (4 * 400 + 2 * 20 * 400 + 4 * 20 * 20) * 561
+
+
+def test_argument_validation_needs_no_gpu():
+    """Null descriptors are rejected on the host with a message, before any launch."""
+    lib = _lib.load()
+    st = lib.ffs_grid_build(None, None, None)
+    assert st == _lib.FFS_ERR_INVALID
+    assert "null" in lib.ffs_last_error().decode()
+    with pytest.raises(ValueError, match="ffs_reml_prep"):
+        _lib.check(lib.ffs_reml_prep(None, None), "ffs_reml_prep")
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")
+def test_ctypes_structures_match_the_header(tmp_path):
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void) {"]
+    for cname, py in STRUCTS.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            parts = line.split()
+            got[(parts[0], parts[1])] = int(parts[2])
+    for cname, py in STRUCTS.items():
+        assert got[(cname, "size")] == C_sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def C_sizeof(py) -> int:
+    import ctypes
+
+    return ctypes.sizeof(py)
