@@ -34,7 +34,8 @@ class GridDesc(C.Structure):
 class GridOut(C.Structure):
     _fields_ = [
         ("coef", C.c_void_p), ("logdet_R", C.c_void_p), ("logdet_XtX", C.c_void_p),
-        ("U", C.c_void_p), ("U_hi", C.c_void_p), ("U_lo", C.c_void_p), ("G", C.c_void_p),
+        ("U", C.c_void_p), ("U_hi", C.c_void_p), ("U_lo", C.c_void_p), ("uexp", C.c_void_p),
+        ("G", C.c_void_p),
         ("Adiag", C.c_void_p), ("XtX", C.c_void_p), ("info", C.c_void_p), ("Ftask", C.c_void_p),
         ("glt_var", C.c_void_p), ("Gsum", C.c_void_p), ("work", C.c_void_p),
     ]
@@ -45,7 +46,7 @@ class PrepArgs(C.Structure):
         ("V", C.c_int), ("T", C.c_int), ("K", C.c_int), ("Y", C.c_void_p), ("Q0", C.c_void_p),
         ("do_scale", C.c_int), ("center", C.c_int), ("ld_y", C.c_int), ("scale", C.c_void_p),
         ("yr_t", C.c_void_p),
-        ("yr_hi", C.c_void_p), ("yr_lo", C.c_void_p),
+        ("yr_hi", C.c_void_p), ("yr_lo", C.c_void_p), ("yexp", C.c_void_p),
     ]
 
 
@@ -53,7 +54,8 @@ class ProjectArgs(C.Structure):
     _fields_ = [
         ("V", C.c_int), ("T", C.c_int), ("K", C.c_int), ("P", C.c_int), ("ld_y", C.c_int),
         ("ld_u", C.c_int), ("yr_hi", C.c_void_p), ("yr_lo", C.c_void_p), ("u_hi", C.c_void_p),
-        ("u_lo", C.c_void_p), ("yr_t", C.c_void_p), ("U", C.c_void_p), ("proj", C.c_void_p),
+        ("u_lo", C.c_void_p), ("yexp", C.c_void_p), ("uexp", C.c_void_p),
+        ("yr_t", C.c_void_p), ("U", C.c_void_p), ("proj", C.c_void_p),
         ("flag", C.c_void_p),
     ]
 

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 #include <stdio.h>
 
@@ -54,6 +55,24 @@ __device__ __forceinline__ void split_bf16(float x, uint16_t& hi, uint16_t& lo) 
   __nv_bfloat16 l = __float2bfloat16_rn(r);
   hi = __bfloat16_as_ushort(h);
   lo = __bfloat16_as_ushort(l);
+}
+
+// x ~ hi + lo with hi = fp16(x), lo = fp16(x - hi): about 22 significant bits
+// while |x| stays in fp16's normal range (the callers scale by a power of two).
+__device__ __forceinline__ void split_fp16(float x, uint16_t& hi, uint16_t& lo) {
+  __half h = __float2half_rn(x);
+  float r = __fsub_rn(x, __half2float(h));
+  __half l = __float2half_rn(r);
+  hi = __half_as_ushort(h);
+  lo = __half_as_ushort(l);
+}
+
+// Power of two that brings amax into [128, 256) (0 for amax == 0).
+__device__ __forceinline__ int scale_exp(float amax) {
+  if (!(amax > 0.f) || !isfinite(amax)) return 0;
+  int e;
+  frexpf(amax, &e);  // amax = f * 2^e, f in [0.5, 1)
+  return 8 - e;
 }
 
 // float32 lambda in the reference's operation order, no contraction:

@@ -137,7 +137,8 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
     double Dprev = 1.0, ld = 0.0;
     for (int t = t0; t < t1; ++t) {
       double c = 0.0, m = 0.0, D = 1.0;
-      if (t > t0) {
+      // lambda == 0: every lag correlation is zero, R = I exactly
+      if (t > t0 && lam != 0.0) {
         const int gap = d.tau[t] - d.tau[t - 1];
         c = pow(a, (double)gap);
         const double rho = lam * pow(a, (double)(gap - 1));
@@ -258,6 +259,7 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
   __syncthreads();
 
   // ---- 6. U = L^-T Q = A' L~^-T D^-1/2 Q (backward recursions), into Xw's slot
+  double umax_local = 0.0;
   for (int j = threadIdx.x; j < K; j += blockDim.x) {
     const double* q = s.Qm + (size_t)j * T;
     double* u = s.Xw + (size_t)j * T;
@@ -267,25 +269,35 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
       const double x = q[t] * cm[3] - mn * xn;
       const double ut = x - cn * xn;
       u[t] = ut;
-      const float uf = (float)ut;
-      o.U[((size_t)p * K + j) * T + t] = uf;
-      if (o.U_hi) {
-        uint16_t hi, lo;
-        split_bf16(uf, hi, lo);
-        const size_t row = ((size_t)p * K + j) * d.ld_u;
-        o.U_hi[row + t] = hi;
-        o.U_lo[row + t] = lo;
-      }
+      o.U[((size_t)p * K + j) * T + t] = (float)ut;
+      umax_local = fmax(umax_local, fabs(ut));
       xn = x;
       mn = cm[1];
       cn = cm[0];
     }
-    if (o.U_hi) {
-      const size_t row = ((size_t)p * K + j) * d.ld_u;
-      for (int t = T; t < d.ld_u; ++t) {
-        o.U_hi[row + t] = 0;
-        o.U_lo[row + t] = 0;
-      }
+  }
+  __syncthreads();
+  if (o.U_hi) {
+    // fp16 hi/lo split of U * 2^e, e placing max|U| in [128, 256)
+    double um = umax_local;
+    for (int off = 16; off > 0; off >>= 1) um = fmax(um, __shfl_xor_sync(0xffffffffu, um, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = um;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double mx = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = fmax(mx, red[w]);
+      red[0] = mx;
+    }
+    __syncthreads();
+    const int e = scale_exp((float)red[0]);
+    if (threadIdx.x == 0) o.uexp[p] = e;
+    for (int idx = threadIdx.x; idx < K * d.ld_u; idx += blockDim.x) {
+      const int j = idx / d.ld_u, t = idx % d.ld_u;
+      uint16_t hi = 0, lo = 0;
+      if (t < T) split_fp16(ldexpf((float)s.Xw[(size_t)j * T + t], e), hi, lo);
+      const size_t at = ((size_t)p * K + j) * d.ld_u + t;
+      o.U_hi[at] = hi;
+      o.U_lo[at] = lo;
     }
   }
   __syncthreads();
@@ -366,6 +378,7 @@ extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, voi
               d->n_runs);
   FFS_REQUIRE(d->K <= d->T, "ffs_grid_build: K=%d exceeds T=%d", d->K, d->T);
   FFS_REQUIRE(d->n_task >= 0 && d->n_task <= d->K, "ffs_grid_build: bad n_task=%d", d->n_task);
+  FFS_REQUIRE(!o->U_hi || (o->U_lo && o->uexp), "ffs_grid_build: U_hi needs U_lo and uexp");
   FFS_REQUIRE(!o->U_hi || (d->ld_u >= d->T && d->ld_u % 8 == 0),
               "ffs_grid_build: ld_u=%d must be >= T and a multiple of 8", d->ld_u);
   FFS_REQUIRE(d->run_start && d->tau && d->a && d->b && d->X, "ffs_grid_build: null input");

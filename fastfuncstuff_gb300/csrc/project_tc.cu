@@ -4,10 +4,11 @@
 //
 // is the ||Q'Y_w||^2 term of the REML criterion (fastfuncstuff/glm/arma.py:
 // 1992-1995) for every voxel and every pair at once, since Q'L^-1 y = U'y with
-// U = L^-T Q. Operands are bf16 hi/lo splits of Y_r (voxel-major) and U, so the
+// U = L^-T Q. Operands are fp16 hi/lo splits of Y_r (voxel-major) and U, each
+// scaled by a power of two that puts its largest entry in [128, 256), so the
 // contraction runs as three tcgen05.mma products per k-step (hi*hi, hi*lo,
-// lo*hi) accumulating in fp32 in tensor memory; dropping lo*lo leaves a
-// relative error near 2^-17 per product.
+// lo*hi) accumulating in fp32 in tensor memory, with a relative error near
+// 2^-22 per product; the epilogue removes the scales exactly.
 //
 // CTA tile: 128 voxels x N columns (g whole pairs, N = roundup16(g*K) <= 256).
 // Warp 0 issues TMA loads (128B-swizzled boxes of 64 k-elements), warp 1 owns
@@ -26,13 +27,15 @@ namespace {
 constexpr int BM = 128;         // voxels per tile (TMEM lanes)
 constexpr int BK = 64;          // k elements per stage (one 128-byte swizzle row)
 constexpr int STAGES = 2;
-constexpr int A_TILE = BM * BK * 2;  // bytes of one A box (hi or lo)
+constexpr int A_TILE = BM * BK * 2;  // bytes of one A box (hi or lo, fp16)
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
 
 struct TcParams {
   int V, K, P, ld;     // ld: padded k extent (multiple of BK)
   int g, N;            // pairs per column tile, MMA N
   int n_col_tiles;
+  const int* yexp;
+  const int* uexp;
   float* proj;
   int* flag;
 };
@@ -84,13 +87,13 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   return d;
 }
 
-// kind::f16 instruction descriptor: fp32 accumulator, bf16 A and B, both
-// K-major, M = 128.
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// kind::f16 instruction descriptor: fp32 accumulator (bits 4-5 = 1), fp16 A
+// and B (format fields 0), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
@@ -162,7 +165,7 @@ __global__ void __launch_bounds__(192, 1)
     }
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer
-    const uint32_t idesc = idesc_bf16(BM, prm.N);
+    const uint32_t idesc = idesc_f16(BM, prm.N);
     bool ok = true;
     for (int kb = 0; kb < nk && ok; ++kb) {
       const int s = kb % STAGES;
@@ -179,11 +182,11 @@ __global__ void __launch_bounds__(192, 1)
       const uint64_t b_lo = sdesc(smem_u32(st + 2 * A_TILE + b_tile));
 #pragma unroll
       for (int kk = 0; kk < BK / 16; ++kk) {
-        const uint64_t off = (uint64_t)((kk * 32) >> 4);  // 16 bf16 = 32 bytes along k
+        const uint64_t off = (uint64_t)((kk * 32) >> 4);  // 16 fp16 = 32 bytes along k
         const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
-        mma_bf16(tmem, a_hi + off, b_hi + off, idesc, acc0);
-        mma_bf16(tmem, a_hi + off, b_lo + off, idesc, 1u);
-        mma_bf16(tmem, a_lo + off, b_hi + off, idesc, 1u);
+        mma_f16(tmem, a_hi + off, b_hi + off, idesc, acc0);
+        mma_f16(tmem, a_hi + off, b_lo + off, idesc, 1u);
+        mma_f16(tmem, a_lo + off, b_hi + off, idesc, 1u);
       }
       mma_commit(empty + s);
     }
@@ -193,6 +196,7 @@ __global__ void __launch_bounds__(192, 1)
     const int q = warp & 3;  // TMEM lane quarter this warp may access
     const int row = q * 32 + lane;
     const int v = v0 + row;
+    const int ey = v < prm.V ? prm.yexp[v] : 0;
     const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
     if (!ok && lane == 0) atomicExch(prm.flag, 3);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -217,7 +221,8 @@ __global__ void __launch_bounds__(192, 1)
             run = fmaf(x, x, run);
             if (++j == prm.K) {
               const int p = p_first + pl;
-              if (p < prm.P && v < prm.V) prm.proj[(size_t)p * prm.V + v] = run;
+              if (p < prm.P && v < prm.V)
+                prm.proj[(size_t)p * prm.V + v] = ldexpf(run, -2 * (ey + prm.uexp[p]));
               run = 0.f;
               j = 0;
               ++pl;
@@ -257,11 +262,11 @@ int make_map(CUtensorMap* m, const void* base, int inner, int rows, int box_rows
   cuuint64_t strides[1] = {(cuuint64_t)inner * 2};
   cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
-    set_error("cuTensorMapEncodeTiled failed (%d) for a %d x %d bf16 operand", (int)r, rows, inner);
+    set_error("cuTensorMapEncodeTiled failed (%d) for a %d x %d fp16 operand", (int)r, rows, inner);
     return FFS_ERR_CUDA;
   }
   return FFS_OK;
@@ -275,7 +280,7 @@ using namespace ffsk;
 extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
   clear_error();
   FFS_REQUIRE(a && a->V > 0 && a->T > 0 && a->K > 0 && a->P > 0, "ffs_reml_project_tc: bad sizes");
-  FFS_REQUIRE(a->yr_hi && a->yr_lo && a->u_hi && a->u_lo && a->proj && a->flag,
+  FFS_REQUIRE(a->yr_hi && a->yr_lo && a->u_hi && a->u_lo && a->yexp && a->uexp && a->proj && a->flag,
               "ffs_reml_project_tc: null buffer");
   FFS_REQUIRE(a->ld_y == a->ld_u && a->ld_y % BK == 0 && a->ld_y >= a->T,
               "ffs_reml_project_tc: ld_y=%d and ld_u=%d must be equal multiples of %d", a->ld_y, a->ld_u, BK);
@@ -294,6 +299,8 @@ extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
   if (prm.g > a->P) prm.g = a->P;
   prm.N = ((prm.g * a->K) + 15) / 16 * 16;
   prm.n_col_tiles = ceil_div(a->P, prm.g);
+  prm.yexp = a->yexp;
+  prm.uexp = a->uexp;
   prm.proj = a->proj;
   prm.flag = a->flag;
   CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;

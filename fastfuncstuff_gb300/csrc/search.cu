@@ -62,11 +62,16 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
     }
     if (lane == 0) a.scale[v] = sc;
     if (a.yr_hi) {
+      float amax = 0.f;
+      for (int t = lane; t < T; t += 32) amax = fmaxf(amax, fabsf(row[t]));
+      for (int off = 16; off > 0; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
+      const int e = scale_exp(amax);
+      if (lane == 0) a.yexp[v] = e;
       uint16_t* hi = a.yr_hi + (size_t)v * a.ld_y;
       uint16_t* lo = a.yr_lo + (size_t)v * a.ld_y;
       for (int t = lane; t < a.ld_y; t += 32) {
         uint16_t h = 0, l = 0;
-        if (t < T) split_bf16(row[t], h, l);
+        if (t < T) split_fp16(ldexpf(row[t], e), h, l);
         hi[t] = h;
         lo[t] = l;
       }
@@ -313,7 +318,7 @@ extern "C" int ffs_reml_prep(const ffs_prep_args* a, void* stream) {
   clear_error();
   FFS_REQUIRE(a && a->V > 0 && a->T > 1 && a->K >= 0, "ffs_reml_prep: bad sizes");
   FFS_REQUIRE(a->Y && a->scale && a->yr_t && (a->K == 0 || a->Q0), "ffs_reml_prep: null buffer");
-  FFS_REQUIRE(!a->yr_hi || (a->yr_lo && a->ld_y >= a->T && a->ld_y % 8 == 0),
+  FFS_REQUIRE(!a->yr_hi || (a->yr_lo && a->yexp && a->ld_y >= a->T && a->ld_y % 8 == 0),
               "ffs_reml_prep: ld_y=%d must be >= T and a multiple of 8", a->ld_y);
   const int ld_s = a->T + ((a->T & 1) ? 2 : 1);  // odd stride: conflict-free transposed reads
   const size_t smem = sizeof(float) * PREP_VOX * ld_s;

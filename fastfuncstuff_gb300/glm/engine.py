@@ -9,8 +9,9 @@ Layouts (V voxels, T time points, K design columns, P pairs):
   Y        [V][T] fp32 voxel-major data
   yr_t     [T][V] fp32 residualised, scaled data (time-major, for the O(T)
            recurrences)
-  yr_hi/lo [V][ld] bf16 bits of the same (the projection GEMM's A operand)
-  U_hi/lo  [P*K][ld] bf16 bits of U = L^-T Q (the GEMM's B operand)
+  yr_hi/lo [V][ld] fp16 bits of the same, scaled by 2^yexp[v] (the projection
+           GEMM's A operand)
+  U_hi/lo  [P*K][ld] fp16 bits of U = L^-T Q scaled by 2^uexp[p] (its B operand)
   proj     [P][V], surf [P][V]
 """
 
@@ -79,6 +80,7 @@ class GridFactors:
     glt: torch.Tensor | None
     Gsum: torch.Tensor | None = None
     center: bool = False
+    uexp: torch.Tensor | None = None
 
     @property
     def P(self) -> int:
@@ -140,12 +142,13 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
         task_idx=task_idx, glt=glt_t,
         Gsum=torch.empty(P, K, **f32),
         center=constant_in_span(X.detach().cpu().numpy()),
+        uexp=torch.empty(P, dtype=torch.int32, device=dev) if with_tc else None,
     )
     d = _lib.GridDesc(T=T, K=K, P=P, n_runs=layout.n_runs, run_start=_p(run_start), tau=_p(tau),
                       a=_p(a), b=_p(b), X=_p(Xc), lambda_fp32=0, ld_u=ld,
                       n_task=nt, task_idx=_p(task_idx), n_glt=ng, glt=_p(glt_t))
     o = _lib.GridOut(coef=_p(f.coef), logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), U=_p(f.U),
-                     U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
+                     U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), uexp=_p(f.uexp), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
                      info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=_p(f.Gsum),
                      work=_p(work))
     _lib.check(lib.ffs_grid_build(C.byref(d), C.byref(o), _stream()), "ffs_grid_build")
@@ -182,15 +185,17 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
         raise ValueError("the factors were built without the tensor-core operands")
     yr_hi = torch.empty(V, ld, dtype=torch.int16, device=dev) if use_tc else None
     yr_lo = torch.empty(V, ld, dtype=torch.int16, device=dev) if use_tc else None
+    yexp = torch.empty(V, dtype=torch.int32, device=dev) if use_tc else None
     q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T])
     pa = _lib.PrepArgs(V=V, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=int(f.center), ld_y=ld,
-                       scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo))
+                       scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp))
     _lib.check(lib.ffs_reml_prep(C.byref(pa), st), "ffs_reml_prep")
 
     proj = torch.empty(P, V, dtype=torch.float32, device=dev)
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
     ja = _lib.ProjectArgs(V=V, T=T, K=K, P=P, ld_y=ld, ld_u=ld, yr_hi=_p(yr_hi), yr_lo=_p(yr_lo),
-                          u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yr_t=_p(yr_t), U=_p(f.U), proj=_p(proj),
+                          u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yexp=_p(yexp), uexp=_p(f.uexp),
+                          yr_t=_p(yr_t), U=_p(f.U), proj=_p(proj),
                           flag=_p(flag))
     if use_tc:
         _lib.check(lib.ffs_reml_project_tc(C.byref(ja), st), "ffs_reml_project_tc")

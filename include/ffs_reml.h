@@ -61,9 +61,13 @@ const char* ffs_last_error(void);
  *   logdet_XtX[p]= 2 sum_j log(|L_xtx,jj| + 1e-10)          (FP64)
  *   U[p]         = L^-T Q, Q = X_w L_xtx^-T, stored [P][K][T] fp32:
  *                  ||Q' L^-1 y||^2 = ||U' y||^2 for any series y.
- *   U_hi/U_lo    = the same as a bf16 split (U ~ hi + lo), rows p*K+j of
- *                  length ld_u (>= T, multiple of 8, zero padded): the B
- *                  operand of the projection GEMM.
+ *   U_hi/U_lo    = the same as an fp16 split of U * 2^uexp[p] (hi + lo carry
+ *                  about 22 significant bits; the power of two puts each
+ *                  pair's largest entry in [128, 256)), rows p*K+j of length
+ *                  ld_u (>= T, multiple of 8, zero padded): the B operand of
+ *                  the projection GEMM.
+ *   pairs with lambda == 0 have R = I exactly; their coefficients are the
+ *   identity (c = m = 0, D = 1), so ties between them stay exact ties.
  *   G[p]         = U L_xtx^-1 = R^-1 X (X'R^-1 X)^-1, [P][K][T] fp32:
  *                  GLS betas b = G' y.
  *   Adiag[p][K]  = diag((X_w'X_w)^-1);  XtX[p][K][K] = X_w'X_w (fp32).
@@ -95,8 +99,9 @@ typedef struct {
   double* logdet_R;     /* [P]                                                    */
   double* logdet_XtX;   /* [P]                                                    */
   float* U;             /* [P][K][T]                                              */
-  uint16_t* U_hi;       /* [P*K][ld_u] bf16 bits (may be NULL)                    */
-  uint16_t* U_lo;       /* [P*K][ld_u] bf16 bits (may be NULL)                    */
+  uint16_t* U_hi;       /* [P*K][ld_u] fp16 bits (may be NULL)                    */
+  uint16_t* U_lo;       /* [P*K][ld_u] fp16 bits (may be NULL)                    */
+  int* uexp;            /* [P] power-of-two scale of U_hi/U_lo (with U_hi)        */
   float* G;             /* [P][K][T]                                              */
   float* Adiag;         /* [P][K]                                                 */
   float* XtX;           /* [P][K][K]                                              */
@@ -116,8 +121,9 @@ int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
  *   scale[v] = max(std(Y[v]) (N-1 divisor), 1e-8);
  *   Y_r[v]   = Y[v]/scale[v] - Q0 Q0' (Y[v]/scale[v]), Q0 an orthonormal basis
  *              of the design's columns (U of the pair (0,0) is that basis).
- * Outputs Y_r time-major fp32 and, when yr_hi/yr_lo are given, voxel-major bf16
- * hi/lo splits with row length ld_y (>= T, multiple of 8, zero padded).
+ * Outputs Y_r time-major fp32 and, when yr_hi/yr_lo are given, voxel-major fp16
+ * hi/lo splits of Y_r * 2^yexp[v] (largest entry in [128, 256)) with row length
+ * ld_y (>= T, multiple of 8, zero padded).
  * With do_scale == 0 the data are used as given (scale = 1). With center != 0
  * (only valid when the constant series lies in the design's span) each voxel's
  * mean is subtracted first: the criterion is unchanged, and the float32
@@ -132,8 +138,9 @@ typedef struct {
   int ld_y;
   float* scale;         /* [V]                                                    */
   float* yr_t;          /* [T][V] time-major residualised data                    */
-  uint16_t* yr_hi;      /* [V][ld_y] bf16 bits or NULL                            */
-  uint16_t* yr_lo;      /* [V][ld_y] bf16 bits or NULL                            */
+  uint16_t* yr_hi;      /* [V][ld_y] fp16 bits or NULL                            */
+  uint16_t* yr_lo;      /* [V][ld_y] fp16 bits or NULL                            */
+  int* yexp;            /* [V] power-of-two scale of yr_hi/yr_lo (with yr_hi)     */
 } ffs_prep_args;
 
 int ffs_reml_prep(const ffs_prep_args* a, void* stream);
@@ -141,16 +148,18 @@ int ffs_reml_prep(const ffs_prep_args* a, void* stream);
 /* ------------------------------------------------------------------ projection
  * The ||Q'Y_w||^2 term of fastfuncstuff/glm/arma.py:1992-1995 for every voxel
  * and pair: proj[p][v] = sum_j (sum_t U[p][j][t] Y_r[v][t])^2.
- * ffs_reml_project_tc runs it as a TMA-fed tcgen05 GEMM in split bf16
+ * ffs_reml_project_tc runs it as a TMA-fed tcgen05 GEMM on fp16 hi/lo splits
  * (hi*hi + hi*lo + lo*hi, fp32 accumulation in TMEM) with the square-and-sum
- * epilogue on chip. ffs_reml_project_simt is the CUDA-core form of the same
+ * epilogue on chip, which also removes the power-of-two scales. ffs_reml_project_simt is the CUDA-core form of the same
  * contraction (fp32), used for small or per-voxel-window problems.
  */
 typedef struct {
   int V, T, K, P;
   int ld_y, ld_u;
-  const uint16_t* yr_hi; const uint16_t* yr_lo;   /* [V][ld_y]  */
-  const uint16_t* u_hi;  const uint16_t* u_lo;    /* [P*K][ld_u] */
+  const uint16_t* yr_hi; const uint16_t* yr_lo;   /* [V][ld_y]  fp16 bits */
+  const uint16_t* u_hi;  const uint16_t* u_lo;    /* [P*K][ld_u] fp16 bits */
+  const int* yexp;      /* [V] */
+  const int* uexp;      /* [P] */
   const float* yr_t;    /* [T][V] (simt form)                                    */
   const float* U;       /* [P][K][T] (simt form)                                 */
   float* proj;          /* [P][V]                                                 */

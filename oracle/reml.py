@@ -227,10 +227,16 @@ class Whitener:
 
 
 def _chol_inv(R: np.ndarray):
+    """Cholesky factor's inverse (LAPACK trtri) and log(diag L + 1e-10)."""
+    from scipy.linalg import lapack
+
     L = np.linalg.cholesky(R)
     logdiag = np.log(np.diagonal(L) + 1e-10)
-    Linv = _solve_lower(L, np.eye(R.shape[0], dtype=R.dtype))
-    return Linv, logdiag
+    trtri = lapack.dtrtri if L.dtype == F64 else lapack.strtri
+    Linv, info = trtri(L, lower=1)
+    if info != 0:
+        raise np.linalg.LinAlgError("singular Cholesky factor")
+    return np.tril(Linv), logdiag
 
 
 def _solve_lower(L: np.ndarray, B: np.ndarray) -> np.ndarray:
@@ -679,7 +685,7 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
                    task_indices=None, glt_matrices=None, want_residuals=False,
                    want_ljung_box=False, save_profile_likelihoods=False,
                    precomputed_arma_params=None, fp64_scaled=False, afni_faithful=False,
-                   autocorr=None):
+                   autocorr=None, subset_descent=False):
     """The reference's ``fit_glm_arma11`` for the options this path covers.
 
     Follows fastfuncstuff/glm/arma.py:3650-5878 on ``device=cpu``:
@@ -695,7 +701,10 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
 
     The selector is the hierarchical descent unless ``force_exhaustive_search``;
     the descent runs on the full surface, which selects the same points as the
-    reference's subset-GEMM descent (fastfuncstuff/glm/arma.py:4688-4743).
+    reference's subset-GEMM descent (fastfuncstuff/glm/arma.py:4688-4743). With
+    ``subset_descent`` the descent instead evaluates only the pairs it visits,
+    one subset GEMM per pair, which is the algorithm (and the cost) of the
+    reference's default CPU run (arma.py:4699-4709).
     """
     dt = F64 if use_double else F32
     Y = np.asarray(data)
@@ -738,6 +747,8 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
                 res.reml_lklhd_surface = surf
             else:
                 idx, lik = out
+        elif subset_descent and not save_profile_likelihoods:
+            idx, lik = search_hierarchical_subset(X, Ys, pre, afni_faithful)
         else:
             _, _, surf = search_exhaustive(X, Ys, pre, return_surface=True)
             idx, lik = select_hierarchical_from_surface(surf, grid, afni_faithful)
@@ -788,8 +799,12 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
                    np.zeros(1, np.int64), np.zeros(1, np.int64))
         if one.lam[0] < 0 or abs(a_opt) >= 1 or abs(b_opt) >= 1:
             raise ValueError(f"Invalid ARMA(1,1) parameters: a={a_opt}, b={b_opt}")
-        whs, _ = arma11_whiteners(one, T, run_starts, tau, dt)
-        o = gls_at(X, Ys[members], whs[0], dof, task_indices, C, want_residuals, lj)
+        if precomputed_arma_params is None:
+            # the search grid already holds this pair's whitener (arma.py:4837-4841)
+            wh = pre.whiteners[int(idx[members[0]])]
+        else:
+            wh = arma11_whiteners(one, T, run_starts, tau, dt)[0][0]
+        o = gls_at(X, Ys[members], wh, dof, task_indices, C, want_residuals, lj)
         ti = list(task_indices) if task_indices else slice(None)
         res.betas[members] = o["beta"][:, ti]
         res.tstats[members] = o["t"][:, ti]

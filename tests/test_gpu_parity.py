@@ -125,9 +125,11 @@ def test_tensor_core_projection_matches_simt(K, T, V):
         outs[proj] = so
     s_tc = outs["tc"].surf.cpu().numpy()
     s_si = outs["simt"].surf.cpu().numpy()
-    # criterion differences agree to well below one grid step
-    assert np.abs(s_tc - s_si).max() < 5e-3, np.abs(s_tc - s_si).max()
-    np.testing.assert_array_equal(outs["tc"].best.cpu().numpy()[:50] >= 0, True)
+    # the two projections agree to float32 level: criterion differences within
+    # 2e-6 of the criterion's size (fp16 hi/lo split: ~2^-22 per product)
+    c0 = np.abs(outs["simt"].crit0.cpu().numpy())[None, :]
+    assert (np.abs(s_tc - s_si) / np.maximum(c0, 1.0)).max() < 2e-6, np.abs(s_tc - s_si).max()
+    np.testing.assert_array_equal(outs["tc"].best.cpu().numpy(), outs["simt"].best.cpu().numpy())
 
 
 # ------------------------------------------------------------- full fits
