@@ -37,6 +37,55 @@ def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 
 
+# kernels each library entry point launches (for launch accounting)
+LAUNCHES = {"ffs_grid_build": 1, "ffs_reml_prep": 1, "ffs_reml_project_tc": 1, "ffs_reml_project_simt": 1,
+            "ffs_reml_surface": 1, "ffs_reml_select": 1, "ffs_reml_group": 3, "ffs_reml_gls": 1,
+            "ffs_reml_gls_ex": 1}
+
+
+class StageTimer:
+    """Records a CUDA event pair around every library call on the current stream.
+
+    ``launches`` counts this library's kernel launches; ``summary()`` returns,
+    per entry point, its number of calls and mean device time in ms (call it
+    after synchronising).
+    """
+
+    def __init__(self):
+        self.events: list[tuple[str, torch.cuda.Event, torch.cuda.Event]] = []
+        self.launches = 0
+
+    def summary(self) -> dict:
+        out: dict = {}
+        for name, e0, e1 in self.events:
+            d = out.setdefault(name, [0, 0.0])
+            d[0] += 1
+            d[1] += e0.elapsed_time(e1)
+        return {k: {"calls": n, "mean_ms": t / n} for k, (n, t) in out.items()}
+
+
+_TIMER: StageTimer | None = None
+
+
+def set_stage_timer(timer: StageTimer | None) -> None:
+    global _TIMER
+    _TIMER = timer
+
+
+def _run(name: str, fn, *args) -> None:
+    t = _TIMER
+    if t is None:
+        _lib.check(fn(*args), name)
+        return
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    _lib.check(fn(*args), name)
+    e1.record()
+    t.events.append((name, e0, e1))
+    t.launches += LAUNCHES.get(name, 1)
+
+
 def padded_ld(T: int) -> int:
     return (T + LD_ALIGN - 1) // LD_ALIGN * LD_ALIGN
 
@@ -151,7 +200,7 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
                      U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), uexp=_p(f.uexp), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
                      info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=_p(f.Gsum),
                      work=_p(work))
-    _lib.check(lib.ffs_grid_build(C.byref(d), C.byref(o), _stream()), "ffs_grid_build")
+    _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
     f._keep = (Xc, run_start, tau, work)  # inputs must outlive the launch
     return f
 
@@ -189,7 +238,7 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
     q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T])
     pa = _lib.PrepArgs(V=V, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=int(f.center), ld_y=ld,
                        scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp))
-    _lib.check(lib.ffs_reml_prep(C.byref(pa), st), "ffs_reml_prep")
+    _run("ffs_reml_prep", lib.ffs_reml_prep, C.byref(pa), st)
 
     proj = torch.empty(P, V, dtype=torch.float32, device=dev)
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -198,9 +247,9 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
                           yr_t=_p(yr_t), U=_p(f.U), proj=_p(proj),
                           flag=_p(flag))
     if use_tc:
-        _lib.check(lib.ffs_reml_project_tc(C.byref(ja), st), "ffs_reml_project_tc")
+        _run("ffs_reml_project_tc", lib.ffs_reml_project_tc, C.byref(ja), st)
     elif projector == "simt":
-        _lib.check(lib.ffs_reml_project_simt(C.byref(ja), st), "ffs_reml_project_simt")
+        _run("ffs_reml_project_simt", lib.ffs_reml_project_simt, C.byref(ja), st)
     else:
         raise ValueError(f"unknown projector {projector!r}")
 
@@ -210,7 +259,7 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
                           logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), proj=_p(proj),
                           chunk_start=_p(f.chunk_start), n_chunks=f.chunk_start.numel() - 1,
                           chunk_pairs=_p(f.chunk_pairs), surf=_p(surf), crit0=_p(crit0))
-    _lib.check(lib.ffs_reml_surface(C.byref(sa), st), "ffs_reml_surface")
+    _run("ffs_reml_surface", lib.ffs_reml_surface, C.byref(sa), st)
 
     best = torch.empty(V, dtype=torch.int32, device=dev)
     best_crit = torch.empty(V, dtype=torch.float32, device=dev)
@@ -218,7 +267,7 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
     se = _lib.SelectArgs(V=V, P=P, surf=_p(surf), crit0=_p(crit0), hierarchical=int(hierarchical),
                          n_a=len(g.a_axis), n_b=len(g.b_axis), ltop=g.ltop, za=g.za, zb=g.zb,
                          lattice=_p(f.lattice), best=_p(best), best_crit=_p(best_crit))
-    _lib.check(lib.ffs_reml_select(C.byref(se), st), "ffs_reml_select")
+    _run("ffs_reml_select", lib.ffs_reml_select, C.byref(se), st)
     out = SearchOut(best=best, best_crit=best_crit, scale=scale)
     out._flag = flag
     if keep_surface:
@@ -253,7 +302,7 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
     Y = Y.to(dtype=torch.float32).contiguous()
     order = torch.empty(V, dtype=torch.int32, device=dev)
     work = torch.empty(P + 1, dtype=torch.int32, device=dev)
-    _lib.check(lib.ffs_reml_group(V, P, _p(best), _p(work), _p(order), st), "ffs_reml_group")
+    _run("ffs_reml_group", lib.ffs_reml_group, V, P, _p(best), _p(work), _p(order), st)
     Xt = X.to(device=dev, dtype=torch.float32).t().contiguous()
     f32 = dict(device=dev, dtype=torch.float32)
     ng = 0 if f.glt is None else f.glt.shape[0]
@@ -277,10 +326,9 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
         ptau_d = None if ptau is None else torch.from_numpy(ptau).to(dev)
         w_d = torch.from_numpy(w).to(dev)
         o.ljung_box = torch.empty(V, **f32)
-        _lib.check(lib.ffs_reml_gls_ex(C.byref(ga), h, _p(ptau_d), _p(w_d), _p(o.ljung_box), st),
-                   "ffs_reml_gls_ex")
+        _run("ffs_reml_gls_ex", lib.ffs_reml_gls_ex, C.byref(ga), h, _p(ptau_d), _p(w_d), _p(o.ljung_box), st)
         o._keep = (ptau_d, w_d)
     else:
-        _lib.check(lib.ffs_reml_gls(C.byref(ga), st), "ffs_reml_gls")
+        _run("ffs_reml_gls", lib.ffs_reml_gls, C.byref(ga), st)
     o._keep2 = (Y, order, work, Xt)
     return o

@@ -107,7 +107,7 @@ class RemlGrid:
     zb: int
     ltop: int
     chunk_start: np.ndarray  # (n_chunks + 1,) int32
-    chunk_pairs: np.ndarray  # (P,) int32
+    chunk_pairs: np.ndarray  # (P,) int32 pairs of each chunk (one AR filter per chunk)
     lambda_fp32: bool
 
     @property
@@ -125,6 +125,31 @@ class RemlGrid:
         bi_c = np.clip(bi, 0, len(self.b_axis) - 1)
         hit = (self.a_axis[ai_c] == a) & (self.b_axis[bi_c] == b)
         return np.where(hit, self.lattice[ai_c, bi_c], -1)
+
+
+def lambda_is_zero(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """lambda == 0 exactly in float64 (a + b of two float32 values is exact)."""
+    return (np.asarray(a, np.float64) + np.asarray(b, np.float64)) == 0.0
+
+
+def coefficient_chunks(a: np.ndarray, b: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Chunks of pairs whose AR filter coefficients c_t are identical.
+
+    Pairs sharing a share c_t = a^gap; pairs with lambda == 0 (R = I) use the
+    identity (c = 0) whatever their a, so they form one class of their own.
+    Each class is split into chunks of at most SURFACE_CHUNK pairs, in pair order.
+    """
+    ident = lambda_is_zero(a, b)
+    classes: dict = {}
+    for p in range(a.size):
+        key = "identity" if ident[p] else float(a[p])
+        classes.setdefault(key, []).append(p)
+    starts, pairs = [0], []
+    for members in classes.values():
+        for i in range(0, len(members), SURFACE_CHUNK):
+            pairs.extend(members[i : i + SURFACE_CHUNK])
+            starts.append(len(pairs))
+    return np.asarray(starts, np.int32), np.asarray(pairs, np.int32)
 
 
 def hierarchical_ltop(n_a: int, n_b: int, afni_faithful: bool) -> int:
@@ -163,15 +188,10 @@ def make_grid(a_grid, b_grid, use_double: bool = False) -> RemlGrid:
     p0 = int(lattice[za, zb])
     if p0 < 0:
         raise ValueError("the (0, 0) pair is missing from the valid grid")
-    # chunks of pairs that share a (pairs are a-major, so these are contiguous runs)
-    starts = [0]
-    for i in range(1, a.size + 1):
-        if i == a.size or a[i] != a[i - 1] or i - starts[-1] == SURFACE_CHUNK:
-            starts.append(i)
+    chunk_start, chunk_pairs = coefficient_chunks(a, b)
     return RemlGrid(a=a, b=b, a_axis=a_axis, b_axis=b_axis, lattice=lattice, p0=p0, za=za, zb=zb,
                     ltop=hierarchical_ltop(len(a_axis), len(b_axis), _REML_MODE.afni_faithful),
-                    chunk_start=np.asarray(starts, dtype=np.int32),
-                    chunk_pairs=np.arange(a.size, dtype=np.int32), lambda_fp32=not use_double)
+                    chunk_start=chunk_start, chunk_pairs=chunk_pairs, lambda_fp32=not use_double)
 
 
 def grid_of_pairs(a: np.ndarray, b: np.ndarray, use_double: bool = False) -> RemlGrid:
@@ -186,13 +206,9 @@ def grid_of_pairs(a: np.ndarray, b: np.ndarray, use_double: bool = False) -> Rem
         raise ValueError(f"Invalid ARMA(1,1) parameters: a={a[i]}, b={b[i]}")
     P = a.size
     lattice = np.arange(P, dtype=np.int32).reshape(P, 1)
-    starts = [0]
-    for i in range(1, P + 1):
-        if i == P or a[i] != a[i - 1] or i - starts[-1] == SURFACE_CHUNK:
-            starts.append(i)
+    chunk_start, chunk_pairs = coefficient_chunks(a, b)
     return RemlGrid(a=a, b=b, a_axis=a.copy(), b_axis=b.copy(), lattice=lattice, p0=0, za=0, zb=0,
-                    ltop=0, chunk_start=np.asarray(starts, np.int32),
-                    chunk_pairs=np.arange(P, dtype=np.int32), lambda_fp32=not use_double)
+                    ltop=0, chunk_start=chunk_start, chunk_pairs=chunk_pairs, lambda_fp32=not use_double)
 
 
 # ---------------------------------------------------------------- runs / censor

@@ -38,11 +38,19 @@ def test_grid_matches_oracle(grids, use_double):
         ai = np.searchsorted(g.a_axis, g.a[p])
         bi = np.searchsorted(g.b_axis, g.b[p])
         assert g.lattice[ai, bi] == p
+    # every chunk shares one AR filter: one a, or only lambda == 0 pairs (identity)
+    ident = G.lambda_is_zero(g.a, g.b)
     for c in range(len(g.chunk_start) - 1):
         s, e = g.chunk_start[c], g.chunk_start[c + 1]
         assert 0 < e - s <= G.SURFACE_CHUNK
-        assert len(set(g.a[s:e].tolist())) == 1
+        members = g.chunk_pairs[s:e]
+        if ident[members].any():
+            assert ident[members].all()
+        else:
+            assert len(set(g.a[members].tolist())) == 1
     assert g.chunk_start[-1] == g.P
+    assert sorted(g.chunk_pairs.tolist()) == list(range(g.P))
+    assert ident[g.p0]
 
 
 def test_grid_counts_and_default():
@@ -143,3 +151,37 @@ def test_synthetic_workloads_are_seeded_and_shaped():
     r1 = (n[:, 1:] * n[:, :-1]).mean(1)
     lam = (0.6 + 0.2) * (1 + 0.12) / (1 + 0.04 + 0.24)
     np.testing.assert_allclose(r1, lam, atol=0.06)
+
+
+@pytest.mark.parametrize("case", ["single", "multirun", "censored"])
+def test_kernel_model_with_host_structures_matches_oracle(case):
+    """The kernels' float32 arithmetic, driven by the product's grid/chunks/runs,
+    selects what the FP64 oracle selects (exact ties included)."""
+    from tests import kernel_model as km
+
+    d = load_golden(case)
+    X, Y = d["X"].astype(np.float64), d["Y"].astype(np.float64)
+    T, K = X.shape
+    rs = d["run_starts"] if "run_starts" in d else None
+    tau = d["tau"] if "tau" in d else None
+    g = G.make_grid(d["a_grid"], d["b_grid"])
+    lay = G.run_layout(T, rs, tau)
+    og = o.valid_grid(d["a_grid"], d["b_grid"], np.float64)
+    pre = o.precompute_reml_grid(X, og, rs, tau)
+    s = np.maximum(np.std(Y, axis=1, ddof=1).astype(np.float32), np.float32(1e-8)).astype(np.float64)
+    Ys = Y / s[:, None]
+    _, _, surf64 = o.search_exhaustive(X, Ys, pre, return_surface=True)
+    Q0, _ = np.linalg.qr(X)
+    yr = (Ys - (Ys @ Q0) @ Q0.T).astype(np.float32)
+    coef = np.stack([km.coefficients(g.a[p], g.b[p], lay.tau, lay.run_start) for p in range(g.P)])
+    proj = np.stack([((yr.astype(np.float64) @ (pre.whiteners[p].dense().T @ pre.Q[p])) ** 2).sum(1)
+                     for p in range(g.P)]).astype(np.float32)
+    const = pre.logdet_R + pre.logdet_XtX
+    dd, crit0 = km.surface(yr, g, coef, proj, const, K)
+    best = km.select_exhaustive(dd, g)
+    ref = np.argmin(surf64, axis=1)
+    agree = (best == ref).mean()
+    assert agree >= 0.99, agree
+    bad = best != ref
+    gap = np.abs(surf64[bad, best[bad]] - surf64[bad, ref[bad]]) / np.abs(surf64[bad, ref[bad]])
+    assert gap.size == 0 or gap.max() <= 1e-6
