@@ -235,6 +235,7 @@ def fit_glm_arma11(
     *,
     projector: str = "tc",
     return_device: bool = False,
+    proposal=None,
 ) -> ARMA11Results:
     """Fit a GLM with ARMA(1,1) REML prewhitening (fastfuncstuff/glm/arma.py:3650).
 
@@ -325,10 +326,23 @@ def fit_glm_arma11(
     chunks = {k: [] for k in ("best", "crit", "surf", "betas", "tstats", "sigma2", "fstats", "r2", "lam",
                               "cb", "ct", "resid", "resid_w", "pred", "lb")}
     proj = projector if (projector != "tc" or factors.U_hi is not None) else "simt"
+    Ut = None
+    if proposal is not None and best_all is None:
+        from . import learned
+
+        Ut = learned.transpose_u(factors)
+        layout_l = layout
+        fallbacks = []
     for v0 in range(0, V, bs):
         v1 = min(V, v0 + bs)
         Yb = Y[v0:v1].to(device=device, dtype=torch.float32, non_blocking=True)
-        if best_all is None:
+        if best_all is None and proposal is not None:
+            lo = learned.learned_search(Yb, factors, proposal, layout_l, do_scale=not use_double, Ut=Ut)
+            best, scale = lo.best, lo.scale
+            chunks["best"].append(best)
+            chunks["crit"].append(lo.best_crit)
+            fallbacks.append(lo.fallback)
+        elif best_all is None:
             so = engine.search(Yb, factors, hierarchical=not force_exhaustive_search, projector=proj,
                                do_scale=not use_double, keep_surface=save_profile_likelihoods)
             best, scale = so.best, so.scale
@@ -404,6 +418,8 @@ def fit_glm_arma11(
     if save_profile_likelihoods and chunks["surf"]:
         res.reml_lklhd_surface = out(cat("surf"))
         res.reml_surface_params = grid.param_list()
+    if proposal is not None and best_all is None:
+        res.learned_fallback = float(torch.cat(fallbacks).float().mean().item())
     if spatial_metadata:
         res.voxel_mask = spatial_metadata.get("voxel_mask")
         res.full_shape = spatial_metadata.get("volume_shape")

@@ -212,13 +212,42 @@ class SearchOut:
     scale: torch.Tensor       # [V] float32 per-voxel std
     surf: torch.Tensor | None = None   # [P][V] criterion relative to (0,0)
     crit0: torch.Tensor | None = None  # [V] float64 criterion at (0,0)
+    yr_t: torch.Tensor | None = None   # [T][V] residualised, scaled data
+
+
+@dataclass
+class PrepOut:
+    scale: torch.Tensor
+    yr_t: torch.Tensor
+    yr_hi: torch.Tensor | None
+    yr_lo: torch.Tensor | None
+    yexp: torch.Tensor | None
+
+
+def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core: bool = True) -> PrepOut:
+    """Per-voxel scaling and residualisation (and the fp16 split for the GEMM)."""
+    lib = _lib.load()
+    dev = Y.device
+    V, T = Y.shape
+    K, ld = f.K, f.ld
+    Y = Y.to(dtype=torch.float32).contiguous()
+    scale = torch.empty(V, dtype=torch.float32, device=dev)
+    yr_t = torch.empty(T, V, dtype=torch.float32, device=dev)
+    yr_hi = torch.empty(V, ld, dtype=torch.int16, device=dev) if tensor_core else None
+    yr_lo = torch.empty(V, ld, dtype=torch.int16, device=dev) if tensor_core else None
+    yexp = torch.empty(V, dtype=torch.int32, device=dev) if tensor_core else None
+    q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T])
+    pa = _lib.PrepArgs(V=V, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=int(f.center), ld_y=ld,
+                       scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp))
+    _run("ffs_reml_prep", lib.ffs_reml_prep, C.byref(pa), _stream())
+    return PrepOut(scale, yr_t, yr_hi, yr_lo, yexp)
 
 
 def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projector: str = "tc",
-           do_scale: bool = True, keep_surface: bool = False) -> SearchOut:
+           do_scale: bool = True, keep_surface: bool = False, keep_yr: bool = False) -> SearchOut:
     """REML grid search of every voxel of ``Y`` (V, T) against the factors ``f``.
 
-    ``projector`` picks the projection kernel: "tc" (tcgen05 split-bf16 GEMM) or
+    ``projector`` picks the projection kernel: "tc" (tcgen05 fp16-split GEMM) or
     "simt" (fp32 CUDA cores).
     """
     lib = _lib.load()
@@ -226,36 +255,26 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
     V, T = Y.shape
     K, P, ld = f.K, f.P, f.ld
     st = _stream()
-    Y = Y.to(dtype=torch.float32).contiguous()
-    scale = torch.empty(V, dtype=torch.float32, device=dev)
-    yr_t = torch.empty(T, V, dtype=torch.float32, device=dev)
     use_tc = projector == "tc"
     if use_tc and f.U_hi is None:
         raise ValueError("the factors were built without the tensor-core operands")
-    yr_hi = torch.empty(V, ld, dtype=torch.int16, device=dev) if use_tc else None
-    yr_lo = torch.empty(V, ld, dtype=torch.int16, device=dev) if use_tc else None
-    yexp = torch.empty(V, dtype=torch.int32, device=dev) if use_tc else None
-    q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T])
-    pa = _lib.PrepArgs(V=V, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=int(f.center), ld_y=ld,
-                       scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp))
-    _run("ffs_reml_prep", lib.ffs_reml_prep, C.byref(pa), st)
+    if projector not in ("tc", "simt"):
+        raise ValueError(f"unknown projector {projector!r}")
+    pr = prep(Y, f, do_scale=do_scale, tensor_core=use_tc)
 
     proj = torch.empty(P, V, dtype=torch.float32, device=dev)
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
-    ja = _lib.ProjectArgs(V=V, T=T, K=K, P=P, ld_y=ld, ld_u=ld, yr_hi=_p(yr_hi), yr_lo=_p(yr_lo),
-                          u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yexp=_p(yexp), uexp=_p(f.uexp),
-                          yr_t=_p(yr_t), U=_p(f.U), proj=_p(proj),
-                          flag=_p(flag))
+    ja = _lib.ProjectArgs(V=V, T=T, K=K, P=P, ld_y=ld, ld_u=ld, yr_hi=_p(pr.yr_hi), yr_lo=_p(pr.yr_lo),
+                          u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yexp=_p(pr.yexp), uexp=_p(f.uexp),
+                          yr_t=_p(pr.yr_t), U=_p(f.U), proj=_p(proj), flag=_p(flag))
     if use_tc:
         _run("ffs_reml_project_tc", lib.ffs_reml_project_tc, C.byref(ja), st)
-    elif projector == "simt":
-        _run("ffs_reml_project_simt", lib.ffs_reml_project_simt, C.byref(ja), st)
     else:
-        raise ValueError(f"unknown projector {projector!r}")
+        _run("ffs_reml_project_simt", lib.ffs_reml_project_simt, C.byref(ja), st)
 
     surf = torch.empty(P, V, dtype=torch.float32, device=dev)
     crit0 = torch.empty(V, dtype=torch.float64, device=dev)
-    sa = _lib.SurfaceArgs(V=V, T=T, K=K, P=P, p0=f.grid.p0, yr_t=_p(yr_t), coef=_p(f.coef),
+    sa = _lib.SurfaceArgs(V=V, T=T, K=K, P=P, p0=f.grid.p0, yr_t=_p(pr.yr_t), coef=_p(f.coef),
                           logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), proj=_p(proj),
                           chunk_start=_p(f.chunk_start), n_chunks=f.chunk_start.numel() - 1,
                           chunk_pairs=_p(f.chunk_pairs), surf=_p(surf), crit0=_p(crit0))
@@ -268,10 +287,12 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
                          n_a=len(g.a_axis), n_b=len(g.b_axis), ltop=g.ltop, za=g.za, zb=g.zb,
                          lattice=_p(f.lattice), best=_p(best), best_crit=_p(best_crit))
     _run("ffs_reml_select", lib.ffs_reml_select, C.byref(se), st)
-    out = SearchOut(best=best, best_crit=best_crit, scale=scale)
+    out = SearchOut(best=best, best_crit=best_crit, scale=pr.scale)
     out._flag = flag
     if keep_surface:
         out.surf, out.crit0 = surf, crit0
+    if keep_yr:
+        out.yr_t = pr.yr_t
     return out
 
 

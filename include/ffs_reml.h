@@ -265,6 +265,55 @@ int ffs_reml_gls_ex(const ffs_gls_args* a, int lj_h, const int* lj_tau, const fl
  * work: int[P + 1]. */
 int ffs_reml_group(int V, int P, const int* best, int* work, int* order, void* stream);
 
+/* --------------------------------------------------------- learned proposal
+ * No counterpart in the reference: this build's learned seed for the grid
+ * search. A 9 -> 64 -> 64 -> 2 GELU MLP maps each voxel's OLS-residual
+ * autocorrelations (lags 1-8) and T/1000 to a proposed (a, b); only the 5 x 5
+ * lattice window around it is evaluated, and voxels whose best pair touches a
+ * valid lattice neighbour outside the window fall back to the full grid.
+ * Parameters are one float32 vector of ffs_mlp_param_count() entries:
+ * W1[64][9], b1[64], W2[64][64], b2[64], W3[2][64], b3[2].
+ */
+int ffs_mlp_param_count(void);
+
+/* Training voxels: per run y_t = a y_{t-1} + e_t + b e_{t-1} (200 burn-in
+ * samples, standardised), Y[v] = X beta + sigma noise, beta ~ N(0,1),
+ * sigma ~ U(0.5, 2); Philox4x32-10 counter-based normals (seed, voxel). */
+int ffs_arma_simulate(int V, int T, int K, int n_runs, const int* run_start, const float* X, const float* a,
+                      const float* b, uint64_t seed, float* Y, void* stream);
+
+/* feats[v] = (sum_runs sum_t r_t r_{t+k} / sum r^2 for k = 1..8, T/1000) of the
+ * residualised series yr_t ([T][V], the prep output). */
+int ffs_reml_features(int V, int T, int n_runs, const int* run_start, const float* yr_t, float* feats,
+                      void* stream);
+
+int ffs_mlp_forward(const float* params, const float* x, int B, float* out, void* stream);
+
+/* grad += d/dparams of sum_b (out_b - y_b)^2 / (2 n_total) over the B samples
+ * idx[0..B) (or 0..B when idx is NULL); loss += the same sum. */
+int ffs_mlp_grad(const float* params, const float* x, const float* y, const int* idx, int B, int n_total,
+                 float* grad, float* loss, void* stream);
+
+/* One bias-corrected Adam step (step >= 1); consumes and zeroes grad. */
+int ffs_mlp_adam(float* params, float* grad, float* m, float* v, int n, float lr, float beta1, float beta2,
+                 float eps, int step, void* stream);
+
+/* center[v] = ai * n_b + bi of the lattice point nearest the proposal prop[v]. */
+int ffs_reml_centers(int V, const float* prop, const float* a_axis, int n_a, const float* b_axis, int n_b,
+                     int* center, void* stream);
+
+/* U [P][K][T] -> Ut [P][T][K] (the windowed refine reads a time point's K values). */
+int ffs_transpose_u(int P, int K, int T, const float* U, float* Ut, void* stream);
+
+/* The windowed refine (see above): per voxel (in `order`, grouped by centre),
+ * best pair of its 5 x 5 window, its criterion relative to (0, 0) (dbest),
+ * crit0 as in ffs_reml_surface, and fallback[v] = 1 when the full grid must
+ * decide. K <= 32. */
+int ffs_reml_window(int V, int T, int K, int P, int p0, int n_a, int n_b, const int* lattice, const int* center,
+                    const int* order, const float* yr_t, const float* coef, const float* Ut,
+                    const double* logdet_R, const double* logdet_XtX, int* best, float* dbest, double* crit0,
+                    int* fallback, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

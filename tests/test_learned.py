@@ -1,0 +1,144 @@
+"""The learned proposal: CPU oracle pinned by finite differences, GPU kernels
+against the oracle, and what the trained network gains in the search."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import mlp as om
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    p = om.init(1).astype(np.float64) + 0.01 * rng.standard_normal(om.N_PARAMS)
+    x = rng.standard_normal((7, om.N_IN))
+    y = rng.standard_normal((7, 2)) * 0.5
+    _, g = om.loss_and_grad(p, x, y)
+    for i in rng.choice(om.N_PARAMS, 40, replace=False):
+        e = np.zeros(om.N_PARAMS)
+        e[i] = 1e-6
+        num = (om.loss_and_grad(p + e, x, y)[0] - om.loss_and_grad(p - e, x, y)[0]) / 2e-6
+        assert abs(num - g[i]) <= 1e-6 + 1e-5 * abs(g[i]), (i, num, g[i])
+
+
+def test_oracle_features_of_an_ar1_series():
+    rng = np.random.default_rng(1)
+    n, a = 20000, 0.6
+    e = rng.standard_normal(n)
+    y = np.zeros(n)
+    for t in range(1, n):
+        y[t] = a * y[t - 1] + e[t]
+    f = om.features(y[None], [0, n])[0]
+    np.testing.assert_allclose(f[:8], a ** np.arange(1, 9), atol=0.03)
+    assert f[8] == n / 1000.0
+    # no lag products across a run boundary
+    z = np.ones((1, 10))
+    f2 = om.features(z, [0, 5, 10])[0]
+    assert f2[0] == pytest.approx(8 / 10)  # 4 + 4 lag-1 products over 10
+
+
+def test_oracle_adam_step():
+    p = np.ones(3)
+    g = np.array([1.0, -2.0, 0.0])
+    p1, m, v = om.adam(p, g, np.zeros(3), np.zeros(3), 1, lr=0.1)
+    np.testing.assert_allclose(p1, [0.9, 1.1, 1.0], atol=1e-6)
+
+
+# ------------------------------------------------------------------ GPU
+
+
+@pytest.mark.gpu
+def test_gpu_mlp_forward_grad_adam_match_oracle():
+    from fastfuncstuff_gb300 import _lib
+    from fastfuncstuff_gb300.glm import learned
+
+    dev = torch.device("cuda:0")
+    assert _lib.load().ffs_mlp_param_count() == om.N_PARAMS
+    rng = np.random.default_rng(3)
+    p = (om.init(5) + 0.02 * rng.standard_normal(om.N_PARAMS)).astype(np.float32)
+    B = 1000
+    x = rng.standard_normal((B, om.N_IN)).astype(np.float32)
+    y = (rng.standard_normal((B, 2)) * 0.4).astype(np.float32)
+    pt = torch.from_numpy(p).to(dev)
+    xt, yt = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
+    out = learned.ArmaProposal(pt).forward(xt).cpu().numpy()
+    np.testing.assert_allclose(out, om.forward(p, x), rtol=1e-4, atol=1e-5)
+    grad = torch.zeros(om.N_PARAMS, device=dev)
+    loss = torch.zeros(1, device=dev)
+    learned.mlp_grad(pt, xt, yt, None, B, grad, loss)
+    L, g = om.loss_and_grad(p.astype(np.float64), x, y)
+    gg = grad.cpu().numpy()
+    assert np.abs(gg - g).max() <= 1e-4 * np.abs(g).max(), np.abs(gg - g).max() / np.abs(g).max()
+    assert float(loss.item()) == pytest.approx(L, rel=1e-4)
+    # Adam consumes the gradient
+    m = torch.zeros_like(grad)
+    v = torch.zeros_like(grad)
+    learned.adam(pt, grad, m, v, 1e-2, 1)
+    p1, _, _ = om.adam(p.astype(np.float64), g, np.zeros_like(g), np.zeros_like(g), 1, lr=1e-2)
+    np.testing.assert_allclose(pt.cpu().numpy(), p1, atol=2e-5)
+    assert float(grad.abs().max()) == 0.0
+
+
+@pytest.mark.gpu
+def test_gpu_features_and_simulator():
+    from fastfuncstuff_gb300 import synth
+    from fastfuncstuff_gb300.glm import engine, learned
+    from fastfuncstuff_gb300.glm import grid as G
+
+    dev = torch.device("cuda:0")
+    w = synth.workload(1, V=64)
+    lay = G.run_layout(w.T, w.run_starts)
+    X = torch.from_numpy(w.X).to(dev)
+    V = 4000
+    a = torch.full((V,), 0.6, device=dev)
+    b = torch.full((V,), 0.2, device=dev)
+    Y = learned.simulate(torch.zeros_like(X), lay, a, b, seed=11)  # zero design: pure noise
+    yn = Y.cpu().numpy().astype(np.float64)
+    r1 = np.concatenate([(yn[:, 1:200] * yn[:, :199]).mean(1), (yn[:, 201:] * yn[:, 200:399]).mean(1)]).mean()
+    lam = (0.6 + 0.2) * (1 + 0.12) / (1 + 0.04 + 0.24)
+    assert abs(r1 - lam) < 0.02, (r1, lam)
+    np.testing.assert_allclose(yn[:, :200].std(1, ddof=1), 1.0, atol=1e-4)  # standardised per run
+    # features of the residualised data against the oracle
+    g = G.make_grid(torch.linspace(-0.8, 0.8, 9), torch.linspace(-0.8, 0.8, 9))
+    f = engine.build_factors(X, g, lay, with_tc=False)
+    Yd = torch.from_numpy(w.Y).to(dev)
+    pre = engine.prep(Yd, f, tensor_core=False)
+    feats = learned.features(pre.yr_t, lay).cpu().numpy()
+    ref = om.features(pre.yr_t.t().cpu().numpy(), lay.run_start)
+    np.testing.assert_allclose(feats, ref, rtol=1e-4, atol=1e-5)
+
+
+@pytest.mark.gpu
+def test_learned_search_agrees_with_full_grid_and_beats_untrained():
+    """Train a small proposal on workload-1 designs, then compare the seeded
+    search with the full-grid exhaustive argmin on held-out simulated voxels,
+    and with the same search seeded by the untrained network."""
+    from fastfuncstuff_gb300 import synth
+    from fastfuncstuff_gb300.glm import engine, learned
+    from fastfuncstuff_gb300.glm import grid as G
+
+    dev = torch.device("cuda:0")
+    w = synth.workload(1, V=64)
+    lay = G.run_layout(w.T, w.run_starts)
+    X = torch.from_numpy(w.X).to(dev)
+    gr = torch.linspace(-0.8, 0.8, 33)
+    f = engine.build_factors(X, G.make_grid(gr, gr), lay)
+    x, y = learned.training_set(X, f, lay, 200_000, seed=5)
+    prop, hist = learned.train(x, y, epochs=8, batch=4096, lr=3e-3, seed=1)
+    assert hist[-1]["holdout_loss"] < 0.5 * hist[0]["holdout_loss"]
+    # held-out voxels
+    a_t = torch.from_numpy(f.grid.a).to(dev)
+    b_t = torch.from_numpy(f.grid.b).to(dev)
+    idx = torch.randint(0, f.P, (20_000,), generator=torch.Generator().manual_seed(9)).to(dev)
+    Y = learned.simulate(X, lay, a_t[idx], b_t[idx], seed=4242)
+    full = engine.search(Y, f, hierarchical=False)
+    seeded = learned.learned_search(Y, f, prop, lay)
+    agree = (seeded.best == full.best).float().mean().item()
+    fb = seeded.fallback.float().mean().item()
+    untrained = learned.learned_search(Y, f, learned.ArmaProposal(learned.init_params(1, dev)), lay)
+    fb0 = untrained.fallback.float().mean().item()
+    print(f"learned: agreement {agree:.5f}, fallback {fb:.4f}; untrained fallback {fb0:.4f}")
+    assert agree >= 0.999
+    assert fb < 0.5 * fb0  # the trained network keeps most voxels inside their window
