@@ -18,6 +18,8 @@
 // kernel emits U = L^-T Q (the projection that lets the search skip the
 // whitening GEMM) and G = U L_xtx^-1 (the GLS solve), and the per-pair GLS
 // constants of fastfuncstuff/glm/arma.py:4853-4905.
+#include <mutex>
+
 #include "common.cuh"
 
 namespace ffsk {
@@ -388,4 +390,84 @@ extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, voi
   BuildArgs args{*d, *o};
   grid_build_kernel<<<d->P, 256, 0, (cudaStream_t)stream>>>(args);
   return check_launch("grid_build_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of ffs_grid_build.
+//
+// Some callers cannot allocate device memory at the point where they build the
+// grid factors: code running under a framework allocator that already owns
+// the device's memory, or an embedding (for example a foreign-language binding
+// driving the library from inside a larger pipeline) that is handed only its
+// input and output buffers and has no allocator of its own. For them the FP64
+// scratch lives in this file-scope device array instead of a caller-provided
+// workspace. Every GPU that loads the library holds the array until the
+// process exits.
+namespace ffsk {
+namespace {
+
+constexpr size_t kStaticGridScratchBytes = (size_t)16 << 20;  // 16 MiB
+static __device__ __align__(256) double g_grid_scratch[kStaticGridScratchBytes / sizeof(double)];
+
+// Device address of g_grid_scratch, resolved once per device with that device
+// current (host code may only pass this address to kernels, never the symbol).
+double* static_grid_scratch(int* status) {
+  static std::mutex mu;
+  static double* addr[256] = {nullptr};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 256) {
+    set_error("ffs_grid_build_noalloc: cudaGetDevice failed (%s)", cudaGetErrorString(e));
+    *status = FFS_ERR_CUDA;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    double* ptr = nullptr;
+    e = cudaGetSymbolAddress((void**)&ptr, g_grid_scratch);
+    if (e != cudaSuccess || !ptr) {
+      set_error("ffs_grid_build_noalloc: cudaGetSymbolAddress failed on device %d (%s)", dev,
+                cudaGetErrorString(e));
+      *status = FFS_ERR_CUDA;
+      return nullptr;
+    }
+    addr[dev] = ptr;
+  }
+  *status = FFS_OK;
+  return addr[dev];
+}
+
+}  // namespace
+}  // namespace ffsk
+
+extern "C" int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream) {
+  using namespace ffsk;
+  clear_error();
+  FFS_REQUIRE(d && o, "ffs_grid_build_noalloc: null descriptor");
+  FFS_REQUIRE(d->T > 0 && d->K > 0 && d->P > 0 && d->n_runs > 0,
+              "ffs_grid_build_noalloc: T=%d K=%d P=%d n_runs=%d must be positive", d->T, d->K, d->P, d->n_runs);
+  FFS_REQUIRE(d->K <= d->T, "ffs_grid_build_noalloc: K=%d exceeds T=%d", d->K, d->T);
+  FFS_REQUIRE(d->n_task >= 0 && d->n_task <= d->K, "ffs_grid_build_noalloc: bad n_task=%d", d->n_task);
+  FFS_REQUIRE(!o->U_hi || (o->U_lo && o->uexp), "ffs_grid_build_noalloc: U_hi needs U_lo and uexp");
+  FFS_REQUIRE(!o->U_hi || (d->ld_u >= d->T && d->ld_u % 8 == 0),
+              "ffs_grid_build_noalloc: ld_u=%d must be >= T and a multiple of 8", d->ld_u);
+  FFS_REQUIRE(d->run_start && d->tau && d->a && d->b && d->X, "ffs_grid_build_noalloc: null input");
+  FFS_REQUIRE(o->coef && o->logdet_R && o->logdet_XtX && o->U && o->G && o->Adiag && o->XtX && o->info,
+              "ffs_grid_build_noalloc: null output");
+  const size_t need = sizeof(double) * pair_doubles(d->T, d->K) * (size_t)d->P;
+  if (need > kStaticGridScratchBytes) {
+    set_error("ffs_grid_build_noalloc: T=%d K=%d P=%d needs %zu bytes of scratch, above the %zu-byte static "
+              "scratch; use ffs_grid_build with a caller-provided workspace",
+              d->T, d->K, d->P, need, kStaticGridScratchBytes);
+    return FFS_ERR_WORKSPACE;
+  }
+  int st = FFS_OK;
+  double* scratch = static_grid_scratch(&st);
+  if (!scratch) return st;
+  // every scratch entry the kernel reads it writes first in the same launch, so
+  // the previous call's contents need no clearing
+  BuildArgs args{*d, *o};
+  args.o.work = scratch;
+  grid_build_kernel<<<d->P, 256, 0, (cudaStream_t)stream>>>(args);
+  return check_launch("grid_build_kernel (static scratch)");
 }

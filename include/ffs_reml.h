@@ -115,6 +115,25 @@ typedef struct {
 size_t ffs_grid_work_bytes(int T, int K, int P);
 int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
 
+/* ffs_grid_build without a workspace argument: this variant has no counterpart
+ * in the reference. It is for callers that cannot allocate device memory where
+ * they build the grid -- code whose device memory is already owned by a
+ * framework's allocator, or a foreign-language embedding that is handed only
+ * its input and output buffers. The FP64 scratch is instead a file-scope
+ * device array of FFS_GRID_STATIC_SCRATCH_BYTES (16 MiB) that every GPU
+ * loading the library holds until the process exits; o->work is ignored.
+ * - Sizes whose ffs_grid_work_bytes(T, K, P) exceeds the limit are rejected
+ *   with FFS_ERR_WORKSPACE and a message.
+ * - The first call on a device resolves the array's device address (with that
+ *   device current); make that first call before any stream capture.
+ * - All calls share the one array: calls whose kernels overlap on the GPU
+ *   (different streams, or different host threads on one device) race and
+ *   must be serialised by the caller. Nothing in the array needs clearing
+ *   between calls.
+ * It calls no cudaMalloc, cudaFree or allocating library routine. */
+#define FFS_GRID_STATIC_SCRATCH_BYTES ((size_t)16 << 20)
+int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
+
 /* ---------------------------------------------------------------- search data
  * Replaces the per-voxel scaling of fastfuncstuff/glm/arma.py:3952-3954,
  * 4685-4686 and _residualize_reml_search_data (arma.py:1554-1571).
