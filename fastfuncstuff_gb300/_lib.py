@@ -111,6 +111,8 @@ SIGNATURES = {
     "ffs_reml_gls": ([C.POINTER(GlsArgs), C.c_void_p], C.c_int),
     "ffs_reml_gls_ex": ([C.POINTER(GlsArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p], C.c_int),
+    "ffs_reml_gls_grouped": ([C.POINTER(GlsArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                              C.c_void_p, C.c_void_p], C.c_int),
     "ffs_reml_group": ([C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "ffs_mlp_param_count": ([], C.c_int),
     "ffs_arma_simulate": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

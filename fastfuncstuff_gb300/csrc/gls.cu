@@ -26,22 +26,15 @@ struct GlsExtra {
   float* ljung_box;     // [V]
 };
 
-__global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, GlsExtra x, int ld_s,
-                                                              int kp, int hb) {
-  extern __shared__ float sm[];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  float* ys = sm + (size_t)wid * (2 * ld_s + kp + hb);
-  float* r = ys + ld_s;
-  float* beta = r + ld_s;
-  float* bins = beta + kp;  // [hb] Ljung-Box lag sums
-  const int i = blockIdx.x * GLS_WARPS + wid;
-  if (i >= a.V) return;
+// GLS of one voxel v at pair g, executed by one warp. Gp = G of pair g and Xt
+// (the transposed design) may live in shared or global memory; ys, r, beta and
+// bins are this warp's shared scratch.
+__device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v, const int g, const float* Gp,
+                          const float* Xt, float* ys, float* r, float* beta, float* bins) {
+  const int lane = threadIdx.x & 31;
   const int T = a.T, K = a.K;
-  const int v = a.order ? a.order[i] : i;
-  const int g = a.best[v];
   const float sc = a.scale[v];
   const float* y = a.Y + (size_t)v * T;
-  const float* Gp = a.G + (size_t)g * K * T;
 
   // optional centring: fit (y - m)/s, then add (m/s) * G'1 to the betas; the
   // residuals, sigma2, R^2 and the t of every column but the constant's are
@@ -67,7 +60,7 @@ __global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, Gls
   // refinement: b += G' (y - X b)
   for (int t = lane; t < T; t += 32) {
     float acc = ys[t];
-    for (int j = 0; j < K; ++j) acc = fmaf(-a.Xt[(size_t)j * T + t], beta[j], acc);
+    for (int j = 0; j < K; ++j) acc = fmaf(-Xt[(size_t)j * T + t], beta[j], acc);
     r[t] = acc;
   }
   __syncwarp();
@@ -83,7 +76,7 @@ __global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, Gls
   float ssr = 0.f, sy = 0.f;
   for (int t = lane; t < T; t += 32) {
     float acc = ys[t];
-    for (int j = 0; j < K; ++j) acc = fmaf(-a.Xt[(size_t)j * T + t], beta[j], acc);
+    for (int j = 0; j < K; ++j) acc = fmaf(-Xt[(size_t)j * T + t], beta[j], acc);
     r[t] = acc;
     ssr = fmaf(acc, acc, ssr);
     sy += ys[t];
@@ -216,6 +209,87 @@ __global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, Gls
   }
 }
 
+// One warp per voxel, matrices read from global memory (any shape).
+__global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, GlsExtra x, int ld_s,
+                                                              int kp, int hb) {
+  extern __shared__ float sm[];
+  const int wid = threadIdx.x >> 5;
+  float* ys = sm + (size_t)wid * (2 * ld_s + kp + hb);
+  const int i = blockIdx.x * GLS_WARPS + wid;
+  if (i >= a.V) return;
+  const int v = a.order ? a.order[i] : i;
+  const int g = a.best[v];
+  gls_voxel(a, x, v, g, a.G + (size_t)g * a.K * a.T, a.Xt, ys, ys + ld_s, ys + 2 * ld_s, ys + 2 * ld_s + kp);
+}
+
+// Tiles of up to GLS_TILE voxels that share one pair (voxels grouped by pair:
+// order[end[g-1] .. end[g]) are pair g's, end[-1] = 0). The pair's G and the
+// transposed design are staged in shared memory once per tile; tile_start[g]
+// numbers the tiles of pair g. Blocks past the last tile exit.
+constexpr int GLS_TILE = 32;
+constexpr int GLS_TWARPS = 8;
+
+__global__ void __launch_bounds__(GLS_TWARPS * 32) gls_tile_kernel(ffs_gls_args a, GlsExtra x, const int* end,
+                                                                   const int* tile_start, int P, int ld_s, int kp,
+                                                                   int hb) {
+  extern __shared__ float sm[];
+  const int tile = blockIdx.x;
+  if (tile >= tile_start[P]) return;
+  int lo = 0, hi = P;  // largest g with tile_start[g] <= tile
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (tile_start[mid] <= tile) lo = mid; else hi = mid;
+  }
+  const int g = lo;
+  const int g0 = g ? end[g - 1] : 0;
+  const int j0 = g0 + (tile - tile_start[g]) * GLS_TILE;
+  const int n = min(GLS_TILE, end[g] - j0);
+  const int KT = a.K * a.T;
+  float* Gs = sm;
+  float* Xs = sm + KT;
+  const float* Gg = a.G + (size_t)g * KT;
+  for (int i = threadIdx.x; i < KT; i += blockDim.x) {
+    Gs[i] = Gg[i];
+    Xs[i] = a.Xt[i];
+  }
+  __syncthreads();
+  const int wid = threadIdx.x >> 5;
+  float* ys = sm + 2 * (size_t)KT + (size_t)wid * (2 * ld_s + kp + hb);
+  for (int i = wid; i < n; i += GLS_TWARPS) {
+    const int v = a.order[j0 + i];
+    gls_voxel(a, x, v, g, Gs, Xs, ys, ys + ld_s, ys + 2 * ld_s, ys + 2 * ld_s + kp);
+    __syncwarp();
+  }
+}
+
+// tile_start[g] = sum over g' < g of ceil(count[g'] / GLS_TILE)
+__global__ void gls_tile_scan(int P, const int* end, int* tile_start) {
+  __shared__ int part[1024];
+  // counts per thread-strided block, then a serial scan over 1024 partials
+  const int tid = threadIdx.x;
+  const int per = (P + blockDim.x - 1) / blockDim.x;
+  int acc = 0;
+  for (int g = tid * per; g < min(P, (tid + 1) * per); ++g)
+    acc += (end[g] - (g ? end[g - 1] : 0) + GLS_TILE - 1) / GLS_TILE;
+  part[tid] = acc;
+  __syncthreads();
+  if (tid == 0) {
+    int run = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      const int c = part[i];
+      part[i] = run;
+      run += c;
+    }
+    tile_start[P] = run;
+  }
+  __syncthreads();
+  int run = part[tid];
+  for (int g = tid * per; g < min(P, (tid + 1) * per); ++g) {
+    tile_start[g] = run;
+    run += (end[g] - (g ? end[g - 1] : 0) + GLS_TILE - 1) / GLS_TILE;
+  }
+}
+
 }  // namespace
 }  // namespace ffsk
 
@@ -242,6 +316,36 @@ extern "C" int ffs_reml_gls_ex(const ffs_gls_args* a, int lj_h, const int* lj_ta
   GlsExtra x{lj_h, lj_tau, lj_w, ljung_box};
   gls_kernel<<<ceil_div(a->V, GLS_WARPS), GLS_WARPS * 32, smem, (cudaStream_t)stream>>>(*a, x, ld_s, kp, hb);
   return check_launch("gls_kernel");
+}
+
+extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* lj_tau, const float* lj_w,
+                                    float* ljung_box, int P, const int* group_end, int* tile_start, void* stream) {
+  clear_error();
+  FFS_REQUIRE(a && a->V > 0 && a->T > 0 && a->K > 0 && a->dof > 0 && P > 0, "ffs_reml_gls_grouped: bad sizes");
+  FFS_REQUIRE(a->order && group_end && tile_start, "ffs_reml_gls_grouped: needs order, group_end, tile_start");
+  FFS_REQUIRE(a->Y && a->scale && a->Xt && a->best && a->coef && a->G && a->Adiag && a->XtX && a->a && a->b &&
+                  a->betas && a->tstats && a->sigma2 && a->fstats && a->r2 && a->lam,
+              "ffs_reml_gls_grouped: null buffer");
+  FFS_REQUIRE(a->n_task == 0 || (a->task_idx && a->Ftask), "ffs_reml_gls_grouped: task columns need Ftask");
+  FFS_REQUIRE(!a->center || a->Gsum, "ffs_reml_gls_grouped: centring needs Gsum");
+  FFS_REQUIRE(a->n_glt == 0 || (a->glt && a->glt_var && a->cbeta && a->ct), "ffs_reml_gls_grouped: GLT buffers");
+  FFS_REQUIRE(lj_h >= 0 && lj_h <= a->T / 2, "ffs_reml_gls_grouped: Ljung-Box lag %d out of range", lj_h);
+  FFS_REQUIRE(lj_h == 0 || (lj_w && ljung_box), "ffs_reml_gls_grouped: Ljung-Box buffers");
+  const int ld_s = a->T + 1;
+  const int kp = (a->K + 3) & ~3;
+  const int hb = (lj_h + 4) & ~3;
+  const size_t mats = sizeof(float) * 2 * (size_t)a->K * a->T;
+  const size_t smem = mats + sizeof(float) * GLS_TWARPS * (size_t)(2 * ld_s + kp + hb);
+  if (smem > 200 * 1024) {  // the pair's matrices do not fit: read them from global memory
+    return ffs_reml_gls_ex(a, lj_h, lj_tau, lj_w, ljung_box, stream);
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  GlsExtra x{lj_h, lj_tau, lj_w, ljung_box};
+  gls_tile_scan<<<1, 1024, 0, st>>>(P, group_end, tile_start);
+  FFS_CUDA(cudaFuncSetAttribute(gls_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int max_tiles = ceil_div(a->V, GLS_TILE) + P;
+  gls_tile_kernel<<<max_tiles, GLS_TWARPS * 32, smem, st>>>(*a, x, group_end, tile_start, P, ld_s, kp, hb);
+  return check_launch("gls_tile_kernel");
 }
 
 extern "C" int ffs_reml_gls(const ffs_gls_args* a, void* stream) {

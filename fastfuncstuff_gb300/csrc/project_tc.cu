@@ -10,7 +10,7 @@
 // lo*hi) accumulating in fp32 in tensor memory, with a relative error near
 // 2^-22 per product; the epilogue removes the scales exactly.
 //
-// CTA tile: 128 voxels x N columns (g whole pairs, N = roundup16(g*K) <= 256).
+// Work item: 128 voxels x N columns (g whole pairs, N = roundup16(g*K) <= 256).
 // Warp 0 issues TMA loads (128B-swizzled boxes of 64 k-elements), warp 1 owns
 // TMEM and issues the MMAs from one thread, warps 2-5 square and sum each
 // pair's K columns straight out of TMEM and store proj. Nothing but proj
@@ -31,9 +31,9 @@ constexpr int A_TILE = BM * BK * 2;  // bytes of one A box (hi or lo, fp16)
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
 
 struct TcParams {
-  int V, K, P, ld;     // ld: padded k extent (multiple of BK)
+  int V, K, P, ld, T;  // ld: padded k extent (multiple of BK); T: real extent
   int g, N;            // pairs per column tile, MMA N
-  int n_col_tiles;
+  int n_col_tiles, n_vox_tiles;
   const int* yexp;
   const int* uexp;
   float* proj;
@@ -105,6 +105,11 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
+// Persistent kernel: CTA b walks work items b, b + gridDim.x, ... where item
+// = vox_tile * n_col_tiles + col_tile (column tiles fastest, so the CTAs that
+// run together share voxel tiles in L2). The TMA ring of STAGES k-blocks runs
+// across items; TMEM holds two 256-column accumulators so the epilogue warps
+// drain item i while the MMA warp accumulates item i + 1.
 __global__ void __launch_bounds__(192, 1)
     project_tc_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
                       const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
@@ -115,30 +120,30 @@ __global__ void __launch_bounds__(192, 1)
   const int stage_bytes = 2 * A_TILE + 2 * b_tile;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
   uint64_t* empty = full + STAGES;
-  uint64_t* done = empty + STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
-  __shared__ int abort_cta;
+  uint64_t* acc_full = empty + STAGES;    // [2] MMA -> epilogue
+  uint64_t* acc_empty = acc_full + 2;     // [2] epilogue -> MMA
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
 
   // a CTA that finds an earlier CTA's wait expired does nothing
   if (*reinterpret_cast<volatile int*>(prm.flag) != 0) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int col_tile = blockIdx.x, vox_tile = blockIdx.y;
-  const int p_first = col_tile * prm.g;
-  const int v0 = vox_tile * BM;
+  const int n_items = prm.n_col_tiles * prm.n_vox_tiles;
   const int nk = prm.ld / BK;
 
   if (threadIdx.x == 0) {
-    abort_cta = 0;
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(full + s, 1);
       mbar_init(empty + s, 1);
     }
-    mbar_init(done, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(acc_full + b, 1);
+      mbar_init(acc_empty + b, 128);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -147,66 +152,90 @@ __global__ void __launch_bounds__(192, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
-    // ---- TMA producer
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % STAGES;
-      if (kb >= STAGES && !mbar_wait(empty + s, ((kb / STAGES) - 1) & 1)) {
-        atomicExch(prm.flag, 1);
-        abort_cta = 1;
-        break;
+    // ---- TMA producer: k-blocks of every item of this CTA through the ring
+    int kc = 0;
+    bool ok = true;
+    for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
+      const int v0 = (item / prm.n_col_tiles) * BM;
+      const int row_b = (item % prm.n_col_tiles) * prm.g * prm.K;
+      for (int kb = 0; kb < nk; ++kb, ++kc) {
+        const int s = kc % STAGES;
+        if (kc >= STAGES && !mbar_wait(empty + s, ((kc / STAGES) - 1) & 1)) {
+          atomicExch(prm.flag, 1);
+          ok = false;
+          break;
+        }
+        uint8_t* st = smem + s * stage_bytes;
+        mbar_expect_tx(full + s, (uint32_t)stage_bytes);
+        const int k0 = kb * BK;
+        tma_load_2d(st, &ta_hi, full + s, k0, v0);
+        tma_load_2d(st + A_TILE, &ta_lo, full + s, k0, v0);
+        tma_load_2d(st + 2 * A_TILE, &tb_hi, full + s, k0, row_b);
+        tma_load_2d(st + 2 * A_TILE + b_tile, &tb_lo, full + s, k0, row_b);
       }
-      uint8_t* st = smem + s * stage_bytes;
-      mbar_expect_tx(full + s, (uint32_t)stage_bytes);
-      const int k0 = kb * BK;
-      tma_load_2d(st, &ta_hi, full + s, k0, v0);
-      tma_load_2d(st + A_TILE, &ta_lo, full + s, k0, v0);
-      tma_load_2d(st + 2 * A_TILE, &tb_hi, full + s, k0, p_first * prm.K);
-      tma_load_2d(st + 2 * A_TILE + b_tile, &tb_lo, full + s, k0, p_first * prm.K);
     }
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer
     const uint32_t idesc = idesc_f16(BM, prm.N);
+    int kc = 0, local = 0;
     bool ok = true;
-    for (int kb = 0; kb < nk && ok; ++kb) {
-      const int s = kb % STAGES;
-      if (!mbar_wait(full + s, (kb / STAGES) & 1)) {
-        atomicExch(prm.flag, 2);
+    for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x, ++local) {
+      const int buf = local & 1;
+      const uint32_t acc = tmem + (uint32_t)(buf * 256);
+      if (local >= 2 && !mbar_wait(acc_empty + buf, ((local >> 1) - 1) & 1)) {
+        atomicExch(prm.flag, 4);
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      uint8_t* st = smem + s * stage_bytes;
-      const uint64_t a_hi = sdesc(smem_u32(st));
-      const uint64_t a_lo = sdesc(smem_u32(st + A_TILE));
-      const uint64_t b_hi = sdesc(smem_u32(st + 2 * A_TILE));
-      const uint64_t b_lo = sdesc(smem_u32(st + 2 * A_TILE + b_tile));
-#pragma unroll
-      for (int kk = 0; kk < BK / 16; ++kk) {
-        const uint64_t off = (uint64_t)((kk * 32) >> 4);  // 16 fp16 = 32 bytes along k
-        const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
-        mma_f16(tmem, a_hi + off, b_hi + off, idesc, acc0);
-        mma_f16(tmem, a_hi + off, b_lo + off, idesc, 1u);
-        mma_f16(tmem, a_lo + off, b_hi + off, idesc, 1u);
+      for (int kb = 0; kb < nk; ++kb, ++kc) {
+        const int s = kc % STAGES;
+        if (!mbar_wait(full + s, (kc / STAGES) & 1)) {
+          atomicExch(prm.flag, 2);
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        uint8_t* st = smem + s * stage_bytes;
+        const uint64_t a_hi = sdesc(smem_u32(st));
+        const uint64_t a_lo = sdesc(smem_u32(st + A_TILE));
+        const uint64_t b_hi = sdesc(smem_u32(st + 2 * A_TILE));
+        const uint64_t b_lo = sdesc(smem_u32(st + 2 * A_TILE + b_tile));
+        // k-steps past T multiply zero padding: skip them
+        const int nkk = min(BK / 16, (prm.T - kb * BK + 15) / 16);
+        for (int kk = 0; kk < nkk; ++kk) {
+          const uint64_t off = (uint64_t)((kk * 32) >> 4);  // 16 fp16 = 32 bytes along k
+          const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
+          mma_f16(acc, a_hi + off, b_hi + off, idesc, acc0);
+          mma_f16(acc, a_hi + off, b_lo + off, idesc, 1u);
+          mma_f16(acc, a_lo + off, b_hi + off, idesc, 1u);
+        }
+        mma_commit(empty + s);
       }
-      mma_commit(empty + s);
+      mma_commit(acc_full + buf);
     }
-    mma_commit(done);
   } else if (warp >= 2) {
     // ---- epilogue: square and sum each pair's K columns from TMEM
     const int q = warp & 3;  // TMEM lane quarter this warp may access
     const int row = q * 32 + lane;
-    const int v = v0 + row;
-    const int ey = v < prm.V ? prm.yexp[v] : 0;
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
-    if (!ok && lane == 0) atomicExch(prm.flag, 3);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok) {
-      const int ncols = prm.g * prm.K;
+    const int ncols = prm.g * prm.K;
+    int local = 0;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++local) {
+      const int buf = local & 1;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(acc_full + buf, (local >> 1) & 1));
+      if (!ok) {
+        if (lane == 0) atomicExch(prm.flag, 3);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int v = (item / prm.n_col_tiles) * BM + row;
+      const int p_first = (item % prm.n_col_tiles) * prm.g;
+      const int ey = v < prm.V ? prm.yexp[v] : 0;
       int j = 0, pl = 0;
       float run = 0.f;
       for (int c0 = 0; c0 < prm.N; c0 += 16) {
         uint32_t r[16];
-        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+        const uint32_t taddr = tmem + (uint32_t)(buf * 256) + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
@@ -230,12 +259,15 @@ __global__ void __launch_bounds__(192, 1)
           }
         }
       }
+      // this accumulator may be overwritten now
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(acc_empty + buf)) : "memory");
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
   }
 }
 
@@ -299,6 +331,8 @@ extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
   if (prm.g > a->P) prm.g = a->P;
   prm.N = ((prm.g * a->K) + 15) / 16 * 16;
   prm.n_col_tiles = ceil_div(a->P, prm.g);
+  prm.n_vox_tiles = ceil_div(a->V, BM);
+  prm.T = a->T;
   prm.yexp = a->yexp;
   prm.uexp = a->uexp;
   prm.proj = a->proj;
@@ -310,10 +344,13 @@ extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
   if ((st = make_map(&tb_hi, a->u_hi, a->ld_u, a->P * a->K, prm.N))) return st;
   if ((st = make_map(&tb_lo, a->u_lo, a->ld_u, a->P * a->K, prm.N))) return st;
   const int stage_bytes = 2 * A_TILE + 2 * prm.N * BK * 2;
-  const size_t smem = (size_t)STAGES * stage_bytes + 1024 + 64;
+  const size_t smem = (size_t)STAGES * stage_bytes + 1024 + 128;
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_project_tc: tile needs %zu bytes of shared memory", smem);
   FFS_CUDA(cudaFuncSetAttribute(project_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid(prm.n_col_tiles, ceil_div(a->V, BM));
-  project_tc_kernel<<<grid, 192, smem, (cudaStream_t)stream>>>(ta_hi, ta_lo, tb_hi, tb_lo, prm);
+  int dev = 0, n_sm = 0;
+  FFS_CUDA(cudaGetDevice(&dev));
+  FFS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  const int n_items = prm.n_col_tiles * prm.n_vox_tiles;
+  project_tc_kernel<<<min(n_items, n_sm), 192, smem, (cudaStream_t)stream>>>(ta_hi, ta_lo, tb_hi, tb_lo, prm);
   return check_launch("project_tc_kernel");
 }

@@ -86,14 +86,22 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
 }
 
 // --------------------------------------------------------------------- surface
-// One thread per voxel, one CTA per (voxel tile, chunk of pairs sharing a).
-// For each pair g of the chunk: v_t = z_t - m_t v_{t-1}, s += v_t^2 / D_t.
+// One thread per voxel, one CTA per (voxel tile, chunk of pairs sharing one AR
+// filter). For each pair g of the chunk: v_t = z_t - m_t v_{t-1},
+// s += v_t^2 / D_t. The chunk's coefficient table is staged in shared memory;
+// a step whose coefficients equal the previous step's for every pair of the
+// chunk (the LDL' factor of a Toeplitz run converges to a constant, so most
+// steps after a short transient are such "steady" steps) reuses the registers
+// instead of reloading them. Each thread prefetches 32 samples of its voxel at
+// a time so the loads overlap instead of stalling every step.
 constexpr int SURF_G = 16;
-constexpr int SURF_THREADS = 128;
+constexpr int SURF_THREADS = 256;
+constexpr int SURF_TB = 32;  // time steps per prefetch block
 
-__global__ void __launch_bounds__(SURF_THREADS) surface_kernel(ffs_surface_args a) {
+__global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_args a) {
   extern __shared__ float2 cf[];  // [T][SURF_G] (m, 1/D)
   float* cs = reinterpret_cast<float*>(cf + (size_t)a.T * SURF_G);  // [T] c_t
+  uint8_t* steady = reinterpret_cast<uint8_t*>(cs + a.T);           // [T]
   const int chunk = blockIdx.y;
   const int c0 = a.chunk_start[chunk], c1 = a.chunk_start[chunk + 1];
   const int ng = c1 - c0;
@@ -108,30 +116,54 @@ __global__ void __launch_bounds__(SURF_THREADS) surface_kernel(ffs_surface_args 
     }
     cf[idx] = val;
   }
-  for (int t = threadIdx.x; t < T; t += blockDim.x)
-    cs[t] = coef[(size_t)a.chunk_pairs[c0] * T + t].x;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) cs[t] = coef[(size_t)a.chunk_pairs[c0] * T + t].x;
+  __syncthreads();
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    bool same = t > 0 && cs[t] == cs[t - 1];
+    for (int g = 0; g < SURF_G && same; ++g) {
+      const float2 x = cf[t * SURF_G + g], y = cf[(t - 1) * SURF_G + g];
+      same = x.x == y.x && x.y == y.y;
+    }
+    steady[t] = same ? 1 : 0;
+  }
   __syncthreads();
 
   const int v = blockIdx.x * SURF_THREADS + threadIdx.x;
   if (v >= a.V) return;
-  float vv[SURF_G], sb[SURF_G], st[SURF_G];
+  float vv[SURF_G], sb[SURF_G], st[SURF_G], m[SURF_G], id[SURF_G];
 #pragma unroll
-  for (int g = 0; g < SURF_G; ++g) vv[g] = sb[g] = st[g] = 0.f;
-  float yy_b = 0.f, yy = 0.f, yp = 0.f;
+  for (int g = 0; g < SURF_G; ++g) vv[g] = sb[g] = st[g] = m[g] = id[g] = 0.f;
+  float c = 0.f, yy_b = 0.f, yy = 0.f, yp = 0.f;
   const float* yc = a.yr_t + v;
-  for (int t0 = 0; t0 < T; t0 += 32) {
-    const int t1 = min(T, t0 + 32);
-    for (int t = t0; t < t1; ++t) {
-      const float y = yc[(size_t)t * a.V];
-      const float z = fmaf(-cs[t], yp, y);
-      yp = y;
-      yy_b = fmaf(y, y, yy_b);
-      const float2* row = cf + (size_t)t * SURF_G;
+  for (int t0 = 0; t0 < T; t0 += SURF_TB) {
+    float yb[SURF_TB];
 #pragma unroll
-      for (int g = 0; g < SURF_G; ++g) {
-        const float2 q = row[g];
-        vv[g] = fmaf(-q.x, vv[g], z);
-        sb[g] = fmaf(vv[g] * q.y, vv[g], sb[g]);
+    for (int k = 0; k < SURF_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * a.V] : 0.f;
+#pragma unroll
+    for (int k = 0; k < SURF_TB; ++k) {
+      const int t = t0 + k;
+      if (t < T) {
+        if (!steady[t]) {
+          c = cs[t];
+          const float4* row = reinterpret_cast<const float4*>(cf + (size_t)t * SURF_G);
+#pragma unroll
+          for (int g = 0; g < SURF_G / 2; ++g) {
+            const float4 q = row[g];
+            m[2 * g] = q.x;
+            id[2 * g] = q.y;
+            m[2 * g + 1] = q.z;
+            id[2 * g + 1] = q.w;
+          }
+        }
+        const float y = yb[k];
+        const float z = fmaf(-c, yp, y);
+        yp = y;
+        yy_b = fmaf(y, y, yy_b);
+#pragma unroll
+        for (int g = 0; g < SURF_G; ++g) {
+          vv[g] = fmaf(-m[g], vv[g], z);
+          sb[g] = fmaf(vv[g] * id[g], vv[g], sb[g]);
+        }
       }
     }
 #pragma unroll
@@ -335,7 +367,7 @@ extern "C" int ffs_reml_surface(const ffs_surface_args* a, void* stream) {
   FFS_REQUIRE(a->yr_t && a->coef && a->logdet_R && a->logdet_XtX && a->proj && a->chunk_start &&
                   a->chunk_pairs && a->surf && a->crit0,
               "ffs_reml_surface: null buffer");
-  const size_t smem = (sizeof(float2) * SURF_G + sizeof(float)) * (size_t)a->T;
+  const size_t smem = (sizeof(float2) * SURF_G + sizeof(float) + 1) * (size_t)a->T;
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_surface: T=%d too long", a->T);
   FFS_CUDA(cudaFuncSetAttribute(surface_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(ceil_div(a->V, SURF_THREADS), a->n_chunks);

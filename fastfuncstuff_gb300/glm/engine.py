@@ -40,7 +40,7 @@ def _stream() -> int:
 # kernels each library entry point launches (for launch accounting)
 LAUNCHES = {"ffs_grid_build": 1, "ffs_reml_prep": 1, "ffs_reml_project_tc": 1, "ffs_reml_project_simt": 1,
             "ffs_reml_surface": 1, "ffs_reml_select": 1, "ffs_reml_group": 3, "ffs_reml_gls": 1,
-            "ffs_reml_gls_ex": 1}
+            "ffs_reml_gls_ex": 1, "ffs_reml_gls_grouped": 2}
 
 
 class StageTimer:
@@ -342,14 +342,15 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
                       glt_var=_p(f.glt_var), betas=_p(o.betas), tstats=_p(o.tstats), sigma2=_p(o.sigma2),
                       fstats=_p(o.fstats), r2=_p(o.r2), lam=_p(o.lam), cbeta=_p(o.cbeta), ct=_p(o.ct),
                       resid=_p(o.resid), resid_w=_p(o.resid_w), pred=_p(o.pred))
+    h, ptau_d, w_d = 0, None, None
     if lj is not None and lj[0] > 0:
         h, ptau, w, _ = lj
         ptau_d = None if ptau is None else torch.from_numpy(ptau).to(dev)
         w_d = torch.from_numpy(w).to(dev)
         o.ljung_box = torch.empty(V, **f32)
-        _run("ffs_reml_gls_ex", lib.ffs_reml_gls_ex, C.byref(ga), h, _p(ptau_d), _p(w_d), _p(o.ljung_box), st)
-        o._keep = (ptau_d, w_d)
-    else:
-        _run("ffs_reml_gls", lib.ffs_reml_gls, C.byref(ga), st)
+    tiles = torch.empty(P + 1, dtype=torch.int32, device=dev)
+    _run("ffs_reml_gls_grouped", lib.ffs_reml_gls_grouped, C.byref(ga), h, _p(ptau_d), _p(w_d), _p(o.ljung_box),
+         P, _p(work), _p(tiles), st)
+    o._keep = (ptau_d, w_d, tiles)
     o._keep2 = (Y, order, work, Xt)
     return o

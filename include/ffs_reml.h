@@ -279,9 +279,16 @@ int ffs_reml_gls(const ffs_gls_args* a, void* stream);
 int ffs_reml_gls_ex(const ffs_gls_args* a, int lj_h, const int* lj_tau, const float* lj_w,
                     float* ljung_box, void* stream);
 
+/* ffs_reml_gls_ex for voxels grouped by pair (after ffs_reml_group): group_end
+ * is ffs_reml_group's work array (group_end[g] = end of pair g's voxels in
+ * order), tile_start a [P + 1] int scratch. Tiles of up to 32 same-pair voxels
+ * share one staging of the pair's G and of the design in shared memory. */
+int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* lj_tau, const float* lj_w,
+                         float* ljung_box, int P, const int* group_end, int* tile_start, void* stream);
+
 /* Counting sort of voxels by pair: order[] lists voxel ids grouped by best[].
  * Replaces the torch.unique / sort grouping of fastfuncstuff/glm/arma.py:4794-4811.
- * work: int[P + 1]. */
+ * work: int[P + 1]; on return work[g] is the end of pair g's voxels in order. */
 int ffs_reml_group(int V, int P, const int* best, int* work, int* order, void* stream);
 
 /* --------------------------------------------------------- learned proposal
