@@ -86,53 +86,88 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
 }
 
 // --------------------------------------------------------------------- surface
-// One thread per voxel, one CTA per (voxel tile, chunk of pairs sharing one AR
-// filter). For each pair g of the chunk: v_t = z_t - m_t v_{t-1},
-// s += v_t^2 / D_t. The chunk's coefficient table is staged in shared memory;
-// a step whose coefficients equal the previous step's for every pair of the
-// chunk (the LDL' factor of a Toeplitz run converges to a constant, so most
-// steps after a short transient are such "steady" steps) reuses the registers
-// instead of reloading them. Each thread prefetches 32 samples of its voxel at
-// a time so the loads overlap instead of stalling every step.
+// One thread per voxel, one CTA per (chunk of pairs sharing one AR filter,
+// voxel tile). For each pair g of the chunk: v_t = z_t - m_t v_{t-1},
+// s += v_t^2 / D_t. The chunk's coefficient table is staged in shared memory
+// as (-m, 1/D) of pair couples, so each couple advances with packed
+// fma.rn.f32x2 / mul.rn.f32x2 instructions. A step whose coefficients equal the
+// previous step's for every pair of the chunk (the LDL' factor of a Toeplitz
+// run converges to a constant, so most steps after a short transient are such
+// "steady" steps) reuses the registers instead of reloading them. Each thread
+// prefetches 32 samples of its voxel at a time so the loads overlap.
 constexpr int SURF_G = 16;
+constexpr int SURF_G2 = SURF_G / 2;
 constexpr int SURF_THREADS = 256;
 constexpr int SURF_TB = 32;  // time steps per prefetch block
 
+__device__ __forceinline__ uint64_t pack2(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void unpack2(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
 __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_args a) {
-  extern __shared__ float2 cf[];  // [T][SURF_G] (m, 1/D)
-  float* cs = reinterpret_cast<float*>(cf + (size_t)a.T * SURF_G);  // [T] c_t
-  uint8_t* steady = reinterpret_cast<uint8_t*>(cs + a.T);           // [T]
-  const int chunk = blockIdx.y;
+  extern __shared__ float4 cf4[];  // [T][SURF_G2] (-m_2k, -m_2k+1, 1/D_2k, 1/D_2k+1)
+  float* cs = reinterpret_cast<float*>(cf4 + (size_t)a.T * SURF_G2);  // [T] c_t
+  uint8_t* steady = reinterpret_cast<uint8_t*>(cs + a.T);            // [T]
+  // chunks are the fast grid dimension: the CTAs of one voxel tile run together
+  // and its samples stay in L2 across the chunks
+  const int chunk = blockIdx.x;
   const int c0 = a.chunk_start[chunk], c1 = a.chunk_start[chunk + 1];
   const int ng = c1 - c0;
   const int T = a.T;
   const float4* coef = reinterpret_cast<const float4*>(a.coef);
-  for (int idx = threadIdx.x; idx < T * SURF_G; idx += blockDim.x) {
-    const int t = idx / SURF_G, g = idx % SURF_G;
-    float2 val = make_float2(0.f, 0.f);
-    if (g < ng) {
-      const float4 q = coef[(size_t)a.chunk_pairs[c0 + g] * T + t];
-      val = make_float2(q.y, q.z);
+  for (int idx = threadIdx.x; idx < T * SURF_G2; idx += blockDim.x) {
+    const int t = idx / SURF_G2, k = idx % SURF_G2;
+    float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (2 * k < ng) {
+      const float4 q = coef[(size_t)a.chunk_pairs[c0 + 2 * k] * T + t];
+      val.x = -q.y;
+      val.z = q.z;
     }
-    cf[idx] = val;
+    if (2 * k + 1 < ng) {
+      const float4 q = coef[(size_t)a.chunk_pairs[c0 + 2 * k + 1] * T + t];
+      val.y = -q.y;
+      val.w = q.z;
+    }
+    cf4[idx] = val;
   }
   for (int t = threadIdx.x; t < T; t += blockDim.x) cs[t] = coef[(size_t)a.chunk_pairs[c0] * T + t].x;
   __syncthreads();
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
     bool same = t > 0 && cs[t] == cs[t - 1];
-    for (int g = 0; g < SURF_G && same; ++g) {
-      const float2 x = cf[t * SURF_G + g], y = cf[(t - 1) * SURF_G + g];
-      same = x.x == y.x && x.y == y.y;
+    for (int k = 0; k < SURF_G2 && same; ++k) {
+      const float4 x = cf4[t * SURF_G2 + k], y = cf4[(t - 1) * SURF_G2 + k];
+      same = x.x == y.x && x.y == y.y && x.z == y.z && x.w == y.w;
     }
     steady[t] = same ? 1 : 0;
   }
   __syncthreads();
 
-  const int v = blockIdx.x * SURF_THREADS + threadIdx.x;
+  const int v = blockIdx.y * SURF_THREADS + threadIdx.x;
   if (v >= a.V) return;
-  float vv[SURF_G], sb[SURF_G], st[SURF_G], m[SURF_G], id[SURF_G];
+  uint64_t vv[SURF_G2], sb[SURF_G2], st[SURF_G2], nm[SURF_G2], id[SURF_G2];
+  const uint64_t zero2 = pack2(0.f, 0.f);
 #pragma unroll
-  for (int g = 0; g < SURF_G; ++g) vv[g] = sb[g] = st[g] = m[g] = id[g] = 0.f;
+  for (int k = 0; k < SURF_G2; ++k) vv[k] = sb[k] = st[k] = nm[k] = id[k] = zero2;
   float c = 0.f, yy_b = 0.f, yy = 0.f, yp = 0.f;
   const float* yc = a.yr_t + v;
   for (int t0 = 0; t0 < T; t0 += SURF_TB) {
@@ -145,31 +180,30 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
       if (t < T) {
         if (!steady[t]) {
           c = cs[t];
-          const float4* row = reinterpret_cast<const float4*>(cf + (size_t)t * SURF_G);
+          const float4* row = cf4 + (size_t)t * SURF_G2;
 #pragma unroll
-          for (int g = 0; g < SURF_G / 2; ++g) {
-            const float4 q = row[g];
-            m[2 * g] = q.x;
-            id[2 * g] = q.y;
-            m[2 * g + 1] = q.z;
-            id[2 * g + 1] = q.w;
+          for (int j = 0; j < SURF_G2; ++j) {
+            const float4 q = row[j];
+            nm[j] = pack2(q.x, q.y);
+            id[j] = pack2(q.z, q.w);
           }
         }
         const float y = yb[k];
         const float z = fmaf(-c, yp, y);
         yp = y;
         yy_b = fmaf(y, y, yy_b);
+        const uint64_t z2 = pack2(z, z);
 #pragma unroll
-        for (int g = 0; g < SURF_G; ++g) {
-          vv[g] = fmaf(-m[g], vv[g], z);
-          sb[g] = fmaf(vv[g] * id[g], vv[g], sb[g]);
+        for (int j = 0; j < SURF_G2; ++j) {
+          vv[j] = fma2(nm[j], vv[j], z2);
+          sb[j] = fma2(mul2(vv[j], id[j]), vv[j], sb[j]);
         }
       }
     }
 #pragma unroll
-    for (int g = 0; g < SURF_G; ++g) {
-      st[g] += sb[g];
-      sb[g] = 0.f;
+    for (int j = 0; j < SURF_G2; ++j) {
+      st[j] = add2(st[j], sb[j]);
+      sb[j] = zero2;
     }
     yy += yy_b;
     yy_b = 0.f;
@@ -178,12 +212,18 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
   const double c_p0 = a.logdet_R[a.p0] + a.logdet_XtX[a.p0];
   const float rss0 = fmaxf(yy - a.proj[(size_t)a.p0 * a.V + v], 0.f);
   const float den = rss0 + 1e-10f;
-  for (int g = 0; g < ng; ++g) {
-    const int p = a.chunk_pairs[c0 + g];
-    const float rss = fmaxf(st[g] - a.proj[(size_t)p * a.V + v], 0.f);
-    const float dc = (float)((a.logdet_R[p] + a.logdet_XtX[p]) - c_p0);
-    const float dv = dc + (float)Tk * log1pf((rss - rss0) / den);
-    a.surf[(size_t)p * a.V + v] = dv;
+  float sg[SURF_G];
+#pragma unroll
+  for (int j = 0; j < SURF_G2; ++j) unpack2(st[j], sg[2 * j], sg[2 * j + 1]);
+#pragma unroll
+  for (int g = 0; g < SURF_G; ++g) {
+    if (g < ng) {
+      const int p = a.chunk_pairs[c0 + g];
+      const float rss = fmaxf(sg[g] - a.proj[(size_t)p * a.V + v], 0.f);
+      const float dc = (float)((a.logdet_R[p] + a.logdet_XtX[p]) - c_p0);
+      const float dv = dc + (float)Tk * log1pf((rss - rss0) / den);
+      a.surf[(size_t)p * a.V + v] = dv;
+    }
   }
   if (chunk == 0) a.crit0[v] = c_p0 + (double)Tk * log((double)rss0 + 1e-10);
 }
@@ -367,10 +407,11 @@ extern "C" int ffs_reml_surface(const ffs_surface_args* a, void* stream) {
   FFS_REQUIRE(a->yr_t && a->coef && a->logdet_R && a->logdet_XtX && a->proj && a->chunk_start &&
                   a->chunk_pairs && a->surf && a->crit0,
               "ffs_reml_surface: null buffer");
-  const size_t smem = (sizeof(float2) * SURF_G + sizeof(float) + 1) * (size_t)a->T;
+  const size_t smem = (sizeof(float4) * SURF_G2 + sizeof(float) + 1) * (size_t)a->T;
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_surface: T=%d too long", a->T);
   FFS_CUDA(cudaFuncSetAttribute(surface_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid(ceil_div(a->V, SURF_THREADS), a->n_chunks);
+  FFS_REQUIRE(ceil_div(a->V, SURF_THREADS) <= 65535, "ffs_reml_surface: V=%d exceeds one launch", a->V);
+  dim3 grid(a->n_chunks, ceil_div(a->V, SURF_THREADS));
   surface_kernel<<<grid, SURF_THREADS, smem, (cudaStream_t)stream>>>(*a);
   return check_launch("surface_kernel");
 }
