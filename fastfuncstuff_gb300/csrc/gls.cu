@@ -13,6 +13,7 @@
 //   Ljung-Box of the whitened residual (arma.py:6058-6141);
 // then unscaled by the voxel's std (arma.py:5827-5862).
 #include "common.cuh"
+#include "tile.cuh"
 
 namespace ffsk {
 namespace {
@@ -25,6 +26,9 @@ struct GlsExtra {
   const float* lj_w;    // [lj_h + 1] 1 / n_k for good bins, 0 otherwise
   float* ljung_box;     // [V]
 };
+
+__device__ void gls_finish(const ffs_gls_args& a, const GlsExtra& x, int v, int g, float* beta, const float* w,
+                           float ssr, float sst, float ssw, float m, float sc, float* bins);
 
 // GLS of one voxel v at pair g, executed by one warp. Gp = G of pair g and Xt
 // (the transposed design) may live in shared or global memory; ys, r, beta and
@@ -115,6 +119,18 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
   float ssw = 0.f;
   for (int t = lane; t < T; t += 32) ssw = fmaf(ys[t], ys[t], ssw);
   ssw = warp_sum(ssw);
+  gls_finish(a, x, v, g, beta, ys, ssr, sst, ssw, m, sc, bins);
+}
+
+// The statistics of voxel v at pair g from its betas (of the centred, scaled
+// series: beta, shared memory), whitened residual w (shared memory, [T]) and
+// sums of squares; executed by one warp.
+__device__ void gls_finish(const ffs_gls_args& a, const GlsExtra& x, const int v, const int g, float* beta,
+                           const float* w, const float ssr, const float sst, const float ssw, const float m,
+                           const float sc, float* bins) {
+  const int lane = threadIdx.x & 31;
+  const int T = a.T, K = a.K;
+  const float* ys = w;
   if (a.resid_w) {
     for (int t = lane; t < T; t += 32) a.resid_w[(size_t)v * T + t] = ys[t] * sc;
   }
@@ -223,16 +239,35 @@ __global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, Gls
 }
 
 // Tiles of up to GLS_TILE voxels that share one pair (voxels grouped by pair:
-// order[end[g-1] .. end[g]) are pair g's, end[-1] = 0). The pair's G and the
-// transposed design are staged in shared memory once per tile; tile_start[g]
-// numbers the tiles of pair g. Blocks past the last tile exit.
-constexpr int GLS_TILE = 32;
-constexpr int GLS_TWARPS = 8;
+// order[end[g-1] .. end[g]) are pair g's, end[-1] = 0); tile_start[g] numbers
+// the tiles of pair g and blocks past the last tile exit. T % 4 == 0.
+//
+// The tile's 32 series sit in shared memory, one voxel per lane (tile.cuh):
+//   b0 = G'y and r = y - X b0, then d = G'r and r -= X d (b = b0 + d) as
+//   register-blocked passes; the whitened residual L^-1 r by 8 segments of
+//   the time axis (one per warp): each warp runs v_t = z_t - m_t v_{t-1} from
+//   v = 0 over its segment, the true state entering segment k is carried
+//   across the segment ends, and each sample adds its term prod(-m) * v_in.
+// The per-voxel statistics (gls_finish) then run one warp per voxel.
+constexpr int GLS_TILE = TILE_V;
 
-__global__ void __launch_bounds__(GLS_TWARPS * 32) gls_tile_kernel(ffs_gls_args a, GlsExtra x, const int* end,
-                                                                   const int* tile_start, int P, int ld_s, int kp,
+__global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_args a, GlsExtra x, const int* end,
+                                                                   const int* tile_start, int P, int ld, int kp,
                                                                    int hb) {
-  extern __shared__ float sm[];
+  extern __shared__ float4 sm4[];
+  const int T = a.T, K = a.K, nq = T >> 2;
+  float* Ys = reinterpret_cast<float*>(sm4);        // [32][ld]
+  float* C0 = Ys + (size_t)TILE_V * ld;             // [K][32] b0
+  float* C1 = C0 + (size_t)K * TILE_V;              // [K][32] d
+  float* part = C1 + (size_t)K * TILE_V;            // [2][K][32]
+  float* red = part + 2 * (size_t)K * TILE_V;       // [3][8][32] SS_res, SS_tot, SS_w partials
+  float* vend = red + 3 * TILE_WARPS * TILE_V;      // [8][32]
+  float* carry = vend + TILE_WARPS * TILE_V;        // [8][32]
+  float* Hs = carry + TILE_WARPS * TILE_V;          // [32]
+  float* st = Hs + TILE_V;                          // [6][32] m, sc, mean, ssr, sst, ssw
+  float* betas = st + 6 * TILE_V;                   // [8][kp]
+  float* bins = betas + (size_t)TILE_WARPS * kp;    // [8][hb]
+
   const int tile = blockIdx.x;
   if (tile >= tile_start[P]) return;
   int lo = 0, hi = P;  // largest g with tile_start[g] <= tile
@@ -244,20 +279,189 @@ __global__ void __launch_bounds__(GLS_TWARPS * 32) gls_tile_kernel(ffs_gls_args 
   const int g0 = g ? end[g - 1] : 0;
   const int j0 = g0 + (tile - tile_start[g]) * GLS_TILE;
   const int n = min(GLS_TILE, end[g] - j0);
-  const int KT = a.K * a.T;
-  float* Gs = sm;
-  float* Xs = sm + KT;
-  const float* Gg = a.G + (size_t)g * KT;
-  for (int i = threadIdx.x; i < KT; i += blockDim.x) {
-    Gs[i] = Gg[i];
-    Xs[i] = a.Xt[i];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+
+  // stage (y - m) / s of each voxel; empty slots of a short tile are zero
+  for (int i = wid; i < TILE_V; i += TILE_WARPS) {
+    float4* row4 = reinterpret_cast<float4*>(Ys + (size_t)i * ld);
+    if (i >= n) {  // warp-uniform
+      for (int q = lane; q < nq; q += 32) row4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (lane == 0) {
+        st[i] = 0.f;
+        st[TILE_V + i] = 1.f;
+        st[2 * TILE_V + i] = 0.f;
+      }
+      continue;
+    }
+    const int v = a.order[j0 + i];
+    const float sc = a.scale[v];
+    const float4* y4 = reinterpret_cast<const float4*>(a.Y + (size_t)v * T);
+    float m = 0.f;
+    if (a.center) {
+      float s = 0.f;
+      for (int q = lane; q < nq; q += 32) {
+        const float4 y = y4[q];
+        s += ((y.x + y.y) + y.z) + y.w;
+      }
+      m = warp_sum(s) / (float)T;
+    }
+    float sy = 0.f;
+    for (int q = lane; q < nq; q += 32) {
+      const float4 y = y4[q];
+      float4 r;
+      r.x = __fdiv_rn(__fsub_rn(y.x, m), sc);
+      r.y = __fdiv_rn(__fsub_rn(y.y, m), sc);
+      r.z = __fdiv_rn(__fsub_rn(y.z, m), sc);
+      r.w = __fdiv_rn(__fsub_rn(y.w, m), sc);
+      row4[q] = r;
+      sy += ((r.x + r.y) + r.z) + r.w;
+    }
+    sy = warp_sum(sy);
+    if (lane == 0) {
+      st[i] = m;
+      st[TILE_V + i] = sc;
+      st[2 * TILE_V + i] = sy / (float)T;
+    }
   }
   __syncthreads();
-  const int wid = threadIdx.x >> 5;
-  float* ys = sm + 2 * (size_t)KT + (size_t)wid * (2 * ld_s + kp + hb);
-  for (int i = wid; i < n; i += GLS_TWARPS) {
+
+  const float* Gg = a.G + (size_t)g * K * T;
+  int q0, q1;
+  tile_qrange(T, wid, q0, q1);
+  float4* rr = reinterpret_cast<float4*>(Ys + (size_t)lane * ld);
+  // b0 = G'y; SS_tot of the owned samples; r = y - X b0
+  tile_project(Gg, Ys, T, ld, K, C0, part);
+  {
+    const float mu = st[2 * TILE_V + lane];
+    float sst = 0.f;
+    for (int q = q0; q < q1; ++q) {
+      const float4 r = rr[q];
+      float d = r.x - mu;
+      sst = fmaf(d, d, sst);
+      d = r.y - mu;
+      sst = fmaf(d, d, sst);
+      d = r.z - mu;
+      sst = fmaf(d, d, sst);
+      d = r.w - mu;
+      sst = fmaf(d, d, sst);
+    }
+    red[(TILE_WARPS + wid) * TILE_V + lane] = sst;
+  }
+  tile_subtract(a.Xt, C0, Ys, T, ld, K);
+  __syncthreads();
+  // d = G'r; r -= X d; SS_res and the unwhitened outputs
+  tile_project(Gg, Ys, T, ld, K, C1, part);
+  tile_subtract(a.Xt, C1, Ys, T, ld, K);
+  {
+    float ssr = 0.f;
+    for (int q = q0; q < q1; ++q) {
+      const float4 r = rr[q];
+      ssr = fmaf(r.x, r.x, ssr);
+      ssr = fmaf(r.y, r.y, ssr);
+      ssr = fmaf(r.z, r.z, ssr);
+      ssr = fmaf(r.w, r.w, ssr);
+    }
+    red[wid * TILE_V + lane] = ssr;
+    if (lane < n && (a.resid || a.pred)) {
+      const int v = a.order[j0 + lane];
+      const float m = st[lane], sc = st[TILE_V + lane];
+      for (int q = q0; q < q1; ++q) {
+        if (a.resid) {
+          const float4 r = rr[q];
+          reinterpret_cast<float4*>(a.resid + (size_t)v * T)[q] = make_float4(r.x * sc, r.y * sc, r.z * sc, r.w * sc);
+        }
+        if (a.pred) {  // X b, b = b0 + d
+          float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int j = 0; j < K; ++j) {
+            const float bj = C0[j * TILE_V + lane] + C1[j * TILE_V + lane];
+            const float4 xj = __ldg(reinterpret_cast<const float4*>(a.Xt + (size_t)j * T) + q);
+            p.x = fmaf(xj.x, bj, p.x);
+            p.y = fmaf(xj.y, bj, p.y);
+            p.z = fmaf(xj.z, bj, p.z);
+            p.w = fmaf(xj.w, bj, p.w);
+          }
+          reinterpret_cast<float4*>(a.pred + (size_t)v * T)[q] =
+              make_float4(fmaf(p.x, sc, m), fmaf(p.y, sc, m), fmaf(p.z, sc, m), fmaf(p.w, sc, m));
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // whitened residual by segments of the time axis
+  const int SQ = (nq + TILE_WARPS - 1) / TILE_WARPS;
+  const int s0 = min(T, wid * SQ * 4), s1 = min(T, (wid + 1) * SQ * 4);
+  const float4* cf = reinterpret_cast<const float4*>(a.coef) + (size_t)g * T;
+  float rp = s0 > 0 ? Ys[(size_t)lane * ld + s0 - 1] : 0.f;
+  __syncthreads();
+  {
+    float vp = 0.f, H = 1.f;
+    for (int t = s0; t < s1; t += 4) {
+      const float4 r = rr[t >> 2];
+      const float rv[4] = {r.x, r.y, r.z, r.w};
+      float o[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float4 q = __ldg(cf + t + k);
+        const float z = fmaf(-q.x, rp, rv[k]);
+        const float vt = fmaf(-q.y, vp, z);
+        o[k] = vt;
+        rp = rv[k];
+        vp = vt;
+        H *= -q.y;
+      }
+      rr[t >> 2] = make_float4(o[0], o[1], o[2], o[3]);
+    }
+    vend[wid * TILE_V + lane] = vp;
+    if (lane == 0) Hs[wid] = H;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    float vin = 0.f;
+    for (int k = 0; k < TILE_WARPS; ++k) {
+      carry[k * TILE_V + lane] = vin;
+      vin = fmaf(Hs[k], vin, vend[k * TILE_V + lane]);
+    }
+  }
+  __syncthreads();
+  {
+    const float cin = carry[wid * TILE_V + lane];
+    float h = 1.f, ssw = 0.f;
+    for (int t = s0; t < s1; t += 4) {
+      const float4 r = rr[t >> 2];
+      const float rv[4] = {r.x, r.y, r.z, r.w};
+      float o[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float4 q = __ldg(cf + t + k);
+        h *= -q.y;
+        const float wt = fmaf(h, cin, rv[k]) * q.w;
+        ssw = fmaf(wt, wt, ssw);
+        o[k] = wt;
+      }
+      rr[t >> 2] = make_float4(o[0], o[1], o[2], o[3]);
+    }
+    red[(2 * TILE_WARPS + wid) * TILE_V + lane] = ssw;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float s = 0.f;
+      for (int w = 0; w < TILE_WARPS; ++w) s += red[(k * TILE_WARPS + w) * TILE_V + lane];
+      st[(3 + k) * TILE_V + lane] = s;
+    }
+  }
+  __syncthreads();
+
+  // per-voxel statistics: warp w takes voxels w, w + 8, ...
+  float* b = betas + (size_t)wid * kp;
+  for (int i = wid; i < n; i += TILE_WARPS) {
     const int v = a.order[j0 + i];
-    gls_voxel(a, x, v, g, Gs, Xs, ys, ys + ld_s, ys + 2 * ld_s, ys + 2 * ld_s + kp);
+    for (int j = lane; j < K; j += 32) b[j] = C0[j * TILE_V + i] + C1[j * TILE_V + i];
+    __syncwarp();
+    gls_finish(a, x, v, g, b, Ys + (size_t)i * ld, st[3 * TILE_V + i], st[4 * TILE_V + i], st[5 * TILE_V + i],
+               st[i], st[TILE_V + i], bins + (size_t)wid * hb);
     __syncwarp();
   }
 }
@@ -331,12 +535,13 @@ extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* 
   FFS_REQUIRE(a->n_glt == 0 || (a->glt && a->glt_var && a->cbeta && a->ct), "ffs_reml_gls_grouped: GLT buffers");
   FFS_REQUIRE(lj_h >= 0 && lj_h <= a->T / 2, "ffs_reml_gls_grouped: Ljung-Box lag %d out of range", lj_h);
   FFS_REQUIRE(lj_h == 0 || (lj_w && ljung_box), "ffs_reml_gls_grouped: Ljung-Box buffers");
-  const int ld_s = a->T + 1;
+  const int ld = tile_ld(a->T);
   const int kp = (a->K + 3) & ~3;
   const int hb = (lj_h + 4) & ~3;
-  const size_t mats = sizeof(float) * 2 * (size_t)a->K * a->T;
-  const size_t smem = mats + sizeof(float) * GLS_TWARPS * (size_t)(2 * ld_s + kp + hb);
-  if (smem > 200 * 1024) {  // the pair's matrices do not fit: read them from global memory
+  const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + 4 * (size_t)a->K * TILE_V +
+                                       (3 + 2) * TILE_WARPS * TILE_V + TILE_V + 6 * TILE_V +
+                                       (size_t)TILE_WARPS * (kp + hb));
+  if (a->T % 4 != 0 || smem > 200 * 1024) {  // no 16-byte rows, or the tile does not fit: one warp per voxel
     return ffs_reml_gls_ex(a, lj_h, lj_tau, lj_w, ljung_box, stream);
   }
   cudaStream_t st = (cudaStream_t)stream;
@@ -344,7 +549,7 @@ extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* 
   gls_tile_scan<<<1, 1024, 0, st>>>(P, group_end, tile_start);
   FFS_CUDA(cudaFuncSetAttribute(gls_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int max_tiles = ceil_div(a->V, GLS_TILE) + P;
-  gls_tile_kernel<<<max_tiles, GLS_TWARPS * 32, smem, st>>>(*a, x, group_end, tile_start, P, ld_s, kp, hb);
+  gls_tile_kernel<<<max_tiles, TILE_WARPS * 32, smem, st>>>(*a, x, group_end, tile_start, P, ld, kp, hb);
   return check_launch("gls_tile_kernel");
 }
 

@@ -6,6 +6,7 @@
 //   group    counting sort of voxels by their chosen pair
 //   project  (CUDA-core form) ||U'y||^2 for every (voxel, pair)
 #include "common.cuh"
+#include "tile.cuh"
 
 namespace ffsk {
 
@@ -85,6 +86,96 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
   }
 }
 
+// Tiled form for T % 4 == 0: 32 voxels per CTA, one per lane, the projection
+// c = Q0 y and the update y -= Q0' c as register-blocked passes over the tile
+// (tile.cuh), i.e. y - Q0'(Q0 y) in one step as the reference's
+// Y - (Y pinv(X)') X' (fastfuncstuff/glm/arma.py:1554-1571).
+__global__ void __launch_bounds__(TILE_WARPS * 32) prep_tile_kernel(ffs_prep_args a, int ld) {
+  extern __shared__ float4 sm4[];
+  float* Ys = reinterpret_cast<float*>(sm4);       // [32][ld]
+  float* Cq = Ys + (size_t)TILE_V * ld;            // [K][32]
+  float* part = Cq + (size_t)a.K * TILE_V;         // [2][K][32]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int T = a.T, K = a.K, nq = T >> 2;
+  const int v0 = blockIdx.x * TILE_V;
+  const int nv = min(TILE_V, a.V - v0);
+  for (int i = wid; i < TILE_V; i += TILE_WARPS) {
+    float* row = Ys + (size_t)i * ld;
+    float4* row4 = reinterpret_cast<float4*>(row);
+    if (i >= nv) {  // warp-uniform: empty lanes of the last tile stay zero
+      for (int q = lane; q < nq; q += 32) row4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
+    const int v = v0 + i;
+    const float4* y4 = reinterpret_cast<const float4*>(a.Y + (size_t)v * T);
+    // mean and (N-1) variance, two passes for accuracy
+    float s = 0.f;
+    for (int q = lane; q < nq; q += 32) {
+      const float4 x = y4[q];
+      row4[q] = x;
+      s += ((x.x + x.y) + x.z) + x.w;
+    }
+    const float mean = warp_sum(s) / (float)T;
+    __syncwarp();
+    float sq = 0.f;
+    for (int t = lane; t < T; t += 32) {
+      const float dlt = row[t] - mean;
+      sq += dlt * dlt;
+    }
+    sq = warp_sum(sq);
+    float sc = 1.0f;
+    if (a.do_scale) {
+      sc = sqrtf(sq / (float)(T - 1));
+      sc = fmaxf(sc, 1e-8f);
+    }
+    const float m = a.center ? mean : 0.f;
+    for (int t = lane; t < T; t += 32) row[t] = __fdiv_rn(__fsub_rn(row[t], m), sc);
+    if (lane == 0) a.scale[v] = sc;
+  }
+  __syncthreads();
+  if (K > 0) {
+    tile_project(a.Q0, Ys, T, ld, K, Cq, part);
+    tile_subtract(a.Q0, Cq, Ys, T, ld, K);
+  }
+  __syncthreads();
+  if (a.yr_hi) {
+    for (int i = wid; i < nv; i += TILE_WARPS) {
+      const float* row = Ys + (size_t)i * ld;
+      const int v = v0 + i;
+      float amax = 0.f;
+      for (int t = lane; t < T; t += 32) amax = fmaxf(amax, fabsf(row[t]));
+      for (int off = 16; off > 0; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
+      const int e = scale_exp(amax);
+      if (lane == 0) a.yexp[v] = e;
+      // two samples per lane: 32-bit stores of (hi_t, hi_t+1)
+      uint32_t* hi = reinterpret_cast<uint32_t*>(a.yr_hi + (size_t)v * a.ld_y);
+      uint32_t* lo = reinterpret_cast<uint32_t*>(a.yr_lo + (size_t)v * a.ld_y);
+      for (int t2 = lane; t2 < (a.ld_y >> 1); t2 += 32) {
+        uint16_t h0 = 0, l0 = 0, h1 = 0, l1 = 0;
+        const int t = 2 * t2;
+        if (t < T) split_fp16(ldexpf(row[t], e), h0, l0);
+        if (t + 1 < T) split_fp16(ldexpf(row[t + 1], e), h1, l1);
+        hi[t2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        lo[t2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+      }
+    }
+  }
+  // time-major store: lane = voxel (coalesced 128-byte rows), warp w takes
+  // quads w, w + 8, ...
+  if (lane < nv) {
+    const float4* r4 = reinterpret_cast<const float4*>(Ys + (size_t)lane * ld);
+    float* out = a.yr_t + v0 + lane;
+    const size_t V = (size_t)a.V;
+    for (int q = wid; q < nq; q += TILE_WARPS) {
+      const float4 r = r4[q];
+      out[(size_t)(4 * q) * V] = r.x;
+      out[(size_t)(4 * q + 1) * V] = r.y;
+      out[(size_t)(4 * q + 2) * V] = r.z;
+      out[(size_t)(4 * q + 3) * V] = r.w;
+    }
+  }
+}
+
 // --------------------------------------------------------------------- surface
 // One thread per voxel, one CTA per (chunk of pairs sharing one AR filter,
 // voxel tile). For each pair g of the chunk: v_t = z_t - m_t v_{t-1},
@@ -94,7 +185,9 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
 // previous step's for every pair of the chunk (the LDL' factor of a Toeplitz
 // run converges to a constant, so most steps after a short transient are such
 // "steady" steps) reuses the registers instead of reloading them. Each thread
-// prefetches 32 samples of its voxel at a time so the loads overlap.
+// prefetches 32 samples of its voxel at a time so the loads overlap; a block of
+// 32 steady steps sums v_t^2 alone and multiplies the block's sum by the
+// common 1/D once (two packed instructions per pair couple and step).
 constexpr int SURF_G = 16;
 constexpr int SURF_G2 = SURF_G / 2;
 constexpr int SURF_THREADS = 256;
@@ -128,6 +221,7 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
   extern __shared__ float4 cf4[];  // [T][SURF_G2] (-m_2k, -m_2k+1, 1/D_2k, 1/D_2k+1)
   float* cs = reinterpret_cast<float*>(cf4 + (size_t)a.T * SURF_G2);  // [T] c_t
   uint8_t* steady = reinterpret_cast<uint8_t*>(cs + a.T);            // [T]
+  uint8_t* bsteady = steady + a.T;                                   // [ceil(T / SURF_TB)]
   // chunks are the fast grid dimension: the CTAs of one voxel tile run together
   // and its samples stay in L2 across the chunks
   const int chunk = blockIdx.x;
@@ -161,6 +255,13 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
     steady[t] = same ? 1 : 0;
   }
   __syncthreads();
+  // a block is steady when all its SURF_TB steps are (a partial last block never is)
+  for (int bk = threadIdx.x; bk * SURF_TB < T; bk += blockDim.x) {
+    bool all = bk * SURF_TB + SURF_TB <= T;
+    for (int t = bk * SURF_TB; t < bk * SURF_TB + SURF_TB && all; ++t) all = steady[t] != 0;
+    bsteady[bk] = all ? 1 : 0;
+  }
+  __syncthreads();
 
   const int v = blockIdx.y * SURF_THREADS + threadIdx.x;
   if (v >= a.V) return;
@@ -174,20 +275,10 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
     float yb[SURF_TB];
 #pragma unroll
     for (int k = 0; k < SURF_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * a.V] : 0.f;
+    if (bsteady[t0 / SURF_TB]) {
+      // 32 steady steps: the coefficients in registers hold for all of them
 #pragma unroll
-    for (int k = 0; k < SURF_TB; ++k) {
-      const int t = t0 + k;
-      if (t < T) {
-        if (!steady[t]) {
-          c = cs[t];
-          const float4* row = cf4 + (size_t)t * SURF_G2;
-#pragma unroll
-          for (int j = 0; j < SURF_G2; ++j) {
-            const float4 q = row[j];
-            nm[j] = pack2(q.x, q.y);
-            id[j] = pack2(q.z, q.w);
-          }
-        }
+      for (int k = 0; k < SURF_TB; ++k) {
         const float y = yb[k];
         const float z = fmaf(-c, yp, y);
         yp = y;
@@ -196,14 +287,46 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
 #pragma unroll
         for (int j = 0; j < SURF_G2; ++j) {
           vv[j] = fma2(nm[j], vv[j], z2);
-          sb[j] = fma2(mul2(vv[j], id[j]), vv[j], sb[j]);
+          sb[j] = fma2(vv[j], vv[j], sb[j]);
         }
       }
-    }
 #pragma unroll
-    for (int j = 0; j < SURF_G2; ++j) {
-      st[j] = add2(st[j], sb[j]);
-      sb[j] = zero2;
+      for (int j = 0; j < SURF_G2; ++j) {
+        st[j] = fma2(sb[j], id[j], st[j]);
+        sb[j] = zero2;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < SURF_TB; ++k) {
+        const int t = t0 + k;
+        if (t < T) {
+          if (!steady[t]) {
+            c = cs[t];
+            const float4* row = cf4 + (size_t)t * SURF_G2;
+#pragma unroll
+            for (int j = 0; j < SURF_G2; ++j) {
+              const float4 q = row[j];
+              nm[j] = pack2(q.x, q.y);
+              id[j] = pack2(q.z, q.w);
+            }
+          }
+          const float y = yb[k];
+          const float z = fmaf(-c, yp, y);
+          yp = y;
+          yy_b = fmaf(y, y, yy_b);
+          const uint64_t z2 = pack2(z, z);
+#pragma unroll
+          for (int j = 0; j < SURF_G2; ++j) {
+            vv[j] = fma2(nm[j], vv[j], z2);
+            sb[j] = fma2(mul2(vv[j], id[j]), vv[j], sb[j]);
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < SURF_G2; ++j) {
+        st[j] = add2(st[j], sb[j]);
+        sb[j] = zero2;
+      }
     }
     yy += yy_b;
     yy_b = 0.f;
@@ -392,6 +515,15 @@ extern "C" int ffs_reml_prep(const ffs_prep_args* a, void* stream) {
   FFS_REQUIRE(a->Y && a->scale && a->yr_t && (a->K == 0 || a->Q0), "ffs_reml_prep: null buffer");
   FFS_REQUIRE(!a->yr_hi || (a->yr_lo && a->yexp && a->ld_y >= a->T && a->ld_y % 8 == 0),
               "ffs_reml_prep: ld_y=%d must be >= T and a multiple of 8", a->ld_y);
+  if (a->T % 4 == 0) {
+    const int ld = tile_ld(a->T);
+    const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + 3 * (size_t)a->K * TILE_V);
+    if (smem <= 200 * 1024) {
+      FFS_CUDA(cudaFuncSetAttribute(prep_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      prep_tile_kernel<<<ceil_div(a->V, TILE_V), TILE_WARPS * 32, smem, (cudaStream_t)stream>>>(*a, ld);
+      return check_launch("prep_tile_kernel");
+    }
+  }
   const int ld_s = a->T + ((a->T & 1) ? 2 : 1);  // odd stride: conflict-free transposed reads
   const size_t smem = sizeof(float) * PREP_VOX * ld_s;
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_prep: T=%d too long for one tile", a->T);
@@ -407,7 +539,7 @@ extern "C" int ffs_reml_surface(const ffs_surface_args* a, void* stream) {
   FFS_REQUIRE(a->yr_t && a->coef && a->logdet_R && a->logdet_XtX && a->proj && a->chunk_start &&
                   a->chunk_pairs && a->surf && a->crit0,
               "ffs_reml_surface: null buffer");
-  const size_t smem = (sizeof(float4) * SURF_G2 + sizeof(float) + 1) * (size_t)a->T;
+  const size_t smem = (sizeof(float4) * SURF_G2 + sizeof(float) + 1) * (size_t)a->T + ceil_div(a->T, SURF_TB);
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_surface: T=%d too long", a->T);
   FFS_CUDA(cudaFuncSetAttribute(surface_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   FFS_REQUIRE(ceil_div(a->V, SURF_THREADS) <= 65535, "ffs_reml_surface: V=%d exceeds one launch", a->V);

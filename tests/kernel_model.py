@@ -57,20 +57,30 @@ def surface(yr: np.ndarray, grid, coef: np.ndarray, proj: np.ndarray, const: np.
         yp = np.zeros(V, F32)
         yyb = np.zeros(V, F32)
         yyt = np.zeros(V, F32)
-        for t in range(T):
-            y = yr[:, t]
-            z = (y - cs[t] * yp).astype(F32)
-            yp = y
-            yyb = (yyb + y * y).astype(F32)
-            m = coef[members, t, 1][:, None]
-            iD = coef[members, t, 2][:, None]
-            v = (z[None, :] - m * v).astype(F32)
-            sb = (sb + (v * iD).astype(F32) * v).astype(F32)
-            if (t + 1) % 32 == 0 or t == T - 1:
-                st = (st + sb).astype(F32)
-                sb[:] = 0
-                yyt = (yyt + yyb).astype(F32)
-                yyb[:] = 0
+        # steady[t]: every member's coefficients equal step t-1's; a block of
+        # 32 steady steps sums v^2 alone and scales the block sum by 1/D once
+        cm = coef[members]
+        steady = np.zeros(T, bool)
+        steady[1:] = (cm[:, 1:, :3] == cm[:, :-1, :3]).all(axis=(0, 2)) & (cs[1:] == cs[:-1])
+        for t0 in range(0, T, 32):
+            block_steady = t0 + 32 <= T and bool(steady[t0 : t0 + 32].all())
+            iD = coef[members, t0, 2][:, None]
+            for t in range(t0, min(T, t0 + 32)):
+                y = yr[:, t]
+                z = (y - cs[t] * yp).astype(F32)
+                yp = y
+                yyb = (yyb + y * y).astype(F32)
+                m = coef[members, t, 1][:, None]
+                v = (z[None, :] - m * v).astype(F32)
+                if block_steady:
+                    sb = (sb + v * v).astype(F32)
+                else:
+                    iD = coef[members, t, 2][:, None]
+                    sb = (sb + (v * iD).astype(F32) * v).astype(F32)
+            st = (st + sb * iD).astype(F32) if block_steady else (st + sb).astype(F32)
+            sb[:] = 0
+            yyt = (yyt + yyb).astype(F32)
+            yyb[:] = 0
         st_all[members] = st
         yy = yyt
     Tk = T - K

@@ -174,6 +174,36 @@ def test_fit_matches_fp64_oracle(case, exhaustive):
     np.testing.assert_allclose(got.r2_partial.numpy()[same], ref.r2_partial[same], atol=1e-4)
 
 
+@pytest.mark.parametrize("T", [96, 94, 93])
+def test_fit_any_series_length_matches_fp64_oracle(T):
+    """T % 4 == 0 runs the 32-voxel tile kernels of prep and GLS; other lengths
+    the one-warp-per-voxel kernels. Both against the FP64 oracle, with the
+    residual, whitened-residual, fitted-value and Ljung-Box outputs."""
+    d = load_golden("single")
+    Y = np.ascontiguousarray(d["Y"][:, :T])
+    X = np.ascontiguousarray(d["X"][:T])
+    kw = dict(a_grid=d["a_grid"], b_grid=d["b_grid"], want_residuals=True, want_ljung_box=True)
+    ref = o.fit_glm_arma11(Y, X, use_double=True, fp64_scaled=True, force_exhaustive_search=True,
+                           save_profile_likelihoods=True, **kw)
+    got = fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, projector=PROJ, force_exhaustive_search=True,
+                         want_predicted=True, **kw)
+    grid = G.make_grid(d["a_grid"], d["b_grid"])
+    idx = _index(got.arma_params.numpy(), grid)
+    check_selection(idx, ref.arma_index, ref.reml_lklhd_surface)
+    same = idx == ref.arma_index
+    assert rel_maxnorm(got.betas.numpy()[same], ref.betas[same]).max() <= BETA_REL
+    assert rel_maxnorm(got.tstats.numpy()[same], ref.tstats[same]).max() <= BETA_REL
+    np.testing.assert_allclose(got.sigma2.numpy()[same], ref.sigma2[same], rtol=1e-4)
+    np.testing.assert_allclose(got.r2.numpy()[same], ref.r2[same], atol=2e-5)
+    np.testing.assert_allclose(got.residuals.numpy()[same], ref.residuals[same], rtol=1e-4, atol=2e-4)
+    np.testing.assert_allclose(got.residuals_whitened.numpy()[same], ref.residuals_whitened[same],
+                               rtol=1e-4, atol=2e-4)
+    np.testing.assert_allclose(got.ljung_box.numpy()[same], ref.ljung_box[same], rtol=2e-3, atol=1e-3)
+    # fitted values + residuals give back the data
+    scale = np.abs(Y).max(axis=1, keepdims=True)
+    np.testing.assert_allclose((got.predicted + got.residuals).numpy() / scale, Y / scale, atol=1e-5)
+
+
 def test_reference_float32_selection_agrees():
     """The reference's own float32 run (golden) selects what the GPU selects."""
     for case in ("single", "multirun", "censored", "baseline"):
