@@ -123,7 +123,6 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
   PairScratch s = scratch_of(o.work, p, T, K);
 
   __shared__ double red[32];
-  __shared__ double run_ld[64];
   __shared__ int flag, bad_r;
 
   const float af = d.a[p], bf = d.b[p];
@@ -132,18 +131,26 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
   if (threadIdx.x == 0) bad_r = 0;
   __syncthreads();
 
-  // ---- 1. per-run LDL' of the AR-filtered tridiagonal correlation
-  double ld_local = 0.0;
+  // ---- 1. per-run LDL' of the AR-filtered tridiagonal correlation: the
+  // serial recursion m_t = T_t,t-1 / D_t-1, D_t = T_tt - m_t T_t,t-1 (one
+  // thread per run; unit gaps need no pow: a^1 = a and a^0 = 1 exactly), then
+  // sqrt, log and the reciprocals of every sample in parallel
   for (int r = threadIdx.x; r < d.n_runs; r += blockDim.x) {
     const int t0 = d.run_start[r], t1 = d.run_start[r + 1];
-    double Dprev = 1.0, ld = 0.0;
+    double Dprev = 1.0;
     for (int t = t0; t < t1; ++t) {
       double c = 0.0, m = 0.0, D = 1.0;
       // lambda == 0: every lag correlation is zero, R = I exactly
       if (t > t0 && lam != 0.0) {
         const int gap = d.tau[t] - d.tau[t - 1];
-        c = pow(a, (double)gap);
-        const double rho = lam * pow(a, (double)(gap - 1));
+        double rho;
+        if (gap == 1) {
+          c = a;
+          rho = lam;
+        } else {
+          c = pow(a, (double)gap);
+          rho = lam * pow(a, (double)(gap - 1));
+        }
         const double Ttt = 1.0 + c * c - 2.0 * c * rho;
         const double Toff = rho - c;
         m = Toff / Dprev;
@@ -153,29 +160,28 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
         bad_r = 1;
         D = 1.0;
       }
-      const double sD = sqrt(D);
-      const double rsD = 1.0 / sD;
-      ld += 2.0 * log(sD + 1e-10);
       double* cm = s.cm + 4 * t;
-      cm[0] = c; cm[1] = m; cm[2] = D; cm[3] = rsD;
-      reinterpret_cast<float4*>(o.coef)[(size_t)p * T + t] =
-          make_float4((float)c, (float)m, (float)(1.0 / D), (float)rsD);
+      cm[0] = c; cm[1] = m; cm[2] = D;
       Dprev = D;
     }
-    if (r < 64) run_ld[r] = ld; else ld_local += ld;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double ld = 0.0;
-    for (int r = 0; r < min(d.n_runs, 64); ++r) ld += run_ld[r];
-    red[1] = ld;
   }
   __syncthreads();
   {
-    // runs beyond 64 (rare) are summed through a block reduction
-    const double extra = block_sum(ld_local, red + 2);
-    if (threadIdx.x == 0) o.logdet_R[p] = red[1] + extra;
+    double ld = 0.0;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+      double* cm = s.cm + 4 * t;
+      const double D = cm[2];
+      const double sD = sqrt(D);
+      const double rsD = 1.0 / sD;
+      ld += 2.0 * log(sD + 1e-10);
+      cm[3] = rsD;
+      reinterpret_cast<float4*>(o.coef)[(size_t)p * T + t] =
+          make_float4((float)cm[0], (float)cm[1], (float)(1.0 / D), (float)rsD);
+    }
+    ld = block_sum(ld, red);
+    if (threadIdx.x == 0) o.logdet_R[p] = ld;
   }
+  __syncthreads();
 
   // ---- 2. X_w = L^-1 X, one column per thread
   for (int j = threadIdx.x; j < K; j += blockDim.x) {

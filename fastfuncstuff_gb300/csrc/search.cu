@@ -177,21 +177,24 @@ __global__ void __launch_bounds__(TILE_WARPS * 32) prep_tile_kernel(ffs_prep_arg
 }
 
 // --------------------------------------------------------------------- surface
-// One thread per voxel, one CTA per (chunk of pairs sharing one AR filter,
-// voxel tile). For each pair g of the chunk: v_t = z_t - m_t v_{t-1},
-// s += v_t^2 / D_t. The chunk's coefficient table is staged in shared memory
-// as (-m, 1/D) of pair couples, so each couple advances with packed
-// fma.rn.f32x2 / mul.rn.f32x2 instructions. A step whose coefficients equal the
-// previous step's for every pair of the chunk (the LDL' factor of a Toeplitz
-// run converges to a constant, so most steps after a short transient are such
+// One thread per voxel, one CTA per (chunk of 16 pair slots, voxel tile). A
+// chunk is 4 quarters of up to 4 pairs; the pairs of a quarter share one AR
+// filter c_t (one a, or lambda == 0), so each step forms z = y_t - c_t y_{t-1}
+// once per quarter. For each pair: v_t = z_t - m_t v_{t-1}, s += v_t^2 / D_t.
+// The chunk's coefficient table is staged in shared memory as (-m, 1/D) of
+// pair couples, so each couple advances with packed fma.rn.f32x2 /
+// mul.rn.f32x2 instructions. A step whose coefficients equal the previous
+// step's for every pair of the chunk (the LDL' factor of a Toeplitz run
+// converges to a constant, so most steps after a short transient are such
 // "steady" steps) reuses the registers instead of reloading them. Each thread
-// prefetches 32 samples of its voxel at a time so the loads overlap; a block of
-// 32 steady steps sums v_t^2 alone and multiplies the block's sum by the
-// common 1/D once (two packed instructions per pair couple and step).
+// prefetches 16 samples of its voxel at a time so the loads overlap; a block of
+// 16 steady steps sums v_t^2 alone and multiplies the block's sum by the
+// common 1/D once (two packed instructions per pair couple and step). A chunk
+// of identity pairs only (R = I) sums y_t^2 once for all of them.
 constexpr int SURF_G = 16;
 constexpr int SURF_G2 = SURF_G / 2;
 constexpr int SURF_THREADS = 256;
-constexpr int SURF_TB = 32;  // time steps per prefetch block
+constexpr int SURF_TB = 16;  // time steps per prefetch block
 
 __device__ __forceinline__ uint64_t pack2(float lo, float hi) {
   uint64_t r;
@@ -219,9 +222,9 @@ __device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
 
 __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_args a) {
   extern __shared__ float4 cf4[];  // [T][SURF_G2] (-m_2k, -m_2k+1, 1/D_2k, 1/D_2k+1)
-  float* cs = reinterpret_cast<float*>(cf4 + (size_t)a.T * SURF_G2);  // [T] c_t
-  uint8_t* steady = reinterpret_cast<uint8_t*>(cs + a.T);            // [T]
-  uint8_t* bsteady = steady + a.T;                                   // [ceil(T / SURF_TB)]
+  float4* cs4 = cf4 + (size_t)a.T * SURF_G2;                        // [T] c_t of the 4 quarters
+  uint8_t* steady = reinterpret_cast<uint8_t*>(cs4 + a.T);          // [T]
+  uint8_t* bsteady = steady + a.T;                                  // [ceil(T / SURF_TB)]
   // chunks are the fast grid dimension: the CTAs of one voxel tile run together
   // and its samples stay in L2 across the chunks
   const int chunk = blockIdx.x;
@@ -229,25 +232,46 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
   const int ng = c1 - c0;
   const int T = a.T;
   const float4* coef = reinterpret_cast<const float4*>(a.coef);
+  auto pair_of = [&](int slot) { return slot < ng ? a.chunk_pairs[c0 + slot] : -1; };
+  // coefficient table; an empty slot keeps m = 0, 1/D = 0 (its sum stays 0).
+  // ident: every filled slot is the identity (lambda == 0: c = m = 0, D = 1)
+  int ident = 1;
   for (int idx = threadIdx.x; idx < T * SURF_G2; idx += blockDim.x) {
     const int t = idx / SURF_G2, k = idx % SURF_G2;
     float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (2 * k < ng) {
-      const float4 q = coef[(size_t)a.chunk_pairs[c0 + 2 * k] * T + t];
+    const int p0 = pair_of(2 * k), p1 = pair_of(2 * k + 1);
+    if (p0 >= 0) {
+      const float4 q = coef[(size_t)p0 * T + t];
       val.x = -q.y;
       val.z = q.z;
+      ident &= q.x == 0.f && q.y == 0.f && q.z == 1.f;
     }
-    if (2 * k + 1 < ng) {
-      const float4 q = coef[(size_t)a.chunk_pairs[c0 + 2 * k + 1] * T + t];
+    if (p1 >= 0) {
+      const float4 q = coef[(size_t)p1 * T + t];
       val.y = -q.y;
       val.w = q.z;
+      ident &= q.x == 0.f && q.y == 0.f && q.z == 1.f;
     }
     cf4[idx] = val;
   }
-  for (int t = threadIdx.x; t < T; t += blockDim.x) cs[t] = coef[(size_t)a.chunk_pairs[c0] * T + t].x;
-  __syncthreads();
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
-    bool same = t > 0 && cs[t] == cs[t - 1];
+    float cq[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      // the quarter's first filled slot carries its AR filter
+      int p = -1;
+      for (int s2 = 4 * q; s2 < 4 * q + 4 && p < 0; ++s2) p = pair_of(s2);
+      cq[q] = p >= 0 ? coef[(size_t)p * T + t].x : 0.f;
+    }
+    cs4[t] = make_float4(cq[0], cq[1], cq[2], cq[3]);
+  }
+  ident = __syncthreads_and(ident);
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    bool same = false;
+    if (t > 0) {
+      const float4 u = cs4[t], w = cs4[t - 1];
+      same = u.x == w.x && u.y == w.y && u.z == w.z && u.w == w.w;
+    }
     for (int k = 0; k < SURF_G2 && same; ++k) {
       const float4 x = cf4[t * SURF_G2 + k], y = cf4[(t - 1) * SURF_G2 + k];
       same = x.x == y.x && x.y == y.y && x.z == y.z && x.w == y.w;
@@ -265,83 +289,108 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
 
   const int v = blockIdx.y * SURF_THREADS + threadIdx.x;
   if (v >= a.V) return;
-  uint64_t vv[SURF_G2], sb[SURF_G2], st[SURF_G2], nm[SURF_G2], id[SURF_G2];
-  const uint64_t zero2 = pack2(0.f, 0.f);
-#pragma unroll
-  for (int k = 0; k < SURF_G2; ++k) vv[k] = sb[k] = st[k] = nm[k] = id[k] = zero2;
-  float c = 0.f, yy_b = 0.f, yy = 0.f, yp = 0.f;
   const float* yc = a.yr_t + v;
-  for (int t0 = 0; t0 < T; t0 += SURF_TB) {
-    float yb[SURF_TB];
-#pragma unroll
-    for (int k = 0; k < SURF_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * a.V] : 0.f;
-    if (bsteady[t0 / SURF_TB]) {
-      // 32 steady steps: the coefficients in registers hold for all of them
-#pragma unroll
+  float yy = 0.f;
+  float sg[SURF_G];
+  if (ident) {
+    // R = I for every pair of the chunk: y'R^-1 y = sum y^2, accumulated in
+    // the same blocks and order as the recurrence (bit-identical to it)
+    for (int t0 = 0; t0 < T; t0 += SURF_TB) {
+      float yy_b = 0.f;
+#pragma unroll 8
       for (int k = 0; k < SURF_TB; ++k) {
-        const float y = yb[k];
-        const float z = fmaf(-c, yp, y);
-        yp = y;
-        yy_b = fmaf(y, y, yy_b);
-        const uint64_t z2 = pack2(z, z);
-#pragma unroll
-        for (int j = 0; j < SURF_G2; ++j) {
-          vv[j] = fma2(nm[j], vv[j], z2);
-          sb[j] = fma2(vv[j], vv[j], sb[j]);
+        if (t0 + k < T) {
+          const float y = yc[(size_t)(t0 + k) * a.V];
+          yy_b = fmaf(y, y, yy_b);
         }
       }
+      yy += yy_b;
+    }
 #pragma unroll
-      for (int j = 0; j < SURF_G2; ++j) {
-        st[j] = fma2(sb[j], id[j], st[j]);
-        sb[j] = zero2;
-      }
-    } else {
+    for (int g = 0; g < SURF_G; ++g) sg[g] = yy;
+  } else {
+    uint64_t vv[SURF_G2], sb[SURF_G2], st[SURF_G2], nm[SURF_G2], id[SURF_G2];
+    const uint64_t zero2 = pack2(0.f, 0.f);
 #pragma unroll
-      for (int k = 0; k < SURF_TB; ++k) {
-        const int t = t0 + k;
-        if (t < T) {
-          if (!steady[t]) {
-            c = cs[t];
-            const float4* row = cf4 + (size_t)t * SURF_G2;
+    for (int k = 0; k < SURF_G2; ++k) vv[k] = sb[k] = st[k] = nm[k] = id[k] = zero2;
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    float yy_b = 0.f, yp = 0.f;
+    for (int t0 = 0; t0 < T; t0 += SURF_TB) {
+      float yb[SURF_TB];
 #pragma unroll
-            for (int j = 0; j < SURF_G2; ++j) {
-              const float4 q = row[j];
-              nm[j] = pack2(q.x, q.y);
-              id[j] = pack2(q.z, q.w);
-            }
-          }
+      for (int k = 0; k < SURF_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * a.V] : 0.f;
+      if (bsteady[t0 / SURF_TB]) {
+        // SURF_TB steady steps: the coefficients in registers hold for all of them
+#pragma unroll
+        for (int k = 0; k < SURF_TB; ++k) {
           const float y = yb[k];
-          const float z = fmaf(-c, yp, y);
+          uint64_t z2[4];
+          z2[0] = pack2(fmaf(-c.x, yp, y), fmaf(-c.x, yp, y));
+          z2[1] = pack2(fmaf(-c.y, yp, y), fmaf(-c.y, yp, y));
+          z2[2] = pack2(fmaf(-c.z, yp, y), fmaf(-c.z, yp, y));
+          z2[3] = pack2(fmaf(-c.w, yp, y), fmaf(-c.w, yp, y));
           yp = y;
           yy_b = fmaf(y, y, yy_b);
-          const uint64_t z2 = pack2(z, z);
 #pragma unroll
-          for (int j = 0; j < SURF_G2; ++j) {
-            vv[j] = fma2(nm[j], vv[j], z2);
-            sb[j] = fma2(mul2(vv[j], id[j]), vv[j], sb[j]);
+          for (int j = 0; j < SURF_G2; ++j) vv[j] = fma2(nm[j], vv[j], z2[j >> 1]);
+#pragma unroll
+          for (int j = 0; j < SURF_G2; ++j) sb[j] = fma2(vv[j], vv[j], sb[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < SURF_G2; ++j) {
+          st[j] = fma2(sb[j], id[j], st[j]);
+          sb[j] = zero2;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < SURF_TB; ++k) {
+          const int t = t0 + k;
+          if (t < T) {
+            if (!steady[t]) {
+              c = cs4[t];
+              const float4* row = cf4 + (size_t)t * SURF_G2;
+#pragma unroll
+              for (int j = 0; j < SURF_G2; ++j) {
+                const float4 q = row[j];
+                nm[j] = pack2(q.x, q.y);
+                id[j] = pack2(q.z, q.w);
+              }
+            }
+            const float y = yb[k];
+            uint64_t z2[4];
+            z2[0] = pack2(fmaf(-c.x, yp, y), fmaf(-c.x, yp, y));
+            z2[1] = pack2(fmaf(-c.y, yp, y), fmaf(-c.y, yp, y));
+            z2[2] = pack2(fmaf(-c.z, yp, y), fmaf(-c.z, yp, y));
+            z2[3] = pack2(fmaf(-c.w, yp, y), fmaf(-c.w, yp, y));
+            yp = y;
+            yy_b = fmaf(y, y, yy_b);
+#pragma unroll
+            for (int j = 0; j < SURF_G2; ++j) {
+              vv[j] = fma2(nm[j], vv[j], z2[j >> 1]);
+              sb[j] = fma2(mul2(vv[j], id[j]), vv[j], sb[j]);
+            }
           }
         }
-      }
 #pragma unroll
-      for (int j = 0; j < SURF_G2; ++j) {
-        st[j] = add2(st[j], sb[j]);
-        sb[j] = zero2;
+        for (int j = 0; j < SURF_G2; ++j) {
+          st[j] = add2(st[j], sb[j]);
+          sb[j] = zero2;
+        }
       }
+      yy += yy_b;
+      yy_b = 0.f;
     }
-    yy += yy_b;
-    yy_b = 0.f;
+#pragma unroll
+    for (int j = 0; j < SURF_G2; ++j) unpack2(st[j], sg[2 * j], sg[2 * j + 1]);
   }
   const int Tk = a.T - a.K;
   const double c_p0 = a.logdet_R[a.p0] + a.logdet_XtX[a.p0];
   const float rss0 = fmaxf(yy - a.proj[(size_t)a.p0 * a.V + v], 0.f);
   const float den = rss0 + 1e-10f;
-  float sg[SURF_G];
-#pragma unroll
-  for (int j = 0; j < SURF_G2; ++j) unpack2(st[j], sg[2 * j], sg[2 * j + 1]);
 #pragma unroll
   for (int g = 0; g < SURF_G; ++g) {
-    if (g < ng) {
-      const int p = a.chunk_pairs[c0 + g];
+    const int p = pair_of(g);
+    if (p >= 0) {
       const float rss = fmaxf(sg[g] - a.proj[(size_t)p * a.V + v], 0.f);
       const float dc = (float)((a.logdet_R[p] + a.logdet_XtX[p]) - c_p0);
       const float dv = dc + (float)Tk * log1pf((rss - rss0) / den);
@@ -539,7 +588,7 @@ extern "C" int ffs_reml_surface(const ffs_surface_args* a, void* stream) {
   FFS_REQUIRE(a->yr_t && a->coef && a->logdet_R && a->logdet_XtX && a->proj && a->chunk_start &&
                   a->chunk_pairs && a->surf && a->crit0,
               "ffs_reml_surface: null buffer");
-  const size_t smem = (sizeof(float4) * SURF_G2 + sizeof(float) + 1) * (size_t)a->T + ceil_div(a->T, SURF_TB);
+  const size_t smem = (sizeof(float4) * (SURF_G2 + 1) + 1) * (size_t)a->T + ceil_div(a->T, SURF_TB);
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_surface: T=%d too long", a->T);
   FFS_CUDA(cudaFuncSetAttribute(surface_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   FFS_REQUIRE(ceil_div(a->V, SURF_THREADS) <= 65535, "ffs_reml_surface: V=%d exceeds one launch", a->V);

@@ -21,7 +21,8 @@ import torch
 DEFAULT_ARMA_A_GRID = (0.0, 0.8, 9)
 DEFAULT_ARMA_B_GRID = (-0.8, 0.8, 17)
 
-SURFACE_CHUNK = 16  # pairs per surface-kernel chunk (csrc/search.cu SURF_G)
+SURFACE_CHUNK = 16  # pair slots per surface-kernel chunk (csrc/search.cu SURF_G)
+SURFACE_QUARTER = 4  # slots per quarter: pairs of one quarter share one AR filter
 
 
 class _RemlMode:
@@ -107,7 +108,7 @@ class RemlGrid:
     zb: int
     ltop: int
     chunk_start: np.ndarray  # (n_chunks + 1,) int32
-    chunk_pairs: np.ndarray  # (P,) int32 pairs of each chunk (one AR filter per chunk)
+    chunk_pairs: np.ndarray  # int32 pair slots of each chunk (-1: empty), one AR filter per quarter
     lambda_fp32: bool
 
     @property
@@ -133,23 +134,41 @@ def lambda_is_zero(a: np.ndarray, b: np.ndarray) -> np.ndarray:
 
 
 def coefficient_chunks(a: np.ndarray, b: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
-    """Chunks of pairs whose AR filter coefficients c_t are identical.
+    """Chunks of SURFACE_CHUNK pair slots for the surface kernel.
 
-    Pairs sharing a share c_t = a^gap; pairs with lambda == 0 (R = I) use the
-    identity (c = 0) whatever their a, so they form one class of their own.
-    Each class is split into chunks of at most SURFACE_CHUNK pairs, in pair order.
+    Pairs sharing a share the AR filter c_t = a^gap; pairs with lambda == 0
+    (R = I) use the identity (c = 0) whatever their a, so they form one class
+    of their own. Each class is cut into quarters of at most SURFACE_QUARTER
+    pairs (padded with -1, an empty slot) and a chunk takes up to four
+    quarters, in class order; identity quarters fill chunks of their own, which
+    the kernel evaluates as one sum of squares.
+    Returns (chunk_start, chunk_pairs): the slots of chunk c are
+    chunk_pairs[chunk_start[c] : chunk_start[c + 1]].
     """
     ident = lambda_is_zero(a, b)
     classes: dict = {}
     for p in range(a.size):
         key = "identity" if ident[p] else float(a[p])
         classes.setdefault(key, []).append(p)
-    starts, pairs = [0], []
-    for members in classes.values():
-        for i in range(0, len(members), SURFACE_CHUNK):
-            pairs.extend(members[i : i + SURFACE_CHUNK])
-            starts.append(len(pairs))
-    return np.asarray(starts, np.int32), np.asarray(pairs, np.int32)
+    q = SURFACE_QUARTER
+    per = SURFACE_CHUNK // q
+
+    def quarters(members):
+        out = []
+        for i in range(0, len(members), q):
+            part = members[i : i + q]
+            out.append(part + [-1] * (q - len(part)))
+        return out
+
+    idq = quarters(classes.pop("identity", []))
+    otherq = [qq for members in classes.values() for qq in quarters(members)]
+    starts, slots = [0], []
+    for group in (idq, otherq):
+        for i in range(0, len(group), per):
+            for qq in group[i : i + per]:
+                slots.extend(qq)
+            starts.append(len(slots))
+    return np.asarray(starts, np.int32), np.asarray(slots, np.int32)
 
 
 def hierarchical_ltop(n_a: int, n_b: int, afni_faithful: bool) -> int:

@@ -198,7 +198,7 @@ int ffs_reml_project_simt(const ffs_project_args* a, void* stream);
  * float32 arithmetic resolves differences between neighbouring pairs:
  *   d[p][v] = (const_p - const_p0) + (T-K) log1p((RSS_p - RSS_p0)/(RSS_p0+1e-10))
  * and crit = crit0[v] + d[p][v], crit0 = const_p0 + (T-K) log(RSS_p0 + 1e-10)
- * evaluated in FP64. Pairs are walked in chunks that share a (work list below).
+ * evaluated in FP64. Pairs are walked in chunks of 4 quarters (work list below).
  */
 typedef struct {
   int V, T, K, P;
@@ -207,9 +207,11 @@ typedef struct {
   const float* coef;      /* [P][T][4]                                            */
   const double* logdet_R; const double* logdet_XtX;  /* [P]                      */
   const float* proj;      /* [P][V]                                               */
-  const int* chunk_start; /* device [n_chunks+1]: pairs of chunk c are           */
-  int n_chunks;           /*   chunk_pairs[chunk_start[c] .. chunk_start[c+1])   */
-  const int* chunk_pairs; /*   all pairs of a chunk share one a                  */
+  const int* chunk_start; /* device [n_chunks+1]: the (at most 16) pair slots of */
+  int n_chunks;           /*   chunk c are chunk_pairs[chunk_start[c] ..         */
+  const int* chunk_pairs; /*   chunk_start[c+1]), -1 an empty slot; slots 4q..4q+3 */
+                          /*   (quarter q) share one AR filter: one a, or all    */
+                          /*   lambda == 0 (identity)                            */
   float* surf;            /* [P][V] d[p][v]                                       */
   double* crit0;          /* [V]                                                  */
 } ffs_surface_args;

@@ -48,9 +48,11 @@ def surface(yr: np.ndarray, grid, coef: np.ndarray, proj: np.ndarray, const: np.
     d = np.zeros((P, V), F32)
     yy = np.zeros(V, F32)
     st_all = np.zeros((P, V), F32)
+    TB = 16  # steps per sample block (SURF_TB)
     for c in range(len(grid.chunk_start) - 1):
-        members = grid.chunk_pairs[grid.chunk_start[c] : grid.chunk_start[c + 1]]
-        cs = coef[members[0], :, 0]
+        slots = grid.chunk_pairs[grid.chunk_start[c] : grid.chunk_start[c + 1]]
+        members = slots[slots >= 0]
+        cs = coef[members, :, 0][:, :, None]  # each pair's own AR filter (shared per quarter)
         v = np.zeros((len(members), V), F32)
         sb = np.zeros((len(members), V), F32)
         st = np.zeros((len(members), V), F32)
@@ -58,20 +60,20 @@ def surface(yr: np.ndarray, grid, coef: np.ndarray, proj: np.ndarray, const: np.
         yyb = np.zeros(V, F32)
         yyt = np.zeros(V, F32)
         # steady[t]: every member's coefficients equal step t-1's; a block of
-        # 32 steady steps sums v^2 alone and scales the block sum by 1/D once
+        # TB steady steps sums v^2 alone and scales the block sum by 1/D once
         cm = coef[members]
         steady = np.zeros(T, bool)
-        steady[1:] = (cm[:, 1:, :3] == cm[:, :-1, :3]).all(axis=(0, 2)) & (cs[1:] == cs[:-1])
-        for t0 in range(0, T, 32):
-            block_steady = t0 + 32 <= T and bool(steady[t0 : t0 + 32].all())
+        steady[1:] = (cm[:, 1:, :3] == cm[:, :-1, :3]).all(axis=(0, 2))
+        for t0 in range(0, T, TB):
+            block_steady = t0 + TB <= T and bool(steady[t0 : t0 + TB].all())
             iD = coef[members, t0, 2][:, None]
-            for t in range(t0, min(T, t0 + 32)):
+            for t in range(t0, min(T, t0 + TB)):
                 y = yr[:, t]
-                z = (y - cs[t] * yp).astype(F32)
+                z = (y[None, :] - cs[:, t] * yp[None, :]).astype(F32)
                 yp = y
                 yyb = (yyb + y * y).astype(F32)
                 m = coef[members, t, 1][:, None]
-                v = (z[None, :] - m * v).astype(F32)
+                v = (z - m * v).astype(F32)
                 if block_steady:
                     sb = (sb + v * v).astype(F32)
                 else:

@@ -38,18 +38,25 @@ def test_grid_matches_oracle(grids, use_double):
         ai = np.searchsorted(g.a_axis, g.a[p])
         bi = np.searchsorted(g.b_axis, g.b[p])
         assert g.lattice[ai, bi] == p
-    # every chunk shares one AR filter: one a, or only lambda == 0 pairs (identity)
+    # every quarter shares one AR filter: one a, or only lambda == 0 pairs
+    # (identity); identity quarters never share a chunk with other quarters
     ident = G.lambda_is_zero(g.a, g.b)
+    Q = G.SURFACE_QUARTER
     for c in range(len(g.chunk_start) - 1):
         s, e = g.chunk_start[c], g.chunk_start[c + 1]
-        assert 0 < e - s <= G.SURFACE_CHUNK
-        members = g.chunk_pairs[s:e]
-        if ident[members].any():
-            assert ident[members].all()
-        else:
-            assert len(set(g.a[members].tolist())) == 1
-    assert g.chunk_start[-1] == g.P
-    assert sorted(g.chunk_pairs.tolist()) == list(range(g.P))
+        assert 0 < e - s <= G.SURFACE_CHUNK and (e - s) % Q == 0
+        slots = g.chunk_pairs[s:e]
+        filled = slots[slots >= 0]
+        assert filled.size > 0
+        assert ident[filled].all() or not ident[filled].any()
+        for q0 in range(0, e - s, Q):
+            members = slots[q0 : q0 + Q]
+            members = members[members >= 0]
+            assert members.size > 0
+            if not ident[members].any():
+                assert len(set(g.a[members].tolist())) == 1
+    filled = g.chunk_pairs[g.chunk_pairs >= 0]
+    assert sorted(filled.tolist()) == list(range(g.P))
     assert ident[g.p0]
 
 
