@@ -223,7 +223,8 @@ __device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
 __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_args a) {
   extern __shared__ float4 cf4[];  // [T][SURF_G2] (-m_2k, -m_2k+1, 1/D_2k, 1/D_2k+1)
   float4* cs4 = cf4 + (size_t)a.T * SURF_G2;                        // [T] c_t of the 4 quarters
-  uint8_t* steady = reinterpret_cast<uint8_t*>(cs4 + a.T);          // [T]
+  float* dcs = reinterpret_cast<float*>(cs4 + a.T);                 // [SURF_G] const_p - const_p0
+  uint8_t* steady = reinterpret_cast<uint8_t*>(dcs + SURF_G);       // [T]
   uint8_t* bsteady = steady + a.T;                                  // [ceil(T / SURF_TB)]
   // chunks are the fast grid dimension: the CTAs of one voxel tile run together
   // and its samples stay in L2 across the chunks
@@ -264,6 +265,11 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
       cq[q] = p >= 0 ? coef[(size_t)p * T + t].x : 0.f;
     }
     cs4[t] = make_float4(cq[0], cq[1], cq[2], cq[3]);
+  }
+  if (threadIdx.x < SURF_G) {
+    const double c_p0 = a.logdet_R[a.p0] + a.logdet_XtX[a.p0];
+    const int p = pair_of(threadIdx.x);
+    dcs[threadIdx.x] = p >= 0 ? (float)((a.logdet_R[p] + a.logdet_XtX[p]) - c_p0) : 0.f;
   }
   ident = __syncthreads_and(ident);
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
@@ -384,7 +390,6 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
     for (int j = 0; j < SURF_G2; ++j) unpack2(st[j], sg[2 * j], sg[2 * j + 1]);
   }
   const int Tk = a.T - a.K;
-  const double c_p0 = a.logdet_R[a.p0] + a.logdet_XtX[a.p0];
   const float rss0 = fmaxf(yy - a.proj[(size_t)a.p0 * a.V + v], 0.f);
   const float den = rss0 + 1e-10f;
 #pragma unroll
@@ -392,12 +397,11 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
     const int p = pair_of(g);
     if (p >= 0) {
       const float rss = fmaxf(sg[g] - a.proj[(size_t)p * a.V + v], 0.f);
-      const float dc = (float)((a.logdet_R[p] + a.logdet_XtX[p]) - c_p0);
-      const float dv = dc + (float)Tk * log1pf((rss - rss0) / den);
+      const float dv = dcs[g] + (float)Tk * log1pf((rss - rss0) / den);
       a.surf[(size_t)p * a.V + v] = dv;
     }
   }
-  if (chunk == 0) a.crit0[v] = c_p0 + (double)Tk * log((double)rss0 + 1e-10);
+  if (chunk == 0) a.crit0[v] = (a.logdet_R[a.p0] + a.logdet_XtX[a.p0]) + (double)Tk * log((double)rss0 + 1e-10);
 }
 
 // ---------------------------------------------------------------------- select
@@ -588,7 +592,8 @@ extern "C" int ffs_reml_surface(const ffs_surface_args* a, void* stream) {
   FFS_REQUIRE(a->yr_t && a->coef && a->logdet_R && a->logdet_XtX && a->proj && a->chunk_start &&
                   a->chunk_pairs && a->surf && a->crit0,
               "ffs_reml_surface: null buffer");
-  const size_t smem = (sizeof(float4) * (SURF_G2 + 1) + 1) * (size_t)a->T + ceil_div(a->T, SURF_TB);
+  const size_t smem = (sizeof(float4) * (SURF_G2 + 1) + 1) * (size_t)a->T + sizeof(float) * SURF_G +
+                      ceil_div(a->T, SURF_TB);
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_surface: T=%d too long", a->T);
   FFS_CUDA(cudaFuncSetAttribute(surface_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   FFS_REQUIRE(ceil_div(a->V, SURF_THREADS) <= 65535, "ffs_reml_surface: V=%d exceeds one launch", a->V);
