@@ -47,6 +47,8 @@ class PrepArgs(C.Structure):
         ("do_scale", C.c_int), ("center", C.c_int), ("ld_y", C.c_int), ("scale", C.c_void_p),
         ("yr_t", C.c_void_p),
         ("yr_hi", C.c_void_p), ("yr_lo", C.c_void_p), ("yexp", C.c_void_p),
+        ("idx", C.c_void_p), ("feats", C.c_void_p), ("n_runs", C.c_int), ("run_start", C.c_void_p),
+        ("yr_rows", C.c_void_p),
     ]
 
 
@@ -117,7 +119,6 @@ SIGNATURES = {
     "ffs_mlp_param_count": ([], C.c_int),
     "ffs_arma_simulate": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_uint64, C.c_void_p, C.c_void_p], C.c_int),
-    "ffs_reml_features": ([C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "ffs_mlp_forward": ([C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
     "ffs_mlp_grad": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                       C.c_void_p], C.c_int),
@@ -125,10 +126,17 @@ SIGNATURES = {
                       C.c_float, C.c_int, C.c_void_p], C.c_int),
     "ffs_reml_centers": ([C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
                          C.c_int),
-    "ffs_transpose_u": ([C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
-    "ffs_reml_window": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
-                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "ffs_reml_gather": ([C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "ffs_reml_window_items": ([C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                               C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+                              C.c_int),
+    "ffs_reml_window": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                         C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                         C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                         C.c_void_p, C.c_void_p], C.c_int),
+    "ffs_reml_project_tc_list": ([C.POINTER(ProjectArgs), C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                  C.c_void_p], C.c_int),
 }
 
 _LIB: C.CDLL | None = None

@@ -1,12 +1,11 @@
-// The learned (a, b) proposal: simulation of training voxels, their features,
-// and a 9 -> 64 -> 64 -> 2 GELU MLP with hand-written forward, backward and
-// Adam kernels.
+// The learned (a, b) proposal: simulation of training voxels and a
+// 9 -> 64 -> 64 -> 2 GELU MLP with hand-written forward, backward and Adam
+// kernels (the features come from the prep kernel, search.cu).
 //
 //   simulate  y_t = a y_{t-1} + e_t + b e_{t-1} per run (200 burn-in samples,
 //             standardised per run), Y = X beta + sigma * noise, beta ~ N(0,1),
 //             sigma ~ U(0.5, 2); normals from Philox4x32-10 (Salmon et al.,
 //             SC'11) through Box-Muller.
-//   features  lag-1..8 autocorrelations of the OLS residual inside runs, + T/1000.
 //   MLP       exact-erf GELU; loss sum (out - y)^2 / (2 B); Adam.
 #include "common.cuh"
 
@@ -116,41 +115,6 @@ __global__ void simulate_kernel(SimArgs s) {
       y[t] = acc;
     }
   }
-}
-
-// ---------------------------------------------------------------- features
-struct FeatArgs {
-  int V, T, n_runs;
-  const int* run_start;
-  const float* yr_t;   // [T][V]
-  float* feats;        // [V][9]
-};
-
-__global__ void features_kernel(FeatArgs f) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= f.V) return;
-  float ring[8];
-  float acc[8], s0 = 0.f;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) acc[k] = ring[k] = 0.f;
-  for (int r = 0; r < f.n_runs; ++r) {
-    const int t0 = f.run_start[r], t1 = f.run_start[r + 1];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) ring[k] = 0.f;  // no products across a run boundary
-    for (int t = t0; t < t1; ++t) {
-      const float y = f.yr_t[(size_t)t * f.V + v];
-      s0 = fmaf(y, y, s0);
-#pragma unroll
-      for (int k = 0; k < 8; ++k) acc[k] = fmaf(y, ring[k], acc[k]);
-#pragma unroll
-      for (int k = 7; k > 0; --k) ring[k] = ring[k - 1];
-      ring[0] = y;
-    }
-  }
-  float* out = f.feats + (size_t)v * 9;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) out[k] = s0 > 0.f ? acc[k] / s0 : 0.f;
-  out[8] = (float)f.T / 1000.0f;
 }
 
 // --------------------------------------------------------------------- MLP
@@ -311,15 +275,6 @@ extern "C" int ffs_arma_simulate(int V, int T, int K, int n_runs, const int* run
   SimArgs s{V, T, K, n_runs, run_start, X, a, b, seed, Y};
   simulate_kernel<<<ceil_div(V, 128), 128, 0, (cudaStream_t)stream>>>(s);
   return check_launch("simulate_kernel");
-}
-
-extern "C" int ffs_reml_features(int V, int T, int n_runs, const int* run_start, const float* yr_t, float* feats,
-                                 void* stream) {
-  clear_error();
-  FFS_REQUIRE(V > 0 && T > 0 && n_runs > 0 && run_start && yr_t && feats, "ffs_reml_features: bad arguments");
-  FeatArgs f{V, T, n_runs, run_start, yr_t, feats};
-  features_kernel<<<ceil_div(V, 128), 128, 0, (cudaStream_t)stream>>>(f);
-  return check_launch("features_kernel");
 }
 
 extern "C" int ffs_mlp_forward(const float* params, const float* x, int B, float* out, void* stream) {

@@ -32,13 +32,47 @@ constexpr uint32_t WAIT_LIMIT = 1u << 22;
 
 struct TcParams {
   int V, K, P, ld, T;  // ld: padded k extent (multiple of BK); T: real extent
-  int g, N;            // pairs per column tile, MMA N
+  int g, N;            // grid mode: pairs per column tile, MMA N
+  int NB;              // rows of every B box (>= the N of any item)
   int n_col_tiles, n_vox_tiles;
+  const ffs_tc_item* items;  // work-list mode: items[0 .. *n_items)
+  const int* n_items;
+  int s_pair, s_vox;   // output strides: out[(slot0 + j) * s_pair + (out0 + r) * s_vox]
   const int* yexp;
   const int* uexp;
   float* proj;
   int* flag;
 };
+
+// One work item: BM operand rows from v0 (nv of them real) against the np
+// pairs whose U rows start at row_b.
+struct Item {
+  int v0, nv, row_b, np, out0, slot0, N;
+};
+
+__device__ __forceinline__ Item item_at(const TcParams& prm, int item) {
+  Item it;
+  if (prm.items) {
+    const ffs_tc_item w = prm.items[item];
+    it.v0 = w.v0;
+    it.nv = w.nv;
+    it.row_b = w.row_b;
+    it.np = w.np;
+    it.out0 = w.out0;
+    it.slot0 = w.slot0;
+    it.N = (w.np * prm.K + 15) / 16 * 16;
+  } else {
+    const int col = item % prm.n_col_tiles;
+    it.v0 = (item / prm.n_col_tiles) * BM;
+    it.nv = min(BM, prm.V - it.v0);
+    it.row_b = col * prm.g * prm.K;
+    it.np = min(prm.g, prm.P - col * prm.g);
+    it.out0 = it.v0;
+    it.slot0 = col * prm.g;
+    it.N = prm.N;
+  }
+  return it;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -116,7 +150,7 @@ __global__ void __launch_bounds__(192, 1)
                       TcParams prm) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int b_tile = prm.N * BK * 2;
+  const int b_tile = prm.NB * BK * 2;
   const int stage_bytes = 2 * A_TILE + 2 * b_tile;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
   uint64_t* empty = full + STAGES;
@@ -127,7 +161,7 @@ __global__ void __launch_bounds__(192, 1)
   // a CTA that finds an earlier CTA's wait expired does nothing
   if (*reinterpret_cast<volatile int*>(prm.flag) != 0) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n_items = prm.n_col_tiles * prm.n_vox_tiles;
+  const int n_items = prm.items ? *prm.n_items : prm.n_col_tiles * prm.n_vox_tiles;
   const int nk = prm.ld / BK;
 
   if (threadIdx.x == 0) {
@@ -156,8 +190,8 @@ __global__ void __launch_bounds__(192, 1)
     int kc = 0;
     bool ok = true;
     for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-      const int v0 = (item / prm.n_col_tiles) * BM;
-      const int row_b = (item % prm.n_col_tiles) * prm.g * prm.K;
+      const Item it = item_at(prm, item);
+      const int v0 = it.v0, row_b = it.row_b;
       for (int kb = 0; kb < nk; ++kb, ++kc) {
         const int s = kc % STAGES;
         if (kc >= STAGES && !mbar_wait(empty + s, ((kc / STAGES) - 1) & 1)) {
@@ -176,10 +210,10 @@ __global__ void __launch_bounds__(192, 1)
     }
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer
-    const uint32_t idesc = idesc_f16(BM, prm.N);
     int kc = 0, local = 0;
     bool ok = true;
     for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x, ++local) {
+      const uint32_t idesc = idesc_f16(BM, item_at(prm, item).N);
       const int buf = local & 1;
       const uint32_t acc = tmem + (uint32_t)(buf * 256);
       if (local >= 2 && !mbar_wait(acc_empty + buf, ((local >> 1) - 1) & 1)) {
@@ -218,7 +252,6 @@ __global__ void __launch_bounds__(192, 1)
     // ---- epilogue: square and sum each pair's K columns from TMEM
     const int q = warp & 3;  // TMEM lane quarter this warp may access
     const int row = q * 32 + lane;
-    const int ncols = prm.g * prm.K;
     int local = 0;
     for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++local) {
       const int buf = local & 1;
@@ -228,12 +261,16 @@ __global__ void __launch_bounds__(192, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int v = (item / prm.n_col_tiles) * BM + row;
-      const int p_first = (item % prm.n_col_tiles) * prm.g;
-      const int ey = v < prm.V ? prm.yexp[v] : 0;
+      const Item it = item_at(prm, item);
+      const bool live = row < it.nv;
+      const int v = it.v0 + row;
+      const int p_first = it.row_b / prm.K;
+      const int ncols = it.np * prm.K;
+      const int ey = live ? prm.yexp[v] : 0;
+      float* out = prm.proj + (size_t)it.slot0 * prm.s_pair + (size_t)(it.out0 + row) * prm.s_vox;
       int j = 0, pl = 0;
       float run = 0.f;
-      for (int c0 = 0; c0 < prm.N; c0 += 16) {
+      for (int c0 = 0; c0 < it.N; c0 += 16) {
         uint32_t r[16];
         const uint32_t taddr = tmem + (uint32_t)(buf * 256) + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
         asm volatile(
@@ -249,9 +286,7 @@ __global__ void __launch_bounds__(192, 1)
             const float x = __uint_as_float(r[i]);
             run = fmaf(x, x, run);
             if (++j == prm.K) {
-              const int p = p_first + pl;
-              if (p < prm.P && v < prm.V)
-                prm.proj[(size_t)p * prm.V + v] = ldexpf(run, -2 * (ey + prm.uexp[p]));
+              if (live) out[(size_t)pl * prm.s_pair] = ldexpf(run, -2 * (ey + prm.uexp[p_first + pl]));
               run = 0.f;
               j = 0;
               ++pl;
@@ -304,6 +339,28 @@ int make_map(CUtensorMap* m, const void* base, int inner, int rows, int box_rows
   return FFS_OK;
 }
 
+// Maps of both operands (B boxes of prm.NB rows) and the persistent launch:
+// one CTA per SM, at most max_items CTAs.
+int launch_tc(const ffs_project_args* a, const TcParams& prm, int max_items, void* stream) {
+  CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;
+  int st;
+  if ((st = make_map(&ta_hi, a->yr_hi, a->ld_y, a->V, BM))) return st;
+  if ((st = make_map(&ta_lo, a->yr_lo, a->ld_y, a->V, BM))) return st;
+  if ((st = make_map(&tb_hi, a->u_hi, a->ld_u, a->P * a->K, prm.NB))) return st;
+  if ((st = make_map(&tb_lo, a->u_lo, a->ld_u, a->P * a->K, prm.NB))) return st;
+  const int stage_bytes = 2 * A_TILE + 2 * prm.NB * BK * 2;
+  const size_t smem = (size_t)STAGES * stage_bytes + 1024 + 128;
+  FFS_REQUIRE(smem <= 227 * 1024, "project_tc: tile needs %zu bytes of shared memory", smem);
+  FFS_CUDA(cudaFuncSetAttribute(project_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int dev = 0, n_sm = 0;
+  FFS_CUDA(cudaGetDevice(&dev));
+  FFS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  if (max_items <= 0) return FFS_OK;
+  project_tc_kernel<<<min(max_items, n_sm), 192, smem, (cudaStream_t)stream>>>(ta_hi, ta_lo, tb_hi, tb_lo,
+                                                                                     prm);
+  return check_launch("project_tc_kernel");
+}
+
 }  // namespace
 }  // namespace ffsk
 
@@ -332,25 +389,50 @@ extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
   prm.N = ((prm.g * a->K) + 15) / 16 * 16;
   prm.n_col_tiles = ceil_div(a->P, prm.g);
   prm.n_vox_tiles = ceil_div(a->V, BM);
+  prm.NB = prm.N;
   prm.T = a->T;
+  prm.items = nullptr;
+  prm.n_items = nullptr;
+  prm.s_pair = a->V;
+  prm.s_vox = 1;
   prm.yexp = a->yexp;
   prm.uexp = a->uexp;
   prm.proj = a->proj;
   prm.flag = a->flag;
-  CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;
-  int st;
-  if ((st = make_map(&ta_hi, a->yr_hi, a->ld_y, a->V, BM))) return st;
-  if ((st = make_map(&ta_lo, a->yr_lo, a->ld_y, a->V, BM))) return st;
-  if ((st = make_map(&tb_hi, a->u_hi, a->ld_u, a->P * a->K, prm.N))) return st;
-  if ((st = make_map(&tb_lo, a->u_lo, a->ld_u, a->P * a->K, prm.N))) return st;
-  const int stage_bytes = 2 * A_TILE + 2 * prm.N * BK * 2;
-  const size_t smem = (size_t)STAGES * stage_bytes + 1024 + 128;
-  FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_project_tc: tile needs %zu bytes of shared memory", smem);
-  FFS_CUDA(cudaFuncSetAttribute(project_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int dev = 0, n_sm = 0;
-  FFS_CUDA(cudaGetDevice(&dev));
-  FFS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
-  const int n_items = prm.n_col_tiles * prm.n_vox_tiles;
-  project_tc_kernel<<<min(n_items, n_sm), 192, smem, (cudaStream_t)stream>>>(ta_hi, ta_lo, tb_hi, tb_lo, prm);
-  return check_launch("project_tc_kernel");
+  return launch_tc(a, prm, prm.n_col_tiles * prm.n_vox_tiles, stream);
+}
+
+extern "C" int ffs_reml_project_tc_list(const ffs_project_args* a, const ffs_tc_item* items, const int* n_items,
+                                        int max_items, int max_pairs, int ld_out, void* stream) {
+  clear_error();
+  FFS_REQUIRE(a && a->V > 0 && a->T > 0 && a->K > 0 && a->P > 0, "ffs_reml_project_tc_list: bad sizes");
+  FFS_REQUIRE(a->yr_hi && a->yr_lo && a->u_hi && a->u_lo && a->yexp && a->uexp && a->proj && a->flag && items &&
+                  n_items,
+              "ffs_reml_project_tc_list: null buffer");
+  FFS_REQUIRE(a->ld_y == a->ld_u && a->ld_y % BK == 0 && a->ld_y >= a->T,
+              "ffs_reml_project_tc_list: ld_y=%d and ld_u=%d must be equal multiples of %d", a->ld_y, a->ld_u, BK);
+  FFS_REQUIRE(max_pairs > 0 && max_pairs * a->K <= 256 && max_items > 0 && ld_out > 0,
+              "ffs_reml_project_tc_list: max_pairs=%d x K=%d must fit one 256-column tile", max_pairs, a->K);
+  for (const void* ptr : {(const void*)a->yr_hi, (const void*)a->yr_lo, (const void*)a->u_hi, (const void*)a->u_lo})
+    FFS_REQUIRE(((uintptr_t)ptr & 15) == 0, "ffs_reml_project_tc_list: operands must be 16-byte aligned");
+  TcParams prm;
+  prm.V = a->V;
+  prm.K = a->K;
+  prm.P = a->P;
+  prm.ld = a->ld_y;
+  prm.T = a->T;
+  prm.g = max_pairs;
+  prm.N = (max_pairs * a->K + 15) / 16 * 16;
+  prm.NB = prm.N;
+  prm.n_col_tiles = 1;
+  prm.n_vox_tiles = 0;
+  prm.items = items;
+  prm.n_items = n_items;
+  prm.s_pair = 1;
+  prm.s_vox = ld_out;
+  prm.yexp = a->yexp;
+  prm.uexp = a->uexp;
+  prm.proj = a->proj;
+  prm.flag = a->flag;
+  return launch_tc(a, prm, max_items, stream);
 }

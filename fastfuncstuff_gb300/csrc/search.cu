@@ -13,6 +13,33 @@ namespace ffsk {
 namespace {
 
 // ------------------------------------------------------------------------ prep
+// Lag 1..8 autocorrelations of one residualised row within runs (products
+// never cross a run boundary) and T/1000, by one warp; lane 0 writes out[9].
+__device__ void row_features(const float* row, int T, int n_runs, const int* run_start, float* out) {
+  const int lane = threadIdx.x & 31;
+  float acc[8], s0 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc[k] = 0.f;
+  for (int r = 0; r < n_runs; ++r) {
+    const int t0 = run_start[r], t1 = run_start[r + 1];
+    for (int t = t0 + lane; t < t1; t += 32) {
+      const float y = row[t];
+      s0 = fmaf(y, y, s0);
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (t + k + 1 < t1) acc[k] = fmaf(y, row[t + k + 1], acc[k]);
+    }
+  }
+  s0 = warp_sum(s0);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc[k] = warp_sum(acc[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) out[k] = s0 > 0.f ? acc[k] / s0 : 0.f;
+    out[8] = (float)T / 1000.0f;
+  }
+}
+
 // 8 warps, 32 voxels per CTA (4 per warp). The residualised rows are staged in
 // shared memory and written out time-major in coalesced 128-byte rows.
 constexpr int PREP_VOX = 32;
@@ -26,8 +53,9 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
     const int lv = wid * (PREP_VOX / 8) + k;
     const int v = v0 + lv;
     if (v >= a.V) break;  // warp-uniform
+    const int vs = a.idx ? a.idx[v] : v;  // source row
     float* row = sm + (size_t)lv * ld_s;
-    const float* y = a.Y + (size_t)v * T;
+    const float* y = a.Y + (size_t)vs * T;
     // mean and (N-1) variance, two passes for accuracy
     float s = 0.f;
     for (int t = lane; t < T; t += 32) {
@@ -61,7 +89,8 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
       for (int t = lane; t < T; t += 32) row[t] -= c * qj[t];
       __syncwarp();
     }
-    if (lane == 0) a.scale[v] = sc;
+    if (lane == 0) a.scale[vs] = sc;
+    if (a.feats) row_features(row, T, a.n_runs, a.run_start, a.feats + (size_t)v * 9);
     if (a.yr_hi) {
       float amax = 0.f;
       for (int t = lane; t < T; t += 32) amax = fmaxf(amax, fabsf(row[t]));
@@ -81,6 +110,14 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
   __syncthreads();
   // time-major store: warp w writes rows t = w, w+8, ...; lane = voxel
   const int nv = min(PREP_VOX, a.V - v0);
+  if (a.yr_rows) {
+    for (int k = 0; k < PREP_VOX / 8; ++k) {
+      const int lv = wid * (PREP_VOX / 8) + k;
+      if (lv >= nv) break;
+      for (int t = lane; t < T; t += 32) a.yr_rows[(size_t)(v0 + lv) * T + t] = sm[(size_t)lv * ld_s + t];
+    }
+  }
+  if (!a.yr_t) return;
   for (int t = wid; t < T; t += 8) {
     if (lane < nv) a.yr_t[(size_t)t * a.V + v0 + lane] = sm[(size_t)lane * ld_s + t];
   }
@@ -106,8 +143,8 @@ __global__ void __launch_bounds__(TILE_WARPS * 32) prep_tile_kernel(ffs_prep_arg
       for (int q = lane; q < nq; q += 32) row4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
       continue;
     }
-    const int v = v0 + i;
-    const float4* y4 = reinterpret_cast<const float4*>(a.Y + (size_t)v * T);
+    const int vs = a.idx ? a.idx[v0 + i] : v0 + i;  // source row
+    const float4* y4 = reinterpret_cast<const float4*>(a.Y + (size_t)vs * T);
     // mean and (N-1) variance, two passes for accuracy
     float s = 0.f;
     for (int q = lane; q < nq; q += 32) {
@@ -130,7 +167,7 @@ __global__ void __launch_bounds__(TILE_WARPS * 32) prep_tile_kernel(ffs_prep_arg
     }
     const float m = a.center ? mean : 0.f;
     for (int t = lane; t < T; t += 32) row[t] = __fdiv_rn(__fsub_rn(row[t], m), sc);
-    if (lane == 0) a.scale[v] = sc;
+    if (lane == 0) a.scale[vs] = sc;
   }
   __syncthreads();
   if (K > 0) {
@@ -138,6 +175,10 @@ __global__ void __launch_bounds__(TILE_WARPS * 32) prep_tile_kernel(ffs_prep_arg
     tile_subtract(a.Q0, Cq, Ys, T, ld, K);
   }
   __syncthreads();
+  if (a.feats) {
+    for (int i = wid; i < nv; i += TILE_WARPS)
+      row_features(Ys + (size_t)i * ld, T, a.n_runs, a.run_start, a.feats + (size_t)(v0 + i) * 9);
+  }
   if (a.yr_hi) {
     for (int i = wid; i < nv; i += TILE_WARPS) {
       const float* row = Ys + (size_t)i * ld;
@@ -160,9 +201,16 @@ __global__ void __launch_bounds__(TILE_WARPS * 32) prep_tile_kernel(ffs_prep_arg
       }
     }
   }
+  if (a.yr_rows) {  // voxel-major rows, a warp per row
+    for (int i = wid; i < nv; i += TILE_WARPS) {
+      const float4* r4 = reinterpret_cast<const float4*>(Ys + (size_t)i * ld);
+      float4* o4 = reinterpret_cast<float4*>(a.yr_rows + (size_t)(v0 + i) * T);
+      for (int q = lane; q < nq; q += 32) o4[q] = r4[q];
+    }
+  }
   // time-major store: lane = voxel (coalesced 128-byte rows), warp w takes
   // quads w, w + 8, ...
-  if (lane < nv) {
+  if (a.yr_t && lane < nv) {
     const float4* r4 = reinterpret_cast<const float4*>(Ys + (size_t)lane * ld);
     float* out = a.yr_t + v0 + lane;
     const size_t V = (size_t)a.V;
@@ -565,7 +613,8 @@ using namespace ffsk;
 extern "C" int ffs_reml_prep(const ffs_prep_args* a, void* stream) {
   clear_error();
   FFS_REQUIRE(a && a->V > 0 && a->T > 1 && a->K >= 0, "ffs_reml_prep: bad sizes");
-  FFS_REQUIRE(a->Y && a->scale && a->yr_t && (a->K == 0 || a->Q0), "ffs_reml_prep: null buffer");
+  FFS_REQUIRE(a->Y && a->scale && (a->K == 0 || a->Q0), "ffs_reml_prep: null buffer");
+  FFS_REQUIRE(!a->feats || (a->n_runs > 0 && a->run_start), "ffs_reml_prep: features need the run layout");
   FFS_REQUIRE(!a->yr_hi || (a->yr_lo && a->yexp && a->ld_y >= a->T && a->ld_y % 8 == 0),
               "ffs_reml_prep: ld_y=%d must be >= T and a multiple of 8", a->ld_y);
   if (a->T % 4 == 0) {

@@ -1,152 +1,282 @@
 // Learned-seeded refine: each voxel evaluates only the 5 x 5 lattice window
-// around its proposed (a, b), with the same criterion as the full grid
-// (fastfuncstuff/glm/arma.py:1983-2002, relative to the pair (0, 0)), and is
-// flagged for the full-grid search when its best pair touches a valid lattice
-// neighbour outside the window.
+// around its proposed (a, b) (clamped to the lattice), with the same
+// criterion as the full grid (fastfuncstuff/glm/arma.py:1983-2002, relative
+// to the pair (0, 0)), and is flagged for the full-grid search when its best
+// pair is not an identity pair and has a valid lattice neighbour outside the
+// window.
 //
-// One thread per voxel, voxels in the order given (grouped by window centre so
-// that a warp reads the same pairs' coefficients). A window row (5 pairs with
-// one a) is one pass over the voxel's series: per time point and pair, the AR
-// filter, the recurrence, the sum of squares and the K-column projection.
+// The voxels arrive sorted by window centre (rows of the sorted operands).
+//   window_items   one work item per (128-row tile of a centre, run of
+//                  consecutive valid pairs of one window row): the tcgen05
+//                  projection kernel's work list (||U'y||^2 per window slot);
+//   window_crit    one thread per sorted voxel: y'R^-1 y of every window pair
+//                  by the O(T) recurrence, the criterion, the argmin and the
+//                  edge test.
+// Pairs with lambda == 0 (R = I, the identity) all have the criterion of the
+// pair (0, 0) exactly (d = 0), and the full grid breaks that tie towards the
+// first identity pair in pair order, p_id. Window identity pairs are not
+// evaluated: a window holding one competes with (p_id, d = 0) instead.
 #include "common.cuh"
 
 namespace ffsk {
 namespace {
 
 constexpr int WIN = 5;
+constexpr int WSLOTS = WIN * WIN;
+constexpr int WTILE = 128;  // operand rows per projection item
 
-struct WinArgs {
-  int V, T, K, P, p0;
-  int n_a, n_b;
-  const int* lattice;     // [n_a][n_b]
-  const int* center;      // [V] ai * n_b + bi
-  const int* order;       // [V] or NULL
-  const float* yr_t;      // [T][V]
-  const float4* coef;     // [P][T]
-  const float* Ut;        // [P][T][K]
-  const double* logdet_R;
-  const double* logdet_XtX;
-  int* best;
+__device__ __forceinline__ void window_of(int c, int n_a, int n_b, int& a0, int& wa, int& b0, int& wb) {
+  const int ca = c / n_b, cb = c % n_b;
+  wa = min(WIN, n_a);
+  wb = min(WIN, n_b);
+  a0 = min(max(ca - WIN / 2, 0), n_a - wa);
+  b0 = min(max(cb - WIN / 2, 0), n_b - wb);
+}
+
+// one thread per lattice cell; cell c's voxels are sorted rows
+// [end[c-1], end[c]) (end[-1] = 0)
+__global__ void window_items_kernel(int ncell, const int* end, int n_a, int n_b, const int* lattice, int K,
+                                    int max_pairs, ffs_tc_item* items, int* n_items, int max_items, int2* tiles,
+                                    int* n_tiles, int max_tiles, int* overflow) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int s0 = c ? end[c - 1] : 0, n = end[c] - s0;
+  if (n <= 0) return;
+  int a0, wa, b0, wb;
+  window_of(c, n_a, n_b, a0, wa, b0, wb);
+  const int ntile = (n + WTILE - 1) / WTILE;
+  const int tt = atomicAdd(n_tiles, ntile);
+  for (int t = 0; t < ntile; ++t) {
+    if (tt + t >= max_tiles) {
+      atomicExch(overflow, 1);
+      break;
+    }
+    tiles[tt + t] = make_int2(s0 + t * WTILE, min(WTILE, n - t * WTILE));
+  }
+  for (int ra = 0; ra < wa; ++ra) {
+    int rb = 0;
+    while (rb < wb) {
+      const int p = lattice[(a0 + ra) * n_b + b0 + rb];
+      if (p < 0) {
+        ++rb;
+        continue;
+      }
+      // run of consecutive pair indices along the row
+      int np = 1;
+      while (rb + np < wb && np < max_pairs && lattice[(a0 + ra) * n_b + b0 + rb + np] == p + np) ++np;
+      const int at = atomicAdd(n_items, ntile);
+      for (int t = 0; t < ntile; ++t) {
+        if (at + t >= max_items) {
+          atomicExch(overflow, 1);
+          break;
+        }
+        ffs_tc_item it;
+        it.v0 = s0 + t * WTILE;
+        it.nv = min(WTILE, n - t * WTILE);
+        it.row_b = p * K;
+        it.np = np;
+        it.out0 = it.v0;
+        it.slot0 = ra * WIN + rb;
+        items[at + t] = it;
+      }
+      rb += np;
+    }
+  }
+}
+
+__global__ void clamp_count_kernel(int* n_items, int max_items, int* n_tiles, int max_tiles) {
+  if (*n_items > max_items) *n_items = max_items;
+  if (*n_tiles > max_tiles) *n_tiles = max_tiles;
+}
+
+struct CritArgs {
+  int n, T, K, n_a, n_b;
+  const int* lattice;       // [n_a][n_b]
+  const int* idx;           // [n] voxel of each sorted row
+  const int* center;        // [n] cell of each sorted row
+  const float* yr_st;       // [T][n] sorted rows, time-major
+  const float4* coef;       // [P][T]
+  const float* winproj;     // [n][25]
+  const float* dcf;         // [P] (logdet_R + logdet_XtX)[p] - that of (0, 0)
+  const uint8_t* ident;     // [P]
+  int p_id;
+  double c_p0;
+  int* best;                // outputs at idx[i]
   float* dbest;
   double* crit0;
   int* fallback;
+  int* best_cell;
 };
 
-template <int KMAX>
-__device__ void eval_row(const WinArgs& w, int v, const int* pr, int npr, float* rss_out, float& yy_out,
-                         bool want_yy) {
-  float vv[WIN], sb[WIN], st[WIN], acc[WIN][KMAX];
+constexpr int CRIT_TB = 16;  // steps per partial sum and sample prefetch
+
+// One CTA per tile of WTILE sorted rows that share a window centre, one thread
+// per row. Each window row's coefficients (c, -m, 1/D of its <= 5 pairs) are
+// staged in shared memory, then every thread runs the 5 recurrences over its
+// series with 16 samples in flight.
+__global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const int2* tiles, const int* n_tiles) {
+  extern __shared__ float4 tab[];  // [WIN][T]
+  if ((int)blockIdx.x >= *n_tiles) return;
+  const int2 tl = tiles[blockIdx.x];
+  const int i = tl.x + threadIdx.x;
+  const bool live = (int)threadIdx.x < tl.y;
+  const int c = w.center[tl.x];  // every row of the tile has this centre
+  int a0, wa, b0, wb;
+  window_of(c, w.n_a, w.n_b, a0, wa, b0, wb);
+  const int T = w.T, Tk = w.T - w.K;
+  const float* yc = w.yr_st + (live ? i : tl.x);
+  // y'y in the full grid's blocks (the identity chunk of the surface kernel)
+  float yy = 0.f;
+  for (int t0 = 0; t0 < T; t0 += CRIT_TB) {
+    float yb[CRIT_TB];
 #pragma unroll
-  for (int g = 0; g < WIN; ++g) {
-    vv[g] = sb[g] = st[g] = 0.f;
+    for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * w.n] : 0.f;
+    float yy_b = 0.f;
 #pragma unroll
-    for (int j = 0; j < KMAX; ++j) acc[g][j] = 0.f;
+    for (int k = 0; k < CRIT_TB; ++k) yy_b = fmaf(yb[k], yb[k], yy_b);
+    yy += yy_b;
   }
-  float yp = 0.f, yyb = 0.f, yyt = 0.f;
-  const int T = w.T, K = w.K;
-  for (int t0 = 0; t0 < T; t0 += 32) {
-    const int t1 = min(T, t0 + 32);
-    for (int t = t0; t < t1; ++t) {
-      const float y = w.yr_t[(size_t)t * w.V + v];
-      yyb = fmaf(y, y, yyb);
+  const float rss0 = yy;  // ||Q0'y_r||^2 of the residualised series is zero to rounding
+  const float den = rss0 + 1e-10f;
+
+  // best non-identity window pair
+  int best = -1, bcell = -1;
+  float bd = INFINITY;
+  bool has_ident = false;
+  for (int ra = 0; ra < wa; ++ra) {
+    int pr[WIN], col[WIN], np = 0;
 #pragma unroll
-      for (int g = 0; g < WIN; ++g) {
-        if (g < npr) {
-          const int p = pr[g];
-          const float4 q = w.coef[(size_t)p * T + t];
-          const float z = fmaf(-q.x, yp, y);
-          vv[g] = fmaf(-q.y, vv[g], z);
-          sb[g] = fmaf(vv[g] * q.z, vv[g], sb[g]);
-          const float* u = w.Ut + ((size_t)p * T + t) * K;
+    for (int rb = 0; rb < WIN; ++rb) {
+      const int p = rb < wb ? w.lattice[(a0 + ra) * w.n_b + b0 + rb] : -1;
+      if (p >= 0 && w.ident[p]) has_ident = true;
+      if (p >= 0 && !w.ident[p]) {
+        pr[np] = p;
+        col[np++] = rb;
+      }
+    }
+    if (np == 0) continue;  // uniform over the CTA
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < np * T; idx += blockDim.x) {
+      const int g = idx / T, t = idx % T;
+      int p = pr[0];
 #pragma unroll
-          for (int j = 0; j < KMAX; ++j)
-            if (j < K) acc[g][j] = fmaf(u[j], y, acc[g][j]);
+      for (int k = 1; k < WIN; ++k)
+        if (g == k) p = pr[k];
+      const float4 q = w.coef[(size_t)p * T + t];
+      tab[(size_t)g * T + t] = make_float4(q.x, -q.y, q.z, 0.f);
+    }
+    __syncthreads();
+    float vv[WIN], sb[WIN], st[WIN];
+#pragma unroll
+    for (int g = 0; g < WIN; ++g) vv[g] = sb[g] = st[g] = 0.f;
+    float yp = 0.f;
+    for (int t0 = 0; t0 < T; t0 += CRIT_TB) {
+      float yb[CRIT_TB];
+#pragma unroll
+      for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * w.n] : 0.f;
+#pragma unroll
+      for (int k = 0; k < CRIT_TB; ++k) {
+        const int t = t0 + k;
+        if (t < T) {
+          const float y = yb[k];
+#pragma unroll
+          for (int g = 0; g < WIN; ++g) {
+            if (g < np) {
+              const float4 q = tab[(size_t)g * T + t];
+              const float z = fmaf(-q.x, yp, y);
+              vv[g] = fmaf(q.y, vv[g], z);
+              sb[g] = fmaf(vv[g] * q.z, vv[g], sb[g]);
+            }
+          }
+          yp = y;
         }
       }
-      yp = y;
+#pragma unroll
+      for (int g = 0; g < WIN; ++g) {
+        st[g] += sb[g];
+        sb[g] = 0.f;
+      }
     }
 #pragma unroll
     for (int g = 0; g < WIN; ++g) {
-      st[g] += sb[g];
-      sb[g] = 0.f;
-    }
-    yyt += yyb;
-    yyb = 0.f;
-  }
-#pragma unroll
-  for (int g = 0; g < WIN; ++g) {
-    if (g < npr) {
-      float pj = 0.f;
-#pragma unroll
-      for (int j = 0; j < KMAX; ++j) pj = fmaf(acc[g][j], acc[g][j], pj);
-      rss_out[g] = fmaxf(st[g] - pj, 0.f);
+      if (g < np && live) {
+        const int p = pr[g];
+        const float rss = fmaxf(st[g] - w.winproj[(size_t)i * WSLOTS + ra * WIN + col[g]], 0.f);
+        const float d = w.dcf[p] + (float)Tk * log1pf((rss - rss0) / den);
+        if (d < bd || (d == bd && p < best) || best < 0) {
+          bd = d;
+          best = p;
+          bcell = (a0 + ra) * w.n_b + b0 + col[g];
+        }
+      }
     }
   }
-  if (want_yy) yy_out = yyt;
+  if (!live) return;
+  // The identity pairs (d = 0) take part when the window holds one of them,
+  // and then a win by them is final. A window without them whose best is not
+  // below 0 goes to the full grid (the identity pairs outside it are at least
+  // as good); otherwise the edge test decides.
+  int fb = 0;
+  if (has_ident && (bd > 0.f || (bd == 0.f && w.p_id < best) || best < 0)) {
+    best = w.p_id;
+    bd = 0.f;
+    bcell = -1;
+  } else if (best < 0 || bd >= 0.f) {
+    fb = 1;
+    if (best < 0) {
+      best = w.p_id;
+      bd = 0.f;
+    }
+  } else {
+    const int ba = bcell / w.n_b, bb = bcell % w.n_b;
+    for (int da = -1; da <= 1 && !fb; ++da)
+      for (int db = -1; db <= 1; ++db) {
+        const int na = ba + da, nb = bb + db;
+        if ((da == 0 && db == 0) || na < 0 || nb < 0 || na >= w.n_a || nb >= w.n_b) continue;
+        const bool inside = na >= a0 && na < a0 + wa && nb >= b0 && nb < b0 + wb;
+        if (!inside && w.lattice[na * w.n_b + nb] >= 0) {
+          fb = 1;
+          break;
+        }
+      }
+  }
+  const int v = w.idx[i];
+  w.best[v] = best;
+  w.dbest[v] = bd;
+  w.crit0[v] = w.c_p0 + (double)Tk * log((double)rss0 + 1e-10);
+  w.fallback[v] = fb;
+  w.best_cell[v] = bcell;
 }
 
-template <int KMAX>
-__global__ void __launch_bounds__(128) window_kernel(WinArgs w) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= w.V) return;
-  const int v = w.order ? w.order[i] : i;
-  const int c = w.center[v];
-  const int ca = c / w.n_b, cb = c % w.n_b;
-  const int wa = min(WIN, w.n_a), wb = min(WIN, w.n_b);
-  const int a0 = min(max(ca - WIN / 2, 0), w.n_a - wa);
-  const int b0 = min(max(cb - WIN / 2, 0), w.n_b - wb);
-  const int Tk = w.T - w.K;
-  const double c_p0 = w.logdet_R[w.p0] + w.logdet_XtX[w.p0];
-
-  // reference pair (0, 0): y'y - ||Q0'y||^2
-  float rss[WIN], yy = 0.f;
-  int pr[WIN];
-  pr[0] = w.p0;
-  eval_row<KMAX>(w, v, pr, 1, rss, yy, true);
-  const float rss0 = rss[0];
-  const float den = rss0 + 1e-10f;
-
-  int best = w.p0, ba = -1, bb = -1;
-  float bl = INFINITY;
-  for (int ra = 0; ra < wa; ++ra) {
-    int npr = 0, col[WIN];
-    for (int rb = 0; rb < wb; ++rb) {
-      const int p = w.lattice[(a0 + ra) * w.n_b + b0 + rb];
-      if (p >= 0) {
-        col[npr] = b0 + rb;
-        pr[npr++] = p;
-      }
-    }
-    if (npr == 0) continue;
-    eval_row<KMAX>(w, v, pr, npr, rss, yy, false);
-    for (int g = 0; g < npr; ++g) {  // lattice order = pair order within the window
-      const int p = pr[g];
-      const float dc = (float)((w.logdet_R[p] + w.logdet_XtX[p]) - c_p0);
-      const float d = dc + (float)Tk * log1pf((rss[g] - rss0) / den);
-      if (d < bl) {
-        bl = d;
-        best = p;
-        ba = a0 + ra;
-        bb = col[g];
-      }
-    }
+// fp16 operand rows and exponents in the order idx: a warp per row, 16-byte words
+__global__ void gather_rows_kernel(int n, int ld_y, const int* idx, const uint4* hi, const uint4* lo, const int* yexp,
+                                   uint4* out_hi, uint4* out_lo, int* out_exp) {
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const int v = idx[i];
+  const int nw = ld_y / 8;  // 8 fp16 per 16-byte word
+  for (int k = lane; k < nw; k += 32) {
+    out_hi[(size_t)i * nw + k] = hi[(size_t)v * nw + k];
+    out_lo[(size_t)i * nw + k] = lo[(size_t)v * nw + k];
   }
-  // edge test: a valid lattice neighbour of the best pair outside the window
-  int fb = (ba < 0) ? 1 : 0;
-  for (int da = -1; da <= 1 && !fb; ++da)
-    for (int db = -1; db <= 1; ++db) {
-      const int na = ba + da, nb = bb + db;
-      if ((da == 0 && db == 0) || na < 0 || nb < 0 || na >= w.n_a || nb >= w.n_b) continue;
-      const bool inside = na >= a0 && na < a0 + wa && nb >= b0 && nb < b0 + wb;
-      if (!inside && w.lattice[na * w.n_b + nb] >= 0) {
-        fb = 1;
-        break;
-      }
-    }
-  w.best[v] = best;
-  w.dbest[v] = bl;
-  w.crit0[v] = c_p0 + (double)Tk * log((double)rss0 + 1e-10);
-  w.fallback[v] = fb;
+  if (lane == 0) out_exp[i] = yexp[v];
+}
+
+// out_t[t][i] = rows[idx[i]][t]: 32 x 32 tiles through shared memory
+__global__ void gather_transpose_kernel(int n, int T, const int* idx, const float* rows, float* out_t) {
+  __shared__ float tile[32][33];
+  const int i0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + r, t = t0 + tx;
+    tile[r][tx] = (i < n && t < T) ? rows[(size_t)idx[i] * T + t] : 0.f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int t = t0 + r, i = i0 + tx;
+    if (t < T && i < n) out_t[(size_t)t * n + i] = tile[tx][r];
+  }
 }
 
 // nearest lattice point of each proposal: centre index ai * n_b + bi
@@ -168,45 +298,68 @@ __global__ void center_kernel(int V, const float* prop, const float* a_axis, int
   center[v] = ia * n_b + ib;
 }
 
-// U [P][K][T] -> Ut [P][T][K]
-__global__ void transpose_u_kernel(int P, int K, int T, const float* U, float* Ut) {
-  const size_t n = (size_t)P * K * T;
-  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
-    const size_t p = idx / ((size_t)K * T), r = idx % ((size_t)K * T);
-    const int j = (int)(r / T), t = (int)(r % T);
-    Ut[(p * T + t) * K + j] = U[idx];
-  }
-}
-
 }  // namespace
 }  // namespace ffsk
 
 using namespace ffsk;
 
-extern "C" int ffs_reml_window(int V, int T, int K, int P, int p0, int n_a, int n_b, const int* lattice,
-                               const int* center, const int* order, const float* yr_t, const float* coef,
-                               const float* Ut, const double* logdet_R, const double* logdet_XtX, int* best,
-                               float* dbest, double* crit0, int* fallback, void* stream) {
+extern "C" int ffs_reml_gather(int n, int T, int ld_y, const int* idx, const uint16_t* yr_hi, const uint16_t* yr_lo,
+                               const int* yexp, const float* yr_rows, uint16_t* out_hi, uint16_t* out_lo,
+                               int* out_exp, float* out_t, void* stream) {
   clear_error();
-  FFS_REQUIRE(V > 0 && T > 0 && K > 0 && P > 0 && n_a > 0 && n_b > 0, "ffs_reml_window: bad sizes");
-  FFS_REQUIRE(p0 >= 0 && p0 < P, "ffs_reml_window: p0 out of range");
-  FFS_REQUIRE(lattice && center && yr_t && coef && Ut && logdet_R && logdet_XtX && best && dbest && crit0 &&
-                  fallback,
-              "ffs_reml_window: null buffer");
-  WinArgs w{V, T, K, P, p0, n_a, n_b, lattice, center, order, yr_t, reinterpret_cast<const float4*>(coef), Ut,
-            logdet_R, logdet_XtX, best, dbest, crit0, fallback};
+  FFS_REQUIRE(n > 0 && T > 0 && ld_y >= T && ld_y % 8 == 0, "ffs_reml_gather: bad sizes");
+  FFS_REQUIRE(idx && yr_hi && yr_lo && yexp && yr_rows && out_hi && out_lo && out_exp && out_t,
+              "ffs_reml_gather: null buffer");
+  for (const void* ptr : {(const void*)yr_hi, (const void*)yr_lo, (const void*)out_hi, (const void*)out_lo})
+    FFS_REQUIRE(((uintptr_t)ptr & 15) == 0, "ffs_reml_gather: fp16 rows must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
-  if (K <= 8) {
-    window_kernel<8><<<ceil_div(V, 128), 128, 0, st>>>(w);
-  } else if (K <= 24) {
-    window_kernel<24><<<ceil_div(V, 128), 128, 0, st>>>(w);
-  } else if (K <= 32) {
-    window_kernel<32><<<ceil_div(V, 128), 128, 0, st>>>(w);
-  } else {
-    set_error("ffs_reml_window: K=%d above the 32 columns the windowed refine supports", K);
-    return FFS_ERR_UNSUPPORTED;
-  }
-  return check_launch("window_kernel");
+  gather_rows_kernel<<<ceil_div(n, 8), 256, 0, st>>>(n, ld_y, idx, reinterpret_cast<const uint4*>(yr_hi),
+                                                      reinterpret_cast<const uint4*>(yr_lo), yexp,
+                                                      reinterpret_cast<uint4*>(out_hi),
+                                                      reinterpret_cast<uint4*>(out_lo), out_exp);
+  FFS_REQUIRE(ceil_div(T, 32) <= 65535, "ffs_reml_gather: T=%d too long", T);
+  gather_transpose_kernel<<<dim3(ceil_div(n, 32), ceil_div(T, 32)), dim3(32, 8), 0, st>>>(n, T, idx, yr_rows, out_t);
+  return check_launch("gather kernels");
+}
+
+extern "C" int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, const int* lattice, int K,
+                                     int max_pairs, ffs_tc_item* items, int* n_items, int max_items, int* tiles,
+                                     int* n_tiles, int max_tiles, int* overflow, void* stream) {
+  clear_error();
+  FFS_REQUIRE(ncell > 0 && n_a > 0 && n_b > 0 && K > 0 && max_pairs > 0 && max_items > 0 && max_tiles > 0,
+              "ffs_reml_window_items: bad sizes");
+  FFS_REQUIRE(cell_end && lattice && items && n_items && tiles && n_tiles && overflow,
+              "ffs_reml_window_items: null buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  FFS_CUDA(cudaMemsetAsync(n_items, 0, sizeof(int), st));
+  FFS_CUDA(cudaMemsetAsync(n_tiles, 0, sizeof(int), st));
+  FFS_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), st));
+  window_items_kernel<<<ceil_div(ncell, 128), 128, 0, st>>>(ncell, cell_end, n_a, n_b, lattice, K, max_pairs, items,
+                                                             n_items, max_items, reinterpret_cast<int2*>(tiles),
+                                                             n_tiles, max_tiles, overflow);
+  clamp_count_kernel<<<1, 1, 0, st>>>(n_items, max_items, n_tiles, max_tiles);
+  return check_launch("window_items_kernel");
+}
+
+extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx,
+                               const int* center, const int* tiles, const int* n_tiles, int max_tiles,
+                               const float* yr_st, const float* coef, const float* winproj, const float* dcf,
+                               const unsigned char* ident, int p_id, double c_p0, int* best, float* dbest,
+                               double* crit0, int* fallback, int* best_cell, void* stream) {
+  clear_error();
+  FFS_REQUIRE(n > 0 && T > K && K > 0 && n_a > 0 && n_b > 0 && p_id >= 0 && max_tiles > 0,
+              "ffs_reml_window: bad sizes");
+  FFS_REQUIRE(lattice && idx && center && tiles && n_tiles && yr_st && coef && winproj && dcf && ident && best &&
+                  dbest && crit0 && fallback && best_cell,
+              "ffs_reml_window: null buffer");
+  const size_t smem = sizeof(float4) * WIN * (size_t)T;
+  FFS_REQUIRE(smem <= 200 * 1024, "ffs_reml_window: T=%d too long", T);
+  FFS_CUDA(cudaFuncSetAttribute(window_crit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, yr_st, reinterpret_cast<const float4*>(coef), winproj, dcf,
+             ident, p_id, c_p0, best, dbest, crit0, fallback, best_cell};
+  window_crit_kernel<<<max_tiles, WTILE, smem, (cudaStream_t)stream>>>(w, reinterpret_cast<const int2*>(tiles),
+                                                                        n_tiles);
+  return check_launch("window_crit_kernel");
 }
 
 extern "C" int ffs_reml_centers(int V, const float* prop, const float* a_axis, int n_a, const float* b_axis, int n_b,
@@ -215,11 +368,4 @@ extern "C" int ffs_reml_centers(int V, const float* prop, const float* a_axis, i
   FFS_REQUIRE(V > 0 && prop && a_axis && b_axis && center && n_a > 0 && n_b > 0, "ffs_reml_centers: bad arguments");
   center_kernel<<<ceil_div(V, 256), 256, 0, (cudaStream_t)stream>>>(V, prop, a_axis, n_a, b_axis, n_b, center);
   return check_launch("center_kernel");
-}
-
-extern "C" int ffs_transpose_u(int P, int K, int T, const float* U, float* Ut, void* stream) {
-  clear_error();
-  FFS_REQUIRE(P > 0 && K > 0 && T > 0 && U && Ut, "ffs_transpose_u: bad arguments");
-  transpose_u_kernel<<<1024, 256, 0, (cudaStream_t)stream>>>(P, K, T, U, Ut);
-  return check_launch("transpose_u_kernel");
 }

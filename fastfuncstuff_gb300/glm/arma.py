@@ -236,6 +236,7 @@ def fit_glm_arma11(
     projector: str = "tc",
     return_device: bool = False,
     proposal=None,
+    proposal_recenter: int = 0,
 ) -> ARMA11Results:
     """Fit a GLM with ARMA(1,1) REML prewhitening (fastfuncstuff/glm/arma.py:3650).
 
@@ -243,9 +244,12 @@ def fit_glm_arma11(
     ``use_qr``, ``use_grid_batching``, ``debug_memory``, ``legacy_contrasts`` and
     ``autocorr_cache`` tune the reference's CPU/GPU memory plan and have no
     counterpart here (the factors are built on the GPU in FP64, with the QR
-    fallback applied per pair when the Cholesky of X_w'X_w fails). Two extra
-    keywords: ``projector`` ("tc" tensor-core GEMM, "simt" CUDA cores) and
-    ``return_device`` (keep result tensors on the GPU).
+    fallback applied per pair when the Cholesky of X_w'X_w fails). Extra
+    keywords: ``projector`` ("tc" tensor-core GEMM, "simt" CUDA cores),
+    ``return_device`` (keep result tensors on the GPU), ``proposal`` (a trained
+    ``learned.ArmaProposal``: search each voxel's 5 x 5 window around its
+    proposal, the full grid for window-edge voxels) and ``proposal_recenter``
+    (re-centred window rounds before that fallback).
     """
     if want_ols or want_ols_residuals or want_ols_predicted or ols_write_callback is not None:
         _unsupported("the OLS side fit (want_ols)")
@@ -326,18 +330,17 @@ def fit_glm_arma11(
     chunks = {k: [] for k in ("best", "crit", "surf", "betas", "tstats", "sigma2", "fstats", "r2", "lam",
                               "cb", "ct", "resid", "resid_w", "pred", "lb")}
     proj = projector if (projector != "tc" or factors.U_hi is not None) else "simt"
-    Ut = None
     if proposal is not None and best_all is None:
         from . import learned
 
-        Ut = learned.transpose_u(factors)
         layout_l = layout
         fallbacks = []
     for v0 in range(0, V, bs):
         v1 = min(V, v0 + bs)
         Yb = Y[v0:v1].to(device=device, dtype=torch.float32, non_blocking=True)
         if best_all is None and proposal is not None:
-            lo = learned.learned_search(Yb, factors, proposal, layout_l, do_scale=not use_double, Ut=Ut)
+            lo = learned.learned_search(Yb, factors, proposal, layout_l, do_scale=not use_double,
+                                        recenter=proposal_recenter)
             best, scale = lo.best, lo.scale
             chunks["best"].append(best)
             chunks["crit"].append(lo.best_crit)

@@ -224,23 +224,46 @@ class PrepOut:
     yexp: torch.Tensor | None
 
 
-def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core: bool = True) -> PrepOut:
-    """Per-voxel scaling and residualisation (and the fp16 split for the GEMM)."""
+def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core: bool = True,
+         idx: torch.Tensor | None = None, want_yr_t: bool = True, layout: RunLayout | None = None,
+         scale: torch.Tensor | None = None, want_rows: bool = False) -> PrepOut:
+    """Per-voxel scaling and residualisation (and the fp16 split for the GEMM).
+
+    ``idx`` (int32, device) processes the rows Y[idx] in that order (every
+    output but ``scale`` is indexed by position in ``idx``; ``scale`` by the
+    row of Y, into ``scale`` when given). With ``layout`` the lag 1..8
+    autocorrelation features of the residualised rows are returned in
+    ``PrepOut.feats``; ``want_rows`` adds the residualised rows voxel-major
+    (``PrepOut.rows``).
+    """
     lib = _lib.load()
     dev = Y.device
     V, T = Y.shape
+    n = V if idx is None else idx.numel()
     K, ld = f.K, f.ld
     Y = Y.to(dtype=torch.float32).contiguous()
-    scale = torch.empty(V, dtype=torch.float32, device=dev)
-    yr_t = torch.empty(T, V, dtype=torch.float32, device=dev)
-    yr_hi = torch.empty(V, ld, dtype=torch.int16, device=dev) if tensor_core else None
-    yr_lo = torch.empty(V, ld, dtype=torch.int16, device=dev) if tensor_core else None
-    yexp = torch.empty(V, dtype=torch.int32, device=dev) if tensor_core else None
+    if scale is None:
+        scale = torch.empty(V, dtype=torch.float32, device=dev)
+    yr_t = torch.empty(T, n, dtype=torch.float32, device=dev) if want_yr_t else None
+    yr_hi = torch.empty(n, ld, dtype=torch.int16, device=dev) if tensor_core else None
+    yr_lo = torch.empty(n, ld, dtype=torch.int16, device=dev) if tensor_core else None
+    yexp = torch.empty(n, dtype=torch.int32, device=dev) if tensor_core else None
+    feats = rs = None
+    if layout is not None:
+        feats = torch.empty(n, 9, dtype=torch.float32, device=dev)
+        rs = torch.from_numpy(layout.run_start).to(dev)
+    rows = torch.empty(n, T, dtype=torch.float32, device=dev) if want_rows else None
     q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T])
-    pa = _lib.PrepArgs(V=V, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=int(f.center), ld_y=ld,
-                       scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp))
+    pa = _lib.PrepArgs(V=n, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=int(f.center), ld_y=ld,
+                       scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp),
+                       idx=_p(idx), feats=_p(feats), n_runs=0 if layout is None else layout.n_runs,
+                       run_start=_p(rs), yr_rows=_p(rows))
     _run("ffs_reml_prep", lib.ffs_reml_prep, C.byref(pa), _stream())
-    return PrepOut(scale, yr_t, yr_hi, yr_lo, yexp)
+    out = PrepOut(scale, yr_t, yr_hi, yr_lo, yexp)
+    out.feats = feats
+    out.rows = rows
+    out._keep = rs
+    return out
 
 
 def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projector: str = "tc",

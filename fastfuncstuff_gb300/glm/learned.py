@@ -29,7 +29,7 @@ import torch
 
 from .. import _lib
 from . import engine
-from .grid import RemlGrid, RunLayout
+from .grid import RemlGrid, RunLayout, lambda_is_zero
 
 N_IN = 9
 
@@ -96,14 +96,10 @@ def simulate(X: torch.Tensor, layout: RunLayout, a: torch.Tensor, b: torch.Tenso
     return Y
 
 
-def features(yr_t: torch.Tensor, layout: RunLayout) -> torch.Tensor:
-    T, V = yr_t.shape
-    dev = yr_t.device
-    feats = torch.empty(V, N_IN, device=dev, dtype=torch.float32)
-    rs = torch.from_numpy(layout.run_start).to(dev)
-    engine._run("ffs_reml_features", _lib.load().ffs_reml_features, V, T, layout.n_runs, _p(rs), _p(yr_t),
-                _p(feats), _st())
-    return feats
+def features(Y: torch.Tensor, factors: engine.GridFactors, layout: RunLayout, *, do_scale: bool = True) -> torch.Tensor:
+    """(V, 9) proposal inputs of the voxels Y (V, T): lag 1..8 autocorrelations
+    of each scaled, residualised series within runs, and T/1000 (one prep pass)."""
+    return engine.prep(Y, factors, do_scale=do_scale, tensor_core=False, want_yr_t=False, layout=layout).feats
 
 
 def mlp_grad(params, x, y, idx, n_total, grad, loss) -> None:
@@ -119,21 +115,28 @@ def adam(params, grad, m, v, lr, step, b1=0.9, b2=0.999, eps=1e-8) -> None:
 
 def training_set(X: torch.Tensor, factors: engine.GridFactors, layout: RunLayout, n: int, seed: int,
                  chunk: int = 250_000):
-    """Simulated voxels, their features and full-grid exhaustive labels (a*, b*)."""
+    """Simulated voxels, their features and full-grid exhaustive labels (a*, b*).
+
+    A voxel whose argmin is an identity pair (lambda == 0: every such pair has
+    the same criterion, so the whole line a = -b is its argmin) is labelled
+    with (0, 0), the line's middle, rather than with the first identity pair
+    the tie-break reports.
+    """
     dev = X.device
     g = factors.grid
     a_t = torch.from_numpy(g.a).to(dev)
     b_t = torch.from_numpy(g.b).to(dev)
+    ident = torch.from_numpy(lambda_is_zero(g.a, g.b)).to(dev)
     gen = torch.Generator(device="cpu").manual_seed(seed)
     feats, labels = [], []
     for c0 in range(0, n, chunk):
         m = min(chunk, n - c0)
         idx = torch.randint(0, g.P, (m,), generator=gen).to(dev)
         Y = simulate(X, layout, a_t[idx], b_t[idx], seed * 7919 + c0)
-        so = engine.search(Y, factors, hierarchical=False, projector="tc" if factors.U_hi is not None else "simt",
-                           keep_yr=True)
-        feats.append(features(so.yr_t, layout))
+        so = engine.search(Y, factors, hierarchical=False, projector="tc" if factors.U_hi is not None else "simt")
+        feats.append(features(Y, factors, layout))
         best = so.best.long()
+        best = torch.where(ident[best], torch.full_like(best, g.p0), best)
         labels.append(torch.stack([a_t[best], b_t[best]], 1))
     return torch.cat(feats), torch.cat(labels)
 
@@ -186,52 +189,136 @@ class LearnedOut:
     scale: torch.Tensor
     fallback: torch.Tensor  # [V] int32, 1 where the full grid decided
     proposal: torch.Tensor  # [V, 2]
+    stats: dict = field(default_factory=dict)
+
+
+WIN_SLOTS = 25
+
+
+def _window_consts(f: engine.GridFactors):
+    """Per-factor constants of the windowed refine (computed once per factors)."""
+    c = getattr(f, "_window_consts", None)
+    if c is None:
+        g = f.grid
+        dev = f.coef.device
+        c_p0 = float((f.logdet_R[g.p0] + f.logdet_XtX[g.p0]).item())
+        dcf = ((f.logdet_R + f.logdet_XtX) - c_p0).float().contiguous()
+        ident_np = lambda_is_zero(g.a, g.b)
+        ident = torch.from_numpy(ident_np.astype(np.uint8)).to(dev)
+        p_id = int(np.nonzero(ident_np)[0][0])
+        a_ax = torch.from_numpy(g.a_axis).to(dev)
+        b_ax = torch.from_numpy(g.b_axis).to(dev)
+        c = dict(c_p0=c_p0, dcf=dcf, ident=ident, p_id=p_id, a_ax=a_ax, b_ax=b_ax)
+        f._window_consts = c
+    return c
+
+
+def _window_round(pre, f, src, cen, out, *, flag):
+    """Evaluate the 5 x 5 windows centred at cen (lattice cells) of the voxels
+    src (None: all voxels, in order), writing out[...] at the voxel ids; pre is
+    the prep of every voxel (fp16 operands and voxel-major rows)."""
+    lib = _lib.load()
+    dev = pre.scale.device
+    g = f.grid
+    K, P, T, ld = f.K, f.P, f.T, f.ld
+    st = _st()
+    n_a, n_b = len(g.a_axis), len(g.b_axis)
+    ncell = n_a * n_b
+    n = cen.numel()
+    c = _window_consts(f)
+    # voxels sorted by window centre
+    order = torch.empty(n, dtype=torch.int32, device=dev)
+    cell_end = torch.empty(ncell + 1, dtype=torch.int32, device=dev)
+    engine._run("ffs_reml_group", lib.ffs_reml_group, n, ncell, _p(cen), _p(cell_end), _p(order), st)
+    ol = order.long()
+    idx = order if src is None else src[ol].to(torch.int32)
+    cen_s = cen[ol].contiguous()
+    hi = torch.empty(n, ld, dtype=torch.int16, device=dev)
+    lo = torch.empty(n, ld, dtype=torch.int16, device=dev)
+    yexp = torch.empty(n, dtype=torch.int32, device=dev)
+    yr_st = torch.empty(T, n, dtype=torch.float32, device=dev)
+    engine._run("ffs_reml_gather", lib.ffs_reml_gather, n, T, ld, _p(idx), _p(pre.yr_hi), _p(pre.yr_lo),
+                _p(pre.yexp), _p(pre.rows), _p(hi), _p(lo), _p(yexp), _p(yr_st), st)
+    # projections of every window pair on the tensor cores
+    max_pairs = max(1, min(5, 256 // K))
+    max_tiles = (n + 127) // 128 + min(n, ncell)
+    max_items = WIN_SLOTS * max_tiles
+    items = torch.empty(max_items, 6, dtype=torch.int32, device=dev)
+    tiles = torch.empty(max_tiles, 2, dtype=torch.int32, device=dev)
+    counts = torch.zeros(3, dtype=torch.int32, device=dev)  # n_items, overflow, n_tiles
+    engine._run("ffs_reml_window_items", lib.ffs_reml_window_items, ncell, _p(cell_end), n_a, n_b, _p(f.lattice),
+                K, max_pairs, _p(items), _p(counts), max_items, _p(tiles), counts.data_ptr() + 8, max_tiles,
+                counts.data_ptr() + 4, st)
+    winproj = torch.empty(n, WIN_SLOTS, dtype=torch.float32, device=dev)
+    ja = _lib.ProjectArgs(V=n, T=T, K=K, P=P, ld_y=ld, ld_u=ld, yr_hi=_p(hi), yr_lo=_p(lo),
+                          u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yexp=_p(yexp), uexp=_p(f.uexp), yr_t=None, U=None,
+                          proj=_p(winproj), flag=_p(flag))
+    engine._run("ffs_reml_project_tc_list", lib.ffs_reml_project_tc_list, C.byref(ja), _p(items), _p(counts),
+                max_items, max_pairs, WIN_SLOTS, st)
+    engine._run("ffs_reml_window", lib.ffs_reml_window, n, T, K, n_a, n_b, _p(f.lattice), _p(idx), _p(cen_s),
+                _p(tiles), counts.data_ptr() + 8, max_tiles, _p(yr_st), _p(f.coef), _p(winproj), _p(c["dcf"]), _p(c["ident"]), c["p_id"], c["c_p0"],
+                _p(out["best"]), _p(out["dbest"]), _p(out["crit0"]), _p(out["fb"]), _p(out["cell"]), st)
+    return counts
 
 
 def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
-                   do_scale: bool = True, Ut: torch.Tensor | None = None) -> LearnedOut:
-    """Learned-seeded REML search: 5 x 5 window around each proposal, full grid on edge hits."""
+                   do_scale: bool = True, recenter: int = 0) -> LearnedOut:
+    """Learned-seeded REML search: the 5 x 5 window around each proposal, the
+    full grid for voxels whose best pair sits on the window edge (or whose
+    window, holding no identity pair, has nothing below the identity pairs'
+    criterion).
+
+    ``recenter`` > 0 first re-evaluates such voxels that many times with the
+    window centred on their best pair; the full grid then takes those still on
+    an edge.
+    """
     lib = _lib.load()
     dev = Y.device
     V, T = Y.shape
-    g = factors.grid
-    K, P = factors.K, factors.P
+    f = factors
+    if f.U_hi is None:
+        raise ValueError("the learned search needs the tensor-core operands of the factors")
+    if T % 4:
+        raise NotImplementedError("the learned search needs T % 4 == 0 (the tiled prep)")
+    g = f.grid
     st = _st()
     Y = Y.float().contiguous()
-    pre = engine.prep(Y, factors, do_scale=do_scale, tensor_core=False)
-    feats = features(pre.yr_t, layout)
-    prop = proposal.forward(feats)
-    a_ax = torch.from_numpy(g.a_axis).to(dev)
-    b_ax = torch.from_numpy(g.b_axis).to(dev)
+    c = _window_consts(f)
+    p1 = engine.prep(Y, f, do_scale=do_scale, tensor_core=True, want_yr_t=False, layout=layout, want_rows=True)
+    scale = p1.scale
+    prop = proposal.forward(p1.feats)
     center = torch.empty(V, dtype=torch.int32, device=dev)
-    engine._run("ffs_reml_centers", lib.ffs_reml_centers, V, _p(prop), _p(a_ax), len(g.a_axis), _p(b_ax),
+    engine._run("ffs_reml_centers", lib.ffs_reml_centers, V, _p(prop), _p(c["a_ax"]), len(g.a_axis), _p(c["b_ax"]),
                 len(g.b_axis), _p(center), st)
-    ncell = len(g.a_axis) * len(g.b_axis)
-    order = torch.empty(V, dtype=torch.int32, device=dev)
-    work = torch.empty(ncell + 1, dtype=torch.int32, device=dev)
-    engine._run("ffs_reml_group", lib.ffs_reml_group, V, ncell, _p(center), _p(work), _p(order), st)
-    if Ut is None:
-        Ut = transpose_u(factors)
-    best = torch.empty(V, dtype=torch.int32, device=dev)
-    dbest = torch.empty(V, dtype=torch.float32, device=dev)
-    crit0 = torch.empty(V, dtype=torch.float64, device=dev)
-    fb = torch.empty(V, dtype=torch.int32, device=dev)
-    engine._run("ffs_reml_window", lib.ffs_reml_window, V, T, K, P, g.p0, len(g.a_axis), len(g.b_axis),
-                _p(factors.lattice), _p(center), _p(order), _p(pre.yr_t), _p(factors.coef), _p(Ut),
-                _p(factors.logdet_R), _p(factors.logdet_XtX), _p(best), _p(dbest), _p(crit0), _p(fb), st)
-    best_crit = (crit0 + dbest.double()).float()
-    # full grid for the voxels whose best pair touched the window edge
+    out = dict(best=torch.empty(V, dtype=torch.int32, device=dev), dbest=torch.empty(V, dtype=torch.float32, device=dev),
+               crit0=torch.empty(V, dtype=torch.float64, device=dev), fb=torch.zeros(V, dtype=torch.int32, device=dev),
+               cell=torch.empty(V, dtype=torch.int32, device=dev))
+    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    counts = [_window_round(p1, f, None, center, out, flag=flag)]
+    stats = {"edge_first": None}
+    for r in range(recenter):
+        if r == 0:
+            stats["edge_first"] = float(out["fb"].float().mean().item())
+        # re-centre on the window's best pair (voxels whose window held no
+        # candidate keep their fallback)
+        sel = torch.nonzero((out["fb"] != 0) & (out["cell"] >= 0), as_tuple=True)[0].to(torch.int32)
+        if sel.numel() == 0:
+            break
+        counts.append(_window_round(p1, f, sel, out["cell"][sel.long()].contiguous(), out, flag=flag))
+    best_crit = (out["crit0"] + out["dbest"].double()).float()
+    best = out["best"]
+    fb = out["fb"]
+    # the full grid for the voxels still on a window edge
     sel = torch.nonzero(fb, as_tuple=True)[0]
+    if stats["edge_first"] is None:
+        stats["edge_first"] = sel.numel() / V
+    stats["fallback"] = sel.numel() / V
     if sel.numel():
-        so = engine.search(Y.index_select(0, sel), factors, hierarchical=False,
-                           projector="tc" if factors.U_hi is not None else "simt", do_scale=do_scale)
+        so = engine.search(Y.index_select(0, sel), f, hierarchical=False, projector="tc", do_scale=do_scale)
         best.index_copy_(0, sel, so.best)
         best_crit.index_copy_(0, sel, so.best_crit)
-    return LearnedOut(best=best, best_crit=best_crit, scale=pre.scale, fallback=fb, proposal=prop)
-
-
-def transpose_u(factors: engine.GridFactors) -> torch.Tensor:
-    P, K, T = factors.U.shape
-    Ut = torch.empty(P, T, K, device=factors.U.device, dtype=torch.float32)
-    engine._run("ffs_transpose_u", _lib.load().ffs_transpose_u, P, K, T, _p(factors.U), _p(Ut), _st())
-    return Ut
+    if int(flag.item()) != 0:
+        raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {int(flag.item())})")
+    if any(int(cn[1].item()) for cn in counts):
+        raise RuntimeError("ffs_reml_window_items: work list overflow")
+    return LearnedOut(best=best, best_crit=best_crit, scale=scale, fallback=fb, proposal=prop, stats=stats)

@@ -160,6 +160,18 @@ typedef struct {
   uint16_t* yr_hi;      /* [V][ld_y] fp16 bits or NULL                            */
   uint16_t* yr_lo;      /* [V][ld_y] fp16 bits or NULL                            */
   int* yexp;            /* [V] power-of-two scale of yr_hi/yr_lo (with yr_hi)     */
+  /* Extensions for the learned-seeded refine (no reference counterpart):
+   * idx   NULL, or [V] rows of Y to process: output row i is Y row idx[i]
+   *       (scale is still written at idx[i]; every other output at i);
+   * feats NULL, or [V][9]: lag 1..8 autocorrelations of each residualised row
+   *       within runs (sum y_t y_t+k / sum y_t^2, 0 for a zero row) and T/1000,
+   *       with run boundaries run_start[0..n_runs] (run_start[n_runs] = T).
+   * yr_t may be NULL when only feats are wanted. */
+  const int* idx;
+  float* feats;
+  int n_runs;
+  const int* run_start;
+  float* yr_rows;       /* NULL, or [V][T] the residualised rows, voxel-major    */
 } ffs_prep_args;
 
 int ffs_reml_prep(const ffs_prep_args* a, void* stream);
@@ -188,6 +200,24 @@ typedef struct {
 
 int ffs_reml_project_tc(const ffs_project_args* a, void* stream);
 int ffs_reml_project_simt(const ffs_project_args* a, void* stream);
+
+/* Work-list form of ffs_reml_project_tc (no reference counterpart: the
+ * learned-seeded refine evaluates each voxel's 5 x 5 window only). Item i
+ * projects the 128 operand rows v0 .. v0+127 (nv of them real) onto the np
+ * consecutive pairs whose U rows start at row_b (= first pair * K) and writes
+ *   proj[(out0 + r) * ld_out + slot0 + j] = ||U_{p+j}' y_{v0+r}||^2
+ * The item count is read on the device from *n_items (<= max_items); every
+ * item has np <= max_pairs and max_pairs * K <= 256. a->V is the number of
+ * operand rows, a->proj the output. */
+typedef struct {
+  int v0, nv;     /* first operand row, real rows (<= 128)                       */
+  int row_b, np;  /* first U row, pairs                                          */
+  int out0;       /* output row of operand row v0                                */
+  int slot0;      /* output column of the first pair                             */
+} ffs_tc_item;
+
+int ffs_reml_project_tc_list(const ffs_project_args* a, const ffs_tc_item* items, const int* n_items,
+                             int max_items, int max_pairs, int ld_out, void* stream);
 
 /* --------------------------------------------------------------------- surface
  * The REML criterion of every voxel at every pair
@@ -297,8 +327,9 @@ int ffs_reml_group(int V, int P, const int* best, int* work, int* order, void* s
  * No counterpart in the reference: this build's learned seed for the grid
  * search. A 9 -> 64 -> 64 -> 2 GELU MLP maps each voxel's OLS-residual
  * autocorrelations (lags 1-8) and T/1000 to a proposed (a, b); only the 5 x 5
- * lattice window around it is evaluated, and voxels whose best pair touches a
- * valid lattice neighbour outside the window fall back to the full grid.
+ * lattice window around it is evaluated, and voxels whose best pair sits on
+ * the window edge (a valid lattice neighbour outside the window) fall back to
+ * the full grid.
  * Parameters are one float32 vector of ffs_mlp_param_count() entries:
  * W1[64][9], b1[64], W2[64][64], b2[64], W3[2][64], b3[2].
  */
@@ -310,10 +341,7 @@ int ffs_mlp_param_count(void);
 int ffs_arma_simulate(int V, int T, int K, int n_runs, const int* run_start, const float* X, const float* a,
                       const float* b, uint64_t seed, float* Y, void* stream);
 
-/* feats[v] = (sum_runs sum_t r_t r_{t+k} / sum r^2 for k = 1..8, T/1000) of the
- * residualised series yr_t ([T][V], the prep output). */
-int ffs_reml_features(int V, int T, int n_runs, const int* run_start, const float* yr_t, float* feats,
-                      void* stream);
+/* Features come from ffs_reml_prep (ffs_prep_args.feats). */
 
 int ffs_mlp_forward(const float* params, const float* x, int B, float* out, void* stream);
 
@@ -330,17 +358,44 @@ int ffs_mlp_adam(float* params, float* grad, float* m, float* v, int n, float lr
 int ffs_reml_centers(int V, const float* prop, const float* a_axis, int n_a, const float* b_axis, int n_b,
                      int* center, void* stream);
 
-/* U [P][K][T] -> Ut [P][T][K] (the windowed refine reads a time point's K values). */
-int ffs_transpose_u(int P, int K, int T, const float* U, float* Ut, void* stream);
+/* Rows of the prep outputs in the order idx[0..n): out_hi/out_lo[i] =
+ * yr_hi/yr_lo[idx[i]] ([.][ld_y] fp16 bits), out_exp[i] = yexp[idx[i]] and
+ * out_t[t][i] = yr_rows[idx[i]][t] ([T][n], time-major) for the windowed
+ * refine's sorted operands. */
+int ffs_reml_gather(int n, int T, int ld_y, const int* idx, const uint16_t* yr_hi, const uint16_t* yr_lo,
+                    const int* yexp, const float* yr_rows, uint16_t* out_hi, uint16_t* out_lo, int* out_exp,
+                    float* out_t, void* stream);
 
-/* The windowed refine (see above): per voxel (in `order`, grouped by centre),
- * best pair of its 5 x 5 window, its criterion relative to (0, 0) (dbest),
- * crit0 as in ffs_reml_surface, and fallback[v] = 1 when the full grid must
- * decide. K <= 32. */
-int ffs_reml_window(int V, int T, int K, int P, int p0, int n_a, int n_b, const int* lattice, const int* center,
-                    const int* order, const float* yr_t, const float* coef, const float* Ut,
-                    const double* logdet_R, const double* logdet_XtX, int* best, float* dbest, double* crit0,
-                    int* fallback, void* stream);
+/* Work list of the windowed refine for voxels sorted by window centre
+ * (cell = ai * n_b + bi; cell c's sorted rows end at cell_end[c], as
+ * ffs_reml_group leaves them): one ffs_tc_item per 128-row tile of a cell and
+ * run of at most max_pairs consecutive valid pairs of one window row, with
+ * slot0 = 5 * window row + window column, and one tile (v0, nv) = tiles[2t],
+ * tiles[2t+1] per 128-row tile of a cell for ffs_reml_window. The counts go to
+ * *n_items and *n_tiles (clamped to max_items, max_tiles; *overflow = 1 if
+ * anything was dropped). */
+int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, const int* lattice, int K,
+                          int max_pairs, ffs_tc_item* items, int* n_items, int max_items, int* tiles,
+                          int* n_tiles, int max_tiles, int* overflow, void* stream);
+
+/* The windowed refine's criterion over the tiles of ffs_reml_window_items
+ * (launched for max_tiles, *n_tiles of them real), one sorted row i < n (voxel
+ * idx[i], window centre center[i]): y'R^-1 y of each non-identity window pair by the O(T)
+ * recurrence of coef over yr_st ([T][n], the sorted rows time-major), its
+ * projection from winproj[i][slot] (ffs_reml_project_tc_list), the criterion
+ * relative to (0, 0) with dcf[p] = (logdet_R + logdet_XtX)[p] - that of (0, 0),
+ * and the argmin. Identity pairs (ident[p] = 1 when lambda == 0) all have
+ * d = 0 and the full grid picks the first of them, p_id: a window holding one
+ * competes with (p_id, 0), and a win by it is final. Writes at voxel idx[i]:
+ * best, dbest (criterion relative to (0, 0)), crit0 (as ffs_reml_surface),
+ * fallback = 1 when the full grid must decide (the best non-identity pair has
+ * a valid lattice neighbour outside the window, or the window holds no
+ * identity pair and nothing below d = 0), best_cell (the lattice cell of the
+ * best non-identity pair, -1 if none). */
+int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx, const int* center,
+                    const int* tiles, const int* n_tiles, int max_tiles, const float* yr_st, const float* coef,
+                    const float* winproj, const float* dcf, const unsigned char* ident, int p_id, double c_p0,
+                    int* best, float* dbest, double* crit0, int* fallback, int* best_cell, void* stream);
 
 #ifdef __cplusplus
 }
