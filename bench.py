@@ -1,13 +1,19 @@
 #!/usr/bin/env python
-"""ARMA(1,1) REML voxelwise GLM throughput on GB300 (voxels/s).
+"""ARMA(1,1) REML voxelwise GLM throughput on GB300 (voxels/s): learned-seeded
+refine vs the full-grid solve.
 
 One step = one complete ``fit_glm_arma11`` of the 200,000-voxel workload
 (N = 400 as 2 runs x 200, p = 20, the 33 x 33 grid on [-0.8, 0.8] -> 561 valid
-(a, b) pairs, default hierarchical selector): FP64 grid factors, per-voxel
-scaling and residualisation, the criterion at every pair, selection and the GLS
-refit with t, F, R^2, sigma2 and lambda. ``value`` keeps the data resident in
-HBM; ``e2e`` calls the same public API with pinned host buffers (host->device
-copy of the data and device->host copy of the results inside the timed region).
+(a, b) pairs): FP64 grid factors, per-voxel scaling and residualisation, the
+(a, b) search, and the GLS refit with t, F, R^2, sigma2 and lambda.
+``value`` is the learned-seeded step (each voxel's 5 x 5 window around the
+proposal of the MLP, one re-centred round, the full grid for the voxels still
+on a window edge); ``full_grid`` is the same fit evaluating all 561 pairs
+(the reference's default hierarchical selector). The proposal is trained on
+the GPU before timing (2M voxels simulated with this design, full-grid
+labels). ``value`` keeps the data resident in HBM; ``e2e`` calls the same
+public API with pinned host buffers (host->device copy of the data and
+device->host copy of the results inside the timed region).
 
 Usage: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 Multi-GPU (torchrun): every rank fits its own 200,000 voxels (weak scaling, no
@@ -36,11 +42,11 @@ GRID = 33
 L2_BYTES = 129 * 2**20
 
 
-def workload_config(V: int, selector: str) -> dict:
+def workload_config(V: int) -> dict:
     return {
         "workload": f"synthetic fMRI, N=400 (2 runs x 200), V={V:,} voxels, p=20, "
-                    f"(a,b) grid 33x33 on [-0.8,0.8] -> 561 valid pairs, {selector} selector",
-        "voxels": V, "timepoints": 400, "regressors": 20, "pairs": 561, "selector": selector,
+                    f"(a,b) grid 33x33 on [-0.8,0.8] -> 561 valid pairs",
+        "voxels": V, "timepoints": 400, "regressors": 20, "pairs": 561,
         "l2": "inputs larger than L2 (Y is 320 MB fp32 > 129 MB L2); no flush needed",
     }
 
@@ -153,7 +159,8 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded workload)",
-        "config": workload_config(args.voxels, "hierarchical"),
+        "config": workload_config(args.voxels),
+        "method": "the reference's default CPU fit (full grid, hierarchical selector)",
         "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": cores, "kind": "port",
                          "sample": f"{n} voxels per step of the same workload on {cores} host threads"},
         "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -161,9 +168,44 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def roofline(dom: str, mean_ms: float, V: int, T: int, K: int, P: int, pk: dict, sm_mhz, extra: dict) -> dict:
+    """Algorithmic work of the dominant kernel per launch against its bound."""
+    sec = mean_ms / 1e3
+    fp32_peak = 152 * 128 * 2 * (sm_mhz or 1900.0) * 1e6 / 1e12
+    if dom in ("ffs_reml_project_tc", "ffs_reml_project_tc_list"):
+        k_eff = (T + 15) // 16 * 16
+        cols = extra.get("pair_evals", V * P) if dom == "ffs_reml_project_tc_list" else V * P
+        flops = 3 * 2.0 * cols * K * k_eff
+        ach = flops / sec / 1e12
+        return {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": ach / pk["bf16_tflops"], "traffic": None, "peak_src": pk["src"] + " (bf16 burst)",
+                "work": "3 fp16 products x 2 x (voxel, pair) x K x T (k rounded to 16)"}
+    if dom in ("ffs_reml_surface", "ffs_reml_window"):
+        n = extra.get("pair_evals", V * P) if dom == "ffs_reml_window" else V * P
+        flops = 4.0 * n * T  # v_t = z_t - m_t v_t-1 and s += v_t^2 / D_t: 2 FMA
+        ach = flops / sec / 1e12
+        return {"kernel": dom, "bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": ach / fp32_peak, "traffic": None, "peak_src": "152 SMs x 128 FMA/clk at the sampled clock",
+                "work": "2 FMA per (voxel, pair, time point) of the O(T) recurrences"}
+    if dom == "ffs_reml_gls_grouped":
+        flops = V * (4 * 2.0 * K * T + 6.0 * T)
+        ach = flops / sec / 1e12
+        return {"kernel": dom, "bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": ach / fp32_peak, "traffic": None, "peak_src": "152 SMs x 128 FMA/clk at the sampled clock",
+                "work": "G'y, X b, G'r, X d (4 K x T products) and the whitening recurrence per voxel"}
+    # the rest stream HBM (prep: Y in; rows/time-major and the fp16 split out)
+    ld = (T + 63) // 64 * 64
+    byts = V * (T * 4 + T * 4 + 2 * ld * 2 + 16)
+    ach = byts / sec / 1e9
+    return {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_src": pk["src"],
+            "work": "bytes: Y read, residualised rows and fp16 hi/lo written"}
+
+
 def run_gb300(args) -> None:
     from fastfuncstuff_gb300 import fit_glm_arma11, synth
-    from fastfuncstuff_gb300.glm import engine
+    from fastfuncstuff_gb300.glm import engine, learned
+    from fastfuncstuff_gb300.glm import grid as G
 
     dist, rank, ws, local = dist_init()
     dev = torch.device(f"cuda:{local}")
@@ -174,90 +216,118 @@ def run_gb300(args) -> None:
     Yd = torch.from_numpy(w.Y).to(dev)
     kw = dict(tr=2.0, a_grid=g, b_grid=g, run_starts=w.run_starts, device=dev, verbose=False,
               force_exhaustive_search=args.selector == "exhaustive", projector=args.projector)
-
-    def step():
-        return fit_glm_arma11(Yd, Xd, return_device=True, **kw)
+    lay = G.run_layout(w.T, w.run_starts)
+    if args.proposal:
+        prop = learned.ArmaProposal.load(args.proposal, dev)
+        tinfo = {"proposal": f"loaded from {Path(args.proposal).name}"}
+    else:
+        prop, tinfo = learned.train_proposal(Xd, lay, g, g, n_voxels=args.train_voxels, epochs=args.train_epochs)
+        if args.save_proposal and rank == 0:
+            prop.save(args.save_proposal)
+    kw_l = dict(kw, proposal=prop, proposal_recenter=args.recenter)
 
     def barrier():
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
 
-    for _ in range(args.warmup):
-        step()
-    barrier()
-    timer = engine.StageTimer()
-    engine.set_stage_timer(timer)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        barrier()
-        e0.record()
-        for _ in range(args.steps):
-            step()
-        e1.record()
-        barrier()
-    engine.set_stage_timer(None)
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * args.voxels / (ms / 1e3)
-    stages = timer.summary()
+    def timed(kwargs):
+        def step():
+            return fit_glm_arma11(Yd, Xd, return_device=True, **kwargs)
 
-    # roofline of the dominant kernel (device time measured above, per launch)
+        for _ in range(args.warmup):
+            step()
+        barrier()
+        timer = engine.StageTimer()
+        engine.set_stage_timer(timer)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            barrier()
+            e0.record()
+            for _ in range(args.steps):
+                step()
+            e1.record()
+            barrier()
+        engine.set_stage_timer(None)
+        ms = e0.elapsed_time(e1) / args.steps
+        if dist is not None:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        st = timer.summary()
+        return ms, st, timer.launches // args.steps, clk.summary()
+
+    ms_f, st_f, l_f, clk_f = timed(kw)
+    ms_l, st_l, l_l, clk_l = timed(kw_l)
+    value = ws * args.voxels / (ms_l / 1e3)
+    value_f = ws * args.voxels / (ms_f / 1e3)
+
+    # quality of the learned step against the full grid (exhaustive argmin)
+    exh = fit_glm_arma11(Yd, Xd, return_device=True, **dict(kw, force_exhaustive_search=True))
+    lr = fit_glm_arma11(Yd, Xd, return_device=True, **kw_l)
+    same = (lr.arma_params == exh.arma_params).all(1)
+    num = (lr.betas.double() - exh.betas.double()).abs().amax(1)
+    den = exh.betas.double().abs().amax(1).clamp(min=1e-12)
+    rel = num / den
+    f_all = engine.build_factors(Xd, G.make_grid(g, g), lay)
+    ls = learned.learned_search(Yd, f_all, prop, lay, recenter=args.recenter)
+    pair_evals = float(ls.stats["pair_evals"].item()) if torch.is_tensor(ls.stats["pair_evals"]) else 0.0
+    quality = {
+        "agreement_with_full_grid": float(same.float().mean().item()),
+        "beta_rel_err_le_1e-4": float((rel <= 1e-4).float().mean().item()),
+        "beta_rel_err_max_where_pair_agrees": float(rel[same].max().item()) if bool(same.any()) else None,
+        "first_window_on_edge": float(ls.stats["edge_first"]), "full_grid_fallback": ls.stats["fallback"],
+        "recenter_rounds": args.recenter, "window_pair_evals_per_voxel": pair_evals / args.voxels,
+    }
+    quality.update({k: round(v, 3) if isinstance(v, float) else v for k, v in tinfo.items()})
+
     pk = peaks()
     V, T, K, P = args.voxels, 400, 20, 561
-    dom = max(stages.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])[0]
-    roof = None
-    if dom == "ffs_reml_project_tc":
-        flops = 3 * 2.0 * V * P * K * 448  # three fp16 products over the padded k extent
-        ach = flops / (stages[dom]["mean_ms"] / 1e3) / 1e12
-        roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": ach / pk["bf16_tflops"], "traffic": None,
-                "work": "issued fp16 tensor flops = 3 x 2 x V x P x K x 448 (k padded to 64)",
-                "peak_src": pk["src"]}
-    elif dom in ("ffs_reml_surface", "ffs_reml_project_simt"):
-        if dom == "ffs_reml_surface":
-            flops = 2.0 * 3 * V * P * T  # 3 FMA per (voxel, pair, time point)
-        else:
-            flops = 2.0 * V * P * K * T
-        ach = flops / (stages[dom]["mean_ms"] / 1e3) / 1e12
-        sm = (clk.summary()["sm_mhz"] or 1900.0) * 1e6
-        fp32_peak = 152 * 128 * 2 * sm / 1e12
-        roof = {"kernel": dom, "bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": ach / fp32_peak, "traffic": None,
-                "work": "fp32 FMA flops of the O(T) recurrences", "peak_src": "152 SMs x 128 FMA/clk at the sampled clock"}
+    dom = max(st_l.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])[0]
+    extra = {"pair_evals": pair_evals}
+    roof = roofline(dom, st_l[dom]["mean_ms"], V, T, K, P, pk, clk_l["sm_mhz"], extra)
+    dom_f = max(st_f.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])[0]
+    roof_f = roofline(dom_f, st_f[dom_f]["mean_ms"], V, T, K, P, pk, clk_f["sm_mhz"], {})
 
     line = {
         "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms_l, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded workload, see fastfuncstuff_gb300/synth.py)",
-        "config": workload_config(args.voxels, args.selector),
+        "config": workload_config(args.voxels),
+        "method": f"learned-seeded 5x5 window refine ({args.recenter} re-centred round), full grid on window edges",
         "roofline": roof,
-        "stages_ms": {k: round(v["mean_ms"], 4) for k, v in stages.items()},
-        "gpu_launches": timer.launches,
-        "clocks": clk.summary(),
+        "stages_ms": {k: round(v["mean_ms"] * v["calls"] / args.steps, 4) for k, v in st_l.items()},
+        "gpu_launches": l_l,
+        "clocks": clk_l,
+        "learned": quality,
+        "full_grid": {"value": value_f, "ms_per_step": ms_f, "selector": args.selector,
+                      "learned_over_full": value / value_f, "roofline": roof_f,
+                      "stages_ms": {k: round(v["mean_ms"] * v["calls"] / args.steps, 4) for k, v in st_f.items()},
+                      "gpu_launches": l_f, "clocks": clk_f},
     }
 
     if rank == 0 and not args.no_e2e:
         # end to end through the public API from pinned host buffers
         Yh = torch.from_numpy(w.Y).pin_memory()
         Xh = torch.from_numpy(w.X)
-        kwh = dict(kw)
-        for _ in range(2):
-            r = fit_glm_arma11(Yh, Xh, **kwh)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            r = fit_glm_arma11(Yh, Xh, **kwh)
-        torch.cuda.synchronize()
-        dt = (time.perf_counter() - t0) / args.e2e_steps
-        d2h = sum(t.numel() * t.element_size() for t in (r.betas, r.tstats, r.r2, r.arma_params, r.arma_lambda,
-                                                         r.reml_likelihood, r.sigma2, r.fstats))
-        line["e2e"] = {"value": args.voxels / dt, "unit": "voxels/s", "h2d_bytes_per_step": Yh.numel() * 4 + Xh.numel() * 4,
-                       "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3}
+        e2e = {}
+        for name, kwh in (("learned", kw_l), ("full_grid", kw)):
+            for _ in range(2):
+                r = fit_glm_arma11(Yh, Xh, **kwh)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                r = fit_glm_arma11(Yh, Xh, **kwh)
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / args.e2e_steps
+            d2h = sum(t.numel() * t.element_size() for t in (r.betas, r.tstats, r.r2, r.arma_params,
+                                                             r.arma_lambda, r.reml_likelihood, r.sigma2, r.fstats))
+            e2e[name] = {"value": args.voxels / dt, "unit": "voxels/s",
+                         "h2d_bytes_per_step": Yh.numel() * 4 + Xh.numel() * 4, "d2h_bytes_per_step": d2h,
+                         "ms_per_step": dt * 1e3}
+        line["e2e"] = e2e["learned"]
+        line["full_grid"]["e2e"] = e2e["full_grid"]
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_voxels)
     if rank == 0:
@@ -279,6 +349,11 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-voxels", type=int, default=4000)
     ap.add_argument("--ref-voxels", type=int, default=4000)
+    ap.add_argument("--recenter", type=int, default=1)
+    ap.add_argument("--train-voxels", type=int, default=2_000_000)
+    ap.add_argument("--train-epochs", type=int, default=30)
+    ap.add_argument("--proposal", default=None, help="load a trained proposal (.npz) instead of training one")
+    ap.add_argument("--save-proposal", default=None, help="save the proposal trained here (.npz)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -37,7 +37,7 @@ struct TcParams {
   int n_col_tiles, n_vox_tiles;
   const ffs_tc_item* items;  // work-list mode: items[0 .. *n_items)
   const int* n_items;
-  int s_pair, s_vox;   // output strides: out[(slot0 + j) * s_pair + (out0 + r) * s_vox]
+  int s_vox;           // work-list mode: proj[(out0 + r) * s_vox + slot0 + j]
   const int* yexp;
   const int* uexp;
   float* proj;
@@ -50,9 +50,10 @@ struct Item {
   int v0, nv, row_b, np, out0, slot0, N;
 };
 
+template <bool LIST>
 __device__ __forceinline__ Item item_at(const TcParams& prm, int item) {
   Item it;
-  if (prm.items) {
+  if (LIST) {
     const ffs_tc_item w = prm.items[item];
     it.v0 = w.v0;
     it.nv = w.nv;
@@ -144,6 +145,7 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 // run together share voxel tiles in L2). The TMA ring of STAGES k-blocks runs
 // across items; TMEM holds two 256-column accumulators so the epilogue warps
 // drain item i while the MMA warp accumulates item i + 1.
+template <bool LIST>
 __global__ void __launch_bounds__(192, 1)
     project_tc_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
                       const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
@@ -161,7 +163,7 @@ __global__ void __launch_bounds__(192, 1)
   // a CTA that finds an earlier CTA's wait expired does nothing
   if (*reinterpret_cast<volatile int*>(prm.flag) != 0) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n_items = prm.items ? *prm.n_items : prm.n_col_tiles * prm.n_vox_tiles;
+  const int n_items = LIST ? *prm.n_items : prm.n_col_tiles * prm.n_vox_tiles;
   const int nk = prm.ld / BK;
 
   if (threadIdx.x == 0) {
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(192, 1)
     int kc = 0;
     bool ok = true;
     for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-      const Item it = item_at(prm, item);
+      const Item it = item_at<LIST>(prm, item);
       const int v0 = it.v0, row_b = it.row_b;
       for (int kb = 0; kb < nk; ++kb, ++kc) {
         const int s = kc % STAGES;
@@ -213,7 +215,7 @@ __global__ void __launch_bounds__(192, 1)
     int kc = 0, local = 0;
     bool ok = true;
     for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x, ++local) {
-      const uint32_t idesc = idesc_f16(BM, item_at(prm, item).N);
+      const uint32_t idesc = idesc_f16(BM, item_at<LIST>(prm, item).N);
       const int buf = local & 1;
       const uint32_t acc = tmem + (uint32_t)(buf * 256);
       if (local >= 2 && !mbar_wait(acc_empty + buf, ((local >> 1) - 1) & 1)) {
@@ -261,16 +263,27 @@ __global__ void __launch_bounds__(192, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const Item it = item_at(prm, item);
-      const bool live = row < it.nv;
-      const int v = it.v0 + row;
-      const int p_first = it.row_b / prm.K;
-      const int ncols = it.np * prm.K;
-      const int ey = live ? prm.yexp[v] : 0;
-      float* out = prm.proj + (size_t)it.slot0 * prm.s_pair + (size_t)(it.out0 + row) * prm.s_vox;
+      // grid mode keeps the exact form whose timing was measured best; the
+      // work-list mode differs in where the result goes
+      int v, p_first, ncols, nmax, out_row;
+      if (LIST) {
+        const Item it = item_at<LIST>(prm, item);
+        v = row < it.nv ? it.v0 + row : prm.V;
+        p_first = it.row_b / prm.K;
+        ncols = it.np * prm.K;
+        nmax = it.N;
+        out_row = (it.out0 + row) * prm.s_vox + it.slot0;
+      } else {
+        v = (item / prm.n_col_tiles) * BM + row;
+        p_first = (item % prm.n_col_tiles) * prm.g;
+        ncols = prm.g * prm.K;
+        nmax = prm.N;
+        out_row = 0;
+      }
+      const int ey = v < prm.V ? prm.yexp[v] : 0;
       int j = 0, pl = 0;
       float run = 0.f;
-      for (int c0 = 0; c0 < it.N; c0 += 16) {
+      for (int c0 = 0; c0 < nmax; c0 += 16) {
         uint32_t r[16];
         const uint32_t taddr = tmem + (uint32_t)(buf * 256) + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
         asm volatile(
@@ -286,7 +299,14 @@ __global__ void __launch_bounds__(192, 1)
             const float x = __uint_as_float(r[i]);
             run = fmaf(x, x, run);
             if (++j == prm.K) {
-              if (live) out[(size_t)pl * prm.s_pair] = ldexpf(run, -2 * (ey + prm.uexp[p_first + pl]));
+              const int p = p_first + pl;
+              if (p < prm.P && v < prm.V) {
+                const float val = ldexpf(run, -2 * (ey + prm.uexp[p]));
+                if (LIST)
+                  prm.proj[(size_t)out_row + pl] = val;
+                else
+                  prm.proj[(size_t)p * prm.V + v] = val;
+              }
               run = 0.f;
               j = 0;
               ++pl;
@@ -351,13 +371,13 @@ int launch_tc(const ffs_project_args* a, const TcParams& prm, int max_items, voi
   const int stage_bytes = 2 * A_TILE + 2 * prm.NB * BK * 2;
   const size_t smem = (size_t)STAGES * stage_bytes + 1024 + 128;
   FFS_REQUIRE(smem <= 227 * 1024, "project_tc: tile needs %zu bytes of shared memory", smem);
-  FFS_CUDA(cudaFuncSetAttribute(project_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto kern = prm.items ? project_tc_kernel<true> : project_tc_kernel<false>;
+  FFS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int dev = 0, n_sm = 0;
   FFS_CUDA(cudaGetDevice(&dev));
   FFS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
   if (max_items <= 0) return FFS_OK;
-  project_tc_kernel<<<min(max_items, n_sm), 192, smem, (cudaStream_t)stream>>>(ta_hi, ta_lo, tb_hi, tb_lo,
-                                                                                     prm);
+  kern<<<min(max_items, n_sm), 192, smem, (cudaStream_t)stream>>>(ta_hi, ta_lo, tb_hi, tb_lo, prm);
   return check_launch("project_tc_kernel");
 }
 
@@ -393,8 +413,7 @@ extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
   prm.T = a->T;
   prm.items = nullptr;
   prm.n_items = nullptr;
-  prm.s_pair = a->V;
-  prm.s_vox = 1;
+  prm.s_vox = 0;
   prm.yexp = a->yexp;
   prm.uexp = a->uexp;
   prm.proj = a->proj;
@@ -428,7 +447,6 @@ extern "C" int ffs_reml_project_tc_list(const ffs_project_args* a, const ffs_tc_
   prm.n_vox_tiles = 0;
   prm.items = items;
   prm.n_items = n_items;
-  prm.s_pair = 1;
   prm.s_vox = ld_out;
   prm.yexp = a->yexp;
   prm.uexp = a->uexp;

@@ -100,7 +100,7 @@ struct CritArgs {
   const float* dcf;         // [P] (logdet_R + logdet_XtX)[p] - that of (0, 0)
   const uint8_t* ident;     // [P]
   int p_id;
-  double c_p0;
+  const double* c_p0;       // device scalar: logdet_R + logdet_XtX of (0, 0)
   int* best;                // outputs at idx[i]
   float* dbest;
   double* crit0;
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
   const int v = w.idx[i];
   w.best[v] = best;
   w.dbest[v] = bd;
-  w.crit0[v] = w.c_p0 + (double)Tk * log((double)rss0 + 1e-10);
+  w.crit0[v] = *w.c_p0 + (double)Tk * log((double)rss0 + 1e-10);
   w.fallback[v] = fb;
   w.best_cell[v] = bcell;
 }
@@ -344,13 +344,13 @@ extern "C" int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, in
 extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx,
                                const int* center, const int* tiles, const int* n_tiles, int max_tiles,
                                const float* yr_st, const float* coef, const float* winproj, const float* dcf,
-                               const unsigned char* ident, int p_id, double c_p0, int* best, float* dbest,
+                               const unsigned char* ident, int p_id, const double* c_p0, int* best, float* dbest,
                                double* crit0, int* fallback, int* best_cell, void* stream) {
   clear_error();
   FFS_REQUIRE(n > 0 && T > K && K > 0 && n_a > 0 && n_b > 0 && p_id >= 0 && max_tiles > 0,
               "ffs_reml_window: bad sizes");
-  FFS_REQUIRE(lattice && idx && center && tiles && n_tiles && yr_st && coef && winproj && dcf && ident && best &&
-                  dbest && crit0 && fallback && best_cell,
+  FFS_REQUIRE(lattice && idx && center && tiles && n_tiles && yr_st && coef && winproj && dcf && ident && c_p0 &&
+                  best && dbest && crit0 && fallback && best_cell,
               "ffs_reml_window: null buffer");
   const size_t smem = sizeof(float4) * WIN * (size_t)T;
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_reml_window: T=%d too long", T);

@@ -195,22 +195,40 @@ class LearnedOut:
 WIN_SLOTS = 25
 
 
+_GRID_CONSTS: dict = {}
+
+
 def _window_consts(f: engine.GridFactors):
-    """Per-factor constants of the windowed refine (computed once per factors)."""
-    c = getattr(f, "_window_consts", None)
+    """Constants of the windowed refine: the grid's (cached by lattice content)
+    and the factors' (device tensors, no host round trip)."""
+    g = f.grid
+    dev = f.coef.device
+    key = (g.a_axis.tobytes(), g.b_axis.tobytes(), g.lattice.tobytes(), str(dev))
+    c = _GRID_CONSTS.get(key)
     if c is None:
-        g = f.grid
-        dev = f.coef.device
-        c_p0 = float((f.logdet_R[g.p0] + f.logdet_XtX[g.p0]).item())
-        dcf = ((f.logdet_R + f.logdet_XtX) - c_p0).float().contiguous()
         ident_np = lambda_is_zero(g.a, g.b)
-        ident = torch.from_numpy(ident_np.astype(np.uint8)).to(dev)
-        p_id = int(np.nonzero(ident_np)[0][0])
-        a_ax = torch.from_numpy(g.a_axis).to(dev)
-        b_ax = torch.from_numpy(g.b_axis).to(dev)
-        c = dict(c_p0=c_p0, dcf=dcf, ident=ident, p_id=p_id, a_ax=a_ax, b_ax=b_ax)
-        f._window_consts = c
-    return c
+        # non-identity pairs of the (clamped) 5 x 5 window of every lattice cell
+        n_a, n_b = g.lattice.shape
+        nonid = np.zeros((n_a, n_b), np.int64)
+        ok = g.lattice >= 0
+        nonid[ok] = (~ident_np[g.lattice[ok]]).astype(np.int64)
+        a0 = np.clip(np.arange(n_a) - 2, 0, n_a - min(5, n_a))
+        b0 = np.clip(np.arange(n_b) - 2, 0, n_b - min(5, n_b))
+        cs = np.zeros((n_a + 1, n_b + 1), np.int64)
+        cs[1:, 1:] = nonid.cumsum(0).cumsum(1)
+        a1 = a0 + min(5, n_a)
+        b1 = b0 + min(5, n_b)
+        evals = (cs[a1][:, b1] - cs[a0][:, b1] - cs[a1][:, b0] + cs[a0][:, b0]).reshape(-1)
+        c = dict(ident=torch.from_numpy(ident_np.astype(np.uint8)).to(dev), p_id=int(np.nonzero(ident_np)[0][0]),
+                 a_ax=torch.from_numpy(g.a_axis).to(dev), b_ax=torch.from_numpy(g.b_axis).to(dev),
+                 evals=torch.from_numpy(evals).to(dev))
+        _GRID_CONSTS[key] = c
+    fc = getattr(f, "_window_consts", None)
+    if fc is None:
+        c_p0 = (f.logdet_R[g.p0] + f.logdet_XtX[g.p0]).reshape(1).contiguous()
+        fc = dict(c, c_p0=c_p0, dcf=((f.logdet_R + f.logdet_XtX) - c_p0).float().contiguous())
+        f._window_consts = fc
+    return fc
 
 
 def _window_round(pre, f, src, cen, out, *, flag):
@@ -256,8 +274,10 @@ def _window_round(pre, f, src, cen, out, *, flag):
     engine._run("ffs_reml_project_tc_list", lib.ffs_reml_project_tc_list, C.byref(ja), _p(items), _p(counts),
                 max_items, max_pairs, WIN_SLOTS, st)
     engine._run("ffs_reml_window", lib.ffs_reml_window, n, T, K, n_a, n_b, _p(f.lattice), _p(idx), _p(cen_s),
-                _p(tiles), counts.data_ptr() + 8, max_tiles, _p(yr_st), _p(f.coef), _p(winproj), _p(c["dcf"]), _p(c["ident"]), c["p_id"], c["c_p0"],
+                _p(tiles), counts.data_ptr() + 8, max_tiles, _p(yr_st), _p(f.coef), _p(winproj), _p(c["dcf"]),
+                _p(c["ident"]), c["p_id"], _p(c["c_p0"]),
                 _p(out["best"]), _p(out["dbest"]), _p(out["crit0"]), _p(out["fb"]), _p(out["cell"]), st)
+    out["pair_evals"] = out.get("pair_evals", 0) + c["evals"][cen.long()].sum()
     return counts
 
 
@@ -298,7 +318,7 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
     stats = {"edge_first": None}
     for r in range(recenter):
         if r == 0:
-            stats["edge_first"] = float(out["fb"].float().mean().item())
+            stats["edge_first"] = out["fb"].float().mean()  # device scalar
         # re-centre on the window's best pair (voxels whose window held no
         # candidate keep their fallback)
         sel = torch.nonzero((out["fb"] != 0) & (out["cell"] >= 0), as_tuple=True)[0].to(torch.int32)
@@ -309,16 +329,42 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
     best = out["best"]
     fb = out["fb"]
     # the full grid for the voxels still on a window edge
+    # one host round trip: the fallback list, the wait flag and the overflow counts
+    bad = torch.stack([flag[0]] + [cn[1] for cn in counts])
     sel = torch.nonzero(fb, as_tuple=True)[0]
+    bad = bad.cpu()
+    if int(bad[0]) != 0:
+        raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {int(bad[0])})")
+    if bool((bad[1:] != 0).any()):
+        raise RuntimeError("ffs_reml_window_items: work list overflow")
     if stats["edge_first"] is None:
         stats["edge_first"] = sel.numel() / V
     stats["fallback"] = sel.numel() / V
+    stats["pair_evals"] = out["pair_evals"]  # device scalar: (voxel, pair) windows evaluated
     if sel.numel():
         so = engine.search(Y.index_select(0, sel), f, hierarchical=False, projector="tc", do_scale=do_scale)
         best.index_copy_(0, sel, so.best)
         best_crit.index_copy_(0, sel, so.best_crit)
-    if int(flag.item()) != 0:
-        raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {int(flag.item())})")
-    if any(int(cn[1].item()) for cn in counts):
-        raise RuntimeError("ffs_reml_window_items: work list overflow")
     return LearnedOut(best=best, best_crit=best_crit, scale=scale, fallback=fb, proposal=prop, stats=stats)
+
+
+def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxels: int = 2_000_000,
+                   epochs: int = 30, batch: int = 8192, lr: float = 3e-3, seed: int = 5):
+    """Train a proposal for design X on the GPU: n_voxels simulated with (a, b)
+    drawn uniformly over the valid pairs, labelled by the full-grid exhaustive
+    argmin, then Adam on the library's forward/backward kernels. Returns
+    (ArmaProposal, info) with the seconds spent."""
+    from .grid import make_grid
+
+    t0 = time.perf_counter()
+    f = engine.build_factors(X, make_grid(a_grid, b_grid), layout)
+    x, y = training_set(X, f, layout, n_voxels, seed=seed)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    prop, hist = train(x, y, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    info = {"train_voxels": n_voxels, "epochs": epochs, "label_s": t1 - t0, "train_s": t2 - t1,
+            "holdout_loss": hist[-1]["holdout_loss"]}
+    prop.meta.update(info)
+    return prop, info

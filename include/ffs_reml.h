@@ -383,7 +383,8 @@ int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, cons
  * idx[i], window centre center[i]): y'R^-1 y of each non-identity window pair by the O(T)
  * recurrence of coef over yr_st ([T][n], the sorted rows time-major), its
  * projection from winproj[i][slot] (ffs_reml_project_tc_list), the criterion
- * relative to (0, 0) with dcf[p] = (logdet_R + logdet_XtX)[p] - that of (0, 0),
+ * relative to (0, 0) with dcf[p] = (logdet_R + logdet_XtX)[p] - that of (0, 0)
+ * (*c_p0, a device scalar),
  * and the argmin. Identity pairs (ident[p] = 1 when lambda == 0) all have
  * d = 0 and the full grid picks the first of them, p_id: a window holding one
  * competes with (p_id, 0), and a win by it is final. Writes at voxel idx[i]:
@@ -394,8 +395,9 @@ int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, cons
  * best non-identity pair, -1 if none). */
 int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx, const int* center,
                     const int* tiles, const int* n_tiles, int max_tiles, const float* yr_st, const float* coef,
-                    const float* winproj, const float* dcf, const unsigned char* ident, int p_id, double c_p0,
-                    int* best, float* dbest, double* crit0, int* fallback, int* best_cell, void* stream);
+                    const float* winproj, const float* dcf, const unsigned char* ident, int p_id,
+                    const double* c_p0, int* best, float* dbest, double* crit0, int* fallback, int* best_cell,
+                    void* stream);
 
 #ifdef __cplusplus
 }
