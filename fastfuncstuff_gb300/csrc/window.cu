@@ -249,11 +249,11 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
 }
 
 // fp16 operand rows and exponents in the order idx: a warp per row, 16-byte words
-__global__ void gather_rows_kernel(int n, int ld_y, const int* idx, const uint4* hi, const uint4* lo, const int* yexp,
-                                   uint4* out_hi, uint4* out_lo, int* out_exp) {
+__global__ void gather_rows_kernel(int n, const int* n_dev, int ld_y, const int* idx, const uint4* hi, const uint4* lo,
+                                   const int* yexp, uint4* out_hi, uint4* out_lo, int* out_exp) {
   const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (i >= n) return;
+  if (i >= n || (n_dev && i >= *n_dev)) return;
   const int v = idx[i];
   const int nw = ld_y / 8;  // 8 fp16 per 16-byte word
   for (int k = lane; k < nw; k += 32) {
@@ -264,18 +264,22 @@ __global__ void gather_rows_kernel(int n, int ld_y, const int* idx, const uint4*
 }
 
 // out_t[t][i] = rows[idx[i]][t]: 32 x 32 tiles through shared memory
-__global__ void gather_transpose_kernel(int n, int T, const int* idx, const float* rows, float* out_t) {
+__global__ void gather_transpose_kernel(int n, const int* n_dev, int T, const int* idx, const float* rows,
+                                        float* out_t) {
   __shared__ float tile[32][33];
   const int i0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
+  // rows taken: i < m (n stays the row stride of out_t)
+  const int m = n_dev ? min(n, *n_dev) : n;
+  if (i0 >= m) return;  // uniform over the CTA
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
   for (int r = ty; r < 32; r += 8) {
     const int i = i0 + r, t = t0 + tx;
-    tile[r][tx] = (i < n && t < T) ? rows[(size_t)idx[i] * T + t] : 0.f;
+    tile[r][tx] = (i < m && t < T) ? rows[(size_t)idx[i] * T + t] : 0.f;
   }
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
     const int t = t0 + r, i = i0 + tx;
-    if (t < T && i < n) out_t[(size_t)t * n + i] = tile[tx][r];
+    if (t < T && i < m) out_t[(size_t)t * n + i] = tile[tx][r];
   }
 }
 
@@ -303,9 +307,9 @@ __global__ void center_kernel(int V, const float* prop, const float* a_axis, int
 
 using namespace ffsk;
 
-extern "C" int ffs_reml_gather(int n, int T, int ld_y, const int* idx, const uint16_t* yr_hi, const uint16_t* yr_lo,
-                               const int* yexp, const float* yr_rows, uint16_t* out_hi, uint16_t* out_lo,
-                               int* out_exp, float* out_t, void* stream) {
+extern "C" int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const int* idx, const uint16_t* yr_hi,
+                               const uint16_t* yr_lo, const int* yexp, const float* yr_rows, uint16_t* out_hi,
+                               uint16_t* out_lo, int* out_exp, float* out_t, void* stream) {
   clear_error();
   FFS_REQUIRE(n > 0 && T > 0 && ld_y >= T && ld_y % 8 == 0, "ffs_reml_gather: bad sizes");
   FFS_REQUIRE(idx && yr_hi && yr_lo && yexp && yr_rows && out_hi && out_lo && out_exp && out_t,
@@ -313,12 +317,13 @@ extern "C" int ffs_reml_gather(int n, int T, int ld_y, const int* idx, const uin
   for (const void* ptr : {(const void*)yr_hi, (const void*)yr_lo, (const void*)out_hi, (const void*)out_lo})
     FFS_REQUIRE(((uintptr_t)ptr & 15) == 0, "ffs_reml_gather: fp16 rows must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
-  gather_rows_kernel<<<ceil_div(n, 8), 256, 0, st>>>(n, ld_y, idx, reinterpret_cast<const uint4*>(yr_hi),
+  gather_rows_kernel<<<ceil_div(n, 8), 256, 0, st>>>(n, n_dev, ld_y, idx, reinterpret_cast<const uint4*>(yr_hi),
                                                       reinterpret_cast<const uint4*>(yr_lo), yexp,
                                                       reinterpret_cast<uint4*>(out_hi),
                                                       reinterpret_cast<uint4*>(out_lo), out_exp);
   FFS_REQUIRE(ceil_div(T, 32) <= 65535, "ffs_reml_gather: T=%d too long", T);
-  gather_transpose_kernel<<<dim3(ceil_div(n, 32), ceil_div(T, 32)), dim3(32, 8), 0, st>>>(n, T, idx, yr_rows, out_t);
+  gather_transpose_kernel<<<dim3(ceil_div(n, 32), ceil_div(T, 32)), dim3(32, 8), 0, st>>>(n, n_dev, T, idx, yr_rows,
+                                                                                          out_t);
   return check_launch("gather kernels");
 }
 

@@ -376,8 +376,8 @@ def fit_glm_arma11(
         return t if return_device else t.cpu()
 
     best = cat("best").long()
-    a_t = torch.from_numpy(grid.a).to(device)
-    b_t = torch.from_numpy(grid.b).to(device)
+    a_t = engine.const_dev(grid.a, device)
+    b_t = engine.const_dev(grid.b, device)
     res.arma_params = out(torch.stack([a_t[best], b_t[best]], 1))
     if precomputed_arma_params is not None:
         res.arma_params = out(_to_tensor(precomputed_arma_params).reshape(-1, 2).to(device))
@@ -422,7 +422,10 @@ def fit_glm_arma11(
         res.reml_lklhd_surface = out(cat("surf"))
         res.reml_surface_params = grid.param_list()
     if proposal is not None and best_all is None:
-        res.learned_fallback = float(torch.cat(fallbacks).float().mean().item())
+        # fraction of voxels the full grid decided (a device scalar when the
+        # results stay on the device, so the call does not wait for the GPU)
+        fb = torch.cat(fallbacks).float().mean()
+        res.learned_fallback = fb if return_device else float(fb.item())
     if spatial_metadata:
         res.voxel_mask = spatial_metadata.get("voxel_mask")
         res.full_shape = spatial_metadata.get("volume_shape")

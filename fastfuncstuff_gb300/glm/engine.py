@@ -87,6 +87,26 @@ def _run(name: str, fn, *args) -> None:
     t.launches += LAUNCHES.get(name, 1)
 
 
+_CONST_CACHE: dict = {}
+
+
+def const_dev(arr: np.ndarray, dev) -> torch.Tensor:
+    """Read-only device copy of a small host array, cached by content.
+
+    A blocking host->device copy synchronises the stream; constants that the
+    same fit (or the next) needs again are copied once instead.
+    """
+    arr = np.ascontiguousarray(arr)
+    key = (str(dev), arr.dtype.str, arr.shape, arr.tobytes())
+    t = _CONST_CACHE.get(key)
+    if t is None:
+        if len(_CONST_CACHE) > 512:
+            _CONST_CACHE.clear()
+        t = torch.from_numpy(arr.copy()).to(dev)
+        _CONST_CACHE[key] = t
+    return t
+
+
 def padded_ld(T: int) -> int:
     return (T + LD_ALIGN - 1) // LD_ALIGN * LD_ALIGN
 
@@ -159,10 +179,10 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     ld = padded_ld(T)
     f32 = dict(device=dev, dtype=torch.float32)
     Xc = X.to(**f32).contiguous()
-    a = torch.from_numpy(grid.a).to(dev)
-    b = torch.from_numpy(grid.b).to(dev)
-    run_start = torch.from_numpy(layout.run_start).to(dev)
-    tau = torch.from_numpy(layout.tau).to(dev)
+    a = const_dev(grid.a, dev)
+    b = const_dev(grid.b, dev)
+    run_start = const_dev(layout.run_start, dev)
+    tau = const_dev(layout.tau, dev)
     task_idx = None
     if task_indices is not None and len(task_indices) > 0:
         task_idx = torch.as_tensor(list(task_indices), dtype=torch.int32, device=dev)
@@ -186,9 +206,9 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
         Ftask=torch.empty(P, nt, nt, **f32) if nt else None,
         glt_var=torch.empty(P, ng, **f32) if ng else None,
         a=a, b=b,
-        chunk_start=torch.from_numpy(grid.chunk_start).to(dev),
-        chunk_pairs=torch.from_numpy(grid.chunk_pairs).to(dev),
-        lattice=torch.from_numpy(grid.lattice.reshape(-1).copy()).to(dev),
+        chunk_start=const_dev(grid.chunk_start, dev),
+        chunk_pairs=const_dev(grid.chunk_pairs, dev),
+        lattice=const_dev(grid.lattice.reshape(-1), dev),
         task_idx=task_idx, glt=glt_t,
         Gsum=torch.empty(P, K, **f32),
         center=constant_in_span(X.detach().cpu().numpy()),
@@ -252,7 +272,7 @@ def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core:
     feats = rs = None
     if layout is not None:
         feats = torch.empty(n, 9, dtype=torch.float32, device=dev)
-        rs = torch.from_numpy(layout.run_start).to(dev)
+        rs = const_dev(layout.run_start, dev)
     rows = torch.empty(n, T, dtype=torch.float32, device=dev) if want_rows else None
     q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T])
     pa = _lib.PrepArgs(V=n, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=int(f.center), ld_y=ld,
@@ -369,8 +389,8 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
     h, ptau_d, w_d = 0, None, None
     if lj is not None and lj[0] > 0:
         h, ptau, w, _ = lj
-        ptau_d = None if ptau is None else torch.from_numpy(ptau).to(dev)
-        w_d = torch.from_numpy(w).to(dev)
+        ptau_d = None if ptau is None else const_dev(ptau, dev)
+        w_d = const_dev(w, dev)
         o.ljung_box = torch.empty(V, **f32)
     tiles = torch.empty(P + 1, dtype=torch.int32, device=dev)
     _run("ffs_reml_gls_grouped", lib.ffs_reml_gls_grouped, C.byref(ga), h, _p(ptau_d), _p(w_d), _p(o.ljung_box),

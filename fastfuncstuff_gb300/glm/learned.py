@@ -221,7 +221,7 @@ def _window_consts(f: engine.GridFactors):
         evals = (cs[a1][:, b1] - cs[a0][:, b1] - cs[a1][:, b0] + cs[a0][:, b0]).reshape(-1)
         c = dict(ident=torch.from_numpy(ident_np.astype(np.uint8)).to(dev), p_id=int(np.nonzero(ident_np)[0][0]),
                  a_ax=torch.from_numpy(g.a_axis).to(dev), b_ax=torch.from_numpy(g.b_axis).to(dev),
-                 evals=torch.from_numpy(evals).to(dev))
+                 evals=torch.from_numpy(np.append(evals, 0)).to(dev))  # [ncell + 1]: 0 for a skipped voxel
         _GRID_CONSTS[key] = c
     fc = getattr(f, "_window_consts", None)
     if fc is None:
@@ -231,10 +231,11 @@ def _window_consts(f: engine.GridFactors):
     return fc
 
 
-def _window_round(pre, f, src, cen, out, *, flag):
-    """Evaluate the 5 x 5 windows centred at cen (lattice cells) of the voxels
-    src (None: all voxels, in order), writing out[...] at the voxel ids; pre is
-    the prep of every voxel (fp16 operands and voxel-major rows)."""
+def _window_round(pre, f, cen, out, *, flag):
+    """Evaluate the 5 x 5 windows centred at cen (one lattice cell per voxel,
+    or ncell = n_a * n_b for a voxel to skip), writing out[...] at the voxel
+    ids. Nothing waits for the host: the number of voxels taken stays on the
+    device. pre is the prep of every voxel (fp16 operands and voxel-major rows)."""
     lib = _lib.load()
     dev = pre.scale.device
     g = f.grid
@@ -244,18 +245,17 @@ def _window_round(pre, f, src, cen, out, *, flag):
     ncell = n_a * n_b
     n = cen.numel()
     c = _window_consts(f)
-    # voxels sorted by window centre
-    order = torch.empty(n, dtype=torch.int32, device=dev)
-    cell_end = torch.empty(ncell + 1, dtype=torch.int32, device=dev)
-    engine._run("ffs_reml_group", lib.ffs_reml_group, n, ncell, _p(cen), _p(cell_end), _p(order), st)
-    ol = order.long()
-    idx = order if src is None else src[ol].to(torch.int32)
-    cen_s = cen[ol].contiguous()
+    # voxels sorted by window centre; the skipped ones (bucket ncell) last
+    idx = torch.empty(n, dtype=torch.int32, device=dev)
+    cell_end = torch.empty(ncell + 2, dtype=torch.int32, device=dev)
+    engine._run("ffs_reml_group", lib.ffs_reml_group, n, ncell + 1, _p(cen), _p(cell_end), _p(idx), st)
+    n_taken = cell_end[ncell - 1 : ncell]  # device count of the voxels with a window
+    cen_s = cen[idx.long()].contiguous()
     hi = torch.empty(n, ld, dtype=torch.int16, device=dev)
     lo = torch.empty(n, ld, dtype=torch.int16, device=dev)
     yexp = torch.empty(n, dtype=torch.int32, device=dev)
     yr_st = torch.empty(T, n, dtype=torch.float32, device=dev)
-    engine._run("ffs_reml_gather", lib.ffs_reml_gather, n, T, ld, _p(idx), _p(pre.yr_hi), _p(pre.yr_lo),
+    engine._run("ffs_reml_gather", lib.ffs_reml_gather, n, _p(n_taken), T, ld, _p(idx), _p(pre.yr_hi), _p(pre.yr_lo),
                 _p(pre.yexp), _p(pre.rows), _p(hi), _p(lo), _p(yexp), _p(yr_st), st)
     # projections of every window pair on the tensor cores
     max_pairs = max(1, min(5, 256 // K))
@@ -314,17 +314,17 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
                crit0=torch.empty(V, dtype=torch.float64, device=dev), fb=torch.zeros(V, dtype=torch.int32, device=dev),
                cell=torch.empty(V, dtype=torch.int32, device=dev))
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
-    counts = [_window_round(p1, f, None, center, out, flag=flag)]
+    counts = [_window_round(p1, f, center, out, flag=flag)]
     stats = {"edge_first": None}
+    ncell = len(g.a_axis) * len(g.b_axis)
     for r in range(recenter):
         if r == 0:
             stats["edge_first"] = out["fb"].float().mean()  # device scalar
-        # re-centre on the window's best pair (voxels whose window held no
-        # candidate keep their fallback)
-        sel = torch.nonzero((out["fb"] != 0) & (out["cell"] >= 0), as_tuple=True)[0].to(torch.int32)
-        if sel.numel() == 0:
-            break
-        counts.append(_window_round(p1, f, sel, out["cell"][sel.long()].contiguous(), out, flag=flag))
+        # re-centre the voxels on a window edge on the window's best pair; the
+        # rest (and those whose window held no candidate) are skipped
+        again = (out["fb"] != 0) & (out["cell"] >= 0)
+        cen = torch.where(again, out["cell"], torch.full_like(out["cell"], ncell)).contiguous()
+        counts.append(_window_round(p1, f, cen, out, flag=flag))
     best_crit = (out["crit0"] + out["dbest"].double()).float()
     best = out["best"]
     fb = out["fb"]

@@ -361,10 +361,11 @@ int ffs_reml_centers(int V, const float* prop, const float* a_axis, int n_a, con
 /* Rows of the prep outputs in the order idx[0..n): out_hi/out_lo[i] =
  * yr_hi/yr_lo[idx[i]] ([.][ld_y] fp16 bits), out_exp[i] = yexp[idx[i]] and
  * out_t[t][i] = yr_rows[idx[i]][t] ([T][n], time-major) for the windowed
- * refine's sorted operands. */
-int ffs_reml_gather(int n, int T, int ld_y, const int* idx, const uint16_t* yr_hi, const uint16_t* yr_lo,
-                    const int* yexp, const float* yr_rows, uint16_t* out_hi, uint16_t* out_lo, int* out_exp,
-                    float* out_t, void* stream);
+ * refine's sorted operands. With n_dev (device int) only the rows
+ * i < min(n, *n_dev) are written. */
+int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const int* idx, const uint16_t* yr_hi,
+                    const uint16_t* yr_lo, const int* yexp, const float* yr_rows, uint16_t* out_hi, uint16_t* out_lo,
+                    int* out_exp, float* out_t, void* stream);
 
 /* Work list of the windowed refine for voxels sorted by window centre
  * (cell = ai * n_b + bi; cell c's sorted rows end at cell_end[c], as

@@ -199,7 +199,7 @@ def test_window_round_matches_full_grid_surface():
                cell=torch.empty(V, dtype=torch.int32, device=dev))
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
     pre = engine.prep(Y, f, want_yr_t=False, want_rows=True)
-    counts = learned._window_round(pre, f, None, torch.from_numpy(cells).to(dev), out, flag=flag)
+    counts = learned._window_round(pre, f, torch.from_numpy(cells).to(dev), out, flag=flag)
     torch.cuda.synchronize()
     assert int(flag.item()) == 0 and int(counts[1].item()) == 0
     ident = G.lambda_is_zero(g.a, g.b)
