@@ -20,4 +20,6 @@ from .glm.arma import (  # noqa: F401
     set_afni_mode,
 )
 
+from . import ops  # noqa: F401,E402  (registers the ffs_gb300:: torch custom operators)
+
 __version__ = "1.0.0"

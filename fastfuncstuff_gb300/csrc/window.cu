@@ -111,11 +111,17 @@ struct CritArgs {
 constexpr int CRIT_TB = 16;  // steps per partial sum and sample prefetch
 
 // One CTA per tile of WTILE sorted rows that share a window centre, one thread
-// per row. Each window row's coefficients (c, -m, 1/D of its <= 5 pairs) are
-// staged in shared memory, then every thread runs the 5 recurrences over its
-// series with 16 samples in flight.
+// per row. Each window row's coefficients (-m, 1/D of its <= 5 non-identity
+// pairs, which share a and so the AR filter c_t) are staged in shared memory,
+// then every thread runs the 5 recurrences over its series with 16 samples in
+// flight. As in the surface kernel, a step whose coefficients equal the
+// previous step's reuses the registers, and a block of 16 such steps sums v^2
+// alone and scales the block sum by 1/D once.
 __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const int2* tiles, const int* n_tiles) {
-  extern __shared__ float4 tab[];  // [WIN][T]
+  extern __shared__ float2 tab[];  // [WIN][T] (-m, 1/D) of the row's pairs
+  float* cs = reinterpret_cast<float*>(tab + WIN * (size_t)w.T);  // [T] the row's AR filter c_t
+  uint8_t* steady = reinterpret_cast<uint8_t*>(cs + w.T);        // [T]
+  uint8_t* bsteady = steady + w.T;                               // [ceil(T / CRIT_TB)]
   if ((int)blockIdx.x >= *n_tiles) return;
   const int2 tl = tiles[blockIdx.x];
   const int i = tl.x + threadIdx.x;
@@ -156,6 +162,7 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
     }
     if (np == 0) continue;  // uniform over the CTA
     __syncthreads();
+    // the row's pairs share a, so one AR filter c_t; stage (-m, 1/D) per pair
     for (int idx = threadIdx.x; idx < np * T; idx += blockDim.x) {
       const int g = idx / T, t = idx % T;
       int p = pr[0];
@@ -163,38 +170,81 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
       for (int k = 1; k < WIN; ++k)
         if (g == k) p = pr[k];
       const float4 q = w.coef[(size_t)p * T + t];
-      tab[(size_t)g * T + t] = make_float4(q.x, -q.y, q.z, 0.f);
+      tab[(size_t)g * T + t] = make_float2(-q.y, q.z);
+      if (g == 0) cs[t] = q.x;
     }
     __syncthreads();
-    float vv[WIN], sb[WIN], st[WIN];
+    // steady steps: every pair's coefficients (and c) equal the previous step's
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+      bool same = t > 0 && cs[t] == cs[t - 1];
+      for (int g = 0; g < np && same; ++g) {
+        const float2 x = tab[(size_t)g * T + t], y = tab[(size_t)g * T + t - 1];
+        same = x.x == y.x && x.y == y.y;
+      }
+      steady[t] = same ? 1 : 0;
+    }
+    __syncthreads();
+    for (int bk = threadIdx.x; bk * CRIT_TB < T; bk += blockDim.x) {
+      bool all = bk * CRIT_TB + CRIT_TB <= T;
+      for (int t = bk * CRIT_TB; t < bk * CRIT_TB + CRIT_TB && all; ++t) all = steady[t] != 0;
+      bsteady[bk] = all ? 1 : 0;
+    }
+    __syncthreads();
+    float vv[WIN], sq[WIN], st[WIN], nm[WIN], id[WIN];
 #pragma unroll
-    for (int g = 0; g < WIN; ++g) vv[g] = sb[g] = st[g] = 0.f;
-    float yp = 0.f;
+    for (int g = 0; g < WIN; ++g) vv[g] = sq[g] = st[g] = nm[g] = id[g] = 0.f;
+    float yp = 0.f, c = 0.f;
     for (int t0 = 0; t0 < T; t0 += CRIT_TB) {
       float yb[CRIT_TB];
 #pragma unroll
       for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * w.n] : 0.f;
+      if (bsteady[t0 / CRIT_TB]) {
+        // CRIT_TB steady steps: coefficients in registers, sum of v^2 alone
 #pragma unroll
-      for (int k = 0; k < CRIT_TB; ++k) {
-        const int t = t0 + k;
-        if (t < T) {
-          const float y = yb[k];
+        for (int k = 0; k < CRIT_TB; ++k) {
+          const float z = fmaf(-c, yp, yb[k]);
+          yp = yb[k];
 #pragma unroll
           for (int g = 0; g < WIN; ++g) {
-            if (g < np) {
-              const float4 q = tab[(size_t)g * T + t];
-              const float z = fmaf(-q.x, yp, y);
-              vv[g] = fmaf(q.y, vv[g], z);
-              sb[g] = fmaf(vv[g] * q.z, vv[g], sb[g]);
+            vv[g] = fmaf(nm[g], vv[g], z);
+            sq[g] = fmaf(vv[g], vv[g], sq[g]);
+          }
+        }
+#pragma unroll
+        for (int g = 0; g < WIN; ++g) {
+          st[g] = fmaf(sq[g], id[g], st[g]);
+          sq[g] = 0.f;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < CRIT_TB; ++k) {
+          const int t = t0 + k;
+          if (t < T) {
+            if (!steady[t]) {
+              c = cs[t];
+#pragma unroll
+              for (int g = 0; g < WIN; ++g) {
+                if (g < np) {
+                  const float2 q = tab[(size_t)g * T + t];
+                  nm[g] = q.x;
+                  id[g] = q.y;
+                }
+              }
+            }
+            const float z = fmaf(-c, yp, yb[k]);
+            yp = yb[k];
+#pragma unroll
+            for (int g = 0; g < WIN; ++g) {
+              vv[g] = fmaf(nm[g], vv[g], z);
+              sq[g] = fmaf(vv[g] * id[g], vv[g], sq[g]);
             }
           }
-          yp = y;
         }
-      }
 #pragma unroll
-      for (int g = 0; g < WIN; ++g) {
-        st[g] += sb[g];
-        sb[g] = 0.f;
+        for (int g = 0; g < WIN; ++g) {
+          st[g] += sq[g];
+          sq[g] = 0.f;
+        }
       }
     }
 #pragma unroll
@@ -357,7 +407,7 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
   FFS_REQUIRE(lattice && idx && center && tiles && n_tiles && yr_st && coef && winproj && dcf && ident && c_p0 &&
                   best && dbest && crit0 && fallback && best_cell,
               "ffs_reml_window: null buffer");
-  const size_t smem = sizeof(float4) * WIN * (size_t)T;
+  const size_t smem = (sizeof(float2) * WIN + sizeof(float) + 1) * (size_t)T + ceil_div(T, CRIT_TB);
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_reml_window: T=%d too long", T);
   FFS_CUDA(cudaFuncSetAttribute(window_crit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, yr_st, reinterpret_cast<const float4*>(coef), winproj, dcf,
