@@ -254,34 +254,51 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
     o.info[p] = info;
   }
 
-  // ---- 5. Q = X_w Lx^-T (row by row forward substitution)
+  // ---- 5. Q = X_w Lx^-T in fp32 (Q, U and G only leave as fp32 or fp16
+  // splits; the factorisation and the logdets above stay FP64). The two [K][T]
+  // FP64 slots are reused as fp32 arrays; the QR fallback converts its Q.
+  float* const xw_f = reinterpret_cast<float*>(s.Xw);
+  float* const qm_f = reinterpret_cast<float*>(s.Qm);
+  float* const lx_f = reinterpret_cast<float*>(s.S);  // [K][K] Lx, then Li in lx_f + K*K
+  float* qf;
+  float* uf;
+  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) lx_f[idx] = (float)s.Lx[idx];
+  __syncthreads();
   if (info != 1) {
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
       for (int j = 0; j < K; ++j) {
-        double acc = s.Xw[(size_t)j * T + t];
-        for (int i = 0; i < j; ++i) acc -= s.Lx[j * K + i] * s.Qm[(size_t)i * T + t];
-        s.Qm[(size_t)j * T + t] = acc / s.Lx[j * K + j];
+        float acc = (float)s.Xw[(size_t)j * T + t];
+        for (int i = 0; i < j; ++i) acc = fmaf(-lx_f[j * K + i], qm_f[(size_t)i * T + t], acc);
+        qm_f[(size_t)j * T + t] = acc / lx_f[j * K + j];
       }
     }
+    qf = qm_f;
+    uf = xw_f;
+  } else {
+    for (int idx = threadIdx.x; idx < K * T; idx += blockDim.x) xw_f[idx] = (float)s.Qm[idx];
+    qf = xw_f;
+    uf = qm_f;
   }
   __syncthreads();
 
-  // ---- 6. U = L^-T Q = A' L~^-T D^-1/2 Q (backward recursions), into Xw's slot
-  double umax_local = 0.0;
+  // ---- 6. U = L^-T Q = A' L~^-T D^-1/2 Q (backward recursions) in fp32, with
+  // the fp32 coefficients of phase 1
+  const float4* cf = reinterpret_cast<const float4*>(o.coef) + (size_t)p * T;
+  float umax_local = 0.f;
   for (int j = threadIdx.x; j < K; j += blockDim.x) {
-    const double* q = s.Qm + (size_t)j * T;
-    double* u = s.Xw + (size_t)j * T;
-    double xn = 0.0, mn = 0.0, cn = 0.0;  // x_{t+1}, m_{t+1}, c_{t+1}
+    const float* q = qf + (size_t)j * T;
+    float* u = uf + (size_t)j * T;
+    float xn = 0.f, mn = 0.f, cn = 0.f;  // x_{t+1}, m_{t+1}, c_{t+1}
     for (int t = T - 1; t >= 0; --t) {
-      const double* cm = s.cm + 4 * t;
-      const double x = q[t] * cm[3] - mn * xn;
-      const double ut = x - cn * xn;
+      const float4 c4 = cf[t];  // (c, m, 1/D, 1/sqrt(D))
+      const float x = fmaf(-mn, xn, q[t] * c4.w);
+      const float ut = fmaf(-cn, xn, x);
       u[t] = ut;
-      o.U[((size_t)p * K + j) * T + t] = (float)ut;
-      umax_local = fmax(umax_local, fabs(ut));
+      o.U[((size_t)p * K + j) * T + t] = ut;
+      umax_local = fmaxf(umax_local, fabsf(ut));
       xn = x;
-      mn = cm[1];
-      cn = cm[0];
+      mn = c4.y;
+      cn = c4.x;
     }
   }
   __syncthreads();
@@ -302,7 +319,7 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
     for (int idx = threadIdx.x; idx < K * d.ld_u; idx += blockDim.x) {
       const int j = idx / d.ld_u, t = idx % d.ld_u;
       uint16_t hi = 0, lo = 0;
-      if (t < T) split_fp16(ldexpf((float)s.Xw[(size_t)j * T + t], e), hi, lo);
+      if (t < T) split_fp16(ldexpf(uf[(size_t)j * T + t], e), hi, lo);
       const size_t at = ((size_t)p * K + j) * d.ld_u + t;
       o.U_hi[at] = hi;
       o.U_lo[at] = lo;
@@ -321,20 +338,23 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
   }
   __syncthreads();
 
-  // ---- 8. G = U Lx^-1: row t of G solves g Lx = u_t; Gsum = G' 1 (FP64)
+  // ---- 8. G = U Lx^-1 in fp32 (row t of G solves g Lx = u_t); Gsum = G' 1
+  // accumulated in FP64
+  float* const li_f = lx_f + (size_t)K * K;
+  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) li_f[idx] = (float)s.Li[idx];
+  __syncthreads();
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
     for (int j = 0; j < K; ++j) {
-      double acc = 0.0;
-      for (int i = j; i < K; ++i) acc += s.Xw[(size_t)i * T + t] * s.Li[i * K + j];
-      o.G[((size_t)p * K + j) * T + t] = (float)acc;
-      s.Qm[(size_t)j * T + t] = acc;  // Q is no longer needed: keep G in FP64
+      float acc = 0.f;
+      for (int i = j; i < K; ++i) acc = fmaf(uf[(size_t)i * T + t], li_f[i * K + j], acc);
+      o.G[((size_t)p * K + j) * T + t] = acc;
     }
   }
   __syncthreads();
   if (o.Gsum) {
     for (int j = threadIdx.x; j < K; j += blockDim.x) {
       double acc = 0.0;
-      for (int t = 0; t < T; ++t) acc += s.Qm[(size_t)j * T + t];
+      for (int t = 0; t < T; ++t) acc += (double)o.G[((size_t)p * K + j) * T + t];
       o.Gsum[(size_t)p * K + j] = (float)acc;
     }
   }

@@ -157,12 +157,20 @@ class GridFactors:
         return self.grid.P
 
 
-def constant_in_span(X: np.ndarray, tol: float = 1e-6) -> bool:
-    """True when the constant series lies in the column span of X (FP64 least squares)."""
+def constant_coefficients(X: np.ndarray, tol: float = 1e-6) -> np.ndarray | None:
+    """c with X c = 1 (FP64 least squares) when the constant series lies in the
+    column span of X, else None."""
     Xd = np.asarray(X, dtype=np.float64)
     ones = np.ones(Xd.shape[0])
     coef, *_ = np.linalg.lstsq(Xd, ones, rcond=None)
-    return float(np.linalg.norm(Xd @ coef - ones)) <= tol * np.sqrt(Xd.shape[0])
+    if float(np.linalg.norm(Xd @ coef - ones)) <= tol * np.sqrt(Xd.shape[0]):
+        return coef
+    return None
+
+
+def constant_in_span(X: np.ndarray, tol: float = 1e-6) -> bool:
+    """True when the constant series lies in the column span of X (FP64 least squares)."""
+    return constant_coefficients(X, tol) is not None
 
 
 def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_indices=None,
@@ -190,6 +198,7 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     nt = 0 if task_idx is None else task_idx.numel()
     ng = 0 if glt_t is None else glt_t.shape[0]
     lib = _lib.load()
+    ccoef = constant_coefficients(X.detach().cpu().numpy())
     work = torch.empty(int(lib.ffs_grid_work_bytes(T, K, P)) // 8 + 1, dtype=torch.float64, device=dev)
     f = GridFactors(
         grid=grid, T=T, K=K, ld=ld,
@@ -211,7 +220,7 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
         lattice=const_dev(grid.lattice.reshape(-1), dev),
         task_idx=task_idx, glt=glt_t,
         Gsum=torch.empty(P, K, **f32),
-        center=constant_in_span(X.detach().cpu().numpy()),
+        center=ccoef is not None,
         uexp=torch.empty(P, dtype=torch.int32, device=dev) if with_tc else None,
     )
     d = _lib.GridDesc(T=T, K=K, P=P, n_runs=layout.n_runs, run_start=_p(run_start), tau=_p(tau),
@@ -222,6 +231,10 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
                      info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=_p(f.Gsum),
                      work=_p(work))
     _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
+    if ccoef is not None:
+        # G' X = I for every pair, so G'1 = c exactly: the centring correction
+        # of the GLS uses the FP64 coefficients rather than the fp32 G's sums
+        f.Gsum = const_dev(ccoef.astype(np.float32), dev).reshape(1, K).expand(P, K).contiguous()
     f._keep = (Xc, run_start, tau, work)  # inputs must outlive the launch
     return f
 
