@@ -48,7 +48,7 @@ class PrepArgs(C.Structure):
         ("yr_t", C.c_void_p),
         ("yr_hi", C.c_void_p), ("yr_lo", C.c_void_p), ("yexp", C.c_void_p),
         ("idx", C.c_void_p), ("feats", C.c_void_p), ("n_runs", C.c_int), ("run_start", C.c_void_p),
-        ("yr_rows", C.c_void_p),
+        ("yr_rows", C.c_void_p), ("center_dev", C.c_void_p),
     ]
 
 
@@ -93,7 +93,7 @@ class GlsArgs(C.Structure):
         ("betas", C.c_void_p), ("tstats", C.c_void_p), ("sigma2", C.c_void_p),
         ("fstats", C.c_void_p), ("r2", C.c_void_p), ("lam", C.c_void_p),
         ("cbeta", C.c_void_p), ("ct", C.c_void_p), ("resid", C.c_void_p),
-        ("resid_w", C.c_void_p), ("pred", C.c_void_p),
+        ("resid_w", C.c_void_p), ("pred", C.c_void_p), ("center_dev", C.c_void_p),
     ]
 
 

@@ -44,7 +44,7 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
   // residuals, sigma2, R^2 and the t of every column but the constant's are
   // unchanged because the constant lies in span(X)
   float m = 0.f;
-  if (a.center) {
+  if (a.center_dev ? (*a.center_dev != 0) : (a.center != 0)) {
     float sm_ = 0.f;
     for (int t = lane; t < T; t += 32) sm_ += y[t];
     m = warp_sum(sm_) / (float)T;
@@ -137,7 +137,7 @@ __device__ void gls_finish(const ffs_gls_args& a, const GlsExtra& x, const int v
   const float sigma2 = ssw / (float)a.dof;
 
   // betas of the uncentred data: add (m/s) * G'1
-  if (a.center) {
+  if (a.center_dev ? (*a.center_dev != 0) : (a.center != 0)) {
     const float ms = m / sc;
     for (int j = lane; j < K; j += 32) beta[j] = fmaf(ms, a.Gsum[(size_t)g * K + j], beta[j]);
   }
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
     const float sc = a.scale[v];
     const float4* y4 = reinterpret_cast<const float4*>(a.Y + (size_t)v * T);
     float m = 0.f;
-    if (a.center) {
+    if (a.center_dev ? (*a.center_dev != 0) : (a.center != 0)) {
       float s = 0.f;
       for (int q = lane; q < nq; q += 32) {
         const float4 y = y4[q];
@@ -507,7 +507,7 @@ extern "C" int ffs_reml_gls_ex(const ffs_gls_args* a, int lj_h, const int* lj_ta
                   a->a && a->b && a->betas && a->tstats && a->sigma2 && a->fstats && a->r2 && a->lam,
               "ffs_reml_gls: null buffer");
   FFS_REQUIRE(a->n_task == 0 || (a->task_idx && a->Ftask), "ffs_reml_gls: task columns need Ftask");
-  FFS_REQUIRE(!a->center || a->Gsum, "ffs_reml_gls: centring needs Gsum");
+  FFS_REQUIRE((!a->center && !a->center_dev) || a->Gsum, "ffs_reml_gls: centring needs Gsum");
   FFS_REQUIRE(a->n_glt == 0 || (a->glt && a->glt_var && a->cbeta && a->ct), "ffs_reml_gls: GLT buffers");
   FFS_REQUIRE(lj_h >= 0 && lj_h <= a->T / 2, "ffs_reml_gls: Ljung-Box lag %d out of range", lj_h);
   FFS_REQUIRE(lj_h == 0 || (lj_w && ljung_box), "ffs_reml_gls: Ljung-Box buffers");
@@ -531,7 +531,7 @@ extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* 
                   a->betas && a->tstats && a->sigma2 && a->fstats && a->r2 && a->lam,
               "ffs_reml_gls_grouped: null buffer");
   FFS_REQUIRE(a->n_task == 0 || (a->task_idx && a->Ftask), "ffs_reml_gls_grouped: task columns need Ftask");
-  FFS_REQUIRE(!a->center || a->Gsum, "ffs_reml_gls_grouped: centring needs Gsum");
+  FFS_REQUIRE((!a->center && !a->center_dev) || a->Gsum, "ffs_reml_gls_grouped: centring needs Gsum");
   FFS_REQUIRE(a->n_glt == 0 || (a->glt && a->glt_var && a->cbeta && a->ct), "ffs_reml_gls_grouped: GLT buffers");
   FFS_REQUIRE(lj_h >= 0 && lj_h <= a->T / 2, "ffs_reml_gls_grouped: Ljung-Box lag %d out of range", lj_h);
   FFS_REQUIRE(lj_h == 0 || (lj_w && ljung_box), "ffs_reml_gls_grouped: Ljung-Box buffers");

@@ -13,6 +13,10 @@ namespace ffsk {
 namespace {
 
 // ------------------------------------------------------------------------ prep
+__device__ __forceinline__ bool centre_on(const ffs_prep_args& a) {
+  return a.center_dev ? (*a.center_dev != 0) : (a.center != 0);
+}
+
 // Lag 1..8 autocorrelations of one residualised row within runs (products
 // never cross a run boundary) and T/1000, by one warp; lane 0 writes out[9].
 __device__ void row_features(const float* row, int T, int n_runs, const int* run_start, float* out) {
@@ -77,7 +81,7 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
     }
     // centring is one subtraction per sample, rounded relative to its (small)
     // result; the criterion ignores the constant when it lies in span(X)
-    const float m = a.center ? mean : 0.f;
+    const float m = centre_on(a) ? mean : 0.f;
     for (int t = lane; t < T; t += 32) row[t] = __fdiv_rn(__fsub_rn(row[t], m), sc);
     __syncwarp();
     // residualise: row -= Q0 (Q0' row)
@@ -165,7 +169,7 @@ __global__ void __launch_bounds__(TILE_WARPS * 32) prep_tile_kernel(ffs_prep_arg
       sc = sqrtf(sq / (float)(T - 1));
       sc = fmaxf(sc, 1e-8f);
     }
-    const float m = a.center ? mean : 0.f;
+    const float m = centre_on(a) ? mean : 0.f;
     for (int t = lane; t < T; t += 32) row[t] = __fdiv_rn(__fsub_rn(row[t], m), sc);
     if (lane == 0) a.scale[vs] = sc;
   }

@@ -53,6 +53,8 @@ __global__ void window_items_kernel(int ncell, const int* end, int n_a, int n_b,
     }
     tiles[tt + t] = make_int2(s0 + t * WTILE, min(WTILE, n - t * WTILE));
   }
+  // the window's runs of consecutive valid pairs (at most one per pair)
+  int seg_p[WSLOTS], seg_np[WSLOTS], seg_slot[WSLOTS], nseg = 0;
   for (int ra = 0; ra < wa; ++ra) {
     int rb = 0;
     while (rb < wb) {
@@ -61,25 +63,32 @@ __global__ void window_items_kernel(int ncell, const int* end, int n_a, int n_b,
         ++rb;
         continue;
       }
-      // run of consecutive pair indices along the row
       int np = 1;
       while (rb + np < wb && np < max_pairs && lattice[(a0 + ra) * n_b + b0 + rb + np] == p + np) ++np;
-      const int at = atomicAdd(n_items, ntile);
-      for (int t = 0; t < ntile; ++t) {
-        if (at + t >= max_items) {
-          atomicExch(overflow, 1);
-          break;
-        }
-        ffs_tc_item it;
-        it.v0 = s0 + t * WTILE;
-        it.nv = min(WTILE, n - t * WTILE);
-        it.row_b = p * K;
-        it.np = np;
-        it.out0 = it.v0;
-        it.slot0 = ra * WIN + rb;
-        items[at + t] = it;
-      }
+      seg_p[nseg] = p;
+      seg_np[nseg] = np;
+      seg_slot[nseg++] = ra * WIN + rb;
       rb += np;
+    }
+  }
+  // tile-major: the segments of one operand tile are consecutive items, so
+  // the CTAs that take them at the same time share the tile in L2
+  const int at = atomicAdd(n_items, ntile * nseg);
+  for (int t = 0; t < ntile; ++t) {
+    for (int sg = 0; sg < nseg; ++sg) {
+      const int k = at + t * nseg + sg;
+      if (k >= max_items) {
+        atomicExch(overflow, 1);
+        return;
+      }
+      ffs_tc_item it;
+      it.v0 = s0 + t * WTILE;
+      it.nv = min(WTILE, n - t * WTILE);
+      it.row_b = seg_p[sg] * K;
+      it.np = seg_np[sg];
+      it.out0 = it.v0;
+      it.slot0 = seg_slot[sg];
+      items[k] = it;
     }
   }
 }

@@ -338,13 +338,32 @@ def fit_glm_arma11(
     for v0 in range(0, V, bs):
         v1 = min(V, v0 + bs)
         Yb = Y[v0:v1].to(device=device, dtype=torch.float32, non_blocking=True)
+        go = None
         if best_all is None and proposal is not None:
+            # the GLS of every voxel at its window's pair is queued before the
+            # host waits for the list of fallback voxels; their rows are redone
+            first = {}
+
+            def gls_first(best_w, scale_w):
+                first["go"] = engine.gls(Yb, scale_w, best_w, factors, Xd, want_residuals=want_residuals,
+                                         want_predicted=want_predicted, lj=lj)
+
             lo = learned.learned_search(Yb, factors, proposal, layout_l, do_scale=not use_double,
-                                        recenter=proposal_recenter)
+                                        recenter=proposal_recenter, before_fallback=gls_first)
             best, scale = lo.best, lo.scale
             chunks["best"].append(best)
             chunks["crit"].append(lo.best_crit)
             fallbacks.append(lo.fallback)
+            go = first["go"]
+            sel = lo.fallback_idx
+            if sel.numel():
+                gs = engine.gls(Yb.index_select(0, sel), scale.index_select(0, sel), best.index_select(0, sel),
+                                factors, Xd, want_residuals=want_residuals, want_predicted=want_predicted, lj=lj)
+                for fld in ("betas", "tstats", "sigma2", "fstats", "r2", "lam", "cbeta", "ct", "resid",
+                            "resid_w", "pred", "ljung_box"):
+                    t_all, t_sub = getattr(go, fld), getattr(gs, fld)
+                    if t_all is not None:
+                        t_all.index_copy_(0, sel, t_sub)
         elif best_all is None:
             so = engine.search(Yb, factors, hierarchical=not force_exhaustive_search, projector=proj,
                                do_scale=not use_double, keep_surface=save_profile_likelihoods)
@@ -357,8 +376,9 @@ def fit_glm_arma11(
             best = best_all[v0:v1].to(device)
             scale = _voxel_scale(Yb, not use_double)
             chunks["best"].append(best)
-        go = engine.gls(Yb, scale, best, factors, Xd, want_residuals=want_residuals,
-                        want_predicted=want_predicted, lj=lj)
+        if go is None:
+            go = engine.gls(Yb, scale, best, factors, Xd, want_residuals=want_residuals,
+                            want_predicted=want_predicted, lj=lj)
         for name, t in (("betas", go.betas), ("tstats", go.tstats), ("sigma2", go.sigma2),
                         ("fstats", go.fstats), ("r2", go.r2), ("lam", go.lam), ("cb", go.cbeta),
                         ("ct", go.ct), ("resid", go.resid), ("resid_w", go.resid_w), ("pred", go.pred),

@@ -18,6 +18,7 @@ Layouts (V voxels, T time points, K design columns, P pairs):
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -149,12 +150,27 @@ class GridFactors:
     task_idx: torch.Tensor | None
     glt: torch.Tensor | None
     Gsum: torch.Tensor | None = None
-    center: bool = False
+    center_flag: torch.Tensor | None = None  # device int32[1]: centre the voxels (constant in span(X))
     uexp: torch.Tensor | None = None
 
     @property
     def P(self) -> int:
         return self.grid.P
+
+
+def constant_flag(X: torch.Tensor, tol: float = 1e-6) -> tuple[torch.Tensor, torch.Tensor]:
+    """On X's device, without a host round trip: (flag int32[1], c float32[K])
+    with flag = 1 and X c = 1 (FP64 normal equations) when the constant series
+    lies in the column span of X, flag = 0 and c = 0 otherwise."""
+    Xd = X.detach().to(torch.float64)
+    T, K = Xd.shape
+    ones = torch.ones(T, 1, dtype=torch.float64, device=Xd.device)
+    L, info = torch.linalg.cholesky_ex(Xd.T @ Xd)
+    c = torch.cholesky_solve(Xd.T @ ones, L)
+    res = torch.linalg.vector_norm(Xd @ c - ones)
+    ok = (info == 0) & (res <= tol * math.sqrt(T))  # a failed factorisation gives NaN: not ok
+    c = torch.where(ok, c.reshape(-1), torch.zeros(K, dtype=torch.float64, device=Xd.device))
+    return ok.to(torch.int32).reshape(1), c.to(torch.float32)
 
 
 def constant_coefficients(X: np.ndarray, tol: float = 1e-6) -> np.ndarray | None:
@@ -198,7 +214,7 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     nt = 0 if task_idx is None else task_idx.numel()
     ng = 0 if glt_t is None else glt_t.shape[0]
     lib = _lib.load()
-    ccoef = constant_coefficients(X.detach().cpu().numpy())
+    cflag, ccoef = constant_flag(Xc)
     work = torch.empty(int(lib.ffs_grid_work_bytes(T, K, P)) // 8 + 1, dtype=torch.float64, device=dev)
     f = GridFactors(
         grid=grid, T=T, K=K, ld=ld,
@@ -220,7 +236,7 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
         lattice=const_dev(grid.lattice.reshape(-1), dev),
         task_idx=task_idx, glt=glt_t,
         Gsum=torch.empty(P, K, **f32),
-        center=ccoef is not None,
+        center_flag=cflag,
         uexp=torch.empty(P, dtype=torch.int32, device=dev) if with_tc else None,
     )
     d = _lib.GridDesc(T=T, K=K, P=P, n_runs=layout.n_runs, run_start=_p(run_start), tau=_p(tau),
@@ -231,10 +247,10 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
                      info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=_p(f.Gsum),
                      work=_p(work))
     _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
-    if ccoef is not None:
-        # G' X = I for every pair, so G'1 = c exactly: the centring correction
-        # of the GLS uses the FP64 coefficients rather than the fp32 G's sums
-        f.Gsum = const_dev(ccoef.astype(np.float32), dev).reshape(1, K).expand(P, K).contiguous()
+    # G' X = I for every pair, so G'1 = c exactly when the constant is in
+    # span(X): the centring correction of the GLS uses the FP64 coefficients
+    # rather than sums of the fp32 G (the flag decides on the device)
+    f.Gsum = ccoef.reshape(1, K).expand(P, K).contiguous()
     f._keep = (Xc, run_start, tau, work)  # inputs must outlive the launch
     return f
 
@@ -288,10 +304,10 @@ def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core:
         rs = const_dev(layout.run_start, dev)
     rows = torch.empty(n, T, dtype=torch.float32, device=dev) if want_rows else None
     q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T])
-    pa = _lib.PrepArgs(V=n, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=int(f.center), ld_y=ld,
+    pa = _lib.PrepArgs(V=n, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=0, ld_y=ld,
                        scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp),
                        idx=_p(idx), feats=_p(feats), n_runs=0 if layout is None else layout.n_runs,
-                       run_start=_p(rs), yr_rows=_p(rows))
+                       run_start=_p(rs), yr_rows=_p(rows), center_dev=_p(f.center_flag))
     _run("ffs_reml_prep", lib.ffs_reml_prep, C.byref(pa), _stream())
     out = PrepOut(scale, yr_t, yr_hi, yr_lo, yexp)
     out.feats = feats
@@ -391,14 +407,14 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
                resid_w=torch.empty(V, T, **f32) if want_residuals else None,
                pred=torch.empty(V, T, **f32) if want_predicted else None)
     nt = 0 if f.task_idx is None else f.task_idx.numel()
-    ga = _lib.GlsArgs(V=V, T=T, K=K, dof=max(1, T - K), center=int(f.center), Gsum=_p(f.Gsum), Y=_p(Y),
+    ga = _lib.GlsArgs(V=V, T=T, K=K, dof=max(1, T - K), center=0, Gsum=_p(f.Gsum), Y=_p(Y),
                       scale=_p(scale), Xt=_p(Xt), best=_p(best),
                       order=_p(order), coef=_p(f.coef), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
                       a=_p(f.a), b=_p(f.b), lambda_fp32=int(f.grid.lambda_fp32), n_task=nt,
                       task_idx=_p(f.task_idx), Ftask=_p(f.Ftask), n_glt=ng, glt=_p(f.glt),
                       glt_var=_p(f.glt_var), betas=_p(o.betas), tstats=_p(o.tstats), sigma2=_p(o.sigma2),
                       fstats=_p(o.fstats), r2=_p(o.r2), lam=_p(o.lam), cbeta=_p(o.cbeta), ct=_p(o.ct),
-                      resid=_p(o.resid), resid_w=_p(o.resid_w), pred=_p(o.pred))
+                      resid=_p(o.resid), resid_w=_p(o.resid_w), pred=_p(o.pred), center_dev=_p(f.center_flag))
     h, ptau_d, w_d = 0, None, None
     if lj is not None and lj[0] > 0:
         h, ptau, w, _ = lj

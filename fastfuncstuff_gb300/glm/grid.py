@@ -188,6 +188,11 @@ def make_grid(a_grid, b_grid, use_double: bool = False) -> RemlGrid:
     fastfuncstuff/glm/arma.py:1339-1342 does before ``build_arma11_covariance_batch``.
     """
     ag, bg = ensure_zero_in_grid(a_grid, b_grid)
+    key = (ag.numpy().tobytes(), bg.numpy().tobytes(), bool(use_double), _REML_MODE.afni_faithful,
+           float(_REML_MODE.corcut))
+    hit = _GRID_CACHE.get(key)
+    if hit is not None:
+        return hit
     dt = torch.float64 if use_double else torch.float32
     am, bm = torch.meshgrid(ag.to(dt), bg.to(dt), indexing="ij")
     a, b = am.reshape(-1), bm.reshape(-1)
@@ -208,9 +213,17 @@ def make_grid(a_grid, b_grid, use_double: bool = False) -> RemlGrid:
     if p0 < 0:
         raise ValueError("the (0, 0) pair is missing from the valid grid")
     chunk_start, chunk_pairs = coefficient_chunks(a, b)
-    return RemlGrid(a=a, b=b, a_axis=a_axis, b_axis=b_axis, lattice=lattice, p0=p0, za=za, zb=zb,
-                    ltop=hierarchical_ltop(len(a_axis), len(b_axis), _REML_MODE.afni_faithful),
-                    chunk_start=chunk_start, chunk_pairs=chunk_pairs, lambda_fp32=not use_double)
+    g = RemlGrid(a=a, b=b, a_axis=a_axis, b_axis=b_axis, lattice=lattice, p0=p0, za=za, zb=zb,
+                 ltop=hierarchical_ltop(len(a_axis), len(b_axis), _REML_MODE.afni_faithful),
+                 chunk_start=chunk_start, chunk_pairs=chunk_pairs, lambda_fp32=not use_double)
+    if len(_GRID_CACHE) > 64:
+        _GRID_CACHE.clear()
+    _GRID_CACHE[key] = g
+    return g
+
+
+# grids by (axes, dtype, AFNI mode): the host-side setup of repeated fits
+_GRID_CACHE: dict = {}
 
 
 def grid_of_pairs(a: np.ndarray, b: np.ndarray, use_double: bool = False) -> RemlGrid:

@@ -282,7 +282,7 @@ def _window_round(pre, f, cen, out, *, flag):
 
 
 def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
-                   do_scale: bool = True, recenter: int = 0) -> LearnedOut:
+                   do_scale: bool = True, recenter: int = 0, before_fallback=None) -> LearnedOut:
     """Learned-seeded REML search: the 5 x 5 window around each proposal, the
     full grid for voxels whose best pair sits on the window edge (or whose
     window, holding no identity pair, has nothing below the identity pairs'
@@ -290,7 +290,10 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
 
     ``recenter`` > 0 first re-evaluates such voxels that many times with the
     window centred on their best pair; the full grid then takes those still on
-    an edge.
+    an edge. ``before_fallback(best, scale)`` is called (with the windows'
+    answer for every voxel) before the one host round trip that lists the
+    fallback voxels, so work it enqueues keeps the GPU busy meanwhile;
+    ``LearnedOut.fallback_idx`` lists the voxels whose pair changed after it.
     """
     lib = _lib.load()
     dev = Y.device
@@ -328,15 +331,26 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
     best_crit = (out["crit0"] + out["dbest"].double()).float()
     best = out["best"]
     fb = out["fb"]
+    # the host needs three numbers (fallback count, wait flag, list overflow):
+    # copy them to pinned memory behind an event, queue the caller's work, and
+    # wait for that event only
+    small = torch.stack([fb.sum().to(torch.int32), flag[0]] + [cn[1] for cn in counts])
+    host = torch.empty(small.numel(), dtype=torch.int32, pin_memory=True)
+    host.copy_(small, non_blocking=True)
+    ready = torch.cuda.Event()
+    ready.record()
+    if before_fallback is not None:
+        before_fallback(best.clone(), scale)
+    ready.synchronize()
     # the full grid for the voxels still on a window edge
-    # one host round trip: the fallback list, the wait flag and the overflow counts
-    bad = torch.stack([flag[0]] + [cn[1] for cn in counts])
-    sel = torch.nonzero(fb, as_tuple=True)[0]
-    bad = bad.cpu()
-    if int(bad[0]) != 0:
-        raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {int(bad[0])})")
-    if bool((bad[1:] != 0).any()):
+    n_fb, code = int(host[0]), int(host[1])
+    if code != 0:
+        raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {code})")
+    if bool((host[2:] != 0).any()):
         raise RuntimeError("ffs_reml_window_items: work list overflow")
+    # the fallback voxels' ids in order, compacted on the device
+    pos = torch.where(fb != 0, torch.cumsum(fb, 0) - 1, torch.full_like(fb, n_fb)).long()
+    sel = torch.empty(n_fb + 1, dtype=torch.long, device=dev).scatter_(0, pos, torch.arange(V, device=dev))[:n_fb]
     if stats["edge_first"] is None:
         stats["edge_first"] = sel.numel() / V
     stats["fallback"] = sel.numel() / V
@@ -345,7 +359,9 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
         so = engine.search(Y.index_select(0, sel), f, hierarchical=False, projector="tc", do_scale=do_scale)
         best.index_copy_(0, sel, so.best)
         best_crit.index_copy_(0, sel, so.best_crit)
-    return LearnedOut(best=best, best_crit=best_crit, scale=scale, fallback=fb, proposal=prop, stats=stats)
+    lo = LearnedOut(best=best, best_crit=best_crit, scale=scale, fallback=fb, proposal=prop, stats=stats)
+    lo.fallback_idx = sel
+    return lo
 
 
 def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxels: int = 2_000_000,

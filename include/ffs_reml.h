@@ -172,6 +172,8 @@ typedef struct {
   int n_runs;
   const int* run_start;
   float* yr_rows;       /* NULL, or [V][T] the residualised rows, voxel-major    */
+  const int* center_dev;/* NULL, or a device int that replaces `center` (set by
+                           the caller's stream, so deciding needs no host sync) */
 } ffs_prep_args;
 
 int ffs_reml_prep(const ffs_prep_args* a, void* stream);
@@ -300,6 +302,7 @@ typedef struct {
   float* sigma2; float* fstats; float* r2; float* lam;   /* [V]                  */
   float* cbeta; float* ct;                           /* [V][n_glt] or NULL        */
   float* resid; float* resid_w; float* pred;         /* [V][T] or NULL            */
+  const int* center_dev; /* NULL, or a device int that replaces `center`        */
 } ffs_gls_args;
 
 int ffs_reml_gls(const ffs_gls_args* a, void* stream);

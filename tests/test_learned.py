@@ -256,3 +256,32 @@ def test_window_round_matches_full_grid_surface():
         if best[v] == p_ref:
             assert fb[v] == exp_fb, v
     assert agree / V >= 0.999, agree / V
+
+
+@pytest.mark.gpu
+def test_fit_with_proposal_matches_full_grid_fit_where_pairs_agree():
+    """fit_glm_arma11(proposal=...) queues the GLS of every voxel at its window
+    pair, then redoes the fallback voxels at their full-grid pair: wherever the
+    pair agrees with the full-grid fit the GLS outputs are identical (same
+    kernels, same inputs), fallback voxels included."""
+    from fastfuncstuff_gb300 import fit_glm_arma11, synth
+    from fastfuncstuff_gb300.glm import learned
+    from fastfuncstuff_gb300.glm import grid as G
+
+    dev = torch.device("cuda:0")
+    w = synth.workload(1, V=6000)
+    lay = G.run_layout(w.T, w.run_starts)
+    X = torch.from_numpy(w.X).to(dev)
+    Y = torch.from_numpy(w.Y).to(dev)
+    gr = torch.linspace(-0.8, 0.8, 33)
+    prop, _ = learned.train_proposal(X, lay, gr, gr, n_voxels=300_000, epochs=6)
+    kw = dict(tr=2.0, a_grid=gr, b_grid=gr, run_starts=w.run_starts, device=dev, verbose=False,
+              force_exhaustive_search=True, return_device=True, want_residuals=True)
+    full = fit_glm_arma11(Y, X, **kw)
+    got = fit_glm_arma11(Y, X, proposal=prop, proposal_recenter=1, **kw)
+    same = (got.arma_params == full.arma_params).all(1)
+    assert float(same.float().mean()) >= 0.97
+    assert 0.0 < float(got.learned_fallback) < 0.5  # some voxels took the fallback path
+    for name in ("betas", "tstats", "sigma2", "fstats", "r2", "arma_lambda", "residuals", "residuals_whitened"):
+        a, b = getattr(got, name)[same], getattr(full, name)[same]
+        assert torch.equal(a, b), name
