@@ -8,6 +8,10 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "../../include/ffs_reml.h"
 
 namespace ffsk {
@@ -98,5 +102,40 @@ __device__ __forceinline__ float lambda_out_f32(float a, float b) {
 }
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) only when a kernel needs
+// more than it was last given on this device: launches then make no other
+// runtime call than the launch itself (also while a stream is being captured).
+inline cudaError_t ensure_dyn_smem(const void* fn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& have = done[{fn, dev}];
+  if (bytes <= have) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) have = bytes;
+  return e;
+}
+
+// SM count of the current device, looked up once per device
+inline cudaError_t sm_count(int* n) {
+  static std::mutex mu;
+  static std::map<int, int> known;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = known.find(dev);
+  if (it != known.end()) {
+    *n = it->second;
+    return cudaSuccess;
+  }
+  e = cudaDeviceGetAttribute(n, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) known[dev] = *n;
+  return e;
+}
 
 }  // namespace ffsk

@@ -259,8 +259,8 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
   float* Ys = reinterpret_cast<float*>(sm4);        // [32][ld]
   float* C0 = Ys + (size_t)TILE_V * ld;             // [K][32] b0
   float* C1 = C0 + (size_t)K * TILE_V;              // [K][32] d
-  float* part = C1 + (size_t)K * TILE_V;            // [2][K][32]
-  float* red = part + 2 * (size_t)K * TILE_V;       // [3][8][32] SS_res, SS_tot, SS_w partials
+  float* part = C1 + (size_t)K * TILE_V;            // [TILE_TS][K][32]
+  float* red = part + TILE_TS * (size_t)K * TILE_V;  // [3][8][32] SS_res, SS_tot, SS_w partials
   float* vend = red + 3 * TILE_WARPS * TILE_V;      // [8][32]
   float* carry = vend + TILE_WARPS * TILE_V;        // [8][32]
   float* Hs = carry + TILE_WARPS * TILE_V;          // [32]
@@ -516,7 +516,7 @@ extern "C" int ffs_reml_gls_ex(const ffs_gls_args* a, int lj_h, const int* lj_ta
   const int hb = (lj_h + 4) & ~3;
   const size_t smem = sizeof(float) * GLS_WARPS * (size_t)(2 * ld_s + kp + hb);
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_gls: T=%d too long", a->T);
-  FFS_CUDA(cudaFuncSetAttribute(gls_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(gls_kernel), smem));
   GlsExtra x{lj_h, lj_tau, lj_w, ljung_box};
   gls_kernel<<<ceil_div(a->V, GLS_WARPS), GLS_WARPS * 32, smem, (cudaStream_t)stream>>>(*a, x, ld_s, kp, hb);
   return check_launch("gls_kernel");
@@ -538,7 +538,7 @@ extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* 
   const int ld = tile_ld(a->T);
   const int kp = (a->K + 3) & ~3;
   const int hb = (lj_h + 4) & ~3;
-  const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + 4 * (size_t)a->K * TILE_V +
+  const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + (2 + TILE_TS) * (size_t)a->K * TILE_V +
                                        (3 + 2) * TILE_WARPS * TILE_V + TILE_V + 6 * TILE_V +
                                        (size_t)TILE_WARPS * (kp + hb));
   if (a->T % 4 != 0 || smem > 200 * 1024) {  // no 16-byte rows, or the tile does not fit: one warp per voxel
@@ -547,7 +547,7 @@ extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* 
   cudaStream_t st = (cudaStream_t)stream;
   GlsExtra x{lj_h, lj_tau, lj_w, ljung_box};
   gls_tile_scan<<<1, 1024, 0, st>>>(P, group_end, tile_start);
-  FFS_CUDA(cudaFuncSetAttribute(gls_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(gls_tile_kernel), smem));
   const int max_tiles = ceil_div(a->V, GLS_TILE) + P;
   gls_tile_kernel<<<max_tiles, TILE_WARPS * 32, smem, st>>>(*a, x, group_end, tile_start, P, ld, kp, hb);
   return check_launch("gls_tile_kernel");

@@ -389,9 +389,80 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
   }
 }
 
+// Orthonormal basis of the design's columns, Q0 = X Lx^-T with Lx the FP64
+// Cholesky factor of X'X (Q0 is U of the pair (0, 0), R = I); modified
+// Gram-Schmidt, twice, when X'X is not positive definite. One CTA. work:
+// [K][K] + [K][T] doubles.
+__global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const float* X, double* work, float* Q0,
+                                                           int* info) {
+  __shared__ double red[32];
+  __shared__ int flag;
+  double* M = work;                    // [K][K]
+  double* Qd = work + (size_t)K * K;   // [K][T] (QR fallback)
+  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
+    const int i = idx / K, j = idx % K;
+    if (j > i) continue;
+    double acc = 0.0;
+    for (int t = 0; t < T; ++t) acc += (double)X[(size_t)t * K + i] * (double)X[(size_t)t * K + j];
+    M[i * K + j] = acc;
+    M[j * K + i] = acc;
+  }
+  __syncthreads();
+  if (block_cholesky(M, K, K, &flag)) {
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+      for (int j = 0; j < K; ++j) {
+        float acc = X[(size_t)t * K + j];
+        for (int i = 0; i < j; ++i) acc = fmaf(-(float)M[j * K + i], Q0[(size_t)i * T + t], acc);
+        Q0[(size_t)j * T + t] = acc / (float)M[j * K + j];
+      }
+    }
+    if (threadIdx.x == 0) *info = 0;
+    return;
+  }
+  // QR of X by modified Gram-Schmidt (twice) in FP64
+  for (int j = 0; j < K; ++j) {
+    double* q = Qd + (size_t)j * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] = (double)X[(size_t)t * K + j];
+    __syncthreads();
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int i = 0; i < j; ++i) {
+        const double* qi = Qd + (size_t)i * T;
+        double part = 0.0;
+        for (int t = threadIdx.x; t < T; t += blockDim.x) part += qi[t] * q[t];
+        const double rij = block_sum(part, red);
+        for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] -= rij * qi[t];
+        __syncthreads();
+      }
+    }
+    double part = 0.0;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) part += q[t] * q[t];
+    const double nrm = sqrt(block_sum(part, red));
+    const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+      q[t] *= inv;
+      Q0[(size_t)j * T + t] = (float)q[t];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *info = 1;
+}
+
 }  // namespace
 
 }  // namespace ffsk
+
+extern "C" size_t ffs_design_basis_work_bytes(int T, int K) {
+  return sizeof(double) * ((size_t)K * K + (size_t)K * T);
+}
+
+extern "C" int ffs_design_basis(int T, int K, const float* X, void* work, float* Q0, int* info, void* stream) {
+  using namespace ffsk;
+  clear_error();
+  FFS_REQUIRE(T > 0 && K > 0 && K <= T, "ffs_design_basis: T=%d K=%d", T, K);
+  FFS_REQUIRE(X && work && Q0 && info, "ffs_design_basis: null buffer");
+  design_basis_kernel<<<1, 256, 0, (cudaStream_t)stream>>>(T, K, X, static_cast<double*>(work), Q0, info);
+  return check_launch("design_basis_kernel");
+}
 
 extern "C" size_t ffs_grid_work_bytes(int T, int K, int P) {
   return sizeof(double) * ffsk::pair_doubles(T, K) * (size_t)P;

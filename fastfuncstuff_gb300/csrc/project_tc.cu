@@ -372,10 +372,9 @@ int launch_tc(const ffs_project_args* a, const TcParams& prm, int max_items, voi
   const size_t smem = (size_t)STAGES * stage_bytes + 1024 + 128;
   FFS_REQUIRE(smem <= 227 * 1024, "project_tc: tile needs %zu bytes of shared memory", smem);
   auto kern = prm.items ? project_tc_kernel<true> : project_tc_kernel<false>;
-  FFS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int dev = 0, n_sm = 0;
-  FFS_CUDA(cudaGetDevice(&dev));
-  FFS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(kern), smem));
+  int n_sm = 0;
+  FFS_CUDA(sm_count(&n_sm));
   if (max_items <= 0) return FFS_OK;
   kern<<<min(max_items, n_sm), 192, smem, (cudaStream_t)stream>>>(ta_hi, ta_lo, tb_hi, tb_lo, prm);
   return check_launch("project_tc_kernel");

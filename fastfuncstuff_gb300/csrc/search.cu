@@ -131,11 +131,11 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
 // c = Q0 y and the update y -= Q0' c as register-blocked passes over the tile
 // (tile.cuh), i.e. y - Q0'(Q0 y) in one step as the reference's
 // Y - (Y pinv(X)') X' (fastfuncstuff/glm/arma.py:1554-1571).
-__global__ void __launch_bounds__(TILE_WARPS * 32) prep_tile_kernel(ffs_prep_args a, int ld) {
+__global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_args a, int ld) {
   extern __shared__ float4 sm4[];
   float* Ys = reinterpret_cast<float*>(sm4);       // [32][ld]
   float* Cq = Ys + (size_t)TILE_V * ld;            // [K][32]
-  float* part = Cq + (size_t)a.K * TILE_V;         // [2][K][32]
+  float* part = Cq + (size_t)a.K * TILE_V;         // [TILE_TS][K][32]
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int T = a.T, K = a.K, nq = T >> 2;
   const int v0 = blockIdx.x * TILE_V;
@@ -623,9 +623,9 @@ extern "C" int ffs_reml_prep(const ffs_prep_args* a, void* stream) {
               "ffs_reml_prep: ld_y=%d must be >= T and a multiple of 8", a->ld_y);
   if (a->T % 4 == 0) {
     const int ld = tile_ld(a->T);
-    const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + 3 * (size_t)a->K * TILE_V);
+    const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + (1 + TILE_TS) * (size_t)a->K * TILE_V);
     if (smem <= 200 * 1024) {
-      FFS_CUDA(cudaFuncSetAttribute(prep_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(prep_tile_kernel), smem));
       prep_tile_kernel<<<ceil_div(a->V, TILE_V), TILE_WARPS * 32, smem, (cudaStream_t)stream>>>(*a, ld);
       return check_launch("prep_tile_kernel");
     }
@@ -633,7 +633,7 @@ extern "C" int ffs_reml_prep(const ffs_prep_args* a, void* stream) {
   const int ld_s = a->T + ((a->T & 1) ? 2 : 1);  // odd stride: conflict-free transposed reads
   const size_t smem = sizeof(float) * PREP_VOX * ld_s;
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_prep: T=%d too long for one tile", a->T);
-  FFS_CUDA(cudaFuncSetAttribute(prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(prep_kernel), smem));
   prep_kernel<<<ceil_div(a->V, PREP_VOX), 256, smem, (cudaStream_t)stream>>>(*a, ld_s);
   return check_launch("prep_kernel");
 }
@@ -648,7 +648,7 @@ extern "C" int ffs_reml_surface(const ffs_surface_args* a, void* stream) {
   const size_t smem = (sizeof(float4) * (SURF_G2 + 1) + 1) * (size_t)a->T + sizeof(float) * SURF_G +
                       ceil_div(a->T, SURF_TB);
   FFS_REQUIRE(smem <= 227 * 1024, "ffs_reml_surface: T=%d too long", a->T);
-  FFS_CUDA(cudaFuncSetAttribute(surface_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(surface_kernel), smem));
   FFS_REQUIRE(ceil_div(a->V, SURF_THREADS) <= 65535, "ffs_reml_surface: V=%d exceeds one launch", a->V);
   dim3 grid(a->n_chunks, ceil_div(a->V, SURF_THREADS));
   surface_kernel<<<grid, SURF_THREADS, smem, (cudaStream_t)stream>>>(*a);

@@ -14,7 +14,9 @@ namespace ffsk {
 
 constexpr int TILE_V = 32;      // voxels per tile (one per lane)
 constexpr int TILE_WARPS = 8;   // warps per CTA
-constexpr int TILE_PROJ_KC = 8; // columns a thread accumulates per pass in tile_project
+constexpr int TILE_PROJ_KC = 12; // columns a thread accumulates per pass in tile_project
+constexpr int TILE_JG = 2;       // column groups of tile_project (warps = TILE_JG x TILE_TS)
+constexpr int TILE_TS = TILE_WARPS / TILE_JG;  // time splits of tile_project
 constexpr int TILE_SUB_KC = 16; // coefficients a thread holds per pass in tile_subtract
 
 // Row stride (floats) of a tile: a multiple of 4 with ld / 4 odd, so the
@@ -34,17 +36,18 @@ __device__ __forceinline__ void tile_qrange(int T, int w, int& q0, int& q1) {
   q1 = (w + 1) * nq / TILE_WARPS;
 }
 
-// C[j][l] = sum_t M[j][t] Ys[l][t] for j < K, l < 32; part is [2][K][32]
-// scratch. Warp w takes the columns j = (w % 4) + 4u and half of the time
-// range (w / 4); the two halves are added at the end. Ends with a barrier.
+// C[j][l] = sum_t M[j][t] Ys[l][t] for j < K, l < 32; part is [TILE_TS][K][32]
+// scratch. Warp w takes the columns j = (w % TILE_JG) + TILE_JG u and one of
+// TILE_TS slices of the time range (w / TILE_JG); the slices are added in
+// order at the end. Ends with a barrier.
 __device__ __forceinline__ void tile_project(const float* __restrict__ M, const float* Ys, int T, int ld, int K,
                                              float* C, float* part) {
   const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int jg = w & 3, ts = w >> 2;
-  const int nq = T >> 2, qm = (nq + 1) >> 1;
-  const int q0 = ts ? qm : 0, q1 = ts ? nq : qm;
+  const int jg = w % TILE_JG, ts = w / TILE_JG;
+  const int nq = T >> 2;
+  const int q0 = ts * nq / TILE_TS, q1 = (ts + 1) * nq / TILE_TS;
   const float4* yr = reinterpret_cast<const float4*>(Ys + (size_t)l * ld);
-  for (int u0 = jg; u0 < K; u0 += 4 * TILE_PROJ_KC) {
+  for (int u0 = jg; u0 < K; u0 += TILE_JG * TILE_PROJ_KC) {
     float acc[TILE_PROJ_KC];
 #pragma unroll
     for (int k = 0; k < TILE_PROJ_KC; ++k) acc[k] = 0.f;
@@ -52,7 +55,7 @@ __device__ __forceinline__ void tile_project(const float* __restrict__ M, const 
       const float4 y = yr[q];
 #pragma unroll
       for (int k = 0; k < TILE_PROJ_KC; ++k) {
-        const int j = u0 + 4 * k;
+        const int j = u0 + TILE_JG * k;
         if (j < K) {
           const float4 m = __ldg(reinterpret_cast<const float4*>(M + (size_t)j * T) + q);
           acc[k] = fmaf(m.x, y.x, acc[k]);
@@ -64,12 +67,17 @@ __device__ __forceinline__ void tile_project(const float* __restrict__ M, const 
     }
 #pragma unroll
     for (int k = 0; k < TILE_PROJ_KC; ++k) {
-      const int j = u0 + 4 * k;
+      const int j = u0 + TILE_JG * k;
       if (j < K) part[((size_t)ts * K + j) * 32 + l] = acc[k];
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < K * 32; i += blockDim.x) C[i] = part[i] + part[(size_t)K * 32 + i];
+  for (int i = threadIdx.x; i < K * 32; i += blockDim.x) {
+    float c = part[i];
+#pragma unroll
+    for (int k = 1; k < TILE_TS; ++k) c += part[(size_t)k * K * 32 + i];
+    C[i] = c;
+  }
   __syncthreads();
 }
 

@@ -418,7 +418,7 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
               "ffs_reml_window: null buffer");
   const size_t smem = (sizeof(float2) * WIN + sizeof(float) + 1) * (size_t)T + ceil_div(T, CRIT_TB);
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_reml_window: T=%d too long", T);
-  FFS_CUDA(cudaFuncSetAttribute(window_crit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(window_crit_kernel), smem));
   CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, yr_st, reinterpret_cast<const float4*>(coef), winproj, dcf,
              ident, p_id, c_p0, best, dbest, crit0, fallback, best_cell};
   window_crit_kernel<<<max_tiles, WTILE, smem, (cudaStream_t)stream>>>(w, reinterpret_cast<const int2*>(tiles),

@@ -182,6 +182,17 @@ def search_voxels_precomputed_grid(X, Y_batch, factors: engine.GridFactors, devi
     return params, out.best_crit
 
 
+_SIDE: dict = {}
+
+
+def _side_stream(device) -> torch.cuda.Stream:
+    """A second stream of device (the grid build runs there beside the prep)."""
+    key = str(device)
+    if key not in _SIDE:
+        _SIDE[key] = torch.cuda.Stream(device)
+    return _SIDE[key]
+
+
 def _batch_size(V: int, T: int, P: int, K: int, batch_size, device) -> int:
     if batch_size:
         return max(1, min(int(batch_size), V))
@@ -237,6 +248,7 @@ def fit_glm_arma11(
     return_device: bool = False,
     proposal=None,
     proposal_recenter: int = 0,
+    cuda_graphs: bool = True,
 ) -> ARMA11Results:
     """Fit a GLM with ARMA(1,1) REML prewhitening (fastfuncstuff/glm/arma.py:3650).
 
@@ -249,7 +261,8 @@ def fit_glm_arma11(
     ``return_device`` (keep result tensors on the GPU), ``proposal`` (a trained
     ``learned.ArmaProposal``: search each voxel's 5 x 5 window around its
     proposal, the full grid for window-edge voxels) and ``proposal_recenter``
-    (re-centred window rounds before that fallback).
+    (re-centred window rounds before that fallback), ``cuda_graphs`` (replay
+    the learned-seeded fit of one voxel batch from CUDA graphs).
     """
     if want_ols or want_ols_residuals or want_ols_predicted or ols_write_callback is not None:
         _unsupported("the OLS side fit (want_ols)")
@@ -320,16 +333,30 @@ def fit_glm_arma11(
         elif b_grid is None:
             b_grid = get_default_arma_grids()[1]
         grid = make_grid(a_grid, b_grid, use_double=use_double)
-        factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt,
-                                       with_tc=projector == "tc" and K <= 256)
+        factors = None  # built below, unless the CUDA-graph plan builds them inside its graph
         best_all = crit_all = None
 
-    P = factors.P
+    P = grid.P
     bs = _batch_size(V, T, P, K, batch_size, device)
+    use_graph = best_all is None and proposal is not None and cuda_graphs and lj is None and bs >= V
+    q0 = join = None
+    if factors is None and not use_graph:
+        # the grid build runs on a side stream while the residualisation of the
+        # first batch (against the design basis) runs on the main one
+        side = _side_stream(device)
+        factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt,
+                                       with_tc=projector == "tc" and K <= 256, stream=side)
+        built = torch.cuda.Event()
+        built.record(side)
+        main = torch.cuda.current_stream()
+        q0 = engine.design_basis(Xd)
+
+        def join():
+            main.wait_event(built)
     keep = [] if return_device else None
     chunks = {k: [] for k in ("best", "crit", "surf", "betas", "tstats", "sigma2", "fstats", "r2", "lam",
                               "cb", "ct", "resid", "resid_w", "pred", "lb")}
-    proj = projector if (projector != "tc" or factors.U_hi is not None) else "simt"
+    proj = projector if (projector != "tc" or factors is None or factors.U_hi is not None) else "simt"
     if proposal is not None and best_all is None:
         from . import learned
 
@@ -339,7 +366,18 @@ def fit_glm_arma11(
         v1 = min(V, v0 + bs)
         Yb = Y[v0:v1].to(device=device, dtype=torch.float32, non_blocking=True)
         go = None
-        if best_all is None and proposal is not None:
+        if use_graph:
+            plan = learned.graph_for(Yb, Xd, grid, layout_l, proposal, recenter=proposal_recenter,
+                                     do_scale=not use_double,
+                                     gls_kw=dict(want_residuals=want_residuals, want_predicted=want_predicted),
+                                     factor_kw=dict(task_indices=ti, glt=glt,
+                                                    with_tc=projector == "tc" and K <= 256))
+            lo, go = plan.run(Yb, Xd)
+            best, scale = lo.best, lo.scale
+            chunks["best"].append(best)
+            chunks["crit"].append(lo.best_crit)
+            fallbacks.append(lo.fallback)
+        elif best_all is None and proposal is not None:
             # the GLS of every voxel at its window's pair is queued before the
             # host waits for the list of fallback voxels; their rows are redone
             first = {}
@@ -349,7 +387,7 @@ def fit_glm_arma11(
                                          want_predicted=want_predicted, lj=lj)
 
             lo = learned.learned_search(Yb, factors, proposal, layout_l, do_scale=not use_double,
-                                        recenter=proposal_recenter, before_fallback=gls_first)
+                                        recenter=proposal_recenter, before_fallback=gls_first, q0=q0, join=join)
             best, scale = lo.best, lo.scale
             chunks["best"].append(best)
             chunks["crit"].append(lo.best_crit)
@@ -366,13 +404,15 @@ def fit_glm_arma11(
                         t_all.index_copy_(0, sel, t_sub)
         elif best_all is None:
             so = engine.search(Yb, factors, hierarchical=not force_exhaustive_search, projector=proj,
-                               do_scale=not use_double, keep_surface=save_profile_likelihoods)
+                               do_scale=not use_double, keep_surface=save_profile_likelihoods, q0=q0, join=join)
             best, scale = so.best, so.scale
             chunks["best"].append(best)
             chunks["crit"].append(so.best_crit)
             if save_profile_likelihoods:
                 chunks["surf"].append((so.surf.double() + so.crit0[None, :]).float().t())
         else:
+            if join is not None:
+                join()
             best = best_all[v0:v1].to(device)
             scale = _voxel_scale(Yb, not use_double)
             chunks["best"].append(best)

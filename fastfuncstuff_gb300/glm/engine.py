@@ -76,7 +76,7 @@ def set_stage_timer(timer: StageTimer | None) -> None:
 
 def _run(name: str, fn, *args) -> None:
     t = _TIMER
-    if t is None:
+    if t is None or torch.cuda.is_current_stream_capturing():
         _lib.check(fn(*args), name)
         return
     e0 = torch.cuda.Event(enable_timing=True)
@@ -190,8 +190,14 @@ def constant_in_span(X: np.ndarray, tol: float = 1e-6) -> bool:
 
 
 def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_indices=None,
-                  glt: np.ndarray | None = None, with_tc: bool = True) -> GridFactors:
+                  glt: np.ndarray | None = None, with_tc: bool = True, center=None,
+                  stream: torch.cuda.Stream | None = None) -> GridFactors:
     """Run the FP64 grid build for design ``X`` (T, K) on its device.
+
+    ``center`` = (flag, coefficients) from ``constant_flag(X)`` when the caller
+    has them already (the CUDA-graph plan computes them outside its capture).
+    With ``stream`` the grid build runs there (the buffers are allocated on the
+    current stream, which must wait for ``stream`` before it reads them).
 
     lambda is always evaluated in float64 from the float32 (a, b) values (the
     FP64 fit's value); the fit's mode only decides the validity filter and the
@@ -209,12 +215,12 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     tau = const_dev(layout.tau, dev)
     task_idx = None
     if task_indices is not None and len(task_indices) > 0:
-        task_idx = torch.as_tensor(list(task_indices), dtype=torch.int32, device=dev)
-    glt_t = None if glt is None else torch.as_tensor(np.asarray(glt, np.float32), device=dev).reshape(-1, K)
+        task_idx = const_dev(np.asarray(list(task_indices), np.int32), dev)
+    glt_t = None if glt is None else const_dev(np.asarray(glt, np.float32).reshape(-1, K), dev)
     nt = 0 if task_idx is None else task_idx.numel()
     ng = 0 if glt_t is None else glt_t.shape[0]
     lib = _lib.load()
-    cflag, ccoef = constant_flag(Xc)
+    cflag, ccoef = constant_flag(Xc) if center is None else center
     work = torch.empty(int(lib.ffs_grid_work_bytes(T, K, P)) // 8 + 1, dtype=torch.float64, device=dev)
     f = GridFactors(
         grid=grid, T=T, K=K, ld=ld,
@@ -235,18 +241,23 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
         chunk_pairs=const_dev(grid.chunk_pairs, dev),
         lattice=const_dev(grid.lattice.reshape(-1), dev),
         task_idx=task_idx, glt=glt_t,
-        Gsum=torch.empty(P, K, **f32),
+        Gsum=None,
         center_flag=cflag,
         uexp=torch.empty(P, dtype=torch.int32, device=dev) if with_tc else None,
     )
     d = _lib.GridDesc(T=T, K=K, P=P, n_runs=layout.n_runs, run_start=_p(run_start), tau=_p(tau),
                       a=_p(a), b=_p(b), X=_p(Xc), lambda_fp32=0, ld_u=ld,
                       n_task=nt, task_idx=_p(task_idx), n_glt=ng, glt=_p(glt_t))
+    # no Gsum from the kernel: G'1 is the FP64 coefficient vector of the constant (set below)
     o = _lib.GridOut(coef=_p(f.coef), logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), U=_p(f.U),
                      U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), uexp=_p(f.uexp), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
-                     info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=_p(f.Gsum),
-                     work=_p(work))
-    _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
+                     info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=None, work=_p(work))
+    if stream is None:
+        _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
+    else:
+        stream.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(stream):
+            _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
     # G' X = I for every pair, so G'1 = c exactly when the constant is in
     # span(X): the centring correction of the GLS uses the FP64 coefficients
     # rather than sums of the fp32 G (the flag decides on the device)
@@ -274,9 +285,24 @@ class PrepOut:
     yexp: torch.Tensor | None
 
 
+def design_basis(X: torch.Tensor) -> torch.Tensor:
+    """Q0 [K][T]: the orthonormal basis of the design's columns (FP64 Cholesky),
+    from X alone, so the residualisation need not wait for the grid build."""
+    lib = _lib.load()
+    dev = X.device
+    T, K = X.shape
+    Xc = X.to(torch.float32).contiguous()
+    work = torch.empty(int(lib.ffs_design_basis_work_bytes(T, K)) // 8 + 1, dtype=torch.float64, device=dev)
+    q0 = torch.empty(K, T, dtype=torch.float32, device=dev)
+    info = torch.empty(1, dtype=torch.int32, device=dev)
+    _run("ffs_design_basis", lib.ffs_design_basis, T, K, _p(Xc), _p(work), _p(q0), _p(info), _stream())
+    q0._keep = (Xc, work, info)
+    return q0
+
+
 def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core: bool = True,
          idx: torch.Tensor | None = None, want_yr_t: bool = True, layout: RunLayout | None = None,
-         scale: torch.Tensor | None = None, want_rows: bool = False) -> PrepOut:
+         scale: torch.Tensor | None = None, want_rows: bool = False, q0: torch.Tensor | None = None) -> PrepOut:
     """Per-voxel scaling and residualisation (and the fp16 split for the GEMM).
 
     ``idx`` (int32, device) processes the rows Y[idx] in that order (every
@@ -303,7 +329,8 @@ def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core:
         feats = torch.empty(n, 9, dtype=torch.float32, device=dev)
         rs = const_dev(layout.run_start, dev)
     rows = torch.empty(n, T, dtype=torch.float32, device=dev) if want_rows else None
-    q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T])
+    if q0 is None:
+        q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T]): U of (0, 0)
     pa = _lib.PrepArgs(V=n, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=0, ld_y=ld,
                        scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp),
                        idx=_p(idx), feats=_p(feats), n_runs=0 if layout is None else layout.n_runs,
@@ -317,7 +344,8 @@ def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core:
 
 
 def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projector: str = "tc",
-           do_scale: bool = True, keep_surface: bool = False, keep_yr: bool = False) -> SearchOut:
+           do_scale: bool = True, keep_surface: bool = False, keep_yr: bool = False,
+           q0: torch.Tensor | None = None, join=None) -> SearchOut:
     """REML grid search of every voxel of ``Y`` (V, T) against the factors ``f``.
 
     ``projector`` picks the projection kernel: "tc" (tcgen05 fp16-split GEMM) or
@@ -333,7 +361,9 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
         raise ValueError("the factors were built without the tensor-core operands")
     if projector not in ("tc", "simt"):
         raise ValueError(f"unknown projector {projector!r}")
-    pr = prep(Y, f, do_scale=do_scale, tensor_core=use_tc)
+    pr = prep(Y, f, do_scale=do_scale, tensor_core=use_tc, q0=q0)
+    if join is not None:  # the factors may still be in flight on another stream
+        join()
 
     proj = torch.empty(P, V, dtype=torch.float32, device=dev)
     flag = torch.zeros(1, dtype=torch.int32, device=dev)

@@ -201,8 +201,18 @@ _GRID_CONSTS: dict = {}
 def _window_consts(f: engine.GridFactors):
     """Constants of the windowed refine: the grid's (cached by lattice content)
     and the factors' (device tensors, no host round trip)."""
-    g = f.grid
-    dev = f.coef.device
+    c = _grid_consts(f.grid, f.coef.device)
+    fc = getattr(f, "_window_consts", None)
+    if fc is None:
+        g = f.grid
+        c_p0 = (f.logdet_R[g.p0] + f.logdet_XtX[g.p0]).reshape(1).contiguous()
+        fc = dict(c, c_p0=c_p0, dcf=((f.logdet_R + f.logdet_XtX) - c_p0).float().contiguous())
+        f._window_consts = fc
+    return fc
+
+
+def _grid_consts(g: RemlGrid, dev):
+    """The grid's constants of the windowed refine on dev (cached by lattice content)."""
     key = (g.a_axis.tobytes(), g.b_axis.tobytes(), g.lattice.tobytes(), str(dev))
     c = _GRID_CONSTS.get(key)
     if c is None:
@@ -223,15 +233,10 @@ def _window_consts(f: engine.GridFactors):
                  a_ax=torch.from_numpy(g.a_axis).to(dev), b_ax=torch.from_numpy(g.b_axis).to(dev),
                  evals=torch.from_numpy(np.append(evals, 0)).to(dev))  # [ncell + 1]: 0 for a skipped voxel
         _GRID_CONSTS[key] = c
-    fc = getattr(f, "_window_consts", None)
-    if fc is None:
-        c_p0 = (f.logdet_R[g.p0] + f.logdet_XtX[g.p0]).reshape(1).contiguous()
-        fc = dict(c, c_p0=c_p0, dcf=((f.logdet_R + f.logdet_XtX) - c_p0).float().contiguous())
-        f._window_consts = fc
-    return fc
+    return c
 
 
-def _window_round(pre, f, cen, out, *, flag):
+def _window_round(pre, f, cen, out, *, flag, join=None):
     """Evaluate the 5 x 5 windows centred at cen (one lattice cell per voxel,
     or ncell = n_a * n_b for a voxel to skip), writing out[...] at the voxel
     ids. Nothing waits for the host: the number of voxels taken stays on the
@@ -244,7 +249,7 @@ def _window_round(pre, f, cen, out, *, flag):
     n_a, n_b = len(g.a_axis), len(g.b_axis)
     ncell = n_a * n_b
     n = cen.numel()
-    c = _window_consts(f)
+    c = _grid_consts(g, dev)
     # voxels sorted by window centre; the skipped ones (bucket ncell) last
     idx = torch.empty(n, dtype=torch.int32, device=dev)
     cell_end = torch.empty(ncell + 2, dtype=torch.int32, device=dev)
@@ -267,6 +272,9 @@ def _window_round(pre, f, cen, out, *, flag):
     engine._run("ffs_reml_window_items", lib.ffs_reml_window_items, ncell, _p(cell_end), n_a, n_b, _p(f.lattice),
                 K, max_pairs, _p(items), _p(counts), max_items, _p(tiles), counts.data_ptr() + 8, max_tiles,
                 counts.data_ptr() + 4, st)
+    if join is not None:  # the factors may still be in flight on another stream
+        join()
+    c = _window_consts(f)
     winproj = torch.empty(n, WIN_SLOTS, dtype=torch.float32, device=dev)
     ja = _lib.ProjectArgs(V=n, T=T, K=K, P=P, ld_y=ld, ld_u=ld, yr_hi=_p(hi), yr_lo=_p(lo),
                           u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yexp=_p(yexp), uexp=_p(f.uexp), yr_t=None, U=None,
@@ -281,8 +289,100 @@ def _window_round(pre, f, cen, out, *, flag):
     return counts
 
 
+@dataclass
+class WindowState:
+    """Device results of the window rounds (nothing read back yet)."""
+
+    best: torch.Tensor      # [V] int32 the windows' pair per voxel
+    best_crit: torch.Tensor  # [V] float32
+    scale: torch.Tensor     # [V] float32
+    fb: torch.Tensor        # [V] int32 1: the full grid must decide
+    proposal: torch.Tensor  # [V, 2]
+    small: torch.Tensor     # int32 [fallback count, wait flag, list overflows...]
+    stats: dict
+
+
+def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
+                    do_scale: bool = True, recenter: int = 0, q0: torch.Tensor | None = None,
+                    join=None) -> WindowState:
+    """The window rounds of the learned-seeded search, with no host round trip
+    (so they also run inside a CUDA graph): prep with the proposal features,
+    the MLP, the 5 x 5 window of every voxel and ``recenter`` re-centred rounds
+    for the voxels on a window edge. With ``q0`` (engine.design_basis) the
+    prep does not read the factors; ``join()`` is then called before their
+    first use (they may be built on another stream meanwhile)."""
+    lib = _lib.load()
+    dev = Y.device
+    V, T = Y.shape
+    f = factors
+    if f.U_hi is None:
+        raise ValueError("the learned search needs the tensor-core operands of the factors")
+    if T % 4:
+        raise NotImplementedError("the learned search needs T % 4 == 0 (the tiled prep)")
+    g = f.grid
+    st = _st()
+    Y = Y.float().contiguous()
+    c = _grid_consts(g, dev)
+    p1 = engine.prep(Y, f, do_scale=do_scale, tensor_core=True, want_yr_t=False, layout=layout, want_rows=True,
+                     q0=q0)
+    scale = p1.scale
+    prop = proposal.forward(p1.feats)
+    center = torch.empty(V, dtype=torch.int32, device=dev)
+    engine._run("ffs_reml_centers", lib.ffs_reml_centers, V, _p(prop), _p(c["a_ax"]), len(g.a_axis), _p(c["b_ax"]),
+                len(g.b_axis), _p(center), st)
+    out = dict(best=torch.empty(V, dtype=torch.int32, device=dev), dbest=torch.empty(V, dtype=torch.float32, device=dev),
+               crit0=torch.empty(V, dtype=torch.float64, device=dev), fb=torch.zeros(V, dtype=torch.int32, device=dev),
+               cell=torch.empty(V, dtype=torch.int32, device=dev))
+    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    counts = [_window_round(p1, f, center, out, flag=flag, join=join)]
+    stats = {"edge_first": out["fb"].float().mean() if recenter else None}
+    ncell = len(g.a_axis) * len(g.b_axis)
+    for _ in range(recenter):
+        # re-centre the voxels on a window edge on the window's best pair; the
+        # rest (and those whose window held no candidate) are skipped
+        again = (out["fb"] != 0) & (out["cell"] >= 0)
+        cen = torch.where(again, out["cell"], torch.full_like(out["cell"], ncell)).contiguous()
+        counts.append(_window_round(p1, f, cen, out, flag=flag))
+    best_crit = (out["crit0"] + out["dbest"].double()).float()
+    fb = out["fb"]
+    small = torch.stack([fb.sum().to(torch.int32), flag[0]] + [cn[1] for cn in counts])
+    stats["pair_evals"] = out["pair_evals"]  # device scalar: (voxel, pair) windows evaluated
+    return WindowState(best=out["best"], best_crit=best_crit, scale=scale, fb=fb, proposal=prop, small=small,
+                       stats=stats)
+
+
+def learned_fallback(Y: torch.Tensor, factors: engine.GridFactors, ws: WindowState, small_host: torch.Tensor, *,
+                     do_scale: bool = True) -> LearnedOut:
+    """The full grid for the voxels the windows left undecided; small_host is
+    ws.small read back to the host."""
+    dev = Y.device
+    V = Y.shape[0]
+    n_fb, code = int(small_host[0]), int(small_host[1])
+    if code != 0:
+        raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {code})")
+    if bool((small_host[2:] != 0).any()):
+        raise RuntimeError("ffs_reml_window_items: work list overflow")
+    fb = ws.fb
+    # the fallback voxels' ids in order, compacted on the device
+    pos = torch.where(fb != 0, torch.cumsum(fb, 0) - 1, torch.full_like(fb, n_fb)).long()
+    sel = torch.empty(n_fb + 1, dtype=torch.long, device=dev).scatter_(0, pos, torch.arange(V, device=dev))[:n_fb]
+    stats = dict(ws.stats)
+    if stats["edge_first"] is None:
+        stats["edge_first"] = n_fb / V
+    stats["fallback"] = n_fb / V
+    best, best_crit = ws.best, ws.best_crit
+    if n_fb:
+        so = engine.search(Y.index_select(0, sel), factors, hierarchical=False, projector="tc", do_scale=do_scale)
+        best = best.index_copy(0, sel, so.best)
+        best_crit = best_crit.index_copy(0, sel, so.best_crit)
+    lo = LearnedOut(best=best, best_crit=best_crit, scale=ws.scale, fallback=fb, proposal=ws.proposal, stats=stats)
+    lo.fallback_idx = sel
+    return lo
+
+
 def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
-                   do_scale: bool = True, recenter: int = 0, before_fallback=None) -> LearnedOut:
+                   do_scale: bool = True, recenter: int = 0, before_fallback=None, q0=None,
+                   join=None) -> LearnedOut:
     """Learned-seeded REML search: the 5 x 5 window around each proposal, the
     full grid for voxels whose best pair sits on the window edge (or whose
     window, holding no identity pair, has nothing below the identity pairs'
@@ -295,73 +395,18 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
     fallback voxels, so work it enqueues keeps the GPU busy meanwhile;
     ``LearnedOut.fallback_idx`` lists the voxels whose pair changed after it.
     """
-    lib = _lib.load()
-    dev = Y.device
-    V, T = Y.shape
-    f = factors
-    if f.U_hi is None:
-        raise ValueError("the learned search needs the tensor-core operands of the factors")
-    if T % 4:
-        raise NotImplementedError("the learned search needs T % 4 == 0 (the tiled prep)")
-    g = f.grid
-    st = _st()
     Y = Y.float().contiguous()
-    c = _window_consts(f)
-    p1 = engine.prep(Y, f, do_scale=do_scale, tensor_core=True, want_yr_t=False, layout=layout, want_rows=True)
-    scale = p1.scale
-    prop = proposal.forward(p1.feats)
-    center = torch.empty(V, dtype=torch.int32, device=dev)
-    engine._run("ffs_reml_centers", lib.ffs_reml_centers, V, _p(prop), _p(c["a_ax"]), len(g.a_axis), _p(c["b_ax"]),
-                len(g.b_axis), _p(center), st)
-    out = dict(best=torch.empty(V, dtype=torch.int32, device=dev), dbest=torch.empty(V, dtype=torch.float32, device=dev),
-               crit0=torch.empty(V, dtype=torch.float64, device=dev), fb=torch.zeros(V, dtype=torch.int32, device=dev),
-               cell=torch.empty(V, dtype=torch.int32, device=dev))
-    flag = torch.zeros(1, dtype=torch.int32, device=dev)
-    counts = [_window_round(p1, f, center, out, flag=flag)]
-    stats = {"edge_first": None}
-    ncell = len(g.a_axis) * len(g.b_axis)
-    for r in range(recenter):
-        if r == 0:
-            stats["edge_first"] = out["fb"].float().mean()  # device scalar
-        # re-centre the voxels on a window edge on the window's best pair; the
-        # rest (and those whose window held no candidate) are skipped
-        again = (out["fb"] != 0) & (out["cell"] >= 0)
-        cen = torch.where(again, out["cell"], torch.full_like(out["cell"], ncell)).contiguous()
-        counts.append(_window_round(p1, f, cen, out, flag=flag))
-    best_crit = (out["crit0"] + out["dbest"].double()).float()
-    best = out["best"]
-    fb = out["fb"]
-    # the host needs three numbers (fallback count, wait flag, list overflow):
-    # copy them to pinned memory behind an event, queue the caller's work, and
-    # wait for that event only
-    small = torch.stack([fb.sum().to(torch.int32), flag[0]] + [cn[1] for cn in counts])
-    host = torch.empty(small.numel(), dtype=torch.int32, pin_memory=True)
-    host.copy_(small, non_blocking=True)
+    ws = learned_windows(Y, factors, proposal, layout, do_scale=do_scale, recenter=recenter, q0=q0, join=join)
+    # copy the few numbers the host needs to pinned memory behind an event,
+    # queue the caller's work, and wait for that event only
+    host = torch.empty(ws.small.numel(), dtype=torch.int32, pin_memory=True)
+    host.copy_(ws.small, non_blocking=True)
     ready = torch.cuda.Event()
     ready.record()
     if before_fallback is not None:
-        before_fallback(best.clone(), scale)
+        before_fallback(ws.best.clone(), ws.scale)
     ready.synchronize()
-    # the full grid for the voxels still on a window edge
-    n_fb, code = int(host[0]), int(host[1])
-    if code != 0:
-        raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {code})")
-    if bool((host[2:] != 0).any()):
-        raise RuntimeError("ffs_reml_window_items: work list overflow")
-    # the fallback voxels' ids in order, compacted on the device
-    pos = torch.where(fb != 0, torch.cumsum(fb, 0) - 1, torch.full_like(fb, n_fb)).long()
-    sel = torch.empty(n_fb + 1, dtype=torch.long, device=dev).scatter_(0, pos, torch.arange(V, device=dev))[:n_fb]
-    if stats["edge_first"] is None:
-        stats["edge_first"] = sel.numel() / V
-    stats["fallback"] = sel.numel() / V
-    stats["pair_evals"] = out["pair_evals"]  # device scalar: (voxel, pair) windows evaluated
-    if sel.numel():
-        so = engine.search(Y.index_select(0, sel), f, hierarchical=False, projector="tc", do_scale=do_scale)
-        best.index_copy_(0, sel, so.best)
-        best_crit.index_copy_(0, sel, so.best_crit)
-    lo = LearnedOut(best=best, best_crit=best_crit, scale=scale, fallback=fb, proposal=prop, stats=stats)
-    lo.fallback_idx = sel
-    return lo
+    return learned_fallback(Y, factors, ws, host, do_scale=do_scale)
 
 
 def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxels: int = 2_000_000,
@@ -384,3 +429,119 @@ def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxe
             "holdout_loss": hist[-1]["holdout_loss"]}
     prop.meta.update(info)
     return prop, info
+
+
+class LearnedFitGraph:
+    """The learned-seeded fit of one shape as two CUDA graphs.
+
+    Graph A builds the grid factors of X on a side stream while the prep with
+    the proposal features (against the design basis of X), the MLP and the
+    first window round's grouping and gathers run on the main one; the window
+    rounds then join them. It ends by copying the few numbers the host needs
+    (fallback count, wait flag, list overflows) to pinned memory.
+    Graph B is the GLS of every voxel at its window pair. ``run`` replays A,
+    records an event, replays B, waits for the event only (B keeps the GPU
+    busy meanwhile), then runs the full grid and the GLS of the fallback
+    voxels eagerly. Inputs are copied into the graphs' static buffers; results
+    are returned as new tensors.
+    """
+
+    def __init__(self, Y: torch.Tensor, X: torch.Tensor, grid: RemlGrid, layout: RunLayout,
+                 proposal: ArmaProposal, *, recenter: int, do_scale: bool, gls_kw: dict, factor_kw: dict):
+        self.Y = Y.float().contiguous().clone()
+        self.X = X.float().contiguous().clone()
+        self.grid, self.layout, self.proposal = grid, layout, proposal
+        self.recenter, self.do_scale, self.gls_kw, self.factor_kw = recenter, do_scale, gls_kw, factor_kw
+        self.cflag, self.ccoef = engine.constant_flag(self.X)
+        self.host = torch.empty(3 + recenter, dtype=torch.int32, pin_memory=True)
+        self.side = torch.cuda.Stream(self.Y.device)  # the grid build runs beside the prep chain
+        self.side_fb = torch.cuda.Stream(self.Y.device)  # the fallback runs beside graph B
+        # one eager pass fills the host-side caches (device constants, tensor
+        # maps, kernel attributes) that a capture must not create
+        self._body_a()
+        self._body_b()
+        torch.cuda.synchronize()
+        self.ga = torch.cuda.CUDAGraph()
+        self.gb = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.ga, capture_error_mode="thread_local"):
+            self._body_a()
+        with torch.cuda.graph(self.gb, pool=self.ga.pool(), capture_error_mode="thread_local"):
+            self._body_b()
+
+    def _body_a(self):
+        main = torch.cuda.current_stream()
+        self.f = engine.build_factors(self.X, self.grid, self.layout, center=(self.cflag, self.ccoef),
+                                      stream=self.side, **self.factor_kw)
+        built = torch.cuda.Event()
+        built.record(self.side)
+        q0 = engine.design_basis(self.X)
+        self.ws = learned_windows(self.Y, self.f, self.proposal, self.layout, do_scale=self.do_scale,
+                                  recenter=self.recenter, q0=q0, join=lambda: main.wait_event(built))
+        self.host.copy_(self.ws.small, non_blocking=True)
+
+    def _body_b(self):
+        self.best_w = self.ws.best.clone()
+        self.go = engine.gls(self.Y, self.ws.scale, self.best_w, self.f, self.X, **self.gls_kw)
+
+    def run(self, Y: torch.Tensor, X: torch.Tensor):
+        """(LearnedOut, engine.GlsOut) of data Y (V, T) and design X (T, K)."""
+        main = torch.cuda.current_stream()
+        self.Y.copy_(Y)
+        self.X.copy_(X)
+        flag, coef = engine.constant_flag(self.X)
+        self.cflag.copy_(flag)
+        self.ccoef.copy_(coef)
+        self.ga.replay()
+        ready = torch.cuda.Event()
+        ready.record()
+        self.gb.replay()
+        ready.synchronize()
+        # the fallback voxels' full grid and GLS on a second stream, beside the
+        # GLS of graph B (both only read the graphs' buffers)
+        fs = self.side_fb
+        fs.wait_event(ready)
+        with torch.cuda.stream(fs):
+            lo = learned_fallback(self.Y, self.f, self.ws, self.host, do_scale=self.do_scale)
+            # the graphs' buffers are overwritten by the next run: hand out copies
+            lo.best, lo.best_crit, lo.scale = lo.best.clone(), lo.best_crit.clone(), lo.scale.clone()
+            lo.fallback, lo.proposal = lo.fallback.clone(), lo.proposal.clone()
+            sel = lo.fallback_idx
+            gs = None
+            if sel.numel():
+                gs = engine.gls(self.Y.index_select(0, sel), lo.scale.index_select(0, sel),
+                                lo.best.index_select(0, sel), self.f, self.X, **self.gls_kw)
+        done = torch.cuda.Event()
+        done.record(fs)
+        go = engine.GlsOut(**{k: (None if v is None else v.clone()) for k, v in vars(self.go).items()
+                              if not k.startswith("_")})
+        main.wait_event(done)
+        used = [lo.best, lo.best_crit, lo.scale, lo.fallback, lo.proposal, sel]
+        if gs is not None:
+            for fld in ("betas", "tstats", "sigma2", "fstats", "r2", "lam", "cbeta", "ct", "resid", "resid_w",
+                        "pred", "ljung_box"):
+                t_all, t_sub = getattr(go, fld), getattr(gs, fld)
+                if t_all is not None:
+                    t_all.index_copy_(0, sel, t_sub)
+                    used.append(t_sub)
+        for t in used:  # made on the fallback stream, read on this one
+            t.record_stream(main)
+        return lo, go
+
+
+_GRAPHS: dict = {}
+
+
+def graph_for(Y, X, grid, layout, proposal, *, recenter, do_scale, gls_kw, factor_kw) -> LearnedFitGraph:
+    """The cached LearnedFitGraph of this shape and these options (built on first use)."""
+    fk = tuple((k, None if v is None else np.asarray(v).tobytes()) for k, v in sorted(factor_kw.items()))
+    key = (tuple(Y.shape), tuple(X.shape), str(Y.device), grid.a.tobytes(), grid.b.tobytes(), grid.lambda_fp32,
+           layout.run_start.tobytes(), layout.tau.tobytes(), id(proposal.params), proposal.params._version,
+           recenter, do_scale, tuple(sorted(gls_kw.items())), fk)
+    gr = _GRAPHS.get(key)
+    if gr is None:
+        while len(_GRAPHS) >= 2:  # a plan holds a few GB of static buffers
+            _GRAPHS.pop(next(iter(_GRAPHS)))
+        gr = LearnedFitGraph(Y, X, grid, layout, proposal, recenter=recenter, do_scale=do_scale, gls_kw=gls_kw,
+                             factor_kw=factor_kw)
+        _GRAPHS[key] = gr
+    return gr

@@ -134,6 +134,15 @@ int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
 #define FFS_GRID_STATIC_SCRATCH_BYTES ((size_t)16 << 20)
 int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
 
+/* Orthonormal basis of the design's columns, Q0 [K][T] fp32 (no reference
+ * counterpart as a separate step: it is U of the pair (0, 0), which
+ * ffs_grid_build also writes). Q0 = X Lx^-T with Lx the FP64 Cholesky factor of
+ * X'X, or modified Gram-Schmidt (twice) when X'X is not positive definite
+ * (*info = 1). Needing only X, it lets the residualisation (ffs_reml_prep) run
+ * while the grid build is still in flight. work: ffs_design_basis_work_bytes. */
+size_t ffs_design_basis_work_bytes(int T, int K);
+int ffs_design_basis(int T, int K, const float* X, void* work, float* Q0, int* info, void* stream);
+
 /* ---------------------------------------------------------------- search data
  * Replaces the per-voxel scaling of fastfuncstuff/glm/arma.py:3952-3954,
  * 4685-4686 and _residualize_reml_search_data (arma.py:1554-1571).
