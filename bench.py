@@ -42,12 +42,21 @@ GRID = 33
 L2_BYTES = 129 * 2**20
 
 
-def workload_config(V: int) -> dict:
+WORKLOADS = {
+    1: "N=400 (2 runs x 200), p=20",
+    2: "N=855 (4 runs of 180/220/240/260, 5% censored), p=18, 20 HRF-group designs (Zipf)",
+    3: "N=600 (3 runs x 200), p=130 single-trial design",
+    4: "N=400 (2 runs x 200), p=20, learned-proposal inference size",
+}
+
+
+def workload_config(V: int, cid: int = 1, T: int = 400, K: int = 20) -> dict:
+    mb = V * T * 4 / 1e6
     return {
-        "workload": f"synthetic fMRI, N=400 (2 runs x 200), V={V:,} voxels, p=20, "
-                    f"(a,b) grid 33x33 on [-0.8,0.8] -> 561 valid pairs",
-        "voxels": V, "timepoints": 400, "regressors": 20, "pairs": 561,
-        "l2": "inputs larger than L2 (Y is 320 MB fp32 > 129 MB L2); no flush needed",
+        "workload": f"synthetic fMRI, {WORKLOADS[cid]}, V={V:,} voxels, (a,b) grid 33x33 on [-0.8,0.8] -> 561 "
+                    f"valid pairs",
+        "voxels": V, "timepoints": T, "regressors": K, "pairs": 561,
+        "l2": f"inputs larger than L2 (Y is {mb:.0f} MB fp32 > 129 MB L2); no flush needed",
     }
 
 
@@ -159,7 +168,7 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded workload)",
-        "config": workload_config(args.voxels),
+        "config": workload_config(args.voxels or 200_000),
         "method": "the reference's default CPU fit (full grid, hierarchical selector)",
         "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": cores, "kind": "port",
                          "sample": f"{n} voxels per step of the same workload on {cores} host threads"},
@@ -210,21 +219,38 @@ def run_gb300(args) -> None:
     dist, rank, ws, local = dist_init()
     dev = torch.device(f"cuda:{local}")
     torch.cuda.set_device(dev)
-    w = synth.workload(1, V=args.voxels, seed=1001 + 7919 * rank)
+    cid = args.workload
+    w = synth.workload(cid, V=args.voxels, seed=1000 + cid + 7919 * rank)
+    V = w.Y.shape[0]
     g = torch.linspace(-0.8, 0.8, GRID)
-    Xd = torch.from_numpy(w.X).to(dev)
     Yd = torch.from_numpy(w.Y).to(dev)
     kw = dict(tr=2.0, a_grid=g, b_grid=g, run_starts=w.run_starts, device=dev, verbose=False,
               force_exhaustive_search=args.selector == "exhaustive", projector=args.projector)
-    lay = G.run_layout(w.T, w.run_starts)
-    if args.proposal:
-        prop = learned.ArmaProposal.load(args.proposal, dev)
-        tinfo = {"proposal": f"loaded from {Path(args.proposal).name}"}
+    grouped = w.designs is not None
+    if grouped:  # one design per HRF group: the grouped API, full grid
+        from fastfuncstuff_gb300 import fit_glm_arma11_grouped
+
+        designs = {h: torch.from_numpy(x).to(dev) for h, x in w.designs.items()}
+        kw["tau"] = w.tau
+        T, K = next(iter(w.designs.values())).shape
+
+        def fit(Yx, Xx, **k):
+            return fit_glm_arma11_grouped(Yx, designs, w.groups, **k)
+        Xd = None
+        prop, tinfo, kw_l = None, {}, None
     else:
-        prop, tinfo = learned.train_proposal(Xd, lay, g, g, n_voxels=args.train_voxels, epochs=args.train_epochs)
-        if args.save_proposal and rank == 0:
-            prop.save(args.save_proposal)
-    kw_l = dict(kw, proposal=prop, proposal_recenter=args.recenter)
+        Xd = torch.from_numpy(w.X).to(dev)
+        T, K = w.X.shape
+        fit = fit_glm_arma11
+        lay = G.run_layout(w.T, w.run_starts)
+        if args.proposal:
+            prop = learned.ArmaProposal.load(args.proposal, dev)
+            tinfo = {"proposal": f"loaded from {Path(args.proposal).name}"}
+        else:
+            prop, tinfo = learned.train_proposal(Xd, lay, g, g, n_voxels=args.train_voxels, epochs=args.train_epochs)
+            if args.save_proposal and rank == 0:
+                prop.save(args.save_proposal)
+        kw_l = dict(kw, proposal=prop, proposal_recenter=args.recenter)
 
     def barrier():
         torch.cuda.synchronize()
@@ -233,7 +259,7 @@ def run_gb300(args) -> None:
 
     def timed(kwargs):
         def step():
-            return fit_glm_arma11(Yd, Xd, return_device=True, **kwargs)
+            return fit(Yd, Xd, return_device=True, **kwargs)
 
         for _ in range(args.warmup):
             step()
@@ -259,46 +285,56 @@ def run_gb300(args) -> None:
         return ms, st, timer.launches // args.steps, clk.summary()
 
     ms_f, st_f, l_f, clk_f = timed(kw)
-    ms_l, st_l, l_l, clk_l = timed(kw_l)
-    value = ws * args.voxels / (ms_l / 1e3)
-    value_f = ws * args.voxels / (ms_f / 1e3)
-
-    # quality of the learned step against the full grid (exhaustive argmin)
-    exh = fit_glm_arma11(Yd, Xd, return_device=True, **dict(kw, force_exhaustive_search=True))
-    lr = fit_glm_arma11(Yd, Xd, return_device=True, **kw_l)
-    same = (lr.arma_params == exh.arma_params).all(1)
-    num = (lr.betas.double() - exh.betas.double()).abs().amax(1)
-    den = exh.betas.double().abs().amax(1).clamp(min=1e-12)
-    rel = num / den
-    f_all = engine.build_factors(Xd, G.make_grid(g, g), lay)
-    ls = learned.learned_search(Yd, f_all, prop, lay, recenter=args.recenter)
-    pair_evals = float(ls.stats["pair_evals"].item()) if torch.is_tensor(ls.stats["pair_evals"]) else 0.0
-    quality = {
-        "agreement_with_full_grid": float(same.float().mean().item()),
-        "beta_rel_err_le_1e-4": float((rel <= 1e-4).float().mean().item()),
-        "beta_rel_err_max_where_pair_agrees": float(rel[same].max().item()) if bool(same.any()) else None,
-        "first_window_on_edge": float(ls.stats["edge_first"]), "full_grid_fallback": ls.stats["fallback"],
-        "recenter_rounds": args.recenter, "window_pair_evals_per_voxel": pair_evals / args.voxels,
-    }
-    quality.update({k: round(v, 3) if isinstance(v, float) else v for k, v in tinfo.items()})
-
+    value_f = ws * V / (ms_f / 1e3)
     pk = peaks()
-    V, T, K, P = args.voxels, 400, 20, 561
-    dom = max(st_l.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])[0]
-    extra = {"pair_evals": pair_evals}
-    roof = roofline(dom, st_l[dom]["mean_ms"], V, T, K, P, pk, clk_l["sm_mhz"], extra)
+    P = 561
     dom_f = max(st_f.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])[0]
     roof_f = roofline(dom_f, st_f[dom_f]["mean_ms"], V, T, K, P, pk, clk_f["sm_mhz"], {})
+    if grouped:
+        ms_l, st_l, l_l, clk_l, value, roof, quality = ms_f, st_f, l_f, clk_f, value_f, roof_f, None
+        st_e, ms_e = st_f, ms_f
+    else:
+        ms_l, st_l, l_l, clk_l = timed(kw_l)
+        value = ws * V / (ms_l / 1e3)
+        # the learned step is replayed from CUDA graphs, which the per-call
+        # timer does not see into: its stage breakdown comes from an eager pass
+        ms_e, st_e, l_e, _ = timed(dict(kw_l, cuda_graphs=False))
 
+        # quality of the learned step against the full grid (exhaustive argmin)
+        exh = fit_glm_arma11(Yd, Xd, return_device=True, **dict(kw, force_exhaustive_search=True))
+        lr = fit_glm_arma11(Yd, Xd, return_device=True, **kw_l)
+        same = (lr.arma_params == exh.arma_params).all(1)
+        num = (lr.betas.double() - exh.betas.double()).abs().amax(1)
+        den = exh.betas.double().abs().amax(1).clamp(min=1e-12)
+        rel = num / den
+        f_all = engine.build_factors(Xd, G.make_grid(g, g), lay)
+        ls = learned.learned_search(Yd, f_all, prop, lay, recenter=args.recenter)
+        pair_evals = float(ls.stats["pair_evals"].item()) if torch.is_tensor(ls.stats["pair_evals"]) else 0.0
+        quality = {
+            "agreement_with_full_grid": float(same.float().mean().item()),
+            "beta_rel_err_le_1e-4": float((rel <= 1e-4).float().mean().item()),
+            "beta_rel_err_max_where_pair_agrees": float(rel[same].max().item()) if bool(same.any()) else None,
+            "first_window_on_edge": float(ls.stats["edge_first"]), "full_grid_fallback": ls.stats["fallback"],
+            "recenter_rounds": args.recenter, "window_pair_evals_per_voxel": pair_evals / V,
+        }
+        quality.update({k: round(v, 3) if isinstance(v, float) else v for k, v in tinfo.items()})
+        dom = max(st_e.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])[0]
+        roof = roofline(dom, st_e[dom]["mean_ms"], V, T, K, P, pk, clk_l["sm_mhz"], {"pair_evals": pair_evals})
+
+    method = ("full grid, one design per HRF group (fit_glm_arma11_grouped)" if grouped else
+              f"learned-seeded 5x5 window refine ({args.recenter} re-centred round), full grid on window edges, "
+              f"replayed from CUDA graphs")
     line = {
         "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_l, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded workload, see fastfuncstuff_gb300/synth.py)",
-        "config": workload_config(args.voxels),
-        "method": f"learned-seeded 5x5 window refine ({args.recenter} re-centred round), full grid on window edges",
+        "config": workload_config(V, cid, T, K),
+        "method": method,
         "roofline": roof,
-        "stages_ms": {k: round(v["mean_ms"] * v["calls"] / args.steps, 4) for k, v in st_l.items()},
-        "gpu_launches": l_l,
+        "stages_ms": {k: round(v["mean_ms"] * v["calls"] / args.steps, 4) for k, v in st_e.items()},
+        "stages_note": "per-call device times of an eager (graphs off) pass of the same step" if not grouped else "",
+        "ms_per_step_eager": ms_e,
+        "gpu_launches": l_l if grouped else l_e,
         "clocks": clk_l,
         "learned": quality,
         "full_grid": {"value": value_f, "ms_per_step": ms_f, "selector": args.selector,
@@ -310,25 +346,25 @@ def run_gb300(args) -> None:
     if rank == 0 and not args.no_e2e:
         # end to end through the public API from pinned host buffers
         Yh = torch.from_numpy(w.Y).pin_memory()
-        Xh = torch.from_numpy(w.X)
+        Xh = None if grouped else torch.from_numpy(w.X)
         e2e = {}
-        for name, kwh in (("learned", kw_l), ("full_grid", kw)):
+        for name, kwh in ((("full_grid", kw),) if grouped else (("learned", kw_l), ("full_grid", kw))):
             for _ in range(2):
-                r = fit_glm_arma11(Yh, Xh, **kwh)
+                r = fit(Yh, Xh, **kwh)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             for _ in range(args.e2e_steps):
-                r = fit_glm_arma11(Yh, Xh, **kwh)
+                r = fit(Yh, Xh, **kwh)
             torch.cuda.synchronize()
             dt = (time.perf_counter() - t0) / args.e2e_steps
             d2h = sum(t.numel() * t.element_size() for t in (r.betas, r.tstats, r.r2, r.arma_params,
                                                              r.arma_lambda, r.reml_likelihood, r.sigma2, r.fstats))
-            e2e[name] = {"value": args.voxels / dt, "unit": "voxels/s",
-                         "h2d_bytes_per_step": Yh.numel() * 4 + Xh.numel() * 4, "d2h_bytes_per_step": d2h,
-                         "ms_per_step": dt * 1e3}
-        line["e2e"] = e2e["learned"]
+            h2d = Yh.numel() * 4 + (0 if Xh is None else Xh.numel() * 4)
+            e2e[name] = {"value": V / dt, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
+                         "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3}
+        line["e2e"] = e2e["full_grid" if grouped else "learned"]
         line["full_grid"]["e2e"] = e2e["full_grid"]
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and not grouped and cid == 1:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_voxels)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -343,7 +379,9 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--voxels", type=int, default=200_000)
+    ap.add_argument("--voxels", type=int, default=None, help="default: the workload's size")
+    ap.add_argument("--workload", type=int, default=1, choices=[1, 2, 3, 4],
+                    help="1: N=400 p=20 V=200k (default); 2: grouped designs, censored; 3: p=130; 4: V=500k")
     ap.add_argument("--selector", default="hierarchical", choices=["hierarchical", "exhaustive"])
     ap.add_argument("--projector", default="tc", choices=["tc", "simt"])
     ap.add_argument("--e2e-steps", type=int, default=3)

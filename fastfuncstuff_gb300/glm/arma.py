@@ -343,16 +343,18 @@ def fit_glm_arma11(
     if factors is None and not use_graph:
         # the grid build runs on a side stream while the residualisation of the
         # first batch (against the design basis) runs on the main one
-        side = _side_stream(device)
+        overlap = K <= engine.BASIS_MAX_K
+        side = _side_stream(device) if overlap else None
         factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt,
                                        with_tc=projector == "tc" and K <= 256, stream=side)
-        built = torch.cuda.Event()
-        built.record(side)
-        main = torch.cuda.current_stream()
-        q0 = engine.design_basis(Xd)
+        if overlap:
+            built = torch.cuda.Event()
+            built.record(side)
+            main = torch.cuda.current_stream()
+            q0 = engine.design_basis(Xd)
 
-        def join():
-            main.wait_event(built)
+            def join():
+                main.wait_event(built)
     keep = [] if return_device else None
     chunks = {k: [] for k in ("best", "crit", "surf", "betas", "tstats", "sigma2", "fstats", "r2", "lam",
                               "cb", "ct", "resid", "resid_w", "pred", "lb")}

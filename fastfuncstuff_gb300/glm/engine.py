@@ -285,6 +285,11 @@ class PrepOut:
     yexp: torch.Tensor | None
 
 
+# the one-CTA design basis pays off (beside the grid build) for small designs;
+# wider ones take Q0 from the grid build (U of the pair (0, 0))
+BASIS_MAX_K = 32
+
+
 def design_basis(X: torch.Tensor) -> torch.Tensor:
     """Q0 [K][T]: the orthonormal basis of the design's columns (FP64 Cholesky),
     from X alone, so the residualisation need not wait for the grid build."""

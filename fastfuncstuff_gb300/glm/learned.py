@@ -470,13 +470,19 @@ class LearnedFitGraph:
 
     def _body_a(self):
         main = torch.cuda.current_stream()
+        overlap = self.X.shape[1] <= engine.BASIS_MAX_K
         self.f = engine.build_factors(self.X, self.grid, self.layout, center=(self.cflag, self.ccoef),
-                                      stream=self.side, **self.factor_kw)
-        built = torch.cuda.Event()
-        built.record(self.side)
-        q0 = engine.design_basis(self.X)
+                                      stream=self.side if overlap else None, **self.factor_kw)
+        q0 = join = None
+        if overlap:
+            built = torch.cuda.Event()
+            built.record(self.side)
+            q0 = engine.design_basis(self.X)
+
+            def join():
+                main.wait_event(built)
         self.ws = learned_windows(self.Y, self.f, self.proposal, self.layout, do_scale=self.do_scale,
-                                  recenter=self.recenter, q0=q0, join=lambda: main.wait_event(built))
+                                  recenter=self.recenter, q0=q0, join=join)
         self.host.copy_(self.ws.small, non_blocking=True)
 
     def _body_b(self):
