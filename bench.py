@@ -202,6 +202,14 @@ def roofline(dom: str, mean_ms: float, V: int, T: int, K: int, P: int, pk: dict,
         return {"kernel": dom, "bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": ach / fp32_peak, "traffic": None, "peak_src": "152 SMs x 128 FMA/clk at the sampled clock",
                 "work": "G'y, X b, G'r, X d (4 K x T products) and the whitening recurrence per voxel"}
+    if dom in ("ffs_grid_build", "ffs_grid_build_designs"):
+        # FP64: the whitened design (2 T K) and its Gram matrix (T K (K + 1)) per (design, pair)
+        items = P * extra.get("designs", 1)
+        flops = items * (2.0 * T * K * (K + 1) + 4.0 * T * K)
+        ach = flops / sec / 1e12
+        return {"kernel": dom, "bound": "fp64", "achieved": ach, "peak": 1.25, "unit": "TFLOP/s",
+                "frac": ach / 1.25, "traffic": None, "peak_src": "nominal GB300 FP64 (not measured)",
+                "work": "FP64 X_w = L^-1 X and X_w'X_w per (design, pair)"}
     # the rest stream HBM (prep: Y in; rows/time-major and the fp16 split out)
     ld = (T + 63) // 64 * 64
     byts = V * (T * 4 + T * 4 + 2 * ld * 2 + 16)
@@ -289,7 +297,8 @@ def run_gb300(args) -> None:
     pk = peaks()
     P = 561
     dom_f = max(st_f.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])[0]
-    roof_f = roofline(dom_f, st_f[dom_f]["mean_ms"], V, T, K, P, pk, clk_f["sm_mhz"], {})
+    roof_f = roofline(dom_f, st_f[dom_f]["mean_ms"], V, T, K, P, pk, clk_f["sm_mhz"],
+                      {"designs": len(w.designs)} if grouped else {})
     if grouped:
         ms_l, st_l, l_l, clk_l, value, roof, quality = ms_f, st_f, l_f, clk_f, value_f, roof_f, None
         st_e, ms_e = st_f, ms_f

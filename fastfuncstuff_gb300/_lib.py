@@ -48,7 +48,7 @@ class PrepArgs(C.Structure):
         ("yr_t", C.c_void_p),
         ("yr_hi", C.c_void_p), ("yr_lo", C.c_void_p), ("yexp", C.c_void_p),
         ("idx", C.c_void_p), ("feats", C.c_void_p), ("n_runs", C.c_int), ("run_start", C.c_void_p),
-        ("yr_rows", C.c_void_p), ("center_dev", C.c_void_p),
+        ("yr_rows", C.c_void_p), ("center_dev", C.c_void_p), ("tile_design", C.c_void_p),
     ]
 
 
@@ -68,7 +68,7 @@ class SurfaceArgs(C.Structure):
         ("yr_t", C.c_void_p), ("coef", C.c_void_p), ("logdet_R", C.c_void_p),
         ("logdet_XtX", C.c_void_p), ("proj", C.c_void_p), ("chunk_start", C.c_void_p),
         ("n_chunks", C.c_int), ("chunk_pairs", C.c_void_p), ("surf", C.c_void_p),
-        ("crit0", C.c_void_p),
+        ("crit0", C.c_void_p), ("tile_design", C.c_void_p),
     ]
 
 
@@ -93,7 +93,7 @@ class GlsArgs(C.Structure):
         ("betas", C.c_void_p), ("tstats", C.c_void_p), ("sigma2", C.c_void_p),
         ("fstats", C.c_void_p), ("r2", C.c_void_p), ("lam", C.c_void_p),
         ("cbeta", C.c_void_p), ("ct", C.c_void_p), ("resid", C.c_void_p),
-        ("resid_w", C.c_void_p), ("pred", C.c_void_p), ("center_dev", C.c_void_p),
+        ("resid_w", C.c_void_p), ("pred", C.c_void_p), ("center_dev", C.c_void_p), ("n_pairs", C.c_int),
     ]
 
 
@@ -104,6 +104,8 @@ SIGNATURES = {
     "ffs_last_error": ([], C.c_char_p),
     "ffs_grid_work_bytes": ([C.c_int, C.c_int, C.c_int], C.c_size_t),
     "ffs_grid_build": ([C.POINTER(GridDesc), C.POINTER(GridOut), C.c_void_p], C.c_int),
+    "ffs_grid_work_bytes_designs": ([C.c_int, C.c_int, C.c_int, C.c_int], C.c_size_t),
+    "ffs_grid_build_designs": ([C.POINTER(GridDesc), C.c_int, C.POINTER(GridOut), C.c_void_p], C.c_int),
     "ffs_grid_build_noalloc": ([C.POINTER(GridDesc), C.POINTER(GridOut), C.c_void_p], C.c_int),
     "ffs_reml_prep": ([C.POINTER(PrepArgs), C.c_void_p], C.c_int),
     "ffs_reml_project_tc": ([C.POINTER(ProjectArgs), C.c_void_p], C.c_int),

@@ -16,6 +16,11 @@
 
 namespace ffsk {
 
+// Row stride of every K x T matrix the library stores (U, G, Q0, Xt): T
+// rounded up to a multiple of 4, so each row starts on a 16-byte boundary;
+// the padding samples are zero.
+__host__ __device__ inline int ld_t(int T) { return (T + 3) & ~3; }
+
 // Records a message for ffs_last_error() on the calling host thread.
 void set_error(const char* fmt, ...);
 void clear_error();

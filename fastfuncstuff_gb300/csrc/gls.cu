@@ -27,6 +27,10 @@ struct GlsExtra {
   float* ljung_box;     // [V]
 };
 
+// A group key g is the pair itself (one design) or design * n_pairs + pair.
+__device__ __forceinline__ int pair_of(const ffs_gls_args& a, int g) { return a.n_pairs > 0 ? g % a.n_pairs : g; }
+__device__ __forceinline__ int design_of(const ffs_gls_args& a, int g) { return a.n_pairs > 0 ? g / a.n_pairs : 0; }
+
 __device__ void gls_finish(const ffs_gls_args& a, const GlsExtra& x, int v, int g, float* beta, const float* w,
                            float ssr, float sst, float ssw, float m, float sc, float* bins);
 
@@ -54,7 +58,7 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
 
   // b0 = G' y
   for (int j = 0; j < K; ++j) {
-    const float* gj = Gp + (size_t)j * T;
+    const float* gj = Gp + (size_t)j * ld_t(T);
     float s = 0.f;
     for (int t = lane; t < T; t += 32) s = fmaf(gj[t], ys[t], s);
     s = warp_sum(s);
@@ -64,12 +68,12 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
   // refinement: b += G' (y - X b)
   for (int t = lane; t < T; t += 32) {
     float acc = ys[t];
-    for (int j = 0; j < K; ++j) acc = fmaf(-Xt[(size_t)j * T + t], beta[j], acc);
+    for (int j = 0; j < K; ++j) acc = fmaf(-Xt[(size_t)j * ld_t(T) + t], beta[j], acc);
     r[t] = acc;
   }
   __syncwarp();
   for (int j = 0; j < K; ++j) {
-    const float* gj = Gp + (size_t)j * T;
+    const float* gj = Gp + (size_t)j * ld_t(T);
     float s = 0.f;
     for (int t = lane; t < T; t += 32) s = fmaf(gj[t], r[t], s);
     s = warp_sum(s);
@@ -80,7 +84,7 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
   float ssr = 0.f, sy = 0.f;
   for (int t = lane; t < T; t += 32) {
     float acc = ys[t];
-    for (int j = 0; j < K; ++j) acc = fmaf(-Xt[(size_t)j * T + t], beta[j], acc);
+    for (int j = 0; j < K; ++j) acc = fmaf(-Xt[(size_t)j * ld_t(T) + t], beta[j], acc);
     r[t] = acc;
     ssr = fmaf(acc, acc, ssr);
     sy += ys[t];
@@ -102,7 +106,7 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
   }
   __syncwarp();
   // whitened residual r_w = L^-1 r (serial recurrence on lane 0), into ys
-  const float4* cf = reinterpret_cast<const float4*>(a.coef) + (size_t)g * T;
+  const float4* cf = reinterpret_cast<const float4*>(a.coef) + (size_t)pair_of(a, g) * T;
   if (lane == 0) {
     float rp = 0.f, vp = 0.f;
     for (int t = 0; t < T; ++t) {
@@ -215,7 +219,7 @@ __device__ void gls_finish(const ffs_gls_args& a, const GlsExtra& x, const int v
     const bool deg = sst <= 1e-10f;
     const float r2 = 1.0f - ssr / fmaxf(sst, 1e-10f);
     a.r2[v] = deg ? 0.f : fminf(r2, 1.0f);
-    const float af = a.a[g], bf = a.b[g];
+    const float af = a.a[pair_of(a, g)], bf = a.b[pair_of(a, g)];
     if (a.lambda_fp32) {
       a.lam[v] = lambda_out_f32(af, bf);
     } else {
@@ -235,7 +239,8 @@ __global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, Gls
   if (i >= a.V) return;
   const int v = a.order ? a.order[i] : i;
   const int g = a.best[v];
-  gls_voxel(a, x, v, g, a.G + (size_t)g * a.K * a.T, a.Xt, ys, ys + ld_s, ys + 2 * ld_s, ys + 2 * ld_s + kp);
+  gls_voxel(a, x, v, g, a.G + (size_t)g * a.K * ld_t(a.T), a.Xt + (size_t)design_of(a, g) * a.K * ld_t(a.T), ys, ys + ld_s,
+            ys + 2 * ld_s, ys + 2 * ld_s + kp);
 }
 
 // Tiles of up to GLS_TILE voxels that share one pair (voxels grouped by pair:
@@ -255,13 +260,13 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
                                                                    const int* tile_start, int P, int ld, int kp,
                                                                    int hb) {
   extern __shared__ float4 sm4[];
-  const int T = a.T, K = a.K, nq = T >> 2;
+  const int T = a.T, K = a.K, LT = ld_t(T), nq = LT >> 2;
+  const bool vec = (T & 3) == 0;  // 16-byte rows of Y and of the [V][T] outputs
   float* Ys = reinterpret_cast<float*>(sm4);        // [32][ld]
   float* C0 = Ys + (size_t)TILE_V * ld;             // [K][32] b0
   float* C1 = C0 + (size_t)K * TILE_V;              // [K][32] d
-  float* part = C1 + (size_t)K * TILE_V;            // [TILE_TS][K][32]
-  float* red = part + TILE_TS * (size_t)K * TILE_V;  // [3][8][32] SS_res, SS_tot, SS_w partials
-  float* vend = red + 3 * TILE_WARPS * TILE_V;      // [8][32]
+  float* red = C1 + (size_t)K * TILE_V;             // [8][32] SS_w partials
+  float* vend = red + TILE_WARPS * TILE_V;          // [8][32]
   float* carry = vend + TILE_WARPS * TILE_V;        // [8][32]
   float* Hs = carry + TILE_WARPS * TILE_V;          // [32]
   float* st = Hs + TILE_V;                          // [6][32] m, sc, mean, ssr, sst, ssw
@@ -295,24 +300,32 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
     }
     const int v = a.order[j0 + i];
     const float sc = a.scale[v];
-    const float4* y4 = reinterpret_cast<const float4*>(a.Y + (size_t)v * T);
+    const float* yv = a.Y + (size_t)v * T;
+    // quad q of the row; samples past T read as zero
+    auto quad = [&](int q) {
+      if (vec) return reinterpret_cast<const float4*>(yv)[q];
+      const int t = 4 * q;
+      return make_float4(yv[t], t + 1 < T ? yv[t + 1] : 0.f, t + 2 < T ? yv[t + 2] : 0.f,
+                         t + 3 < T ? yv[t + 3] : 0.f);
+    };
     float m = 0.f;
     if (a.center_dev ? (*a.center_dev != 0) : (a.center != 0)) {
       float s = 0.f;
       for (int q = lane; q < nq; q += 32) {
-        const float4 y = y4[q];
+        const float4 y = quad(q);
         s += ((y.x + y.y) + y.z) + y.w;
       }
       m = warp_sum(s) / (float)T;
     }
     float sy = 0.f;
     for (int q = lane; q < nq; q += 32) {
-      const float4 y = y4[q];
+      const float4 y = quad(q);
+      const int t = 4 * q;
       float4 r;
       r.x = __fdiv_rn(__fsub_rn(y.x, m), sc);
-      r.y = __fdiv_rn(__fsub_rn(y.y, m), sc);
-      r.z = __fdiv_rn(__fsub_rn(y.z, m), sc);
-      r.w = __fdiv_rn(__fsub_rn(y.w, m), sc);
+      r.y = t + 1 < T ? __fdiv_rn(__fsub_rn(y.y, m), sc) : 0.f;
+      r.z = t + 2 < T ? __fdiv_rn(__fsub_rn(y.z, m), sc) : 0.f;
+      r.w = t + 3 < T ? __fdiv_rn(__fsub_rn(y.w, m), sc) : 0.f;
       row4[q] = r;
       sy += ((r.x + r.y) + r.z) + r.w;
     }
@@ -325,73 +338,94 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
   }
   __syncthreads();
 
-  const float* Gg = a.G + (size_t)g * K * T;
-  int q0, q1;
-  tile_qrange(T, wid, q0, q1);
-  float4* rr = reinterpret_cast<float4*>(Ys + (size_t)lane * ld);
-  // b0 = G'y; SS_tot of the owned samples; r = y - X b0
-  tile_project(Gg, Ys, T, ld, K, C0, part);
-  {
-    const float mu = st[2 * TILE_V + lane];
+  const float* Gg = a.G + (size_t)g * K * LT;
+  const float* Xt = a.Xt + (size_t)design_of(a, g) * K * LT;
+  // b0 = G'y; SS_tot; r = y - X b0. Warp w owns the rows 4w .. 4w+3 in the
+  // row passes (tile_subtract's layout), lanes over quads.
+  tile_project(Gg, LT, Ys, ld, K, C0);
+#pragma unroll
+  for (int i = 0; i < TILE_SUB_VB; ++i) {
+    const int l = TILE_SUB_VB * wid + i;
+    const float mu = st[2 * TILE_V + l];
+    const float4* r4 = reinterpret_cast<const float4*>(Ys + (size_t)l * ld);
     float sst = 0.f;
-    for (int q = q0; q < q1; ++q) {
-      const float4 r = rr[q];
+    for (int q = lane; q < nq; q += 32) {
+      const float4 r = r4[q];
+      const int t = 4 * q;
       float d = r.x - mu;
       sst = fmaf(d, d, sst);
-      d = r.y - mu;
+      d = t + 1 < T ? r.y - mu : 0.f;
       sst = fmaf(d, d, sst);
-      d = r.z - mu;
+      d = t + 2 < T ? r.z - mu : 0.f;
       sst = fmaf(d, d, sst);
-      d = r.w - mu;
+      d = t + 3 < T ? r.w - mu : 0.f;
       sst = fmaf(d, d, sst);
     }
-    red[(TILE_WARPS + wid) * TILE_V + lane] = sst;
+    sst = warp_sum(sst);
+    if (lane == 0) st[4 * TILE_V + l] = sst;
   }
-  tile_subtract(a.Xt, C0, Ys, T, ld, K);
+  tile_subtract(Xt, LT, C0, Ys, ld, K);
   __syncthreads();
   // d = G'r; r -= X d; SS_res and the unwhitened outputs
-  tile_project(Gg, Ys, T, ld, K, C1, part);
-  tile_subtract(a.Xt, C1, Ys, T, ld, K);
-  {
+  tile_project(Gg, LT, Ys, ld, K, C1);
+  tile_subtract(Xt, LT, C1, Ys, ld, K);
+#pragma unroll
+  for (int i = 0; i < TILE_SUB_VB; ++i) {
+    const int l = TILE_SUB_VB * wid + i;
+    const float4* r4 = reinterpret_cast<const float4*>(Ys + (size_t)l * ld);
     float ssr = 0.f;
-    for (int q = q0; q < q1; ++q) {
-      const float4 r = rr[q];
+    for (int q = lane; q < nq; q += 32) {
+      const float4 r = r4[q];
       ssr = fmaf(r.x, r.x, ssr);
       ssr = fmaf(r.y, r.y, ssr);
       ssr = fmaf(r.z, r.z, ssr);
       ssr = fmaf(r.w, r.w, ssr);
     }
-    red[wid * TILE_V + lane] = ssr;
-    if (lane < n && (a.resid || a.pred)) {
-      const int v = a.order[j0 + lane];
-      const float m = st[lane], sc = st[TILE_V + lane];
-      for (int q = q0; q < q1; ++q) {
+    ssr = warp_sum(ssr);
+    if (lane == 0) st[3 * TILE_V + l] = ssr;
+    if (l < n && (a.resid || a.pred)) {  // warp-uniform
+      const int v = a.order[j0 + l];
+      const float m = st[l], sc = st[TILE_V + l];
+      // [V][T] rows: 16-byte words when T % 4 == 0, single samples otherwise
+      auto put = [&](float* row, int q, float4 x) {
+        if (vec) {
+          reinterpret_cast<float4*>(row)[q] = x;
+          return;
+        }
+        const int t = 4 * q;
+        row[t] = x.x;
+        if (t + 1 < T) row[t + 1] = x.y;
+        if (t + 2 < T) row[t + 2] = x.z;
+        if (t + 3 < T) row[t + 3] = x.w;
+      };
+      for (int q = lane; q < nq; q += 32) {
         if (a.resid) {
-          const float4 r = rr[q];
-          reinterpret_cast<float4*>(a.resid + (size_t)v * T)[q] = make_float4(r.x * sc, r.y * sc, r.z * sc, r.w * sc);
+          const float4 r = r4[q];
+          put(a.resid + (size_t)v * T, q, make_float4(r.x * sc, r.y * sc, r.z * sc, r.w * sc));
         }
         if (a.pred) {  // X b, b = b0 + d
           float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
           for (int j = 0; j < K; ++j) {
-            const float bj = C0[j * TILE_V + lane] + C1[j * TILE_V + lane];
-            const float4 xj = __ldg(reinterpret_cast<const float4*>(a.Xt + (size_t)j * T) + q);
+            const float bj = C0[j * TILE_V + l] + C1[j * TILE_V + l];
+            const float4 xj = __ldg(reinterpret_cast<const float4*>(Xt + (size_t)j * LT) + q);
             p.x = fmaf(xj.x, bj, p.x);
             p.y = fmaf(xj.y, bj, p.y);
             p.z = fmaf(xj.z, bj, p.z);
             p.w = fmaf(xj.w, bj, p.w);
           }
-          reinterpret_cast<float4*>(a.pred + (size_t)v * T)[q] =
-              make_float4(fmaf(p.x, sc, m), fmaf(p.y, sc, m), fmaf(p.z, sc, m), fmaf(p.w, sc, m));
+          put(a.pred + (size_t)v * T, q, make_float4(fmaf(p.x, sc, m), fmaf(p.y, sc, m), fmaf(p.z, sc, m),
+                                                     fmaf(p.w, sc, m)));
         }
       }
     }
   }
   __syncthreads();
+  float4* rr = reinterpret_cast<float4*>(Ys + (size_t)lane * ld);
 
   // whitened residual by segments of the time axis
   const int SQ = (nq + TILE_WARPS - 1) / TILE_WARPS;
   const int s0 = min(T, wid * SQ * 4), s1 = min(T, (wid + 1) * SQ * 4);
-  const float4* cf = reinterpret_cast<const float4*>(a.coef) + (size_t)g * T;
+  const float4* cf = reinterpret_cast<const float4*>(a.coef) + (size_t)pair_of(a, g) * T;
   float rp = s0 > 0 ? Ys[(size_t)lane * ld + s0 - 1] : 0.f;
   __syncthreads();
   {
@@ -399,16 +433,18 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
     for (int t = s0; t < s1; t += 4) {
       const float4 r = rr[t >> 2];
       const float rv[4] = {r.x, r.y, r.z, r.w};
-      float o[4];
+      float o[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const float4 q = __ldg(cf + t + k);
-        const float z = fmaf(-q.x, rp, rv[k]);
-        const float vt = fmaf(-q.y, vp, z);
-        o[k] = vt;
-        rp = rv[k];
-        vp = vt;
-        H *= -q.y;
+        if (t + k < s1) {  // s1 = T ends the last segment inside a quad
+          const float4 q = __ldg(cf + t + k);
+          const float z = fmaf(-q.x, rp, rv[k]);
+          const float vt = fmaf(-q.y, vp, z);
+          o[k] = vt;
+          rp = rv[k];
+          vp = vt;
+          H *= -q.y;
+        }
       }
       rr[t >> 2] = make_float4(o[0], o[1], o[2], o[3]);
     }
@@ -430,27 +466,26 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
     for (int t = s0; t < s1; t += 4) {
       const float4 r = rr[t >> 2];
       const float rv[4] = {r.x, r.y, r.z, r.w};
-      float o[4];
+      float o[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const float4 q = __ldg(cf + t + k);
-        h *= -q.y;
-        const float wt = fmaf(h, cin, rv[k]) * q.w;
-        ssw = fmaf(wt, wt, ssw);
-        o[k] = wt;
+        if (t + k < s1) {
+          const float4 q = __ldg(cf + t + k);
+          h *= -q.y;
+          const float wt = fmaf(h, cin, rv[k]) * q.w;
+          ssw = fmaf(wt, wt, ssw);
+          o[k] = wt;
+        }
       }
       rr[t >> 2] = make_float4(o[0], o[1], o[2], o[3]);
     }
-    red[(2 * TILE_WARPS + wid) * TILE_V + lane] = ssw;
+    red[wid * TILE_V + lane] = ssw;
   }
   __syncthreads();
   if (wid == 0) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      float s = 0.f;
-      for (int w = 0; w < TILE_WARPS; ++w) s += red[(k * TILE_WARPS + w) * TILE_V + lane];
-      st[(3 + k) * TILE_V + lane] = s;
-    }
+    float s = 0.f;
+    for (int w = 0; w < TILE_WARPS; ++w) s += red[w * TILE_V + lane];
+    st[5 * TILE_V + lane] = s;
   }
   __syncthreads();
 
@@ -538,10 +573,10 @@ extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* 
   const int ld = tile_ld(a->T);
   const int kp = (a->K + 3) & ~3;
   const int hb = (lj_h + 4) & ~3;
-  const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + (2 + TILE_TS) * (size_t)a->K * TILE_V +
-                                       (3 + 2) * TILE_WARPS * TILE_V + TILE_V + 6 * TILE_V +
+  const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + 2 * (size_t)a->K * TILE_V +
+                                       (1 + 2) * TILE_WARPS * TILE_V + TILE_V + 6 * TILE_V +
                                        (size_t)TILE_WARPS * (kp + hb));
-  if (a->T % 4 != 0 || smem > 200 * 1024) {  // no 16-byte rows, or the tile does not fit: one warp per voxel
+  if (smem > 200 * 1024) {  // the tile does not fit: one warp per voxel
     return ffs_reml_gls_ex(a, lj_h, lj_tau, lj_w, ljung_box, stream);
   }
   cudaStream_t st = (cudaStream_t)stream;

@@ -115,277 +115,288 @@ struct BuildArgs {
   ffs_grid_out o;
 };
 
-__global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args) {
+// Items are (design, pair) = (item / P, item % P); a CTA takes items
+// blockIdx.x, blockIdx.x + gridDim.x, ... with scratch slot blockIdx.x.
+// Design-dependent outputs sit at pd = design * P + pair; coef and logdet_R
+// depend on the pair only and are written (with identical values) by the
+// items of every design.
+__global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_designs) {
   const ffs_grid_desc& d = args.d;
   const ffs_grid_out& o = args.o;
-  const int p = blockIdx.x;
-  const int T = d.T, K = d.K;
-  PairScratch s = scratch_of(o.work, p, T, K);
+  const int T = d.T, K = d.K, LT = ld_t(T);
+  PairScratch s = scratch_of(o.work, blockIdx.x, T, K);
 
   __shared__ double red[32];
   __shared__ int flag, bad_r;
 
-  const float af = d.a[p], bf = d.b[p];
-  const double a = (double)af;
-  const double lam = d.lambda_fp32 ? (double)lambda_f32(af, bf) : lambda_f64(a, (double)bf);
-  if (threadIdx.x == 0) bad_r = 0;
-  __syncthreads();
+  for (int item = blockIdx.x; item < d.P * n_designs; item += gridDim.x) {
+    const int p = item % d.P, pd = item;
+    const float* Xd = d.X + (size_t)(item / d.P) * T * K;
+    const float af = d.a[p], bf = d.b[p];
+    const double a = (double)af;
+    const double lam = d.lambda_fp32 ? (double)lambda_f32(af, bf) : lambda_f64(a, (double)bf);
+    if (threadIdx.x == 0) bad_r = 0;
+    __syncthreads();
 
-  // ---- 1. per-run LDL' of the AR-filtered tridiagonal correlation: the
-  // serial recursion m_t = T_t,t-1 / D_t-1, D_t = T_tt - m_t T_t,t-1 (one
-  // thread per run; unit gaps need no pow: a^1 = a and a^0 = 1 exactly), then
-  // sqrt, log and the reciprocals of every sample in parallel
-  for (int r = threadIdx.x; r < d.n_runs; r += blockDim.x) {
-    const int t0 = d.run_start[r], t1 = d.run_start[r + 1];
-    double Dprev = 1.0;
-    for (int t = t0; t < t1; ++t) {
-      double c = 0.0, m = 0.0, D = 1.0;
-      // lambda == 0: every lag correlation is zero, R = I exactly
-      if (t > t0 && lam != 0.0) {
-        const int gap = d.tau[t] - d.tau[t - 1];
-        double rho;
-        if (gap == 1) {
-          c = a;
-          rho = lam;
-        } else {
-          c = pow(a, (double)gap);
-          rho = lam * pow(a, (double)(gap - 1));
+    // ---- 1. per-run LDL' of the AR-filtered tridiagonal correlation: the
+    // serial recursion m_t = T_t,t-1 / D_t-1, D_t = T_tt - m_t T_t,t-1 (one
+    // thread per run; unit gaps need no pow: a^1 = a and a^0 = 1 exactly), then
+    // sqrt, log and the reciprocals of every sample in parallel
+    for (int r = threadIdx.x; r < d.n_runs; r += blockDim.x) {
+      const int t0 = d.run_start[r], t1 = d.run_start[r + 1];
+      double Dprev = 1.0;
+      for (int t = t0; t < t1; ++t) {
+        double c = 0.0, m = 0.0, D = 1.0;
+        // lambda == 0: every lag correlation is zero, R = I exactly
+        if (t > t0 && lam != 0.0) {
+          const int gap = d.tau[t] - d.tau[t - 1];
+          double rho;
+          if (gap == 1) {
+            c = a;
+            rho = lam;
+          } else {
+            c = pow(a, (double)gap);
+            rho = lam * pow(a, (double)(gap - 1));
+          }
+          const double Ttt = 1.0 + c * c - 2.0 * c * rho;
+          const double Toff = rho - c;
+          m = Toff / Dprev;
+          D = Ttt - m * Toff;
         }
-        const double Ttt = 1.0 + c * c - 2.0 * c * rho;
-        const double Toff = rho - c;
-        m = Toff / Dprev;
-        D = Ttt - m * Toff;
-      }
-      if (!(D > 0.0)) {
-        bad_r = 1;
-        D = 1.0;
-      }
-      double* cm = s.cm + 4 * t;
-      cm[0] = c; cm[1] = m; cm[2] = D;
-      Dprev = D;
-    }
-  }
-  __syncthreads();
-  {
-    double ld = 0.0;
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
-      double* cm = s.cm + 4 * t;
-      const double D = cm[2];
-      const double sD = sqrt(D);
-      const double rsD = 1.0 / sD;
-      ld += 2.0 * log(sD + 1e-10);
-      cm[3] = rsD;
-      reinterpret_cast<float4*>(o.coef)[(size_t)p * T + t] =
-          make_float4((float)cm[0], (float)cm[1], (float)(1.0 / D), (float)rsD);
-    }
-    ld = block_sum(ld, red);
-    if (threadIdx.x == 0) o.logdet_R[p] = ld;
-  }
-  __syncthreads();
-
-  // ---- 2. X_w = L^-1 X, one column per thread
-  for (int j = threadIdx.x; j < K; j += blockDim.x) {
-    double xp = 0.0, vp = 0.0;
-    for (int t = 0; t < T; ++t) {
-      const double* cm = s.cm + 4 * t;
-      const double x = (double)d.X[(size_t)t * K + j];
-      const double z = x - cm[0] * xp;
-      const double v = z - cm[1] * vp;
-      s.Xw[(size_t)j * T + t] = v * cm[3];
-      xp = x;
-      vp = v;
-    }
-  }
-  __syncthreads();
-
-  // ---- 3. X_w'X_w (full symmetric) into Lx, and the fp32 copy
-  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
-    const int i = idx / K, j = idx % K;
-    if (j > i) continue;
-    const double* xi = s.Xw + (size_t)i * T;
-    const double* xj = s.Xw + (size_t)j * T;
-    double acc = 0.0;
-    for (int t = 0; t < T; ++t) acc += xi[t] * xj[t];
-    s.Lx[i * K + j] = acc;
-    s.Lx[j * K + i] = acc;
-    o.XtX[(size_t)p * K * K + i * K + j] = (float)acc;
-    o.XtX[(size_t)p * K * K + j * K + i] = (float)acc;
-  }
-  __syncthreads();
-
-  // ---- 4. Cholesky of X_w'X_w, QR (modified Gram-Schmidt, twice) otherwise
-  int info = 0;
-  if (!block_cholesky(s.Lx, K, K, &flag)) {
-    info = 1;
-    // Q and R from X_w; Lx := R' (lower), so that X_w'X_w = Lx Lx'.
-    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) s.Lx[idx] = 0.0;
-    __syncthreads();
-    for (int j = 0; j < K; ++j) {
-      double* q = s.Qm + (size_t)j * T;
-      for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] = s.Xw[(size_t)j * T + t];
-      __syncthreads();
-      for (int pass = 0; pass < 2; ++pass) {
-        for (int i = 0; i < j; ++i) {
-          const double* qi = s.Qm + (size_t)i * T;
-          double part = 0.0;
-          for (int t = threadIdx.x; t < T; t += blockDim.x) part += qi[t] * q[t];
-          const double rij = block_sum(part, red);
-          for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] -= rij * qi[t];
-          if (threadIdx.x == 0) s.Lx[j * K + i] += rij;
-          __syncthreads();
+        if (!(D > 0.0)) {
+          bad_r = 1;
+          D = 1.0;
         }
-      }
-      double part = 0.0;
-      for (int t = threadIdx.x; t < T; t += blockDim.x) part += q[t] * q[t];
-      const double nrm = sqrt(block_sum(part, red));
-      const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
-      for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] *= inv;
-      if (threadIdx.x == 0) s.Lx[j * K + j] = nrm;
-      __syncthreads();
-    }
-  }
-  if (bad_r) info = 2;
-  __syncthreads();
-
-  if (threadIdx.x == 0) {
-    double ld = 0.0;
-    for (int j = 0; j < K; ++j) ld += 2.0 * log(fabs(s.Lx[j * K + j]) + 1e-10);
-    o.logdet_XtX[p] = ld;
-    o.info[p] = info;
-  }
-
-  // ---- 5. Q = X_w Lx^-T in fp32 (Q, U and G only leave as fp32 or fp16
-  // splits; the factorisation and the logdets above stay FP64). The two [K][T]
-  // FP64 slots are reused as fp32 arrays; the QR fallback converts its Q.
-  float* const xw_f = reinterpret_cast<float*>(s.Xw);
-  float* const qm_f = reinterpret_cast<float*>(s.Qm);
-  float* const lx_f = reinterpret_cast<float*>(s.S);  // [K][K] Lx, then Li in lx_f + K*K
-  float* qf;
-  float* uf;
-  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) lx_f[idx] = (float)s.Lx[idx];
-  __syncthreads();
-  if (info != 1) {
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
-      for (int j = 0; j < K; ++j) {
-        float acc = (float)s.Xw[(size_t)j * T + t];
-        for (int i = 0; i < j; ++i) acc = fmaf(-lx_f[j * K + i], qm_f[(size_t)i * T + t], acc);
-        qm_f[(size_t)j * T + t] = acc / lx_f[j * K + j];
+        double* cm = s.cm + 4 * t;
+        cm[0] = c; cm[1] = m; cm[2] = D;
+        Dprev = D;
       }
     }
-    qf = qm_f;
-    uf = xw_f;
-  } else {
-    for (int idx = threadIdx.x; idx < K * T; idx += blockDim.x) xw_f[idx] = (float)s.Qm[idx];
-    qf = xw_f;
-    uf = qm_f;
-  }
-  __syncthreads();
-
-  // ---- 6. U = L^-T Q = A' L~^-T D^-1/2 Q (backward recursions) in fp32, with
-  // the fp32 coefficients of phase 1
-  const float4* cf = reinterpret_cast<const float4*>(o.coef) + (size_t)p * T;
-  float umax_local = 0.f;
-  for (int j = threadIdx.x; j < K; j += blockDim.x) {
-    const float* q = qf + (size_t)j * T;
-    float* u = uf + (size_t)j * T;
-    float xn = 0.f, mn = 0.f, cn = 0.f;  // x_{t+1}, m_{t+1}, c_{t+1}
-    for (int t = T - 1; t >= 0; --t) {
-      const float4 c4 = cf[t];  // (c, m, 1/D, 1/sqrt(D))
-      const float x = fmaf(-mn, xn, q[t] * c4.w);
-      const float ut = fmaf(-cn, xn, x);
-      u[t] = ut;
-      o.U[((size_t)p * K + j) * T + t] = ut;
-      umax_local = fmaxf(umax_local, fabsf(ut));
-      xn = x;
-      mn = c4.y;
-      cn = c4.x;
-    }
-  }
-  __syncthreads();
-  if (o.U_hi) {
-    // fp16 hi/lo split of U * 2^e, e placing max|U| in [128, 256)
-    double um = umax_local;
-    for (int off = 16; off > 0; off >>= 1) um = fmax(um, __shfl_xor_sync(0xffffffffu, um, off));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = um;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double mx = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = fmax(mx, red[w]);
-      red[0] = mx;
+    {
+      double ld = 0.0;
+      for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        double* cm = s.cm + 4 * t;
+        const double D = cm[2];
+        const double sD = sqrt(D);
+        const double rsD = 1.0 / sD;
+        ld += 2.0 * log(sD + 1e-10);
+        cm[3] = rsD;
+        reinterpret_cast<float4*>(o.coef)[(size_t)p * T + t] =
+            make_float4((float)cm[0], (float)cm[1], (float)(1.0 / D), (float)rsD);
+      }
+      ld = block_sum(ld, red);
+      if (threadIdx.x == 0) o.logdet_R[p] = ld;
     }
     __syncthreads();
-    const int e = scale_exp((float)red[0]);
-    if (threadIdx.x == 0) o.uexp[p] = e;
-    for (int idx = threadIdx.x; idx < K * d.ld_u; idx += blockDim.x) {
-      const int j = idx / d.ld_u, t = idx % d.ld_u;
-      uint16_t hi = 0, lo = 0;
-      if (t < T) split_fp16(ldexpf(uf[(size_t)j * T + t], e), hi, lo);
-      const size_t at = ((size_t)p * K + j) * d.ld_u + t;
-      o.U_hi[at] = hi;
-      o.U_lo[at] = lo;
-    }
-  }
-  __syncthreads();
 
-  // ---- 7. Lx^-1, A = Lx^-T Lx^-1, diag(A)
-  block_tri_inverse(s.Lx, s.Li, K, K);
-  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
-    const int i = idx / K, j = idx % K;
-    double acc = 0.0;
-    for (int k = max(i, j); k < K; ++k) acc += s.Li[k * K + i] * s.Li[k * K + j];
-    s.A[i * K + j] = acc;
-    if (i == j) o.Adiag[(size_t)p * K + j] = (float)acc;
-  }
-  __syncthreads();
-
-  // ---- 8. G = U Lx^-1 in fp32 (row t of G solves g Lx = u_t); Gsum = G' 1
-  // accumulated in FP64
-  float* const li_f = lx_f + (size_t)K * K;
-  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) li_f[idx] = (float)s.Li[idx];
-  __syncthreads();
-  for (int t = threadIdx.x; t < T; t += blockDim.x) {
-    for (int j = 0; j < K; ++j) {
-      float acc = 0.f;
-      for (int i = j; i < K; ++i) acc = fmaf(uf[(size_t)i * T + t], li_f[i * K + j], acc);
-      o.G[((size_t)p * K + j) * T + t] = acc;
-    }
-  }
-  __syncthreads();
-  if (o.Gsum) {
+    // ---- 2. X_w = L^-1 X, one column per thread
     for (int j = threadIdx.x; j < K; j += blockDim.x) {
-      double acc = 0.0;
-      for (int t = 0; t < T; ++t) acc += (double)o.G[((size_t)p * K + j) * T + t];
-      o.Gsum[(size_t)p * K + j] = (float)acc;
-    }
-  }
-
-  // ---- 9. task-column F matrix inv(A_task + 1e-8 I) and GLT variances c A c'
-  const int nt = d.n_task;
-  if (nt > 0 && o.Ftask) {
-    for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
-      const int i = idx / nt, j = idx % nt;
-      s.S[i * nt + j] = s.A[d.task_idx[i] * K + d.task_idx[j]] + (i == j ? 1e-8 : 0.0);
+      double xp = 0.0, vp = 0.0;
+      for (int t = 0; t < T; ++t) {
+        const double* cm = s.cm + 4 * t;
+        const double x = (double)Xd[(size_t)t * K + j];
+        const double z = x - cm[0] * xp;
+        const double v = z - cm[1] * vp;
+        s.Xw[(size_t)j * T + t] = v * cm[3];
+        xp = x;
+        vp = v;
+      }
     }
     __syncthreads();
-    block_cholesky(s.S, nt, nt, &flag);
-    // Li (free now) holds the inverse factor; Ftask = Li' Li
-    block_tri_inverse(s.S, s.Li, nt, nt);
-    for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
-      const int i = idx / nt, j = idx % nt;
+
+    // ---- 3. X_w'X_w (full symmetric) into Lx, and the fp32 copy
+    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
+      const int i = idx / K, j = idx % K;
+      if (j > i) continue;
+      const double* xi = s.Xw + (size_t)i * T;
+      const double* xj = s.Xw + (size_t)j * T;
       double acc = 0.0;
-      for (int k = max(i, j); k < nt; ++k) acc += s.Li[k * nt + i] * s.Li[k * nt + j];
-      o.Ftask[(size_t)p * nt * nt + idx] = (float)acc;
+      for (int t = 0; t < T; ++t) acc += xi[t] * xj[t];
+      s.Lx[i * K + j] = acc;
+      s.Lx[j * K + i] = acc;
+      o.XtX[(size_t)pd * K * K + i * K + j] = (float)acc;
+      o.XtX[(size_t)pd * K * K + j * K + i] = (float)acc;
     }
-  }
-  if (d.n_glt > 0 && o.glt_var) {
-    for (int c = 0; c < d.n_glt; ++c) {
-      const float* gc = d.glt + (size_t)c * K;
-      double part = 0.0;
-      for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x)
-        part += (double)gc[idx / K] * s.A[idx] * (double)gc[idx % K];
-      const double v = block_sum(part, red);
-      if (threadIdx.x == 0) o.glt_var[(size_t)p * d.n_glt + c] = (float)v;
+    __syncthreads();
+
+    // ---- 4. Cholesky of X_w'X_w, QR (modified Gram-Schmidt, twice) otherwise
+    int info = 0;
+    if (!block_cholesky(s.Lx, K, K, &flag)) {
+      info = 1;
+      // Q and R from X_w; Lx := R' (lower), so that X_w'X_w = Lx Lx'.
+      for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) s.Lx[idx] = 0.0;
+      __syncthreads();
+      for (int j = 0; j < K; ++j) {
+        double* q = s.Qm + (size_t)j * T;
+        for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] = s.Xw[(size_t)j * T + t];
+        __syncthreads();
+        for (int pass = 0; pass < 2; ++pass) {
+          for (int i = 0; i < j; ++i) {
+            const double* qi = s.Qm + (size_t)i * T;
+            double part = 0.0;
+            for (int t = threadIdx.x; t < T; t += blockDim.x) part += qi[t] * q[t];
+            const double rij = block_sum(part, red);
+            for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] -= rij * qi[t];
+            if (threadIdx.x == 0) s.Lx[j * K + i] += rij;
+            __syncthreads();
+          }
+        }
+        double part = 0.0;
+        for (int t = threadIdx.x; t < T; t += blockDim.x) part += q[t] * q[t];
+        const double nrm = sqrt(block_sum(part, red));
+        const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+        for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] *= inv;
+        if (threadIdx.x == 0) s.Lx[j * K + j] = nrm;
+        __syncthreads();
+      }
     }
+    if (bad_r) info = 2;
+    __syncthreads();
+
+    if (threadIdx.x == 0) {
+      double ld = 0.0;
+      for (int j = 0; j < K; ++j) ld += 2.0 * log(fabs(s.Lx[j * K + j]) + 1e-10);
+      o.logdet_XtX[pd] = ld;
+      o.info[pd] = info;
+    }
+
+    // ---- 5. Q = X_w Lx^-T in fp32 (Q, U and G only leave as fp32 or fp16
+    // splits; the factorisation and the logdets above stay FP64). The two [K][T]
+    // FP64 slots are reused as fp32 arrays; the QR fallback converts its Q.
+    float* const xw_f = reinterpret_cast<float*>(s.Xw);
+    float* const qm_f = reinterpret_cast<float*>(s.Qm);
+    float* const lx_f = reinterpret_cast<float*>(s.S);  // [K][K] Lx, then Li in lx_f + K*K
+    float* qf;
+    float* uf;
+    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) lx_f[idx] = (float)s.Lx[idx];
+    __syncthreads();
+    if (info != 1) {
+      for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        for (int j = 0; j < K; ++j) {
+          float acc = (float)s.Xw[(size_t)j * T + t];
+          for (int i = 0; i < j; ++i) acc = fmaf(-lx_f[j * K + i], qm_f[(size_t)i * T + t], acc);
+          qm_f[(size_t)j * T + t] = acc / lx_f[j * K + j];
+        }
+      }
+      qf = qm_f;
+      uf = xw_f;
+    } else {
+      for (int idx = threadIdx.x; idx < K * T; idx += blockDim.x) xw_f[idx] = (float)s.Qm[idx];
+      qf = xw_f;
+      uf = qm_f;
+    }
+    __syncthreads();
+
+    // ---- 6. U = L^-T Q = A' L~^-T D^-1/2 Q (backward recursions) in fp32, with
+    // the fp32 coefficients of phase 1
+    const float4* cf = reinterpret_cast<const float4*>(o.coef) + (size_t)p * T;
+    float umax_local = 0.f;
+    for (int j = threadIdx.x; j < K; j += blockDim.x) {
+      const float* q = qf + (size_t)j * T;
+      float* u = uf + (size_t)j * T;
+      float xn = 0.f, mn = 0.f, cn = 0.f;  // x_{t+1}, m_{t+1}, c_{t+1}
+      for (int t = T - 1; t >= 0; --t) {
+        const float4 c4 = cf[t];  // (c, m, 1/D, 1/sqrt(D))
+        const float x = fmaf(-mn, xn, q[t] * c4.w);
+        const float ut = fmaf(-cn, xn, x);
+        u[t] = ut;
+        o.U[((size_t)pd * K + j) * LT + t] = ut;
+        umax_local = fmaxf(umax_local, fabsf(ut));
+        xn = x;
+        mn = c4.y;
+        cn = c4.x;
+      }
+      for (int t = T; t < LT; ++t) o.U[((size_t)pd * K + j) * LT + t] = 0.f;
+    }
+    __syncthreads();
+    if (o.U_hi) {
+      // fp16 hi/lo split of U * 2^e, e placing max|U| in [128, 256)
+      double um = umax_local;
+      for (int off = 16; off > 0; off >>= 1) um = fmax(um, __shfl_xor_sync(0xffffffffu, um, off));
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = um;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double mx = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = fmax(mx, red[w]);
+        red[0] = mx;
+      }
+      __syncthreads();
+      const int e = scale_exp((float)red[0]);
+      if (threadIdx.x == 0) o.uexp[pd] = e;
+      for (int idx = threadIdx.x; idx < K * d.ld_u; idx += blockDim.x) {
+        const int j = idx / d.ld_u, t = idx % d.ld_u;
+        uint16_t hi = 0, lo = 0;
+        if (t < T) split_fp16(ldexpf(uf[(size_t)j * T + t], e), hi, lo);
+        const size_t at = ((size_t)pd * K + j) * d.ld_u + t;
+        o.U_hi[at] = hi;
+        o.U_lo[at] = lo;
+      }
+    }
+    __syncthreads();
+
+    // ---- 7. Lx^-1, A = Lx^-T Lx^-1, diag(A)
+    block_tri_inverse(s.Lx, s.Li, K, K);
+    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
+      const int i = idx / K, j = idx % K;
+      double acc = 0.0;
+      for (int k = max(i, j); k < K; ++k) acc += s.Li[k * K + i] * s.Li[k * K + j];
+      s.A[i * K + j] = acc;
+      if (i == j) o.Adiag[(size_t)pd * K + j] = (float)acc;
+    }
+    __syncthreads();
+
+    // ---- 8. G = U Lx^-1 in fp32 (row t of G solves g Lx = u_t); Gsum = G' 1
+    // accumulated in FP64
+    float* const li_f = lx_f + (size_t)K * K;
+    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) li_f[idx] = (float)s.Li[idx];
+    __syncthreads();
+    for (int t = threadIdx.x; t < LT; t += blockDim.x) {
+      for (int j = 0; j < K; ++j) {
+        float acc = 0.f;
+        if (t < T)
+          for (int i = j; i < K; ++i) acc = fmaf(uf[(size_t)i * T + t], li_f[i * K + j], acc);
+        o.G[((size_t)pd * K + j) * LT + t] = acc;
+      }
+    }
+    __syncthreads();
+    if (o.Gsum) {
+      for (int j = threadIdx.x; j < K; j += blockDim.x) {
+        double acc = 0.0;
+        for (int t = 0; t < T; ++t) acc += (double)o.G[((size_t)pd * K + j) * LT + t];
+        o.Gsum[(size_t)pd * K + j] = (float)acc;
+      }
+    }
+
+    // ---- 9. task-column F matrix inv(A_task + 1e-8 I) and GLT variances c A c'
+    const int nt = d.n_task;
+    if (nt > 0 && o.Ftask) {
+      for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
+        const int i = idx / nt, j = idx % nt;
+        s.S[i * nt + j] = s.A[d.task_idx[i] * K + d.task_idx[j]] + (i == j ? 1e-8 : 0.0);
+      }
+      __syncthreads();
+      block_cholesky(s.S, nt, nt, &flag);
+      // Li (free now) holds the inverse factor; Ftask = Li' Li
+      block_tri_inverse(s.S, s.Li, nt, nt);
+      for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
+        const int i = idx / nt, j = idx % nt;
+        double acc = 0.0;
+        for (int k = max(i, j); k < nt; ++k) acc += s.Li[k * nt + i] * s.Li[k * nt + j];
+        o.Ftask[(size_t)pd * nt * nt + idx] = (float)acc;
+      }
+    }
+    if (d.n_glt > 0 && o.glt_var) {
+      for (int c = 0; c < d.n_glt; ++c) {
+        const float* gc = d.glt + (size_t)c * K;
+        double part = 0.0;
+        for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x)
+          part += (double)gc[idx / K] * s.A[idx] * (double)gc[idx % K];
+        const double v = block_sum(part, red);
+        if (threadIdx.x == 0) o.glt_var[(size_t)pd * d.n_glt + c] = (float)v;
+      }
+    }
+    __syncthreads();  // the next item reuses the scratch slot and the shared state
   }
 }
 
@@ -397,6 +408,9 @@ __global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const f
                                                            int* info) {
   __shared__ double red[32];
   __shared__ int flag;
+  const int LT = ld_t(T);
+  for (int idx = threadIdx.x; idx < K * (LT - T); idx += blockDim.x)
+    Q0[(size_t)(idx / (LT - T)) * LT + T + idx % (LT - T)] = 0.f;
   double* M = work;                    // [K][K]
   double* Qd = work + (size_t)K * K;   // [K][T] (QR fallback)
   for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
@@ -412,8 +426,8 @@ __global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const f
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
       for (int j = 0; j < K; ++j) {
         float acc = X[(size_t)t * K + j];
-        for (int i = 0; i < j; ++i) acc = fmaf(-(float)M[j * K + i], Q0[(size_t)i * T + t], acc);
-        Q0[(size_t)j * T + t] = acc / (float)M[j * K + j];
+        for (int i = 0; i < j; ++i) acc = fmaf(-(float)M[j * K + i], Q0[(size_t)i * LT + t], acc);
+        Q0[(size_t)j * LT + t] = acc / (float)M[j * K + j];
       }
     }
     if (threadIdx.x == 0) *info = 0;
@@ -440,7 +454,7 @@ __global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const f
     const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
       q[t] *= inv;
-      Q0[(size_t)j * T + t] = (float)q[t];
+      Q0[(size_t)j * LT + t] = (float)q[t];
     }
     __syncthreads();
   }
@@ -468,6 +482,11 @@ extern "C" size_t ffs_grid_work_bytes(int T, int K, int P) {
   return sizeof(double) * ffsk::pair_doubles(T, K) * (size_t)P;
 }
 
+extern "C" size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs) {
+  const long long items = (long long)P * (n_designs > 0 ? n_designs : 1);
+  return sizeof(double) * ffsk::pair_doubles(T, K) * (size_t)(items < FFS_GRID_MAX_SLOTS ? items : FFS_GRID_MAX_SLOTS);
+}
+
 extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream) {
   using namespace ffsk;
   clear_error();
@@ -485,8 +504,31 @@ extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, voi
                   o->info && o->work,
               "ffs_grid_build: null output");
   BuildArgs args{*d, *o};
-  grid_build_kernel<<<d->P, 256, 0, (cudaStream_t)stream>>>(args);
+  grid_build_kernel<<<d->P, 256, 0, (cudaStream_t)stream>>>(args, 1);
   return check_launch("grid_build_kernel");
+}
+
+extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, const ffs_grid_out* o, void* stream) {
+  using namespace ffsk;
+  clear_error();
+  FFS_REQUIRE(d && o, "ffs_grid_build_designs: null descriptor");
+  FFS_REQUIRE(n_designs > 0, "ffs_grid_build_designs: n_designs=%d must be positive", n_designs);
+  FFS_REQUIRE(d->T > 0 && d->K > 0 && d->P > 0 && d->n_runs > 0,
+              "ffs_grid_build_designs: T=%d K=%d P=%d n_runs=%d must be positive", d->T, d->K, d->P, d->n_runs);
+  FFS_REQUIRE((long long)d->P * n_designs < (1LL << 31), "ffs_grid_build_designs: too many items");
+  FFS_REQUIRE(d->K <= d->T, "ffs_grid_build_designs: K=%d exceeds T=%d", d->K, d->T);
+  FFS_REQUIRE(d->n_task >= 0 && d->n_task <= d->K, "ffs_grid_build_designs: bad n_task=%d", d->n_task);
+  FFS_REQUIRE(!o->U_hi || (o->U_lo && o->uexp), "ffs_grid_build_designs: U_hi needs U_lo and uexp");
+  FFS_REQUIRE(!o->U_hi || (d->ld_u >= d->T && d->ld_u % 8 == 0),
+              "ffs_grid_build_designs: ld_u=%d must be >= T and a multiple of 8", d->ld_u);
+  FFS_REQUIRE(d->run_start && d->tau && d->a && d->b && d->X, "ffs_grid_build_designs: null input");
+  FFS_REQUIRE(o->coef && o->logdet_R && o->logdet_XtX && o->U && o->G && o->Adiag && o->XtX && o->info && o->work,
+              "ffs_grid_build_designs: null output");
+  const long long items = (long long)d->P * n_designs;
+  const int grid = (int)(items < FFS_GRID_MAX_SLOTS ? items : FFS_GRID_MAX_SLOTS);
+  BuildArgs args{*d, *o};
+  grid_build_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(args, n_designs);
+  return check_launch("grid_build_kernel (designs)");
 }
 
 // ---------------------------------------------------------------------------
@@ -565,6 +607,6 @@ extern "C" int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out
   // the previous call's contents need no clearing
   BuildArgs args{*d, *o};
   args.o.work = scratch;
-  grid_build_kernel<<<d->P, 256, 0, (cudaStream_t)stream>>>(args);
+  grid_build_kernel<<<d->P, 256, 0, (cudaStream_t)stream>>>(args, 1);
   return check_launch("grid_build_kernel (static scratch)");
 }

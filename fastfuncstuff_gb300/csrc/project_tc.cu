@@ -37,7 +37,8 @@ struct TcParams {
   int n_col_tiles, n_vox_tiles;
   const ffs_tc_item* items;  // work-list mode: items[0 .. *n_items)
   const int* n_items;
-  int s_vox;           // work-list mode: proj[(out0 + r) * s_vox + slot0 + j]
+  int s_vox;           // work-list mode: proj[(out0 + r) * s_vox + slot0 + j], or with
+                       // s_vox == 0 pair-major proj[(slot0 + j) * V + out0 + r]
   const int* yexp;
   const int* uexp;
   float* proj;
@@ -265,14 +266,15 @@ __global__ void __launch_bounds__(192, 1)
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       // grid mode keeps the exact form whose timing was measured best; the
       // work-list mode differs in where the result goes
-      int v, p_first, ncols, nmax, out_row;
+      int v, p_first, ncols, nmax, out_row, out_slot = 0;
       if (LIST) {
         const Item it = item_at<LIST>(prm, item);
         v = row < it.nv ? it.v0 + row : prm.V;
         p_first = it.row_b / prm.K;
         ncols = it.np * prm.K;
         nmax = it.N;
-        out_row = (it.out0 + row) * prm.s_vox + it.slot0;
+        out_row = prm.s_vox > 0 ? (it.out0 + row) * prm.s_vox + it.slot0 : it.out0 + row;
+        out_slot = it.slot0;
       } else {
         v = (item / prm.n_col_tiles) * BM + row;
         p_first = (item % prm.n_col_tiles) * prm.g;
@@ -302,8 +304,10 @@ __global__ void __launch_bounds__(192, 1)
               const int p = p_first + pl;
               if (p < prm.P && v < prm.V) {
                 const float val = ldexpf(run, -2 * (ey + prm.uexp[p]));
-                if (LIST)
+                if (LIST && prm.s_vox > 0)
                   prm.proj[(size_t)out_row + pl] = val;
+                else if (LIST)
+                  prm.proj[(size_t)(out_slot + pl) * prm.V + out_row] = val;
                 else
                   prm.proj[(size_t)p * prm.V + v] = val;
               }
@@ -429,7 +433,7 @@ extern "C" int ffs_reml_project_tc_list(const ffs_project_args* a, const ffs_tc_
               "ffs_reml_project_tc_list: null buffer");
   FFS_REQUIRE(a->ld_y == a->ld_u && a->ld_y % BK == 0 && a->ld_y >= a->T,
               "ffs_reml_project_tc_list: ld_y=%d and ld_u=%d must be equal multiples of %d", a->ld_y, a->ld_u, BK);
-  FFS_REQUIRE(max_pairs > 0 && max_pairs * a->K <= 256 && max_items > 0 && ld_out > 0,
+  FFS_REQUIRE(max_pairs > 0 && max_pairs * a->K <= 256 && max_items > 0 && ld_out >= 0,
               "ffs_reml_project_tc_list: max_pairs=%d x K=%d must fit one 256-column tile", max_pairs, a->K);
   for (const void* ptr : {(const void*)a->yr_hi, (const void*)a->yr_lo, (const void*)a->u_hi, (const void*)a->u_lo})
     FFS_REQUIRE(((uintptr_t)ptr & 15) == 0, "ffs_reml_project_tc_list: operands must be 16-byte aligned");

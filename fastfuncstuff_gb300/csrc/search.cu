@@ -53,17 +53,19 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int T = a.T, K = a.K;
   const int v0 = blockIdx.x * PREP_VOX;
+  const int LT = ld_t(T);
+  const float* Q0 = a.Q0 + (a.tile_design ? (size_t)a.tile_design[blockIdx.x] * K * LT : 0);
   for (int k = 0; k < PREP_VOX / 8; ++k) {
     const int lv = wid * (PREP_VOX / 8) + k;
     const int v = v0 + lv;
     if (v >= a.V) break;  // warp-uniform
-    const int vs = a.idx ? a.idx[v] : v;  // source row
+    const int vs = a.idx ? a.idx[v] : v;  // source row (< 0: an empty row)
     float* row = sm + (size_t)lv * ld_s;
-    const float* y = a.Y + (size_t)vs * T;
+    const float* y = vs >= 0 ? a.Y + (size_t)vs * T : nullptr;
     // mean and (N-1) variance, two passes for accuracy
     float s = 0.f;
     for (int t = lane; t < T; t += 32) {
-      const float x = y[t];
+      const float x = y ? y[t] : 0.f;
       row[t] = x;
       s += x;
     }
@@ -86,14 +88,14 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
     __syncwarp();
     // residualise: row -= Q0 (Q0' row)
     for (int j = 0; j < K; ++j) {
-      const float* qj = a.Q0 + (size_t)j * T;
+      const float* qj = Q0 + (size_t)j * LT;
       float c = 0.f;
       for (int t = lane; t < T; t += 32) c += qj[t] * row[t];
       c = warp_sum(c);
       for (int t = lane; t < T; t += 32) row[t] -= c * qj[t];
       __syncwarp();
     }
-    if (lane == 0) a.scale[vs] = sc;
+    if (lane == 0 && vs >= 0) a.scale[vs] = sc;
     if (a.feats) row_features(row, T, a.n_runs, a.run_start, a.feats + (size_t)v * 9);
     if (a.yr_hi) {
       float amax = 0.f;
@@ -127,17 +129,19 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
   }
 }
 
-// Tiled form for T % 4 == 0: 32 voxels per CTA, one per lane, the projection
-// c = Q0 y and the update y -= Q0' c as register-blocked passes over the tile
-// (tile.cuh), i.e. y - Q0'(Q0 y) in one step as the reference's
-// Y - (Y pinv(X)') X' (fastfuncstuff/glm/arma.py:1554-1571).
+// Tiled form: 32 voxels per CTA, the projection c = Q0 y and the update
+// y -= Q0' c as register-blocked passes over the tile (tile.cuh), i.e.
+// y - Q0'(Q0 y) in one step as the reference's Y - (Y pinv(X)') X'
+// (fastfuncstuff/glm/arma.py:1554-1571). Rows of Y are read as 16-byte words
+// when T % 4 == 0 and as single samples otherwise; the tile's samples
+// T .. ld_t(T) stay zero.
 __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_args a, int ld) {
   extern __shared__ float4 sm4[];
   float* Ys = reinterpret_cast<float*>(sm4);       // [32][ld]
   float* Cq = Ys + (size_t)TILE_V * ld;            // [K][32]
-  float* part = Cq + (size_t)a.K * TILE_V;         // [TILE_TS][K][32]
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int T = a.T, K = a.K, nq = T >> 2;
+  const int T = a.T, K = a.K, LT = ld_t(T), nq = LT >> 2;
+  const bool vec = (T & 3) == 0;
   const int v0 = blockIdx.x * TILE_V;
   const int nv = min(TILE_V, a.V - v0);
   for (int i = wid; i < TILE_V; i += TILE_WARPS) {
@@ -148,11 +152,24 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
       continue;
     }
     const int vs = a.idx ? a.idx[v0 + i] : v0 + i;  // source row
-    const float4* y4 = reinterpret_cast<const float4*>(a.Y + (size_t)vs * T);
+    if (vs < 0) {  // warp-uniform: an empty (padding) row stays zero
+      for (int q = lane; q < nq; q += 32) row4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
+    const float* yv = a.Y + (size_t)vs * T;
     // mean and (N-1) variance, two passes for accuracy
     float s = 0.f;
     for (int q = lane; q < nq; q += 32) {
-      const float4 x = y4[q];
+      float4 x;
+      if (vec) {
+        x = reinterpret_cast<const float4*>(yv)[q];
+      } else {
+        const int t = 4 * q;
+        x.x = t < T ? yv[t] : 0.f;
+        x.y = t + 1 < T ? yv[t + 1] : 0.f;
+        x.z = t + 2 < T ? yv[t + 2] : 0.f;
+        x.w = t + 3 < T ? yv[t + 3] : 0.f;
+      }
       row4[q] = x;
       s += ((x.x + x.y) + x.z) + x.w;
     }
@@ -175,8 +192,9 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
   }
   __syncthreads();
   if (K > 0) {
-    tile_project(a.Q0, Ys, T, ld, K, Cq, part);
-    tile_subtract(a.Q0, Cq, Ys, T, ld, K);
+    const float* Q0 = a.Q0 + (a.tile_design ? (size_t)a.tile_design[blockIdx.x] * K * LT : 0);
+    tile_project(Q0, LT, Ys, ld, K, Cq);
+    tile_subtract(Q0, LT, Cq, Ys, ld, K);
   }
   __syncthreads();
   if (a.feats) {
@@ -207,9 +225,13 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
   }
   if (a.yr_rows) {  // voxel-major rows, a warp per row
     for (int i = wid; i < nv; i += TILE_WARPS) {
-      const float4* r4 = reinterpret_cast<const float4*>(Ys + (size_t)i * ld);
-      float4* o4 = reinterpret_cast<float4*>(a.yr_rows + (size_t)(v0 + i) * T);
-      for (int q = lane; q < nq; q += 32) o4[q] = r4[q];
+      const float* r = Ys + (size_t)i * ld;
+      float* o = a.yr_rows + (size_t)(v0 + i) * T;
+      if (vec) {
+        for (int q = lane; q < nq; q += 32) reinterpret_cast<float4*>(o)[q] = reinterpret_cast<const float4*>(r)[q];
+      } else {
+        for (int t = lane; t < T; t += 32) o[t] = r[t];
+      }
     }
   }
   // time-major store: lane = voxel (coalesced 128-byte rows), warp w takes
@@ -220,10 +242,11 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
     const size_t V = (size_t)a.V;
     for (int q = wid; q < nq; q += TILE_WARPS) {
       const float4 r = r4[q];
-      out[(size_t)(4 * q) * V] = r.x;
-      out[(size_t)(4 * q + 1) * V] = r.y;
-      out[(size_t)(4 * q + 2) * V] = r.z;
-      out[(size_t)(4 * q + 3) * V] = r.w;
+      const int t = 4 * q;
+      out[(size_t)t * V] = r.x;
+      if (t + 1 < T) out[(size_t)(t + 1) * V] = r.y;
+      if (t + 2 < T) out[(size_t)(t + 2) * V] = r.z;
+      if (t + 3 < T) out[(size_t)(t + 3) * V] = r.w;
     }
   }
 }
@@ -318,10 +341,11 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
     }
     cs4[t] = make_float4(cq[0], cq[1], cq[2], cq[3]);
   }
+  const double* ldx = a.logdet_XtX + (a.tile_design ? (size_t)a.tile_design[blockIdx.y] * a.P : 0);
   if (threadIdx.x < SURF_G) {
-    const double c_p0 = a.logdet_R[a.p0] + a.logdet_XtX[a.p0];
+    const double c_p0 = a.logdet_R[a.p0] + ldx[a.p0];
     const int p = pair_of(threadIdx.x);
-    dcs[threadIdx.x] = p >= 0 ? (float)((a.logdet_R[p] + a.logdet_XtX[p]) - c_p0) : 0.f;
+    dcs[threadIdx.x] = p >= 0 ? (float)((a.logdet_R[p] + ldx[p]) - c_p0) : 0.f;
   }
   ident = __syncthreads_and(ident);
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
@@ -453,7 +477,7 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
       a.surf[(size_t)p * a.V + v] = dv;
     }
   }
-  if (chunk == 0) a.crit0[v] = (a.logdet_R[a.p0] + a.logdet_XtX[a.p0]) + (double)Tk * log((double)rss0 + 1e-10);
+  if (chunk == 0) a.crit0[v] = (a.logdet_R[a.p0] + ldx[a.p0]) + (double)Tk * log((double)rss0 + 1e-10);
 }
 
 // ---------------------------------------------------------------------- select
@@ -522,9 +546,16 @@ __global__ void select_kernel(ffs_select_args a) {
 }
 
 // ----------------------------------------------------------------------- group
+// Counting with warp-aggregated atomics: the lanes of a warp holding the same
+// key add their count once (neighbouring voxels of a smooth parameter map
+// mostly share a pair, so a popular bin sees one atomic per warp, not 32).
 __global__ void group_hist(int V, const int* best, int* cnt) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v < V) atomicAdd(cnt + best[v], 1);
+  const unsigned act = __ballot_sync(0xffffffffu, v < V);
+  if (v >= V) return;
+  const int key = best[v];
+  const unsigned same = __match_any_sync(act, key);
+  if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(cnt + key, __popc(same));
 }
 
 __global__ void group_scan(int P, int* cnt) {
@@ -563,9 +594,20 @@ __global__ void group_scan(int P, int* cnt) {
   if (threadIdx.x == 0) cnt[P] = carry;
 }
 
+// The leader of each set of equal keys reserves the set's slots with one
+// atomic; every lane takes the slot of its rank within the set.
 __global__ void group_scatter(int V, const int* best, int* cursor, int* order) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v < V) order[atomicAdd(cursor + best[v], 1)] = v;
+  const unsigned act = __ballot_sync(0xffffffffu, v < V);
+  if (v >= V) return;
+  const int lane = threadIdx.x & 31;
+  const int key = best[v];
+  const unsigned same = __match_any_sync(act, key);
+  const int leader = __ffs(same) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(cursor + key, __popc(same));
+  base = __shfl_sync(same, base, leader);
+  order[base + __popc(same & ((1u << lane) - 1u))] = v;
 }
 
 // --------------------------------------------------------- projection (CUDA cores)
@@ -590,7 +632,7 @@ __global__ void __launch_bounds__(128) project_simt_kernel(ffs_project_args a) {
       __syncthreads();
       for (int idx = threadIdx.x; idx < PJ_COLS * PJ_TT; idx += 128) {
         const int j = idx / PJ_TT, t = idx % PJ_TT;
-        us[j][t] = (j < nc && t < nt) ? a.U[((size_t)p * K + c0 + j) * T + t0 + t] : 0.f;
+        us[j][t] = (j < nc && t < nt) ? a.U[((size_t)p * K + c0 + j) * ld_t(T) + t0 + t] : 0.f;
       }
       __syncthreads();
       if (v < a.V) {
@@ -621,9 +663,9 @@ extern "C" int ffs_reml_prep(const ffs_prep_args* a, void* stream) {
   FFS_REQUIRE(!a->feats || (a->n_runs > 0 && a->run_start), "ffs_reml_prep: features need the run layout");
   FFS_REQUIRE(!a->yr_hi || (a->yr_lo && a->yexp && a->ld_y >= a->T && a->ld_y % 8 == 0),
               "ffs_reml_prep: ld_y=%d must be >= T and a multiple of 8", a->ld_y);
-  if (a->T % 4 == 0) {
+  {
     const int ld = tile_ld(a->T);
-    const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + (1 + TILE_TS) * (size_t)a->K * TILE_V);
+    const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + (size_t)a->K * TILE_V);
     if (smem <= 200 * 1024) {
       FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(prep_tile_kernel), smem));
       prep_tile_kernel<<<ceil_div(a->V, TILE_V), TILE_WARPS * 32, smem, (cudaStream_t)stream>>>(*a, ld);

@@ -1,111 +1,159 @@
-// Tiles of 32 voxel series in shared memory, one voxel per lane, worked on by
-// a CTA of 8 warps: the K x T products of the residualisation (prep) and of
-// the GLS refit run as register-blocked passes over the tile instead of one
-// warp reduction per design column.
+// Tiles of 32 voxel series in shared memory, worked on by a CTA of 8 warps:
+// the K x T products of the residualisation (prep) and of the GLS refit run
+// as register-blocked passes over the tile instead of one warp reduction per
+// design column.
 //
-// Layout: Ys[l][t] (l < 32 voxels, t < T, row stride tile_ld(T)); K x T
-// matrices stay in global memory ([K][T], rows 16-byte aligned, T % 4 == 0)
-// and are read as warp-uniform float4 loads that the L1 cache serves to every
-// warp of the CTA.
+// Layout: Ys[l][t] (l < 32 voxels, row stride tile_ld(T)), zero for t >= T;
+// K x T matrices stay in global memory (row stride lm = ld_t(T), a multiple
+// of 4, zero padded) and are read through the L1 cache, which every CTA
+// working on the same matrix shares. The passes run over nq = lm / 4 quads of
+// samples; the zero padding adds nothing to the products.
+//
+// Cost model. The L1 / shared-memory data path delivers 128 bytes per cycle
+// to the registers of a warp, whether the 32 lanes read one address or 32;
+// a 16-byte load of the whole warp is 4 such cycles even when every lane
+// reads the same float4. A product whose operands are both loaded for every
+// FMA is therefore bound by that path, not by the FMA pipe. Each thread here
+// keeps a block of operands in registers instead: in the projection 8 voxels
+// x up to 5 columns (every loaded matrix entry serves 8 voxels, every loaded
+// sample up to 5 columns), in the update 4 voxels x up to 10 columns.
 #pragma once
 #include "common.cuh"
 
 namespace ffsk {
 
-constexpr int TILE_V = 32;      // voxels per tile (one per lane)
-constexpr int TILE_WARPS = 8;   // warps per CTA
-constexpr int TILE_PROJ_KC = 12; // columns a thread accumulates per pass in tile_project
-constexpr int TILE_JG = 2;       // column groups of tile_project (warps = TILE_JG x TILE_TS)
-constexpr int TILE_TS = TILE_WARPS / TILE_JG;  // time splits of tile_project
-constexpr int TILE_SUB_KC = 16; // coefficients a thread holds per pass in tile_subtract
+constexpr int TILE_V = 32;       // voxels per tile
+constexpr int TILE_WARPS = 8;    // warps per CTA
+constexpr int TILE_SLICES = 16;  // time slices of tile_project (lane bits 0..3)
+constexpr int TILE_VB = 8;       // voxels per thread in tile_project
+constexpr int TILE_KB_MAX = 5;   // columns per thread and pass in tile_project
+constexpr int TILE_SUB_VB = 4;   // voxels per warp in tile_subtract (warp w: 4w .. 4w+3)
+constexpr int TILE_SUB_KC = 10;  // columns per pass in tile_subtract
 
-// Row stride (floats) of a tile: a multiple of 4 with ld / 4 odd, so the
-// 128-bit loads of 8 consecutive lanes from 8 rows fall in distinct banks.
+// Row stride (floats) of a tile: a multiple of 4 with ld / 4 odd, so 128-bit
+// loads of 8 lanes from 8 different rows fall in distinct banks.
 __host__ __device__ inline int tile_ld(int T) {
   int ld = (T + 3) & ~3;
   if (((ld >> 2) & 1) == 0) ld += 4;
   return ld;
 }
 
-// Quads [q0, q1) of every row owned by warp w in the row-update passes; the
-// same thread always owns the same samples, so consecutive passes over them
-// need no barrier.
-__device__ __forceinline__ void tile_qrange(int T, int w, int& q0, int& q1) {
-  const int nq = T >> 2;
-  q0 = w * nq / TILE_WARPS;
-  q1 = (w + 1) * nq / TILE_WARPS;
-}
-
-// C[j][l] = sum_t M[j][t] Ys[l][t] for j < K, l < 32; part is [TILE_TS][K][32]
-// scratch. Warp w takes the columns j = (w % TILE_JG) + TILE_JG u and one of
-// TILE_TS slices of the time range (w / TILE_JG); the slices are added in
-// order at the end. Ends with a barrier.
-__device__ __forceinline__ void tile_project(const float* __restrict__ M, const float* Ys, int T, int ld, int K,
-                                             float* C, float* part) {
-  const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int jg = w % TILE_JG, ts = w / TILE_JG;
-  const int nq = T >> 2;
-  const int q0 = ts * nq / TILE_TS, q1 = (ts + 1) * nq / TILE_TS;
-  const float4* yr = reinterpret_cast<const float4*>(Ys + (size_t)l * ld);
-  for (int u0 = jg; u0 < K; u0 += TILE_JG * TILE_PROJ_KC) {
-    float acc[TILE_PROJ_KC];
+// C[j][l] = sum_t M[j][t] Ys[l][t] for j < K, l < 32 with KB columns per
+// thread and pass. Thread layout: s = lane & 15 is the time slice (quads
+// q = s, s + 16, ...), unit u = 2 * warp + (lane >> 4) is voxel group
+// u & 3 (voxels 8 (u & 3) + i, i < 8) and column group u >> 2 (columns
+// j0 + KB (u >> 2) + k, k < KB, of the pass starting at j0). The 16 slice
+// partials are summed by recursive halving across lane bits 3, 2, 1 (each
+// exchange ships half of the remaining values) and a final exchange across
+// bit 0; lanes s and s ^ 1 then hold the KB sums of voxel s >> 1.
+template <int KB>
+__device__ __forceinline__ void tile_project_kb(const float* __restrict__ M, int lm, const float* Ys, int ld, int K,
+                                                float* C) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int s = lane & 15;
+  const int u = 2 * w + (lane >> 4);
+  const int vg = u & 3, cg = u >> 2;  // cg is warp-uniform
+  const int nq = lm >> 2, ld4 = ld >> 2;
+  const float4* y4 = reinterpret_cast<const float4*>(Ys) + (size_t)(vg * TILE_VB) * ld4;
+  for (int j0 = 0; j0 < K; j0 += 4 * KB) {
+    const int jb = j0 + cg * KB;
+    float acc[TILE_VB * KB];
 #pragma unroll
-    for (int k = 0; k < TILE_PROJ_KC; ++k) acc[k] = 0.f;
-    for (int q = q0; q < q1; ++q) {
-      const float4 y = yr[q];
+    for (int i = 0; i < TILE_VB * KB; ++i) acc[i] = 0.f;
+    const float4* mb = reinterpret_cast<const float4*>(M + (size_t)min(jb, K - 1) * lm);  // row jb, stride nq
+    for (int q = s; q < nq; q += TILE_SLICES) {
+      float4 m[KB];
 #pragma unroll
-      for (int k = 0; k < TILE_PROJ_KC; ++k) {
-        const int j = u0 + TILE_JG * k;
-        if (j < K) {
-          const float4 m = __ldg(reinterpret_cast<const float4*>(M + (size_t)j * T) + q);
-          acc[k] = fmaf(m.x, y.x, acc[k]);
-          acc[k] = fmaf(m.y, y.y, acc[k]);
-          acc[k] = fmaf(m.z, y.z, acc[k]);
-          acc[k] = fmaf(m.w, y.w, acc[k]);
+      for (int k = 0; k < KB; ++k)
+        m[k] = (jb + k < K) ? __ldg(mb + (size_t)k * nq + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int i = 0; i < TILE_VB; ++i) {
+        const float4 y = y4[(size_t)i * ld4 + q];
+#pragma unroll
+        for (int k = 0; k < KB; ++k) {
+          float a = acc[i * KB + k];
+          a = fmaf(m[k].x, y.x, a);
+          a = fmaf(m[k].y, y.y, a);
+          a = fmaf(m[k].z, y.z, a);
+          a = fmaf(m[k].w, y.w, a);
+          acc[i * KB + k] = a;
         }
       }
     }
+    // recursive halving over lane bits 3, 2, 1: the lane whose bit is set
+    // keeps the upper half of its values, its partner the lower half
 #pragma unroll
-    for (int k = 0; k < TILE_PROJ_KC; ++k) {
-      const int j = u0 + TILE_JG * k;
-      if (j < K) part[((size_t)ts * K + j) * 32 + l] = acc[k];
+    for (int b = 8, n = TILE_VB * KB; b >= 2; b >>= 1, n >>= 1) {
+      const bool up = (lane & b) != 0;
+#pragma unroll
+      for (int i = 0; i < n / 2; ++i) {
+        const float send = up ? acc[i] : acc[i + n / 2];
+        const float keep = up ? acc[i + n / 2] : acc[i];
+        acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, b);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < KB; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 1);
+    if ((lane & 1) == 0) {
+      const int l = vg * TILE_VB + (s >> 1);
+#pragma unroll
+      for (int k = 0; k < KB; ++k)
+        if (jb + k < K) C[(size_t)(jb + k) * TILE_V + l] = acc[k];
     }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < K * 32; i += blockDim.x) {
-    float c = part[i];
-#pragma unroll
-    for (int k = 1; k < TILE_TS; ++k) c += part[(size_t)k * K * 32 + i];
-    C[i] = c;
+}
+
+// C[j][l] = sum_t M[j][t] Ys[l][t] for j < K, l < 32 (C is [K][32]; M has
+// row stride lm). Ends with a barrier.
+__device__ __forceinline__ void tile_project(const float* __restrict__ M, int lm, const float* Ys, int ld, int K,
+                                             float* C) {
+  const int passes = (K + 4 * TILE_KB_MAX - 1) / (4 * TILE_KB_MAX);
+  const int kb = (K + 4 * passes - 1) / (4 * passes);  // columns per thread and pass, <= TILE_KB_MAX
+  switch (kb) {
+    case 1: tile_project_kb<1>(M, lm, Ys, ld, K, C); break;
+    case 2: tile_project_kb<2>(M, lm, Ys, ld, K, C); break;
+    case 3: tile_project_kb<3>(M, lm, Ys, ld, K, C); break;
+    case 4: tile_project_kb<4>(M, lm, Ys, ld, K, C); break;
+    default: tile_project_kb<5>(M, lm, Ys, ld, K, C); break;
   }
   __syncthreads();
 }
 
-// Ys[l][t] -= sum_j N[j][t] C[j][l] over the quads this thread owns
-// (tile_qrange). No barrier.
-__device__ __forceinline__ void tile_subtract(const float* __restrict__ N, const float* C, float* Ys, int T, int ld,
+// Ys[l][t] -= sum_j N[j][t] C[j][l] (N has row stride lm). Warp w updates the rows 4w .. 4w+3
+// (lanes over quads), so a thread's later reads of those rows need no
+// barrier; rows of other warps do. No barrier.
+__device__ __forceinline__ void tile_subtract(const float* __restrict__ N, int lm, const float* C, float* Ys, int ld,
                                               int K) {
-  const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int q0, q1;
-  tile_qrange(T, w, q0, q1);
-  float4* rr = reinterpret_cast<float4*>(Ys + (size_t)l * ld);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int nq = lm >> 2, ld4 = ld >> 2;
+  float4* r4 = reinterpret_cast<float4*>(Ys) + (size_t)(TILE_SUB_VB * w) * ld4;
   for (int j0 = 0; j0 < K; j0 += TILE_SUB_KC) {
-    float c[TILE_SUB_KC];
+    float c[TILE_SUB_VB][TILE_SUB_KC];
 #pragma unroll
-    for (int k = 0; k < TILE_SUB_KC; ++k) c[k] = (j0 + k < K) ? C[(size_t)(j0 + k) * 32 + l] : 0.f;
-    for (int q = q0; q < q1; ++q) {
-      float4 r = rr[q];
+    for (int k = 0; k < TILE_SUB_KC; ++k) {
+#pragma unroll
+      for (int i = 0; i < TILE_SUB_VB; ++i)
+        c[i][k] = (j0 + k < K) ? C[(size_t)(j0 + k) * TILE_V + TILE_SUB_VB * w + i] : 0.f;
+    }
+    for (int q = lane; q < nq; q += 32) {
+      float4 r[TILE_SUB_VB];
+#pragma unroll
+      for (int i = 0; i < TILE_SUB_VB; ++i) r[i] = r4[(size_t)i * ld4 + q];
 #pragma unroll
       for (int k = 0; k < TILE_SUB_KC; ++k) {
         if (j0 + k < K) {
-          const float4 n = __ldg(reinterpret_cast<const float4*>(N + (size_t)(j0 + k) * T) + q);
-          r.x = fmaf(-n.x, c[k], r.x);
-          r.y = fmaf(-n.y, c[k], r.y);
-          r.z = fmaf(-n.z, c[k], r.z);
-          r.w = fmaf(-n.w, c[k], r.w);
+          const float4 n = __ldg(reinterpret_cast<const float4*>(N + (size_t)(j0 + k) * lm) + q);
+#pragma unroll
+          for (int i = 0; i < TILE_SUB_VB; ++i) {
+            r[i].x = fmaf(-n.x, c[i][k], r[i].x);
+            r[i].y = fmaf(-n.y, c[i][k], r[i].y);
+            r[i].z = fmaf(-n.z, c[i][k], r[i].z);
+            r[i].w = fmaf(-n.w, c[i][k], r[i].w);
+          }
         }
       }
-      rr[q] = r;
+#pragma unroll
+      for (int i = 0; i < TILE_SUB_VB; ++i) r4[(size_t)i * ld4 + q] = r[i];
     }
   }
 }

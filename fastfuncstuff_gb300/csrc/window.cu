@@ -120,17 +120,24 @@ struct CritArgs {
 constexpr int CRIT_TB = 16;  // steps per partial sum and sample prefetch
 
 // One CTA per tile of WTILE sorted rows that share a window centre, one thread
-// per row. Each window row's coefficients (-m, 1/D of its <= 5 non-identity
-// pairs, which share a and so the AR filter c_t) are staged in shared memory,
-// then every thread runs the 5 recurrences over its series with 16 samples in
-// flight. As in the surface kernel, a step whose coefficients equal the
-// previous step's reuses the registers, and a block of 16 such steps sums v^2
-// alone and scales the block sum by 1/D once.
+// per row. The window rows are walked two at a time (CRIT_ROWS), so the
+// series is read ceil(5 / 2) = 3 times instead of once per window row; y'y is
+// summed in the first pass. Each window row's coefficients (-m, 1/D of its
+// <= 5 non-identity pairs, which share a and so the AR filter c_t) are staged
+// in shared memory, then every thread runs the recurrences of both rows over
+// its series with 16 samples in flight. As in the surface kernel, a step whose
+// coefficients equal the previous step's (for every pair of that window row)
+// reuses the registers, and a block of 16 such steps sums v^2 alone and
+// scales the block sum by 1/D once; each row keeps its own steady flags, so a
+// pair's arithmetic does not depend on which row it is walked beside.
+constexpr int CRIT_ROWS = 1;
+
 __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const int2* tiles, const int* n_tiles) {
-  extern __shared__ float2 tab[];  // [WIN][T] (-m, 1/D) of the row's pairs
-  float* cs = reinterpret_cast<float*>(tab + WIN * (size_t)w.T);  // [T] the row's AR filter c_t
-  uint8_t* steady = reinterpret_cast<uint8_t*>(cs + w.T);        // [T]
-  uint8_t* bsteady = steady + w.T;                               // [ceil(T / CRIT_TB)]
+  extern __shared__ float2 tab[];  // [CRIT_ROWS][WIN][T] (-m, 1/D) of the rows' pairs
+  float* cs = reinterpret_cast<float*>(tab + CRIT_ROWS * WIN * (size_t)w.T);  // [CRIT_ROWS][T] AR filter c_t
+  uint8_t* steady = reinterpret_cast<uint8_t*>(cs + CRIT_ROWS * (size_t)w.T);  // [CRIT_ROWS][T]
+  const int nblk = (w.T + CRIT_TB - 1) / CRIT_TB;
+  uint8_t* bsteady = steady + CRIT_ROWS * (size_t)w.T;                          // [CRIT_ROWS][nblk]
   if ((int)blockIdx.x >= *n_tiles) return;
   const int2 tl = tiles[blockIdx.x];
   const int i = tl.x + threadIdx.x;
@@ -140,136 +147,182 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
   window_of(c, w.n_a, w.n_b, a0, wa, b0, wb);
   const int T = w.T, Tk = w.T - w.K;
   const float* yc = w.yr_st + (live ? i : tl.x);
-  // y'y in the full grid's blocks (the identity chunk of the surface kernel)
-  float yy = 0.f;
-  for (int t0 = 0; t0 < T; t0 += CRIT_TB) {
-    float yb[CRIT_TB];
-#pragma unroll
-    for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * w.n] : 0.f;
-    float yy_b = 0.f;
-#pragma unroll
-    for (int k = 0; k < CRIT_TB; ++k) yy_b = fmaf(yb[k], yb[k], yy_b);
-    yy += yy_b;
-  }
-  const float rss0 = yy;  // ||Q0'y_r||^2 of the residualised series is zero to rounding
-  const float den = rss0 + 1e-10f;
+
+  // identity pairs of the window (R = I: criterion d = 0)
+  bool has_ident = false;
+  for (int ra = 0; ra < wa; ++ra)
+    for (int rb = 0; rb < wb; ++rb) {
+      const int p = w.lattice[(a0 + ra) * w.n_b + b0 + rb];
+      if (p >= 0 && w.ident[p]) has_ident = true;
+    }
 
   // best non-identity window pair
   int best = -1, bcell = -1;
   float bd = INFINITY;
-  bool has_ident = false;
-  for (int ra = 0; ra < wa; ++ra) {
-    int pr[WIN], col[WIN], np = 0;
+  float yy = 0.f;  // y'y in the full grid's blocks (the identity chunk of the surface kernel)
+  for (int ra0 = 0; ra0 < wa; ra0 += CRIT_ROWS) {
+    int pr[CRIT_ROWS][WIN], col[CRIT_ROWS][WIN], np[CRIT_ROWS];
 #pragma unroll
-    for (int rb = 0; rb < WIN; ++rb) {
-      const int p = rb < wb ? w.lattice[(a0 + ra) * w.n_b + b0 + rb] : -1;
-      if (p >= 0 && w.ident[p]) has_ident = true;
-      if (p >= 0 && !w.ident[p]) {
-        pr[np] = p;
-        col[np++] = rb;
+    for (int r = 0; r < CRIT_ROWS; ++r) {
+      np[r] = 0;
+      const int ra = ra0 + r;
+#pragma unroll
+      for (int rb = 0; rb < WIN; ++rb) {
+        pr[r][rb] = -1;
+        col[r][rb] = 0;
+        const int p = (ra < wa && rb < wb) ? w.lattice[(a0 + ra) * w.n_b + b0 + rb] : -1;
+        if (p >= 0 && !w.ident[p]) {
+#pragma unroll
+          for (int k = 0; k < WIN; ++k)
+            if (k == np[r]) {
+              pr[r][k] = p;
+              col[r][k] = rb;
+            }
+          ++np[r];
+        }
       }
     }
-    if (np == 0) continue;  // uniform over the CTA
+    const bool first = ra0 == 0;
+    if (np[0] == 0 && (CRIT_ROWS < 2 || np[1] == 0) && !first) continue;  // uniform over the CTA
     __syncthreads();
-    // the row's pairs share a, so one AR filter c_t; stage (-m, 1/D) per pair
-    for (int idx = threadIdx.x; idx < np * T; idx += blockDim.x) {
-      const int g = idx / T, t = idx % T;
-      int p = pr[0];
+    // each row's pairs share a, so one AR filter c_t; stage (-m, 1/D) per pair
+    for (int idx = threadIdx.x; idx < CRIT_ROWS * WIN * T; idx += blockDim.x) {
+      const int rg = idx / T, t = idx % T;
+      const int r = rg / WIN, g = rg % WIN;
+      int p = -1;
 #pragma unroll
-      for (int k = 1; k < WIN; ++k)
-        if (g == k) p = pr[k];
-      const float4 q = w.coef[(size_t)p * T + t];
-      tab[(size_t)g * T + t] = make_float2(-q.y, q.z);
-      if (g == 0) cs[t] = q.x;
+      for (int rr = 0; rr < CRIT_ROWS; ++rr)
+#pragma unroll
+        for (int k = 0; k < WIN; ++k)
+          if (rr == r && k == g) p = pr[rr][k];
+      if (p >= 0) {
+        const float4 q = w.coef[(size_t)p * T + t];
+        tab[(size_t)rg * T + t] = make_float2(-q.y, q.z);
+        if (g == 0) cs[(size_t)r * T + t] = q.x;
+      } else if (g == 0) {
+        cs[(size_t)r * T + t] = 0.f;
+      }
     }
     __syncthreads();
-    // steady steps: every pair's coefficients (and c) equal the previous step's
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
-      bool same = t > 0 && cs[t] == cs[t - 1];
-      for (int g = 0; g < np && same; ++g) {
-        const float2 x = tab[(size_t)g * T + t], y = tab[(size_t)g * T + t - 1];
+    // steady steps of each row: every pair's coefficients (and c) equal the
+    // previous step's
+    for (int idx = threadIdx.x; idx < CRIT_ROWS * T; idx += blockDim.x) {
+      const int r = idx / T, t = idx % T;
+      int nr = 0;
+#pragma unroll
+      for (int rr = 0; rr < CRIT_ROWS; ++rr)
+        if (rr == r) nr = np[rr];
+      const float* cr = cs + (size_t)r * T;
+      bool same = t > 0 && cr[t] == cr[t - 1];
+      for (int g = 0; g < nr && same; ++g) {
+        const float2 x = tab[((size_t)r * WIN + g) * T + t], y = tab[((size_t)r * WIN + g) * T + t - 1];
         same = x.x == y.x && x.y == y.y;
       }
-      steady[t] = same ? 1 : 0;
+      steady[idx] = same ? 1 : 0;
     }
     __syncthreads();
-    for (int bk = threadIdx.x; bk * CRIT_TB < T; bk += blockDim.x) {
+    for (int idx = threadIdx.x; idx < CRIT_ROWS * nblk; idx += blockDim.x) {
+      const int r = idx / nblk, bk = idx % nblk;
       bool all = bk * CRIT_TB + CRIT_TB <= T;
-      for (int t = bk * CRIT_TB; t < bk * CRIT_TB + CRIT_TB && all; ++t) all = steady[t] != 0;
-      bsteady[bk] = all ? 1 : 0;
+      for (int t = bk * CRIT_TB; t < bk * CRIT_TB + CRIT_TB && all; ++t) all = steady[(size_t)r * T + t] != 0;
+      bsteady[idx] = all ? 1 : 0;
     }
     __syncthreads();
-    float vv[WIN], sq[WIN], st[WIN], nm[WIN], id[WIN];
+    float vv[CRIT_ROWS][WIN], sq[CRIT_ROWS][WIN], st[CRIT_ROWS][WIN], nm[CRIT_ROWS][WIN], id[CRIT_ROWS][WIN];
+    float cc[CRIT_ROWS];
 #pragma unroll
-    for (int g = 0; g < WIN; ++g) vv[g] = sq[g] = st[g] = nm[g] = id[g] = 0.f;
-    float yp = 0.f, c = 0.f;
+    for (int r = 0; r < CRIT_ROWS; ++r) {
+      cc[r] = 0.f;
+#pragma unroll
+      for (int g = 0; g < WIN; ++g) vv[r][g] = sq[r][g] = st[r][g] = nm[r][g] = id[r][g] = 0.f;
+    }
+    float yp = 0.f;
     for (int t0 = 0; t0 < T; t0 += CRIT_TB) {
       float yb[CRIT_TB];
 #pragma unroll
       for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * w.n] : 0.f;
-      if (bsteady[t0 / CRIT_TB]) {
-        // CRIT_TB steady steps: coefficients in registers, sum of v^2 alone
+      if (first) {
+        float yy_b = 0.f;
 #pragma unroll
-        for (int k = 0; k < CRIT_TB; ++k) {
-          const float z = fmaf(-c, yp, yb[k]);
-          yp = yb[k];
+        for (int k = 0; k < CRIT_TB; ++k) yy_b = fmaf(yb[k], yb[k], yy_b);
+        yy += yy_b;
+      }
 #pragma unroll
-          for (int g = 0; g < WIN; ++g) {
-            vv[g] = fmaf(nm[g], vv[g], z);
-            sq[g] = fmaf(vv[g], vv[g], sq[g]);
-          }
-        }
+      for (int r = 0; r < CRIT_ROWS; ++r) {
+        if (np[r] == 0) continue;  // uniform over the CTA
+        float ypr = yp;
+        if (bsteady[(size_t)r * nblk + t0 / CRIT_TB]) {
+          // CRIT_TB steady steps: coefficients in registers, sum of v^2 alone
 #pragma unroll
-        for (int g = 0; g < WIN; ++g) {
-          st[g] = fmaf(sq[g], id[g], st[g]);
-          sq[g] = 0.f;
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < CRIT_TB; ++k) {
-          const int t = t0 + k;
-          if (t < T) {
-            if (!steady[t]) {
-              c = cs[t];
-#pragma unroll
-              for (int g = 0; g < WIN; ++g) {
-                if (g < np) {
-                  const float2 q = tab[(size_t)g * T + t];
-                  nm[g] = q.x;
-                  id[g] = q.y;
-                }
-              }
-            }
-            const float z = fmaf(-c, yp, yb[k]);
-            yp = yb[k];
+          for (int k = 0; k < CRIT_TB; ++k) {
+            const float z = fmaf(-cc[r], ypr, yb[k]);
+            ypr = yb[k];
 #pragma unroll
             for (int g = 0; g < WIN; ++g) {
-              vv[g] = fmaf(nm[g], vv[g], z);
-              sq[g] = fmaf(vv[g] * id[g], vv[g], sq[g]);
+              vv[r][g] = fmaf(nm[r][g], vv[r][g], z);
+              sq[r][g] = fmaf(vv[r][g], vv[r][g], sq[r][g]);
             }
           }
-        }
 #pragma unroll
-        for (int g = 0; g < WIN; ++g) {
-          st[g] += sq[g];
-          sq[g] = 0.f;
+          for (int g = 0; g < WIN; ++g) {
+            st[r][g] = fmaf(sq[r][g], id[r][g], st[r][g]);
+            sq[r][g] = 0.f;
+          }
+        } else {
+          const uint8_t* sr = steady + (size_t)r * T;
+          const float2* tr = tab + (size_t)r * WIN * T;
+#pragma unroll
+          for (int k = 0; k < CRIT_TB; ++k) {
+            const int t = t0 + k;
+            if (t < T) {
+              if (!sr[t]) {
+                cc[r] = cs[(size_t)r * T + t];
+#pragma unroll
+                for (int g = 0; g < WIN; ++g) {
+                  if (g < np[r]) {
+                    const float2 q = tr[(size_t)g * T + t];
+                    nm[r][g] = q.x;
+                    id[r][g] = q.y;
+                  }
+                }
+              }
+              const float z = fmaf(-cc[r], ypr, yb[k]);
+              ypr = yb[k];
+#pragma unroll
+              for (int g = 0; g < WIN; ++g) {
+                vv[r][g] = fmaf(nm[r][g], vv[r][g], z);
+                sq[r][g] = fmaf(vv[r][g] * id[r][g], vv[r][g], sq[r][g]);
+              }
+            }
+          }
+#pragma unroll
+          for (int g = 0; g < WIN; ++g) {
+            st[r][g] += sq[r][g];
+            sq[r][g] = 0.f;
+          }
         }
       }
+      yp = yb[CRIT_TB - 1];
     }
 #pragma unroll
-    for (int g = 0; g < WIN; ++g) {
-      if (g < np && live) {
-        const int p = pr[g];
-        const float rss = fmaxf(st[g] - w.winproj[(size_t)i * WSLOTS + ra * WIN + col[g]], 0.f);
-        const float d = w.dcf[p] + (float)Tk * log1pf((rss - rss0) / den);
-        if (d < bd || (d == bd && p < best) || best < 0) {
-          bd = d;
-          best = p;
-          bcell = (a0 + ra) * w.n_b + b0 + col[g];
+    for (int r = 0; r < CRIT_ROWS; ++r) {
+      const int ra = ra0 + r;
+#pragma unroll
+      for (int g = 0; g < WIN; ++g) {
+        if (g < np[r] && live) {
+          const int p = pr[r][g];
+          const float rss = fmaxf(st[r][g] - w.winproj[(size_t)i * WSLOTS + ra * WIN + col[r][g]], 0.f);
+          const float d = w.dcf[p] + (float)Tk * log1pf((rss - yy) / (yy + 1e-10f));
+          if (d < bd || (d == bd && p < best) || best < 0) {
+            bd = d;
+            best = p;
+            bcell = (a0 + ra) * w.n_b + b0 + col[r][g];
+          }
         }
       }
     }
   }
+  const float rss0 = yy;  // ||Q0'y_r||^2 of the residualised series is zero to rounding
   if (!live) return;
   // The identity pairs (d = 0) take part when the window holds one of them,
   // and then a win by them is final. A window without them whose best is not
@@ -308,37 +361,66 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
 }
 
 // fp16 operand rows and exponents in the order idx: a warp per row, 16-byte words
-__global__ void gather_rows_kernel(int n, const int* n_dev, int ld_y, const int* idx, const uint4* hi, const uint4* lo,
-                                   const int* yexp, uint4* out_hi, uint4* out_lo, int* out_exp) {
+__global__ void gather_rows_kernel(int n, const int* n_dev, int ld_y, const int* __restrict__ idx,
+                                   const uint4* __restrict__ hi, const uint4* __restrict__ lo,
+                                   const int* __restrict__ yexp, uint4* __restrict__ out_hi,
+                                   uint4* __restrict__ out_lo, int* __restrict__ out_exp) {
   const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (i >= n || (n_dev && i >= *n_dev)) return;
   const int v = idx[i];
   const int nw = ld_y / 8;  // 8 fp16 per 16-byte word
-  for (int k = lane; k < nw; k += 32) {
-    out_hi[(size_t)i * nw + k] = hi[(size_t)v * nw + k];
-    out_lo[(size_t)i * nw + k] = lo[(size_t)v * nw + k];
+  const uint4* sh = hi + (size_t)v * nw;
+  const uint4* sl = lo + (size_t)v * nw;
+  uint4* dh = out_hi + (size_t)i * nw;
+  uint4* dl = out_lo + (size_t)i * nw;
+  int k = lane;
+  for (; k + 32 < nw; k += 64) {  // four 16-byte loads in flight per lane
+    const uint4 h0 = sh[k], h1 = sh[k + 32], l0 = sl[k], l1 = sl[k + 32];
+    dh[k] = h0;
+    dh[k + 32] = h1;
+    dl[k] = l0;
+    dl[k + 32] = l1;
+  }
+  if (k < nw) {
+    const uint4 h0 = sh[k], l0 = sl[k];
+    dh[k] = h0;
+    dl[k] = l0;
   }
   if (lane == 0) out_exp[i] = yexp[v];
 }
 
 // out_t[t][i] = rows[idx[i]][t]: 32 x 32 tiles through shared memory
-__global__ void gather_transpose_kernel(int n, const int* n_dev, int T, const int* idx, const float* rows,
-                                        float* out_t) {
-  __shared__ float tile[32][33];
-  const int i0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
+// out_t[t][i] = rows[idx[i]][t]: 32 rows x 64 samples per CTA through shared
+// memory (eight loads in flight per thread)
+__global__ void gather_transpose_kernel(int n, const int* n_dev, int T, const int* __restrict__ idx,
+                                        const float* __restrict__ rows, float* __restrict__ out_t) {
+  __shared__ float tile[64][33];
+  const int i0 = blockIdx.x * 32, t0 = blockIdx.y * 64;
   // rows taken: i < m (n stays the row stride of out_t)
   const int m = n_dev ? min(n, *n_dev) : n;
   if (i0 >= m) return;  // uniform over the CTA
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-  for (int r = ty; r < 32; r += 8) {
-    const int i = i0 + r, t = t0 + tx;
-    tile[r][tx] = (i < m && t < T) ? rows[(size_t)idx[i] * T + t] : 0.f;
+  float x[8];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int r = ty + 8 * k, i = i0 + r;
+    const float* src = rows + (size_t)(i < m ? idx[i] : 0) * T;
+    const int ta = t0 + tx, tb = t0 + 32 + tx;
+    x[2 * k] = (i < m && ta < T) ? src[ta] : 0.f;
+    x[2 * k + 1] = (i < m && tb < T) ? src[tb] : 0.f;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int r = ty + 8 * k;
+    tile[tx][r] = x[2 * k];
+    tile[32 + tx][r] = x[2 * k + 1];
   }
   __syncthreads();
-  for (int r = ty; r < 32; r += 8) {
-    const int t = t0 + r, i = i0 + tx;
-    if (t < T && i < m) out_t[(size_t)t * n + i] = tile[tx][r];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int tt = ty + 8 * k, t = t0 + tt, i = i0 + tx;
+    if (t < T && i < m) out_t[(size_t)t * n + i] = tile[tt][tx];
   }
 }
 
@@ -380,8 +462,8 @@ extern "C" int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const i
                                                       reinterpret_cast<const uint4*>(yr_lo), yexp,
                                                       reinterpret_cast<uint4*>(out_hi),
                                                       reinterpret_cast<uint4*>(out_lo), out_exp);
-  FFS_REQUIRE(ceil_div(T, 32) <= 65535, "ffs_reml_gather: T=%d too long", T);
-  gather_transpose_kernel<<<dim3(ceil_div(n, 32), ceil_div(T, 32)), dim3(32, 8), 0, st>>>(n, n_dev, T, idx, yr_rows,
+  FFS_REQUIRE(ceil_div(T, 64) <= 65535, "ffs_reml_gather: T=%d too long", T);
+  gather_transpose_kernel<<<dim3(ceil_div(n, 32), ceil_div(T, 64)), dim3(32, 8), 0, st>>>(n, n_dev, T, idx, yr_rows,
                                                                                           out_t);
   return check_launch("gather kernels");
 }
@@ -416,7 +498,7 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
   FFS_REQUIRE(lattice && idx && center && tiles && n_tiles && yr_st && coef && winproj && dcf && ident && c_p0 &&
                   best && dbest && crit0 && fallback && best_cell,
               "ffs_reml_window: null buffer");
-  const size_t smem = (sizeof(float2) * WIN + sizeof(float) + 1) * (size_t)T + ceil_div(T, CRIT_TB);
+  const size_t smem = CRIT_ROWS * ((sizeof(float2) * WIN + sizeof(float) + 1) * (size_t)T + ceil_div(T, CRIT_TB));
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_reml_window: T=%d too long", T);
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(window_crit_kernel), smem));
   CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, yr_st, reinterpret_cast<const float4*>(coef), winproj, dcf,

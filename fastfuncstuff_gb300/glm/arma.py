@@ -249,6 +249,7 @@ def fit_glm_arma11(
     proposal=None,
     proposal_recenter: int = 0,
     cuda_graphs: bool = True,
+    _group_designs=None,
 ) -> ARMA11Results:
     """Fit a GLM with ARMA(1,1) REML prewhitening (fastfuncstuff/glm/arma.py:3650).
 
@@ -340,6 +341,14 @@ def fit_glm_arma11(
     bs = _batch_size(V, T, P, K, batch_size, device)
     use_graph = best_all is None and proposal is not None and cuda_graphs and lj is None and bs >= V
     q0 = join = None
+    slots = None
+    if _group_designs is not None:
+        # grouped fit (fit_glm_arma11_grouped): every design's factors in one
+        # grid build, every voxel against its own design in one pass per stage
+        Xs, gid = _group_designs
+        factors = engine.build_factors(Xs, grid, layout, task_indices=ti, glt=glt, with_tc=True)
+        slots = engine.design_slots(gid, Xs.shape[0], K, P, device)
+        bs = V
     if factors is None and not use_graph:
         # the grid build runs on a side stream while the residualisation of the
         # first batch (against the design basis) runs on the main one
@@ -404,6 +413,14 @@ def fit_glm_arma11(
                     t_all, t_sub = getattr(go, fld), getattr(gs, fld)
                     if t_all is not None:
                         t_all.index_copy_(0, sel, t_sub)
+        elif slots is not None:
+            so = engine.search_designs(Yb, factors, slots, hierarchical=not force_exhaustive_search,
+                                       do_scale=not use_double)
+            best, scale = so.best, so.scale
+            chunks["best"].append(best)
+            chunks["crit"].append(so.best_crit)
+            go = engine.gls(Yb, scale, best, factors, _group_designs[0], want_residuals=want_residuals,
+                            want_predicted=want_predicted, lj=lj, design=slots.design)
         elif best_all is None:
             so = engine.search(Yb, factors, hierarchical=not force_exhaustive_search, projector=proj,
                                do_scale=not use_double, keep_surface=save_profile_likelihoods, q0=q0, join=join)
@@ -565,6 +582,20 @@ def fit_glm_arma11_grouped(data, designs_by_group: dict, group_indices, tr: floa
                              "designs must share dims")
     pre = fit_kwargs.pop("precomputed_arma_params", None)
     fit_kwargs.setdefault("verbose", False)
+    batched_ok = (pre is None and fit_kwargs.get("proposal") is None
+                  and not fit_kwargs.get("save_profile_likelihoods", False)
+                  and fit_kwargs.get("projector", "tc") == "tc" and fit_kwargs.get("batch_size") is None
+                  and shape0[1] <= 256 and len(groups) > 1)
+    if batched_ok:
+        # one fit over all groups: the designs stacked (D, T, K), each voxel
+        # tagged with its design's index
+        device = engine.require_cuda(fit_kwargs.get("device"))
+        Xs = torch.stack([_to_tensor(designs_by_group[h]) for h in groups]).to(device=device,
+                                                                                dtype=torch.float32)
+        dense = np.searchsorted(np.asarray(groups), gid.numpy()).astype(np.int32)
+        kw = dict(fit_kwargs)
+        kw["device"] = device
+        return fit_glm_arma11(Y, Xs[0], tr, _group_designs=(Xs, dense), **kw)
     per = {}
     for h in groups:
         m = gid == h

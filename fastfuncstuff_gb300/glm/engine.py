@@ -39,7 +39,7 @@ def _stream() -> int:
 
 
 # kernels each library entry point launches (for launch accounting)
-LAUNCHES = {"ffs_grid_build": 1, "ffs_reml_prep": 1, "ffs_reml_project_tc": 1, "ffs_reml_project_simt": 1,
+LAUNCHES = {"ffs_grid_build": 1, "ffs_grid_build_designs": 1, "ffs_reml_prep": 1, "ffs_reml_project_tc": 1, "ffs_reml_project_simt": 1,
             "ffs_reml_surface": 1, "ffs_reml_select": 1, "ffs_reml_group": 3, "ffs_reml_gls": 1,
             "ffs_reml_gls_ex": 1, "ffs_reml_gls_grouped": 2, "ffs_reml_gather": 2, "ffs_reml_window_items": 2,
             "ffs_reml_window": 1, "ffs_reml_project_tc_list": 1, "ffs_mlp_forward": 1, "ffs_reml_centers": 1}
@@ -108,6 +108,20 @@ def const_dev(arr: np.ndarray, dev) -> torch.Tensor:
     return t
 
 
+def ld_t(T: int) -> int:
+    """Row stride of the library's K x T matrices (U, G, Q0, Xt): T rounded up
+    to a multiple of 4 (16-byte rows); the padding samples are zero."""
+    return (T + 3) & ~3
+
+
+def padded_design_t(X: torch.Tensor) -> torch.Tensor:
+    """X' as [K][ld_t(T)] fp32 with zero padding (the GLS's design operand)."""
+    T, K = X.shape
+    Xt = torch.zeros(K, ld_t(T), device=X.device, dtype=torch.float32)
+    Xt[:, :T] = X.to(torch.float32).t()
+    return Xt
+
+
 def padded_ld(T: int) -> int:
     return (T + LD_ALIGN - 1) // LD_ALIGN * LD_ALIGN
 
@@ -152,6 +166,7 @@ class GridFactors:
     Gsum: torch.Tensor | None = None
     center_flag: torch.Tensor | None = None  # device int32[1]: centre the voxels (constant in span(X))
     uexp: torch.Tensor | None = None
+    n_designs: int = 1  # > 1: design-dependent factors are [n_designs * P] (design-major)
 
     @property
     def P(self) -> int:
@@ -163,6 +178,9 @@ def constant_flag(X: torch.Tensor, tol: float = 1e-6) -> tuple[torch.Tensor, tor
     with flag = 1 and X c = 1 (FP64 normal equations) when the constant series
     lies in the column span of X, flag = 0 and c = 0 otherwise."""
     Xd = X.detach().to(torch.float64)
+    if Xd.ndim == 3:  # D designs: one flag (the constant in every span), c [D][K]
+        oks, cs = zip(*(constant_flag(x, tol) for x in Xd))
+        return torch.stack(oks).amin(0), torch.stack(cs)
     T, K = Xd.shape
     ones = torch.ones(T, 1, dtype=torch.float64, device=Xd.device)
     L, info = torch.linalg.cholesky_ex(Xd.T @ Xd)
@@ -204,7 +222,8 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     reported per-voxel lambda.
     """
     dev = X.device
-    T, K = X.shape
+    D = X.shape[0] if X.ndim == 3 else 1  # (D, T, K): one design per voxel group
+    T, K = X.shape[-2:]
     P = grid.P
     ld = padded_ld(T)
     f32 = dict(device=dev, dtype=torch.float32)
@@ -221,21 +240,23 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     ng = 0 if glt_t is None else glt_t.shape[0]
     lib = _lib.load()
     cflag, ccoef = constant_flag(Xc) if center is None else center
-    work = torch.empty(int(lib.ffs_grid_work_bytes(T, K, P)) // 8 + 1, dtype=torch.float64, device=dev)
+    wbytes = lib.ffs_grid_work_bytes(T, K, P) if D == 1 else lib.ffs_grid_work_bytes_designs(T, K, P, D)
+    work = torch.empty(int(wbytes) // 8 + 1, dtype=torch.float64, device=dev)
+    DP = D * P
     f = GridFactors(
         grid=grid, T=T, K=K, ld=ld,
         coef=torch.empty(P, T, 4, **f32),
         logdet_R=torch.empty(P, dtype=torch.float64, device=dev),
-        logdet_XtX=torch.empty(P, dtype=torch.float64, device=dev),
-        U=torch.empty(P, K, T, **f32),
-        U_hi=torch.empty(P * K, ld, dtype=torch.int16, device=dev) if with_tc else None,
-        U_lo=torch.empty(P * K, ld, dtype=torch.int16, device=dev) if with_tc else None,
-        G=torch.empty(P, K, T, **f32),
-        Adiag=torch.empty(P, K, **f32),
-        XtX=torch.empty(P, K, K, **f32),
-        info=torch.empty(P, dtype=torch.int32, device=dev),
-        Ftask=torch.empty(P, nt, nt, **f32) if nt else None,
-        glt_var=torch.empty(P, ng, **f32) if ng else None,
+        logdet_XtX=torch.empty(DP, dtype=torch.float64, device=dev),
+        U=torch.empty(DP, K, ld_t(T), **f32),
+        U_hi=torch.empty(DP * K, ld, dtype=torch.int16, device=dev) if with_tc else None,
+        U_lo=torch.empty(DP * K, ld, dtype=torch.int16, device=dev) if with_tc else None,
+        G=torch.empty(DP, K, ld_t(T), **f32),
+        Adiag=torch.empty(DP, K, **f32),
+        XtX=torch.empty(DP, K, K, **f32),
+        info=torch.empty(DP, dtype=torch.int32, device=dev),
+        Ftask=torch.empty(DP, nt, nt, **f32) if nt else None,
+        glt_var=torch.empty(DP, ng, **f32) if ng else None,
         a=a, b=b,
         chunk_start=const_dev(grid.chunk_start, dev),
         chunk_pairs=const_dev(grid.chunk_pairs, dev),
@@ -243,7 +264,8 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
         task_idx=task_idx, glt=glt_t,
         Gsum=None,
         center_flag=cflag,
-        uexp=torch.empty(P, dtype=torch.int32, device=dev) if with_tc else None,
+        uexp=torch.empty(DP, dtype=torch.int32, device=dev) if with_tc else None,
+        n_designs=D,
     )
     d = _lib.GridDesc(T=T, K=K, P=P, n_runs=layout.n_runs, run_start=_p(run_start), tau=_p(tau),
                       a=_p(a), b=_p(b), X=_p(Xc), lambda_fp32=0, ld_u=ld,
@@ -252,16 +274,22 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     o = _lib.GridOut(coef=_p(f.coef), logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), U=_p(f.U),
                      U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), uexp=_p(f.uexp), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
                      info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=None, work=_p(work))
+    def launch():
+        if D == 1:
+            _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
+        else:
+            _run("ffs_grid_build_designs", lib.ffs_grid_build_designs, C.byref(d), D, C.byref(o), _stream())
+
     if stream is None:
-        _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
+        launch()
     else:
         stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(stream):
-            _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
+            launch()
     # G' X = I for every pair, so G'1 = c exactly when the constant is in
     # span(X): the centring correction of the GLS uses the FP64 coefficients
     # rather than sums of the fp32 G (the flag decides on the device)
-    f.Gsum = ccoef.reshape(1, K).expand(P, K).contiguous()
+    f.Gsum = ccoef.reshape(D, 1, K).expand(D, P, K).reshape(DP, K).contiguous()
     f._keep = (Xc, run_start, tau, work)  # inputs must outlive the launch
     return f
 
@@ -291,14 +319,14 @@ BASIS_MAX_K = 32
 
 
 def design_basis(X: torch.Tensor) -> torch.Tensor:
-    """Q0 [K][T]: the orthonormal basis of the design's columns (FP64 Cholesky),
+    """Q0 [K][ld_t(T)]: the orthonormal basis of the design's columns (FP64 Cholesky),
     from X alone, so the residualisation need not wait for the grid build."""
     lib = _lib.load()
     dev = X.device
     T, K = X.shape
     Xc = X.to(torch.float32).contiguous()
     work = torch.empty(int(lib.ffs_design_basis_work_bytes(T, K)) // 8 + 1, dtype=torch.float64, device=dev)
-    q0 = torch.empty(K, T, dtype=torch.float32, device=dev)
+    q0 = torch.empty(K, ld_t(T), dtype=torch.float32, device=dev)
     info = torch.empty(1, dtype=torch.int32, device=dev)
     _run("ffs_design_basis", lib.ffs_design_basis, T, K, _p(Xc), _p(work), _p(q0), _p(info), _stream())
     q0._keep = (Xc, work, info)
@@ -405,6 +433,118 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
 
 
 @dataclass
+class DesignSlots:
+    """Voxel layout of a grouped fit (one design per voxel group).
+
+    The voxels of each design occupy a run of slots padded to a multiple of 256,
+    so every 32-voxel tile of the residualisation, 128-row tile of the
+    projection and 256-voxel tile of the criterion belongs to one design.
+    """
+
+    V: int                 # voxels
+    Vp: int                # slots
+    idx: torch.Tensor      # [Vp] int32 voxel of each slot, -1 for padding
+    real: torch.Tensor     # [V] int64 slot of each voxel
+    design: torch.Tensor   # [V] int32 design of each voxel
+    tile32: torch.Tensor   # [Vp / 32] int32
+    tile256: torch.Tensor  # [Vp / 256] int32
+    items: torch.Tensor    # [n_items][6] int32 projection work list (ffs_tc_item)
+    n_items: torch.Tensor  # [1] int32
+    max_pairs: int
+
+
+def design_slots(gid: np.ndarray, n_designs: int, K: int, P: int, dev) -> DesignSlots:
+    """Slots and the (design, voxel tile, pair block) projection work list of a
+    grouped fit; ``gid`` [V] holds each voxel's design index (host)."""
+    gid = np.asarray(gid, dtype=np.int64).reshape(-1)
+    V = gid.size
+    order = np.argsort(gid, kind="stable")
+    counts = np.bincount(gid, minlength=n_designs)
+    padded = (counts + 255) // 256 * 256
+    start = np.concatenate([[0], np.cumsum(padded)])
+    first = np.concatenate([[0], np.cumsum(counts)])
+    Vp = int(start[-1])
+    idx = np.full(Vp, -1, np.int32)
+    real = np.empty(V, np.int64)
+    for d in range(n_designs):
+        vox = order[first[d]:first[d + 1]]
+        idx[start[d]:start[d] + counts[d]] = vox
+        real[vox] = np.arange(start[d], start[d] + counts[d])
+    tile_of = np.repeat(np.arange(n_designs, dtype=np.int32), padded // 32)
+    g = max(1, min(P, 256 // K))
+    rows = []
+    for d in range(n_designs):
+        for v0 in range(int(start[d]), int(start[d + 1]), 128):
+            for p0 in range(0, P, g):
+                n = min(g, P - p0)
+                rows.append((v0, 128, (d * P + p0) * K, n, v0, p0))
+    items = np.asarray(rows, np.int32).reshape(-1, 6)
+    return DesignSlots(V=V, Vp=Vp, idx=torch.from_numpy(idx).to(dev), real=torch.from_numpy(real).to(dev),
+                       design=torch.from_numpy(gid.astype(np.int32)).to(dev),
+                       tile32=torch.from_numpy(tile_of).to(dev),
+                       tile256=torch.from_numpy(tile_of[::8].copy()).to(dev),
+                       items=torch.from_numpy(items).to(dev),
+                       n_items=torch.tensor([items.shape[0]], dtype=torch.int32, device=dev), max_pairs=g)
+
+
+def search_designs(Y: torch.Tensor, f: GridFactors, slots: DesignSlots, *, hierarchical: bool = True,
+                   do_scale: bool = True) -> SearchOut:
+    """Full-grid REML search of a grouped fit: every voxel against its group's
+    design, all designs in one launch per stage (residualisation, tcgen05
+    projection work list, criterion, selection)."""
+    lib = _lib.load()
+    dev = Y.device
+    V, T = Y.shape
+    K, P, ld, D = f.K, f.P, f.ld, f.n_designs
+    if f.U_hi is None:
+        raise ValueError("the factors were built without the tensor-core operands")
+    st = _stream()
+    Vp = slots.Vp
+    Y = Y.to(dtype=torch.float32).contiguous()
+    q0 = f.U.view(D, P, K, -1)[:, f.grid.p0].contiguous()  # [D][K][ld_t]: U of (0, 0) per design
+    scale = torch.empty(V, dtype=torch.float32, device=dev)
+    yr_t = torch.empty(T, Vp, dtype=torch.float32, device=dev)
+    yr_hi = torch.empty(Vp, ld, dtype=torch.int16, device=dev)
+    yr_lo = torch.empty(Vp, ld, dtype=torch.int16, device=dev)
+    yexp = torch.empty(Vp, dtype=torch.int32, device=dev)
+    pa = _lib.PrepArgs(V=Vp, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=0, ld_y=ld,
+                       scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp),
+                       idx=_p(slots.idx), feats=None, n_runs=0, run_start=None, yr_rows=None,
+                       center_dev=_p(f.center_flag), tile_design=_p(slots.tile32))
+    _run("ffs_reml_prep", lib.ffs_reml_prep, C.byref(pa), st)
+
+    proj = torch.empty(P, Vp, dtype=torch.float32, device=dev)
+    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    ja = _lib.ProjectArgs(V=Vp, T=T, K=K, P=D * P, ld_y=ld, ld_u=ld, yr_hi=_p(yr_hi), yr_lo=_p(yr_lo),
+                          u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yexp=_p(yexp), uexp=_p(f.uexp), yr_t=None, U=None,
+                          proj=_p(proj), flag=_p(flag))
+    n_items = slots.items.shape[0]
+    _run("ffs_reml_project_tc_list", lib.ffs_reml_project_tc_list, C.byref(ja), _p(slots.items), _p(slots.n_items),
+         n_items, slots.max_pairs, 0, st)
+
+    surf = torch.empty(P, Vp, dtype=torch.float32, device=dev)
+    crit0 = torch.empty(Vp, dtype=torch.float64, device=dev)
+    sa = _lib.SurfaceArgs(V=Vp, T=T, K=K, P=P, p0=f.grid.p0, yr_t=_p(yr_t), coef=_p(f.coef),
+                          logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), proj=_p(proj),
+                          chunk_start=_p(f.chunk_start), n_chunks=f.chunk_start.numel() - 1,
+                          chunk_pairs=_p(f.chunk_pairs), surf=_p(surf), crit0=_p(crit0),
+                          tile_design=_p(slots.tile256))
+    _run("ffs_reml_surface", lib.ffs_reml_surface, C.byref(sa), st)
+
+    best = torch.empty(Vp, dtype=torch.int32, device=dev)
+    best_crit = torch.empty(Vp, dtype=torch.float32, device=dev)
+    g = f.grid
+    se = _lib.SelectArgs(V=Vp, P=P, surf=_p(surf), crit0=_p(crit0), hierarchical=int(hierarchical),
+                         n_a=len(g.a_axis), n_b=len(g.b_axis), ltop=g.ltop, za=g.za, zb=g.zb,
+                         lattice=_p(f.lattice), best=_p(best), best_crit=_p(best_crit))
+    _run("ffs_reml_select", lib.ffs_reml_select, C.byref(se), st)
+    out = SearchOut(best=best[slots.real], best_crit=best_crit[slots.real], scale=scale)
+    out._flag = flag
+    out._keep = (q0, yr_t, yr_hi, yr_lo, yexp, proj, surf, crit0)
+    return out
+
+
+@dataclass
 class GlsOut:
     betas: torch.Tensor   # [V][K] (unscaled)
     tstats: torch.Tensor  # [V][K]
@@ -421,18 +561,28 @@ class GlsOut:
 
 
 def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors, X: torch.Tensor, *,
-        want_residuals: bool = False, want_predicted: bool = False, lj=None) -> GlsOut:
-    """GLS refit of every voxel at its pair ``best`` (indices into ``f``)."""
+        want_residuals: bool = False, want_predicted: bool = False, lj=None,
+        design: torch.Tensor | None = None) -> GlsOut:
+    """GLS refit of every voxel at its pair ``best`` (indices into ``f``).
+
+    Grouped fits pass X as (D, T, K) and ``design`` [V] (each voxel's design):
+    voxels are then grouped by design * P + pair."""
     lib = _lib.load()
     dev = Y.device
     V, T = Y.shape
     K, P = f.K, f.P
     st = _stream()
     Y = Y.to(dtype=torch.float32).contiguous()
+    n_pairs = 0
+    if design is not None:
+        best = (design.to(torch.int32) * P + best.to(torch.int32)).contiguous()
+        n_pairs = P
+        P = P * f.n_designs
     order = torch.empty(V, dtype=torch.int32, device=dev)
     work = torch.empty(P + 1, dtype=torch.int32, device=dev)
     _run("ffs_reml_group", lib.ffs_reml_group, V, P, _p(best), _p(work), _p(order), st)
-    Xt = X.to(device=dev, dtype=torch.float32).t().contiguous()
+    X = X.to(device=dev)
+    Xt = padded_design_t(X) if X.ndim == 2 else torch.stack([padded_design_t(x) for x in X])
     f32 = dict(device=dev, dtype=torch.float32)
     ng = 0 if f.glt is None else f.glt.shape[0]
     o = GlsOut(betas=torch.empty(V, K, **f32), tstats=torch.empty(V, K, **f32), sigma2=torch.empty(V, **f32),
@@ -449,7 +599,8 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
                       task_idx=_p(f.task_idx), Ftask=_p(f.Ftask), n_glt=ng, glt=_p(f.glt),
                       glt_var=_p(f.glt_var), betas=_p(o.betas), tstats=_p(o.tstats), sigma2=_p(o.sigma2),
                       fstats=_p(o.fstats), r2=_p(o.r2), lam=_p(o.lam), cbeta=_p(o.cbeta), ct=_p(o.ct),
-                      resid=_p(o.resid), resid_w=_p(o.resid_w), pred=_p(o.pred), center_dev=_p(f.center_flag))
+                      resid=_p(o.resid), resid_w=_p(o.resid_w), pred=_p(o.pred), center_dev=_p(f.center_flag),
+                      n_pairs=n_pairs)
     h, ptau_d, w_d = 0, None, None
     if lj is not None and lj[0] > 0:
         h, ptau, w, _ = lj
@@ -460,5 +611,5 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
     _run("ffs_reml_gls_grouped", lib.ffs_reml_gls_grouped, C.byref(ga), h, _p(ptau_d), _p(w_d), _p(o.ljung_box),
          P, _p(work), _p(tiles), st)
     o._keep = (ptau_d, w_d, tiles)
-    o._keep2 = (Y, order, work, Xt)
+    o._keep2 = (Y, order, work, Xt, best)
     return o

@@ -15,7 +15,8 @@
  *
  * Notation: V voxels, T retained time points, K design columns, P valid (a,b)
  * pairs, R runs. "time-major" = [T][V] (voxel index fastest), "voxel-major" =
- * [V][T].
+ * [V][T]. Every K x T matrix (U, G, Q0, Xt) is stored with row stride
+ * ld_t = T rounded up to a multiple of 4 (16-byte rows), the padding zero.
  */
 #ifndef FFS_REML_H
 #define FFS_REML_H
@@ -59,7 +60,7 @@ const char* ffs_last_error(void);
  *                  c_t = m_t = 0 at every run start.
  *   logdet_R[p]  = 2 sum_t log(sqrt(D_t) + 1e-10)          (FP64)
  *   logdet_XtX[p]= 2 sum_j log(|L_xtx,jj| + 1e-10)          (FP64)
- *   U[p]         = L^-T Q, Q = X_w L_xtx^-T, stored [P][K][T] fp32:
+ *   U[p]         = L^-T Q, Q = X_w L_xtx^-T, stored [P][K][ld_t] fp32:
  *                  ||Q' L^-1 y||^2 = ||U' y||^2 for any series y.
  *   U_hi/U_lo    = the same as an fp16 split of U * 2^uexp[p] (hi + lo carry
  *                  about 22 significant bits; the power of two puts each
@@ -68,7 +69,7 @@ const char* ffs_last_error(void);
  *                  the projection GEMM.
  *   pairs with lambda == 0 have R = I exactly; their coefficients are the
  *   identity (c = m = 0, D = 1), so ties between them stay exact ties.
- *   G[p]         = U L_xtx^-1 = R^-1 X (X'R^-1 X)^-1, [P][K][T] fp32:
+ *   G[p]         = U L_xtx^-1 = R^-1 X (X'R^-1 X)^-1, [P][K][ld_t] fp32:
  *                  GLS betas b = G' y.
  *   Adiag[p][K]  = diag((X_w'X_w)^-1);  XtX[p][K][K] = X_w'X_w (fp32).
  *   Ftask[p]     = inv(A_task + 1e-8 I) for the task-column F statistic
@@ -98,11 +99,11 @@ typedef struct {
   float* coef;          /* [P][T][4]                                              */
   double* logdet_R;     /* [P]                                                    */
   double* logdet_XtX;   /* [P]                                                    */
-  float* U;             /* [P][K][T]                                              */
+  float* U;             /* [P][K][ld_t]                                           */
   uint16_t* U_hi;       /* [P*K][ld_u] fp16 bits (may be NULL)                    */
   uint16_t* U_lo;       /* [P*K][ld_u] fp16 bits (may be NULL)                    */
   int* uexp;            /* [P] power-of-two scale of U_hi/U_lo (with U_hi)        */
-  float* G;             /* [P][K][T]                                              */
+  float* G;             /* [P][K][ld_t]                                           */
   float* Adiag;         /* [P][K]                                                 */
   float* XtX;           /* [P][K][K]                                              */
   int* info;            /* [P]                                                    */
@@ -114,6 +115,17 @@ typedef struct {
 
 size_t ffs_grid_work_bytes(int T, int K, int P);
 int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
+
+/* ffs_grid_build for n_designs designs of one shape at once (the per-group
+ * designs of fastfuncstuff/glm/arma.py:2836-3183, which the reference fits one
+ * group after another): d->X is [n_designs][T][K]. coef and logdet_R depend on
+ * the pair only and keep their [P] layout; every other output is indexed by
+ * pd = design * P + pair (U [n_designs * P][K][T], logdet_XtX [n_designs * P],
+ * U_hi rows pd * K + j, ...). One launch walks the n_designs * P items with
+ * at most FFS_GRID_MAX_SLOTS CTAs; work: ffs_grid_work_bytes_designs. */
+#define FFS_GRID_MAX_SLOTS 2048
+size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs);
+int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, const ffs_grid_out* o, void* stream);
 
 /* ffs_grid_build without a workspace argument: this variant has no counterpart
  * in the reference. It is for callers that cannot allocate device memory where
@@ -134,7 +146,7 @@ int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
 #define FFS_GRID_STATIC_SCRATCH_BYTES ((size_t)16 << 20)
 int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
 
-/* Orthonormal basis of the design's columns, Q0 [K][T] fp32 (no reference
+/* Orthonormal basis of the design's columns, Q0 [K][ld_t] fp32 (no reference
  * counterpart as a separate step: it is U of the pair (0, 0), which
  * ffs_grid_build also writes). Q0 = X Lx^-T with Lx the FP64 Cholesky factor of
  * X'X, or modified Gram-Schmidt (twice) when X'X is not positive definite
@@ -160,7 +172,7 @@ int ffs_design_basis(int T, int K, const float* X, void* work, float* Q0, int* i
 typedef struct {
   int V, T, K;
   const float* Y;       /* device [V][T] voxel-major input                       */
-  const float* Q0;      /* device [K][T]: orthonormal basis of the design columns*/
+  const float* Q0;      /* device [K][ld_t]: orthonormal basis of the design columns */
   int do_scale;
   int center;
   int ld_y;
@@ -183,6 +195,11 @@ typedef struct {
   float* yr_rows;       /* NULL, or [V][T] the residualised rows, voxel-major    */
   const int* center_dev;/* NULL, or a device int that replaces `center` (set by
                            the caller's stream, so deciding needs no host sync) */
+  /* Grouped fits (one design per voxel group): with tile_design, Q0 is
+   * [n_designs][K][T] and tile v / 32 of the output rows uses design
+   * tile_design[v / 32]; idx[i] < 0 marks an empty (padding) output row,
+   * whose outputs are zero and which writes no scale. */
+  const int* tile_design;
 } ffs_prep_args;
 
 int ffs_reml_prep(const ffs_prep_args* a, void* stream);
@@ -203,7 +220,7 @@ typedef struct {
   const int* yexp;      /* [V] */
   const int* uexp;      /* [P] */
   const float* yr_t;    /* [T][V] (simt form)                                    */
-  const float* U;       /* [P][K][T] (simt form)                                 */
+  const float* U;       /* [P][K][ld_t] (simt form)                              */
   float* proj;          /* [P][V]                                                 */
   int* flag;            /* device int, 0 on entry; set non-zero if a bounded
                            device-side wait expired (tc form)                    */
@@ -213,13 +230,17 @@ int ffs_reml_project_tc(const ffs_project_args* a, void* stream);
 int ffs_reml_project_simt(const ffs_project_args* a, void* stream);
 
 /* Work-list form of ffs_reml_project_tc (no reference counterpart: the
- * learned-seeded refine evaluates each voxel's 5 x 5 window only). Item i
- * projects the 128 operand rows v0 .. v0+127 (nv of them real) onto the np
- * consecutive pairs whose U rows start at row_b (= first pair * K) and writes
+ * learned-seeded refine evaluates each voxel's 5 x 5 window only, and the
+ * grouped fit walks (design, pair block, voxel tile) items in one launch).
+ * Item i projects the 128 operand rows v0 .. v0+127 (nv of them real) onto the
+ * np consecutive pairs whose U rows start at row_b (= first pair * K) and
+ * writes, for ld_out > 0,
  *   proj[(out0 + r) * ld_out + slot0 + j] = ||U_{p+j}' y_{v0+r}||^2
+ * or, for ld_out == 0, pair-major proj[(slot0 + j) * a->V + out0 + r].
  * The item count is read on the device from *n_items (<= max_items); every
  * item has np <= max_pairs and max_pairs * K <= 256. a->V is the number of
- * operand rows, a->proj the output. */
+ * operand rows, a->P the number of U row blocks (pairs, or designs x pairs:
+ * uexp[row_b / K + j] scales pair j), a->proj the output. */
 typedef struct {
   int v0, nv;     /* first operand row, real rows (<= 128)                       */
   int row_b, np;  /* first U row, pairs                                          */
@@ -255,6 +276,9 @@ typedef struct {
                           /*   lambda == 0 (identity)                            */
   float* surf;            /* [P][V] d[p][v]                                       */
   double* crit0;          /* [V]                                                  */
+  const int* tile_design; /* NULL, or [ceil(V / 256)]: the design of each tile of */
+                          /*   256 voxels (grouped fits); logdet_XtX is then      */
+                          /*   [n_designs][P] and read at design * P + pair       */
 } ffs_surface_args;
 
 int ffs_reml_surface(const ffs_surface_args* a, void* stream);
@@ -296,7 +320,7 @@ typedef struct {
   const float* Gsum;      /* [P][K] (used with center)                            */
   const float* Y;         /* [V][T] voxel-major input data (unscaled)             */
   const float* scale;     /* [V]                                                  */
-  const float* Xt;        /* [K][T] the design, transposed                        */
+  const float* Xt;        /* [K][ld_t] the design, transposed                     */
   const int* best;        /* [V] pair per voxel                                   */
   const int* order;       /* [V] voxel permutation (grouped by pair) or NULL      */
   const float* coef; const float* G; const float* Adiag; const float* XtX;
@@ -312,6 +336,11 @@ typedef struct {
   float* cbeta; float* ct;                           /* [V][n_glt] or NULL        */
   float* resid; float* resid_w; float* pred;         /* [V][T] or NULL            */
   const int* center_dev; /* NULL, or a device int that replaces `center`        */
+  int n_pairs;            /* 0: one design, best[] / the groups are pairs.        */
+                          /* > 0 (grouped fits): they are keys design * n_pairs + */
+                          /*   pair; G, Adiag, XtX, Gsum, Ftask and glt_var are   */
+                          /*   read at the key, coef, a, b at the pair and Xt is  */
+                          /*   [n_designs][K][T], read at the design              */
 } ffs_gls_args;
 
 int ffs_reml_gls(const ffs_gls_args* a, void* stream);

@@ -95,8 +95,10 @@ def test_grid_factors_match_reference_precompute():
     # U = L^-T Q and G = R^-1 X (X'R^-1 X)^-1 against the dense FP64 restatement
     og = o.valid_grid(d["a_grid"], d["b_grid"], np.float64)
     pre = o.precompute_reml_grid(Xd, og, run_starts=d["run_starts"])
-    U = f.U.cpu().numpy()
-    Gm = f.G.cpu().numpy()
+    T = Xd.shape[0]
+    assert f.U.shape[2] == (T + 3) // 4 * 4 and not f.U[:, :, T:].any() and not f.G[:, :, T:].any()
+    U = f.U[:, :, :T].cpu().numpy()
+    Gm = f.G[:, :, :T].cpu().numpy()
     for p in range(0, f.P, 5):
         Li = pre.whiteners[p].dense()
         U_ref = Li.T @ pre.Q[p]
@@ -176,8 +178,9 @@ def test_fit_matches_fp64_oracle(case, exhaustive):
 
 @pytest.mark.parametrize("T", [96, 94, 93])
 def test_fit_any_series_length_matches_fp64_oracle(T):
-    """T % 4 == 0 runs the 32-voxel tile kernels of prep and GLS; other lengths
-    the one-warp-per-voxel kernels. Both against the FP64 oracle, with the
+    """The 32-voxel tile kernels of prep and GLS read 16-byte words of Y when
+    T % 4 == 0 and single samples otherwise (the K x T matrices are padded to
+    a multiple of 4 either way). Both against the FP64 oracle, with the
     residual, whitened-residual, fitted-value and Ljung-Box outputs."""
     d = load_golden("single")
     Y = np.ascontiguousarray(d["Y"][:, :T])
@@ -238,6 +241,32 @@ def test_grouped_matches_reference():
     assert agree >= 0.99, agree
     same = idx == ref_idx
     assert rel_maxnorm(got.betas.numpy()[same], d["f64_exh__betas"][same]).max() <= BETA_REL
+
+
+@pytest.mark.parametrize("selector", ["hierarchical", "exhaustive"])
+def test_grouped_batched_fit_equals_per_group_fits(selector):
+    """The grouped fit runs every design in one pass per stage (one grid build
+    over designs x pairs, a (design, voxel tile, pair block) projection work
+    list, per-tile designs in prep and the criterion, design x pair keys in
+    the GLS). Each voxel's arithmetic is the per-group fit's, so the results
+    are those of fitting every group on its own: workload-2 shapes (4 censored
+    runs, N=855, Zipf group sizes), fewer voxels and 6 of the 20 designs."""
+    w = synth.workload(2, V=6000)
+    keep = np.isin(w.groups, np.arange(6))
+    Y, gid = w.Y[keep], w.groups[keep]
+    designs = {h: w.designs[h] for h in range(6)}
+    kw = dict(a_grid=np.linspace(-0.8, 0.8, 17), b_grid=np.linspace(-0.8, 0.8, 17), run_starts=w.run_starts,
+              tau=w.tau, device=DEV, verbose=False, force_exhaustive_search=selector == "exhaustive",
+              want_residuals=True, glt_labels=["t0-t1"], glt_matrices=[np.eye(18)[0] - np.eye(18)[1]])
+    got = fit_glm_arma11_grouped(Y, designs, gid, tr=2.0, **kw)
+    for h in range(6):
+        m = gid == h
+        ref = fit_glm_arma11(Y[m], designs[h], tr=2.0, **kw)
+        np.testing.assert_array_equal(got.arma_params.numpy()[m], ref.arma_params.numpy())
+        np.testing.assert_array_equal(got.reml_likelihood.numpy()[m], ref.reml_likelihood.numpy())
+        for name in ("betas", "tstats", "sigma2", "fstats", "r2", "arma_lambda", "contrast_betas",
+                     "contrast_tstats", "residuals", "residuals_whitened"):
+            np.testing.assert_array_equal(getattr(got, name).numpy()[m], getattr(ref, name).numpy(), err_msg=name)
 
 
 def test_precomputed_params_path():

@@ -192,3 +192,34 @@ def test_kernel_model_with_host_structures_matches_oracle(case):
     bad = best != ref
     gap = np.abs(surf64[bad, best[bad]] - surf64[bad, ref[bad]]) / np.abs(surf64[bad, ref[bad]])
     assert gap.size == 0 or gap.max() <= 1e-6
+
+
+def test_design_slots_layout():
+    """Grouped-fit slots: each design's voxels contiguous and padded to 256
+    slots, every voxel in exactly one slot, the projection work list covering
+    every (slot tile of 128, pair) once with the design's U rows."""
+    from fastfuncstuff_gb300.glm import engine
+
+    rng = np.random.default_rng(3)
+    D, K, P = 5, 18, 561
+    gid = rng.choice(D, 3001, p=[0.5, 0.2, 0.15, 0.1, 0.05])
+    gid[gid == 3] = 4  # one design without voxels
+    s = engine.design_slots(gid, D, K, P, "cpu")
+    idx = s.idx.numpy()
+    assert s.Vp % 256 == 0 and s.Vp == idx.size
+    real = idx >= 0
+    assert np.array_equal(np.sort(idx[real]), np.arange(gid.size))
+    assert np.array_equal(idx[s.real.numpy()], np.arange(gid.size))
+    design_of_slot = np.repeat(s.tile32.numpy(), 32)
+    assert np.array_equal(design_of_slot[s.real.numpy()], gid)
+    assert np.array_equal(np.repeat(s.tile256.numpy(), 256), design_of_slot)
+    items = s.items.numpy()
+    assert int(s.n_items[0]) == items.shape[0] and s.max_pairs * K <= 256
+    cover = np.zeros((s.Vp // 128, P), np.int32)
+    for v0, nv, row_b, npr, out0, slot0 in items:
+        assert nv == 128 and out0 == v0 and 1 <= npr <= s.max_pairs
+        d = design_of_slot[v0]
+        assert row_b == (d * P + slot0) * K
+        cover[v0 // 128, slot0:slot0 + npr] += 1
+    assert (cover == 1).all()
+

@@ -43,6 +43,7 @@ def _build(entry, g, lay, X, with_work):
     T, K = X.shape
     P = g.P
     ld = (T + 63) // 64 * 64
+    lt = (T + 3) // 4 * 4  # row stride of U and G
     f32 = dict(device=DEV, dtype=torch.float32)
     keep = dict(
         a=torch.from_numpy(g.a).to(DEV), b=torch.from_numpy(g.b).to(DEV),
@@ -50,9 +51,9 @@ def _build(entry, g, lay, X, with_work):
     )
     out = dict(
         coef=torch.full((P, T, 4), np.nan, **f32), logdet_R=torch.full((P,), np.nan, dtype=torch.float64, device=DEV),
-        logdet_XtX=torch.full((P,), np.nan, dtype=torch.float64, device=DEV), U=torch.full((P, K, T), np.nan, **f32),
+        logdet_XtX=torch.full((P,), np.nan, dtype=torch.float64, device=DEV), U=torch.full((P, K, lt), np.nan, **f32),
         U_hi=torch.zeros(P * K, ld, dtype=torch.int16, device=DEV), U_lo=torch.zeros(P * K, ld, dtype=torch.int16, device=DEV),
-        uexp=torch.zeros(P, dtype=torch.int32, device=DEV), G=torch.full((P, K, T), np.nan, **f32),
+        uexp=torch.zeros(P, dtype=torch.int32, device=DEV), G=torch.full((P, K, lt), np.nan, **f32),
         Adiag=torch.full((P, K), np.nan, **f32), XtX=torch.full((P, K, K), np.nan, **f32),
         info=torch.full((P,), -1, dtype=torch.int32, device=DEV), Gsum=torch.full((P, K), np.nan, **f32),
     )
