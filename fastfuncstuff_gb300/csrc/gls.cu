@@ -32,7 +32,13 @@ __device__ __forceinline__ int pair_of(const ffs_gls_args& a, int g) { return a.
 __device__ __forceinline__ int design_of(const ffs_gls_args& a, int g) { return a.n_pairs > 0 ? g / a.n_pairs : 0; }
 
 __device__ void gls_finish(const ffs_gls_args& a, const GlsExtra& x, int v, int g, float* beta, const float* w,
-                           float ssr, float sst, float ssw, float m, float sc, float* bins);
+                           float ssr, float sst, float ssw, float m, float sc, float* bins, const float* Mq);
+
+// The F statistic's matrix of group g: inv(A_task + 1e-8 I) for task columns,
+// X_w'X_w for the full model.
+__device__ __forceinline__ const float* quad_matrix(const ffs_gls_args& a, int g) {
+  return a.n_task > 0 ? a.Ftask + (size_t)g * a.n_task * a.n_task : a.XtX + (size_t)g * a.K * a.K;
+}
 
 // GLS of one voxel v at pair g, executed by one warp. Gp = G of pair g and Xt
 // (the transposed design) may live in shared or global memory; ys, r, beta and
@@ -123,7 +129,7 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
   float ssw = 0.f;
   for (int t = lane; t < T; t += 32) ssw = fmaf(ys[t], ys[t], ssw);
   ssw = warp_sum(ssw);
-  gls_finish(a, x, v, g, beta, ys, ssr, sst, ssw, m, sc, bins);
+  gls_finish(a, x, v, g, beta, ys, ssr, sst, ssw, m, sc, bins, quad_matrix(a, g));
 }
 
 // The statistics of voxel v at pair g from its betas (of the centred, scaled
@@ -131,7 +137,7 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
 // sums of squares; executed by one warp.
 __device__ void gls_finish(const ffs_gls_args& a, const GlsExtra& x, const int v, const int g, float* beta,
                            const float* w, const float ssr, const float sst, const float ssw, const float m,
-                           const float sc, float* bins) {
+                           const float sc, float* bins, const float* Mq) {
   const int lane = threadIdx.x & 31;
   const int T = a.T, K = a.K;
   const float* ys = w;
@@ -154,14 +160,14 @@ __device__ void gls_finish(const ffs_gls_args& a, const GlsExtra& x, const int v
   }
   float quad = 0.f;
   if (a.n_task > 0) {
-    const float* M = a.Ftask + (size_t)g * a.n_task * a.n_task;
+    const float* M = Mq;
     for (int k = lane; k < a.n_task; k += 32) {
       float s = 0.f;
       for (int l = 0; l < a.n_task; ++l) s = fmaf(M[k * a.n_task + l], beta[a.task_idx[l]], s);
       quad = fmaf(beta[a.task_idx[k]], s, quad);
     }
   } else {
-    const float* M = a.XtX + (size_t)g * K * K;
+    const float* M = Mq;
     for (int k = lane; k < K; k += 32) {
       float s = 0.f;
       for (int l = 0; l < K; ++l) s = fmaf(M[k * K + l], beta[l], s);
@@ -258,10 +264,10 @@ constexpr int GLS_TILE = TILE_V;
 
 __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_args a, GlsExtra x, const int* end,
                                                                    const int* tile_start, int P, int ld, int kp,
-                                                                   int hb) {
+                                                                   int hb, int msz) {
   extern __shared__ float4 sm4[];
   const int T = a.T, K = a.K, LT = ld_t(T), nq = LT >> 2;
-  const bool vec = (T & 3) == 0;  // 16-byte rows of Y and of the [V][T] outputs
+  const bool vec = (T & 3) == 0;  // 16-byte rows of the [V][T] outputs
   float* Ys = reinterpret_cast<float*>(sm4);        // [32][ld]
   float* C0 = Ys + (size_t)TILE_V * ld;             // [K][32] b0
   float* C1 = C0 + (size_t)K * TILE_V;              // [K][32] d
@@ -272,6 +278,7 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
   float* st = Hs + TILE_V;                          // [6][32] m, sc, mean, ssr, sst, ssw
   float* betas = st + 6 * TILE_V;                   // [8][kp]
   float* bins = betas + (size_t)TILE_WARPS * kp;    // [8][hb]
+  float* Ms = bins + (size_t)TILE_WARPS * hb;       // [msz] the F matrix of the tile's group (msz > 0)
 
   const int tile = blockIdx.x;
   if (tile >= tile_start[P]) return;
@@ -287,10 +294,19 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 
   // stage (y - m) / s of each voxel; empty slots of a short tile are zero
+  __shared__ int src_row[TILE_V];
+  if (threadIdx.x < TILE_V) src_row[threadIdx.x] = (int)threadIdx.x < n ? a.order[j0 + threadIdx.x] : -1;
+  const float* Mq = quad_matrix(a, g);
+  if (msz > 0) {  // read by every voxel's F statistic
+    for (int i = threadIdx.x; i < msz; i += blockDim.x) Ms[i] = Mq[i];
+    Mq = Ms;
+  }
+  __syncthreads();
+  tile_stage_rows(a.Y, T, nq, src_row, Ys, ld);
+  const bool centre = a.center_dev ? (*a.center_dev != 0) : (a.center != 0);
   for (int i = wid; i < TILE_V; i += TILE_WARPS) {
     float4* row4 = reinterpret_cast<float4*>(Ys + (size_t)i * ld);
     if (i >= n) {  // warp-uniform
-      for (int q = lane; q < nq; q += 32) row4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (lane == 0) {
         st[i] = 0.f;
         st[TILE_V + i] = 1.f;
@@ -298,28 +314,19 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
       }
       continue;
     }
-    const int v = a.order[j0 + i];
-    const float sc = a.scale[v];
-    const float* yv = a.Y + (size_t)v * T;
-    // quad q of the row; samples past T read as zero
-    auto quad = [&](int q) {
-      if (vec) return reinterpret_cast<const float4*>(yv)[q];
-      const int t = 4 * q;
-      return make_float4(yv[t], t + 1 < T ? yv[t + 1] : 0.f, t + 2 < T ? yv[t + 2] : 0.f,
-                         t + 3 < T ? yv[t + 3] : 0.f);
-    };
+    const float sc = a.scale[src_row[i]];
     float m = 0.f;
-    if (a.center_dev ? (*a.center_dev != 0) : (a.center != 0)) {
+    if (centre) {
       float s = 0.f;
       for (int q = lane; q < nq; q += 32) {
-        const float4 y = quad(q);
+        const float4 y = row4[q];
         s += ((y.x + y.y) + y.z) + y.w;
       }
       m = warp_sum(s) / (float)T;
     }
     float sy = 0.f;
     for (int q = lane; q < nq; q += 32) {
-      const float4 y = quad(q);
+      const float4 y = row4[q];
       const int t = 4 * q;
       float4 r;
       r.x = __fdiv_rn(__fsub_rn(y.x, m), sc);
@@ -496,7 +503,7 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
     for (int j = lane; j < K; j += 32) b[j] = C0[j * TILE_V + i] + C1[j * TILE_V + i];
     __syncwarp();
     gls_finish(a, x, v, g, b, Ys + (size_t)i * ld, st[3 * TILE_V + i], st[4 * TILE_V + i], st[5 * TILE_V + i],
-               st[i], st[TILE_V + i], bins + (size_t)wid * hb);
+               st[i], st[TILE_V + i], bins + (size_t)wid * hb, Mq);
     __syncwarp();
   }
 }
@@ -573,9 +580,11 @@ extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* 
   const int ld = tile_ld(a->T);
   const int kp = (a->K + 3) & ~3;
   const int hb = (lj_h + 4) & ~3;
+  const int nm = a->n_task > 0 ? a->n_task : a->K;
+  const int msz = nm * nm <= 4096 ? nm * nm : 0;  // F matrix staged per tile when it is small
   const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + 2 * (size_t)a->K * TILE_V +
                                        (1 + 2) * TILE_WARPS * TILE_V + TILE_V + 6 * TILE_V +
-                                       (size_t)TILE_WARPS * (kp + hb));
+                                       (size_t)TILE_WARPS * (kp + hb) + msz);
   if (smem > 200 * 1024) {  // the tile does not fit: one warp per voxel
     return ffs_reml_gls_ex(a, lj_h, lj_tau, lj_w, ljung_box, stream);
   }
@@ -584,7 +593,7 @@ extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* 
   gls_tile_scan<<<1, 1024, 0, st>>>(P, group_end, tile_start);
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(gls_tile_kernel), smem));
   const int max_tiles = ceil_div(a->V, GLS_TILE) + P;
-  gls_tile_kernel<<<max_tiles, TILE_WARPS * 32, smem, st>>>(*a, x, group_end, tile_start, P, ld, kp, hb);
+  gls_tile_kernel<<<max_tiles, TILE_WARPS * 32, smem, st>>>(*a, x, group_end, tile_start, P, ld, kp, hb, msz);
   return check_launch("gls_tile_kernel");
 }
 

@@ -26,6 +26,8 @@ namespace ffsk {
 
 namespace {
 
+constexpr int GB_PF = 8;  // samples loaded ahead in the sequential recursions
+
 struct PairScratch {
   double* cm;  // [T][4]  c, m, D, 1/sqrt(D)
   double* Xw;  // [K][T]  whitened design, later U = L^-T Q
@@ -128,6 +130,7 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
 
   __shared__ double red[32];
   __shared__ int flag, bad_r;
+  extern __shared__ double cms[];  // [T][4] c, m, D, 1/sqrt(D) of the current pair
 
   for (int item = blockIdx.x; item < d.P * n_designs; item += gridDim.x) {
     const int p = item % d.P, pd = item;
@@ -167,7 +170,7 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
           bad_r = 1;
           D = 1.0;
         }
-        double* cm = s.cm + 4 * t;
+        double* cm = cms + 4 * t;
         cm[0] = c; cm[1] = m; cm[2] = D;
         Dprev = D;
       }
@@ -176,7 +179,7 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
     {
       double ld = 0.0;
       for (int t = threadIdx.x; t < T; t += blockDim.x) {
-        double* cm = s.cm + 4 * t;
+        double* cm = cms + 4 * t;
         const double D = cm[2];
         const double sD = sqrt(D);
         const double rsD = 1.0 / sD;
@@ -190,17 +193,27 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
     }
     __syncthreads();
 
-    // ---- 2. X_w = L^-1 X, one column per thread
+    // ---- 2. X_w = L^-1 X, one column per thread; the design samples of
+    // GB_PF steps are loaded ahead of the recursion that needs them
     for (int j = threadIdx.x; j < K; j += blockDim.x) {
       double xp = 0.0, vp = 0.0;
-      for (int t = 0; t < T; ++t) {
-        const double* cm = s.cm + 4 * t;
-        const double x = (double)Xd[(size_t)t * K + j];
-        const double z = x - cm[0] * xp;
-        const double v = z - cm[1] * vp;
-        s.Xw[(size_t)j * T + t] = v * cm[3];
-        xp = x;
-        vp = v;
+      for (int t0 = 0; t0 < T; t0 += GB_PF) {
+        float xb[GB_PF];
+#pragma unroll
+        for (int k = 0; k < GB_PF; ++k) xb[k] = t0 + k < T ? __ldg(Xd + (size_t)(t0 + k) * K + j) : 0.f;
+#pragma unroll
+        for (int k = 0; k < GB_PF; ++k) {
+          const int t = t0 + k;
+          if (t < T) {
+            const double* cm = cms + 4 * t;
+            const double x = (double)xb[k];
+            const double z = x - cm[0] * xp;
+            const double v = z - cm[1] * vp;
+            s.Xw[(size_t)j * T + t] = v * cm[3];
+            xp = x;
+            vp = v;
+          }
+        }
       }
     }
     __syncthreads();
@@ -212,7 +225,17 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
       const double* xi = s.Xw + (size_t)i * T;
       const double* xj = s.Xw + (size_t)j * T;
       double acc = 0.0;
-      for (int t = 0; t < T; ++t) acc += xi[t] * xj[t];
+      for (int t0 = 0; t0 < T; t0 += GB_PF) {  // GB_PF samples of both columns in flight
+        double ai[GB_PF], aj[GB_PF];
+#pragma unroll
+        for (int k = 0; k < GB_PF; ++k) {
+          ai[k] = t0 + k < T ? xi[t0 + k] : 0.0;
+          aj[k] = t0 + k < T ? xj[t0 + k] : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < GB_PF; ++k)
+          if (t0 + k < T) acc += ai[k] * aj[k];
+      }
       s.Lx[i * K + j] = acc;
       s.Lx[j * K + i] = acc;
       o.XtX[(size_t)pd * K * K + i * K + j] = (float)acc;
@@ -296,16 +319,30 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
       const float* q = qf + (size_t)j * T;
       float* u = uf + (size_t)j * T;
       float xn = 0.f, mn = 0.f, cn = 0.f;  // x_{t+1}, m_{t+1}, c_{t+1}
-      for (int t = T - 1; t >= 0; --t) {
-        const float4 c4 = cf[t];  // (c, m, 1/D, 1/sqrt(D))
-        const float x = fmaf(-mn, xn, q[t] * c4.w);
-        const float ut = fmaf(-cn, xn, x);
-        u[t] = ut;
-        o.U[((size_t)pd * K + j) * LT + t] = ut;
-        umax_local = fmaxf(umax_local, fabsf(ut));
-        xn = x;
-        mn = c4.y;
-        cn = c4.x;
+      for (int t1 = T - 1; t1 >= 0; t1 -= GB_PF) {  // GB_PF steps of q and coef loaded ahead
+        float qb[GB_PF];
+        float4 cb[GB_PF];
+#pragma unroll
+        for (int k = 0; k < GB_PF; ++k) {
+          const int t = t1 - k;
+          qb[k] = t >= 0 ? q[t] : 0.f;
+          cb[k] = t >= 0 ? cf[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < GB_PF; ++k) {
+          const int t = t1 - k;
+          if (t >= 0) {
+            const float4 c4 = cb[k];  // (c, m, 1/D, 1/sqrt(D))
+            const float x = fmaf(-mn, xn, qb[k] * c4.w);
+            const float ut = fmaf(-cn, xn, x);
+            u[t] = ut;
+            o.U[((size_t)pd * K + j) * LT + t] = ut;
+            umax_local = fmaxf(umax_local, fabsf(ut));
+            xn = x;
+            mn = c4.y;
+            cn = c4.x;
+          }
+        }
       }
       for (int t = T; t < LT; ++t) o.U[((size_t)pd * K + j) * LT + t] = 0.f;
     }
@@ -504,7 +541,10 @@ extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, voi
                   o->info && o->work,
               "ffs_grid_build: null output");
   BuildArgs args{*d, *o};
-  grid_build_kernel<<<d->P, 256, 0, (cudaStream_t)stream>>>(args, 1);
+  const size_t smem = sizeof(double) * 4 * (size_t)d->T;
+  FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build: T=%d too long", d->T);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel), smem));
+  grid_build_kernel<<<d->P, 256, smem, (cudaStream_t)stream>>>(args, 1);
   return check_launch("grid_build_kernel");
 }
 
@@ -527,7 +567,10 @@ extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, con
   const long long items = (long long)d->P * n_designs;
   const int grid = (int)(items < FFS_GRID_MAX_SLOTS ? items : FFS_GRID_MAX_SLOTS);
   BuildArgs args{*d, *o};
-  grid_build_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(args, n_designs);
+  const size_t smem = sizeof(double) * 4 * (size_t)d->T;
+  FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build_designs: T=%d too long", d->T);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel), smem));
+  grid_build_kernel<<<grid, 256, smem, (cudaStream_t)stream>>>(args, n_designs);
   return check_launch("grid_build_kernel (designs)");
 }
 
@@ -607,6 +650,9 @@ extern "C" int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out
   // the previous call's contents need no clearing
   BuildArgs args{*d, *o};
   args.o.work = scratch;
-  grid_build_kernel<<<d->P, 256, 0, (cudaStream_t)stream>>>(args, 1);
+  const size_t smem = sizeof(double) * 4 * (size_t)d->T;
+  FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build_noalloc: T=%d too long", d->T);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel), smem));
+  grid_build_kernel<<<d->P, 256, smem, (cudaStream_t)stream>>>(args, 1);
   return check_launch("grid_build_kernel (static scratch)");
 }

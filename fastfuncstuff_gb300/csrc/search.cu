@@ -141,40 +141,28 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
   float* Cq = Ys + (size_t)TILE_V * ld;            // [K][32]
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int T = a.T, K = a.K, LT = ld_t(T), nq = LT >> 2;
-  const bool vec = (T & 3) == 0;
+  const bool vec = (T & 3) == 0;  // 16-byte rows of the [V][T] outputs
   const int v0 = blockIdx.x * TILE_V;
   const int nv = min(TILE_V, a.V - v0);
-  for (int i = wid; i < TILE_V; i += TILE_WARPS) {
+  __shared__ int src_row[TILE_V];  // source row of each tile row (-1: zero row)
+  if (threadIdx.x < TILE_V) {
+    const int i = threadIdx.x;
+    src_row[i] = i >= nv ? -1 : (a.idx ? a.idx[v0 + i] : v0 + i);
+  }
+  __syncthreads();
+  tile_stage_rows(a.Y, T, nq, src_row, Ys, ld);
+  for (int i = wid; i < nv; i += TILE_WARPS) {
+    const int vs = src_row[i];
+    if (vs < 0) continue;  // warp-uniform: an empty (padding) row stays zero
     float* row = Ys + (size_t)i * ld;
-    float4* row4 = reinterpret_cast<float4*>(row);
-    if (i >= nv) {  // warp-uniform: empty lanes of the last tile stay zero
-      for (int q = lane; q < nq; q += 32) row4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-      continue;
-    }
-    const int vs = a.idx ? a.idx[v0 + i] : v0 + i;  // source row
-    if (vs < 0) {  // warp-uniform: an empty (padding) row stays zero
-      for (int q = lane; q < nq; q += 32) row4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-      continue;
-    }
-    const float* yv = a.Y + (size_t)vs * T;
+    const float4* row4 = reinterpret_cast<const float4*>(row);
     // mean and (N-1) variance, two passes for accuracy
     float s = 0.f;
     for (int q = lane; q < nq; q += 32) {
-      float4 x;
-      if (vec) {
-        x = reinterpret_cast<const float4*>(yv)[q];
-      } else {
-        const int t = 4 * q;
-        x.x = t < T ? yv[t] : 0.f;
-        x.y = t + 1 < T ? yv[t + 1] : 0.f;
-        x.z = t + 2 < T ? yv[t + 2] : 0.f;
-        x.w = t + 3 < T ? yv[t + 3] : 0.f;
-      }
-      row4[q] = x;
+      const float4 x = row4[q];
       s += ((x.x + x.y) + x.z) + x.w;
     }
     const float mean = warp_sum(s) / (float)T;
-    __syncwarp();
     float sq = 0.f;
     for (int t = lane; t < T; t += 32) {
       const float dlt = row[t] - mean;

@@ -38,6 +38,39 @@ __host__ __device__ inline int tile_ld(int T) {
   return ld;
 }
 
+// Copies the series rows[l] of Y ([V][T], l < 32; rows[l] < 0: a zero row)
+// into Ys[l][0 .. 4 nq) with asynchronous copies, all in flight at once (16
+// bytes each when T % 4 == 0, single samples otherwise; samples T .. 4 nq are
+// zero), then waits for them and ends with a barrier. rows is in shared
+// memory.
+__device__ __forceinline__ void tile_stage_rows(const float* __restrict__ Y, int T, int nq, const int* rows,
+                                                float* Ys, int ld) {
+  if ((T & 3) == 0) {
+    for (int idx = threadIdx.x; idx < TILE_V * nq; idx += blockDim.x) {
+      const int l = idx / nq, q = idx % nq;
+      const int v = rows[l];
+      const float* src = v >= 0 ? Y + (size_t)v * T + 4 * q : Y;
+      const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(Ys + (size_t)l * ld + 4 * q));
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(v >= 0 ? 16 : 0)
+                   : "memory");
+    }
+  } else {
+    const int n4 = 4 * nq;
+    for (int idx = threadIdx.x; idx < TILE_V * n4; idx += blockDim.x) {
+      const int l = idx / n4, t = idx % n4;
+      const int v = rows[l];
+      const bool in = v >= 0 && t < T;
+      const float* src = in ? Y + (size_t)v * T + t : Y;
+      const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(Ys + (size_t)l * ld + t));
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(in ? 4 : 0)
+                   : "memory");
+    }
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  __syncthreads();
+}
+
 // C[j][l] = sum_t M[j][t] Ys[l][t] for j < K, l < 32 with KB columns per
 // thread and pass. Thread layout: s = lane & 15 is the time slice (quads
 // q = s, s + 16, ...), unit u = 2 * warp + (lane >> 4) is voxel group
