@@ -254,8 +254,12 @@ __global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, Gls
 // the tiles of pair g and blocks past the last tile exit. T % 4 == 0.
 //
 // The tile's 32 series sit in shared memory, one voxel per lane (tile.cuh):
-//   b0 = G'y and r = y - X b0, then d = G'r and r -= X d (b = b0 + d) as
-//   register-blocked passes; the whitened residual L^-1 r by 8 segments of
+//   b0 = G'y and r = y - X b0, then the refinement d = G'r (b = b0 + d) as
+//   register-blocked passes. The residual statistics use r: the refined
+//   residual r - X d differs from it by X d, which changes the whitened
+//   residual sum of squares only to second order (L^-1 r is orthogonal to
+//   L^-1 X up to d), so the update is not formed. The whitened residual
+//   L^-1 r is computed by 8 segments of
 //   the time axis (one per warp): each warp runs v_t = z_t - m_t v_{t-1} from
 //   v = 0 over its segment, the true state entering segment k is carried
 //   across the segment ends, and each sample adds its term prod(-m) * v_in.
@@ -373,9 +377,8 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
   }
   tile_subtract(Xt, LT, C0, Ys, ld, K);
   __syncthreads();
-  // d = G'r; r -= X d; SS_res and the unwhitened outputs
+  // the refinement d = G'r; SS_res and the unwhitened outputs
   tile_project(Gg, LT, Ys, ld, K, C1);
-  tile_subtract(Xt, LT, C1, Ys, ld, K);
 #pragma unroll
   for (int i = 0; i < TILE_SUB_VB; ++i) {
     const int l = TILE_SUB_VB * wid + i;

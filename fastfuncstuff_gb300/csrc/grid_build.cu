@@ -26,7 +26,7 @@ namespace ffsk {
 
 namespace {
 
-constexpr int GB_PF = 8;  // samples loaded ahead in the sequential recursions
+constexpr int GB_PF = 4;  // samples loaded ahead in the sequential recursions
 
 struct PairScratch {
   double* cm;  // [T][4]  c, m, D, 1/sqrt(D)
@@ -147,7 +147,8 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
     // sqrt, log and the reciprocals of every sample in parallel
     for (int r = threadIdx.x; r < d.n_runs; r += blockDim.x) {
       const int t0 = d.run_start[r], t1 = d.run_start[r + 1];
-      double Dprev = 1.0;
+      double Dprev = 1.0, mprev = 0.0;
+      int prev_gap = 0;
       for (int t = t0; t < t1; ++t) {
         double c = 0.0, m = 0.0, D = 1.0;
         // lambda == 0: every lag correlation is zero, R = I exactly
@@ -158,13 +159,29 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
             c = a;
             rho = lam;
           } else {
-            c = pow(a, (double)gap);
-            rho = lam * pow(a, (double)(gap - 1));
+            // a^gap and a^(gap - 1) of small integer gaps by products
+            double ag1 = 1.0;
+            if (gap <= 16) {
+              for (int k = 1; k < gap; ++k) ag1 *= a;
+            } else {
+              ag1 = pow(a, (double)(gap - 1));
+            }
+            c = ag1 * a;
+            rho = lam * ag1;
           }
           const double Ttt = 1.0 + c * c - 2.0 * c * rho;
           const double Toff = rho - c;
-          m = Toff / Dprev;
-          D = Ttt - m * Toff;
+          if (gap == 1 && prev_gap == 1 && Dprev == cms[4 * (t - 1) - 4 + 2]) {
+            // the previous step left D unchanged: the recursion has reached
+            // its fixed point, and every step of this stretch of unit gaps
+            // repeats it
+            m = mprev;
+            D = Dprev;
+          } else {
+            m = Toff / Dprev;
+            D = Ttt - m * Toff;
+          }
+          prev_gap = gap;
         }
         if (!(D > 0.0)) {
           bad_r = 1;
@@ -173,6 +190,7 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
         double* cm = cms + 4 * t;
         cm[0] = c; cm[1] = m; cm[2] = D;
         Dprev = D;
+        mprev = m;
       }
     }
     __syncthreads();
@@ -225,17 +243,7 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
       const double* xi = s.Xw + (size_t)i * T;
       const double* xj = s.Xw + (size_t)j * T;
       double acc = 0.0;
-      for (int t0 = 0; t0 < T; t0 += GB_PF) {  // GB_PF samples of both columns in flight
-        double ai[GB_PF], aj[GB_PF];
-#pragma unroll
-        for (int k = 0; k < GB_PF; ++k) {
-          ai[k] = t0 + k < T ? xi[t0 + k] : 0.0;
-          aj[k] = t0 + k < T ? xj[t0 + k] : 0.0;
-        }
-#pragma unroll
-        for (int k = 0; k < GB_PF; ++k)
-          if (t0 + k < T) acc += ai[k] * aj[k];
-      }
+      for (int t = 0; t < T; ++t) acc += xi[t] * xj[t];
       s.Lx[i * K + j] = acc;
       s.Lx[j * K + i] = acc;
       o.XtX[(size_t)pd * K * K + i * K + j] = (float)acc;
@@ -372,14 +380,14 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
     }
     __syncthreads();
 
-    // ---- 7. Lx^-1, A = Lx^-T Lx^-1, diag(A)
+    // ---- 7. Lx^-1 and diag(A), A = Lx^-T Lx^-1 = (X_w'X_w)^-1 (only the
+    // entries the statistics read are formed: the diagonal here, the task
+    // block and c A c' in phase 9)
     block_tri_inverse(s.Lx, s.Li, K, K);
-    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
-      const int i = idx / K, j = idx % K;
+    for (int j = threadIdx.x; j < K; j += blockDim.x) {
       double acc = 0.0;
-      for (int k = max(i, j); k < K; ++k) acc += s.Li[k * K + i] * s.Li[k * K + j];
-      s.A[i * K + j] = acc;
-      if (i == j) o.Adiag[(size_t)pd * K + j] = (float)acc;
+      for (int k = j; k < K; ++k) acc += s.Li[k * K + j] * s.Li[k * K + j];
+      o.Adiag[(size_t)pd * K + j] = (float)acc;
     }
     __syncthreads();
 
@@ -407,30 +415,36 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
 
     // ---- 9. task-column F matrix inv(A_task + 1e-8 I) and GLT variances c A c'
     const int nt = d.n_task;
-    if (nt > 0 && o.Ftask) {
-      for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
-        const int i = idx / nt, j = idx % nt;
-        s.S[i * nt + j] = s.A[d.task_idx[i] * K + d.task_idx[j]] + (i == j ? 1e-8 : 0.0);
-      }
-      __syncthreads();
-      block_cholesky(s.S, nt, nt, &flag);
-      // Li (free now) holds the inverse factor; Ftask = Li' Li
-      block_tri_inverse(s.S, s.Li, nt, nt);
-      for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
-        const int i = idx / nt, j = idx % nt;
-        double acc = 0.0;
-        for (int k = max(i, j); k < nt; ++k) acc += s.Li[k * nt + i] * s.Li[k * nt + j];
-        o.Ftask[(size_t)pd * nt * nt + idx] = (float)acc;
-      }
-    }
-    if (d.n_glt > 0 && o.glt_var) {
+    if (d.n_glt > 0 && o.glt_var) {  // c A c' = ||Lx^-1 c||^2
       for (int c = 0; c < d.n_glt; ++c) {
         const float* gc = d.glt + (size_t)c * K;
         double part = 0.0;
-        for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x)
-          part += (double)gc[idx / K] * s.A[idx] * (double)gc[idx % K];
+        for (int k = threadIdx.x; k < K; k += blockDim.x) {
+          double w = 0.0;
+          for (int j = 0; j <= k; ++j) w += s.Li[k * K + j] * (double)gc[j];
+          part += w * w;
+        }
         const double v = block_sum(part, red);
         if (threadIdx.x == 0) o.glt_var[(size_t)pd * d.n_glt + c] = (float)v;
+      }
+    }
+    if (nt > 0 && o.Ftask) {
+      for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
+        const int i = idx / nt, j = idx % nt;
+        const int ti = d.task_idx[i], tj = d.task_idx[j];
+        double acc = 0.0;
+        for (int k = max(ti, tj); k < K; ++k) acc += s.Li[k * K + ti] * s.Li[k * K + tj];
+        s.S[i * nt + j] = acc + (i == j ? 1e-8 : 0.0);
+      }
+      __syncthreads();
+      block_cholesky(s.S, nt, nt, &flag);
+      // the inverse factor goes to the A slot; Ftask = Li' Li
+      block_tri_inverse(s.S, s.A, nt, nt);
+      for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
+        const int i = idx / nt, j = idx % nt;
+        double acc = 0.0;
+        for (int k = max(i, j); k < nt; ++k) acc += s.A[k * nt + i] * s.A[k * nt + j];
+        o.Ftask[(size_t)pd * nt * nt + idx] = (float)acc;
       }
     }
     __syncthreads();  // the next item reuses the scratch slot and the shared state
