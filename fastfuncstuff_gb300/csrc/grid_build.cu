@@ -455,13 +455,19 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
 // Cholesky factor of X'X (Q0 is U of the pair (0, 0), R = I); modified
 // Gram-Schmidt, twice, when X'X is not positive definite. One CTA. work:
 // [K][K] + [K][T] doubles.
-__global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const float* X, double* work, float* Q0,
-                                                           int* info) {
+__global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const float* Xg, double* work, float* Q0,
+                                                           int* info, int staged) {
   __shared__ double red[32];
   __shared__ int flag;
+  extern __shared__ float xs[];  // [T][K] copy of X when staged
   const int LT = ld_t(T);
   for (int idx = threadIdx.x; idx < K * (LT - T); idx += blockDim.x)
     Q0[(size_t)(idx / (LT - T)) * LT + T + idx % (LT - T)] = 0.f;
+  if (staged) {
+    for (int idx = threadIdx.x; idx < T * K; idx += blockDim.x) xs[idx] = Xg[idx];
+    __syncthreads();
+  }
+  const float* X = staged ? xs : Xg;
   double* M = work;                    // [K][K]
   double* Qd = work + (size_t)K * K;   // [K][T] (QR fallback)
   for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
@@ -525,7 +531,12 @@ extern "C" int ffs_design_basis(int T, int K, const float* X, void* work, float*
   clear_error();
   FFS_REQUIRE(T > 0 && K > 0 && K <= T, "ffs_design_basis: T=%d K=%d", T, K);
   FFS_REQUIRE(X && work && Q0 && info, "ffs_design_basis: null buffer");
-  design_basis_kernel<<<1, 256, 0, (cudaStream_t)stream>>>(T, K, X, static_cast<double*>(work), Q0, info);
+  // X staged in shared memory (the K (K + 1) / 2 dot products read it T times)
+  const size_t xs = sizeof(float) * (size_t)T * K;
+  const int staged = xs <= 96 * 1024;
+  if (staged) FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(design_basis_kernel), xs));
+  design_basis_kernel<<<1, 256, staged ? xs : 0, (cudaStream_t)stream>>>(T, K, X, static_cast<double*>(work), Q0,
+                                                                          info, staged);
   return check_launch("design_basis_kernel");
 }
 

@@ -21,6 +21,7 @@ import ctypes as C
 import io
 import json
 import time
+import types
 from dataclasses import dataclass, field
 from pathlib import Path
 
@@ -456,6 +457,7 @@ class LearnedFitGraph:
         self.host = torch.empty(3 + recenter, dtype=torch.int32, pin_memory=True)
         self.side = torch.cuda.Stream(self.Y.device)  # the grid build runs beside the prep chain
         self.side_fb = torch.cuda.Stream(self.Y.device)  # the fallback runs beside graph B
+        self._fb_graphs: dict = {}
         # one eager pass fills the host-side caches (device constants, tensor
         # maps, kernel attributes) that a capture must not create
         self._body_a()
@@ -502,36 +504,81 @@ class LearnedFitGraph:
         ready.record()
         self.gb.replay()
         ready.synchronize()
-        # the fallback voxels' full grid and GLS on a second stream, beside the
-        # GLS of graph B (both only read the graphs' buffers)
+        n_fb, code = int(self.host[0]), int(self.host[1])
+        if code != 0:
+            raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {code})")
+        if bool((self.host[2:] != 0).any()):
+            raise RuntimeError("ffs_reml_window_items: work list overflow")
+        # the fallback voxels' full grid and GLS: graph C (of a padded voxel
+        # count) on a second stream, beside the GLS of graph B (both only read
+        # the graphs' buffers)
         fs = self.side_fb
-        fs.wait_event(ready)
-        with torch.cuda.stream(fs):
-            lo = learned_fallback(self.Y, self.f, self.ws, self.host, do_scale=self.do_scale)
-            # the graphs' buffers are overwritten by the next run: hand out copies
-            lo.best, lo.best_crit, lo.scale = lo.best.clone(), lo.best_crit.clone(), lo.scale.clone()
-            lo.fallback, lo.proposal = lo.fallback.clone(), lo.proposal.clone()
-            sel = lo.fallback_idx
-            gs = None
-            if sel.numel():
-                gs = engine.gls(self.Y.index_select(0, sel), lo.scale.index_select(0, sel),
-                                lo.best.index_select(0, sel), self.f, self.X, **self.gls_kw)
-        done = torch.cuda.Event()
-        done.record(fs)
+        fc = self._fallback_graph(n_fb) if n_fb else None
+        if fc is not None:
+            fs.wait_event(ready)
+            with torch.cuda.stream(fs):
+                fc.graph.replay()
+            done = torch.cuda.Event()
+            done.record(fs)
+        V = self.Y.shape[0]
+        stats = dict(self.ws.stats)
+        if stats["edge_first"] is None:
+            stats["edge_first"] = n_fb / V
+        stats["fallback"] = n_fb / V
+        # the graphs' buffers are overwritten by the next run: hand out copies
+        lo = LearnedOut(best=self.ws.best.clone(), best_crit=self.ws.best_crit.clone(), scale=self.ws.scale.clone(),
+                        fallback=self.ws.fb.clone(), proposal=self.ws.proposal.clone(), stats=stats)
         go = engine.GlsOut(**{k: (None if v is None else v.clone()) for k, v in vars(self.go).items()
                               if not k.startswith("_")})
+        if fc is None:
+            lo.fallback_idx = torch.empty(0, dtype=torch.long, device=self.Y.device)
+            return lo, go
         main.wait_event(done)
-        used = [lo.best, lo.best_crit, lo.scale, lo.fallback, lo.proposal, sel]
-        if gs is not None:
-            for fld in ("betas", "tstats", "sigma2", "fstats", "r2", "lam", "cbeta", "ct", "resid", "resid_w",
-                        "pred", "ljung_box"):
-                t_all, t_sub = getattr(go, fld), getattr(gs, fld)
-                if t_all is not None:
-                    t_all.index_copy_(0, sel, t_sub)
-                    used.append(t_sub)
-        for t in used:  # made on the fallback stream, read on this one
-            t.record_stream(main)
+        sel = fc.sel[:n_fb]
+        lo.fallback_idx = sel.clone()
+        lo.best.index_copy_(0, sel, fc.so.best[:n_fb])
+        lo.best_crit.index_copy_(0, sel, fc.so.best_crit[:n_fb])
+        for fld in ("betas", "tstats", "sigma2", "fstats", "r2", "lam", "cbeta", "ct", "resid", "resid_w", "pred",
+                    "ljung_box"):
+            t_all, t_sub = getattr(go, fld), getattr(fc.gs, fld)
+            if t_all is not None:
+                t_all.index_copy_(0, sel, t_sub[:n_fb])
         return lo, go
+
+    def _fallback_graph(self, n_fb: int):
+        """Graph C: the full-grid search and GLS of up to n_pad >= n_fb
+        fallback voxels (their ids compacted on the device from the window
+        rounds' flags; rows past the real count repeat voxel 0 and are
+        ignored), captured once per padded count."""
+        n_pad = (n_fb + 1023) // 1024 * 1024
+        fc = self._fb_graphs.get(n_pad)
+        if fc is not None:
+            return fc
+        while len(self._fb_graphs) >= 3:
+            self._fb_graphs.pop(next(iter(self._fb_graphs)))
+        dev = self.Y.device
+        fc = types.SimpleNamespace(sel=torch.zeros(n_pad + 1, dtype=torch.long, device=dev),
+                                   ids=torch.arange(self.Y.shape[0], device=dev))
+
+        def body():
+            fb = self.ws.fb
+            pos = torch.where(fb != 0, torch.cumsum(fb, 0) - 1, torch.full_like(fb, n_pad)).long()
+            fc.sel.zero_()
+            fc.sel.scatter_(0, pos.clamp_(max=n_pad), fc.ids)
+            sel = fc.sel[:n_pad]
+            Yf = self.Y.index_select(0, sel)
+            fc.so = engine.search(Yf, self.f, hierarchical=False, projector="tc", do_scale=self.do_scale)
+            fc.gs = engine.gls(Yf, fc.so.scale, fc.so.best, self.f, self.X, **self.gls_kw)
+
+        with torch.cuda.stream(self.side_fb):
+            body()  # fills the host-side caches a capture must not create
+        self.side_fb.synchronize()
+        fc.graph = torch.cuda.CUDAGraph()
+        # its own memory pool: graph C runs concurrently with graph B
+        with torch.cuda.graph(fc.graph, capture_error_mode="thread_local"):
+            body()
+        self._fb_graphs[n_pad] = fc
+        return fc
 
 
 _GRAPHS: dict = {}

@@ -259,11 +259,14 @@ def test_window_round_matches_full_grid_surface():
 
 
 @pytest.mark.gpu
-def test_fit_with_proposal_matches_full_grid_fit_where_pairs_agree():
+@pytest.mark.parametrize("cuda_graphs", [True, False])
+def test_fit_with_proposal_matches_full_grid_fit_where_pairs_agree(cuda_graphs):
     """fit_glm_arma11(proposal=...) queues the GLS of every voxel at its window
     pair, then redoes the fallback voxels at their full-grid pair: wherever the
     pair agrees with the full-grid fit the GLS outputs are identical (same
-    kernels, same inputs), fallback voxels included."""
+    kernels, same inputs), fallback voxels included. With CUDA graphs the
+    fallback voxels' search and GLS replay from a graph of a padded voxel
+    count beside the GLS graph; without, they run eagerly."""
     from fastfuncstuff_gb300 import fit_glm_arma11, synth
     from fastfuncstuff_gb300.glm import learned
     from fastfuncstuff_gb300.glm import grid as G
@@ -278,7 +281,9 @@ def test_fit_with_proposal_matches_full_grid_fit_where_pairs_agree():
     kw = dict(tr=2.0, a_grid=gr, b_grid=gr, run_starts=w.run_starts, device=dev, verbose=False,
               force_exhaustive_search=True, return_device=True, want_residuals=True)
     full = fit_glm_arma11(Y, X, **kw)
-    got = fit_glm_arma11(Y, X, proposal=prop, proposal_recenter=1, **kw)
+    got = fit_glm_arma11(Y, X, proposal=prop, proposal_recenter=1, cuda_graphs=cuda_graphs, **kw)
+    again = fit_glm_arma11(Y, X, proposal=prop, proposal_recenter=1, cuda_graphs=cuda_graphs, **kw)
+    assert torch.equal(got.betas, again.betas)  # a replay gives the same results
     same = (got.arma_params == full.arma_params).all(1)
     assert float(same.float().mean()) >= 0.97
     assert 0.0 < float(got.learned_fallback) < 0.5  # some voxels took the fallback path
