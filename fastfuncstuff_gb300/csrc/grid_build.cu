@@ -456,39 +456,90 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
 // Gram-Schmidt, twice, when X'X is not positive definite. One CTA. work:
 // [K][K] + [K][T] doubles.
 __global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const float* Xg, double* work, float* Q0,
-                                                           int* info, int staged) {
+                                                           int* info, int staged, int* const_flag, float* const_coef) {
   __shared__ double red[32];
   __shared__ int flag;
-  extern __shared__ float xs[];  // [T][K] copy of X when staged
+  extern __shared__ double xd[];  // staged: [T][K] X in FP64, then [T][K] X in fp32, then [K][K] Lx in fp32
   const int LT = ld_t(T);
   for (int idx = threadIdx.x; idx < K * (LT - T); idx += blockDim.x)
     Q0[(size_t)(idx / (LT - T)) * LT + T + idx % (LT - T)] = 0.f;
+  float* xs = reinterpret_cast<float*>(xd + (size_t)T * K);
+  float* mf = xs + (size_t)T * K;
   if (staged) {
-    for (int idx = threadIdx.x; idx < T * K; idx += blockDim.x) xs[idx] = Xg[idx];
+    for (int idx = threadIdx.x; idx < T * K; idx += blockDim.x) {
+      const float x = Xg[idx];
+      xs[idx] = x;
+      xd[idx] = (double)x;
+    }
     __syncthreads();
   }
   const float* X = staged ? xs : Xg;
+  auto xdbl = [&](size_t idx) { return staged ? xd[idx] : (double)Xg[idx]; };
   double* M = work;                    // [K][K]
   double* Qd = work + (size_t)K * K;   // [K][T] (QR fallback)
   for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
     const int i = idx / K, j = idx % K;
     if (j > i) continue;
     double acc = 0.0;
-    for (int t = 0; t < T; ++t) acc += (double)X[(size_t)t * K + i] * (double)X[(size_t)t * K + j];
+    for (int t = 0; t < T; ++t) acc += xdbl((size_t)t * K + i) * xdbl((size_t)t * K + j);
     M[i * K + j] = acc;
     M[j * K + i] = acc;
   }
   __syncthreads();
   if (block_cholesky(M, K, K, &flag)) {
+    const float* Mq = mf;
+    if (staged) {
+      for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) mf[idx] = (float)M[idx];
+      __syncthreads();
+    }
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
       for (int j = 0; j < K; ++j) {
         float acc = X[(size_t)t * K + j];
-        for (int i = 0; i < j; ++i) acc = fmaf(-(float)M[j * K + i], Q0[(size_t)i * LT + t], acc);
-        Q0[(size_t)j * LT + t] = acc / (float)M[j * K + j];
+        for (int i = 0; i < j; ++i)
+          acc = fmaf(-(staged ? Mq[j * K + i] : (float)M[j * K + i]), Q0[(size_t)i * LT + t], acc);
+        Q0[(size_t)j * LT + t] = acc / (staged ? Mq[j * K + j] : (float)M[j * K + j]);
       }
+    }
+    if (const_flag) {
+      // the constant series in span(X): c = (X'X)^-1 X'1 from the same FP64
+      // factor, accepted when ||X c - 1|| <= 1e-6 sqrt(T)
+      double* cv = Qd;  // [K] X'1, then c
+      for (int j = threadIdx.x; j < K; j += blockDim.x) {
+        double b = 0.0;
+        for (int t = 0; t < T; ++t) b += xdbl((size_t)t * K + j);
+        cv[j] = b;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        for (int j = 0; j < K; ++j) {  // L y = b
+          double v = cv[j];
+          for (int i = 0; i < j; ++i) v -= M[j * K + i] * cv[i];
+          cv[j] = v / M[j * K + j];
+        }
+        for (int j = K - 1; j >= 0; --j) {  // L' c = y
+          double v = cv[j];
+          for (int i = j + 1; i < K; ++i) v -= M[i * K + j] * cv[i];
+          cv[j] = v / M[j * K + j];
+        }
+      }
+      __syncthreads();
+      double part = 0.0;
+      for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        double r = -1.0;
+        for (int j = 0; j < K; ++j) r += xdbl((size_t)t * K + j) * cv[j];
+        part += r * r;
+      }
+      const double ss = block_sum(part, red);
+      const bool ok = ss <= 1e-12 * (double)T;
+      for (int j = threadIdx.x; j < K; j += blockDim.x) const_coef[j] = ok ? (float)cv[j] : 0.f;
+      if (threadIdx.x == 0) *const_flag = ok ? 1 : 0;
     }
     if (threadIdx.x == 0) *info = 0;
     return;
+  }
+  if (const_flag) {  // X'X not positive definite: no centring
+    for (int j = threadIdx.x; j < K; j += blockDim.x) const_coef[j] = 0.f;
+    if (threadIdx.x == 0) *const_flag = 0;
   }
   // QR of X by modified Gram-Schmidt (twice) in FP64
   for (int j = 0; j < K; ++j) {
@@ -526,17 +577,20 @@ extern "C" size_t ffs_design_basis_work_bytes(int T, int K) {
   return sizeof(double) * ((size_t)K * K + (size_t)K * T);
 }
 
-extern "C" int ffs_design_basis(int T, int K, const float* X, void* work, float* Q0, int* info, void* stream) {
+extern "C" int ffs_design_basis(int T, int K, const float* X, void* work, float* Q0, int* info, int* const_flag,
+                                float* const_coef, void* stream) {
   using namespace ffsk;
   clear_error();
   FFS_REQUIRE(T > 0 && K > 0 && K <= T, "ffs_design_basis: T=%d K=%d", T, K);
   FFS_REQUIRE(X && work && Q0 && info, "ffs_design_basis: null buffer");
-  // X staged in shared memory (the K (K + 1) / 2 dot products read it T times)
-  const size_t xs = sizeof(float) * (size_t)T * K;
-  const int staged = xs <= 96 * 1024;
+  FFS_REQUIRE(!const_flag == !const_coef, "ffs_design_basis: const_flag and const_coef go together");
+  // X staged in shared memory in FP64 and fp32 (the K (K + 1) / 2 dot
+  // products read it T times), with the fp32 factor
+  const size_t xs = (sizeof(double) + sizeof(float)) * (size_t)T * K + sizeof(float) * (size_t)K * K;
+  const int staged = xs <= 160 * 1024;
   if (staged) FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(design_basis_kernel), xs));
   design_basis_kernel<<<1, 256, staged ? xs : 0, (cudaStream_t)stream>>>(T, K, X, static_cast<double*>(work), Q0,
-                                                                          info, staged);
+                                                                          info, staged, const_flag, const_coef);
   return check_launch("design_basis_kernel");
 }
 

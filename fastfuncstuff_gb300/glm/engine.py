@@ -318,9 +318,12 @@ class PrepOut:
 BASIS_MAX_K = 32
 
 
-def design_basis(X: torch.Tensor) -> torch.Tensor:
+def design_basis(X: torch.Tensor, with_constant: bool = False):
     """Q0 [K][ld_t(T)]: the orthonormal basis of the design's columns (FP64 Cholesky),
-    from X alone, so the residualisation need not wait for the grid build."""
+    from X alone, so the residualisation need not wait for the grid build.
+
+    ``with_constant`` also returns the centring test of ``constant_flag``
+    (flag int32[1], c float32[K]) from the same kernel: (q0, flag, c)."""
     lib = _lib.load()
     dev = X.device
     T, K = X.shape
@@ -328,9 +331,12 @@ def design_basis(X: torch.Tensor) -> torch.Tensor:
     work = torch.empty(int(lib.ffs_design_basis_work_bytes(T, K)) // 8 + 1, dtype=torch.float64, device=dev)
     q0 = torch.empty(K, ld_t(T), dtype=torch.float32, device=dev)
     info = torch.empty(1, dtype=torch.int32, device=dev)
-    _run("ffs_design_basis", lib.ffs_design_basis, T, K, _p(Xc), _p(work), _p(q0), _p(info), _stream())
+    flag = torch.empty(1, dtype=torch.int32, device=dev) if with_constant else None
+    coef = torch.empty(K, dtype=torch.float32, device=dev) if with_constant else None
+    _run("ffs_design_basis", lib.ffs_design_basis, T, K, _p(Xc), _p(work), _p(q0), _p(info), _p(flag), _p(coef),
+         _stream())
     q0._keep = (Xc, work, info)
-    return q0
+    return (q0, flag, coef) if with_constant else q0
 
 
 def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core: bool = True,

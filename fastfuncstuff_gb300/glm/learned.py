@@ -473,13 +473,18 @@ class LearnedFitGraph:
     def _body_a(self):
         main = torch.cuda.current_stream()
         overlap = self.X.shape[1] <= engine.BASIS_MAX_K
-        self.f = engine.build_factors(self.X, self.grid, self.layout, center=(self.cflag, self.ccoef),
-                                      stream=self.side if overlap else None, **self.factor_kw)
         q0 = join = None
+        center = (self.cflag, self.ccoef)
+        if overlap:
+            # the design basis and the centring test first (one kernel), then
+            # the grid build on the side stream beside the prep chain
+            q0, cflag, ccoef = engine.design_basis(self.X, with_constant=True)
+            center = (cflag, ccoef)
+        self.f = engine.build_factors(self.X, self.grid, self.layout, center=center,
+                                      stream=self.side if overlap else None, **self.factor_kw)
         if overlap:
             built = torch.cuda.Event()
             built.record(self.side)
-            q0 = engine.design_basis(self.X)
 
             def join():
                 main.wait_event(built)
@@ -496,9 +501,10 @@ class LearnedFitGraph:
         main = torch.cuda.current_stream()
         self.Y.copy_(Y)
         self.X.copy_(X)
-        flag, coef = engine.constant_flag(self.X)
-        self.cflag.copy_(flag)
-        self.ccoef.copy_(coef)
+        if self.X.shape[1] > engine.BASIS_MAX_K:  # else graph A runs the centring test
+            flag, coef = engine.constant_flag(self.X)
+            self.cflag.copy_(flag)
+            self.ccoef.copy_(coef)
         self.ga.replay()
         ready = torch.cuda.Event()
         ready.record()

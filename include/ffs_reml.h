@@ -151,9 +151,14 @@ int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out* o, void* 
  * ffs_grid_build also writes). Q0 = X Lx^-T with Lx the FP64 Cholesky factor of
  * X'X, or modified Gram-Schmidt (twice) when X'X is not positive definite
  * (*info = 1). Needing only X, it lets the residualisation (ffs_reml_prep) run
- * while the grid build is still in flight. work: ffs_design_basis_work_bytes. */
+ * while the grid build is still in flight. work: ffs_design_basis_work_bytes.
+ * With const_flag / const_coef (both or neither) it also decides whether the
+ * constant series lies in span(X): c = (X'X)^-1 X'1 from the same FP64
+ * factor, *const_flag = 1 and const_coef[K] = c when ||X c - 1|| <= 1e-6
+ * sqrt(T), else 0 and zeros (the centring test of ffs_reml_prep and the GLS). */
 size_t ffs_design_basis_work_bytes(int T, int K);
-int ffs_design_basis(int T, int K, const float* X, void* work, float* Q0, int* info, void* stream);
+int ffs_design_basis(int T, int K, const float* X, void* work, float* Q0, int* info, int* const_flag,
+                     float* const_coef, void* stream);
 
 /* ---------------------------------------------------------------- search data
  * Replaces the per-voxel scaling of fastfuncstuff/glm/arma.py:3952-3954,

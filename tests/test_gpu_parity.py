@@ -243,6 +243,34 @@ def test_grouped_matches_reference():
     assert rel_maxnorm(got.betas.numpy()[same], d["f64_exh__betas"][same]).max() <= BETA_REL
 
 
+def test_design_basis_centring_test_matches_normal_equations():
+    """The design-basis kernel's centring test (FP64 Cholesky of X'X, c with
+    X c = 1) agrees with the torch FP64 normal equations: constant in the span
+    (intercept; per-run drift), not in the span, and a rank-deficient X'X."""
+    rng = np.random.default_rng(7)
+    T = 200
+    t = np.linspace(-1, 1, T)
+    cases = {
+        "intercept": np.column_stack([rng.standard_normal((T, 3)), np.ones(T)]),
+        "runs": np.column_stack([rng.standard_normal(T), (np.arange(T) < 90), (np.arange(T) >= 90), t]),
+        "no_constant": np.column_stack([rng.standard_normal((T, 3)), t]),
+        "rank_deficient": np.column_stack([t, 2 * t, t**2]),  # no constant, X'X singular
+    }
+    for name, X in cases.items():
+        Xd = torch.from_numpy(X.astype(np.float32)).to(DEV)
+        q0, flag, coef = engine.design_basis(Xd, with_constant=True)
+        ref_flag, ref_coef = engine.constant_flag(Xd)
+        torch.cuda.synchronize()
+        assert int(flag[0]) == int(ref_flag[0]), name
+        np.testing.assert_allclose(coef.cpu().numpy(), ref_coef.cpu().numpy(), rtol=1e-5, atol=1e-6, err_msg=name)
+        if int(flag[0]):
+            np.testing.assert_allclose(X @ coef.cpu().numpy().astype(np.float64), np.ones(T), atol=1e-5)
+        # Q0 spans the design's columns, orthonormal (full-rank cases)
+        if name != "rank_deficient":
+            Q = q0[:, :T].cpu().numpy().astype(np.float64).T
+            np.testing.assert_allclose(Q.T @ Q, np.eye(Q.shape[1]), atol=1e-5)
+
+
 @pytest.mark.parametrize("selector", ["hierarchical", "exhaustive"])
 def test_grouped_batched_fit_equals_per_group_fits(selector):
     """The grouped fit runs every design in one pass per stage (one grid build
