@@ -565,6 +565,9 @@ class LearnedFitGraph:
         dev = self.Y.device
         fc = types.SimpleNamespace(sel=torch.zeros(n_pad + 1, dtype=torch.long, device=dev),
                                    ids=torch.arange(self.Y.shape[0], device=dev))
+        # the buffers above are filled on the current stream, behind graph B:
+        # the warm-up pass on the fallback stream must not start before them
+        torch.cuda.current_stream().synchronize()
 
         def body():
             fb = self.ws.fb
