@@ -27,6 +27,10 @@ namespace ffsk {
 namespace {
 
 constexpr int GB_PF = 4;  // samples loaded ahead in the sequential recursions
+// Threads per CTA (one (design, pair) item at a time); 128 measured no faster
+// at K = 20 and slower at K = 130, where the Gram matrix and the O(K^3)
+// phases use every thread.
+constexpr int GB_THREADS = 256;
 
 struct PairScratch {
   double* cm;  // [T][4]  c, m, D, 1/sqrt(D)
@@ -122,7 +126,7 @@ struct BuildArgs {
 // Design-dependent outputs sit at pd = design * P + pair; coef and logdet_R
 // depend on the pair only and are written (with identical values) by the
 // items of every design.
-__global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_designs) {
+__global__ void __launch_bounds__(GB_THREADS) grid_build_kernel(BuildArgs args, int n_designs) {
   const ffs_grid_desc& d = args.d;
   const ffs_grid_out& o = args.o;
   const int T = d.T, K = d.K, LT = ld_t(T);
@@ -178,7 +182,17 @@ __global__ void __launch_bounds__(256) grid_build_kernel(BuildArgs args, int n_d
             m = mprev;
             D = Dprev;
           } else {
-            m = Toff / Dprev;
+            // 1/D_{t-1}: fp32 estimate refined by two Newton steps r (2 - D r)
+            // (error ~2^-24 -> ~2^-48 -> below 2^-53), cheaper than a
+            // correctly rounded FP64 division in this serial chain
+            if (Dprev > 1e-30 && Dprev < 1e30) {
+              double r = (double)__frcp_rn((float)Dprev);
+              r = r * fma(-Dprev, r, 2.0);
+              r = r * fma(-Dprev, r, 2.0);
+              m = Toff * r;
+            } else {
+              m = Toff / Dprev;
+            }
             D = Ttt - m * Toff;
           }
           prev_gap = gap;
@@ -623,7 +637,7 @@ extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, voi
   const size_t smem = sizeof(double) * 4 * (size_t)d->T;
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build: T=%d too long", d->T);
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel), smem));
-  grid_build_kernel<<<d->P, 256, smem, (cudaStream_t)stream>>>(args, 1);
+  grid_build_kernel<<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, 1);
   return check_launch("grid_build_kernel");
 }
 
@@ -649,7 +663,7 @@ extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, con
   const size_t smem = sizeof(double) * 4 * (size_t)d->T;
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build_designs: T=%d too long", d->T);
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel), smem));
-  grid_build_kernel<<<grid, 256, smem, (cudaStream_t)stream>>>(args, n_designs);
+  grid_build_kernel<<<grid, GB_THREADS, smem, (cudaStream_t)stream>>>(args, n_designs);
   return check_launch("grid_build_kernel (designs)");
 }
 
@@ -732,6 +746,6 @@ extern "C" int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out
   const size_t smem = sizeof(double) * 4 * (size_t)d->T;
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build_noalloc: T=%d too long", d->T);
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel), smem));
-  grid_build_kernel<<<d->P, 256, smem, (cudaStream_t)stream>>>(args, 1);
+  grid_build_kernel<<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, 1);
   return check_launch("grid_build_kernel (static scratch)");
 }
