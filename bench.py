@@ -177,8 +177,27 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes per voxel of one launch (dram__bytes_read.sum + dram__bytes_write.sum)
+# from ncu --set full captures of the N=400, p=20, 561-pair workload at
+# 100k-217k voxels; traffic grows with the voxels, so a launch's traffic is this
+# times the voxels it processes. None for other shapes.
+NCU_DRAM_BYTES_PER_VOXEL = {
+    (400, 20, "ffs_reml_gls_grouped"): 1866.0,
+    (400, 20, "ffs_reml_surface"): 5524.0,
+}
+
+
 def roofline(dom: str, mean_ms: float, V: int, T: int, K: int, P: int, pk: dict, sm_mhz, extra: dict) -> dict:
     """Algorithmic work of the dominant kernel per launch against its bound."""
+    r = _roofline(dom, mean_ms, V, T, K, P, pk, sm_mhz, extra)
+    per_voxel = NCU_DRAM_BYTES_PER_VOXEL.get((T, K, dom)) if P == 561 else None
+    if per_voxel is not None:
+        r["traffic"] = per_voxel * V
+        r["traffic_unit"] = "bytes per launch (ncu DRAM read + write, scaled from a 100k-217k voxel capture)"
+    return r
+
+
+def _roofline(dom: str, mean_ms: float, V: int, T: int, K: int, P: int, pk: dict, sm_mhz, extra: dict) -> dict:
     sec = mean_ms / 1e3
     fp32_peak = 152 * 128 * 2 * (sm_mhz or 1900.0) * 1e6 / 1e12
     if dom in ("ffs_reml_project_tc", "ffs_reml_project_tc_list"):
@@ -197,11 +216,11 @@ def roofline(dom: str, mean_ms: float, V: int, T: int, K: int, P: int, pk: dict,
                 "frac": ach / fp32_peak, "traffic": None, "peak_src": "152 SMs x 128 FMA/clk at the sampled clock",
                 "work": "2 FMA per (voxel, pair, time point) of the O(T) recurrences"}
     if dom == "ffs_reml_gls_grouped":
-        flops = V * (4 * 2.0 * K * T + 6.0 * T)
+        flops = V * (3 * 2.0 * K * T + 6.0 * T)
         ach = flops / sec / 1e12
         return {"kernel": dom, "bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": ach / fp32_peak, "traffic": None, "peak_src": "152 SMs x 128 FMA/clk at the sampled clock",
-                "work": "G'y, X b, G'r, X d (4 K x T products) and the whitening recurrence per voxel"}
+                "work": "G'y, X b0 and G'r (3 K x T products) and the whitening recurrence per voxel"}
     if dom in ("ffs_grid_build", "ffs_grid_build_designs"):
         # FP64: the whitened design (2 T K) and its Gram matrix (T K (K + 1)) per (design, pair)
         items = P * extra.get("designs", 1)

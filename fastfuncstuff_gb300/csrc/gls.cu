@@ -266,6 +266,97 @@ __global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, Gls
 // The per-voxel statistics (gls_finish) then run one warp per voxel.
 constexpr int GLS_TILE = TILE_V;
 
+// gls_finish for the n <= 32 voxels of a tile at once (no Ljung-Box): b =
+// C0 + C1 (in C0) with the constant's betas added back, then t, F, R^2,
+// sigma2, lambda and the GLT contrasts, spread over the CTA's threads instead
+// of one warp per voxel. st holds m, sc, mean, ssr, sst, ssw per voxel; red
+// (>= 8 x 32 floats) is scratch. Ends with the outputs written.
+__device__ void gls_finish_tile(const ffs_gls_args& a, int g, int j0, int n, float* C0, const float* C1,
+                                const float* Ys, int ld, const float* st, float* red, const float* Mq) {
+  const int K = a.K, T = a.T, tid = threadIdx.x, nth = blockDim.x;
+  const bool centre = a.center_dev ? (*a.center_dev != 0) : (a.center != 0);
+  for (int idx = tid; idx < K * TILE_V; idx += nth) {
+    const int j = idx / TILE_V, l = idx % TILE_V;
+    float bj = C0[idx] + C1[idx];
+    // betas of the uncentred data: add (m/s) * G'1
+    if (centre) bj = fmaf(st[l] / st[TILE_V + l], a.Gsum[(size_t)g * K + j], bj);
+    C0[idx] = bj;
+  }
+  __syncthreads();
+  // betas and t statistics, voxel-major stores
+  for (int idx = tid; idx < n * K; idx += nth) {
+    const int l = idx / K, j = idx % K;
+    const int v = a.order[j0 + l];
+    const float sc = st[TILE_V + l], sigma2 = st[5 * TILE_V + l] / (float)a.dof;
+    const float bj = C0[j * TILE_V + l];
+    const float se = sqrtf(sigma2 * a.Adiag[(size_t)g * K + j]);
+    a.betas[(size_t)v * K + j] = bj * sc;
+    a.tstats[(size_t)v * K + j] = bj / (se + 1e-10f);
+  }
+  // whitened residual output
+  if (a.resid_w) {
+    for (int l = tid >> 5; l < n; l += nth >> 5) {
+      const int v = a.order[j0 + l];
+      const float sc = st[TILE_V + l];
+      for (int t = tid & 31; t < T; t += 32) a.resid_w[(size_t)v * T + t] = Ys[(size_t)l * ld + t] * sc;
+    }
+  }
+  // F: quad = b' M b over the model's (or the task) columns, 8 slices of the
+  // rows k summed in order
+  const int nk = a.n_task > 0 ? a.n_task : K;
+  {
+    const int l = tid & 31, ks = tid >> 5;
+    float part = 0.f;
+    if (l < n) {
+      for (int k = ks; k < nk; k += TILE_WARPS) {
+        const int ck = a.n_task > 0 ? a.task_idx[k] : k;
+        float s = 0.f;
+        for (int c = 0; c < nk; ++c) {
+          const int cl = a.n_task > 0 ? a.task_idx[c] : c;
+          s = fmaf(Mq[k * nk + c], C0[cl * TILE_V + l], s);
+        }
+        part = fmaf(C0[ck * TILE_V + l], s, part);
+      }
+    }
+    red[ks * TILE_V + l] = part;
+  }
+  // GLT contrasts c'b and their t
+  for (int idx = tid; idx < n * a.n_glt; idx += nth) {
+    const int l = idx / a.n_glt, c = idx % a.n_glt;
+    const int v = a.order[j0 + l];
+    const float* gc = a.glt + (size_t)c * K;
+    float cb = 0.f;
+    for (int j = 0; j < K; ++j) cb = fmaf(gc[j], C0[j * TILE_V + l], cb);
+    const float sigma2 = st[5 * TILE_V + l] / (float)a.dof;
+    const float var = a.glt_var[(size_t)g * a.n_glt + c] * sigma2;
+    a.cbeta[(size_t)v * a.n_glt + c] = cb * st[TILE_V + l];
+    a.ct[(size_t)v * a.n_glt + c] = cb / (sqrtf(fmaxf(var, 0.f)) + 1e-10f);
+  }
+  __syncthreads();
+  if (tid < n) {
+    const int l = tid;
+    const int v = a.order[j0 + l];
+    float quad = 0.f;
+    for (int w = 0; w < TILE_WARPS; ++w) quad += red[w * TILE_V + l];
+    const float sc = st[TILE_V + l], ssr = st[3 * TILE_V + l], sst = st[4 * TILE_V + l];
+    const float sigma2 = st[5 * TILE_V + l] / (float)a.dof;
+    const float q = a.n_task > 0 ? (float)a.n_task : (float)K;
+    a.fstats[v] = quad / (sigma2 * q + 1e-10f);
+    a.sigma2[v] = sigma2 * sc * sc;
+    const bool deg = sst <= 1e-10f;
+    const float r2 = 1.0f - ssr / fmaxf(sst, 1e-10f);
+    a.r2[v] = deg ? 0.f : fminf(r2, 1.0f);
+    const int p = pair_of(a, g);
+    const float af = a.a[p], bf = a.b[p];
+    if (a.lambda_fp32) {
+      a.lam[v] = lambda_out_f32(af, bf);
+    } else {
+      const double ad = af, bd = bf;
+      a.lam[v] = (float)((bd + ad) * (1.0 + ad * bd) / (1.0 + 2.0 * ad * bd + bd * bd + 1e-10));
+    }
+  }
+}
+
 __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_args a, GlsExtra x, const int* end,
                                                                    const int* tile_start, int P, int ld, int kp,
                                                                    int hb, int msz) {
@@ -499,16 +590,20 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
   }
   __syncthreads();
 
-  // per-voxel statistics: warp w takes voxels w, w + 8, ...
-  float* b = betas + (size_t)wid * kp;
-  for (int i = wid; i < n; i += TILE_WARPS) {
-    const int v = a.order[j0 + i];
-    for (int j = lane; j < K; j += 32) b[j] = C0[j * TILE_V + i] + C1[j * TILE_V + i];
-    __syncwarp();
-    gls_finish(a, x, v, g, b, Ys + (size_t)i * ld, st[3 * TILE_V + i], st[4 * TILE_V + i], st[5 * TILE_V + i],
-               st[i], st[TILE_V + i], bins + (size_t)wid * hb, Mq);
-    __syncwarp();
+  if (x.lj_h > 0 && x.ljung_box) {
+    // per-voxel statistics with the Ljung-Box lags: warp w takes voxels w, w + 8, ...
+    float* b = betas + (size_t)wid * kp;
+    for (int i = wid; i < n; i += TILE_WARPS) {
+      const int v = a.order[j0 + i];
+      for (int j = lane; j < K; j += 32) b[j] = C0[j * TILE_V + i] + C1[j * TILE_V + i];
+      __syncwarp();
+      gls_finish(a, x, v, g, b, Ys + (size_t)i * ld, st[3 * TILE_V + i], st[4 * TILE_V + i], st[5 * TILE_V + i],
+                 st[i], st[TILE_V + i], bins + (size_t)wid * hb, Mq);
+      __syncwarp();
+    }
+    return;
   }
+  gls_finish_tile(a, g, j0, n, C0, C1, Ys, ld, st, red, Mq);
 }
 
 // tile_start[g] = sum over g' < g of ceil(count[g'] / GLS_TILE)

@@ -103,7 +103,7 @@ struct CritArgs {
   const int* lattice;       // [n_a][n_b]
   const int* idx;           // [n] voxel of each sorted row
   const int* center;        // [n] cell of each sorted row
-  const float* yr_st;       // [T][n] sorted rows, time-major
+  const float* rows;        // [V][T] residualised rows, voxel-major (read at idx[i])
   const float4* coef;       // [P][T]
   const float* winproj;     // [n][25]
   const float* dcf;         // [P] (logdet_R + logdet_XtX)[p] - that of (0, 0)
@@ -146,7 +146,10 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
   int a0, wa, b0, wb;
   window_of(c, w.n_a, w.n_b, a0, wa, b0, wb);
   const int T = w.T, Tk = w.T - w.K;
-  const float* yc = w.yr_st + (live ? i : tl.x);
+  // this thread's residualised series, voxel-major: 16 samples per block as
+  // four 16-byte loads when T % 4 == 0
+  const float* yrow = w.rows + (size_t)w.idx[live ? i : tl.x] * w.T;
+  const bool vec = (w.T & 3) == 0;
 
   // identity pairs of the window (R = I: criterion d = 0)
   bool has_ident = false;
@@ -239,8 +242,20 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
     float yp = 0.f;
     for (int t0 = 0; t0 < T; t0 += CRIT_TB) {
       float yb[CRIT_TB];
+      if (vec) {
 #pragma unroll
-      for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yc[(size_t)(t0 + k) * w.n] : 0.f;
+        for (int k = 0; k < CRIT_TB; k += 4) {
+          const float4 q = t0 + k < T ? *reinterpret_cast<const float4*>(yrow + t0 + k)
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+          yb[k] = q.x;
+          yb[k + 1] = q.y;
+          yb[k + 2] = q.z;
+          yb[k + 3] = q.w;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yrow[t0 + k] : 0.f;
+      }
       if (first) {
         float yy_b = 0.f;
 #pragma unroll
@@ -453,7 +468,7 @@ extern "C" int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const i
                                uint16_t* out_lo, int* out_exp, float* out_t, void* stream) {
   clear_error();
   FFS_REQUIRE(n > 0 && T > 0 && ld_y >= T && ld_y % 8 == 0, "ffs_reml_gather: bad sizes");
-  FFS_REQUIRE(idx && yr_hi && yr_lo && yexp && yr_rows && out_hi && out_lo && out_exp && out_t,
+  FFS_REQUIRE(idx && yr_hi && yr_lo && yexp && out_hi && out_lo && out_exp && (!out_t || yr_rows),
               "ffs_reml_gather: null buffer");
   for (const void* ptr : {(const void*)yr_hi, (const void*)yr_lo, (const void*)out_hi, (const void*)out_lo})
     FFS_REQUIRE(((uintptr_t)ptr & 15) == 0, "ffs_reml_gather: fp16 rows must be 16-byte aligned");
@@ -462,9 +477,11 @@ extern "C" int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const i
                                                       reinterpret_cast<const uint4*>(yr_lo), yexp,
                                                       reinterpret_cast<uint4*>(out_hi),
                                                       reinterpret_cast<uint4*>(out_lo), out_exp);
-  FFS_REQUIRE(ceil_div(T, 64) <= 65535, "ffs_reml_gather: T=%d too long", T);
-  gather_transpose_kernel<<<dim3(ceil_div(n, 32), ceil_div(T, 64)), dim3(32, 8), 0, st>>>(n, n_dev, T, idx, yr_rows,
-                                                                                          out_t);
+  if (out_t) {
+    FFS_REQUIRE(ceil_div(T, 64) <= 65535, "ffs_reml_gather: T=%d too long", T);
+    gather_transpose_kernel<<<dim3(ceil_div(n, 32), ceil_div(T, 64)), dim3(32, 8), 0, st>>>(n, n_dev, T, idx,
+                                                                                            yr_rows, out_t);
+  }
   return check_launch("gather kernels");
 }
 
@@ -489,19 +506,20 @@ extern "C" int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, in
 
 extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx,
                                const int* center, const int* tiles, const int* n_tiles, int max_tiles,
-                               const float* yr_st, const float* coef, const float* winproj, const float* dcf,
+                               const float* rows, const float* coef, const float* winproj, const float* dcf,
                                const unsigned char* ident, int p_id, const double* c_p0, int* best, float* dbest,
                                double* crit0, int* fallback, int* best_cell, void* stream) {
   clear_error();
   FFS_REQUIRE(n > 0 && T > K && K > 0 && n_a > 0 && n_b > 0 && p_id >= 0 && max_tiles > 0,
               "ffs_reml_window: bad sizes");
-  FFS_REQUIRE(lattice && idx && center && tiles && n_tiles && yr_st && coef && winproj && dcf && ident && c_p0 &&
+  FFS_REQUIRE(lattice && idx && center && tiles && n_tiles && rows && coef && winproj && dcf && ident && c_p0 &&
                   best && dbest && crit0 && fallback && best_cell,
               "ffs_reml_window: null buffer");
   const size_t smem = CRIT_ROWS * ((sizeof(float2) * WIN + sizeof(float) + 1) * (size_t)T + ceil_div(T, CRIT_TB));
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_reml_window: T=%d too long", T);
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(window_crit_kernel), smem));
-  CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, yr_st, reinterpret_cast<const float4*>(coef), winproj, dcf,
+  FFS_REQUIRE(((uintptr_t)rows & 15) == 0, "ffs_reml_window: rows must be 16-byte aligned");
+  CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, rows, reinterpret_cast<const float4*>(coef), winproj, dcf,
              ident, p_id, c_p0, best, dbest, crit0, fallback, best_cell};
   window_crit_kernel<<<max_tiles, WTILE, smem, (cudaStream_t)stream>>>(w, reinterpret_cast<const int2*>(tiles),
                                                                         n_tiles);

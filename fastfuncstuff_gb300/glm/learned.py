@@ -260,9 +260,10 @@ def _window_round(pre, f, cen, out, *, flag, join=None):
     hi = torch.empty(n, ld, dtype=torch.int16, device=dev)
     lo = torch.empty(n, ld, dtype=torch.int16, device=dev)
     yexp = torch.empty(n, dtype=torch.int32, device=dev)
-    yr_st = torch.empty(T, n, dtype=torch.float32, device=dev)
+    # the tensor-core operands in window order (the window criterion reads the
+    # voxel-major rows through idx)
     engine._run("ffs_reml_gather", lib.ffs_reml_gather, n, _p(n_taken), T, ld, _p(idx), _p(pre.yr_hi), _p(pre.yr_lo),
-                _p(pre.yexp), _p(pre.rows), _p(hi), _p(lo), _p(yexp), _p(yr_st), st)
+                _p(pre.yexp), _p(pre.rows), _p(hi), _p(lo), _p(yexp), None, st)
     # projections of every window pair on the tensor cores
     max_pairs = max(1, min(5, 256 // K))
     max_tiles = (n + 127) // 128 + min(n, ncell)
@@ -283,7 +284,7 @@ def _window_round(pre, f, cen, out, *, flag, join=None):
     engine._run("ffs_reml_project_tc_list", lib.ffs_reml_project_tc_list, C.byref(ja), _p(items), _p(counts),
                 max_items, max_pairs, WIN_SLOTS, st)
     engine._run("ffs_reml_window", lib.ffs_reml_window, n, T, K, n_a, n_b, _p(f.lattice), _p(idx), _p(cen_s),
-                _p(tiles), counts.data_ptr() + 8, max_tiles, _p(yr_st), _p(f.coef), _p(winproj), _p(c["dcf"]),
+                _p(tiles), counts.data_ptr() + 8, max_tiles, _p(pre.rows), _p(f.coef), _p(winproj), _p(c["dcf"]),
                 _p(c["ident"]), c["p_id"], _p(c["c_p0"]),
                 _p(out["best"]), _p(out["dbest"]), _p(out["crit0"]), _p(out["fb"]), _p(out["cell"]), st)
     out["pair_evals"] = out.get("pair_evals", 0) + c["evals"][cen.long()].sum()

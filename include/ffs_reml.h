@@ -405,10 +405,10 @@ int ffs_reml_centers(int V, const float* prop, const float* a_axis, int n_a, con
                      int* center, void* stream);
 
 /* Rows of the prep outputs in the order idx[0..n): out_hi/out_lo[i] =
- * yr_hi/yr_lo[idx[i]] ([.][ld_y] fp16 bits), out_exp[i] = yexp[idx[i]] and
- * out_t[t][i] = yr_rows[idx[i]][t] ([T][n], time-major) for the windowed
- * refine's sorted operands. With n_dev (device int) only the rows
- * i < min(n, *n_dev) are written. */
+ * yr_hi/yr_lo[idx[i]] ([.][ld_y] fp16 bits), out_exp[i] = yexp[idx[i]] and,
+ * when out_t is given, out_t[t][i] = yr_rows[idx[i]][t] ([T][n], time-major)
+ * for the windowed refine's sorted operands. With n_dev (device int) only the
+ * rows i < min(n, *n_dev) are written. */
 int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const int* idx, const uint16_t* yr_hi,
                     const uint16_t* yr_lo, const int* yexp, const float* yr_rows, uint16_t* out_hi, uint16_t* out_lo,
                     int* out_exp, float* out_t, void* stream);
@@ -428,7 +428,8 @@ int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, cons
 /* The windowed refine's criterion over the tiles of ffs_reml_window_items
  * (launched for max_tiles, *n_tiles of them real), one sorted row i < n (voxel
  * idx[i], window centre center[i]): y'R^-1 y of each non-identity window pair by the O(T)
- * recurrence of coef over yr_st ([T][n], the sorted rows time-major), its
+ * recurrence of coef over rows[idx[i]] (rows: [V][T] residualised series,
+ * voxel-major, 16-byte aligned: ffs_reml_prep's yr_rows), its
  * projection from winproj[i][slot] (ffs_reml_project_tc_list), the criterion
  * relative to (0, 0) with dcf[p] = (logdet_R + logdet_XtX)[p] - that of (0, 0)
  * (*c_p0, a device scalar),
@@ -441,7 +442,7 @@ int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, cons
  * identity pair and nothing below d = 0), best_cell (the lattice cell of the
  * best non-identity pair, -1 if none). */
 int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx, const int* center,
-                    const int* tiles, const int* n_tiles, int max_tiles, const float* yr_st, const float* coef,
+                    const int* tiles, const int* n_tiles, int max_tiles, const float* rows, const float* coef,
                     const float* winproj, const float* dcf, const unsigned char* ident, int p_id,
                     const double* c_p0, int* best, float* dbest, double* crit0, int* fallback, int* best_cell,
                     void* stream);
