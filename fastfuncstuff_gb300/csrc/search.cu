@@ -19,6 +19,8 @@ __device__ __forceinline__ bool centre_on(const ffs_prep_args& a) {
 
 // Lag 1..8 autocorrelations of one residualised row within runs (products
 // never cross a run boundary) and T/1000, by one warp; lane 0 writes out[9].
+// Each lane walks a contiguous stretch of every run backwards, keeping the 8
+// following samples in registers, so a sample is read once.
 __device__ void row_features(const float* row, int T, int n_runs, const int* run_start, float* out) {
   const int lane = threadIdx.x & 31;
   float acc[8], s0 = 0.f;
@@ -26,12 +28,19 @@ __device__ void row_features(const float* row, int T, int n_runs, const int* run
   for (int k = 0; k < 8; ++k) acc[k] = 0.f;
   for (int r = 0; r < n_runs; ++r) {
     const int t0 = run_start[r], t1 = run_start[r + 1];
-    for (int t = t0 + lane; t < t1; t += 32) {
+    const int len = (t1 - t0 + 31) / 32;
+    const int a = min(t1, t0 + lane * len), b = min(t1, a + len);
+    float w[8];  // w[k] = y_{t+1+k} (0 past the run's end)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) w[k] = b + k < t1 ? row[b + k] : 0.f;
+    for (int t = b - 1; t >= a; --t) {
       const float y = row[t];
       s0 = fmaf(y, y, s0);
 #pragma unroll
-      for (int k = 0; k < 8; ++k)
-        if (t + k + 1 < t1) acc[k] = fmaf(y, row[t + k + 1], acc[k]);
+      for (int k = 0; k < 8; ++k) acc[k] = fmaf(y, w[k], acc[k]);
+#pragma unroll
+      for (int k = 7; k > 0; --k) w[k] = w[k - 1];
+      w[0] = y;
     }
   }
   s0 = warp_sum(s0);

@@ -16,6 +16,8 @@
 // pair (0, 0) exactly (d = 0), and the full grid breaks that tie towards the
 // first identity pair in pair order, p_id. Window identity pairs are not
 // evaluated: a window holding one competes with (p_id, d = 0) instead.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace ffsk {
@@ -376,33 +378,24 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
 }
 
 // fp16 operand rows and exponents in the order idx: a warp per row, 16-byte words
-__global__ void gather_rows_kernel(int n, const int* n_dev, int ld_y, const int* __restrict__ idx,
-                                   const uint4* __restrict__ hi, const uint4* __restrict__ lo,
-                                   const int* __restrict__ yexp, uint4* __restrict__ out_hi,
-                                   uint4* __restrict__ out_lo, int* __restrict__ out_exp) {
-  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (i >= n || (n_dev && i >= *n_dev)) return;
-  const int v = idx[i];
+__global__ void __launch_bounds__(256) gather_rows_kernel(int n, const int* n_dev, int ld_y, const int* __restrict__ idx,
+                                                          const uint4* __restrict__ hi, const uint4* __restrict__ lo,
+                                                          const int* __restrict__ yexp, uint4* __restrict__ out_hi,
+                                                          uint4* __restrict__ out_lo, int* __restrict__ out_exp) {
+  // one 16-byte word of one row per thread, grid-stride over rows x words:
+  // consecutive threads copy consecutive words, every copy independent
+  const int m = n_dev ? min(n, *n_dev) : n;
   const int nw = ld_y / 8;  // 8 fp16 per 16-byte word
-  const uint4* sh = hi + (size_t)v * nw;
-  const uint4* sl = lo + (size_t)v * nw;
-  uint4* dh = out_hi + (size_t)i * nw;
-  uint4* dl = out_lo + (size_t)i * nw;
-  int k = lane;
-  for (; k + 32 < nw; k += 64) {  // four 16-byte loads in flight per lane
-    const uint4 h0 = sh[k], h1 = sh[k + 32], l0 = sl[k], l1 = sl[k + 32];
-    dh[k] = h0;
-    dh[k + 32] = h1;
-    dl[k] = l0;
-    dl[k + 32] = l1;
+  const long long total = (long long)m * nw;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / nw), k = (int)(e % nw);
+    const int v = idx[i];
+    const uint4 h = hi[(size_t)v * nw + k], l = lo[(size_t)v * nw + k];
+    out_hi[(size_t)i * nw + k] = h;
+    out_lo[(size_t)i * nw + k] = l;
+    if (k == 0) out_exp[i] = yexp[v];
   }
-  if (k < nw) {
-    const uint4 h0 = sh[k], l0 = sl[k];
-    dh[k] = h0;
-    dl[k] = l0;
-  }
-  if (lane == 0) out_exp[i] = yexp[v];
 }
 
 // out_t[t][i] = rows[idx[i]][t]: 32 x 32 tiles through shared memory
@@ -473,7 +466,10 @@ extern "C" int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const i
   for (const void* ptr : {(const void*)yr_hi, (const void*)yr_lo, (const void*)out_hi, (const void*)out_lo})
     FFS_REQUIRE(((uintptr_t)ptr & 15) == 0, "ffs_reml_gather: fp16 rows must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
-  gather_rows_kernel<<<ceil_div(n, 8), 256, 0, st>>>(n, n_dev, ld_y, idx, reinterpret_cast<const uint4*>(yr_hi),
+  int sms = 0;
+  FFS_CUDA(sm_count(&sms));
+  const int blocks = (int)std::min<long long>(ceil_div((long long)n * (ld_y / 8), 256), (long long)sms * 8);
+  gather_rows_kernel<<<blocks, 256, 0, st>>>(n, n_dev, ld_y, idx, reinterpret_cast<const uint4*>(yr_hi),
                                                       reinterpret_cast<const uint4*>(yr_lo), yexp,
                                                       reinterpret_cast<uint4*>(out_hi),
                                                       reinterpret_cast<uint4*>(out_lo), out_exp);
