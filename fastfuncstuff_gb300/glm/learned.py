@@ -556,8 +556,8 @@ class LearnedFitGraph:
         """Graph C: the full-grid search and GLS of up to n_pad >= n_fb
         fallback voxels (their ids compacted on the device from the window
         rounds' flags; rows past the real count repeat voxel 0 and are
-        ignored), captured once per padded count."""
-        n_pad = (n_fb + 1023) // 1024 * 1024
+        ignored), captured once per padded count (a multiple of 256)."""
+        n_pad = (n_fb + 255) // 256 * 256
         fc = self._fb_graphs.get(n_pad)
         if fc is not None:
             return fc
