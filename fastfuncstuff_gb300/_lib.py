@@ -104,8 +104,8 @@ SIGNATURES = {
     "ffs_last_error": ([], C.c_char_p),
     "ffs_grid_work_bytes": ([C.c_int, C.c_int, C.c_int], C.c_size_t),
     "ffs_grid_build": ([C.POINTER(GridDesc), C.POINTER(GridOut), C.c_void_p], C.c_int),
-    "ffs_grid_work_bytes_designs": ([C.c_int, C.c_int, C.c_int, C.c_int], C.c_size_t),
-    "ffs_grid_build_designs": ([C.POINTER(GridDesc), C.c_int, C.POINTER(GridOut), C.c_void_p], C.c_int),
+    "ffs_grid_work_bytes_designs": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int], C.c_size_t),
+    "ffs_grid_build_designs": ([C.POINTER(GridDesc), C.c_int, C.c_int, C.POINTER(GridOut), C.c_void_p], C.c_int),
     "ffs_grid_build_noalloc": ([C.POINTER(GridDesc), C.POINTER(GridOut), C.c_void_p], C.c_int),
     "ffs_reml_prep": ([C.POINTER(PrepArgs), C.c_void_p], C.c_int),
     "ffs_reml_project_tc": ([C.POINTER(ProjectArgs), C.c_void_p], C.c_int),

@@ -612,9 +612,10 @@ extern "C" size_t ffs_grid_work_bytes(int T, int K, int P) {
   return sizeof(double) * ffsk::pair_doubles(T, K) * (size_t)P;
 }
 
-extern "C" size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs) {
+extern "C" size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs, int max_ctas) {
   const long long items = (long long)P * (n_designs > 0 ? n_designs : 1);
-  return sizeof(double) * ffsk::pair_doubles(T, K) * (size_t)(items < FFS_GRID_MAX_SLOTS ? items : FFS_GRID_MAX_SLOTS);
+  const long long cap = max_ctas > 0 && max_ctas < FFS_GRID_MAX_SLOTS ? max_ctas : FFS_GRID_MAX_SLOTS;
+  return sizeof(double) * ffsk::pair_doubles(T, K) * (size_t)(items < cap ? items : cap);
 }
 
 extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream) {
@@ -641,7 +642,8 @@ extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, voi
   return check_launch("grid_build_kernel");
 }
 
-extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, const ffs_grid_out* o, void* stream) {
+extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int max_ctas, const ffs_grid_out* o,
+                                      void* stream) {
   using namespace ffsk;
   clear_error();
   FFS_REQUIRE(d && o, "ffs_grid_build_designs: null descriptor");
@@ -658,7 +660,8 @@ extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, con
   FFS_REQUIRE(o->coef && o->logdet_R && o->logdet_XtX && o->U && o->G && o->Adiag && o->XtX && o->info && o->work,
               "ffs_grid_build_designs: null output");
   const long long items = (long long)d->P * n_designs;
-  const int grid = (int)(items < FFS_GRID_MAX_SLOTS ? items : FFS_GRID_MAX_SLOTS);
+  const long long cap = max_ctas > 0 && max_ctas < FFS_GRID_MAX_SLOTS ? max_ctas : FFS_GRID_MAX_SLOTS;
+  const int grid = (int)(items < cap ? items : cap);
   BuildArgs args{*d, *o};
   const size_t smem = sizeof(double) * 4 * (size_t)d->T;
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build_designs: T=%d too long", d->T);

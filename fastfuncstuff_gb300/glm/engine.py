@@ -209,13 +209,15 @@ def constant_in_span(X: np.ndarray, tol: float = 1e-6) -> bool:
 
 def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_indices=None,
                   glt: np.ndarray | None = None, with_tc: bool = True, center=None,
-                  stream: torch.cuda.Stream | None = None) -> GridFactors:
+                  stream: torch.cuda.Stream | None = None, max_ctas: int = 0) -> GridFactors:
     """Run the FP64 grid build for design ``X`` (T, K) on its device.
 
     ``center`` = (flag, coefficients) from ``constant_flag(X)`` when the caller
     has them already (the CUDA-graph plan computes them outside its capture).
     With ``stream`` the grid build runs there (the buffers are allocated on the
-    current stream, which must wait for ``stream`` before it reads them).
+    current stream, which must wait for ``stream`` before it reads them);
+    ``max_ctas`` > 0 caps its CTAs (the rest of the GPU stays free for work
+    beside it).
 
     lambda is always evaluated in float64 from the float32 (a, b) values (the
     FP64 fit's value); the fit's mode only decides the validity filter and the
@@ -240,7 +242,8 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     ng = 0 if glt_t is None else glt_t.shape[0]
     lib = _lib.load()
     cflag, ccoef = constant_flag(Xc) if center is None else center
-    wbytes = lib.ffs_grid_work_bytes(T, K, P) if D == 1 else lib.ffs_grid_work_bytes_designs(T, K, P, D)
+    single = D == 1 and max_ctas <= 0  # else the designs entry point, which takes a CTA cap
+    wbytes = lib.ffs_grid_work_bytes(T, K, P) if single else lib.ffs_grid_work_bytes_designs(T, K, P, D, max_ctas)
     work = torch.empty(int(wbytes) // 8 + 1, dtype=torch.float64, device=dev)
     DP = D * P
     f = GridFactors(
@@ -275,10 +278,11 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
                      U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), uexp=_p(f.uexp), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
                      info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=None, work=_p(work))
     def launch():
-        if D == 1:
+        if single:
             _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
         else:
-            _run("ffs_grid_build_designs", lib.ffs_grid_build_designs, C.byref(d), D, C.byref(o), _stream())
+            _run("ffs_grid_build_designs", lib.ffs_grid_build_designs, C.byref(d), D, max_ctas, C.byref(o),
+                 _stream())
 
     if stream is None:
         launch()

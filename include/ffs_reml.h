@@ -122,10 +122,12 @@ int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
  * the pair only and keep their [P] layout; every other output is indexed by
  * pd = design * P + pair (U [n_designs * P][K][T], logdet_XtX [n_designs * P],
  * U_hi rows pd * K + j, ...). One launch walks the n_designs * P items with
- * at most FFS_GRID_MAX_SLOTS CTAs; work: ffs_grid_work_bytes_designs. */
+ * at most max_ctas CTAs (0 or more than FFS_GRID_MAX_SLOTS: that limit) --
+ * fewer CTAs leave SMs to kernels running beside the build on other streams;
+ * work: ffs_grid_work_bytes_designs with the same max_ctas. */
 #define FFS_GRID_MAX_SLOTS 2048
-size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs);
-int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, const ffs_grid_out* o, void* stream);
+size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs, int max_ctas);
+int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int max_ctas, const ffs_grid_out* o, void* stream);
 
 /* ffs_grid_build without a workspace argument: this variant has no counterpart
  * in the reference. It is for callers that cannot allocate device memory where
