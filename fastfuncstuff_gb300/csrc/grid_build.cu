@@ -75,22 +75,88 @@ __device__ double block_sum(double v, double* red) {
   return red[0];
 }
 
+// 1/sqrt(d) by the Newton-Raphson iteration r <- r + r (1 - d r^2) / 2 from
+// the fp32 estimate (relative error about 2^-22; each step squares it, so two
+// steps reach FP64 rounding). On this GPU an FP64 square root or division
+// takes about ten dependent FMAs' time; the factorisations below have one of
+// each per column on their critical path. Outside the range where the fp32
+// estimate is a normal number, the plain expression.
+__device__ __forceinline__ double rsqrt_newton(double d) {
+  if (!(d > 1e-30 && d < 1e30)) return 1.0 / sqrt(d);
+  double r = (double)rsqrtf((float)d);
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const double h = d * r;
+    r = fma(0.5 * r, fma(-h, r, 1.0), r);
+  }
+  return r;
+}
+
+// Exact float -> double by its bit fields (sign, exponent rebiased by
+// 1023 - 127 = 896, mantissa shifted into place), on the integer pipe;
+// zeros, subnormals, infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ double f2d_exact(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t ax = u & 0x7fffffffu;
+  if (ax - 0x00800000u >= 0x7f000000u) return (double)x;
+  const uint32_t hi = (u & 0x80000000u) | ((ax >> 3) + (896u << 20));
+  return __hiloint2double((int)hi, (int)(ax << 29));
+}
+
+// (i, j), j <= i, of the packed lower-triangle index e = i (i + 1) / 2 + j
+__device__ __forceinline__ void tri_index(int e, int& i, int& j) {
+  int r = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);
+  while (r > 0 && r * (r + 1) / 2 > e) --r;
+  while ((r + 1) * (r + 2) / 2 <= e) ++r;
+  i = r;
+  j = e - r * (r + 1) / 2;
+}
+
+// A Gram entry sum_t x_i[t] x_j[t] as four interleaved FP64 chains (t mod 4),
+// added pairwise at the end: a quarter of the dependent-FMA latency of one
+// chain, and a fixed operation order, so every kernel that forms a Gram entry
+// through Dot4 gets the same bits. run() continues the chains over n further
+// samples; every run but the last must cover a multiple of 4 samples.
+struct Dot4 {
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  __device__ __forceinline__ void run(const double* xi, const double* xj, int n) {
+    int t = 0;
+    for (; t + 4 <= n; t += 4) {
+      s0 = fma(xi[t], xj[t], s0);
+      s1 = fma(xi[t + 1], xj[t + 1], s1);
+      s2 = fma(xi[t + 2], xj[t + 2], s2);
+      s3 = fma(xi[t + 3], xj[t + 3], s3);
+    }
+    if (t < n) s0 = fma(xi[t], xj[t], s0);
+    if (t + 1 < n) s1 = fma(xi[t + 1], xj[t + 1], s1);
+    if (t + 2 < n) s2 = fma(xi[t + 2], xj[t + 2], s2);
+  }
+  __device__ __forceinline__ double sum() const { return (s0 + s1) + (s2 + s3); }
+};
+
 // In-place right-looking Cholesky of the leading n x n block of M (row stride
-// ld, lower triangle used). Returns false if a pivot is not positive
-// (LAPACK potrf's failure test).
-__device__ bool block_cholesky(double* M, int n, int ld, int* flag) {
+// ld, lower triangle used): the pivot's reciprocal square root by
+// rsqrt_newton, the column scaled by it, L_kk = d / sqrt(d). rdiag (optional)
+// receives 1 / L_kk. Returns false if a pivot is not positive (LAPACK potrf's
+// failure test).
+__device__ bool block_cholesky(double* M, int n, int ld, int* flag, double* rdiag = nullptr) {
+  __shared__ double rk;
   if (threadIdx.x == 0) *flag = 0;
   __syncthreads();
   for (int k = 0; k < n; ++k) {
     if (threadIdx.x == 0) {
-      double d = M[k * ld + k];
-      if (!(d > 0.0)) *flag = 1;
-      M[k * ld + k] = d > 0.0 ? sqrt(d) : 1.0;
+      const double d = M[k * ld + k];
+      const bool pos = d > 0.0;
+      if (!pos) *flag = 1;
+      const double r = pos ? rsqrt_newton(d) : 1.0;
+      M[k * ld + k] = pos ? d * r : 1.0;
+      rk = r;
+      if (rdiag) rdiag[k] = r;
     }
     __syncthreads();
     if (*flag) return false;
-    const double dk = M[k * ld + k];
-    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) M[i * ld + k] /= dk;
+    const double r = rk;
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) M[i * ld + k] *= r;
     __syncthreads();
     const int m = n - k - 1;
     for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
@@ -103,14 +169,16 @@ __device__ bool block_cholesky(double* M, int n, int ld, int* flag) {
 }
 
 // Li = L^-1 for lower-triangular L (n x n, row stride ld); column-parallel.
-__device__ void block_tri_inverse(const double* L, double* Li, int n, int ld) {
+// With rdiag (1 / L_ii from block_cholesky) the diagonal divisions of the
+// column recursions become products.
+__device__ void block_tri_inverse(const double* L, double* Li, int n, int ld, const double* rdiag = nullptr) {
   for (int c = threadIdx.x; c < n; c += blockDim.x) {
     for (int i = 0; i < c; ++i) Li[i * ld + c] = 0.0;
     for (int i = c; i < n; ++i) {
       double s = (i == c) ? 1.0 : 0.0;
       for (int k = c; k < i; ++k) s -= L[i * ld + k] * Li[k * ld + c];
       const double d = L[i * ld + i];
-      Li[i * ld + c] = d != 0.0 ? s / d : 0.0;
+      Li[i * ld + c] = rdiag ? s * rdiag[i] : (d != 0.0 ? s / d : 0.0);
     }
   }
   __syncthreads();
@@ -238,7 +306,7 @@ __global__ void __launch_bounds__(GB_THREADS) grid_build_kernel(BuildArgs args, 
           const int t = t0 + k;
           if (t < T) {
             const double* cm = cms + 4 * t;
-            const double x = (double)xb[k];
+            const double x = f2d_exact(xb[k]);
             const double z = x - cm[0] * xp;
             const double v = z - cm[1] * vp;
             s.Xw[(size_t)j * T + t] = v * cm[3];
@@ -250,24 +318,26 @@ __global__ void __launch_bounds__(GB_THREADS) grid_build_kernel(BuildArgs args, 
     }
     __syncthreads();
 
-    // ---- 3. X_w'X_w (full symmetric) into Lx, and the fp32 copy
-    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
-      const int i = idx / K, j = idx % K;
-      if (j > i) continue;
-      const double* xi = s.Xw + (size_t)i * T;
-      const double* xj = s.Xw + (size_t)j * T;
-      double acc = 0.0;
-      for (int t = 0; t < T; ++t) acc += xi[t] * xj[t];
-      s.Lx[i * K + j] = acc;
-      s.Lx[j * K + i] = acc;
-      o.XtX[(size_t)pd * K * K + i * K + j] = (float)acc;
-      o.XtX[(size_t)pd * K * K + j * K + i] = (float)acc;
+    // ---- 3. X_w'X_w (full symmetric) into Lx, and the fp32 copy: one thread
+    // per lower-triangle entry (full warps), four chains each
+    for (int e = threadIdx.x; e < K * (K + 1) / 2; e += blockDim.x) {
+      int i, j;
+      tri_index(e, i, j);
+      Dot4 acc;
+      acc.run(s.Xw + (size_t)i * T, s.Xw + (size_t)j * T, T);
+      const double v = acc.sum();
+      s.Lx[i * K + j] = v;
+      s.Lx[j * K + i] = v;
+      o.XtX[(size_t)pd * K * K + i * K + j] = (float)v;
+      o.XtX[(size_t)pd * K * K + j * K + i] = (float)v;
     }
     __syncthreads();
 
     // ---- 4. Cholesky of X_w'X_w, QR (modified Gram-Schmidt, twice) otherwise
+    // 1 / diag(Lx) goes to the A slot, free until phase 9
     int info = 0;
-    if (!block_cholesky(s.Lx, K, K, &flag)) {
+    const bool chol = block_cholesky(s.Lx, K, K, &flag, s.A);
+    if (!chol) {
       info = 1;
       // Q and R from X_w; Lx := R' (lower), so that X_w'X_w = Lx Lx'.
       for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) s.Lx[idx] = 0.0;
@@ -397,7 +467,7 @@ __global__ void __launch_bounds__(GB_THREADS) grid_build_kernel(BuildArgs args, 
     // ---- 7. Lx^-1 and diag(A), A = Lx^-T Lx^-1 = (X_w'X_w)^-1 (only the
     // entries the statistics read are formed: the diagonal here, the task
     // block and c A c' in phase 9)
-    block_tri_inverse(s.Lx, s.Li, K, K);
+    block_tri_inverse(s.Lx, s.Li, K, K, chol ? s.A : nullptr);
     for (int j = threadIdx.x; j < K; j += blockDim.x) {
       double acc = 0.0;
       for (int k = j; k < K; ++k) acc += s.Li[k * K + j] * s.Li[k * K + j];
@@ -465,83 +535,127 @@ __global__ void __launch_bounds__(GB_THREADS) grid_build_kernel(BuildArgs args, 
   }
 }
 
-// Orthonormal basis of the design's columns, Q0 = X Lx^-T with Lx the FP64
-// Cholesky factor of X'X (Q0 is U of the pair (0, 0), R = I); modified
-// Gram-Schmidt, twice, when X'X is not positive definite. One CTA. work:
-// [K][K] + [K][T] doubles.
-__global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const float* Xg, double* work, float* Q0,
-                                                           int* info, int staged, int* const_flag, float* const_coef) {
-  __shared__ double red[32];
-  __shared__ int flag;
-  extern __shared__ double xd[];  // staged: [T][K] X in FP64, then [T][K] X in fp32, then [K][K] Lx in fp32
-  const int LT = ld_t(T);
-  for (int idx = threadIdx.x; idx < K * (LT - T); idx += blockDim.x)
-    Q0[(size_t)(idx / (LT - T)) * LT + T + idx % (LT - T)] = 0.f;
-  float* xs = reinterpret_cast<float*>(xd + (size_t)T * K);
-  float* mf = xs + (size_t)T * K;
-  if (staged) {
-    for (int idx = threadIdx.x; idx < T * K; idx += blockDim.x) {
-      const float x = Xg[idx];
-      xs[idx] = x;
-      xd[idx] = (double)x;
+// ---- Design basis: Q0 = X Lx^-T, Lx the FP64 Cholesky factor of X'X (Q0 is
+// U of the pair (0, 0), where R = I and X_w = X, and comes out bit for bit
+// equal to the grid build's: the same Dot4 entries, block_cholesky and fp32
+// recursion), and the centring test c = (X'X)^-1 X'1. Two launches: the Gram
+// entries of [X | 1] spread over CTAs (each entry a chain of FP64 FMAs whose
+// latency, not the FP64 rate, bounds it), then one CTA for the factor, Q0 and
+// c. work: [NE] Gram entries of [X | 1] (packed lower triangle), [K][T]
+// doubles (QR fallback), then K x K doubles when K > DB_SMEM_K.
+
+constexpr int DB_ENTRIES = 32;   // Gram entries per CTA: one warp's lanes
+constexpr int DB_SMEM_K = 64;    // the factor stays in shared memory up to this K
+constexpr int DB_THREADS = 256;  // the finishing CTA (its MGS fallback's sums depend on it)
+
+__host__ __device__ inline int db_entries(int K) { return (K + 1) * (K + 2) / 2; }
+
+// Samples of the design staged per pass: a multiple of 4 (the Dot4 chains
+// continue across passes), with (K + 1) columns of (chunk + 1) doubles within
+// 96 KB of shared memory.
+inline int db_chunk(int T, int K) {
+  const int fit = (96 * 1024 / (8 * (K + 1)) - 1) & ~3;
+  const int t4 = (T + 3) & ~3;
+  return fit < t4 ? fit : t4;
+}
+
+__global__ void __launch_bounds__(256) design_gram_kernel(int T, int K, int chunk, const float* __restrict__ Xg,
+                                                          double* __restrict__ gram) {
+  extern __shared__ double xt[];  // [ncol][chunk + 1]: the columns this CTA reads, FP64, odd row stride
+  const int ne = db_entries(K);
+  const int e0 = blockIdx.x * DB_ENTRIES;
+  const int e1 = min(e0 + DB_ENTRIES, ne);
+  int ihi, jhi;
+  tri_index(e1 - 1, ihi, jhi);
+  const int ncol = ihi + 1;  // the entries' rows i <= ihi read columns 0..ihi (column K is the constant)
+  const int ld = chunk + 1;
+  const int e = e0 + (int)threadIdx.x;
+  int i = 0, j = 0;
+  if (threadIdx.x < 32 && e < e1) tri_index(e, i, j);
+  Dot4 acc;
+  for (int t0 = 0; t0 < T; t0 += chunk) {
+    const int n = min(chunk, T - t0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * ncol; idx += blockDim.x) {
+      const int t = idx / ncol, c = idx % ncol;
+      xt[c * ld + t] = c < K ? f2d_exact(Xg[(size_t)(t0 + t) * K + c]) : 1.0;
     }
     __syncthreads();
+    if (threadIdx.x < 32 && e < e1) acc.run(xt + i * ld, xt + j * ld, n);
   }
-  const float* X = staged ? xs : Xg;
-  auto xdbl = [&](size_t idx) { return staged ? xd[idx] : (double)Xg[idx]; };
-  double* M = work;                    // [K][K]
-  double* Qd = work + (size_t)K * K;   // [K][T] (QR fallback)
-  for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
-    const int i = idx / K, j = idx % K;
-    if (j > i) continue;
-    double acc = 0.0;
-    for (int t = 0; t < T; ++t) acc += xdbl((size_t)t * K + i) * xdbl((size_t)t * K + j);
-    M[i * K + j] = acc;
-    M[j * K + i] = acc;
+  if (threadIdx.x < 32 && e < e1) gram[e] = acc.sum();
+}
+
+__global__ void __launch_bounds__(DB_THREADS) design_basis_kernel(int T, int K, const float* __restrict__ X,
+                                                                  const double* __restrict__ gram, double* work,
+                                                                  float* Q0, int* info, int* const_flag,
+                                                                  float* const_coef) {
+  __shared__ double red[32];
+  __shared__ int flag;
+  extern __shared__ double sm[];  // rd [K], cv [K]; K <= DB_SMEM_K: M [K][K], mf [K][K] fp32, q [K][DB_THREADS] fp32
+  const int LT = ld_t(T);
+  const bool small = K <= DB_SMEM_K;
+  double* rd = sm;
+  double* cv = rd + K;
+  double* Qd = work + db_entries(K);  // [K][T] (QR fallback)
+  double* M = small ? cv + K : Qd + (size_t)K * T;
+  // the fp32 factor: in shared memory, else in the QR slot (unused once the
+  // Cholesky factor exists)
+  float* mf = small ? reinterpret_cast<float*>(M + (size_t)K * K) : reinterpret_cast<float*>(Qd);
+  float* qs = small ? mf + (size_t)K * K : nullptr;
+  for (int idx = threadIdx.x; idx < K * (LT - T); idx += blockDim.x)
+    Q0[(size_t)(idx / (LT - T)) * LT + T + idx % (LT - T)] = 0.f;
+  for (int e = threadIdx.x; e < K * (K + 1) / 2; e += blockDim.x) {
+    int i, j;
+    tri_index(e, i, j);
+    M[i * K + j] = gram[e];
+    M[j * K + i] = gram[e];
   }
+  for (int j = threadIdx.x; j < K; j += blockDim.x) cv[j] = gram[K * (K + 1) / 2 + j];  // row K: X'1
   __syncthreads();
-  if (block_cholesky(M, K, K, &flag)) {
-    const float* Mq = mf;
-    if (staged) {
-      for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) mf[idx] = (float)M[idx];
-      __syncthreads();
-    }
+  if (block_cholesky(M, K, K, &flag, rd)) {
+    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) mf[idx] = (float)M[idx];
+    __syncthreads();
+    // Q0 row by row, the grid build's fp32 recursion; a row's earlier entries
+    // are read back from shared memory (from Q0 itself when K is large)
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
+      float* q = small ? qs + threadIdx.x : Q0 + t;
+      const size_t qst = small ? DB_THREADS : LT;
       for (int j = 0; j < K; ++j) {
         float acc = X[(size_t)t * K + j];
-        for (int i = 0; i < j; ++i)
-          acc = fmaf(-(staged ? Mq[j * K + i] : (float)M[j * K + i]), Q0[(size_t)i * LT + t], acc);
-        Q0[(size_t)j * LT + t] = acc / (staged ? Mq[j * K + j] : (float)M[j * K + j]);
+        for (int i = 0; i < j; ++i) acc = fmaf(-mf[j * K + i], q[i * qst], acc);
+        const float v = acc / mf[j * K + j];
+        q[j * qst] = v;
+        if (small) Q0[(size_t)j * LT + t] = v;
       }
     }
     if (const_flag) {
-      // the constant series in span(X): c = (X'X)^-1 X'1 from the same FP64
-      // factor, accepted when ||X c - 1|| <= 1e-6 sqrt(T)
-      double* cv = Qd;  // [K] X'1, then c
-      for (int j = threadIdx.x; j < K; j += blockDim.x) {
-        double b = 0.0;
-        for (int t = 0; t < T; ++t) b += xdbl((size_t)t * K + j);
-        cv[j] = b;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        for (int j = 0; j < K; ++j) {  // L y = b
-          double v = cv[j];
-          for (int i = 0; i < j; ++i) v -= M[j * K + i] * cv[i];
-          cv[j] = v / M[j * K + j];
+      // c = (X'X)^-1 X'1 from the same factor (one warp: forward and back
+      // substitution, a column of updates per step), accepted when
+      // ||X c - 1||^2 <= 1e-12 T
+      if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        for (int j = 0; j < K; ++j) {
+          const double yj = cv[j] * rd[j];
+          __syncwarp();
+          for (int i = j + 1 + lane; i < K; i += 32) cv[i] = fma(-M[i * K + j], yj, cv[i]);
+          if (lane == 0) cv[j] = yj;
+          __syncwarp();
         }
-        for (int j = K - 1; j >= 0; --j) {  // L' c = y
-          double v = cv[j];
-          for (int i = j + 1; i < K; ++i) v -= M[i * K + j] * cv[i];
-          cv[j] = v / M[j * K + j];
+        for (int j = K - 1; j >= 0; --j) {
+          const double cj = cv[j] * rd[j];
+          __syncwarp();
+          for (int i = lane; i < j; i += 32) cv[i] = fma(-M[j * K + i], cj, cv[i]);
+          if (lane == 0) cv[j] = cj;
+          __syncwarp();
         }
       }
       __syncthreads();
       double part = 0.0;
       for (int t = threadIdx.x; t < T; t += blockDim.x) {
         double r = -1.0;
-        for (int j = 0; j < K; ++j) r += xdbl((size_t)t * K + j) * cv[j];
-        part += r * r;
+        for (int j = 0; j < K; ++j) r = fma(f2d_exact(X[(size_t)t * K + j]), cv[j], r);
+        part = fma(r, r, part);
       }
       const double ss = block_sum(part, red);
       const bool ok = ss <= 1e-12 * (double)T;
@@ -555,7 +669,8 @@ __global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const f
     for (int j = threadIdx.x; j < K; j += blockDim.x) const_coef[j] = 0.f;
     if (threadIdx.x == 0) *const_flag = 0;
   }
-  // QR of X by modified Gram-Schmidt (twice) in FP64
+  // QR of X by modified Gram-Schmidt (twice) in FP64, the grid build's
+  // fallback on X_w = X
   for (int j = 0; j < K; ++j) {
     double* q = Qd + (size_t)j * T;
     for (int t = threadIdx.x; t < T; t += blockDim.x) q[t] = (double)X[(size_t)t * K + j];
@@ -588,7 +703,8 @@ __global__ void __launch_bounds__(256) design_basis_kernel(int T, int K, const f
 }  // namespace ffsk
 
 extern "C" size_t ffs_design_basis_work_bytes(int T, int K) {
-  return sizeof(double) * ((size_t)K * K + (size_t)K * T);
+  const size_t kk = K > ffsk::DB_SMEM_K ? (size_t)K * K : 0;
+  return sizeof(double) * ((size_t)ffsk::db_entries(K) + (size_t)K * T + kk);
 }
 
 extern "C" int ffs_design_basis(int T, int K, const float* X, void* work, float* Q0, int* info, int* const_flag,
@@ -598,13 +714,20 @@ extern "C" int ffs_design_basis(int T, int K, const float* X, void* work, float*
   FFS_REQUIRE(T > 0 && K > 0 && K <= T, "ffs_design_basis: T=%d K=%d", T, K);
   FFS_REQUIRE(X && work && Q0 && info, "ffs_design_basis: null buffer");
   FFS_REQUIRE(!const_flag == !const_coef, "ffs_design_basis: const_flag and const_coef go together");
-  // X staged in shared memory in FP64 and fp32 (the K (K + 1) / 2 dot
-  // products read it T times), with the fp32 factor
-  const size_t xs = (sizeof(double) + sizeof(float)) * (size_t)T * K + sizeof(float) * (size_t)K * K;
-  const int staged = xs <= 160 * 1024;
-  if (staged) FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(design_basis_kernel), xs));
-  design_basis_kernel<<<1, 256, staged ? xs : 0, (cudaStream_t)stream>>>(T, K, X, static_cast<double*>(work), Q0,
-                                                                          info, staged, const_flag, const_coef);
+  double* gram = static_cast<double*>(work);
+  const int chunk = db_chunk(T, K);
+  FFS_REQUIRE(chunk >= 4, "ffs_design_basis: K=%d too wide", K);
+  const size_t gsm = sizeof(double) * (size_t)(K + 1) * (chunk + 1);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(design_gram_kernel), gsm));
+  const int nb = ceil_div(db_entries(K), DB_ENTRIES);
+  design_gram_kernel<<<nb, 256, gsm, (cudaStream_t)stream>>>(T, K, chunk, X, gram);
+  if (const int rc = check_launch("design_gram_kernel")) return rc;
+  const size_t fsm = K <= DB_SMEM_K ? sizeof(double) * 2 * K + sizeof(double) * (size_t)K * K +
+                                          sizeof(float) * (size_t)K * K + sizeof(float) * (size_t)K * DB_THREADS
+                                    : sizeof(double) * 2 * K;
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(design_basis_kernel), fsm));
+  design_basis_kernel<<<1, DB_THREADS, fsm, (cudaStream_t)stream>>>(T, K, X, gram, gram, Q0, info, const_flag,
+                                                                   const_coef);
   return check_launch("design_basis_kernel");
 }
 

@@ -153,7 +153,9 @@ int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out* o, void* 
  * ffs_grid_build also writes). Q0 = X Lx^-T with Lx the FP64 Cholesky factor of
  * X'X, or modified Gram-Schmidt (twice) when X'X is not positive definite
  * (*info = 1). Needing only X, it lets the residualisation (ffs_reml_prep) run
- * while the grid build is still in flight. work: ffs_design_basis_work_bytes.
+ * while the grid build is still in flight; Q0 equals the grid build's U of
+ * (0, 0) bit for bit. Two kernel launches (the Gram entries of [X | 1] over
+ * several CTAs, then one CTA for the factor). work: ffs_design_basis_work_bytes.
  * With const_flag / const_coef (both or neither) it also decides whether the
  * constant series lies in span(X): c = (X'X)^-1 X'1 from the same FP64
  * factor, *const_flag = 1 and const_coef[K] = c when ||X c - 1|| <= 1e-6

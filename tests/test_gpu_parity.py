@@ -271,6 +271,30 @@ def test_design_basis_centring_test_matches_normal_equations():
             np.testing.assert_allclose(Q.T @ Q, np.eye(Q.shape[1]), atol=1e-5)
 
 
+@pytest.mark.parametrize("T,K", [(400, 20), (201, 7), (300, 70), (300, 200)])
+def test_design_basis_equals_grid_build_identity_pair(T, K):
+    """Q0 of the design-basis kernels is U of the pair (0, 0) bit for bit (the
+    grouped fit takes its basis from the grid build, the per-group fit from
+    the design basis): the factor in shared memory (K <= 64), in global
+    memory (K = 70), and a Gram formed over several staged passes of the
+    samples (K = 200). It also spans X (orthonormal, X = Q0' R)."""
+    rng = np.random.default_rng(K)
+    t = np.linspace(-1, 1, T)
+    X = np.column_stack([np.ones(T), t, rng.standard_normal((T, K - 2))]).astype(np.float32)
+    Xd = torch.from_numpy(X).to(DEV)
+    g = G.make_grid(torch.linspace(-0.6, 0.6, 3), torch.linspace(-0.6, 0.6, 3))
+    lay = G.run_layout(T, [0])
+    f = engine.build_factors(Xd, g, lay, with_tc=False)
+    q0 = engine.design_basis(Xd)
+    torch.cuda.synchronize()
+    u00 = f.U[g.p0]
+    assert torch.equal(q0, u00)
+    Q = q0[:, :T].cpu().numpy().astype(np.float64).T
+    np.testing.assert_allclose(Q.T @ Q, np.eye(K), atol=2e-5)
+    R = Q.T @ X.astype(np.float64)
+    np.testing.assert_allclose(Q @ R, X, atol=2e-4 * np.abs(X).max())
+
+
 @pytest.mark.parametrize("selector", ["hierarchical", "exhaustive"])
 def test_grouped_batched_fit_equals_per_group_fits(selector):
     """The grouped fit runs every design in one pass per stage (one grid build
