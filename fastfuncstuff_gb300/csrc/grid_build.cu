@@ -189,12 +189,122 @@ struct BuildArgs {
   ffs_grid_out o;
 };
 
+// Phase 1 of an item: the per-run LDL' of pair p's AR-filtered tridiagonal
+// correlation, the serial recursion m_t = T_t,t-1 / D_t-1, D_t = T_tt - m_t
+// T_t,t-1 (one thread per run; unit gaps need no pow: a^1 = a and a^0 = 1
+// exactly), then sqrt, log and the reciprocals of every sample in parallel:
+// cms[t] = (c, m, D, 1/sqrt(D)) in shared memory, coef[p] and logdet_R[p].
+// *bad_r = 1 if a pivot D_t was not positive. Ends with a barrier.
+__device__ __forceinline__ void ldl_of_pair(const ffs_grid_desc& d, const ffs_grid_out& o, int p, double* cms, double* red,
+                            int* bad_r) {
+  const int T = d.T;
+  const float af = d.a[p], bf = d.b[p];
+  const double a = (double)af;
+  const double lam = d.lambda_fp32 ? (double)lambda_f32(af, bf) : lambda_f64(a, (double)bf);
+  if (threadIdx.x == 0) *bad_r = 0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < d.n_runs; r += blockDim.x) {
+    const int t0 = d.run_start[r], t1 = d.run_start[r + 1];
+    double Dprev = 1.0, mprev = 0.0;
+    int prev_gap = 0;
+    for (int t = t0; t < t1; ++t) {
+      double c = 0.0, m = 0.0, D = 1.0;
+      // lambda == 0: every lag correlation is zero, R = I exactly
+      if (t > t0 && lam != 0.0) {
+        const int gap = d.tau[t] - d.tau[t - 1];
+        double rho;
+        if (gap == 1) {
+          c = a;
+          rho = lam;
+        } else {
+          // a^gap and a^(gap - 1) of small integer gaps by products
+          double ag1 = 1.0;
+          if (gap <= 16) {
+            for (int k = 1; k < gap; ++k) ag1 *= a;
+          } else {
+            ag1 = pow(a, (double)(gap - 1));
+          }
+          c = ag1 * a;
+          rho = lam * ag1;
+        }
+        const double Ttt = 1.0 + c * c - 2.0 * c * rho;
+        const double Toff = rho - c;
+        if (gap == 1 && prev_gap == 1 && Dprev == cms[4 * (t - 1) - 4 + 2]) {
+          // the previous step left D unchanged: the recursion has reached
+          // its fixed point, and every step of this stretch of unit gaps
+          // repeats it
+          m = mprev;
+          D = Dprev;
+        } else {
+          // 1/D_{t-1}: fp32 estimate refined by two Newton steps r (2 - D r)
+          // (error ~2^-24 -> ~2^-48 -> below 2^-53), cheaper than a
+          // correctly rounded FP64 division in this serial chain
+          if (Dprev > 1e-30 && Dprev < 1e30) {
+            double r = (double)__frcp_rn((float)Dprev);
+            r = r * fma(-Dprev, r, 2.0);
+            r = r * fma(-Dprev, r, 2.0);
+            m = Toff * r;
+          } else {
+            m = Toff / Dprev;
+          }
+          D = Ttt - m * Toff;
+        }
+        prev_gap = gap;
+      }
+      if (!(D > 0.0)) {
+        *bad_r = 1;
+        D = 1.0;
+      }
+      double* cm = cms + 4 * t;
+      cm[0] = c; cm[1] = m; cm[2] = D;
+      Dprev = D;
+      mprev = m;
+    }
+  }
+  __syncthreads();
+  {
+    double ld = 0.0;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+      double* cm = cms + 4 * t;
+      const double D = cm[2];
+      const double sD = sqrt(D);
+      const double rsD = 1.0 / sD;
+      ld += 2.0 * log(sD + 1e-10);
+      cm[3] = rsD;
+      reinterpret_cast<float4*>(o.coef)[(size_t)p * T + t] =
+          make_float4((float)cm[0], (float)cm[1], (float)(1.0 / D), (float)rsD);
+    }
+    ld = block_sum(ld, red);
+    if (threadIdx.x == 0) o.logdet_R[p] = ld;
+  }
+  __syncthreads();
+}
+
+// Phase 1 of every pair once, for the items of all designs (coef and
+// logdet_R depend on the pair only): cm [P][T][4] and bad [P] in the
+// workspace, read back by grid_build_kernel.
+__global__ void __launch_bounds__(GB_THREADS) pair_ldl_kernel(BuildArgs args, double* cm, int* bad) {
+  __shared__ double red[32];
+  __shared__ int bad_r;
+  extern __shared__ double cms[];  // [T][4]
+  const int T = args.d.T;
+  ldl_of_pair(args.d, args.o, blockIdx.x, cms, red, &bad_r);
+  double2* dst = reinterpret_cast<double2*>(cm + (size_t)blockIdx.x * 4 * T);
+  for (int i = threadIdx.x; i < 2 * T; i += blockDim.x) dst[i] = reinterpret_cast<const double2*>(cms)[i];
+  if (threadIdx.x == 0) bad[blockIdx.x] = bad_r;
+}
+
 // Items are (design, pair) = (item / P, item % P); a CTA takes items
 // blockIdx.x, blockIdx.x + gridDim.x, ... with scratch slot blockIdx.x.
-// Design-dependent outputs sit at pd = design * P + pair; coef and logdet_R
-// depend on the pair only and are written (with identical values) by the
-// items of every design.
-__global__ void __launch_bounds__(GB_THREADS) grid_build_kernel(BuildArgs args, int n_designs) {
+// Design-dependent outputs sit at pd = design * P + pair. With SHARED_LDL
+// (more than one design) phase 1 comes from pair_ldl_kernel (pair_cm,
+// pair_bad), which also wrote coef and logdet_R; without it every item
+// factors its pair's R itself. The SHARED_LDL kernel is capped at 64
+// registers (left free, the compiler takes 80 and spills).
+template <bool SHARED_LDL>
+__global__ void __launch_bounds__(GB_THREADS, SHARED_LDL ? 4 : 0) grid_build_kernel(BuildArgs args, int n_designs,
+                                                                                  const double* pair_cm,
+                                                                                  const int* pair_bad) {
   const ffs_grid_desc& d = args.d;
   const ffs_grid_out& o = args.o;
   const int T = d.T, K = d.K, LT = ld_t(T);
@@ -207,91 +317,15 @@ __global__ void __launch_bounds__(GB_THREADS) grid_build_kernel(BuildArgs args, 
   for (int item = blockIdx.x; item < d.P * n_designs; item += gridDim.x) {
     const int p = item % d.P, pd = item;
     const float* Xd = d.X + (size_t)(item / d.P) * T * K;
-    const float af = d.a[p], bf = d.b[p];
-    const double a = (double)af;
-    const double lam = d.lambda_fp32 ? (double)lambda_f32(af, bf) : lambda_f64(a, (double)bf);
-    if (threadIdx.x == 0) bad_r = 0;
-    __syncthreads();
-
-    // ---- 1. per-run LDL' of the AR-filtered tridiagonal correlation: the
-    // serial recursion m_t = T_t,t-1 / D_t-1, D_t = T_tt - m_t T_t,t-1 (one
-    // thread per run; unit gaps need no pow: a^1 = a and a^0 = 1 exactly), then
-    // sqrt, log and the reciprocals of every sample in parallel
-    for (int r = threadIdx.x; r < d.n_runs; r += blockDim.x) {
-      const int t0 = d.run_start[r], t1 = d.run_start[r + 1];
-      double Dprev = 1.0, mprev = 0.0;
-      int prev_gap = 0;
-      for (int t = t0; t < t1; ++t) {
-        double c = 0.0, m = 0.0, D = 1.0;
-        // lambda == 0: every lag correlation is zero, R = I exactly
-        if (t > t0 && lam != 0.0) {
-          const int gap = d.tau[t] - d.tau[t - 1];
-          double rho;
-          if (gap == 1) {
-            c = a;
-            rho = lam;
-          } else {
-            // a^gap and a^(gap - 1) of small integer gaps by products
-            double ag1 = 1.0;
-            if (gap <= 16) {
-              for (int k = 1; k < gap; ++k) ag1 *= a;
-            } else {
-              ag1 = pow(a, (double)(gap - 1));
-            }
-            c = ag1 * a;
-            rho = lam * ag1;
-          }
-          const double Ttt = 1.0 + c * c - 2.0 * c * rho;
-          const double Toff = rho - c;
-          if (gap == 1 && prev_gap == 1 && Dprev == cms[4 * (t - 1) - 4 + 2]) {
-            // the previous step left D unchanged: the recursion has reached
-            // its fixed point, and every step of this stretch of unit gaps
-            // repeats it
-            m = mprev;
-            D = Dprev;
-          } else {
-            // 1/D_{t-1}: fp32 estimate refined by two Newton steps r (2 - D r)
-            // (error ~2^-24 -> ~2^-48 -> below 2^-53), cheaper than a
-            // correctly rounded FP64 division in this serial chain
-            if (Dprev > 1e-30 && Dprev < 1e30) {
-              double r = (double)__frcp_rn((float)Dprev);
-              r = r * fma(-Dprev, r, 2.0);
-              r = r * fma(-Dprev, r, 2.0);
-              m = Toff * r;
-            } else {
-              m = Toff / Dprev;
-            }
-            D = Ttt - m * Toff;
-          }
-          prev_gap = gap;
-        }
-        if (!(D > 0.0)) {
-          bad_r = 1;
-          D = 1.0;
-        }
-        double* cm = cms + 4 * t;
-        cm[0] = c; cm[1] = m; cm[2] = D;
-        Dprev = D;
-        mprev = m;
-      }
+    if constexpr (SHARED_LDL) {
+      // the pre-pass factored R for every pair once: copy this pair's rows
+      const double2* src = reinterpret_cast<const double2*>(pair_cm + (size_t)p * 4 * T);
+      for (int i = threadIdx.x; i < 2 * T; i += blockDim.x) reinterpret_cast<double2*>(cms)[i] = src[i];
+      if (threadIdx.x == 0) bad_r = pair_bad[p];
+      __syncthreads();
+    } else {
+      ldl_of_pair(d, o, p, cms, red, &bad_r);
     }
-    __syncthreads();
-    {
-      double ld = 0.0;
-      for (int t = threadIdx.x; t < T; t += blockDim.x) {
-        double* cm = cms + 4 * t;
-        const double D = cm[2];
-        const double sD = sqrt(D);
-        const double rsD = 1.0 / sD;
-        ld += 2.0 * log(sD + 1e-10);
-        cm[3] = rsD;
-        reinterpret_cast<float4*>(o.coef)[(size_t)p * T + t] =
-            make_float4((float)cm[0], (float)cm[1], (float)(1.0 / D), (float)rsD);
-      }
-      ld = block_sum(ld, red);
-      if (threadIdx.x == 0) o.logdet_R[p] = ld;
-    }
-    __syncthreads();
 
     // ---- 2. X_w = L^-1 X, one column per thread; the design samples of
     // GB_PF steps are loaded ahead of the recursion that needs them
@@ -735,10 +769,18 @@ extern "C" size_t ffs_grid_work_bytes(int T, int K, int P) {
   return sizeof(double) * ffsk::pair_doubles(T, K) * (size_t)P;
 }
 
-extern "C" size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs, int max_ctas) {
+// Per-slot scratch of the CTAs, then (more than one design) the pre-pass's
+// factors of R: cm [P][T][4] doubles and bad [P] ints.
+static size_t designs_slot_doubles(int T, int K, int P, int n_designs, int max_ctas) {
   const long long items = (long long)P * (n_designs > 0 ? n_designs : 1);
   const long long cap = max_ctas > 0 && max_ctas < FFS_GRID_MAX_SLOTS ? max_ctas : FFS_GRID_MAX_SLOTS;
-  return sizeof(double) * ffsk::pair_doubles(T, K) * (size_t)(items < cap ? items : cap);
+  return (ffsk::pair_doubles(T, K) * (size_t)(items < cap ? items : cap) + 1) & ~(size_t)1;  // 16-byte aligned end
+}
+
+extern "C" size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs, int max_ctas) {
+  size_t n = designs_slot_doubles(T, K, P, n_designs, max_ctas);
+  if (n_designs > 1) n += (size_t)P * 4 * T + ((size_t)P + 1) / 2;
+  return sizeof(double) * n;
 }
 
 extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream) {
@@ -760,8 +802,8 @@ extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, voi
   BuildArgs args{*d, *o};
   const size_t smem = sizeof(double) * 4 * (size_t)d->T;
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build: T=%d too long", d->T);
-  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel), smem));
-  grid_build_kernel<<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, 1);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel<false>), smem));
+  grid_build_kernel<false><<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, 1, nullptr, nullptr);
   return check_launch("grid_build_kernel");
 }
 
@@ -788,8 +830,21 @@ extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int
   BuildArgs args{*d, *o};
   const size_t smem = sizeof(double) * 4 * (size_t)d->T;
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build_designs: T=%d too long", d->T);
-  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel), smem));
-  grid_build_kernel<<<grid, GB_THREADS, smem, (cudaStream_t)stream>>>(args, n_designs);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel<false>), smem));
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel<true>), smem));
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(pair_ldl_kernel), smem));
+  double* pair_cm = nullptr;
+  int* pair_bad = nullptr;
+  if (n_designs > 1) {
+    pair_cm = o->work + designs_slot_doubles(d->T, d->K, d->P, n_designs, max_ctas);
+    pair_bad = reinterpret_cast<int*>(pair_cm + (size_t)d->P * 4 * d->T);
+    pair_ldl_kernel<<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, pair_cm, pair_bad);
+    if (const int rc = check_launch("pair_ldl_kernel")) return rc;
+  }
+  if (pair_cm)
+    grid_build_kernel<true><<<grid, GB_THREADS, smem, (cudaStream_t)stream>>>(args, n_designs, pair_cm, pair_bad);
+  else
+    grid_build_kernel<false><<<grid, GB_THREADS, smem, (cudaStream_t)stream>>>(args, n_designs, nullptr, nullptr);
   return check_launch("grid_build_kernel (designs)");
 }
 
@@ -871,7 +926,7 @@ extern "C" int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out
   args.o.work = scratch;
   const size_t smem = sizeof(double) * 4 * (size_t)d->T;
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build_noalloc: T=%d too long", d->T);
-  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel), smem));
-  grid_build_kernel<<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, 1);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel<false>), smem));
+  grid_build_kernel<false><<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, 1, nullptr, nullptr);
   return check_launch("grid_build_kernel (static scratch)");
 }

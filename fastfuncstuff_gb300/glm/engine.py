@@ -75,7 +75,7 @@ def set_stage_timer(timer: StageTimer | None) -> None:
     _TIMER = timer
 
 
-def _run(name: str, fn, *args) -> None:
+def _run(name: str, fn, *args, launches: int | None = None) -> None:
     t = _TIMER
     if t is None or torch.cuda.is_current_stream_capturing():
         _lib.check(fn(*args), name)
@@ -86,7 +86,7 @@ def _run(name: str, fn, *args) -> None:
     _lib.check(fn(*args), name)
     e1.record()
     t.events.append((name, e0, e1))
-    t.launches += LAUNCHES.get(name, 1)
+    t.launches += LAUNCHES.get(name, 1) if launches is None else launches
 
 
 _CONST_CACHE: dict = {}
@@ -282,8 +282,9 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
         if single:
             _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
         else:
+            # more than one design: a pre-pass factors R once per pair
             _run("ffs_grid_build_designs", lib.ffs_grid_build_designs, C.byref(d), D, max_ctas, C.byref(o),
-                 _stream())
+                 _stream(), launches=2 if D > 1 else 1)
 
     if stream is None:
         launch()

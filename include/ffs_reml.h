@@ -124,7 +124,9 @@ int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
  * U_hi rows pd * K + j, ...). One launch walks the n_designs * P items with
  * at most max_ctas CTAs (0 or more than FFS_GRID_MAX_SLOTS: that limit) --
  * fewer CTAs leave SMs to kernels running beside the build on other streams;
- * work: ffs_grid_work_bytes_designs with the same max_ctas. */
+ * work: ffs_grid_work_bytes_designs with the same max_ctas. With more than one
+ * design a first launch factors R once per pair (it depends on the pair
+ * only) and the items of every design read that factor. */
 #define FFS_GRID_MAX_SLOTS 2048
 size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs, int max_ctas);
 int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int max_ctas, const ffs_grid_out* o, void* stream);
