@@ -28,6 +28,7 @@ class GridDesc(C.Structure):
         ("run_start", C.c_void_p), ("tau", C.c_void_p), ("a", C.c_void_p), ("b", C.c_void_p),
         ("X", C.c_void_p), ("lambda_fp32", C.c_int), ("ld_u", C.c_int),
         ("n_task", C.c_int), ("task_idx", C.c_void_p), ("n_glt", C.c_int), ("glt", C.c_void_p),
+        ("n_sets", C.c_int), ("set_ptr", C.c_void_p), ("set_idx", C.c_void_p),
     ]
 
 
@@ -37,7 +38,17 @@ class GridOut(C.Structure):
         ("U", C.c_void_p), ("U_hi", C.c_void_p), ("U_lo", C.c_void_p), ("uexp", C.c_void_p),
         ("G", C.c_void_p),
         ("Adiag", C.c_void_p), ("XtX", C.c_void_p), ("info", C.c_void_p), ("Ftask", C.c_void_p),
-        ("glt_var", C.c_void_p), ("Gsum", C.c_void_p), ("work", C.c_void_p),
+        ("glt_var", C.c_void_p), ("Gsum", C.c_void_p), ("work", C.c_void_p), ("Fsets", C.c_void_p),
+    ]
+
+
+class SetStatsArgs(C.Structure):
+    _fields_ = [
+        ("V", C.c_int), ("K", C.c_int), ("n_sets", C.c_int), ("n_out", C.c_int),
+        ("set_ptr", C.c_void_p), ("set_idx", C.c_void_p), ("set_col", C.c_void_p), ("msum", C.c_int),
+        ("Fsets", C.c_void_p), ("Csets", C.c_void_p), ("best", C.c_void_p), ("design", C.c_void_p),
+        ("n_pairs", C.c_int), ("betas", C.c_void_p), ("sigma2", C.c_void_p), ("scale", C.c_void_p),
+        ("set_fstats", C.c_void_p), ("set_sd", C.c_void_p), ("set_coef", C.c_void_p),
     ]
 
 
@@ -113,6 +124,7 @@ SIGNATURES = {
     "ffs_reml_surface": ([C.POINTER(SurfaceArgs), C.c_void_p], C.c_int),
     "ffs_reml_select": ([C.POINTER(SelectArgs), C.c_void_p], C.c_int),
     "ffs_reml_gls": ([C.POINTER(GlsArgs), C.c_void_p], C.c_int),
+    "ffs_reml_set_stats": ([C.POINTER(SetStatsArgs), C.c_void_p], C.c_int),
     "ffs_reml_gls_ex": ([C.POINTER(GlsArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p], C.c_int),
     "ffs_reml_gls_grouped": ([C.POINTER(GlsArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,

@@ -606,6 +606,44 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
   gls_finish_tile(a, g, j0, n, C0, C1, Ys, ld, st, red, Mq);
 }
 
+// Column-set statistics, one thread per voxel (the sets are a few small
+// blocks; betas and sigma2 come back to the scaled series' units first, as
+// the reference computes them before its unscale step)
+__global__ void __launch_bounds__(256) set_stats_kernel(ffs_set_stats_args a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.V) return;
+  const int p = a.best[v];
+  const int dsg = a.design ? a.design[v] : 0;
+  const size_t key = a.design ? (size_t)dsg * a.n_pairs + p : (size_t)p;
+  const float* Fm = a.Fsets + key * a.msum;
+  const float* Cm = a.Csets + (size_t)dsg * a.msum;
+  const float sc = a.scale[v];
+  const float* bv = a.betas + (size_t)v * a.K;
+  const float s2 = __fdiv_rn(a.sigma2[v], sc * sc);
+  size_t off = 0;
+  for (int g = 0; g < a.n_sets; ++g) {
+    const int b0 = a.set_ptr[g], q = a.set_ptr[g + 1] - b0;
+    const int* ix = a.set_idx + b0;
+    float quad = 0.f, cq = 0.f;
+    for (int i = 0; i < q; ++i) {
+      float fi = 0.f, ci = 0.f;
+      for (int j = 0; j < q; ++j) {
+        const float bj = __fdiv_rn(bv[ix[j]], sc);
+        fi = fmaf(Fm[off + (size_t)i * q + j], bj, fi);
+        ci = fmaf(Cm[off + (size_t)i * q + j], bj, ci);
+      }
+      const float bi = __fdiv_rn(bv[ix[i]], sc);
+      quad = fmaf(bi, fi, quad);
+      cq = fmaf(bi, ci, cq);
+    }
+    const size_t o = (size_t)v * a.n_out + a.set_col[g];
+    a.set_fstats[o] = quad / ((float)q * s2 + 1e-30f);
+    a.set_sd[o] = sqrtf(fmaxf(cq, 0.f)) * sc;
+    a.set_coef[o] = q == 1 ? bv[ix[0]] : __int_as_float(0x7fc00000);
+    off += (size_t)q * q;
+  }
+}
+
 // tile_start[g] = sum over g' < g of ceil(count[g'] / GLS_TILE)
 __global__ void gls_tile_scan(int P, const int* end, int* tile_start) {
   __shared__ int part[1024];
@@ -697,4 +735,19 @@ extern "C" int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* 
 
 extern "C" int ffs_reml_gls(const ffs_gls_args* a, void* stream) {
   return ffs_reml_gls_ex(a, 0, nullptr, nullptr, nullptr, stream);
+}
+
+extern "C" int ffs_reml_set_stats(const ffs_set_stats_args* a, void* stream) {
+  clear_error();
+  FFS_REQUIRE(a, "ffs_reml_set_stats: null args");
+  FFS_REQUIRE(a->V >= 0 && a->K > 0 && a->n_sets >= 0 && a->n_out >= a->n_sets && a->msum >= 0,
+              "ffs_reml_set_stats: V=%d K=%d n_sets=%d n_out=%d msum=%d", a->V, a->K, a->n_sets, a->n_out,
+              a->msum);
+  if (a->V == 0 || a->n_sets == 0) return FFS_OK;
+  FFS_REQUIRE(a->set_ptr && a->set_idx && a->set_col && a->Fsets && a->Csets && a->best && a->betas &&
+                  a->sigma2 && a->scale && a->set_fstats && a->set_sd && a->set_coef,
+              "ffs_reml_set_stats: null buffer");
+  FFS_REQUIRE(!a->design || a->n_pairs > 0, "ffs_reml_set_stats: design needs n_pairs");
+  set_stats_kernel<<<ceil_div(a->V, 256), 256, 0, (cudaStream_t)stream>>>(*a);
+  return check_launch("set_stats_kernel");
 }

@@ -184,6 +184,30 @@ __device__ void block_tri_inverse(const double* L, double* Li, int n, int ld, co
   __syncthreads();
 }
 
+// out[n][n] = inv(A_SS + 1e-8 I) for the columns idx[0 .. n) of A = Li' Li
+// = (X_w'X_w)^-1: S = A_SS + 1e-8 I (the S slot), its Cholesky factor, that
+// factor's inverse (the A slot) and out = inverse' inverse, in FP64. Ends
+// with a barrier.
+__device__ __forceinline__ void sub_block_inverse(const PairScratch& s, int K, const int* idx, int n, int* flag, float* out) {
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e % n;
+    const int ti = idx[i], tj = idx[j];
+    double acc = 0.0;
+    for (int k = max(ti, tj); k < K; ++k) acc += s.Li[k * K + ti] * s.Li[k * K + tj];
+    s.S[i * n + j] = acc + (i == j ? 1e-8 : 0.0);
+  }
+  __syncthreads();
+  block_cholesky(s.S, n, n, flag);
+  block_tri_inverse(s.S, s.A, n, n);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e % n;
+    double acc = 0.0;
+    for (int k = max(i, j); k < n; ++k) acc += s.A[k * n + i] * s.A[k * n + j];
+    out[e] = (float)acc;
+  }
+  __syncthreads();
+}
+
 struct BuildArgs {
   ffs_grid_desc d;
   ffs_grid_out o;
@@ -299,10 +323,10 @@ __global__ void __launch_bounds__(GB_THREADS) pair_ldl_kernel(BuildArgs args, do
 // Design-dependent outputs sit at pd = design * P + pair. With SHARED_LDL
 // (more than one design) phase 1 comes from pair_ldl_kernel (pair_cm,
 // pair_bad), which also wrote coef and logdet_R; without it every item
-// factors its pair's R itself. The SHARED_LDL kernel is capped at 64
-// registers (left free, the compiler takes 80 and spills).
+// factors its pair's R itself. Capped at 64 registers (4 CTAs per SM): left
+// free, the compiler takes 80 to 126 of them.
 template <bool SHARED_LDL>
-__global__ void __launch_bounds__(GB_THREADS, SHARED_LDL ? 4 : 0) grid_build_kernel(BuildArgs args, int n_designs,
+__global__ void __launch_bounds__(GB_THREADS, 4) grid_build_kernel(BuildArgs args, int n_designs,
                                                                                   const double* pair_cm,
                                                                                   const int* pair_bad) {
   const ffs_grid_desc& d = args.d;
@@ -546,24 +570,22 @@ __global__ void __launch_bounds__(GB_THREADS, SHARED_LDL ? 4 : 0) grid_build_ker
         if (threadIdx.x == 0) o.glt_var[(size_t)pd * d.n_glt + c] = (float)v;
       }
     }
-    if (nt > 0 && o.Ftask) {
-      for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
-        const int i = idx / nt, j = idx % nt;
-        const int ti = d.task_idx[i], tj = d.task_idx[j];
-        double acc = 0.0;
-        for (int k = max(ti, tj); k < K; ++k) acc += s.Li[k * K + ti] * s.Li[k * K + tj];
-        s.S[i * nt + j] = acc + (i == j ? 1e-8 : 0.0);
-      }
-      __syncthreads();
-      block_cholesky(s.S, nt, nt, &flag);
-      // the inverse factor goes to the A slot; Ftask = Li' Li
-      block_tri_inverse(s.S, s.A, nt, nt);
-      for (int idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
-        const int i = idx / nt, j = idx % nt;
-        double acc = 0.0;
-        for (int k = max(i, j); k < nt; ++k) acc += s.A[k * nt + i] * s.A[k * nt + j];
-        o.Ftask[(size_t)pd * nt * nt + idx] = (float)acc;
-      }
+    // the task block, then the column sets' blocks one after another
+    const int has_task = nt > 0 && o.Ftask ? 1 : 0;
+    const int nsets = o.Fsets ? d.n_sets : 0;
+    size_t msum = 0, off = 0;
+    for (int g = 0; g < nsets; ++g) {
+      const size_t q = (size_t)(d.set_ptr[g + 1] - d.set_ptr[g]);
+      msum += q * q;
+    }
+    for (int bk = 0; bk < has_task + nsets; ++bk) {
+      const bool task = bk < has_task;
+      const int g = bk - has_task;
+      const int n = task ? nt : d.set_ptr[g + 1] - d.set_ptr[g];
+      const int* idx = task ? d.task_idx : d.set_idx + d.set_ptr[g];
+      float* out = task ? o.Ftask + (size_t)pd * nt * nt : o.Fsets + (size_t)pd * msum + off;
+      sub_block_inverse(s, K, idx, n, &flag, out);
+      if (!task) off += (size_t)n * n;
     }
     __syncthreads();  // the next item reuses the scratch slot and the shared state
   }
@@ -783,6 +805,14 @@ extern "C" size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs
   return sizeof(double) * n;
 }
 
+// n_sets needs its index arrays and the Fsets output
+static int check_sets(const ffs_grid_desc* d, const ffs_grid_out* o, const char* who) {
+  FFS_REQUIRE(d->n_sets >= 0, "%s: n_sets=%d", who, d->n_sets);
+  FFS_REQUIRE(d->n_sets == 0 || (d->set_ptr && d->set_idx && o->Fsets), "%s: column sets need set_ptr, set_idx and Fsets",
+              who);
+  return FFS_OK;
+}
+
 extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream) {
   using namespace ffsk;
   clear_error();
@@ -792,6 +822,7 @@ extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, voi
               d->n_runs);
   FFS_REQUIRE(d->K <= d->T, "ffs_grid_build: K=%d exceeds T=%d", d->K, d->T);
   FFS_REQUIRE(d->n_task >= 0 && d->n_task <= d->K, "ffs_grid_build: bad n_task=%d", d->n_task);
+  if (const int rc = check_sets(d, o, "ffs_grid_build")) return rc;
   FFS_REQUIRE(!o->U_hi || (o->U_lo && o->uexp), "ffs_grid_build: U_hi needs U_lo and uexp");
   FFS_REQUIRE(!o->U_hi || (d->ld_u >= d->T && d->ld_u % 8 == 0),
               "ffs_grid_build: ld_u=%d must be >= T and a multiple of 8", d->ld_u);
@@ -818,6 +849,7 @@ extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int
   FFS_REQUIRE((long long)d->P * n_designs < (1LL << 31), "ffs_grid_build_designs: too many items");
   FFS_REQUIRE(d->K <= d->T, "ffs_grid_build_designs: K=%d exceeds T=%d", d->K, d->T);
   FFS_REQUIRE(d->n_task >= 0 && d->n_task <= d->K, "ffs_grid_build_designs: bad n_task=%d", d->n_task);
+  if (const int rc = check_sets(d, o, "ffs_grid_build_designs")) return rc;
   FFS_REQUIRE(!o->U_hi || (o->U_lo && o->uexp), "ffs_grid_build_designs: U_hi needs U_lo and uexp");
   FFS_REQUIRE(!o->U_hi || (d->ld_u >= d->T && d->ld_u % 8 == 0),
               "ffs_grid_build_designs: ld_u=%d must be >= T and a multiple of 8", d->ld_u);
@@ -904,6 +936,7 @@ extern "C" int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out
               "ffs_grid_build_noalloc: T=%d K=%d P=%d n_runs=%d must be positive", d->T, d->K, d->P, d->n_runs);
   FFS_REQUIRE(d->K <= d->T, "ffs_grid_build_noalloc: K=%d exceeds T=%d", d->K, d->T);
   FFS_REQUIRE(d->n_task >= 0 && d->n_task <= d->K, "ffs_grid_build_noalloc: bad n_task=%d", d->n_task);
+  if (const int rc = check_sets(d, o, "ffs_grid_build_noalloc")) return rc;
   FFS_REQUIRE(!o->U_hi || (o->U_lo && o->uexp), "ffs_grid_build_noalloc: U_hi needs U_lo and uexp");
   FFS_REQUIRE(!o->U_hi || (d->ld_u >= d->T && d->ld_u % 8 == 0),
               "ffs_grid_build_noalloc: ld_u=%d must be >= T and a multiple of 8", d->ld_u);

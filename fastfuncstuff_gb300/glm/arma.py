@@ -20,8 +20,8 @@ and lambda in float64, no std scaling: the likelihood is that of the raw data)
 and returns float64 tensors; the arithmetic is this build's (FP64 factors,
 fp32 / split-bf16 voxel work).
 
-Options outside this path (OLS side fits, ``dsort``, ``column_sets``, global
-ARMA estimation, AFNI-faithful banded covariances) raise NotImplementedError.
+Options outside this path (OLS side fits, ``dsort``, global ARMA estimation,
+AFNI-faithful banded covariances) raise NotImplementedError.
 """
 
 from __future__ import annotations
@@ -269,8 +269,6 @@ def fit_glm_arma11(
         _unsupported("the OLS side fit (want_ols)")
     if dsort is not None or want_dsort_nods:
         _unsupported("voxelwise regressors (dsort)")
-    if column_sets:
-        _unsupported("column_sets")
     if not estimate_per_voxel:
         _unsupported("global ARMA estimation (estimate_per_voxel=False)")
     if _REML_MODE.afni_faithful:
@@ -307,6 +305,10 @@ def fit_glm_arma11(
             rows.append(g.reshape(-1))
         glt = np.stack(rows)
     ti = list(task_indices) if task_indices else None
+    sets = None
+    if column_sets:
+        sets = engine.column_sets_plan(column_sets, _group_designs[0].cpu().numpy() if _group_designs is not None
+                                       else X.numpy())
     layout = run_layout(T, run_starts, tau)
     lj = ljung_box_plan(T, K, run_starts, tau) if want_ljung_box else None
 
@@ -323,7 +325,7 @@ def fit_glm_arma11(
             raise ValueError(f"precomputed_arma_params must have shape ({V}, 2), got {tuple(pa.shape)}")
         pairs, inv = np.unique(pa.numpy().astype(np.float32), axis=0, return_inverse=True)
         grid = grid_of_pairs(pairs[:, 0], pairs[:, 1], use_double=use_double)
-        factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt, with_tc=False)
+        factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt, with_tc=False, sets=sets)
         best_all = torch.from_numpy(inv.reshape(-1).astype(np.int32))
         crit_all = None
     else:
@@ -346,7 +348,7 @@ def fit_glm_arma11(
         # grouped fit (fit_glm_arma11_grouped): every design's factors in one
         # grid build, every voxel against its own design in one pass per stage
         Xs, gid = _group_designs
-        factors = engine.build_factors(Xs, grid, layout, task_indices=ti, glt=glt, with_tc=True)
+        factors = engine.build_factors(Xs, grid, layout, task_indices=ti, glt=glt, with_tc=True, sets=sets)
         slots = engine.design_slots(gid, Xs.shape[0], K, P, device)
         bs = V
     if factors is None and not use_graph:
@@ -355,7 +357,7 @@ def fit_glm_arma11(
         overlap = K <= engine.BASIS_MAX_K
         side = _side_stream(device) if overlap else None
         factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt,
-                                       with_tc=projector == "tc" and K <= 256, stream=side)
+                                       with_tc=projector == "tc" and K <= 256, stream=side, sets=sets)
         if overlap:
             built = torch.cuda.Event()
             built.record(side)
@@ -366,7 +368,8 @@ def fit_glm_arma11(
                 main.wait_event(built)
     keep = [] if return_device else None
     chunks = {k: [] for k in ("best", "crit", "surf", "betas", "tstats", "sigma2", "fstats", "r2", "lam",
-                              "cb", "ct", "resid", "resid_w", "pred", "lb")}
+                              "cb", "ct", "resid", "resid_w", "pred", "lb", "scale")}
+    factors_used = factors
     proj = projector if (projector != "tc" or factors is None or factors.U_hi is not None) else "simt"
     if proposal is not None and best_all is None:
         from . import learned
@@ -382,8 +385,9 @@ def fit_glm_arma11(
                                      do_scale=not use_double,
                                      gls_kw=dict(want_residuals=want_residuals, want_predicted=want_predicted),
                                      factor_kw=dict(task_indices=ti, glt=glt,
-                                                    with_tc=projector == "tc" and K <= 256))
+                                                    with_tc=projector == "tc" and K <= 256, sets=sets))
             lo, go = plan.run(Yb, Xd)
+            factors_used = plan.f
             best, scale = lo.best, lo.scale
             chunks["best"].append(best)
             chunks["crit"].append(lo.best_crit)
@@ -438,6 +442,8 @@ def fit_glm_arma11(
         if go is None:
             go = engine.gls(Yb, scale, best, factors, Xd, want_residuals=want_residuals,
                             want_predicted=want_predicted, lj=lj)
+        if sets is not None:
+            chunks["scale"].append(scale)
         for name, t in (("betas", go.betas), ("tstats", go.tstats), ("sigma2", go.sigma2),
                         ("fstats", go.fstats), ("r2", go.r2), ("lam", go.lam), ("cb", go.cbeta),
                         ("ct", go.ct), ("resid", go.resid), ("resid_w", go.resid_w), ("pred", go.pred),
@@ -489,6 +495,12 @@ def fit_glm_arma11(
         if want_r2_semipartial:
             rem = torch.clamp(1.0 - cat("r2").to(ct.dtype)[:, None], min=0.0)
             res.contrast_r2_semipartial = out(ct**2 / (ct**2 + dof) * rem)
+    if sets is not None:
+        # the column sets' Wald F, temporal SD and coefficient (NaN for a set
+        # outside the design), fastfuncstuff/glm/arma.py:3564-3586
+        F, sd, coef = engine.set_stats(betas, cat("sigma2"), cat("scale"), best, factors_used,
+                                       design=slots.design if slots is not None else None)
+        res.set_fstats, res.set_sd, res.set_coef = out(F), out(sd), out(coef)
     if want_residuals:
         res.residuals = out(cat("resid"))
         res.residuals_whitened = out(cat("resid_w"))

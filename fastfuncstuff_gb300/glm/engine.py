@@ -168,6 +168,8 @@ class GridFactors:
     center_flag: torch.Tensor | None = None  # device int32[1]: centre the voxels (constant in span(X))
     uexp: torch.Tensor | None = None
     n_designs: int = 1  # > 1: design-dependent factors are [n_designs * P] (design-major)
+    Fsets: torch.Tensor | None = None  # [n_designs * P][msum] column-set blocks
+    sets: "ColumnSets | None" = None
 
     @property
     def P(self) -> int:
@@ -208,10 +210,104 @@ def constant_in_span(X: np.ndarray, tol: float = 1e-6) -> bool:
     return constant_coefficients(X, tol) is not None
 
 
+@dataclass
+class ColumnSets:
+    """The column sets of a fit (the reference's ``column_sets``) laid out for
+    the kernels: the sets whose columns all lie in the design, as offsets
+    (set_ptr) into one index list (set_idx), each with its output column
+    (set_col); the other sets' statistics stay NaN. ``C`` [n_designs][msum]
+    holds each set's Xc_S' Xc_S / T (Xc the column-centred design) block."""
+
+    n_out: int
+    set_ptr: np.ndarray
+    set_idx: np.ndarray
+    set_col: np.ndarray
+    C: np.ndarray
+
+    @property
+    def n_sets(self) -> int:
+        return len(self.set_col)
+
+    @property
+    def msum(self) -> int:
+        q = np.diff(self.set_ptr)
+        return int((q * q).sum())
+
+    def key(self) -> bytes:
+        return b"|".join(a.tobytes() for a in (np.array([self.n_out]), self.set_ptr, self.set_idx, self.set_col))
+
+    def device_arrays(self, dev):
+        return const_dev(self.set_ptr.astype(np.int32), dev), const_dev(self.set_idx.astype(np.int32), dev)
+
+
+def column_sets_plan(column_sets, designs) -> ColumnSets:
+    """``column_sets`` (lists of column indices) against the design(s) (T, K)
+    or (D, T, K), as fastfuncstuff/glm/arma.py:3542-3561 reads them: a set
+    naming a column >= K (or empty) has no statistics; a negative index is an
+    error."""
+    Xs = np.asarray(designs, dtype=np.float64)
+    if Xs.ndim == 2:
+        Xs = Xs[None]
+    _, T, K = Xs.shape
+    ptr, idx, col = [0], [], []
+    for g, cols in enumerate(column_sets):
+        cols = [int(c) for c in cols]
+        if any(c < 0 for c in cols):
+            raise IndexError(f"column_sets[{g}] has a negative column index: {cols}")
+        if not cols or any(c >= K for c in cols):
+            continue
+        idx.extend(cols)
+        ptr.append(len(idx))
+        col.append(g)
+    ptr, idx = np.asarray(ptr, np.int64), np.asarray(idx, np.int64)
+    blocks = []
+    for X in Xs:
+        Xc = X - X.mean(0, keepdims=True)
+        per = [(Xc[:, idx[ptr[s]:ptr[s + 1]]].T @ Xc[:, idx[ptr[s]:ptr[s + 1]]] / T).reshape(-1)
+               for s in range(len(col))]
+        blocks.append(np.concatenate(per) if per else np.zeros(0))
+    return ColumnSets(n_out=len(column_sets), set_ptr=ptr, set_idx=idx, set_col=np.asarray(col, np.int64),
+                      C=np.stack(blocks).astype(np.float32))
+
+
+def set_stats(betas: torch.Tensor, sigma2: torch.Tensor, scale: torch.Tensor, best: torch.Tensor,
+              f: GridFactors, design: torch.Tensor | None = None):
+    """(set_fstats, set_sd, set_coef) [V][n_out] of the fitted voxels (betas
+    [V][K] of every column and sigma2 as ``gls`` returns them, unscaled; best
+    the pair of each voxel; ``design`` each voxel's design in a grouped fit).
+    NaN where a set names a column outside the design."""
+    cs = f.sets
+    V = betas.shape[0]
+    dev = betas.device
+    out = [torch.full((V, cs.n_out), float("nan"), device=dev, dtype=torch.float32) for _ in range(3)]
+    if cs.n_sets == 0 or V == 0:
+        return tuple(out)
+    lib = _lib.load()
+    ptr, idx = cs.device_arrays(dev)
+    col = const_dev(cs.set_col.astype(np.int32), dev)
+    Cd = const_dev(cs.C, dev)
+    bst = best.to(device=dev, dtype=torch.int32).contiguous()
+    dsg = design.to(device=dev, dtype=torch.int32).contiguous() if design is not None else None
+    b = betas.to(torch.float32).contiguous()
+    s2 = sigma2.to(torch.float32).contiguous()
+    sc = scale.to(torch.float32).contiguous()
+    a = _lib.SetStatsArgs(V=V, K=b.shape[1], n_sets=cs.n_sets, n_out=cs.n_out, set_ptr=_p(ptr), set_idx=_p(idx),
+                          set_col=_p(col), msum=cs.msum, Fsets=_p(f.Fsets), Csets=_p(Cd), best=_p(bst),
+                          design=_p(dsg), n_pairs=f.P if dsg is not None else 0, betas=_p(b), sigma2=_p(s2),
+                          scale=_p(sc), set_fstats=_p(out[0]), set_sd=_p(out[1]), set_coef=_p(out[2]))
+    _run("ffs_reml_set_stats", lib.ffs_reml_set_stats, C.byref(a), _stream())
+    out[0]._keep = (ptr, idx, col, Cd, bst, dsg, b, s2, sc)
+    return tuple(out)
+
+
 def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_indices=None,
                   glt: np.ndarray | None = None, with_tc: bool = True, center=None,
-                  stream: torch.cuda.Stream | None = None, max_ctas: int = 0) -> GridFactors:
+                  stream: torch.cuda.Stream | None = None, max_ctas: int = 0,
+                  sets: ColumnSets | None = None) -> GridFactors:
     """Run the FP64 grid build for design ``X`` (T, K) on its device.
+
+    ``sets`` (``column_sets_plan``) adds each column set's inv(A_SS + 1e-8 I)
+    per pair (``Fsets``) for ``set_stats``.
 
     ``center`` = (flag, coefficients) from ``constant_flag(X)`` when the caller
     has them already (the CUDA-graph plan computes them outside its capture).
@@ -271,13 +367,22 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
         uexp=torch.empty(DP, dtype=torch.int32, device=dev) if with_tc else None,
         n_designs=D,
     )
+    if sets is not None and sets.n_sets:
+        f.sets = sets
+        f.Fsets = torch.empty(DP, sets.msum, **f32)
+        sets_dev = sets.device_arrays(dev)
+    else:
+        sets_dev = (None, None)
     d = _lib.GridDesc(T=T, K=K, P=P, n_runs=layout.n_runs, run_start=_p(run_start), tau=_p(tau),
                       a=_p(a), b=_p(b), X=_p(Xc), lambda_fp32=0, ld_u=ld,
-                      n_task=nt, task_idx=_p(task_idx), n_glt=ng, glt=_p(glt_t))
+                      n_task=nt, task_idx=_p(task_idx), n_glt=ng, glt=_p(glt_t),
+                      n_sets=sets.n_sets if f.Fsets is not None else 0, set_ptr=_p(sets_dev[0]),
+                      set_idx=_p(sets_dev[1]))
     # no Gsum from the kernel: G'1 is the FP64 coefficient vector of the constant (set below)
     o = _lib.GridOut(coef=_p(f.coef), logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), U=_p(f.U),
                      U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), uexp=_p(f.uexp), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
-                     info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=None, work=_p(work))
+                     info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=None, work=_p(work),
+                     Fsets=_p(f.Fsets))
     def launch():
         if single:
             _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
@@ -296,7 +401,7 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     # span(X): the centring correction of the GLS uses the FP64 coefficients
     # rather than sums of the fp32 G (the flag decides on the device)
     f.Gsum = ccoef.reshape(D, 1, K).expand(D, P, K).reshape(DP, K).contiguous()
-    f._keep = (Xc, run_start, tau, work)  # inputs must outlive the launch
+    f._keep = (Xc, run_start, tau, work, sets_dev)  # inputs must outlive the launch
     return f
 
 

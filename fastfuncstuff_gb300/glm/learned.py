@@ -596,7 +596,8 @@ _GRAPHS: dict = {}
 
 def graph_for(Y, X, grid, layout, proposal, *, recenter, do_scale, gls_kw, factor_kw) -> LearnedFitGraph:
     """The cached LearnedFitGraph of this shape and these options (built on first use)."""
-    fk = tuple((k, None if v is None else np.asarray(v).tobytes()) for k, v in sorted(factor_kw.items()))
+    fk = tuple((k, None if v is None else v.key() if hasattr(v, "key") else np.asarray(v).tobytes())
+               for k, v in sorted(factor_kw.items()))
     key = (tuple(Y.shape), tuple(X.shape), str(Y.device), grid.a.tobytes(), grid.b.tobytes(), grid.lambda_fp32,
            layout.run_start.tobytes(), layout.tau.tobytes(), id(proposal.params), proposal.params._version,
            recenter, do_scale, tuple(sorted(gls_kw.items())), fk)

@@ -75,6 +75,9 @@ const char* ffs_last_error(void);
  *   Ftask[p]     = inv(A_task + 1e-8 I) for the task-column F statistic
  *                  (fastfuncstuff/glm/arma.py:4891-4898), A = (X_w'X_w)^-1.
  *   glt_var[p][c]= c A c' for each single-row GLT c (arma.py:5455-5466).
+ *   Fsets[p]     = inv(A_SS + 1e-8 I) of every column set S (the column_sets
+ *                  Wald F, arma.py:3542-3561), the sets' q_S x q_S blocks one
+ *                  after another ([P][sum q_S^2]).
  *   info[p]      = 0 Cholesky of X_w'X_w, 1 QR fallback used (the design is
  *                  rank deficient at this pair), 2 a pivot of R's factor was
  *                  not positive.
@@ -93,6 +96,9 @@ typedef struct {
   const int* task_idx;  /* device [n_task]                                       */
   int n_glt;            /* single-row GLT contrasts                              */
   const float* glt;     /* device [n_glt][K]                                     */
+  int n_sets;           /* column sets for Fsets (0: none)                       */
+  const int* set_ptr;   /* device [n_sets + 1]: set s is set_idx[set_ptr[s] ..]  */
+  const int* set_idx;   /* device [set_ptr[n_sets]] column indices (< K)         */
 } ffs_grid_desc;
 
 typedef struct {
@@ -111,6 +117,7 @@ typedef struct {
   float* glt_var;       /* [P][n_glt] c A c', or NULL                             */
   float* Gsum;          /* [P][K] G' 1: the betas of the constant series          */
   double* work;         /* scratch, ffs_grid_work_bytes() bytes                   */
+  float* Fsets;         /* [P][sum q_S^2] (with n_sets), or NULL                  */
 } ffs_grid_out;
 
 size_t ffs_grid_work_bytes(int T, int K, int P);
@@ -355,6 +362,37 @@ typedef struct {
 } ffs_gls_args;
 
 int ffs_reml_gls(const ffs_gls_args* a, void* stream);
+
+/* Column-set statistics of every voxel after the GLS (the reference's
+ * -nuisance_summary sets, fastfuncstuff/glm/arma.py:3564-3586, unscaled at
+ * :5845-5848): with b the betas of the scaled series (betas / scale[v]) and
+ * s2 = sigma2 / scale[v]^2,
+ *   F    = b_S' Fsets b_S / (q_S s2 + 1e-30),
+ *   sd   = sqrt(max(b_S' Csets b_S, 0)) * scale[v]  (temporal SD of X_S b_S),
+ *   coef = betas[v][S_0] for a one-column set, else NaN.
+ * Set s writes column set_col[s] of the [V][n_out] outputs; the caller fills
+ * the other columns (sets naming a column outside the design) with NaN.
+ */
+typedef struct {
+  int V, K, n_sets, n_out;
+  const int* set_ptr;     /* device [n_sets + 1]                                  */
+  const int* set_idx;     /* device [set_ptr[n_sets]]                             */
+  const int* set_col;     /* device [n_sets] output column of each set            */
+  int msum;               /* sum of q_S^2                                         */
+  const float* Fsets;     /* [keys][msum] from the grid build                     */
+  const float* Csets;     /* [n_designs][msum] Xc_S' Xc_S / T, Xc the column-     */
+                          /*   centred design                                     */
+  const int* best;        /* [V] pair of each voxel                               */
+  const int* design;      /* [V] design of each voxel (grouped fits) or NULL:     */
+                          /*   key = design * n_pairs + pair                      */
+  int n_pairs;
+  const float* betas;     /* [V][K] every column, unscaled (ffs_reml_gls)         */
+  const float* sigma2;    /* [V] unscaled                                         */
+  const float* scale;     /* [V]                                                  */
+  float* set_fstats; float* set_sd; float* set_coef;  /* [V][n_out]              */
+} ffs_set_stats_args;
+
+int ffs_reml_set_stats(const ffs_set_stats_args* a, void* stream);
 
 /* ffs_reml_gls plus the Ljung-Box statistic of each voxel's whitened residual
  * (fastfuncstuff/glm/arma.py:6058-6141, AFNI ljung_box_uneven): lj_h is the

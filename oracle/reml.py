@@ -620,12 +620,56 @@ class Results:
     contrast_betas: np.ndarray = None
     contrast_tstats: np.ndarray = None
     r2_partial: np.ndarray = None
+    set_fstats: np.ndarray = None
+    set_sd: np.ndarray = None
+    set_coef: np.ndarray = None
     reml_lklhd_surface: np.ndarray = None
     extra: dict = field(default_factory=dict)
 
 
+def column_set_matrices(A: np.ndarray, X: np.ndarray, column_sets):
+    """Per column set: (indices, inv(A_SS + 1e-8 I), Xc_S' Xc_S / T) with A =
+    (X_w'X_w)^-1 of one (a, b) and Xc the column-centred unwhitened design;
+    None for a set naming a column outside the design (or an empty set).
+    Follows fastfuncstuff/glm/arma.py:3542-3561."""
+    K, T = X.shape[1], X.shape[0]
+    Xc = X - X.mean(0, keepdims=True)
+    out = []
+    for cols in column_sets:
+        keep = [c for c in cols if c < K]
+        if len(keep) != len(cols) or not keep:
+            out.append(None)
+            continue
+        ix = np.asarray(keep)
+        M = np.linalg.inv(A[np.ix_(ix, ix)] + 1e-8 * np.eye(len(ix), dtype=A.dtype))
+        Xs = Xc[:, ix]
+        out.append((ix, M, Xs.T @ Xs / T))
+    return out
+
+
+def column_set_stats(beta: np.ndarray, sigma2: np.ndarray, mats):
+    """(F, SD, coef) per voxel and set of the betas and sigma2 of the scaled
+    data: F = b_S' M b_S / (q sigma2 + 1e-30), SD = sqrt(max(b_S' C b_S, 0)),
+    coef = b for a one-column set; NaN where a set is absent (coef: or wider).
+    Follows fastfuncstuff/glm/arma.py:3564-3586."""
+    V, G = beta.shape[0], len(mats)
+    F = np.full((V, G), np.nan, beta.dtype)
+    sd = np.full((V, G), np.nan, beta.dtype)
+    coef = np.full((V, G), np.nan, beta.dtype)
+    for g, m in enumerate(mats):
+        if m is None:
+            continue
+        ix, M, C = m
+        b = beta[:, ix]
+        F[:, g] = np.einsum("vi,ij,vj->v", b, M, b) / (len(ix) * sigma2 + 1e-30)
+        sd[:, g] = np.sqrt(np.maximum(np.einsum("vi,ij,vj->v", b, C, b), 0.0))
+        if len(ix) == 1:
+            coef[:, g] = b[:, 0]
+    return F, sd, coef
+
+
 def gls_at(Xd, Y, whitener: Whitener, dof: int, task_indices=None, glt=None, want_resid=False,
-           lj=None):
+           lj=None, column_sets=None):
     """GLS refit of voxels that share one (a, b).
 
     Follows fastfuncstuff/glm/arma.py:4853-4905 (group constants: X_w'X_w,
@@ -677,6 +721,8 @@ def gls_at(Xd, Y, whitener: Whitener, dof: int, task_indices=None, glt=None, wan
         out["pred"] = pred
     if lj is not None:
         out["lb"] = ljung_box(rw, lj[0], lj[1])
+    if column_sets:
+        out["sets"] = column_set_stats(beta, sigma2, column_set_matrices(A, Xd, column_sets))
     return out
 
 
@@ -685,7 +731,7 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
                    task_indices=None, glt_matrices=None, want_residuals=False,
                    want_ljung_box=False, save_profile_likelihoods=False,
                    precomputed_arma_params=None, fp64_scaled=False, afni_faithful=False,
-                   autocorr=None, subset_descent=False):
+                   autocorr=None, subset_descent=False, column_sets=None):
     """The reference's ``fit_glm_arma11`` for the options this path covers.
 
     Follows fastfuncstuff/glm/arma.py:3650-5878 on ``device=cpu``:
@@ -784,6 +830,10 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
         lj = (h, build_ljung_box_tau(T, run_starts, tau))
         res.ljung_box = np.zeros(V, F32)
         res.ljung_box_dof = max(1, resolve_ljung_box_lag(T, h) - 2)
+    if column_sets:
+        res.set_fstats = np.full((V, len(column_sets)), np.nan, dt)
+        res.set_sd = np.full((V, len(column_sets)), np.nan, dt)
+        res.set_coef = np.full((V, len(column_sets)), np.nan, dt)
     if glt_matrices is not None:
         C = np.stack([np.asarray(c, dtype=dt).reshape(-1) for c in glt_matrices])
         res.contrast_betas = np.zeros((V, C.shape[0]), dt)
@@ -804,7 +854,7 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
             wh = pre.whiteners[int(idx[members[0]])]
         else:
             wh = arma11_whiteners(one, T, run_starts, tau, dt)[0][0]
-        o = gls_at(X, Ys[members], wh, dof, task_indices, C, want_residuals, lj)
+        o = gls_at(X, Ys[members], wh, dof, task_indices, C, want_residuals, lj, column_sets)
         ti = list(task_indices) if task_indices else slice(None)
         res.betas[members] = o["beta"][:, ti]
         res.tstats[members] = o["t"][:, ti]
@@ -821,12 +871,17 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
             res.predicted[members] = o["pred"]
         if lj is not None:
             res.ljung_box[members] = o["lb"]
+        if column_sets:
+            res.set_fstats[members], res.set_sd[members], res.set_coef[members] = o["sets"]
     if scale is not None:
         s = scale.astype(dt)
         res.betas *= s[:, None]
         res.sigma2 *= s**2
         if res.contrast_betas is not None:
             res.contrast_betas *= s[:, None]
+        if column_sets:  # fastfuncstuff/glm/arma.py:5845-5848
+            res.set_sd *= s[:, None]
+            res.set_coef *= s[:, None]
         if want_residuals:
             res.residuals *= s[:, None]
             res.residuals_whitened *= s[:, None]

@@ -20,10 +20,12 @@ Cases (all on ``device=cpu``):
 * ``baseline`` a raw 1000-baseline series (the conditioning test's shape)
 * ``ljung``    the reference test-suite's Ljung-Box series and AFNI golden values
 * ``grid``     logdet(R), logdet(X_w'X_w), X_w and Q of a small precompute
+* ``sets``     column_sets (Wald F, temporal SD and coefficient of each set),
+               two runs, one set naming a column outside the design
 
 Each fit is run in four reference modes: FP64 exhaustive, FP64 default
 (hierarchical), float32 default and float32 exhaustive, with the likelihood
-surface saved where the reference offers it.
+surface saved where the reference offers it. ``--only NAME`` writes one case.
 """
 
 from __future__ import annotations
@@ -94,7 +96,7 @@ def _case(seed, lens, p_task=2, V=240, censor=None, baseline=0.0):
     return X.astype(np.float32), Y.astype(np.float32), keep
 
 
-def main(ref_root: str) -> None:
+def main(ref_root: str, only: str | None = None) -> None:
     tmp = Path(tempfile.mkdtemp(prefix="ffs_stub_"))
     _stub_nibabel(tmp)
     sys.path[:0] = [str(tmp), ref_root]
@@ -140,6 +142,25 @@ def main(ref_root: str) -> None:
             if r.ljung_box_dof is not None:
                 out[f"{name}__ljung_box_dof"] = np.array(r.ljung_box_dof)
         return out
+
+    # column sets: Wald F, SD and coefficient per set (one set is outside the
+    # design, so its statistics are NaN)
+    X, Y, _ = _case(19, [64, 64], p_task=3, V=160)
+    sets = [[0], [0, 1], [2, 3, 4], [1, 99], [5]]
+    kw = dict(a_grid=g17, b_grid=g17, run_starts=[0, 64], column_sets=sets)
+    out = {}
+    for name, extra in {"f64_def": dict(use_double=True), "f32_def": dict(),
+                        "f32_exh": dict(force_exhaustive_search=True)}.items():
+        r = fit_glm_arma11(torch.from_numpy(Y), torch.from_numpy(X), tr=2.0, device=cpu, verbose=False,
+                           **extra, **kw)
+        for attr in ("betas", "sigma2", "arma_params", "set_fstats", "set_sd", "set_coef"):
+            out[f"{name}__{attr}"] = getattr(r, attr).numpy()
+    np.savez_compressed(OUT / "sets.npz", X=X, Y=Y, a_grid=g17.numpy(), b_grid=g17.numpy(),
+                        run_starts=np.array([0, 64]), set_ptr=np.cumsum([0] + [len(c) for c in sets]),
+                        set_idx=np.concatenate([np.asarray(c) for c in sets]), **out)
+    if only == "sets":
+        print("wrote", OUT / "sets.npz")
+        return
 
     # single run
     X, Y, _ = _case(11, [96])
@@ -246,4 +267,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FFS_REFERENCE", "."))
+    args = [a for a in sys.argv[1:] if not a.startswith("--only")]
+    only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
+    main(args[0] if args else os.environ.get("FFS_REFERENCE", "."), only)

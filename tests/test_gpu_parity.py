@@ -271,6 +271,50 @@ def test_design_basis_centring_test_matches_normal_equations():
             np.testing.assert_allclose(Q.T @ Q, np.eye(Q.shape[1]), atol=1e-5)
 
 
+@pytest.mark.parametrize("exhaustive", [True, False])
+def test_column_sets_match_oracle_and_reference(exhaustive):
+    """column_sets on the device (per-pair inv(A_SS + 1e-8 I) from the grid
+    build, per-voxel F / SD / coefficient after the GLS) against the FP64
+    oracle on the float32 mode's semantics, and against the reference's own
+    float32 outputs on the voxels whose pair agrees; the set naming a column
+    outside the design stays NaN."""
+    d = load_golden("sets")
+    kw = case_kwargs(d)
+    ref = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, fp64_scaled=True, force_exhaustive_search=exhaustive,
+                           save_profile_likelihoods=True, **kw)
+    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=PROJ,
+                         force_exhaustive_search=exhaustive, **kw)
+    grid = G.make_grid(d["a_grid"], d["b_grid"])
+    idx = _index(got.arma_params.numpy(), grid)
+    check_selection(idx, ref.arma_index, ref.reml_lklhd_surface)
+    same = idx == ref.arma_index
+
+    def check_sets(g, r, betas_ref, bound):
+        # the set statistics inherit the betas' error, which is bounded
+        # relative to each voxel's largest beta (t's to its largest t): F
+        # through sqrt(F) (a t-like scale), per voxel over the sets; SD and
+        # coefficient against the voxel's largest |beta|
+        for name in ("set_fstats", "set_sd", "set_coef"):
+            np.testing.assert_array_equal(np.isnan(g[name]), np.isnan(r[name]), err_msg=name)
+        ok = ~np.isnan(r["set_fstats"][0])
+        assert rel_maxnorm(np.sqrt(g["set_fstats"][:, ok]), np.sqrt(r["set_fstats"][:, ok])).max() <= bound
+        scale = np.abs(betas_ref).max(1)
+        for name in ("set_sd", "set_coef"):
+            col = ~np.isnan(r[name][0])
+            err = np.abs(g[name][:, col] - r[name][:, col]).max(1) / scale
+            assert err.max() <= bound, (name, err.max())
+
+    fields = ("set_fstats", "set_sd", "set_coef")
+    check_sets({k: getattr(got, k).numpy()[same] for k in fields}, {k: getattr(ref, k)[same] for k in fields},
+               ref.betas[same], 2 * BETA_REL)
+    # the reference's own float32 run, on the voxels whose pair agrees
+    mode = "f32_exh" if exhaustive else "f32_def"
+    agree = (got.arma_params.numpy() == d[mode + "__arma_params"]).all(1)
+    assert agree.mean() >= 0.97
+    check_sets({k: getattr(got, k).numpy()[agree] for k in fields}, {k: d[f"{mode}__{k}"][agree] for k in fields},
+               d[mode + "__betas"][agree], 2e-3)
+
+
 @pytest.mark.parametrize("T,K", [(400, 20), (201, 7), (300, 70), (300, 200)])
 def test_design_basis_equals_grid_build_identity_pair(T, K):
     """Q0 of the design-basis kernels is U of the pair (0, 0) bit for bit (the
@@ -309,7 +353,8 @@ def test_grouped_batched_fit_equals_per_group_fits(selector):
     designs = {h: w.designs[h] for h in range(6)}
     kw = dict(a_grid=np.linspace(-0.8, 0.8, 17), b_grid=np.linspace(-0.8, 0.8, 17), run_starts=w.run_starts,
               tau=w.tau, device=DEV, verbose=False, force_exhaustive_search=selector == "exhaustive",
-              want_residuals=True, glt_labels=["t0-t1"], glt_matrices=[np.eye(18)[0] - np.eye(18)[1]])
+              want_residuals=True, glt_labels=["t0-t1"], glt_matrices=[np.eye(18)[0] - np.eye(18)[1]],
+              column_sets=[[0], [0, 1], [2, 3, 4, 5], [17, 18]])
     got = fit_glm_arma11_grouped(Y, designs, gid, tr=2.0, **kw)
     for h in range(6):
         m = gid == h
@@ -317,7 +362,7 @@ def test_grouped_batched_fit_equals_per_group_fits(selector):
         np.testing.assert_array_equal(got.arma_params.numpy()[m], ref.arma_params.numpy())
         np.testing.assert_array_equal(got.reml_likelihood.numpy()[m], ref.reml_likelihood.numpy())
         for name in ("betas", "tstats", "sigma2", "fstats", "r2", "arma_lambda", "contrast_betas",
-                     "contrast_tstats", "residuals", "residuals_whitened"):
+                     "contrast_tstats", "residuals", "residuals_whitened", "set_fstats", "set_sd", "set_coef"):
             np.testing.assert_array_equal(getattr(got, name).numpy()[m], getattr(ref, name).numpy(), err_msg=name)
 
 

@@ -223,3 +223,31 @@ def test_design_slots_layout():
         cover[v0 // 128, slot0:slot0 + npr] += 1
     assert (cover == 1).all()
 
+
+
+def test_column_sets_plan_layout_and_blocks():
+    """column_sets as the kernels read them: sets inside the design packed
+    (offsets, indices, output columns), sets naming a column >= K or empty left
+    out (their statistics stay NaN), each set's Xc_S' Xc_S / T block per
+    design; a negative index is an error, as index_select makes it in the
+    reference (fastfuncstuff/glm/arma.py:3542-3561)."""
+    from fastfuncstuff_gb300.glm import engine
+
+    d = load_golden("sets")
+    X = d["X"].astype(np.float64)
+    sets = [[0], [0, 1], [2, 3, 4], [1, 99], [5], []]
+    cs = engine.column_sets_plan(sets, d["X"])
+    assert cs.n_out == 6 and cs.n_sets == 4
+    np.testing.assert_array_equal(cs.set_col, [0, 1, 2, 4])
+    np.testing.assert_array_equal(cs.set_ptr, [0, 1, 3, 6, 7])
+    np.testing.assert_array_equal(cs.set_idx, [0, 0, 1, 2, 3, 4, 5])
+    assert cs.msum == 1 + 4 + 9 + 1
+    Xc = X - X.mean(0)
+    mats = o.column_set_matrices(np.eye(X.shape[1]), X, [s for s in sets if s and max(s) < X.shape[1]])
+    ref = np.concatenate([m[2].reshape(-1) for m in mats])
+    np.testing.assert_allclose(cs.C[0], ref, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(cs.C[0][:1], [(Xc[:, 0] ** 2).mean()], rtol=1e-6)
+    two = engine.column_sets_plan(sets, np.stack([d["X"], 2 * d["X"]]))
+    np.testing.assert_allclose(two.C[1], 4 * two.C[0], rtol=1e-6)
+    with pytest.raises(IndexError):
+        engine.column_sets_plan([[0, -1]], d["X"])

@@ -30,6 +30,9 @@ def case_kwargs(d) -> dict:
     if "task_indices" in d:
         args.update(task_indices=list(d["task_indices"]), glt_matrices=[d["glt"][0]],
                     want_ljung_box=True, want_residuals=True)
+    if "set_ptr" in d:
+        ptr, idx = d["set_ptr"], d["set_idx"]
+        args["column_sets"] = [[int(c) for c in idx[ptr[g]:ptr[g + 1]]] for g in range(len(ptr) - 1)]
     return args
 
 
@@ -147,6 +150,29 @@ def test_fp32_mode_matches_reference(case):
         same = (r.arma_params == d[mode + "__arma_params"]).all(1)
         _close(r.betas[same], d[mode + "__betas"][same], rtol=2e-3, atol=2e-3)
         _close(r.reml_likelihood[same], d[mode + "__reml_likelihood"][same], rtol=1e-5, atol=1e-3)
+
+
+def test_column_sets_match_reference():
+    """column_sets (fastfuncstuff/glm/arma.py:3542-3586, unscaled at :5845-5848):
+    the Wald F, temporal SD and one-column coefficient of each set, NaN for the
+    set that names a column outside the design; FP64 and float32 modes."""
+    d = load_golden("sets")
+    r = _fit(d, use_double=True)
+    np.testing.assert_array_equal(r.arma_params, d["f64_def__arma_params"])
+    for name in ("set_fstats", "set_sd", "set_coef"):
+        ref = d["f64_def__" + name]
+        got = getattr(r, name)
+        np.testing.assert_array_equal(np.isnan(got), np.isnan(ref), err_msg=name)
+        _close(np.nan_to_num(got), np.nan_to_num(ref), rtol=1e-7, atol=1e-9)
+    for mode, kw in (("f32_def", {}), ("f32_exh", dict(force_exhaustive_search=True))):
+        r = _fit(d, use_double=False, **kw)
+        same = (r.arma_params == d[mode + "__arma_params"]).all(1)
+        assert same.mean() >= 0.97, (mode, same.mean())
+        for name in ("set_fstats", "set_sd", "set_coef"):
+            ref = d[f"{mode}__{name}"][same]
+            got = getattr(r, name)[same]
+            np.testing.assert_array_equal(np.isnan(got), np.isnan(ref), err_msg=name)
+            _close(np.nan_to_num(got), np.nan_to_num(ref), rtol=2e-3, atol=2e-3)
 
 
 def test_fp64_scaled_oracle_tracks_fp32_reference():
