@@ -408,3 +408,33 @@ def test_workload0_subset_parity_exhaustive_and_hierarchical():
         idx = _index(got.arma_params.numpy(), G.make_grid(g, g))
         agree = check_selection(idx, ref_idx, surf)
         print(f"workload0 exhaustive={exhaustive}: agreement {agree:.5f}")
+
+
+def test_rvar_round_trip_reuses_the_fitted_pairs(tmp_path):
+    """fit -> -Rvar file -> load_arma_params -> fit with precomputed_arma_params:
+    the second fit reuses the first's (a, b) and reproduces its GLS; the file's
+    StDev, -LogLik and LjungBox volumes are the first fit's."""
+    from fastfuncstuff_gb300 import load_arma_params, save_arma_rvar
+
+    d = load_golden("multirun")
+    kw = case_kwargs(d)
+    kw["glt_labels"] = ["c0"]
+    first = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=PROJ, **kw)
+    V = d["Y"].shape[0]
+    mask = np.zeros(V + 7, bool)
+    mask[3:3 + V] = True
+    path = save_arma_rvar(first, tmp_path / "rvar.nii.gz", volume_shape=(V + 7, 1, 1), voxel_mask=mask)
+    ab = load_arma_params(path, mask)
+    np.testing.assert_array_equal(ab, first.arma_params.numpy())
+    again = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=PROJ,
+                           precomputed_arma_params=ab, **kw)
+    np.testing.assert_array_equal(again.arma_params.numpy(), first.arma_params.numpy())
+    assert rel_maxnorm(again.betas.numpy(), first.betas.numpy()).max() <= 1e-5
+    import gzip
+    import struct
+    raw = gzip.decompress(path.read_bytes())
+    off = int(struct.unpack_from("<f", raw, 108)[0])
+    vol = np.frombuffer(raw, np.float32, offset=off).reshape((V + 7, 1, 1, 6), order="F")[mask, 0, 0]
+    np.testing.assert_allclose(vol[:, 3], np.sqrt(first.sigma2.numpy()), rtol=1e-6)
+    np.testing.assert_array_equal(vol[:, 4], first.reml_likelihood.numpy())
+    np.testing.assert_array_equal(vol[:, 5], first.ljung_box.numpy())
