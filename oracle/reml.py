@@ -623,6 +623,8 @@ class Results:
     set_fstats: np.ndarray = None
     set_sd: np.ndarray = None
     set_coef: np.ndarray = None
+    dsort_betas: np.ndarray = None
+    dsort_tstats: np.ndarray = None
     reml_lklhd_surface: np.ndarray = None
     extra: dict = field(default_factory=dict)
 
@@ -726,12 +728,117 @@ def gls_at(Xd, Y, whitener: Whitener, dof: int, task_indices=None, glt=None, wan
     return out
 
 
+def dsort_constant_guard(D: np.ndarray) -> np.ndarray:
+    """A -dsort series that is constant and nonzero through time is replaced by
+    its dataset's mean series over the other voxels (all-zero, run-padded
+    columns are left alone). Follows fastfuncstuff/glm/arma.py:3207-3245."""
+    D = np.array(D, copy=True)
+    sd = D.astype(F64).std(2, ddof=1)
+    mean_abs = np.abs(D).astype(F64).mean(2)
+    bad = (sd < 1e-8) & (mean_abs > 1e-8)
+    for d in range(D.shape[1]):
+        if bad[:, d].any():
+            good = ~bad[:, d]
+            src = D[good, d] if good.any() else D[:, d]
+            D[bad[:, d], d] = src.mean(0)
+    return D
+
+
+def dsort_expand(D: np.ndarray, run_bounds=None) -> np.ndarray:
+    """(V, n_sets, T) -> (V, n_sets * n_runs, T) with one zero-padded column per
+    set and run when run_bounds [t0, t1, ..., T] is given (set-major, then
+    run). Follows fastfuncstuff/glm/arma.py:3385-3397."""
+    if run_bounds is None:
+        return D
+    V, n_sets, T = D.shape
+    n_runs = len(run_bounds) - 1
+    out = np.zeros((V, n_sets * n_runs, T), D.dtype)
+    for si in range(n_sets):
+        for r in range(n_runs):
+            t0, t1 = run_bounds[r], run_bounds[r + 1]
+            out[:, si * n_runs + r, t0:t1] = D[:, si, t0:t1]
+    return out
+
+
+def gls_dsort_at(Xd, Ys, D, whitener: Whitener, dof: int, task_indices=None, glt=None, lj=None,
+                 column_sets=None):
+    """The per-voxel GLS with the extended design [X | D_v] at one (a, b).
+
+    Follows fastfuncstuff/glm/arma.py:3367-3539: X_ext = [X_w | D_w]; betas
+    from the Cholesky factor of X_ext'X_ext + 1e-8 I, its inverse for the
+    standard errors; sigma2 = sum r_w^2 / dof (float64 sum); t = b/(se+1e-10);
+    R^2 of the unwhitened fit; F over the task (or all base) columns with
+    inv(A_task + 1e-8 I) and 1e-30; GLT on the base block; Ljung-Box of r_w;
+    column sets over [X | D] with the voxel's own inverse block.
+    """
+    dt = Ys.dtype
+    V, q, T = D.shape
+    K = Xd.shape[1]
+    Xw = whitener.cols(Xd)
+    Yw = whitener.rows(Ys)
+    out = {k: [] for k in ("beta", "t", "sigma2", "F", "r2", "resid", "resid_w", "pred", "cb", "ct", "lb",
+                           "sets")}
+    Xc_all = None
+    for v in range(V):
+        Dw = whitener.cols(D[v].T.astype(dt))
+        Xe = np.concatenate([Xw, Dw], 1)
+        M = Xe.T @ Xe + 1e-8 * np.eye(K + q, dtype=dt)
+        L = np.linalg.cholesky(M)
+        Li = _solve_lower(L, np.eye(K + q, dtype=dt))
+        Minv = Li.T @ Li
+        b = Minv @ (Xe.T @ Yw[v])
+        rw = Yw[v] - Xe @ b
+        s2 = dt.type((rw.astype(F64) ** 2).sum() / dof)
+        t = b / (np.sqrt(s2 * np.diagonal(Minv)) + 1e-10)
+        pred = Xd @ b[:K] + b[K:] @ D[v]
+        ti = list(task_indices) if task_indices is not None else list(range(K))
+        A = Minv[np.ix_(ti, ti)]
+        Ai = np.linalg.inv(A + 1e-8 * np.eye(len(ti), dtype=dt))
+        bt = b[ti]
+        out["F"].append(bt @ Ai @ bt / (s2 * len(ti) + 1e-30))
+        out["beta"].append(b)
+        out["t"].append(t)
+        out["sigma2"].append(s2)
+        out["r2"].append(_cod(Ys[v][None], pred[None])[0])
+        out["resid"].append(Ys[v] - pred)
+        out["resid_w"].append(rw)
+        out["pred"].append(pred)
+        if glt is not None:
+            C = np.asarray(glt, dtype=dt)
+            cb = C @ b[:K]
+            var = np.einsum("cr,rs,cs->c", C, s2 * Minv[:K, :K], C)
+            out["cb"].append(cb)
+            out["ct"].append(cb / (np.sqrt(np.maximum(var, 0.0)) + 1e-10))
+        if column_sets:
+            if Xc_all is None:
+                Xc_all = Xd - Xd.mean(0, keepdims=True)
+            Xo = np.concatenate([Xc_all, (D[v] - D[v].mean(1, keepdims=True)).T], 1)
+            F_, sd_, co_ = [], [], []
+            for cols in column_sets:
+                ix = np.asarray(cols)
+                if len(ix) == 0 or ix.max() >= K + q:
+                    F_.append(np.nan), sd_.append(np.nan), co_.append(np.nan)
+                    continue
+                bs = b[ix]
+                As = Minv[np.ix_(ix, ix)] + 1e-8 * np.eye(len(ix), dtype=dt)
+                F_.append(bs @ np.linalg.solve(As, bs) / (len(ix) * s2 + 1e-30))
+                sd_.append((Xo[:, ix] @ bs).std())
+                co_.append(bs[0] if len(ix) == 1 else np.nan)
+            out["sets"].append((F_, sd_, co_))
+    res = {k: np.asarray(v) for k, v in out.items() if v and k not in ("sets",)}
+    if lj is not None:
+        res["lb"] = ljung_box(res["resid_w"], lj[0], lj[1])
+    if column_sets:
+        res["sets"] = tuple(np.asarray([s[i] for s in out["sets"]], dt) for i in range(3))
+    return res
+
+
 def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double=True,
                    force_exhaustive_search=False, run_starts=None, tau=None,
                    task_indices=None, glt_matrices=None, want_residuals=False,
                    want_ljung_box=False, save_profile_likelihoods=False,
                    precomputed_arma_params=None, fp64_scaled=False, afni_faithful=False,
-                   autocorr=None, subset_descent=False, column_sets=None):
+                   autocorr=None, subset_descent=False, column_sets=None, dsort=None, dsort_run_bounds=None):
     """The reference's ``fit_glm_arma11`` for the options this path covers.
 
     Follows fastfuncstuff/glm/arma.py:3650-5878 on ``device=cpu``:
@@ -873,10 +980,56 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
             res.ljung_box[members] = o["lb"]
         if column_sets:
             res.set_fstats[members], res.set_sd[members], res.set_coef[members] = o["sets"]
+    if dsort is not None:
+        # the per-voxel GLS with [X | D_v] at the pairs estimated without D
+        # (fastfuncstuff/glm/arma.py:3248-3539); dof drops by the D columns
+        D = np.asarray(dsort, dtype=dt)
+        if D.ndim == 2:
+            D = D[:, None, :]
+        D = dsort_expand(dsort_constant_guard(D), dsort_run_bounds)
+        q = D.shape[1]
+        dof = max(1, T - K - q)
+        res.dof = dof
+        res.dsort_betas = np.zeros((V, q), dt)
+        res.dsort_tstats = np.zeros((V, q), dt)
+        for gi in range(pairs.shape[0]):
+            members = np.nonzero(inv == gi)[0]
+            if precomputed_arma_params is None:
+                wh = pre.whiteners[int(idx[members[0]])]
+            else:
+                one = Grid(np.array([pairs[gi, 0]], F32), np.array([pairs[gi, 1]], F32),
+                           np.array([pairs[gi, 0]], F32), np.array([pairs[gi, 1]], F32),
+                           arma_lambda_f32(np.array([pairs[gi, 0]], F32), np.array([pairs[gi, 1]], F32), dt),
+                           np.zeros(1, np.int64), np.zeros(1, np.int64))
+                wh = arma11_whiteners(one, T, run_starts, tau, dt)[0][0]
+            o = gls_dsort_at(X, Ys[members], D[members], wh, dof, task_indices, C, lj, column_sets)
+            ti = list(task_indices) if task_indices else slice(None)
+            res.betas[members] = o["beta"][:, :K][:, ti]
+            res.tstats[members] = o["t"][:, :K][:, ti]
+            res.dsort_betas[members] = o["beta"][:, K:]
+            res.dsort_tstats[members] = o["t"][:, K:]
+            res.sigma2[members] = o["sigma2"]
+            res.fstats[members] = o["F"]
+            res.r2[members] = o["r2"]
+            t2 = o["t"][:, :K] ** 2
+            res.r2_partial[members] = (t2 / (t2 + dof))[:, ti]
+            if C is not None:
+                res.contrast_betas[members] = o["cb"]
+                res.contrast_tstats[members] = o["ct"]
+            if want_residuals:
+                res.residuals[members] = o["resid"]
+                res.residuals_whitened[members] = o["resid_w"]
+                res.predicted[members] = o["pred"]
+            if lj is not None:
+                res.ljung_box[members] = o["lb"]
+            if column_sets:
+                res.set_fstats[members], res.set_sd[members], res.set_coef[members] = o["sets"]
     if scale is not None:
         s = scale.astype(dt)
         res.betas *= s[:, None]
         res.sigma2 *= s**2
+        if res.dsort_betas is not None:
+            res.dsort_betas *= s[:, None]
         if res.contrast_betas is not None:
             res.contrast_betas *= s[:, None]
         if column_sets:  # fastfuncstuff/glm/arma.py:5845-5848

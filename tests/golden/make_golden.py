@@ -22,6 +22,9 @@ Cases (all on ``device=cpu``):
 * ``grid``     logdet(R), logdet(X_w'X_w), X_w and Q of a small precompute
 * ``sets``     column_sets (Wald F, temporal SD and coefficient of each set),
                two runs, one set naming a column outside the design
+* ``dsort``    voxelwise regressors (-dsort): two datasets per voxel, and one
+               dataset expanded per run (dsort_run_bounds), with task columns,
+               a GLT, Ljung-Box, residuals and column sets over [X | D]
 
 Each fit is run in four reference modes: FP64 exhaustive, FP64 default
 (hierarchical), float32 default and float32 exhaustive, with the likelihood
@@ -143,6 +146,45 @@ def main(ref_root: str, only: str | None = None) -> None:
                 out[f"{name}__ljung_box_dof"] = np.array(r.ljung_box_dof)
         return out
 
+    # -dsort: per-voxel regressors (one smooth series correlated with the data,
+    # one independent; three voxels with a constant series that the guard
+    # replaces), then one dataset expanded per run
+    X, Y, _ = _case(20, [64, 64], p_task=2, V=120)
+    rng = np.random.default_rng(21)
+    T = X.shape[0]
+    sm = np.apply_along_axis(lambda c: np.convolve(c, np.ones(5) / 5, mode="same"), 1, rng.standard_normal((120, T)))
+    D = np.stack([0.3 * Y / Y.std(1, keepdims=True) + sm, rng.standard_normal((120, T))], 1).astype(np.float32)
+    D[:3, 1] = 2.5
+    glt = np.zeros((1, X.shape[1]), np.float32)
+    glt[0, 0], glt[0, 1] = 1.0, -1.0
+    K = X.shape[1]
+    base = dict(a_grid=g17, b_grid=g17, run_starts=[0, 64], task_indices=[0, 1], glt_labels=["t0-t1"],
+                glt_matrices=[glt], want_ljung_box=True, want_residuals=True)
+    out = {}
+    for tag, dkw, sets in (("two", dict(dsort=torch.from_numpy(D)), [[0], [K], [K, K + 1], [0, 1, K]]),
+                           ("runs", dict(dsort=torch.from_numpy(D[:, :1]), dsort_run_bounds=[0, 64, 128]),
+                            [[K], [K, K + 1], [2, 3]])):
+        for name, extra in {"f64_def": dict(use_double=True), "f32_def": dict(),
+                            "f32_exh": dict(force_exhaustive_search=True)}.items():
+            r = fit_glm_arma11(torch.from_numpy(Y), torch.from_numpy(X), tr=2.0, device=cpu, verbose=False,
+                               column_sets=sets, **base, **dkw, **extra)
+            for attr in ("betas", "tstats", "dsort_betas", "dsort_tstats", "sigma2", "fstats", "r2",
+                         "arma_params", "residuals", "residuals_whitened", "predicted", "ljung_box",
+                         "contrast_betas", "contrast_tstats", "set_fstats", "set_sd", "set_coef", "r2_partial"):
+                v = getattr(r, attr, None)
+                if attr in ("residuals", "residuals_whitened", "predicted") and name != "f64_def":
+                    continue
+                if v is not None:
+                    out[f"{tag}_{name}__{attr}"] = v.numpy()
+            out[f"{tag}_{name}__dof"] = np.array(r.dof)
+        out[f"{tag}__sets_ptr"] = np.cumsum([0] + [len(c) for c in sets])
+        out[f"{tag}__sets_idx"] = np.concatenate([np.asarray(c) for c in sets])
+    np.savez_compressed(OUT / "dsort.npz", X=X, Y=Y, D=D, glt=glt, a_grid=g17.numpy(), b_grid=g17.numpy(),
+                        run_starts=np.array([0, 64]), task_indices=np.array([0, 1]), **out)
+    if only == "dsort":
+        print("wrote", OUT / "dsort.npz")
+        return
+
     # column sets: Wald F, SD and coefficient per set (one set is outside the
     # design, so its statistics are NaN)
     X, Y, _ = _case(19, [64, 64], p_task=3, V=160)
@@ -161,6 +203,7 @@ def main(ref_root: str, only: str | None = None) -> None:
     if only == "sets":
         print("wrote", OUT / "sets.npz")
         return
+
 
     # single run
     X, Y, _ = _case(11, [96])

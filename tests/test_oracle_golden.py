@@ -263,3 +263,41 @@ def test_ljung_box_afni_golden():
 def test_ljung_box_max_lag_formula():
     assert o.ljung_box_max_lag(200, n_regressors=10, min_run=200) == 28
     assert o.ljung_box_max_lag(60, n_regressors=40, min_run=60) == 30
+
+
+@pytest.mark.parametrize("tag", ["two", "runs"])
+def test_dsort_matches_reference(tag):
+    """-dsort (fastfuncstuff/glm/arma.py:3207-3539): the per-voxel GLS with
+    [X | D_v] at the pairs estimated without D, the constant-series guard, the
+    per-run expansion of a compact dataset (dsort_run_bounds), dof T - p - q,
+    and every statistic of the extended fit, in FP64 and float32 modes."""
+    d = load_golden("dsort")
+    K = d["X"].shape[1]
+    ptr, idx = d[f"{tag}__sets_ptr"], d[f"{tag}__sets_idx"]
+    sets = [[int(c) for c in idx[ptr[g]:ptr[g + 1]]] for g in range(len(ptr) - 1)]
+    kw = dict(a_grid=d["a_grid"], b_grid=d["b_grid"], run_starts=d["run_starts"], task_indices=[0, 1],
+              glt_matrices=[d["glt"][0]], want_ljung_box=True, want_residuals=True, column_sets=sets)
+    if tag == "two":
+        kw["dsort"] = d["D"]
+    else:
+        kw.update(dsort=d["D"][:, :1], dsort_run_bounds=[0, 64, 128])
+    r = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, **kw)
+    ref = f"{tag}_f64_def__"
+    assert r.dof == int(d[ref + "dof"])
+    np.testing.assert_array_equal(r.arma_params, d[ref + "arma_params"])
+    for name, rtol, atol in (("betas", 1e-6, 1e-6), ("tstats", 1e-6, 1e-6), ("dsort_betas", 1e-6, 1e-6),
+                             ("dsort_tstats", 1e-6, 1e-6), ("sigma2", 1e-7, 0), ("fstats", 1e-6, 1e-6),
+                             ("r2", 0, 1e-7), ("residuals", 1e-6, 1e-6), ("residuals_whitened", 1e-6, 1e-6),
+                             ("ljung_box", 1e-5, 1e-5), ("contrast_betas", 1e-6, 1e-6),
+                             ("contrast_tstats", 1e-6, 1e-6)):
+        _close(getattr(r, name), d[ref + name], rtol=rtol, atol=atol)
+    for name in ("set_fstats", "set_sd", "set_coef"):
+        got, want = getattr(r, name), d[ref + name]
+        np.testing.assert_array_equal(np.isnan(got), np.isnan(want), err_msg=name)
+        _close(np.nan_to_num(got), np.nan_to_num(want), rtol=1e-6, atol=1e-7)
+    for mode, extra in (("f32_def", {}), ("f32_exh", dict(force_exhaustive_search=True))):
+        r = o.fit_glm_arma11(d["Y"], d["X"], use_double=False, **kw, **extra)
+        same = (r.arma_params == d[f"{tag}_{mode}__arma_params"]).all(1)
+        assert same.mean() >= 0.97, (mode, same.mean())
+        for name in ("betas", "dsort_betas", "sigma2"):
+            _close(getattr(r, name)[same], d[f"{tag}_{mode}__{name}"][same], rtol=2e-3, atol=2e-3)
