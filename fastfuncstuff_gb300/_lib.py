@@ -20,6 +20,7 @@ _c_double_p = C.POINTER(C.c_double)
 _c_u16_p = C.POINTER(C.c_uint16)
 
 FFS_OK, FFS_ERR_INVALID, FFS_ERR_CUDA, FFS_ERR_UNSUPPORTED, FFS_ERR_WORKSPACE, FFS_ERR_TIMEOUT = range(6)
+FFS_DSORT_QMAX = 16  # most voxelwise columns of ffs_reml_gls_dsort
 
 
 class GridDesc(C.Structure):
@@ -39,6 +40,29 @@ class GridOut(C.Structure):
         ("G", C.c_void_p),
         ("Adiag", C.c_void_p), ("XtX", C.c_void_p), ("info", C.c_void_p), ("Ftask", C.c_void_p),
         ("glt_var", C.c_void_p), ("Gsum", C.c_void_p), ("work", C.c_void_p), ("Fsets", C.c_void_p),
+        ("Afull", C.c_void_p),
+    ]
+
+
+class DsortArgs(C.Structure):
+    _fields_ = [
+        ("V", C.c_int), ("T", C.c_int), ("K", C.c_int), ("q", C.c_int), ("dof", C.c_int),
+        ("Y", C.c_void_p), ("scale", C.c_void_p), ("D", C.c_void_p), ("Xt", C.c_void_p), ("xmean", C.c_void_p),
+        ("best", C.c_void_p), ("n_pairs", C.c_int),
+        ("coef", C.c_void_p), ("G", C.c_void_p), ("U", C.c_void_p), ("Adiag", C.c_void_p), ("XtX", C.c_void_p),
+        ("Afull", C.c_void_p),
+        ("n_task", C.c_int), ("task_idx", C.c_void_p), ("Ftask", C.c_void_p),
+        ("n_glt", C.c_int), ("glt", C.c_void_p), ("glt_var", C.c_void_p),
+        ("n_sets", C.c_int), ("set_ptr", C.c_void_p), ("set_idx", C.c_void_p), ("set_col", C.c_void_p),
+        ("n_set_out", C.c_int),
+        ("lj_h", C.c_int), ("lj_tau", C.c_void_p), ("lj_w", C.c_void_p),
+        ("betas", C.c_void_p), ("tstats", C.c_void_p), ("dbetas", C.c_void_p), ("dtstats", C.c_void_p),
+        ("sigma2", C.c_void_p), ("fstats", C.c_void_p), ("r2", C.c_void_p),
+        ("cbeta", C.c_void_p), ("ct", C.c_void_p),
+        ("resid", C.c_void_p), ("resid_w", C.c_void_p), ("pred", C.c_void_p),
+        ("ljung_box", C.c_void_p),
+        ("set_fstats", C.c_void_p), ("set_sd", C.c_void_p), ("set_coef", C.c_void_p),
+        ("status", C.c_void_p),
     ]
 
 
@@ -125,6 +149,7 @@ SIGNATURES = {
     "ffs_reml_select": ([C.POINTER(SelectArgs), C.c_void_p], C.c_int),
     "ffs_reml_gls": ([C.POINTER(GlsArgs), C.c_void_p], C.c_int),
     "ffs_reml_set_stats": ([C.POINTER(SetStatsArgs), C.c_void_p], C.c_int),
+    "ffs_reml_gls_dsort": ([C.POINTER(DsortArgs), C.c_void_p], C.c_int),
     "ffs_reml_gls_ex": ([C.POINTER(GlsArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p], C.c_int),
     "ffs_reml_gls_grouped": ([C.POINTER(GlsArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,

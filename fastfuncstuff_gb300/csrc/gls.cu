@@ -132,6 +132,43 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
   gls_finish(a, x, v, g, beta, ys, ssr, sst, ssw, m, sc, bins, quad_matrix(a, g));
 }
 
+// Ljung-Box statistic of one series ys[T] (shared memory) with sum of squares
+// ssw, by one warp: c_k = sum r_j r_{j+k} / ssw binned by time lag (plain
+// index lags without tau), LB = T (T + 2) sum_k c_k^2 w_k, clamped at 1e10;
+// 0 when T < 10 or ssw < 1e-10 (fastfuncstuff/glm/arma.py:6058-6141). bins:
+// [h + 1] floats of shared memory. The value is returned on lane 0.
+__device__ float ljung_box_warp(int h, const int* tau, const float* w, const float* ys, int T, float ssw,
+                                float* bins) {
+  const int lane = threadIdx.x & 31;
+  for (int k = lane; k <= h; k += 32) bins[k] = 0.f;
+  __syncwarp();
+  for (int k = 1; k <= h; ++k) {
+    if (!tau) {
+      float part = 0.f;
+      for (int t = lane; t + k < T; t += 32) part = fmaf(ys[t], ys[t + k], part);
+      part = warp_sum(part);
+      if (lane == 0) bins[k] += part;
+    } else {
+      for (int t = lane; t + k < T; t += 32) {
+        const int dj = tau[t + k] - tau[t];
+        if (dj > 0 && dj <= h) atomicAdd(bins + dj, ys[t] * ys[t + k]);
+      }
+    }
+  }
+  __syncwarp();
+  float lb = 0.f;
+  if (lane == 0 && ssw >= 1e-10f && T >= 10) {
+    double acc = 0.0;
+    for (int k = 1; k <= h; ++k) {
+      const double ck = (double)bins[k] / (double)ssw;
+      acc += ck * ck * (double)w[k];
+    }
+    acc *= (double)T * ((double)T + 2.0);
+    lb = (float)fmin(acc, 1.0e10);
+  }
+  return lb;
+}
+
 // The statistics of voxel v at pair g from its betas (of the centred, scaled
 // series: beta, shared memory), whitened residual w (shared memory, [T]) and
 // sums of squares; executed by one warp.
@@ -184,38 +221,9 @@ __device__ void gls_finish(const ffs_gls_args& a, const GlsExtra& x, const int v
     a.ct[(size_t)v * a.n_glt + c] = cb / (sqrtf(fmaxf(var, 0.f)) + 1e-10f);
   }
 
-  // Ljung-Box: c_k = sum r_j r_{j+k} / sum r^2, binned by time lag
-  float lb = 0.f;
   if (x.lj_h > 0 && x.ljung_box) {
-    const int h = x.lj_h;
-    for (int k = lane; k <= h; k += 32) bins[k] = 0.f;
-    __syncwarp();
-    for (int k = 1; k <= h; ++k) {
-      float part = 0.f;
-      if (!x.lj_tau) {
-        for (int t = lane; t + k < T; t += 32) part = fmaf(ys[t], ys[t + k], part);
-        part = warp_sum(part);
-        if (lane == 0) bins[k] += part;
-      } else {
-        for (int t = lane; t + k < T; t += 32) {
-          const int dj = x.lj_tau[t + k] - x.lj_tau[t];
-          if (dj > 0 && dj <= h) atomicAdd(bins + dj, ys[t] * ys[t + k]);
-        }
-      }
-    }
-    __syncwarp();
-    if (lane == 0) {
-      if (ssw >= 1e-10f && T >= 10) {
-        double acc = 0.0;
-        for (int k = 1; k <= h; ++k) {
-          const double ck = (double)bins[k] / (double)ssw;
-          acc += ck * ck * (double)x.lj_w[k];
-        }
-        acc *= (double)T * ((double)T + 2.0);
-        lb = (float)fmin(acc, 1.0e10);
-      }
-      x.ljung_box[v] = lb;
-    }
+    const float lb = ljung_box_warp(x.lj_h, x.lj_tau, x.lj_w, ys, T, ssw, bins);
+    if (lane == 0) x.ljung_box[v] = lb;
   }
 
   if (lane == 0) {
@@ -644,6 +652,369 @@ __global__ void __launch_bounds__(256) set_stats_kernel(ffs_set_stats_args a) {
   }
 }
 
+// ------------------------------------------------------------------ -dsort
+// One warp per voxel. Per-warp shared memory (floats): the scaled series ys,
+// the residual r, the whitened series / residual w [T] each; D and D_w
+// [q][T] each; then the small arrays of ds_layout.
+constexpr int DS_WARPS = 4;
+
+struct DsLayout {
+  int ys, r, w, D, Dw, b0, Py, bx, H, PD, HS, S, Si, bd, e, u, FH, W, blk, bins, total;
+};
+
+__host__ __device__ inline DsLayout ds_layout(int T, int K, int q, int n_f, int ns_max, int h) {
+  DsLayout l;
+  int o = 0;
+  auto take = [&](int n) { const int at = o; o += (n + 3) & ~3; return at; };
+  l.ys = take(T); l.r = take(T); l.w = take(T); l.D = take(q * T); l.Dw = take(q * T);
+  l.b0 = take(K); l.Py = take(K); l.bx = take(K); l.H = take(K * q); l.PD = take(K * q); l.HS = take(K * q);
+  l.S = take(q * q); l.Si = take(q * q); l.bd = take(q); l.e = take(q); l.u = take(n_f > q ? n_f : q);
+  const int blk = ns_max * ns_max + 2 * ns_max;  // a column set's block, b_S and the solve; q for the F step
+  l.FH = take(n_f * q); l.W = take(q * q); l.blk = take(blk > q ? blk : q); l.bins = take(h + 1);
+  l.total = o;
+  return l;
+}
+
+// In-place Cholesky of the n x n matrix M (one thread), L in the lower
+// triangle; false if a pivot is not positive.
+__device__ bool chol_small(float* M, int n) {
+  for (int k = 0; k < n; ++k) {
+    float d = M[k * n + k];
+    for (int j = 0; j < k; ++j) d = fmaf(-M[k * n + j], M[k * n + j], d);
+    if (!(d > 0.f)) return false;
+    const float lk = sqrtf(d);
+    M[k * n + k] = lk;
+    for (int i = k + 1; i < n; ++i) {
+      float x = M[i * n + k];
+      for (int j = 0; j < k; ++j) x = fmaf(-M[i * n + j], M[k * n + j], x);
+      M[i * n + k] = x / lk;
+    }
+  }
+  return true;
+}
+
+// x := (L L')^-1 x for the factor L of chol_small (one thread)
+__device__ void chol_solve_small(const float* L, int n, float* x) {
+  for (int i = 0; i < n; ++i) {
+    float v = x[i];
+    for (int j = 0; j < i; ++j) v = fmaf(-L[i * n + j], x[j], v);
+    x[i] = v / L[i * n + i];
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    float v = x[i];
+    for (int j = i + 1; j < n; ++j) v = fmaf(-L[j * n + i], x[j], v);
+    x[i] = v / L[i * n + i];
+  }
+}
+
+// L^-1 x of one series (a run-aware recurrence on coef (c, m, ., 1/sqrt D)),
+// by one thread: out[t] = (z_t - m_t v_{t-1}) / sqrt(D_t), z_t = x_t - c_t x_{t-1}
+__device__ void whiten_series(const float4* cf, const float* x, float* out, int T) {
+  float xp = 0.f, vp = 0.f;
+  for (int t = 0; t < T; ++t) {
+    const float4 q = cf[t];
+    const float z = fmaf(-q.x, xp, x[t]);
+    const float v = fmaf(-q.y, vp, z);
+    out[t] = v * q.w;
+    xp = x[t];
+    vp = v;
+  }
+}
+
+__global__ void __launch_bounds__(DS_WARPS * 32) gls_dsort_kernel(ffs_dsort_args a, int n_f, int ns_max) {
+  extern __shared__ float dsm[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int v = blockIdx.x * DS_WARPS + wid;
+  if (v >= a.V) return;  // warp-uniform
+  const int T = a.T, K = a.K, q = a.q, LT = ld_t(T);
+  const DsLayout L = ds_layout(T, K, q, n_f, ns_max, a.lj_h);
+  float* sm = dsm + (size_t)wid * L.total;
+  float *ys = sm + L.ys, *r = sm + L.r, *w = sm + L.w, *Ds = sm + L.D, *Dw = sm + L.Dw;
+  float *b0 = sm + L.b0, *Py = sm + L.Py, *bx = sm + L.bx, *H = sm + L.H, *PD = sm + L.PD, *HS = sm + L.HS;
+  float *S = sm + L.S, *Si = sm + L.Si, *bd = sm + L.bd, *ev = sm + L.e, *u = sm + L.u, *FH = sm + L.FH;
+  float *W = sm + L.W, *blk = sm + L.blk, *bins = sm + L.bins;
+  const int g = a.best[v];
+  const int p = a.n_pairs > 0 ? g % a.n_pairs : g;
+  const int dsg = a.n_pairs > 0 ? g / a.n_pairs : 0;
+  const float* Gg = a.G + (size_t)g * K * LT;
+  const float* Ug = a.U + (size_t)g * K * LT;
+  const float* Xt = a.Xt + (size_t)dsg * K * LT;
+  const float4* cf = reinterpret_cast<const float4*>(a.coef) + (size_t)p * T;
+  const float sc = a.scale[v];
+
+  // scaled series and the voxel's regressors
+  float sy = 0.f;
+  for (int t = lane; t < T; t += 32) {
+    const float y = __fdiv_rn(a.Y[(size_t)v * T + t], sc);
+    ys[t] = y;
+    sy += y;
+  }
+  for (int i = lane; i < q * T; i += 32) Ds[i] = a.D[(size_t)v * q * T + i];
+  const float mean = warp_sum(sy) / (float)T;
+  __syncwarp();
+
+  // G'y, U'y, G'D, U'D (lanes over t)
+  for (int j = 0; j < K; ++j) {
+    const float* gr = Gg + (size_t)j * LT;
+    const float* ur = Ug + (size_t)j * LT;
+    float ag = 0.f, au = 0.f;
+    float hg[FFS_DSORT_QMAX], hu[FFS_DSORT_QMAX];
+#pragma unroll
+    for (int k = 0; k < FFS_DSORT_QMAX; ++k) hg[k] = hu[k] = 0.f;
+    for (int t = lane; t < T; t += 32) {
+      const float gt = gr[t], ut = ur[t];
+      ag = fmaf(gt, ys[t], ag);
+      au = fmaf(ut, ys[t], au);
+#pragma unroll
+      for (int k = 0; k < FFS_DSORT_QMAX; ++k)
+        if (k < q) {
+          hg[k] = fmaf(gt, Ds[k * T + t], hg[k]);
+          hu[k] = fmaf(ut, Ds[k * T + t], hu[k]);
+        }
+    }
+    ag = warp_sum(ag);
+    au = warp_sum(au);
+    if (lane == 0) {
+      b0[j] = ag;
+      Py[j] = au;
+    }
+#pragma unroll
+    for (int k = 0; k < FFS_DSORT_QMAX; ++k)
+      if (k < q) {
+        const float x = warp_sum(hg[k]), y = warp_sum(hu[k]);
+        if (lane == 0) {
+          H[j * q + k] = x;
+          PD[j * q + k] = y;
+        }
+      }
+  }
+  // whitened y (into w) and D (one lane per series)
+  if (lane <= q) whiten_series(cf, lane == 0 ? ys : Ds + (lane - 1) * T, lane == 0 ? w : Dw + (lane - 1) * T, T);
+  __syncwarp();
+  // D_w'D_w and D_w'y_w
+  for (int k = 0; k < q; ++k) {
+    for (int l = 0; l <= k; ++l) {
+      float acc = 0.f;
+      for (int t = lane; t < T; t += 32) acc = fmaf(Dw[k * T + t], Dw[l * T + t], acc);
+      acc = warp_sum(acc);
+      if (lane == 0) {
+        float x = acc;
+        for (int j = 0; j < K; ++j) x = fmaf(-PD[j * q + k], PD[j * q + l], x);
+        S[k * q + l] = S[l * q + k] = x + (k == l ? 1e-8f : 0.f);
+      }
+    }
+    float acc = 0.f;
+    for (int t = lane; t < T; t += 32) acc = fmaf(Dw[k * T + t], w[t], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      float x = acc;
+      for (int j = 0; j < K; ++j) x = fmaf(-PD[j * q + k], Py[j], x);
+      ev[k] = x;
+    }
+  }
+  __syncwarp();
+  // S^-1 (Cholesky on lane 0), b_D = S^-1 e
+  if (lane == 0) {
+    for (int i = 0; i < q * q; ++i) W[i] = S[i];
+    if (!chol_small(W, q)) {
+      if (a.status) *a.status = 1;
+      for (int i = 0; i < q * q; ++i) W[i] = 0.f;
+      for (int i = 0; i < q; ++i) W[i * q + i] = 1.f;  // identity factor: b_D = e, finite
+    }
+    for (int c = 0; c < q; ++c) {
+      for (int i = 0; i < q; ++i) u[i] = (i == c) ? 1.f : 0.f;
+      chol_solve_small(W, q, u);
+      for (int i = 0; i < q; ++i) Si[i * q + c] = u[i];
+    }
+    for (int i = 0; i < q; ++i) {
+      float x = 0.f;
+      for (int k = 0; k < q; ++k) x = fmaf(Si[i * q + k], ev[k], x);
+      bd[i] = x;
+    }
+  }
+  __syncwarp();
+  // b_X = b0 - H b_D; HS = H S^-1 (lanes over columns)
+  for (int j = lane; j < K; j += 32) {
+    float x = b0[j];
+    for (int k = 0; k < q; ++k) x = fmaf(-H[j * q + k], bd[k], x);
+    bx[j] = x;
+    for (int k = 0; k < q; ++k) {
+      float y = 0.f;
+      for (int l = 0; l < q; ++l) y = fmaf(H[j * q + l], Si[l * q + k], y);
+      HS[j * q + k] = y;
+    }
+  }
+  __syncwarp();
+  // unwhitened residual, R^2 sums
+  float ssr = 0.f, sst = 0.f;
+  for (int t = lane; t < T; t += 32) {
+    float x = ys[t];
+    for (int j = 0; j < K; ++j) x = fmaf(-Xt[(size_t)j * LT + t], bx[j], x);
+    for (int k = 0; k < q; ++k) x = fmaf(-Ds[k * T + t], bd[k], x);
+    r[t] = x;
+    ssr = fmaf(x, x, ssr);
+    const float dy = ys[t] - mean;
+    sst = fmaf(dy, dy, sst);
+  }
+  ssr = warp_sum(ssr);
+  sst = warp_sum(sst);
+  __syncwarp();
+  // whitened residual (lane 0) and its sum of squares (blocks of 32 terms)
+  if (lane == 0) whiten_series(cf, r, w, T);
+  __syncwarp();
+  double ssw_d = 0.0;
+  for (int t0 = 0; t0 < T; t0 += 32) {
+    const float x = t0 + lane < T ? w[t0 + lane] : 0.f;
+    ssw_d += (double)warp_sum(x * x);
+  }
+  const float ssw = (float)ssw_d;
+  const float s2 = ssw / (float)a.dof;
+
+  // t of the base and the D columns
+  for (int j = lane; j < K; j += 32) {
+    float c = a.Adiag[(size_t)g * K + j];
+    for (int k = 0; k < q; ++k) c = fmaf(HS[j * q + k], H[j * q + k], c);
+    const float se = sqrtf(s2 * c);
+    a.betas[(size_t)v * K + j] = bx[j] * sc;
+    a.tstats[(size_t)v * K + j] = bx[j] / (se + 1e-10f);
+  }
+  for (int k = lane; k < q; k += 32) {
+    const float se = sqrtf(s2 * Si[k * q + k]);
+    a.dbetas[(size_t)v * q + k] = bd[k] * sc;
+    a.dtstats[(size_t)v * q + k] = bd[k] / (se + 1e-10f);
+  }
+  // F over the task (or all base) columns: inv(A_t + H_t S^-1 H_t' + 1e-8 I)
+  // by the Woodbury identity around Fm = inv(A_t + 1e-8 I) (X_w'X_w for the
+  // full model): quad = b'Fm b - u'(S + H_t'Fm H_t)^-1 u, u = H_t'Fm b
+  const float* Fm = a.n_task > 0 ? a.Ftask + (size_t)g * n_f * n_f : a.XtX + (size_t)g * K * K;
+  float quad0 = 0.f;
+  for (int i = lane; i < n_f; i += 32) {
+    float fb = 0.f;
+    for (int l = 0; l < n_f; ++l) fb = fmaf(Fm[i * n_f + l], bx[a.n_task > 0 ? a.task_idx[l] : l], fb);
+    quad0 = fmaf(bx[a.n_task > 0 ? a.task_idx[i] : i], fb, quad0);
+    for (int k = 0; k < q; ++k) {
+      float fh = 0.f;
+      for (int l = 0; l < n_f; ++l) fh = fmaf(Fm[i * n_f + l], H[(a.n_task > 0 ? a.task_idx[l] : l) * q + k], fh);
+      FH[i * q + k] = fh;
+    }
+  }
+  quad0 = warp_sum(quad0);
+  __syncwarp();
+  if (lane == 0) {
+    for (int k = 0; k < q; ++k) {
+      float uk = 0.f;
+      for (int i = 0; i < n_f; ++i) uk = fmaf(FH[i * q + k], bx[a.n_task > 0 ? a.task_idx[i] : i], uk);
+      u[k] = uk;
+      for (int l = 0; l < q; ++l) {
+        float x = S[k * q + l];
+        for (int i = 0; i < n_f; ++i) x = fmaf(H[(a.n_task > 0 ? a.task_idx[i] : i) * q + k], FH[i * q + l], x);
+        W[k * q + l] = x;
+      }
+    }
+    float quad = quad0;
+    for (int k = 0; k < q; ++k) blk[k] = u[k];
+    if (chol_small(W, q)) {
+      chol_solve_small(W, q, blk);
+      for (int k = 0; k < q; ++k) quad = fmaf(-u[k], blk[k], quad);
+    }
+    a.fstats[v] = quad / (s2 * (float)n_f + 1e-30f);
+    a.sigma2[v] = s2 * sc * sc;
+    const bool deg = sst <= 1e-10f;
+    a.r2[v] = deg ? 0.f : fminf(1.0f - ssr / fmaxf(sst, 1e-10f), 1.0f);
+  }
+  // GLT on the base block: var = s2 (c A c' + (H'c)' S^-1 (H'c))
+  for (int c = lane; c < a.n_glt; c += 32) {
+    const float* gc = a.glt + (size_t)c * K;
+    float cb = 0.f;
+    for (int j = 0; j < K; ++j) cb = fmaf(gc[j], bx[j], cb);
+    float hc[FFS_DSORT_QMAX];
+    for (int k = 0; k < q; ++k) {
+      float x = 0.f;
+      for (int j = 0; j < K; ++j) x = fmaf(H[j * q + k], gc[j], x);
+      hc[k] = x;
+    }
+    float var = a.glt_var[(size_t)g * a.n_glt + c];
+    for (int k = 0; k < q; ++k)
+      for (int l = 0; l < q; ++l) var = fmaf(hc[k] * Si[k * q + l], hc[l], var);
+    var *= s2;
+    a.cbeta[(size_t)v * a.n_glt + c] = cb * sc;
+    a.ct[(size_t)v * a.n_glt + c] = cb / (sqrtf(fmaxf(var, 0.f)) + 1e-10f);
+  }
+  // series outputs
+  if (a.resid || a.resid_w || a.pred) {
+    for (int t = lane; t < T; t += 32) {
+      if (a.resid) a.resid[(size_t)v * T + t] = r[t] * sc;
+      if (a.resid_w) a.resid_w[(size_t)v * T + t] = w[t] * sc;
+      if (a.pred) a.pred[(size_t)v * T + t] = (ys[t] - r[t]) * sc;
+    }
+  }
+  // column sets over [X | D]: the voxel's block of the covariance, + 1e-8 I
+  for (int sg = 0; sg < a.n_sets; ++sg) {
+    const int b0i = a.set_ptr[sg], ns = a.set_ptr[sg + 1] - b0i;
+    const int* ix = a.set_idx + b0i;
+    float* B = blk;
+    float* bs = blk + ns * ns;
+    for (int e = lane; e < ns * ns; e += 32) {
+      const int i = ix[e / ns], j = ix[e % ns];
+      float x;
+      if (i < K && j < K) {
+        x = a.Afull[(size_t)g * K * K + i * K + j];
+        for (int k = 0; k < q; ++k) x = fmaf(HS[i * q + k], H[j * q + k], x);
+      } else if (i < K) {
+        x = -HS[i * q + (j - K)];
+      } else if (j < K) {
+        x = -HS[j * q + (i - K)];
+      } else {
+        x = Si[(i - K) * q + (j - K)];
+      }
+      B[e] = x + (e / ns == e % ns ? 1e-8f : 0.f);
+    }
+    for (int i = lane; i < ns; i += 32) bs[i] = ix[i] < K ? bx[ix[i]] : bd[ix[i] - K];
+    __syncwarp();
+    // SD over time of the centred [X | D]_S b_S (two passes)
+    float sum = 0.f;
+    for (int t = lane; t < T; t += 32) {
+      float x = 0.f;
+      for (int i = 0; i < ns; ++i) {
+        const int c = ix[i];
+        const float col = c < K ? Xt[(size_t)c * LT + t] - a.xmean[(size_t)dsg * K + c] : Ds[(c - K) * T + t];
+        x = fmaf(col, bs[i], x);
+      }
+      r[t] = x;  // the residual is no longer needed
+      sum += x;
+    }
+    const float mu = warp_sum(sum) / (float)T;
+    float ss = 0.f;
+    for (int t = lane; t < T; t += 32) {
+      const float d = r[t] - mu;
+      ss = fmaf(d, d, ss);
+    }
+    ss = warp_sum(ss);
+    __syncwarp();
+    if (lane == 0) {
+      const size_t o = (size_t)v * a.n_set_out + a.set_col[sg];
+      float* x = bs + ns;
+      for (int i = 0; i < ns; ++i) x[i] = bs[i];
+      float quad = 0.f;
+      if (chol_small(B, ns)) {
+        chol_solve_small(B, ns, x);
+        for (int i = 0; i < ns; ++i) quad = fmaf(bs[i], x[i], quad);
+      } else {
+        quad = __int_as_float(0x7fc00000);
+      }
+      a.set_fstats[o] = quad / ((float)ns * s2 + 1e-30f);
+      a.set_sd[o] = sqrtf(ss / (float)T) * sc;
+      a.set_coef[o] = ns == 1 ? bs[0] * sc : __int_as_float(0x7fc00000);
+    }
+    __syncwarp();
+  }
+  // Ljung-Box of the whitened residual
+  if (a.lj_h > 0 && a.ljung_box) {
+    const float lb = ljung_box_warp(a.lj_h, a.lj_tau, a.lj_w, w, T, ssw, bins);
+    if (lane == 0) a.ljung_box[v] = lb;
+  }
+}
+
 // tile_start[g] = sum over g' < g of ceil(count[g'] / GLS_TILE)
 __global__ void gls_tile_scan(int P, const int* end, int* tile_start) {
   __shared__ int part[1024];
@@ -750,4 +1121,34 @@ extern "C" int ffs_reml_set_stats(const ffs_set_stats_args* a, void* stream) {
   FFS_REQUIRE(!a->design || a->n_pairs > 0, "ffs_reml_set_stats: design needs n_pairs");
   set_stats_kernel<<<ceil_div(a->V, 256), 256, 0, (cudaStream_t)stream>>>(*a);
   return check_launch("set_stats_kernel");
+}
+
+extern "C" int ffs_reml_gls_dsort(const ffs_dsort_args* a, void* stream) {
+  clear_error();
+  FFS_REQUIRE(a, "ffs_reml_gls_dsort: null args");
+  FFS_REQUIRE(a->V >= 0 && a->T > 0 && a->K > 0 && a->q > 0 && a->q <= FFS_DSORT_QMAX && a->dof > 0,
+              "ffs_reml_gls_dsort: V=%d T=%d K=%d q=%d (1..%d) dof=%d", a->V, a->T, a->K, a->q, FFS_DSORT_QMAX,
+              a->dof);
+  if (a->V == 0) return FFS_OK;
+  FFS_REQUIRE(a->Y && a->scale && a->D && a->Xt && a->best && a->coef && a->G && a->U && a->Adiag && a->XtX &&
+                  a->betas && a->tstats && a->dbetas && a->dtstats && a->sigma2 && a->fstats && a->r2,
+              "ffs_reml_gls_dsort: null buffer");
+  FFS_REQUIRE(a->n_task == 0 || (a->task_idx && a->Ftask), "ffs_reml_gls_dsort: task columns need task_idx, Ftask");
+  FFS_REQUIRE(a->n_glt == 0 || (a->glt && a->glt_var && a->cbeta && a->ct), "ffs_reml_gls_dsort: GLT buffers");
+  FFS_REQUIRE(a->n_sets == 0 || (a->set_ptr && a->set_idx && a->set_col && a->Afull && a->xmean && a->set_fstats &&
+                                 a->set_sd && a->set_coef),
+              "ffs_reml_gls_dsort: column sets need set_ptr, set_idx, set_col, Afull, xmean and outputs");
+  FFS_REQUIRE(a->lj_h == 0 || (a->lj_w && a->ljung_box), "ffs_reml_gls_dsort: Ljung-Box buffers");
+  // the set sizes live on the device; a set of distinct columns of [X | D]
+  // has at most K + q of them (the caller removes repeats)
+  const int ns_max = a->n_sets > 0 ? a->K + a->q : 0;
+  const int n_f = a->n_task > 0 ? a->n_task : a->K;
+  const DsLayout L = ds_layout(a->T, a->K, a->q, n_f, ns_max, a->lj_h);
+  const size_t per_warp = sizeof(float) * (size_t)L.total;
+  FFS_REQUIRE(per_warp * DS_WARPS <= 200 * 1024, "ffs_reml_gls_dsort: T=%d K=%d q=%d need %zu bytes of shared memory",
+              a->T, a->K, a->q, per_warp * DS_WARPS);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(gls_dsort_kernel), per_warp * DS_WARPS));
+  gls_dsort_kernel<<<ceil_div(a->V, DS_WARPS), DS_WARPS * 32, per_warp * DS_WARPS, (cudaStream_t)stream>>>(
+      *a, n_f, ns_max);
+  return check_launch("gls_dsort_kernel");
 }

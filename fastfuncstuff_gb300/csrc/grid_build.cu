@@ -531,6 +531,14 @@ __global__ void __launch_bounds__(GB_THREADS, 4) grid_build_kernel(BuildArgs arg
       for (int k = j; k < K; ++k) acc += s.Li[k * K + j] * s.Li[k * K + j];
       o.Adiag[(size_t)pd * K + j] = (float)acc;
     }
+    if (o.Afull) {  // all of A, for the per-voxel blocks of the -dsort fit
+      for (int e = threadIdx.x; e < K * K; e += blockDim.x) {
+        const int i = e / K, j = e % K;
+        double acc = 0.0;
+        for (int k = max(i, j); k < K; ++k) acc += s.Li[k * K + i] * s.Li[k * K + j];
+        o.Afull[(size_t)pd * K * K + e] = (float)acc;
+      }
+    }
     __syncthreads();
 
     // ---- 8. G = U Lx^-1 in fp32 (row t of G solves g Lx = u_t); Gsum = G' 1

@@ -35,6 +35,7 @@ import numpy as np
 import torch
 
 from . import engine
+from .._lib import FFS_DSORT_QMAX
 from .grid import (
     _REML_MODE,
     RemlGrid,
@@ -267,8 +268,8 @@ def fit_glm_arma11(
     """
     if want_ols or want_ols_residuals or want_ols_predicted or ols_write_callback is not None:
         _unsupported("the OLS side fit (want_ols)")
-    if dsort is not None or want_dsort_nods:
-        _unsupported("voxelwise regressors (dsort)")
+    if want_dsort_nods and dsort is None:
+        raise ValueError("want_dsort_nods needs dsort")
     if not estimate_per_voxel:
         _unsupported("global ARMA estimation (estimate_per_voxel=False)")
     if _REML_MODE.afni_faithful:
@@ -305,6 +306,13 @@ def fit_glm_arma11(
             rows.append(g.reshape(-1))
         glt = np.stack(rows)
     ti = list(task_indices) if task_indices else None
+    Dd = None
+    if dsort is not None:
+        # voxelwise regressors: (a, b) is estimated on the base design only; the
+        # final GLS of every voxel is redone with [X | D_v] (gls_dsort)
+        Dd = engine.dsort_prepare(dsort, V, T, dsort_run_bounds, device)
+        if Dd.shape[1] > FFS_DSORT_QMAX:
+            raise NotImplementedError(f"-dsort with {Dd.shape[1]} columns (at most {FFS_DSORT_QMAX})")
     sets = None
     if column_sets:
         sets = engine.column_sets_plan(column_sets, _group_designs[0].cpu().numpy() if _group_designs is not None
@@ -325,7 +333,8 @@ def fit_glm_arma11(
             raise ValueError(f"precomputed_arma_params must have shape ({V}, 2), got {tuple(pa.shape)}")
         pairs, inv = np.unique(pa.numpy().astype(np.float32), axis=0, return_inverse=True)
         grid = grid_of_pairs(pairs[:, 0], pairs[:, 1], use_double=use_double)
-        factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt, with_tc=False, sets=sets)
+        factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt, with_tc=False, sets=sets,
+                                       afull=Dd is not None and bool(column_sets))
         best_all = torch.from_numpy(inv.reshape(-1).astype(np.int32))
         crit_all = None
     else:
@@ -341,14 +350,17 @@ def fit_glm_arma11(
 
     P = grid.P
     bs = _batch_size(V, T, P, K, batch_size, device)
-    use_graph = best_all is None and proposal is not None and cuda_graphs and lj is None and bs >= V
+    use_graph = (best_all is None and proposal is not None and cuda_graphs and lj is None and bs >= V
+                 and Dd is None)
+    afull = Dd is not None and bool(column_sets)
     q0 = join = None
     slots = None
     if _group_designs is not None:
         # grouped fit (fit_glm_arma11_grouped): every design's factors in one
         # grid build, every voxel against its own design in one pass per stage
         Xs, gid = _group_designs
-        factors = engine.build_factors(Xs, grid, layout, task_indices=ti, glt=glt, with_tc=True, sets=sets)
+        factors = engine.build_factors(Xs, grid, layout, task_indices=ti, glt=glt, with_tc=True, sets=sets,
+                                       afull=afull)
         slots = engine.design_slots(gid, Xs.shape[0], K, P, device)
         bs = V
     if factors is None and not use_graph:
@@ -357,7 +369,8 @@ def fit_glm_arma11(
         overlap = K <= engine.BASIS_MAX_K
         side = _side_stream(device) if overlap else None
         factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt,
-                                       with_tc=projector == "tc" and K <= 256, stream=side, sets=sets)
+                                       with_tc=projector == "tc" and K <= 256, stream=side, sets=sets,
+                                       afull=afull)
         if overlap:
             built = torch.cuda.Event()
             built.record(side)
@@ -370,6 +383,7 @@ def fit_glm_arma11(
     chunks = {k: [] for k in ("best", "crit", "surf", "betas", "tstats", "sigma2", "fstats", "r2", "lam",
                               "cb", "ct", "resid", "resid_w", "pred", "lb", "scale")}
     factors_used = factors
+    dchunks = []
     proj = projector if (projector != "tc" or factors is None or factors.U_hi is not None) else "simt"
     if proposal is not None and best_all is None:
         from . import learned
@@ -442,6 +456,11 @@ def fit_glm_arma11(
         if go is None:
             go = engine.gls(Yb, scale, best, factors, Xd, want_residuals=want_residuals,
                             want_predicted=want_predicted, lj=lj)
+        if Dd is not None:
+            do = engine.gls_dsort(Yb, scale, best, factors, _group_designs[0] if slots is not None else Xd,
+                                  Dd[v0:v1], want_residuals=want_residuals, want_predicted=want_predicted, lj=lj,
+                                  design=slots.design if slots is not None else None, column_sets=column_sets)
+            dchunks.append(do)
         if sets is not None:
             chunks["scale"].append(scale)
         for name, t in (("betas", go.betas), ("tstats", go.tstats), ("sigma2", go.sigma2),
@@ -509,6 +528,9 @@ def fit_glm_arma11(
     if want_ljung_box:
         res.ljung_box = out(cat("lb"), torch.float32) if chunks["lb"] else out(torch.zeros(V), torch.float32)
         res.ljung_box_dof = lj[3]
+    if Dd is not None:
+        _apply_dsort(res, dchunks, ti, K, T, dsort_labels, want_dsort_nods, want_r2_partial, r2_partial_mode,
+                     want_r2_semipartial, r2_semipartial_mode, out, device)
     if save_profile_likelihoods and chunks["surf"]:
         res.reml_lklhd_surface = out(cat("surf"))
         res.reml_surface_params = grid.param_list()
@@ -524,6 +546,61 @@ def fit_glm_arma11(
     if verbose:
         print(f"ARMA(1,1) REML: {V:,} voxels x {P} pairs, T={T}, K={K} on {torch.cuda.get_device_name(device)}")
     return res
+
+
+def _apply_dsort(res, dchunks, ti, K, T, labels, want_nods, want_p, mode_p, want_s, mode_s, out, device):
+    """Overwrite the fit's GLS outputs with those of the -dsort GLS
+    (fastfuncstuff/glm/arma.py:3449-3536, :5781-5824): base betas and t
+    (task-filtered), dsort_betas / dsort_tstats, sigma2, F, R^2, GLT, partial
+    R^2 with dof T - K - q, residuals, Ljung-Box and column sets; with
+    ``want_nods`` the base-design fit is kept as ``nods_results``."""
+    import copy
+
+    if want_nods:
+        res.nods_results = copy.copy(res)
+
+    def cat(name):
+        xs = [getattr(d, name) for d in dchunks]
+        return torch.cat(xs) if xs and xs[0] is not None else None
+
+    q = dchunks[0].dbetas.shape[1]
+    dof = max(1, T - K - q)
+    res.dof = dof
+    status = torch.stack([d.status for d in dchunks]).amax()
+    betas, tstats = cat("betas"), cat("tstats")
+    sel = torch.as_tensor(ti, device=device) if ti else None
+    res.betas = out(betas if sel is None else betas[:, sel])
+    res.tstats = out(tstats if sel is None else tstats[:, sel])
+    res.dsort_betas = out(cat("dbetas"))
+    res.dsort_tstats = out(cat("dtstats"))
+    res.dsort_labels = list(labels) if labels else [f"dsort#{k}" for k in range(q)]
+    res.sigma2 = out(cat("sigma2"))
+    res.fstats = out(cat("fstats"))
+    r2 = cat("r2")
+    res.r2 = out(r2, torch.float32)
+    if want_p or want_s:
+        _partial_r2(res, tstats, res.r2, ti, K, dof, want_p, mode_p, want_s, mode_s, out)
+    if res.contrast_betas is not None:
+        res.contrast_betas = out(cat("cbeta"))
+        ct = cat("ct")
+        res.contrast_tstats = out(ct)
+        if want_p:
+            res.contrast_r2_partial = out(ct**2 / (ct**2 + dof))
+        if want_s:
+            rem = torch.clamp(1.0 - r2.to(ct.dtype)[:, None], min=0.0)
+            res.contrast_r2_semipartial = out(ct**2 / (ct**2 + dof) * rem)
+    if res.residuals is not None:
+        res.residuals = out(cat("resid"))
+        res.residuals_whitened = out(cat("resid_w"))
+    if res.predicted is not None:
+        res.predicted = out(cat("pred"))
+    if res.ljung_box is not None and dchunks[0].ljung_box is not None:
+        res.ljung_box = out(cat("ljung_box"), torch.float32)
+    if dchunks[0].set_fstats is not None:
+        res.set_fstats, res.set_sd, res.set_coef = out(cat("set_fstats")), out(cat("set_sd")), out(cat("set_coef"))
+    if int(status.item()):
+        warnings.warn("-dsort: a voxel's regressors lie in the span of the design at its (a, b); their betas "
+                      "there are not determined", stacklevel=3)
 
 
 def _voxel_scale(Y: torch.Tensor, do_scale: bool) -> torch.Tensor:
@@ -609,11 +686,15 @@ def fit_glm_arma11_grouped(data, designs_by_group: dict, group_indices, tr: floa
         kw["device"] = device
         return fit_glm_arma11(Y, Xs[0], tr, _group_designs=(Xs, dense), **kw)
     per = {}
+    dsort_all = fit_kwargs.get("dsort")
     for h in groups:
         m = gid == h
         kw = dict(fit_kwargs)
         if pre is not None:
             kw["precomputed_arma_params"] = _to_tensor(pre).reshape(-1, 2)[m]
+        if dsort_all is not None:  # each group's voxels' regressors (fastfuncstuff/glm/arma.py:3035-3036)
+            kw["dsort"] = (dsort_all if isinstance(dsort_all, torch.Tensor)
+                           else torch.as_tensor(np.asarray(dsort_all)))[m.to(torch.bool)]
         per[h] = (m, fit_glm_arma11(Y[m], designs_by_group[h], tr, **kw))
     merged = ARMA11Results()
     first = per[groups[0]][1]

@@ -170,6 +170,7 @@ class GridFactors:
     n_designs: int = 1  # > 1: design-dependent factors are [n_designs * P] (design-major)
     Fsets: torch.Tensor | None = None  # [n_designs * P][msum] column-set blocks
     sets: "ColumnSets | None" = None
+    Afull: torch.Tensor | None = None  # [n_designs * P][K][K] (X_w'X_w)^-1
 
     @property
     def P(self) -> int:
@@ -303,11 +304,12 @@ def set_stats(betas: torch.Tensor, sigma2: torch.Tensor, scale: torch.Tensor, be
 def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_indices=None,
                   glt: np.ndarray | None = None, with_tc: bool = True, center=None,
                   stream: torch.cuda.Stream | None = None, max_ctas: int = 0,
-                  sets: ColumnSets | None = None) -> GridFactors:
+                  sets: ColumnSets | None = None, afull: bool = False) -> GridFactors:
     """Run the FP64 grid build for design ``X`` (T, K) on its device.
 
     ``sets`` (``column_sets_plan``) adds each column set's inv(A_SS + 1e-8 I)
-    per pair (``Fsets``) for ``set_stats``.
+    per pair (``Fsets``) for ``set_stats``; ``afull`` all of (X_w'X_w)^-1
+    (``Afull``, for the column sets of a -dsort fit).
 
     ``center`` = (flag, coefficients) from ``constant_flag(X)`` when the caller
     has them already (the CUDA-graph plan computes them outside its capture).
@@ -367,6 +369,8 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
         uexp=torch.empty(DP, dtype=torch.int32, device=dev) if with_tc else None,
         n_designs=D,
     )
+    if afull:
+        f.Afull = torch.empty(DP, K, K, **f32)
     if sets is not None and sets.n_sets:
         f.sets = sets
         f.Fsets = torch.empty(DP, sets.msum, **f32)
@@ -382,7 +386,7 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     o = _lib.GridOut(coef=_p(f.coef), logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), U=_p(f.U),
                      U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), uexp=_p(f.uexp), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
                      info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=None, work=_p(work),
-                     Fsets=_p(f.Fsets))
+                     Fsets=_p(f.Fsets), Afull=_p(f.Afull))
     def launch():
         if single:
             _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
@@ -730,3 +734,150 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
     o._keep = (ptau_d, w_d, tiles)
     o._keep2 = (Y, order, work, Xt, best)
     return o
+
+
+@dataclass
+class DsortOut:
+    betas: torch.Tensor
+    tstats: torch.Tensor
+    dbetas: torch.Tensor
+    dtstats: torch.Tensor
+    sigma2: torch.Tensor
+    fstats: torch.Tensor
+    r2: torch.Tensor
+    cbeta: torch.Tensor | None = None
+    ct: torch.Tensor | None = None
+    resid: torch.Tensor | None = None
+    resid_w: torch.Tensor | None = None
+    pred: torch.Tensor | None = None
+    ljung_box: torch.Tensor | None = None
+    set_fstats: torch.Tensor | None = None
+    set_sd: torch.Tensor | None = None
+    set_coef: torch.Tensor | None = None
+    status: torch.Tensor | None = None
+
+
+def dsort_sets_plan(column_sets, K: int, q: int):
+    """(set_ptr, set_idx, set_col, n_out) of column sets over [X | D] (indices
+    >= K name D columns): the sets with every index < K + q, repeats removed;
+    the others stay NaN (fastfuncstuff/glm/arma.py:3461-3479)."""
+    ptr, idx, col = [0], [], []
+    for g, cols in enumerate(column_sets):
+        cols = list(dict.fromkeys(int(c) for c in cols))
+        if any(c < 0 for c in cols):
+            raise IndexError(f"column_sets[{g}] has a negative column index: {cols}")
+        if not cols or any(c >= K + q for c in cols):
+            continue
+        idx.extend(cols)
+        ptr.append(len(idx))
+        col.append(g)
+    return np.asarray(ptr, np.int32), np.asarray(idx, np.int32), np.asarray(col, np.int32), len(column_sets)
+
+
+def gls_dsort(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors, X: torch.Tensor,
+              D: torch.Tensor, *, want_residuals: bool = False, want_predicted: bool = False, lj=None,
+              design: torch.Tensor | None = None, column_sets=None) -> DsortOut:
+    """The -dsort GLS of every voxel with [X | D_v] at its pair (``ffs_reml_gls_dsort``).
+
+    ``D`` (V, q, T) holds each voxel's regressors after the constant guard and
+    any per-run expansion; grouped fits pass X as (D, T, K) and ``design``."""
+    lib = _lib.load()
+    dev = Y.device
+    V, T = Y.shape
+    K, P = f.K, f.P
+    q = D.shape[1]
+    st = _stream()
+    Y = Y.to(dtype=torch.float32).contiguous()
+    D = D.to(device=dev, dtype=torch.float32).contiguous()
+    n_pairs = 0
+    key = best.to(torch.int32)
+    if design is not None:
+        key = design.to(torch.int32) * P + key
+        n_pairs = P
+    key = key.contiguous()
+    X = X.to(device=dev, dtype=torch.float32)
+    Xt = padded_design_t(X) if X.ndim == 2 else torch.stack([padded_design_t(x) for x in X])
+    xmean = (X.double().mean(-2) if X.ndim == 3 else X.double().mean(0, keepdim=True)).float().contiguous()
+    f32 = dict(device=dev, dtype=torch.float32)
+    ng = 0 if f.glt is None else f.glt.shape[0]
+    o = DsortOut(betas=torch.empty(V, K, **f32), tstats=torch.empty(V, K, **f32), dbetas=torch.empty(V, q, **f32),
+                 dtstats=torch.empty(V, q, **f32), sigma2=torch.empty(V, **f32), fstats=torch.empty(V, **f32),
+                 r2=torch.empty(V, **f32), cbeta=torch.empty(V, ng, **f32) if ng else None,
+                 ct=torch.empty(V, ng, **f32) if ng else None,
+                 resid=torch.empty(V, T, **f32) if want_residuals else None,
+                 resid_w=torch.empty(V, T, **f32) if want_residuals else None,
+                 pred=torch.empty(V, T, **f32) if want_predicted else None,
+                 status=torch.zeros(1, dtype=torch.int32, device=dev))
+    sp = si = sc_ = None
+    n_sets = n_out = 0
+    if column_sets:
+        ptr, idx, col, n_out = dsort_sets_plan(column_sets, K, q)
+        n_sets = len(col)
+        o.set_fstats = torch.full((V, n_out), float("nan"), **f32)
+        o.set_sd = torch.full((V, n_out), float("nan"), **f32)
+        o.set_coef = torch.full((V, n_out), float("nan"), **f32)
+        if n_sets:
+            if f.Afull is None:
+                raise ValueError("gls_dsort: column sets need the factors' Afull (build_factors(afull=True))")
+            sp, si, sc_ = const_dev(ptr, dev), const_dev(idx, dev), const_dev(col, dev)
+    h, ptau_d, w_d = 0, None, None
+    if lj is not None and lj[0] > 0:
+        h, ptau, w, _ = lj
+        ptau_d = None if ptau is None else const_dev(ptau, dev)
+        w_d = const_dev(w, dev)
+        o.ljung_box = torch.empty(V, **f32)
+    nt = 0 if f.task_idx is None else f.task_idx.numel()
+    a = _lib.DsortArgs(V=V, T=T, K=K, q=q, dof=max(1, T - K - q), Y=_p(Y), scale=_p(scale), D=_p(D), Xt=_p(Xt),
+                       xmean=_p(xmean), best=_p(key), n_pairs=n_pairs, coef=_p(f.coef), G=_p(f.G), U=_p(f.U),
+                       Adiag=_p(f.Adiag), XtX=_p(f.XtX), Afull=_p(f.Afull), n_task=nt, task_idx=_p(f.task_idx),
+                       Ftask=_p(f.Ftask), n_glt=ng, glt=_p(f.glt), glt_var=_p(f.glt_var), n_sets=n_sets,
+                       set_ptr=_p(sp), set_idx=_p(si), set_col=_p(sc_), n_set_out=n_out, lj_h=h, lj_tau=_p(ptau_d),
+                       lj_w=_p(w_d), betas=_p(o.betas), tstats=_p(o.tstats), dbetas=_p(o.dbetas),
+                       dtstats=_p(o.dtstats), sigma2=_p(o.sigma2), fstats=_p(o.fstats), r2=_p(o.r2),
+                       cbeta=_p(o.cbeta), ct=_p(o.ct), resid=_p(o.resid), resid_w=_p(o.resid_w), pred=_p(o.pred),
+                       ljung_box=_p(o.ljung_box), set_fstats=_p(o.set_fstats), set_sd=_p(o.set_sd),
+                       set_coef=_p(o.set_coef), status=_p(o.status))
+    _run("ffs_reml_gls_dsort", lib.ffs_reml_gls_dsort, C.byref(a), st)
+    o._keep = (Y, D, key, Xt, xmean, sp, si, sc_, ptau_d, w_d)
+    return o
+
+
+def dsort_prepare(dsort, V: int, T: int, run_bounds=None, dev=None) -> torch.Tensor:
+    """The -dsort regressors as the kernel reads them, (V, q, T) float32 on the
+    device: (V, T) taken as one dataset, the shape checked as the reference
+    does (ValueError), a series constant and nonzero through time replaced by
+    its dataset's mean over the other voxels (with a warning), then one column
+    per set and run when ``run_bounds`` [t0, ..., T] is given
+    (fastfuncstuff/glm/arma.py:3207-3245, :3931-3945, :3385-3397)."""
+    import warnings
+
+    Dt = dsort if isinstance(dsort, torch.Tensor) else torch.as_tensor(np.asarray(dsort))
+    Dt = Dt.to(device=dev, dtype=torch.float32)
+    if Dt.ndim == 2:
+        Dt = Dt.unsqueeze(1)
+    if Dt.ndim != 3 or Dt.shape[0] != V or Dt.shape[2] != T:
+        raise ValueError(f"dsort must be (n_voxels={V}, n_dsort, n_timepoints={T}); got {tuple(Dt.shape)}")
+    sd = Dt.double().std(dim=2)
+    mabs = Dt.double().abs().mean(dim=2)
+    bad = (sd < 1e-8) & (mabs > 1e-8)
+    n_bad = int(bad.sum().item())
+    if n_bad:
+        Dt = Dt.clone()
+        for d in range(Dt.shape[1]):
+            bd = bad[:, d]
+            if bool(bd.any()):
+                good = ~bd
+                src = Dt[good, d] if bool(good.any()) else Dt[:, d]
+                Dt[bd, d] = src.double().mean(0).float()
+        warnings.warn(f"-dsort: {n_bad} voxel timeseries were ~constant through time and were replaced by "
+                      "their dataset mean (matches 3dREMLfit).", stacklevel=3)
+    if run_bounds is not None:
+        rb = [int(x) for x in run_bounds]
+        n_runs = len(rb) - 1
+        n_sets = Dt.shape[1]
+        out = torch.zeros(V, n_sets * n_runs, T, device=Dt.device, dtype=torch.float32)
+        for si in range(n_sets):
+            for r in range(n_runs):
+                out[:, si * n_runs + r, rb[r]:rb[r + 1]] = Dt[:, si, rb[r]:rb[r + 1]]
+        Dt = out
+    return Dt.contiguous()

@@ -118,6 +118,7 @@ typedef struct {
   float* Gsum;          /* [P][K] G' 1: the betas of the constant series          */
   double* work;         /* scratch, ffs_grid_work_bytes() bytes                   */
   float* Fsets;         /* [P][sum q_S^2] (with n_sets), or NULL                  */
+  float* Afull;         /* [P][K][K] (X_w'X_w)^-1 (fp32), or NULL                 */
 } ffs_grid_out;
 
 size_t ffs_grid_work_bytes(int T, int K, int P);
@@ -393,6 +394,53 @@ typedef struct {
 } ffs_set_stats_args;
 
 int ffs_reml_set_stats(const ffs_set_stats_args* a, void* stream);
+
+/* -dsort: the GLS of every voxel with the extended design [X | D_v] at its
+ * pair, D_v its q voxelwise regressors (fastfuncstuff/glm/arma.py:3248-3539,
+ * after the constant guard and any per-run expansion, which the caller does).
+ * Block elimination against the pair's factors: with b0 = G'y, H = G'D,
+ * P_y = U'y, P_D = U'D (U'x = Q'L^-1 x) and the whitened D_w, y_w,
+ *   S   = D_w'D_w - P_D'P_D + 1e-8 I,   b_D = S^-1 (D_w'y_w - P_D'P_y),
+ *   b_X = b0 - H b_D,   cov / sigma2 = [[A + H S^-1 H', -H S^-1], [., S^-1]]
+ * (A = (X_w'X_w)^-1), then sigma2 = ||L^-1 r||^2 / dof of the unwhitened
+ * residual r, t, F over the task (or all base) columns through the Woodbury
+ * form of inv(cov_task + 1e-8 I) with Ftask (or X_w'X_w), R^2, GLT on the
+ * base block, column sets over [X | D] (indices >= K are D columns; needs
+ * Afull) and Ljung-Box of the whitened residual; all unscaled by scale[v].
+ * The data are divided by scale[v]; D stays in its own units.
+ */
+typedef struct {
+  int V, T, K, q;
+  int dof;                /* max(1, T - K - q)                                    */
+  const float* Y;         /* [V][T] data (unscaled)                               */
+  const float* scale;     /* [V]                                                  */
+  const float* D;         /* [V][q][T] voxelwise regressors                       */
+  const float* Xt;        /* [n_designs][K][ld_t] the design(s), transposed       */
+  const float* xmean;     /* [n_designs][K] column means of the design(s) (sets)  */
+  const int* best;        /* [V] pair, or key design * n_pairs + pair             */
+  int n_pairs;            /* 0: one design                                        */
+  const float* coef;      /* [P][T] float4 (indexed by pair)                      */
+  const float* G; const float* U;   /* [keys][K][ld_t]                            */
+  const float* Adiag;     /* [keys][K]                                            */
+  const float* XtX;       /* [keys][K][K]                                         */
+  const float* Afull;     /* [keys][K][K] or NULL (needed with column sets)       */
+  int n_task; const int* task_idx; const float* Ftask;  /* [keys][n_task]^2       */
+  int n_glt; const float* glt; const float* glt_var;    /* [n_glt][K], [keys][n_glt] */
+  int n_sets; const int* set_ptr; const int* set_idx; const int* set_col; int n_set_out;
+  int lj_h; const int* lj_tau; const float* lj_w;
+  float* betas; float* tstats;      /* [V][K] every base column                   */
+  float* dbetas; float* dtstats;    /* [V][q]                                     */
+  float* sigma2; float* fstats; float* r2;             /* [V]                     */
+  float* cbeta; float* ct;          /* [V][n_glt] or NULL                         */
+  float* resid; float* resid_w; float* pred;           /* [V][T] or NULL          */
+  float* ljung_box;                 /* [V] or NULL                                */
+  float* set_fstats; float* set_sd; float* set_coef;   /* [V][n_set_out] or NULL  */
+  int* status;            /* device int: set to 1 if some voxel's S had a pivot   */
+                          /*   <= 0 (D in the span of X); NULL to skip            */
+} ffs_dsort_args;
+
+#define FFS_DSORT_QMAX 16
+int ffs_reml_gls_dsort(const ffs_dsort_args* a, void* stream);
 
 /* ffs_reml_gls plus the Ljung-Box statistic of each voxel's whitened residual
  * (fastfuncstuff/glm/arma.py:6058-6141, AFNI ljung_box_uneven): lj_h is the

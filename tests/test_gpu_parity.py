@@ -438,3 +438,71 @@ def test_rvar_round_trip_reuses_the_fitted_pairs(tmp_path):
     np.testing.assert_allclose(vol[:, 3], np.sqrt(first.sigma2.numpy()), rtol=1e-6)
     np.testing.assert_array_equal(vol[:, 4], first.reml_likelihood.numpy())
     np.testing.assert_array_equal(vol[:, 5], first.ljung_box.numpy())
+
+
+@pytest.mark.parametrize("tag", ["two", "runs"])
+@pytest.mark.parametrize("exhaustive", [True, False])
+def test_dsort_matches_oracle_and_reference(tag, exhaustive):
+    """-dsort on the device (ffs_reml_gls_dsort: block elimination against the
+    pair's G and U, a q x q solve per voxel) against the FP64 oracle on the
+    float32 mode's semantics, and against the reference's own float32 run:
+    base and voxelwise betas and t, sigma2, F, R^2, GLT, Ljung-Box, residuals
+    and column sets over [X | D]; two datasets per voxel (one with constant
+    series the guard replaces), and one dataset expanded per run."""
+    d = load_golden("dsort")
+    K = d["X"].shape[1]
+    ptr, idx = d[f"{tag}__sets_ptr"], d[f"{tag}__sets_idx"]
+    sets = [[int(c) for c in idx[ptr[g]:ptr[g + 1]]] for g in range(len(ptr) - 1)]
+    kw = dict(a_grid=d["a_grid"], b_grid=d["b_grid"], run_starts=d["run_starts"], task_indices=[0, 1],
+              glt_matrices=[d["glt"][0]], want_ljung_box=True, want_residuals=True, column_sets=sets)
+    if tag == "two":
+        kw["dsort"] = d["D"]
+    else:
+        kw.update(dsort=d["D"][:, :1], dsort_run_bounds=[0, 64, 128])
+    with pytest.warns(UserWarning, match="constant") if tag == "two" else _no_warning():
+        got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=PROJ,
+                             force_exhaustive_search=exhaustive, glt_labels=["t0-t1"], **kw)
+    ref = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, fp64_scaled=True, force_exhaustive_search=exhaustive,
+                           save_profile_likelihoods=True, **kw)
+    assert got.dof == ref.dof == int(d[f"{tag}_f64_def__dof"])
+    grid = G.make_grid(d["a_grid"], d["b_grid"])
+    idx_g = _index(got.arma_params.numpy(), grid)
+    check_selection(idx_g, ref.arma_index, ref.reml_lklhd_surface)
+    same = idx_g == ref.arma_index
+    q = ref.dsort_betas.shape[1]
+    assert got.dsort_betas.shape == (d["Y"].shape[0], q)
+    full_got = np.concatenate([got.betas.numpy(), got.dsort_betas.numpy()], 1)[same]
+    full_ref = np.concatenate([ref.betas, ref.dsort_betas], 1)[same]
+    assert rel_maxnorm(full_got, full_ref).max() <= BETA_REL
+    t_got = np.concatenate([got.tstats.numpy(), got.dsort_tstats.numpy()], 1)[same]
+    t_ref = np.concatenate([ref.tstats, ref.dsort_tstats], 1)[same]
+    assert rel_maxnorm(t_got, t_ref).max() <= BETA_REL
+    np.testing.assert_allclose(got.sigma2.numpy()[same], ref.sigma2[same], rtol=1e-4)
+    assert rel_maxnorm(np.sqrt(got.fstats.numpy()[same])[:, None], np.sqrt(ref.fstats[same])[:, None]).max() <= 2e-4
+    np.testing.assert_allclose(got.r2.numpy()[same], ref.r2[same], atol=2e-5)
+    assert rel_maxnorm(got.contrast_tstats.numpy()[same], ref.contrast_tstats[same]).max() <= 2e-4
+    np.testing.assert_allclose(got.ljung_box.numpy()[same], ref.ljung_box[same], rtol=2e-3, atol=1e-3)
+    scale = np.abs(ref.residuals[same]).max(1, keepdims=True)
+    assert (np.abs(got.residuals.numpy()[same] - ref.residuals[same]) / scale).max() <= 2e-4
+    for name in ("set_fstats", "set_sd", "set_coef"):
+        np.testing.assert_array_equal(np.isnan(getattr(got, name).numpy()), np.isnan(getattr(ref, name)))
+    ok = ~np.isnan(ref.set_fstats[0])
+    assert rel_maxnorm(np.sqrt(got.set_fstats.numpy()[same][:, ok]), np.sqrt(ref.set_fstats[same][:, ok])).max() <= 2e-4
+    col = ~np.isnan(ref.set_sd[0])
+    err = np.abs(got.set_sd.numpy()[same][:, col] - ref.set_sd[same][:, col]).max(1) / np.abs(full_ref).max(1)
+    assert err.max() <= 2e-4
+    # the reference's own float32 run, on the voxels whose pair agrees
+    mode = f"{tag}_{'f32_exh' if exhaustive else 'f32_def'}"
+    agree = (got.arma_params.numpy() == d[mode + "__arma_params"]).all(1)
+    assert agree.mean() >= 0.97
+    for name in ("betas", "dsort_betas"):
+        g, r = getattr(got, name).numpy()[agree], d[f"{mode}__{name}"][agree]
+        assert rel_maxnorm(g, r).max() <= 5e-3, name
+
+
+class _no_warning:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
