@@ -371,6 +371,28 @@ def run_gb300(args) -> None:
                       "gpu_launches": l_f, "clocks": clk_f},
     }
 
+    if args.dsort > 0 and not grouped and rank == 0:
+        # the full-grid fit with Q voxelwise regressors per voxel (-dsort): the
+        # search is unchanged, the final GLS is the extended one
+        rng = np.random.default_rng(77)
+        base = rng.standard_normal((args.dsort, T)).astype(np.float32)
+        Dd = (torch.from_numpy(base).to(dev)[None] +
+              0.3 * torch.randn(V, args.dsort, T, device=dev, generator=torch.Generator(dev).manual_seed(5)))
+        kw_d = dict(kw, dsort=Dd)
+        ms_d, st_d, l_d, clk_d = timed(kw_d)
+        dk = st_d.get("ffs_reml_gls_dsort", {"mean_ms": float("nan"), "calls": 1})
+        q = args.dsort
+        # per voxel: G'y, U'y, G'D, U'D (2 + 2q K x T products), whitening of y,
+        # D and the residual, the residual itself (K + q per sample)
+        flops = V * ((2 + 2 * q) * 2.0 * K * T + (2 + q) * 6.0 * T + 2.0 * (K + q) * T)
+        sec = dk["mean_ms"] * 1e-3
+        peak = 152 * 128 * 2 * clk_d["sm_mhz"] * 1e6 / 1e12 if clk_d.get("sm_mhz") else float("nan")
+        line["dsort"] = {"q": q, "value": ws * V / (ms_d / 1e3), "unit": "voxels/s", "ms_per_step": ms_d,
+                         "gls_dsort_ms": dk["mean_ms"], "gpu_launches": l_d, "clocks": clk_d,
+                         "roofline": {"kernel": "ffs_reml_gls_dsort", "bound": "fp32", "achieved": flops / sec / 1e12,
+                                      "peak": peak, "unit": "TFLOP/s", "frac": flops / sec / 1e12 / peak,
+                                      "work": "G'y, U'y, G'D, U'D, the whitening recurrences and the residual"},
+                         "stages_ms": {k: round(v["mean_ms"] * v["calls"] / args.steps, 4) for k, v in st_d.items()}}
     if rank == 0 and not args.no_e2e:
         # end to end through the public API from pinned host buffers
         Yh = torch.from_numpy(w.Y).pin_memory()
@@ -420,6 +442,8 @@ def main() -> None:
     ap.add_argument("--train-epochs", type=int, default=30)
     ap.add_argument("--proposal", default=None, help="load a trained proposal (.npz) instead of training one")
     ap.add_argument("--save-proposal", default=None, help="save the proposal trained here (.npz)")
+    ap.add_argument("--dsort", type=int, default=0,
+                    help="also time the full-grid fit with this many voxelwise regressors (-dsort)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

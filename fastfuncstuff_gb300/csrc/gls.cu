@@ -707,20 +707,51 @@ __device__ void chol_solve_small(const float* L, int n, float* x) {
   }
 }
 
-// L^-1 x of one series (a run-aware recurrence on coef (c, m, ., 1/sqrt D)),
-// by one thread: out[t] = (z_t - m_t v_{t-1}) / sqrt(D_t), z_t = x_t - c_t x_{t-1}
-__device__ void whiten_series(const float4* cf, const float* x, float* out, int T) {
-  float xp = 0.f, vp = 0.f;
-  for (int t = 0; t < T; ++t) {
-    const float4 q = cf[t];
-    const float z = fmaf(-q.x, xp, x[t]);
-    const float v = fmaf(-q.y, vp, z);
-    out[t] = v * q.w;
-    xp = x[t];
+// L^-1 x of one series by the whole warp: out[t] = (z_t - m_t v_{t-1}) /
+// sqrt(D_t), z_t = x_t - c_t x_{t-1} (coef (c, m, ., 1/sqrt D), c = m = 0 at
+// run starts). Lane l takes the segment [l S, (l + 1) S) of the time axis:
+// it runs the recursion from v = 0 (z needs only x of the previous sample),
+// the warp composes the segments' affine maps v_out = E + H v_in (H the
+// product of -m over the segment) in a shuffle scan, and a second pass adds
+// each segment's carry-in times the running product. x and out do not overlap.
+__device__ void whiten_warp(const float4* __restrict__ cf, const float* x, float* out, int T) {
+  const int lane = threadIdx.x & 31;
+  const int seg = (T + 31) >> 5;
+  const int s0 = min(T, lane * seg), s1 = min(T, s0 + seg);
+  float xp = s0 > 0 ? x[s0 - 1] : 0.f;
+  float vp = 0.f, H = 1.f;
+  for (int t = s0; t < s1; ++t) {
+    const float4 q = __ldg(cf + t);
+    const float xt = x[t];
+    const float v = fmaf(-q.y, vp, fmaf(-q.x, xp, xt));
+    out[t] = v;
+    xp = xt;
     vp = v;
+    H *= -q.y;
   }
+  float E = vp;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const float Hp = __shfl_up_sync(0xffffffffu, H, o), Ep = __shfl_up_sync(0xffffffffu, E, o);
+    if (lane >= o) {
+      E = fmaf(H, Ep, E);
+      H *= Hp;
+    }
+  }
+  float vin = __shfl_up_sync(0xffffffffu, E, 1);
+  if (lane == 0) vin = 0.f;
+  float h = 1.f;
+  for (int t = s0; t < s1; ++t) {
+    const float4 q = __ldg(cf + t);
+    h *= -q.y;
+    out[t] = fmaf(h, vin, out[t]) * q.w;
+  }
+  __syncwarp();
 }
 
+// QB: the projection loop's unrolled bound on q (q itself for 1..4, the
+// maximum otherwise), so that small q issues no predicated-off work
+template <int QB>
 __global__ void __launch_bounds__(DS_WARPS * 32) gls_dsort_kernel(ffs_dsort_args a, int n_f, int ns_max) {
   extern __shared__ float dsm[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -758,15 +789,16 @@ __global__ void __launch_bounds__(DS_WARPS * 32) gls_dsort_kernel(ffs_dsort_args
     const float* gr = Gg + (size_t)j * LT;
     const float* ur = Ug + (size_t)j * LT;
     float ag = 0.f, au = 0.f;
-    float hg[FFS_DSORT_QMAX], hu[FFS_DSORT_QMAX];
+    float hg[QB], hu[QB];
 #pragma unroll
-    for (int k = 0; k < FFS_DSORT_QMAX; ++k) hg[k] = hu[k] = 0.f;
+    for (int k = 0; k < QB; ++k) hg[k] = hu[k] = 0.f;
+#pragma unroll 4
     for (int t = lane; t < T; t += 32) {
       const float gt = gr[t], ut = ur[t];
       ag = fmaf(gt, ys[t], ag);
       au = fmaf(ut, ys[t], au);
 #pragma unroll
-      for (int k = 0; k < FFS_DSORT_QMAX; ++k)
+      for (int k = 0; k < QB; ++k)
         if (k < q) {
           hg[k] = fmaf(gt, Ds[k * T + t], hg[k]);
           hu[k] = fmaf(ut, Ds[k * T + t], hu[k]);
@@ -779,7 +811,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) gls_dsort_kernel(ffs_dsort_args
       Py[j] = au;
     }
 #pragma unroll
-    for (int k = 0; k < FFS_DSORT_QMAX; ++k)
+    for (int k = 0; k < QB; ++k)
       if (k < q) {
         const float x = warp_sum(hg[k]), y = warp_sum(hu[k]);
         if (lane == 0) {
@@ -788,9 +820,9 @@ __global__ void __launch_bounds__(DS_WARPS * 32) gls_dsort_kernel(ffs_dsort_args
         }
       }
   }
-  // whitened y (into w) and D (one lane per series)
-  if (lane <= q) whiten_series(cf, lane == 0 ? ys : Ds + (lane - 1) * T, lane == 0 ? w : Dw + (lane - 1) * T, T);
-  __syncwarp();
+  // whitened y (into w) and D
+  whiten_warp(cf, ys, w, T);
+  for (int k = 0; k < q; ++k) whiten_warp(cf, Ds + k * T, Dw + k * T, T);
   // D_w'D_w and D_w'y_w
   for (int k = 0; k < q; ++k) {
     for (int l = 0; l <= k; ++l) {
@@ -847,6 +879,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) gls_dsort_kernel(ffs_dsort_args
   __syncwarp();
   // unwhitened residual, R^2 sums
   float ssr = 0.f, sst = 0.f;
+#pragma unroll 2
   for (int t = lane; t < T; t += 32) {
     float x = ys[t];
     for (int j = 0; j < K; ++j) x = fmaf(-Xt[(size_t)j * LT + t], bx[j], x);
@@ -859,9 +892,8 @@ __global__ void __launch_bounds__(DS_WARPS * 32) gls_dsort_kernel(ffs_dsort_args
   ssr = warp_sum(ssr);
   sst = warp_sum(sst);
   __syncwarp();
-  // whitened residual (lane 0) and its sum of squares (blocks of 32 terms)
-  if (lane == 0) whiten_series(cf, r, w, T);
-  __syncwarp();
+  // whitened residual and its sum of squares (blocks of 32 terms)
+  whiten_warp(cf, r, w, T);
   double ssw_d = 0.0;
   for (int t0 = 0; t0 < T; t0 += 32) {
     const float x = t0 + lane < T ? w[t0 + lane] : 0.f;
@@ -1147,8 +1179,20 @@ extern "C" int ffs_reml_gls_dsort(const ffs_dsort_args* a, void* stream) {
   const size_t per_warp = sizeof(float) * (size_t)L.total;
   FFS_REQUIRE(per_warp * DS_WARPS <= 200 * 1024, "ffs_reml_gls_dsort: T=%d K=%d q=%d need %zu bytes of shared memory",
               a->T, a->K, a->q, per_warp * DS_WARPS);
-  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(gls_dsort_kernel), per_warp * DS_WARPS));
-  gls_dsort_kernel<<<ceil_div(a->V, DS_WARPS), DS_WARPS * 32, per_warp * DS_WARPS, (cudaStream_t)stream>>>(
-      *a, n_f, ns_max);
+  const size_t smem = per_warp * DS_WARPS;
+  const int nb = ceil_div(a->V, DS_WARPS);
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (a->q) {
+#define FFS_DSORT_LAUNCH(QB)                                                                  \
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(gls_dsort_kernel<QB>), smem));      \
+  gls_dsort_kernel<QB><<<nb, DS_WARPS * 32, smem, st>>>(*a, n_f, ns_max);                     \
+  break;
+    case 1: FFS_DSORT_LAUNCH(1)
+    case 2: FFS_DSORT_LAUNCH(2)
+    case 3: FFS_DSORT_LAUNCH(3)
+    case 4: FFS_DSORT_LAUNCH(4)
+    default: FFS_DSORT_LAUNCH(FFS_DSORT_QMAX)
+#undef FFS_DSORT_LAUNCH
+  }
   return check_launch("gls_dsort_kernel");
 }
