@@ -150,6 +150,7 @@ SIGNATURES = {
     "ffs_reml_gls": ([C.POINTER(GlsArgs), C.c_void_p], C.c_int),
     "ffs_reml_set_stats": ([C.POINTER(SetStatsArgs), C.c_void_p], C.c_int),
     "ffs_reml_gls_dsort": ([C.POINTER(DsortArgs), C.c_void_p], C.c_int),
+    "ffs_reml_tune_tc_pairs": ([C.c_int, C.c_int], C.c_int),
     "ffs_reml_gls_ex": ([C.POINTER(GlsArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p], C.c_int),
     "ffs_reml_gls_grouped": ([C.POINTER(GlsArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,

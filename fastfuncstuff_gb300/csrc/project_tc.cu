@@ -19,6 +19,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace ffsk {
@@ -384,10 +386,34 @@ int launch_tc(const ffs_project_args* a, const TcParams& prm, int max_items, voi
   return check_launch("project_tc_kernel");
 }
 
+// Pairs per B tile of the grid-mode projection, per K (0: the widest tile,
+// 256 / K pairs); set by the autotuner through ffs_reml_tune_tc_pairs.
+std::mutex g_tune_mu;
+int g_tune_pairs[257] = {0};
+
+int tc_pairs_for(int K, int P) {
+  int g = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g = g_tune_pairs[K];
+  }
+  if (g <= 0 || g * K > 256) g = 256 / K;
+  return g < P ? g : P;
+}
+
 }  // namespace
 }  // namespace ffsk
 
 using namespace ffsk;
+
+extern "C" int ffs_reml_tune_tc_pairs(int K, int pairs) {
+  clear_error();
+  FFS_REQUIRE(K > 0 && K <= 256 && pairs >= 0 && pairs * K <= 256,
+              "ffs_reml_tune_tc_pairs: K=%d pairs=%d (pairs x K <= 256; 0 resets)", K, pairs);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_pairs[K] = pairs;
+  return FFS_OK;
+}
 
 extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
   clear_error();
@@ -407,8 +433,7 @@ extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
   prm.K = a->K;
   prm.P = a->P;
   prm.ld = a->ld_y;
-  prm.g = 256 / a->K;
-  if (prm.g > a->P) prm.g = a->P;
+  prm.g = tc_pairs_for(a->K, a->P);
   prm.N = ((prm.g * a->K) + 15) / 16 * 16;
   prm.n_col_tiles = ceil_div(a->P, prm.g);
   prm.n_vox_tiles = ceil_div(a->V, BM);

@@ -123,6 +123,63 @@ def padded_design_t(X: torch.Tensor) -> torch.Tensor:
     return Xt
 
 
+_TUNED: dict = {}
+
+
+def autotune_projection(T: int, K: int, P: int, dev, V: int = 65536, reps: int = 3) -> dict:
+    """Choose the tcgen05 projection's tile shape for this (T, K, P) by timing.
+
+    The candidates are the B tiles of 256, 128 and 64 MMA columns (256 // K,
+    128 // K, 64 // K pairs per tile); each runs the grid-mode projection of V
+    synthetic voxels against P synthetic pairs (fp16 operands of the real
+    shapes) ``reps`` times after one warm-up, timed with CUDA events, and the
+    fastest is set through ``ffs_reml_tune_tc_pairs`` (process-wide, per K).
+    The choice changes no result, only the speed; it is made once per shape
+    and device and cached. Returns {"pairs": best, "ms": {pairs: time}}."""
+    key = (T, K, P, str(dev))
+    lib = _lib.load()
+    if key in _TUNED:  # the table is per K: restore this shape's choice
+        _lib.check(lib.ffs_reml_tune_tc_pairs(K, _TUNED[key]["pairs"]), "ffs_reml_tune_tc_pairs")
+        return _TUNED[key]
+    cands = sorted({n // K for n in (256, 128, 64) if n // K >= 1}, reverse=True)
+    if len(cands) == 1 or P <= 1:
+        _lib.check(lib.ffs_reml_tune_tc_pairs(K, cands[0]), "ffs_reml_tune_tc_pairs")
+        _TUNED[key] = {"pairs": cands[0], "ms": {}}
+        return _TUNED[key]
+    ld = padded_ld(T)
+    gen = torch.Generator(device=dev).manual_seed(1)
+    f16 = dict(device=dev, dtype=torch.float16)
+    y_hi = torch.randn(V, ld, generator=gen, **f16).view(torch.int16)
+    y_lo = (torch.randn(V, ld, generator=gen, **f16) * 1e-3).view(torch.int16)
+    u_hi = torch.randn(P * K, ld, generator=gen, **f16).view(torch.int16)
+    u_lo = (torch.randn(P * K, ld, generator=gen, **f16) * 1e-3).view(torch.int16)
+    yexp = torch.zeros(V, dtype=torch.int32, device=dev)
+    uexp = torch.zeros(P, dtype=torch.int32, device=dev)
+    proj = torch.empty(P, V, dtype=torch.float32, device=dev)
+    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    ja = _lib.ProjectArgs(V=V, T=T, K=K, P=P, ld_y=ld, ld_u=ld, yr_hi=_p(y_hi), yr_lo=_p(y_lo), u_hi=_p(u_hi),
+                          u_lo=_p(u_lo), yexp=_p(yexp), uexp=_p(uexp), yr_t=None, U=None, proj=_p(proj),
+                          flag=_p(flag))
+    st = _stream()
+    times = {}
+    for g in cands:
+        _lib.check(lib.ffs_reml_tune_tc_pairs(K, g), "ffs_reml_tune_tc_pairs")
+        _lib.check(lib.ffs_reml_project_tc(C.byref(ja), st), "ffs_reml_project_tc")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            _lib.check(lib.ffs_reml_project_tc(C.byref(ja), st), "ffs_reml_project_tc")
+        e1.record()
+        e1.synchronize()
+        times[g] = e0.elapsed_time(e1) / reps
+    if int(flag.item()) != 0:
+        raise RuntimeError("ffs_reml_project_tc: a bounded wait expired during autotuning")
+    best = min(times, key=times.get)
+    _lib.check(lib.ffs_reml_tune_tc_pairs(K, best), "ffs_reml_tune_tc_pairs")
+    _TUNED[key] = {"pairs": best, "ms": times}
+    return _TUNED[key]
+
+
 def padded_ld(T: int) -> int:
     return (T + LD_ALIGN - 1) // LD_ALIGN * LD_ALIGN
 
@@ -521,6 +578,8 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
 
     proj = torch.empty(P, V, dtype=torch.float32, device=dev)
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    if use_tc and not torch.cuda.is_current_stream_capturing():
+        autotune_projection(T, K, P, dev)
     ja = _lib.ProjectArgs(V=V, T=T, K=K, P=P, ld_y=ld, ld_u=ld, yr_hi=_p(pr.yr_hi), yr_lo=_p(pr.yr_lo),
                           u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yexp=_p(pr.yexp), uexp=_p(f.uexp),
                           yr_t=_p(pr.yr_t), U=_p(f.U), proj=_p(proj), flag=_p(flag))

@@ -246,6 +246,14 @@ typedef struct {
 } ffs_project_args;
 
 int ffs_reml_project_tc(const ffs_project_args* a, void* stream);
+
+/* Tile shape of ffs_reml_project_tc for designs of K columns: the pairs that
+ * share one B tile (pairs x K <= 256 columns of the MMA's N; 0 restores the
+ * widest tile, 256 / K pairs). Process-wide, thread-safe; the results do not
+ * depend on it (every pair's sums are formed in the same order), only the
+ * speed. The Python autotuner (fastfuncstuff_gb300.autotune_projection) times
+ * the candidates on the fit's shape and sets the fastest. */
+int ffs_reml_tune_tc_pairs(int K, int pairs);
 int ffs_reml_project_simt(const ffs_project_args* a, void* stream);
 
 /* Work-list form of ffs_reml_project_tc (no reference counterpart: the

@@ -506,3 +506,34 @@ class _no_warning:
 
     def __exit__(self, *a):
         return False
+
+
+def test_autotuner_picks_a_tile_and_results_do_not_depend_on_it():
+    """The projection's tile shape (pairs per B tile) is chosen by timing; every
+    candidate gives the same surface bit for bit (each pair's sums are formed
+    in the same order), so the choice only changes the speed."""
+    from fastfuncstuff_gb300 import autotune_projection
+    from fastfuncstuff_gb300 import _lib
+
+    rng = np.random.default_rng(9)
+    T, K, V = 300, 20, 3000
+    X = rng.standard_normal((T, K)).astype(np.float32)
+    Y = torch.from_numpy(rng.standard_normal((V, T)).astype(np.float32)).to(DEV)
+    g = torch.linspace(-0.8, 0.8, 17)
+    f = precompute_reml_grid(torch.from_numpy(X), T, g, g, DEV, run_starts=[0, 150])
+    tuned = autotune_projection(T, K, f.P, DEV, V=8192, reps=2)
+    assert tuned["pairs"] in (12, 6, 3) and set(tuned["ms"]) == {12, 6, 3}
+    lib = _lib.load()
+    surfs = []
+    orig = engine.autotune_projection
+    engine.autotune_projection = lambda *a, **k: None  # keep each forced tile shape
+    try:
+        for pairs in (12, 6, 3):
+            _lib.check(lib.ffs_reml_tune_tc_pairs(K, pairs), "tune")
+            so = engine.search(Y, f, hierarchical=False, projector="tc", keep_surface=True)
+            torch.cuda.synchronize()
+            surfs.append(so.surf.cpu())
+    finally:
+        engine.autotune_projection = orig
+        _lib.check(lib.ffs_reml_tune_tc_pairs(K, tuned["pairs"]), "tune")
+    assert torch.equal(surfs[0], surfs[1]) and torch.equal(surfs[0], surfs[2])
