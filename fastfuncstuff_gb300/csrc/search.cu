@@ -106,12 +106,13 @@ __global__ void __launch_bounds__(256) prep_kernel(ffs_prep_args a, int ld_s) {
     }
     if (lane == 0 && vs >= 0) a.scale[vs] = sc;
     if (a.feats) row_features(row, T, a.n_runs, a.run_start, a.feats + (size_t)v * 9);
-    if (a.yr_hi) {
+    if (a.yr_hi || a.yexp) {
       float amax = 0.f;
       for (int t = lane; t < T; t += 32) amax = fmaxf(amax, fabsf(row[t]));
       for (int off = 16; off > 0; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
       const int e = scale_exp(amax);
       if (lane == 0) a.yexp[v] = e;
+      if (!a.yr_hi) continue;
       uint16_t* hi = a.yr_hi + (size_t)v * a.ld_y;
       uint16_t* lo = a.yr_lo + (size_t)v * a.ld_y;
       for (int t = lane; t < a.ld_y; t += 32) {
@@ -198,15 +199,19 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
     for (int i = wid; i < nv; i += TILE_WARPS)
       row_features(Ys + (size_t)i * ld, T, a.n_runs, a.run_start, a.feats + (size_t)(v0 + i) * 9);
   }
-  if (a.yr_hi) {
+  if (a.yr_hi || a.yexp) {  // the split's exponent; the split itself with yr_hi
     for (int i = wid; i < nv; i += TILE_WARPS) {
       const float* row = Ys + (size_t)i * ld;
       const int v = v0 + i;
       float amax = 0.f;
-      for (int t = lane; t < T; t += 32) amax = fmaxf(amax, fabsf(row[t]));
+      for (int q = lane; q < nq; q += 32) {
+        const float4 x = reinterpret_cast<const float4*>(row)[q];
+        amax = fmaxf(fmaxf(amax, fabsf(x.x)), fmaxf(fabsf(x.y), fmaxf(fabsf(x.z), fabsf(x.w))));
+      }
       for (int off = 16; off > 0; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
       const int e = scale_exp(amax);
       if (lane == 0) a.yexp[v] = e;
+      if (!a.yr_hi) continue;
       // two samples per lane: 32-bit stores of (hi_t, hi_t+1)
       uint32_t* hi = reinterpret_cast<uint32_t*>(a.yr_hi + (size_t)v * a.ld_y);
       uint32_t* lo = reinterpret_cast<uint32_t*>(a.yr_lo + (size_t)v * a.ld_y);

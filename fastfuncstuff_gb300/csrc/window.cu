@@ -398,6 +398,49 @@ __global__ void __launch_bounds__(256) gather_rows_kernel(int n, const int* n_de
   }
 }
 
+// The same gathered fp16 rows formed from the fp32 rows: each thread one
+// 16-byte output word (8 samples) of one row, split as the prep kernel splits
+// (fp16 hi/lo of x * 2^yexp), so the prep need not store the split of every
+// voxel when only the windows' rows are gathered. Samples past T are zero.
+__global__ void __launch_bounds__(256) gather_split_kernel(int n, const int* n_dev, int T, int ld_y,
+                                                           const int* __restrict__ idx, const float* __restrict__ rows,
+                                                           const int* __restrict__ yexp, uint4* __restrict__ out_hi,
+                                                           uint4* __restrict__ out_lo, int* __restrict__ out_exp) {
+  const int m = n_dev ? min(n, *n_dev) : n;
+  const int nw = ld_y / 8;
+  const bool vec = (T & 3) == 0;
+  const long long total = (long long)m * nw;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / nw), k = (int)(e % nw);
+    const int v = idx[i];
+    const int ex = yexp[v];
+    const float* src = rows + (size_t)v * T;
+    const int t0 = 8 * k;
+    float x[8];
+    if (vec) {
+      const float4 a = t0 < T ? *reinterpret_cast<const float4*>(src + t0) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 b = t0 + 4 < T ? *reinterpret_cast<const float4*>(src + t0 + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+      x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) x[j] = t0 + j < T ? src[t0 + j] : 0.f;
+    }
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      uint16_t h0 = 0, l0 = 0, h1 = 0, l1 = 0;
+      if (t0 + 2 * j < T) split_fp16(ldexpf(x[2 * j], ex), h0, l0);
+      if (t0 + 2 * j + 1 < T) split_fp16(ldexpf(x[2 * j + 1], ex), h1, l1);
+      hw[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+      lw[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+    }
+    out_hi[(size_t)i * nw + k] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    out_lo[(size_t)i * nw + k] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+    if (k == 0) out_exp[i] = ex;
+  }
+}
+
 // out_t[t][i] = rows[idx[i]][t]: 32 x 32 tiles through shared memory
 // out_t[t][i] = rows[idx[i]][t]: 32 rows x 64 samples per CTA through shared
 // memory (eight loads in flight per thread)
@@ -461,18 +504,25 @@ extern "C" int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const i
                                uint16_t* out_lo, int* out_exp, float* out_t, void* stream) {
   clear_error();
   FFS_REQUIRE(n > 0 && T > 0 && ld_y >= T && ld_y % 8 == 0, "ffs_reml_gather: bad sizes");
-  FFS_REQUIRE(idx && yr_hi && yr_lo && yexp && out_hi && out_lo && out_exp && (!out_t || yr_rows),
-              "ffs_reml_gather: null buffer");
+  FFS_REQUIRE(idx && yexp && out_hi && out_lo && out_exp && (!out_t || yr_rows), "ffs_reml_gather: null buffer");
+  FFS_REQUIRE((yr_hi && yr_lo) || (!yr_hi && !yr_lo && yr_rows),
+              "ffs_reml_gather: yr_hi and yr_lo, or (both NULL) the fp32 rows to split");
   for (const void* ptr : {(const void*)yr_hi, (const void*)yr_lo, (const void*)out_hi, (const void*)out_lo})
     FFS_REQUIRE(((uintptr_t)ptr & 15) == 0, "ffs_reml_gather: fp16 rows must be 16-byte aligned");
+  FFS_REQUIRE(yr_hi || ((uintptr_t)yr_rows & 15) == 0, "ffs_reml_gather: fp32 rows must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
   int sms = 0;
   FFS_CUDA(sm_count(&sms));
   const int blocks = (int)std::min<long long>(ceil_div((long long)n * (ld_y / 8), 256), (long long)sms * 8);
-  gather_rows_kernel<<<blocks, 256, 0, st>>>(n, n_dev, ld_y, idx, reinterpret_cast<const uint4*>(yr_hi),
-                                                      reinterpret_cast<const uint4*>(yr_lo), yexp,
-                                                      reinterpret_cast<uint4*>(out_hi),
-                                                      reinterpret_cast<uint4*>(out_lo), out_exp);
+  if (yr_hi) {
+    gather_rows_kernel<<<blocks, 256, 0, st>>>(n, n_dev, ld_y, idx, reinterpret_cast<const uint4*>(yr_hi),
+                                                        reinterpret_cast<const uint4*>(yr_lo), yexp,
+                                                        reinterpret_cast<uint4*>(out_hi),
+                                                        reinterpret_cast<uint4*>(out_lo), out_exp);
+  } else {
+    gather_split_kernel<<<blocks, 256, 0, st>>>(n, n_dev, T, ld_y, idx, yr_rows, yexp, reinterpret_cast<uint4*>(out_hi),
+                                                reinterpret_cast<uint4*>(out_lo), out_exp);
+  }
   if (out_t) {
     FFS_REQUIRE(ceil_div(T, 64) <= 65535, "ffs_reml_gather: T=%d too long", T);
     gather_transpose_kernel<<<dim3(ceil_div(n, 32), ceil_div(T, 64)), dim3(32, 8), 0, st>>>(n, n_dev, T, idx,

@@ -513,8 +513,13 @@ def design_basis(X: torch.Tensor, with_constant: bool = False):
 
 def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core: bool = True,
          idx: torch.Tensor | None = None, want_yr_t: bool = True, layout: RunLayout | None = None,
-         scale: torch.Tensor | None = None, want_rows: bool = False, q0: torch.Tensor | None = None) -> PrepOut:
+         scale: torch.Tensor | None = None, want_rows: bool = False, q0: torch.Tensor | None = None,
+         split: bool = True) -> PrepOut:
     """Per-voxel scaling and residualisation (and the fp16 split for the GEMM).
+
+    With ``tensor_core`` and ``split=False`` only the split's exponents
+    (``yexp``) are formed: a caller that gathers a subset of the rows splits
+    them from ``rows`` while gathering (``ffs_reml_gather``).
 
     ``idx`` (int32, device) processes the rows Y[idx] in that order (every
     output but ``scale`` is indexed by position in ``idx``; ``scale`` by the
@@ -532,8 +537,8 @@ def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core:
     if scale is None:
         scale = torch.empty(V, dtype=torch.float32, device=dev)
     yr_t = torch.empty(T, n, dtype=torch.float32, device=dev) if want_yr_t else None
-    yr_hi = torch.empty(n, ld, dtype=torch.int16, device=dev) if tensor_core else None
-    yr_lo = torch.empty(n, ld, dtype=torch.int16, device=dev) if tensor_core else None
+    yr_hi = torch.empty(n, ld, dtype=torch.int16, device=dev) if tensor_core and split else None
+    yr_lo = torch.empty(n, ld, dtype=torch.int16, device=dev) if tensor_core and split else None
     yexp = torch.empty(n, dtype=torch.int32, device=dev) if tensor_core else None
     feats = rs = None
     if layout is not None:

@@ -325,8 +325,9 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
     st = _st()
     Y = Y.float().contiguous()
     c = _grid_consts(g, dev)
+    # the windows' rows are split to fp16 while they are gathered (from rows)
     p1 = engine.prep(Y, f, do_scale=do_scale, tensor_core=True, want_yr_t=False, layout=layout, want_rows=True,
-                     q0=q0)
+                     q0=q0, split=False)
     scale = p1.scale
     prop = proposal.forward(p1.feats)
     center = torch.empty(V, dtype=torch.int32, device=dev)

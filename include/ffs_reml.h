@@ -505,7 +505,9 @@ int ffs_reml_centers(int V, const float* prop, const float* a_axis, int n_a, con
                      int* center, void* stream);
 
 /* Rows of the prep outputs in the order idx[0..n): out_hi/out_lo[i] =
- * yr_hi/yr_lo[idx[i]] ([.][ld_y] fp16 bits), out_exp[i] = yexp[idx[i]] and,
+ * yr_hi/yr_lo[idx[i]] ([.][ld_y] fp16 bits) -- or, with yr_hi = yr_lo = NULL,
+ * the same split formed here from yr_rows[idx[i]] and yexp (so the prep need
+ * not store every voxel's split) --, out_exp[i] = yexp[idx[i]] and,
  * when out_t is given, out_t[t][i] = yr_rows[idx[i]][t] ([T][n], time-major)
  * for the windowed refine's sorted operands. With n_dev (device int) only the
  * rows i < min(n, *n_dev) are written. */
