@@ -368,14 +368,19 @@ def fit_glm_arma11(
         # first batch (against the design basis) runs on the main one
         overlap = K <= engine.BASIS_MAX_K
         side = _side_stream(device) if overlap else None
+        center = None
+        if overlap:
+            # Q0 and the centring test of the design (one kernel pair), queued
+            # first: the build's stream waits for them
+            q0, cflag, ccoef = engine.design_basis(Xd, with_constant=True)
+            center = (cflag, ccoef)
         factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt,
                                        with_tc=projector == "tc" and K <= 256, stream=side, sets=sets,
-                                       afull=afull)
+                                       afull=afull, center=center)
         if overlap:
             built = torch.cuda.Event()
             built.record(side)
             main = torch.cuda.current_stream()
-            q0 = engine.design_basis(Xd)
 
             def join():
                 main.wait_event(built)
