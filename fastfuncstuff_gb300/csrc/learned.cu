@@ -127,34 +127,58 @@ __device__ __forceinline__ float gelu_grad(float z) {
   return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * expf(-0.5f * z * z) * 0.3989422804014327f;
 }
 
+// Two samples per thread: every weight read from shared memory serves both,
+// and the two dependent FMA chains of a unit interleave.
+constexpr int FWD_PER_THREAD = 2;
+
 __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* __restrict__ prm, const float* __restrict__ x,
                                                           int B, float* __restrict__ out) {
   __shared__ float P[N_PARAMS];
   for (int i = threadIdx.x; i < N_PARAMS; i += blockDim.x) P[i] = prm[i];
   __syncthreads();
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= B) return;
-  float xi[NI], h1[NH];
+  const int s0 = (blockIdx.x * blockDim.x + threadIdx.x) * FWD_PER_THREAD;
+  if (s0 >= B) return;
+  const bool two = s0 + 1 < B;
+  float xa[NI], xb[NI], ha[NH], hb[NH];
 #pragma unroll
-  for (int i = 0; i < NI; ++i) xi[i] = x[(size_t)s * NI + i];
-#pragma unroll 4
-  for (int u = 0; u < NH; ++u) {
-    float z = P[OFF_B1 + u];
-#pragma unroll
-    for (int i = 0; i < NI; ++i) z = fmaf(P[OFF_W1 + u * NI + i], xi[i], z);
-    h1[u] = gelu(z);
+  for (int i = 0; i < NI; ++i) {
+    xa[i] = x[(size_t)s0 * NI + i];
+    xb[i] = two ? x[(size_t)(s0 + 1) * NI + i] : 0.f;
   }
-  float o0 = P[OFF_B3], o1 = P[OFF_B3 + 1];
-  for (int u = 0; u < NH; ++u) {
-    float z = P[OFF_B2 + u];
 #pragma unroll
-    for (int k = 0; k < NH; ++k) z = fmaf(P[OFF_W2 + u * NH + k], h1[k], z);
-    const float h = gelu(z);
-    o0 = fmaf(P[OFF_W3 + u], h, o0);
-    o1 = fmaf(P[OFF_W3 + NH + u], h, o1);
+  for (int u = 0; u < NH; ++u) {
+    float za = P[OFF_B1 + u], zb = za;
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+      const float w = P[OFF_W1 + u * NI + i];
+      za = fmaf(w, xa[i], za);
+      zb = fmaf(w, xb[i], zb);
+    }
+    ha[u] = gelu(za);
+    hb[u] = gelu(zb);
   }
-  out[(size_t)s * NO] = o0;
-  out[(size_t)s * NO + 1] = o1;
+  float oa0 = P[OFF_B3], oa1 = P[OFF_B3 + 1], ob0 = oa0, ob1 = oa1;
+  for (int u = 0; u < NH; ++u) {
+    float za = P[OFF_B2 + u], zb = za;
+#pragma unroll
+    for (int k = 0; k < NH; ++k) {
+      const float w = P[OFF_W2 + u * NH + k];
+      za = fmaf(w, ha[k], za);
+      zb = fmaf(w, hb[k], zb);
+    }
+    const float ga = gelu(za), gb = gelu(zb);
+    const float w0 = P[OFF_W3 + u], w1 = P[OFF_W3 + NH + u];
+    oa0 = fmaf(w0, ga, oa0);
+    oa1 = fmaf(w1, ga, oa1);
+    ob0 = fmaf(w0, gb, ob0);
+    ob1 = fmaf(w1, gb, ob1);
+  }
+  out[(size_t)s0 * NO] = oa0;
+  out[(size_t)s0 * NO + 1] = oa1;
+  if (two) {
+    out[(size_t)(s0 + 1) * NO] = ob0;
+    out[(size_t)(s0 + 1) * NO + 1] = ob1;
+  }
 }
 
 // One CTA = TILE samples. Forward, loss, backward into shared memory, then the
@@ -280,7 +304,7 @@ extern "C" int ffs_arma_simulate(int V, int T, int K, int n_runs, const int* run
 extern "C" int ffs_mlp_forward(const float* params, const float* x, int B, float* out, void* stream) {
   clear_error();
   FFS_REQUIRE(params && x && out && B > 0, "ffs_mlp_forward: bad arguments");
-  mlp_forward_kernel<<<ceil_div(B, 128), 128, 0, (cudaStream_t)stream>>>(params, x, B, out);
+  mlp_forward_kernel<<<ceil_div(B, 128 * FWD_PER_THREAD), 128, 0, (cudaStream_t)stream>>>(params, x, B, out);
   return check_launch("mlp_forward_kernel");
 }
 
