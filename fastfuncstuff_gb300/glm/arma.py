@@ -367,7 +367,9 @@ def fit_glm_arma11(
         # the grid build runs on a side stream while the residualisation of the
         # first batch (against the design basis) runs on the main one
         overlap = K <= engine.BASIS_MAX_K
-        side = _side_stream(device) if overlap else None
+        # beside the prep on a side stream, except under the per-call stage
+        # timer, whose stage times are then each kernel's own
+        side = _side_stream(device) if overlap and not engine.stage_timer_active() else None
         center = None
         if overlap:
             # Q0 and the centring test of the design (one kernel pair), queued

@@ -75,6 +75,10 @@ def set_stage_timer(timer: StageTimer | None) -> None:
     _TIMER = timer
 
 
+def stage_timer_active() -> bool:
+    return _TIMER is not None
+
+
 def _run(name: str, fn, *args, launches: int | None = None) -> None:
     t = _TIMER
     if t is None or torch.cuda.is_current_stream_capturing():
