@@ -122,28 +122,38 @@ struct CritArgs {
 constexpr int CRIT_TB = 16;  // steps per partial sum and sample prefetch
 
 // One CTA per tile of WTILE sorted rows that share a window centre, one thread
-// per row. The window rows are walked two at a time (CRIT_ROWS), so the
-// series is read ceil(5 / 2) = 3 times instead of once per window row; y'y is
-// summed in the first pass. Each window row's coefficients (-m, 1/D of its
-// <= 5 non-identity pairs, which share a and so the AR filter c_t) are staged
-// in shared memory, then every thread runs the recurrences of both rows over
-// its series with 16 samples in flight. As in the surface kernel, a step whose
-// coefficients equal the previous step's (for every pair of that window row)
-// reuses the registers, and a block of 16 such steps sums v^2 alone and
-// scales the block sum by 1/D once; each row keeps its own steady flags, so a
-// pair's arithmetic does not depend on which row it is walked beside.
-constexpr int CRIT_ROWS = 1;
+// per row, one pass over each series: the time axis is walked in chunks of
+// WCH steps, for which the coefficients (-m, 1/D) of every window row's <= 5
+// non-identity pairs and the row's AR filter c_t (its pairs share a) are
+// staged in shared memory; each 16-sample block of the series is loaded once
+// and advances the recurrences of all window rows, whose per-thread states
+// (v_{t-1} and the running sum of v^2 / D of each pair) live in shared memory
+// between blocks. As in the surface kernel, a step whose coefficients equal
+// the previous step's (for every pair of that window row) reuses the
+// registers, and a block of 16 such steps sums v^2 alone and scales the block
+// sum by 1/D once; each row keeps its own steady flags, so a pair's
+// arithmetic does not depend on the other rows. y'y is summed on the way.
+constexpr int WCH = 64;  // steps per staged chunk (a multiple of CRIT_TB)
+constexpr int WCB = WCH / CRIT_TB;
+
+__host__ __device__ inline size_t crit_smem_bytes() {
+  return sizeof(float2) * WIN * WIN * (WCH + 1) + sizeof(float) * WIN * (WCH + 1) +
+         2 * sizeof(float) * WIN * WIN * WTILE + WIN * WCH + WIN * WCB;
+}
 
 __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const int2* tiles, const int* n_tiles) {
-  extern __shared__ float2 tab[];  // [CRIT_ROWS][WIN][T] (-m, 1/D) of the rows' pairs
-  float* cs = reinterpret_cast<float*>(tab + CRIT_ROWS * WIN * (size_t)w.T);  // [CRIT_ROWS][T] AR filter c_t
-  uint8_t* steady = reinterpret_cast<uint8_t*>(cs + CRIT_ROWS * (size_t)w.T);  // [CRIT_ROWS][T]
-  const int nblk = (w.T + CRIT_TB - 1) / CRIT_TB;
-  uint8_t* bsteady = steady + CRIT_ROWS * (size_t)w.T;                          // [CRIT_ROWS][nblk]
+  extern __shared__ float2 tab[];  // [WIN rows][WIN pairs][WCH + 1]: steps c0 - 1 .. c0 + WCH - 1
+  float* cs = reinterpret_cast<float*>(tab + WIN * WIN * (WCH + 1));  // [WIN][WCH + 1] AR filter c_t
+  float* svv = cs + WIN * (WCH + 1);                                   // [WIN * WIN][WTILE] v_{t-1}
+  float* sst = svv + WIN * WIN * WTILE;                                // [WIN * WIN][WTILE] sum of v^2 / D
+  uint8_t* steady = reinterpret_cast<uint8_t*>(sst + WIN * WIN * WTILE);  // [WIN][WCH]
+  uint8_t* bsteady = steady + WIN * WCH;                                   // [WIN][WCB]
+  __shared__ int s_pr[WIN][WIN], s_col[WIN][WIN], s_np[WIN], s_ident;
   if ((int)blockIdx.x >= *n_tiles) return;
   const int2 tl = tiles[blockIdx.x];
-  const int i = tl.x + threadIdx.x;
-  const bool live = (int)threadIdx.x < tl.y;
+  const int tid = threadIdx.x;
+  const int i = tl.x + tid;
+  const bool live = tid < tl.y;
   const int c = w.center[tl.x];  // every row of the tile has this centre
   int a0, wa, b0, wb;
   window_of(c, w.n_a, w.n_b, a0, wa, b0, wb);
@@ -153,96 +163,82 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
   const float* yrow = w.rows + (size_t)w.idx[live ? i : tl.x] * w.T;
   const bool vec = (w.T & 3) == 0;
 
-  // identity pairs of the window (R = I: criterion d = 0)
-  bool has_ident = false;
-  for (int ra = 0; ra < wa; ++ra)
-    for (int rb = 0; rb < wb; ++rb) {
-      const int p = w.lattice[(a0 + ra) * w.n_b + b0 + rb];
-      if (p >= 0 && w.ident[p]) has_ident = true;
-    }
-
-  // best non-identity window pair
-  int best = -1, bcell = -1;
-  float bd = INFINITY;
-  float yy = 0.f;  // y'y in the full grid's blocks (the identity chunk of the surface kernel)
-  for (int ra0 = 0; ra0 < wa; ra0 += CRIT_ROWS) {
-    int pr[CRIT_ROWS][WIN], col[CRIT_ROWS][WIN], np[CRIT_ROWS];
-#pragma unroll
-    for (int r = 0; r < CRIT_ROWS; ++r) {
-      np[r] = 0;
-      const int ra = ra0 + r;
-#pragma unroll
+  // the window's non-identity pairs by row (compacted), and whether it holds
+  // an identity pair (R = I: criterion d = 0)
+  if (tid == 0) {
+    int hid = 0;
+    for (int ra = 0; ra < WIN; ++ra) {
+      int n = 0;
       for (int rb = 0; rb < WIN; ++rb) {
-        pr[r][rb] = -1;
-        col[r][rb] = 0;
+        s_pr[ra][rb] = -1;
+        s_col[ra][rb] = 0;
+      }
+      for (int rb = 0; rb < WIN; ++rb) {
         const int p = (ra < wa && rb < wb) ? w.lattice[(a0 + ra) * w.n_b + b0 + rb] : -1;
-        if (p >= 0 && !w.ident[p]) {
-#pragma unroll
-          for (int k = 0; k < WIN; ++k)
-            if (k == np[r]) {
-              pr[r][k] = p;
-              col[r][k] = rb;
-            }
-          ++np[r];
+        if (p < 0) continue;
+        if (w.ident[p]) {
+          hid = 1;
+        } else {
+          s_pr[ra][n] = p;
+          s_col[ra][n] = rb;
+          ++n;
         }
       }
+      s_np[ra] = n;
     }
-    const bool first = ra0 == 0;
-    if (np[0] == 0 && (CRIT_ROWS < 2 || np[1] == 0) && !first) continue;  // uniform over the CTA
-    __syncthreads();
-    // each row's pairs share a, so one AR filter c_t; stage (-m, 1/D) per pair
-    for (int idx = threadIdx.x; idx < CRIT_ROWS * WIN * T; idx += blockDim.x) {
-      const int rg = idx / T, t = idx % T;
+    s_ident = hid;
+  }
+  for (int e = tid; e < WIN * WIN * WTILE; e += blockDim.x) {
+    svv[e] = 0.f;
+    sst[e] = 0.f;
+  }
+  __syncthreads();
+  const bool has_ident = s_ident != 0;
+
+  float yy = 0.f;  // y'y in the full grid's blocks (the identity chunk of the surface kernel)
+  float yp = 0.f;
+  for (int c0 = 0; c0 < T; c0 += WCH) {
+    const int cn = min(WCH, T - c0);
+    __syncthreads();  // the previous chunk's tables are no longer read
+    for (int e = tid; e < WIN * WIN * (cn + 1); e += blockDim.x) {
+      const int rg = e / (cn + 1), s = e % (cn + 1);
       const int r = rg / WIN, g = rg % WIN;
-      int p = -1;
-#pragma unroll
-      for (int rr = 0; rr < CRIT_ROWS; ++rr)
-#pragma unroll
-        for (int k = 0; k < WIN; ++k)
-          if (rr == r && k == g) p = pr[rr][k];
-      if (p >= 0) {
+      const int t = c0 - 1 + s;
+      const int p = s_pr[r][g];
+      float2 v2 = make_float2(0.f, 0.f);
+      float cv = 0.f;
+      if (p >= 0 && t >= 0) {
         const float4 q = w.coef[(size_t)p * T + t];
-        tab[(size_t)rg * T + t] = make_float2(-q.y, q.z);
-        if (g == 0) cs[(size_t)r * T + t] = q.x;
-      } else if (g == 0) {
-        cs[(size_t)r * T + t] = 0.f;
+        v2 = make_float2(-q.y, q.z);
+        cv = q.x;
       }
+      tab[(size_t)rg * (WCH + 1) + s] = v2;
+      if (g == 0) cs[(size_t)r * (WCH + 1) + s] = cv;
     }
     __syncthreads();
     // steady steps of each row: every pair's coefficients (and c) equal the
     // previous step's
-    for (int idx = threadIdx.x; idx < CRIT_ROWS * T; idx += blockDim.x) {
-      const int r = idx / T, t = idx % T;
-      int nr = 0;
-#pragma unroll
-      for (int rr = 0; rr < CRIT_ROWS; ++rr)
-        if (rr == r) nr = np[rr];
-      const float* cr = cs + (size_t)r * T;
-      bool same = t > 0 && cr[t] == cr[t - 1];
-      for (int g = 0; g < nr && same; ++g) {
-        const float2 x = tab[((size_t)r * WIN + g) * T + t], y = tab[((size_t)r * WIN + g) * T + t - 1];
+    for (int e = tid; e < WIN * cn; e += blockDim.x) {
+      const int r = e / cn, s = e % cn;
+      const float* cr = cs + (size_t)r * (WCH + 1);
+      bool same = c0 + s > 0 && cr[s + 1] == cr[s];
+      for (int g = 0; g < s_np[r] && same; ++g) {
+        const float2 x = tab[(size_t)(r * WIN + g) * (WCH + 1) + s + 1];
+        const float2 y = tab[(size_t)(r * WIN + g) * (WCH + 1) + s];
         same = x.x == y.x && x.y == y.y;
       }
-      steady[idx] = same ? 1 : 0;
+      steady[r * WCH + s] = same ? 1 : 0;
     }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < CRIT_ROWS * nblk; idx += blockDim.x) {
-      const int r = idx / nblk, bk = idx % nblk;
-      bool all = bk * CRIT_TB + CRIT_TB <= T;
-      for (int t = bk * CRIT_TB; t < bk * CRIT_TB + CRIT_TB && all; ++t) all = steady[(size_t)r * T + t] != 0;
-      bsteady[idx] = all ? 1 : 0;
+    for (int e = tid; e < WIN * WCB; e += blockDim.x) {
+      const int r = e / WCB, bk = e % WCB;
+      bool all = bk * CRIT_TB + CRIT_TB <= cn;
+      for (int s = bk * CRIT_TB; s < bk * CRIT_TB + CRIT_TB && all; ++s) all = steady[r * WCH + s] != 0;
+      bsteady[e] = all ? 1 : 0;
     }
     __syncthreads();
-    float vv[CRIT_ROWS][WIN], sq[CRIT_ROWS][WIN], st[CRIT_ROWS][WIN], nm[CRIT_ROWS][WIN], id[CRIT_ROWS][WIN];
-    float cc[CRIT_ROWS];
-#pragma unroll
-    for (int r = 0; r < CRIT_ROWS; ++r) {
-      cc[r] = 0.f;
-#pragma unroll
-      for (int g = 0; g < WIN; ++g) vv[r][g] = sq[r][g] = st[r][g] = nm[r][g] = id[r][g] = 0.f;
-    }
-    float yp = 0.f;
-    for (int t0 = 0; t0 < T; t0 += CRIT_TB) {
+    for (int bs = 0; bs < cn; bs += CRIT_TB) {
+      const int t0 = c0 + bs;
       float yb[CRIT_TB];
       if (vec) {
 #pragma unroll
@@ -258,84 +254,100 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
 #pragma unroll
         for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yrow[t0 + k] : 0.f;
       }
-      if (first) {
+      {
         float yy_b = 0.f;
 #pragma unroll
         for (int k = 0; k < CRIT_TB; ++k) yy_b = fmaf(yb[k], yb[k], yy_b);
         yy += yy_b;
       }
+      for (int r = 0; r < WIN; ++r) {
+        const int npr = s_np[r];
+        if (npr == 0) continue;  // uniform over the CTA
+        const float2* tr = tab + (size_t)r * WIN * (WCH + 1);
+        const float* crr = cs + (size_t)r * (WCH + 1);
+        float vv[WIN], st[WIN], sq[WIN], nm[WIN], id[WIN];
+        // the coefficients at the block's first step: the table's value there
+        // equals what a step-by-step walk holds in its registers
+        float cc = crr[bs + 1];
 #pragma unroll
-      for (int r = 0; r < CRIT_ROWS; ++r) {
-        if (np[r] == 0) continue;  // uniform over the CTA
+        for (int g = 0; g < WIN; ++g) {
+          const bool on = g < npr;
+          vv[g] = on ? svv[(r * WIN + g) * WTILE + tid] : 0.f;
+          st[g] = on ? sst[(r * WIN + g) * WTILE + tid] : 0.f;
+          const float2 q = on ? tr[(size_t)g * (WCH + 1) + bs + 1] : make_float2(0.f, 0.f);
+          nm[g] = q.x;
+          id[g] = q.y;
+          sq[g] = 0.f;
+        }
         float ypr = yp;
-        if (bsteady[(size_t)r * nblk + t0 / CRIT_TB]) {
+        if (bsteady[r * WCB + bs / CRIT_TB]) {
           // CRIT_TB steady steps: coefficients in registers, sum of v^2 alone
 #pragma unroll
           for (int k = 0; k < CRIT_TB; ++k) {
-            const float z = fmaf(-cc[r], ypr, yb[k]);
+            const float z = fmaf(-cc, ypr, yb[k]);
             ypr = yb[k];
 #pragma unroll
             for (int g = 0; g < WIN; ++g) {
-              vv[r][g] = fmaf(nm[r][g], vv[r][g], z);
-              sq[r][g] = fmaf(vv[r][g], vv[r][g], sq[r][g]);
+              vv[g] = fmaf(nm[g], vv[g], z);
+              sq[g] = fmaf(vv[g], vv[g], sq[g]);
             }
           }
 #pragma unroll
-          for (int g = 0; g < WIN; ++g) {
-            st[r][g] = fmaf(sq[r][g], id[r][g], st[r][g]);
-            sq[r][g] = 0.f;
-          }
+          for (int g = 0; g < WIN; ++g) st[g] = fmaf(sq[g], id[g], st[g]);
         } else {
-          const uint8_t* sr = steady + (size_t)r * T;
-          const float2* tr = tab + (size_t)r * WIN * T;
+          const uint8_t* sr = steady + r * WCH;
 #pragma unroll
           for (int k = 0; k < CRIT_TB; ++k) {
-            const int t = t0 + k;
-            if (t < T) {
-              if (!sr[t]) {
-                cc[r] = cs[(size_t)r * T + t];
+            if (t0 + k < T) {
+              if (!sr[bs + k]) {
+                cc = crr[bs + k + 1];
 #pragma unroll
                 for (int g = 0; g < WIN; ++g) {
-                  if (g < np[r]) {
-                    const float2 q = tr[(size_t)g * T + t];
-                    nm[r][g] = q.x;
-                    id[r][g] = q.y;
+                  if (g < npr) {
+                    const float2 q = tr[(size_t)g * (WCH + 1) + bs + k + 1];
+                    nm[g] = q.x;
+                    id[g] = q.y;
                   }
                 }
               }
-              const float z = fmaf(-cc[r], ypr, yb[k]);
+              const float z = fmaf(-cc, ypr, yb[k]);
               ypr = yb[k];
 #pragma unroll
               for (int g = 0; g < WIN; ++g) {
-                vv[r][g] = fmaf(nm[r][g], vv[r][g], z);
-                sq[r][g] = fmaf(vv[r][g] * id[r][g], vv[r][g], sq[r][g]);
+                vv[g] = fmaf(nm[g], vv[g], z);
+                sq[g] = fmaf(vv[g] * id[g], vv[g], sq[g]);
               }
             }
           }
 #pragma unroll
-          for (int g = 0; g < WIN; ++g) {
-            st[r][g] += sq[r][g];
-            sq[r][g] = 0.f;
+          for (int g = 0; g < WIN; ++g) st[g] += sq[g];
+        }
+#pragma unroll
+        for (int g = 0; g < WIN; ++g) {
+          if (g < npr) {
+            svv[(r * WIN + g) * WTILE + tid] = vv[g];
+            sst[(r * WIN + g) * WTILE + tid] = st[g];
           }
         }
       }
       yp = yb[CRIT_TB - 1];
     }
-#pragma unroll
-    for (int r = 0; r < CRIT_ROWS; ++r) {
-      const int ra = ra0 + r;
-#pragma unroll
-      for (int g = 0; g < WIN; ++g) {
-        if (g < np[r] && live) {
-          const int p = pr[r][g];
-          const float rss = fmaxf(st[r][g] - w.winproj[(size_t)i * WSLOTS + ra * WIN + col[r][g]], 0.f);
-          const float d = w.dcf[p] + (float)Tk * log1pf((rss - yy) / (yy + 1e-10f));
-          if (d < bd || (d == bd && p < best) || best < 0) {
-            bd = d;
-            best = p;
-            bcell = (a0 + ra) * w.n_b + b0 + col[r][g];
-          }
-        }
+  }
+
+  // best non-identity window pair
+  int best = -1, bcell = -1;
+  float bd = INFINITY;
+  for (int ra = 0; ra < WIN; ++ra) {
+    for (int g = 0; g < s_np[ra]; ++g) {
+      if (!live) break;
+      const int p = s_pr[ra][g];
+      const float stv = sst[(ra * WIN + g) * WTILE + tid];
+      const float rss = fmaxf(stv - w.winproj[(size_t)i * WSLOTS + ra * WIN + s_col[ra][g]], 0.f);
+      const float d = w.dcf[p] + (float)Tk * log1pf((rss - yy) / (yy + 1e-10f));
+      if (d < bd || (d == bd && p < best) || best < 0) {
+        bd = d;
+        best = p;
+        bcell = (a0 + ra) * w.n_b + b0 + s_col[ra][g];
       }
     }
   }
@@ -561,8 +573,7 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
   FFS_REQUIRE(lattice && idx && center && tiles && n_tiles && rows && coef && winproj && dcf && ident && c_p0 &&
                   best && dbest && crit0 && fallback && best_cell,
               "ffs_reml_window: null buffer");
-  const size_t smem = CRIT_ROWS * ((sizeof(float2) * WIN + sizeof(float) + 1) * (size_t)T + ceil_div(T, CRIT_TB));
-  FFS_REQUIRE(smem <= 200 * 1024, "ffs_reml_window: T=%d too long", T);
+  const size_t smem = crit_smem_bytes();
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(window_crit_kernel), smem));
   FFS_REQUIRE(((uintptr_t)rows & 15) == 0, "ffs_reml_window: rows must be 16-byte aligned");
   CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, rows, reinterpret_cast<const float4*>(coef), winproj, dcf,
