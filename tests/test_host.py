@@ -251,3 +251,31 @@ def test_column_sets_plan_layout_and_blocks():
     np.testing.assert_allclose(two.C[1], 4 * two.C[0], rtol=1e-6)
     with pytest.raises(IndexError):
         engine.column_sets_plan([[0, -1]], d["X"])
+
+
+def test_dsort_prepare_guard_expansion_and_errors():
+    """-dsort inputs as the kernel reads them (fastfuncstuff/glm/arma.py:3207-3245,
+    :3385-3397, :3931-3945): (V, T) is one dataset; a constant nonzero series is
+    replaced by its dataset's mean over the other voxels (all-zero columns stay);
+    dsort_run_bounds expands each set into one zero-padded column per run; a
+    wrong shape is a ValueError. Checked against the oracle's restatement."""
+    from fastfuncstuff_gb300.glm import engine
+
+    rng = np.random.default_rng(8)
+    V, T = 12, 30
+    D = rng.standard_normal((V, 2, T)).astype(np.float32)
+    D[1, 0] = 3.0          # constant: replaced
+    D[2, 1] = 0.0          # all zero: kept
+    with pytest.warns(UserWarning, match="constant"):
+        got = engine.dsort_prepare(D, V, T, None, torch.device("cpu")).numpy()
+    ref = o.dsort_constant_guard(D)
+    np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-7)
+    assert not got[2, 1].any()
+    one = engine.dsort_prepare(D[:, 1], V, T, None, torch.device("cpu"))
+    assert one.shape == (V, 1, T)
+    rb = [0, 12, 30]
+    exp = engine.dsort_prepare(D[3:5], 2, T, rb, torch.device("cpu")).numpy()
+    np.testing.assert_allclose(exp, o.dsort_expand(D[3:5], rb), rtol=0, atol=0)
+    assert exp.shape == (2, 4, T) and not exp[:, 0, 12:].any() and not exp[:, 1, :12].any()
+    with pytest.raises(ValueError, match="dsort must be"):
+        engine.dsort_prepare(D[:, :, :T - 1], V, T, None, torch.device("cpu"))
