@@ -428,16 +428,29 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
       m = warp_sum(s) / (float)T;
     }
     float sy = 0.f;
-    for (int q = lane; q < nq; q += 32) {
-      const float4 y = row4[q];
-      const int t = 4 * q;
-      float4 r;
-      r.x = __fdiv_rn(__fsub_rn(y.x, m), sc);
-      r.y = t + 1 < T ? __fdiv_rn(__fsub_rn(y.y, m), sc) : 0.f;
-      r.z = t + 2 < T ? __fdiv_rn(__fsub_rn(y.z, m), sc) : 0.f;
-      r.w = t + 3 < T ? __fdiv_rn(__fsub_rn(y.w, m), sc) : 0.f;
-      row4[q] = r;
-      sy += ((r.x + r.y) + r.z) + r.w;
+    if (vec) {  // whole quads: no padding inside the row
+      for (int q = lane; q < nq; q += 32) {
+        const float4 y = row4[q];
+        float4 r;
+        r.x = __fdiv_rn(__fsub_rn(y.x, m), sc);
+        r.y = __fdiv_rn(__fsub_rn(y.y, m), sc);
+        r.z = __fdiv_rn(__fsub_rn(y.z, m), sc);
+        r.w = __fdiv_rn(__fsub_rn(y.w, m), sc);
+        row4[q] = r;
+        sy += ((r.x + r.y) + r.z) + r.w;
+      }
+    } else {
+      for (int q = lane; q < nq; q += 32) {
+        const float4 y = row4[q];
+        const int t = 4 * q;
+        float4 r;
+        r.x = __fdiv_rn(__fsub_rn(y.x, m), sc);
+        r.y = t + 1 < T ? __fdiv_rn(__fsub_rn(y.y, m), sc) : 0.f;
+        r.z = t + 2 < T ? __fdiv_rn(__fsub_rn(y.z, m), sc) : 0.f;
+        r.w = t + 3 < T ? __fdiv_rn(__fsub_rn(y.w, m), sc) : 0.f;
+        row4[q] = r;
+        sy += ((r.x + r.y) + r.z) + r.w;
+      }
     }
     sy = warp_sum(sy);
     if (lane == 0) {
@@ -464,11 +477,11 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
       const int t = 4 * q;
       float d = r.x - mu;
       sst = fmaf(d, d, sst);
-      d = t + 1 < T ? r.y - mu : 0.f;
+      d = (vec || t + 1 < T) ? r.y - mu : 0.f;
       sst = fmaf(d, d, sst);
-      d = t + 2 < T ? r.z - mu : 0.f;
+      d = (vec || t + 2 < T) ? r.z - mu : 0.f;
       sst = fmaf(d, d, sst);
-      d = t + 3 < T ? r.w - mu : 0.f;
+      d = (vec || t + 3 < T) ? r.w - mu : 0.f;
       sst = fmaf(d, d, sst);
     }
     sst = warp_sum(sst);
