@@ -1,4 +1,4 @@
-"""The reference's default CPU fit restated with torch CPU kernels -- TIMED BASELINE ONLY.
+"""The reference's default CPU fit restated with torch CPU kernels -- timed CPU baseline only.
 
 This is the CPU baseline that ``bench.py`` times (``cpu_baseline`` and
 ``--impl reference``): the reference's own CPU algorithm for the float32 default
