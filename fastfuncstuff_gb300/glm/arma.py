@@ -20,8 +20,8 @@ and lambda in float64, no std scaling: the likelihood is that of the raw data)
 and returns float64 tensors; the arithmetic is this build's (FP64 factors,
 fp32 / split-bf16 voxel work).
 
-Options outside this path (OLS side fits, ``dsort``, global ARMA estimation,
-AFNI-faithful banded covariances) raise NotImplementedError.
+Options outside this path (OLS side fits, AFNI-faithful banded covariances)
+raise NotImplementedError.
 """
 
 from __future__ import annotations
@@ -270,8 +270,8 @@ def fit_glm_arma11(
         _unsupported("the OLS side fit (want_ols)")
     if want_dsort_nods and dsort is None:
         raise ValueError("want_dsort_nods needs dsort")
-    if not estimate_per_voxel:
-        _unsupported("global ARMA estimation (estimate_per_voxel=False)")
+    if not estimate_per_voxel and _group_designs is not None:
+        _unsupported("global ARMA estimation (estimate_per_voxel=False) of grouped designs")
     if _REML_MODE.afni_faithful:
         _unsupported("the AFNI-faithful banded covariance (set_afni_mode)")
     out_dtype = torch.float64 if use_double else torch.float32
@@ -348,6 +348,17 @@ def fit_glm_arma11(
         factors = None  # built below, unless the CUDA-graph plan builds them inside its graph
         best_all = crit_all = None
 
+    global_crit = None
+    if not estimate_per_voxel and best_all is None:
+        # one (a, b) for every voxel, from the mean series (unscaled), by the
+        # full grid's exhaustive argmin; its criterion is every voxel's
+        # (fastfuncstuff/glm/arma.py:5603-5628)
+        factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt, with_tc=False, sets=sets,
+                                       afull=Dd is not None and bool(column_sets))
+        ym = Y.to(device=device, dtype=torch.float32).mean(0, keepdim=True)
+        so = engine.search(ym, factors, hierarchical=False, projector="simt", do_scale=False)
+        best_all = so.best.expand(V).to(torch.int32).cpu()
+        global_crit = so.best_crit[:1].expand(V)
     P = grid.P
     bs = _batch_size(V, T, P, K, batch_size, device)
     use_graph = (best_all is None and proposal is not None and cuda_graphs and lj is None and bs >= V
@@ -493,6 +504,8 @@ def fit_glm_arma11(
     if precomputed_arma_params is not None:
         res.arma_params = out(_to_tensor(precomputed_arma_params).reshape(-1, 2).to(device))
         res.reml_likelihood = out(torch.zeros(V, device=device))
+    elif global_crit is not None:
+        res.reml_likelihood = out(global_crit)
     else:
         res.reml_likelihood = out(cat("crit"))
     lam = cat("lam")

@@ -728,6 +728,41 @@ def gls_at(Xd, Y, whitener: Whitener, dof: int, task_indices=None, glt=None, wan
     return out
 
 
+def global_arma(X, y, a_grid, b_grid, run_starts=None, tau=None):
+    """((a, b), criterion) of one series over the raw grid, a outer and b
+    inner, the first strict minimum (fastfuncstuff/glm/arma.py:1189-1294 with
+    :1106-1186): pairs with |a| or |b| >= 1 or lambda < 0 are skipped; the
+    criterion is 2 sum log(diag L + 1e-10) + logdet(X_w'X_w + 1e-6 I) + (n - p)
+    log(||y_w - X_w b||^2 + 1e-10), b from the regularised normal equations.
+    FP64."""
+    X = np.asarray(X, F64)
+    y = np.asarray(y, F64)
+    n, p = X.shape
+    best, best_ab = np.inf, (0.5, 0.0)
+    for a in np.asarray(a_grid, F32):
+        for b in np.asarray(b_grid, F32):
+            af, bf = float(a), float(b)
+            if abs(af) >= 1 or abs(bf) >= 1:
+                continue
+            if (bf + af) * (1 + af * bf) / (1 + 2 * af * bf + bf * bf) < 0:
+                continue
+            one = Grid(np.array([a], F32), np.array([b], F32), np.array([a], F32), np.array([b], F32),
+                       np.array([(bf + af) * (1 + af * bf) / (1 + 2 * af * bf + bf * bf)]),
+                       np.zeros(1, np.int64), np.zeros(1, np.int64))
+            whs, logdets = arma11_whiteners(one, n, run_starts, tau, F64)[:2]
+            wh = whs[0]
+            Xw = wh.cols(X)
+            yw = wh.cols(y[:, None])[:, 0]
+            M = Xw.T @ Xw + 1e-6 * np.eye(p)
+            sign, ld = np.linalg.slogdet(M)
+            beta = np.linalg.solve(M, Xw.T @ yw)
+            rss = ((yw - Xw @ beta) ** 2).sum()
+            lik = float(logdets[0]) + (ld if sign > 0 else 1e10) + (n - p) * np.log(rss + 1e-10)
+            if lik < best:
+                best, best_ab = lik, (af, bf)
+    return best_ab, best
+
+
 def dsort_constant_guard(D: np.ndarray) -> np.ndarray:
     """A -dsort series that is constant and nonzero through time is replaced by
     its dataset's mean series over the other voxels (all-zero, run-padded
@@ -838,7 +873,8 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
                    task_indices=None, glt_matrices=None, want_residuals=False,
                    want_ljung_box=False, save_profile_likelihoods=False,
                    precomputed_arma_params=None, fp64_scaled=False, afni_faithful=False,
-                   autocorr=None, subset_descent=False, column_sets=None, dsort=None, dsort_run_bounds=None):
+                   autocorr=None, subset_descent=False, column_sets=None, dsort=None, dsort_run_bounds=None,
+                   estimate_per_voxel=True):
     """The reference's ``fit_glm_arma11`` for the options this path covers.
 
     Follows fastfuncstuff/glm/arma.py:3650-5878 on ``device=cpu``:
@@ -885,6 +921,10 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
     if b_grid is None:
         b_grid = np.linspace(-0.8, 0.8, 17).astype(F32)
     grid = valid_grid(a_grid, b_grid, dt)
+    global_lik = None
+    if not estimate_per_voxel and precomputed_arma_params is None:
+        (a_opt, b_opt), global_lik = global_arma(X, Y.mean(0), a_grid, b_grid, run_starts, tau)
+        precomputed_arma_params = np.tile(np.array([[a_opt, b_opt]], F32), (V, 1))
     if precomputed_arma_params is not None:
         pa = np.asarray(precomputed_arma_params, dtype=F32).reshape(V, 2)
         pairs, inv = np.unique(pa, axis=0, return_inverse=True)
@@ -912,6 +952,8 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
         res.arma_params = np.stack([grid.a[idx], grid.b[idx]], 1).astype(dt)
         pairs, inv = np.unique(res.arma_params.astype(F32), axis=0, return_inverse=True)
         inv = inv.reshape(-1)
+    if global_lik is not None:
+        res.reml_likelihood = np.full(V, global_lik, dt)
     lam = arma_lambda_output_f32(res.arma_params[:, 0], res.arma_params[:, 1]).astype(dt)
     if use_double:
         a64 = res.arma_params[:, 0].astype(F64)

@@ -22,6 +22,8 @@ Cases (all on ``device=cpu``):
 * ``grid``     logdet(R), logdet(X_w'X_w), X_w and Q of a small precompute
 * ``sets``     column_sets (Wald F, temporal SD and coefficient of each set),
                two runs, one set naming a column outside the design
+* ``global``   estimate_per_voxel=False: one (a, b) from the mean series, then
+               the GLS of every voxel at it
 * ``dsort``    voxelwise regressors (-dsort): two datasets per voxel, and one
                dataset expanded per run (dsort_run_bounds), with task columns,
                a GLT, Ljung-Box, residuals and column sets over [X | D]
@@ -145,6 +147,20 @@ def main(ref_root: str, only: str | None = None) -> None:
             if r.ljung_box_dof is not None:
                 out[f"{name}__ljung_box_dof"] = np.array(r.ljung_box_dof)
         return out
+
+    # global ARMA: (a, b) estimated once from the mean series
+    X, Y, _ = _case(22, [60, 60], p_task=2, V=150)
+    out = {}
+    for name, extra in {"f64": dict(use_double=True), "f32": dict()}.items():
+        r = fit_glm_arma11(torch.from_numpy(Y), torch.from_numpy(X), tr=2.0, device=cpu, verbose=False,
+                           a_grid=g17, b_grid=g17, run_starts=[0, 60], estimate_per_voxel=False, **extra)
+        for attr in ("betas", "tstats", "arma_params", "reml_likelihood", "sigma2", "fstats", "r2", "arma_lambda"):
+            out[f"{name}__{attr}"] = getattr(r, attr).numpy()
+    np.savez_compressed(OUT / "global.npz", X=X, Y=Y, a_grid=g17.numpy(), b_grid=g17.numpy(),
+                        run_starts=np.array([0, 60]), **out)
+    if only == "global":
+        print("wrote", OUT / "global.npz")
+        return
 
     # -dsort: per-voxel regressors (one smooth series correlated with the data,
     # one independent; three voxels with a constant series that the guard

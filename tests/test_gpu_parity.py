@@ -537,3 +537,22 @@ def test_autotuner_picks_a_tile_and_results_do_not_depend_on_it():
         engine.autotune_projection = orig
         _lib.check(lib.ffs_reml_tune_tc_pairs(K, tuned["pairs"]), "tune")
     assert torch.equal(surfs[0], surfs[1]) and torch.equal(surfs[0], surfs[2])
+
+
+def test_global_arma_matches_oracle_and_reference():
+    """estimate_per_voxel=False: one (a, b) from the unscaled mean series (the
+    full grid's exhaustive argmin on the device), its criterion for every
+    voxel, then the GLS of every voxel at that pair; against the reference's
+    own outputs and the FP64 oracle."""
+    d = load_golden("global")
+    kw = dict(a_grid=d["a_grid"], b_grid=d["b_grid"], run_starts=d["run_starts"], estimate_per_voxel=False)
+    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, **kw)
+    np.testing.assert_array_equal(got.arma_params.numpy(), d["f32__arma_params"])
+    np.testing.assert_allclose(got.reml_likelihood.numpy(), d["f32__reml_likelihood"], rtol=1e-5)
+    ref = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, fp64_scaled=True, **kw)
+    np.testing.assert_array_equal(got.arma_params.numpy(), ref.arma_params.astype(np.float32))
+    assert rel_maxnorm(got.betas.numpy(), ref.betas).max() <= BETA_REL
+    assert rel_maxnorm(got.tstats.numpy(), ref.tstats).max() <= BETA_REL
+    np.testing.assert_allclose(got.sigma2.numpy(), ref.sigma2, rtol=1e-4)
+    np.testing.assert_allclose(got.r2.numpy(), ref.r2, atol=2e-5)
+    assert rel_maxnorm(got.betas.numpy(), d["f32__betas"]).max() <= 2e-3

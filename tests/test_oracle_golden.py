@@ -301,3 +301,20 @@ def test_dsort_matches_reference(tag):
         assert same.mean() >= 0.97, (mode, same.mean())
         for name in ("betas", "dsort_betas", "sigma2"):
             _close(getattr(r, name)[same], d[f"{tag}_{mode}__{name}"][same], rtol=2e-3, atol=2e-3)
+
+
+def test_global_arma_matches_reference():
+    """estimate_per_voxel=False (fastfuncstuff/glm/arma.py:5603-5778): (a, b)
+    from the mean series over the raw grid with the regularised scalar
+    criterion (:1106-1294), its criterion for every voxel, then the GLS of
+    every voxel at that pair."""
+    d = load_golden("global")
+    kw = dict(a_grid=d["a_grid"], b_grid=d["b_grid"], run_starts=d["run_starts"], estimate_per_voxel=False)
+    r = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, **kw)
+    np.testing.assert_array_equal(r.arma_params, d["f64__arma_params"])
+    _close(r.reml_likelihood, d["f64__reml_likelihood"], rtol=1e-6)  # the reference forms R in float32
+    for name in ("betas", "tstats", "sigma2", "fstats", "r2"):
+        _close(getattr(r, name), d["f64__" + name], rtol=2e-5, atol=1e-6)
+    r = o.fit_glm_arma11(d["Y"], d["X"], use_double=False, **kw)
+    np.testing.assert_array_equal(r.arma_params, d["f32__arma_params"])
+    _close(r.betas, d["f32__betas"], rtol=2e-3, atol=2e-3)
