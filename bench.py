@@ -128,21 +128,46 @@ def dist_init():
     return None, 0, 1, 0
 
 
-def cpu_baseline(w, n_voxels: int) -> dict:
-    """The reference's default CPU fit (torch CPU port) on a bounded voxel sample."""
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            if ln.lower().startswith(("model name", "cpu model")):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def cpu_baseline(w, n_voxels: int, n_exhaustive: int) -> dict:
+    """The reference's CPU fit (torch CPU port) on bounded voxel samples: the
+    default hierarchical selector (``value``) and force_exhaustive_search."""
     from oracle import cpu_port
 
     cores = len(os.sched_getaffinity(0))
     torch.set_num_threads(cores)
     g = torch.linspace(-0.8, 0.8, GRID).numpy()
-    sub = w.Y[:n_voxels]
-    cpu_port.fit(sub[:64], w.X, g, g, w.run_starts)  # warm the kernels
+    cpu_port.fit(w.Y[:64], w.X, g, g, w.run_starts)  # warm the kernels
     t0 = time.perf_counter()
-    cpu_port.fit(sub, w.X, g, g, w.run_starts)
+    cpu_port.fit(w.Y[:n_voxels], w.X, g, g, w.run_starts)
     dt = time.perf_counter() - t0
-    return {"value": n_voxels / dt, "unit": "voxels/s", "cores": cores, "kind": "port",
-            "sample": f"{n_voxels} voxels of the same workload, float32, default hierarchical selector, "
-                      f"{dt:.1f} s"}
+    out = {"value": n_voxels / dt, "unit": "voxels/s", "cores": cores, "cpu": cpu_model(), "kind": "port",
+           "sample": f"{n_voxels} voxels of the same workload, float32, default hierarchical selector, "
+                     f"{dt:.1f} s on {cores} threads"}
+    if n_exhaustive > 0:
+        t0 = time.perf_counter()
+        cpu_port.fit(w.Y[:n_exhaustive], w.X, g, g, w.run_starts, exhaustive=True)
+        de = time.perf_counter() - t0
+        out["exhaustive"] = {"value": n_exhaustive / de, "unit": "voxels/s",
+                             "sample": f"{n_exhaustive} voxels, float32, force_exhaustive_search, {de:.1f} s"}
+    return out
 
 
 def run_reference(args) -> None:
@@ -170,7 +195,7 @@ def run_reference(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded workload)",
         "config": workload_config(args.voxels or 200_000),
         "method": "the reference's default CPU fit (full grid, hierarchical selector)",
-        "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": cores, "cpu": cpu_model(), "kind": "port",
                          "sample": f"{n} voxels per step of the same workload on {cores} host threads"},
         "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -187,29 +212,38 @@ NCU_DRAM_BYTES_PER_VOXEL = {
 }
 
 
-def roofline(dom: str, mean_ms: float, V: int, T: int, K: int, P: int, pk: dict, sm_mhz, extra: dict) -> dict:
-    """Algorithmic work of the dominant kernel per launch against its bound."""
-    r = _roofline(dom, mean_ms, V, T, K, P, pk, sm_mhz, extra)
+def roofline(dom: str, ms_step: float, launches: float, T: int, K: int, P: int, pk: dict, sm_mhz,
+             work: dict) -> dict:
+    """The dominant kernel against its bound: the algorithmic work of ALL its
+    launches in one step (``work``: "voxels" it processed, "pair_evals" for the
+    window kernels, "designs" for the grid build) over their summed device time
+    ``ms_step`` (per-call CUDA events of an eager pass), i.e. the launches'
+    average rate; ``launches`` is how many there were per step."""
+    r = _roofline(dom, ms_step, T, K, P, pk, sm_mhz, work)
+    r["ms_per_step"] = ms_step
+    r["launches_per_step"] = launches
     per_voxel = NCU_DRAM_BYTES_PER_VOXEL.get((T, K, dom)) if P == 561 else None
     if per_voxel is not None:
-        r["traffic"] = per_voxel * V
-        r["traffic_unit"] = "bytes per launch (ncu DRAM read + write, scaled from a 100k-217k voxel capture)"
+        r["traffic"] = per_voxel * work["voxels"] / max(launches, 1)
+        r["traffic_unit"] = ("bytes per launch: ncu DRAM read + write per voxel (from a 100k-217k voxel capture) x "
+                             "the voxels of the step's launches / launches")
     return r
 
 
-def _roofline(dom: str, mean_ms: float, V: int, T: int, K: int, P: int, pk: dict, sm_mhz, extra: dict) -> dict:
-    sec = mean_ms / 1e3
+def _roofline(dom: str, ms_step: float, T: int, K: int, P: int, pk: dict, sm_mhz, work: dict) -> dict:
+    sec = ms_step / 1e3
+    V = work["voxels"]
     fp32_peak = 152 * 128 * 2 * (sm_mhz or 1900.0) * 1e6 / 1e12
     if dom in ("ffs_reml_project_tc", "ffs_reml_project_tc_list"):
         k_eff = (T + 15) // 16 * 16
-        cols = extra.get("pair_evals", V * P) if dom == "ffs_reml_project_tc_list" else V * P
+        cols = work.get("pair_evals", V * P) if dom == "ffs_reml_project_tc_list" else V * P
         flops = 3 * 2.0 * cols * K * k_eff
         ach = flops / sec / 1e12
         return {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": ach / pk["bf16_tflops"], "traffic": None, "peak_src": pk["src"] + " (bf16 burst)",
                 "work": "3 fp16 products x 2 x (voxel, pair) x K x T (k rounded to 16)"}
     if dom in ("ffs_reml_surface", "ffs_reml_window"):
-        n = extra.get("pair_evals", V * P) if dom == "ffs_reml_window" else V * P
+        n = work.get("pair_evals", V * P) if dom == "ffs_reml_window" else V * P
         flops = 4.0 * n * T  # v_t = z_t - m_t v_t-1 and s += v_t^2 / D_t: 2 FMA
         ach = flops / sec / 1e12
         return {"kernel": dom, "bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
@@ -223,7 +257,7 @@ def _roofline(dom: str, mean_ms: float, V: int, T: int, K: int, P: int, pk: dict
                 "work": "G'y, X b0 and G'r (3 K x T products) and the whitening recurrence per voxel"}
     if dom in ("ffs_grid_build", "ffs_grid_build_designs"):
         # FP64: the whitened design (2 T K) and its Gram matrix (T K (K + 1)) per (design, pair)
-        items = P * extra.get("designs", 1)
+        items = P * work.get("designs", 1)
         flops = items * (2.0 * T * K * (K + 1) + 4.0 * T * K)
         ach = flops / sec / 1e12
         return {"kernel": dom, "bound": "fp64", "achieved": ach, "peak": 1.25, "unit": "TFLOP/s",
@@ -236,6 +270,76 @@ def _roofline(dom: str, mean_ms: float, V: int, T: int, K: int, P: int, pk: dict
     return {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_src": pk["src"],
             "work": "bytes: Y read, residualised rows and fp16 hi/lo written"}
+
+
+def learned_quality(args, w, Yd, Xd, kw, kw_l, prop, lay, g, tinfo) -> tuple[dict, float, int]:
+    """Correctness of the learned-seeded fit on this workload.
+
+    * against the GPU full grid (exhaustive argmin) on every voxel: agreement,
+      and for the voxels that disagree the criterion gap
+      (crit_learned - crit_full) / |crit_full|;
+    * against the FP64 oracle (exhaustive, the float32 mode's scaling in
+      float64) on a fixed sample (every (V // fp64_voxels)-th voxel):
+      agreement with its argmin, the gap of the disagreeing voxels on the FP64
+      surface, and the betas' and t's relative error (per voxel, max-norm).
+    Returns (quality, window (voxel, pair) evaluations, fallback voxels)."""
+    from fastfuncstuff_gb300 import fit_glm_arma11
+    from fastfuncstuff_gb300.glm import engine, learned
+    from fastfuncstuff_gb300.glm import grid as G
+
+    V = Yd.shape[0]
+    exh = fit_glm_arma11(Yd, Xd, return_device=True, **dict(kw, force_exhaustive_search=True))
+    lr = fit_glm_arma11(Yd, Xd, return_device=True, **kw_l)
+    same = (lr.arma_params == exh.arma_params).all(1)
+    c_l = lr.reml_likelihood.double()
+    c_f = exh.reml_likelihood.double()
+    gap = ((c_l - c_f) / c_f.abs().clamp(min=1.0))[~same]
+    f_all = engine.build_factors(Xd, G.make_grid(g, g), lay)
+    ls = learned.learned_search(Yd, f_all, prop, lay, recenter=args.recenter)
+    pair_evals = float(ls.stats["pair_evals"].item()) if torch.is_tensor(ls.stats["pair_evals"]) else 0.0
+    n_fb = int(round(ls.stats["fallback"] * V))
+    q = {
+        "agreement_with_full_grid": float(same.float().mean().item()),
+        "disagreeing_voxels": int((~same).sum().item()),
+        "crit_gap_max_of_disagreeing": float(gap.max().item()) if gap.numel() else 0.0,
+        "disagreeing_with_gap_gt_1e-6": int((gap > 1e-6).sum().item()),
+        "first_window_on_edge": float(ls.stats["edge_first"]), "full_grid_fallback": ls.stats["fallback"],
+        "recenter_rounds": args.recenter, "window_pair_evals_per_voxel": pair_evals / V,
+    }
+    if args.fp64_voxels > 0:
+        from oracle import reml as o
+
+        step = max(1, V // args.fp64_voxels)
+        sub = np.arange(0, V, step)[: args.fp64_voxels]
+        t0 = time.perf_counter()
+        ref = o.fit_glm_arma11(w.Y[sub], w.X, a_grid=g.numpy(), b_grid=g.numpy(), run_starts=w.run_starts,
+                               use_double=True, fp64_scaled=True, force_exhaustive_search=True,
+                               save_profile_likelihoods=True)
+        grid = G.make_grid(g, g)
+        pa = lr.arma_params[sub].cpu().numpy().astype(np.float32)
+        idx_l = grid.index_of(pa[:, 0], pa[:, 1])
+        agree = idx_l == ref.arma_index
+        v = np.nonzero(~agree)[0]
+        surf = ref.reml_lklhd_surface
+        g64 = (surf[v, idx_l[v]] - surf[v, ref.arma_index[v]]) / np.maximum(np.abs(surf[v, ref.arma_index[v]]), 1.0)
+
+        def rel(got, want):
+            num = np.abs(got.astype(np.float64) - want).max(-1)
+            return num / np.maximum(np.abs(want).max(-1), 1e-12)
+
+        rb = rel(lr.betas[sub].cpu().numpy(), ref.betas)
+        rt = rel(lr.tstats[sub].cpu().numpy(), ref.tstats)
+        q["vs_fp64"] = {
+            "sample": f"{sub.size} voxels (every {step}th), FP64 oracle exhaustive search and GLS "
+                      f"({time.perf_counter() - t0:.1f} s on the host)",
+            "agreement": float(agree.mean()), "disagreeing_voxels": int(v.size),
+            "crit_gap_max_of_disagreeing": float(g64.max()) if v.size else 0.0,
+            "beta_rel_err_max": float(rb[agree].max()), "tstat_rel_err_max": float(rt[agree].max()),
+            "beta_rel_err_le_1e-4": float((rb <= 1e-4).mean()),
+            "beta_rel_err_max_all_voxels": float(rb.max()),
+        }
+    q.update({k: round(v, 3) if isinstance(v, float) else v for k, v in tinfo.items()})
+    return q, pair_evals, n_fb
 
 
 def run_gb300(args) -> None:
@@ -252,7 +356,7 @@ def run_gb300(args) -> None:
     g = torch.linspace(-0.8, 0.8, GRID)
     Yd = torch.from_numpy(w.Y).to(dev)
     kw = dict(tr=2.0, a_grid=g, b_grid=g, run_starts=w.run_starts, device=dev, verbose=False,
-              force_exhaustive_search=args.selector == "exhaustive", projector=args.projector)
+              force_exhaustive_search=args.selector == "exhaustive")
     grouped = w.designs is not None
     if grouped:  # one design per HRF group: the grouped API, full grid
         from fastfuncstuff_gb300 import fit_glm_arma11_grouped
@@ -323,9 +427,17 @@ def run_gb300(args) -> None:
     value_f = ws * V / (ms_f / 1e3)
     pk = peaks()
     P = 561
-    dom_f = max(st_f.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])[0]
-    roof_f = roofline(dom_f, st_f[dom_f]["mean_ms"], V, T, K, P, pk, clk_f["sm_mhz"],
-                      {"designs": len(w.designs)} if grouped else {})
+
+    def dominant(st, voxels_of):
+        """(name, roofline) of the entry point with the most device time per step."""
+        name, d = max(st.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])
+        work = {"voxels": voxels_of(name)}
+        return name, d["mean_ms"] * d["calls"] / args.steps, d["calls"] / args.steps, work
+
+    dom_f, ms_df, n_df, work_f = dominant(st_f, lambda n: V)
+    if grouped:
+        work_f["designs"] = len(w.designs)
+    roof_f = roofline(dom_f, ms_df, n_df, T, K, P, pk, clk_f["sm_mhz"], work_f)
     if grouped:
         ms_l, st_l, l_l, clk_l, value, roof, quality = ms_f, st_f, l_f, clk_f, value_f, roof_f, None
         st_e, ms_e = st_f, ms_f
@@ -335,27 +447,12 @@ def run_gb300(args) -> None:
         # the learned step is replayed from CUDA graphs, which the per-call
         # timer does not see into: its stage breakdown comes from an eager pass
         ms_e, st_e, l_e, _ = timed(dict(kw_l, cuda_graphs=False), "learned_eager")
-
-        # quality of the learned step against the full grid (exhaustive argmin)
-        exh = fit_glm_arma11(Yd, Xd, return_device=True, **dict(kw, force_exhaustive_search=True))
-        lr = fit_glm_arma11(Yd, Xd, return_device=True, **kw_l)
-        same = (lr.arma_params == exh.arma_params).all(1)
-        num = (lr.betas.double() - exh.betas.double()).abs().amax(1)
-        den = exh.betas.double().abs().amax(1).clamp(min=1e-12)
-        rel = num / den
-        f_all = engine.build_factors(Xd, G.make_grid(g, g), lay)
-        ls = learned.learned_search(Yd, f_all, prop, lay, recenter=args.recenter)
-        pair_evals = float(ls.stats["pair_evals"].item()) if torch.is_tensor(ls.stats["pair_evals"]) else 0.0
-        quality = {
-            "agreement_with_full_grid": float(same.float().mean().item()),
-            "beta_rel_err_le_1e-4": float((rel <= 1e-4).float().mean().item()),
-            "beta_rel_err_max_where_pair_agrees": float(rel[same].max().item()) if bool(same.any()) else None,
-            "first_window_on_edge": float(ls.stats["edge_first"]), "full_grid_fallback": ls.stats["fallback"],
-            "recenter_rounds": args.recenter, "window_pair_evals_per_voxel": pair_evals / V,
-        }
-        quality.update({k: round(v, 3) if isinstance(v, float) else v for k, v in tinfo.items()})
-        dom = max(st_e.items(), key=lambda kv: kv[1]["mean_ms"] * kv[1]["calls"])[0]
-        roof = roofline(dom, st_e[dom]["mean_ms"], V, T, K, P, pk, clk_l["sm_mhz"], {"pair_evals": pair_evals})
+        quality, pair_evals, n_fb = learned_quality(args, w, Yd, Xd, kw, kw_l, prop, lay, g, tinfo)
+        # the eager step's GLS launches cover every voxel and, again, the
+        # fallback voxels; its window kernels cover pair_evals (voxel, pair)s
+        dom, ms_d, n_d, work = dominant(st_e, lambda n: V + n_fb if n == "ffs_reml_gls_grouped" else V)
+        work["pair_evals"] = pair_evals
+        roof = roofline(dom, ms_d, n_d, T, K, P, pk, clk_l["sm_mhz"], work)
 
     method = ("full grid, one design per HRF group (fit_glm_arma11_grouped)" if grouped else
               f"learned-seeded 5x5 window refine ({args.recenter} re-centred round), full grid on window edges, "
@@ -424,7 +521,7 @@ def run_gb300(args) -> None:
         line["e2e"] = e2e["full_grid" if grouped else "learned"]
         line["full_grid"]["e2e"] = e2e["full_grid"]
     if rank == 0 and not args.no_cpu_baseline and not grouped and cid == 1:
-        line["cpu_baseline"] = cpu_baseline(w, args.cpu_voxels)
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_voxels, args.cpu_exhaustive_voxels)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -442,10 +539,14 @@ def main() -> None:
     ap.add_argument("--workload", type=int, default=1, choices=[1, 2, 3, 4],
                     help="1: N=400 p=20 V=200k (default); 2: grouped designs, censored; 3: p=130; 4: V=500k")
     ap.add_argument("--selector", default="hierarchical", choices=["hierarchical", "exhaustive"])
-    ap.add_argument("--projector", default="tc", choices=["tc", "simt"])
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-voxels", type=int, default=4000)
-    ap.add_argument("--ref-voxels", type=int, default=4000)
+    ap.add_argument("--cpu-voxels", type=int, default=20_000,
+                    help="CPU baseline sample, default selector (the 561-pair precompute amortised as in a full fit)")
+    ap.add_argument("--cpu-exhaustive-voxels", type=int, default=5_000,
+                    help="CPU baseline sample of the exhaustive selector")
+    ap.add_argument("--ref-voxels", type=int, default=20_000)
+    ap.add_argument("--fp64-voxels", type=int, default=2000,
+                    help="voxels of the learned fit checked against the FP64 oracle (0: skip)")
     ap.add_argument("--recenter", type=int, default=1)
     ap.add_argument("--train-voxels", type=int, default=2_000_000)
     ap.add_argument("--train-epochs", type=int, default=30)

@@ -15,6 +15,7 @@ from .glm.arma import (  # noqa: F401
     fit_glm_arma11_grouped,
     fit_glm_arma11_perhrf,
     get_default_arma_grids,
+    parse_grid_arg,
     precompute_reml_grid,
     search_voxels_precomputed_grid,
     set_afni_mode,

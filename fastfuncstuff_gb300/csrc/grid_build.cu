@@ -907,6 +907,8 @@ static __device__ __align__(256) double g_grid_scratch[kStaticGridScratchBytes /
 
 // Device address of g_grid_scratch, resolved once per device with that device
 // current (host code may only pass this address to kernels, never the symbol).
+// The cache lives as long as the process; a cudaDeviceReset would leave it
+// stale (documented in the header).
 double* static_grid_scratch(int* status) {
   static std::mutex mu;
   static double* addr[256] = {nullptr};

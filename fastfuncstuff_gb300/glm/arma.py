@@ -47,6 +47,7 @@ from .grid import (
     grid_of_pairs,
     ljung_box_plan,
     make_grid,
+    parse_grid_arg,
     run_bounds,
     run_layout,
     set_afni_mode,
@@ -63,6 +64,7 @@ __all__ = [
     "fit_glm_arma11_grouped",
     "fit_glm_arma11_perhrf",
     "get_default_arma_grids",
+    "parse_grid_arg",
     "precompute_reml_grid",
     "run_bounds",
     "search_voxels_precomputed_grid",
@@ -143,8 +145,7 @@ def _unsupported(name: str) -> None:
 
 
 def precompute_reml_grid(X, n_timepoints: int, a_grid, b_grid, device=None, *, run_starts=None, tau=None,
-                         use_double: bool = False, task_indices=None, glt_matrices=None,
-                         tensor_cores: bool = True) -> engine.GridFactors:
+                         use_double: bool = False, task_indices=None, glt_matrices=None) -> engine.GridFactors:
     """The per-pair factors of a design (replaces fastfuncstuff/glm/arma.py:1371-1531).
 
     Returns the device-resident ``GridFactors`` (logdets, the recurrence
@@ -159,12 +160,12 @@ def precompute_reml_grid(X, n_timepoints: int, a_grid, b_grid, device=None, *, r
     glt = None
     if glt_matrices is not None:
         glt = np.stack([np.asarray(g, np.float32).reshape(-1) for g in glt_matrices])
-    return engine.build_factors(X, grid, layout, task_indices=task_indices, glt=glt, with_tc=tensor_cores)
+    return engine.build_factors(X, grid, layout, task_indices=task_indices, glt=glt,
+                                with_tc=X.shape[1] <= TC_MAX_K)
 
 
 def search_voxels_precomputed_grid(X, Y_batch, factors: engine.GridFactors, device=None, *,
-                                   hierarchical: bool = False, return_profile: bool = False,
-                                   projector: str = "tc"):
+                                   hierarchical: bool = False, return_profile: bool = False):
     """Search seam of fastfuncstuff/glm/arma.py:1886-2018 on the GPU.
 
     Returns ``(best_params (V, 2), best_likelihoods (V,))`` and, with
@@ -173,7 +174,8 @@ def search_voxels_precomputed_grid(X, Y_batch, factors: engine.GridFactors, devi
     """
     device = engine.require_cuda(device)
     Y = _to_tensor(Y_batch).to(device)
-    out = engine.search(Y, factors, hierarchical=hierarchical, projector=projector, keep_surface=return_profile)
+    out = engine.search(Y, factors, hierarchical=hierarchical, projector=_projector(factors),
+                        keep_surface=return_profile)
     g = factors.grid
     best = out.best.long()
     params = torch.stack([torch.from_numpy(g.a).to(device)[best], torch.from_numpy(g.b).to(device)[best]], 1)
@@ -181,6 +183,17 @@ def search_voxels_precomputed_grid(X, Y_batch, factors: engine.GridFactors, devi
         surface = (out.surf.double() + out.crit0[None, :]).float().t().contiguous()
         return params, out.best_crit, surface, g.param_list()
     return params, out.best_crit
+
+
+# Widest design the tcgen05 projection takes (one 256-column MMA tile holds a
+# pair's K columns); wider designs are projected on the CUDA cores.
+TC_MAX_K = 256
+
+
+def _projector(factors: engine.GridFactors) -> str:
+    """The projection kernel of the factors: tcgen05 when they carry its fp16
+    operands (K <= TC_MAX_K), else the CUDA-core kernel."""
+    return "tc" if factors.U_hi is not None else "simt"
 
 
 _SIDE: dict = {}
@@ -245,7 +258,6 @@ def fit_glm_arma11(
     tau=None,
     column_sets=None,
     *,
-    projector: str = "tc",
     return_device: bool = False,
     proposal=None,
     proposal_recenter: int = 0,
@@ -259,8 +271,7 @@ def fit_glm_arma11(
     ``autocorr_cache`` tune the reference's CPU/GPU memory plan and have no
     counterpart here (the factors are built on the GPU in FP64, with the QR
     fallback applied per pair when the Cholesky of X_w'X_w fails). Extra
-    keywords: ``projector`` ("tc" tensor-core GEMM, "simt" CUDA cores),
-    ``return_device`` (keep result tensors on the GPU), ``proposal`` (a trained
+    keywords: ``return_device`` (keep result tensors on the GPU), ``proposal`` (a trained
     ``learned.ArmaProposal``: search each voxel's 5 x 5 window around its
     proposal, the full grid for window-edge voxels) and ``proposal_recenter``
     (re-centred window rounds before that fallback), ``cuda_graphs`` (replay
@@ -353,10 +364,10 @@ def fit_glm_arma11(
         # one (a, b) for every voxel, from the mean series (unscaled), by the
         # full grid's exhaustive argmin; its criterion is every voxel's
         # (fastfuncstuff/glm/arma.py:5603-5628)
-        factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt, with_tc=False, sets=sets,
-                                       afull=Dd is not None and bool(column_sets))
+        factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt, with_tc=K <= TC_MAX_K,
+                                       sets=sets, afull=Dd is not None and bool(column_sets))
         ym = Y.to(device=device, dtype=torch.float32).mean(0, keepdim=True)
-        so = engine.search(ym, factors, hierarchical=False, projector="simt", do_scale=False)
+        so = engine.search(ym, factors, hierarchical=False, projector=_projector(factors), do_scale=False)
         best_all = so.best.expand(V).to(torch.int32).cpu()
         global_crit = so.best_crit[:1].expand(V)
     P = grid.P
@@ -388,7 +399,7 @@ def fit_glm_arma11(
             q0, cflag, ccoef = engine.design_basis(Xd, with_constant=True)
             center = (cflag, ccoef)
         factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt,
-                                       with_tc=projector == "tc" and K <= 256, stream=side, sets=sets,
+                                       with_tc=K <= TC_MAX_K, stream=side, sets=sets,
                                        afull=afull, center=center)
         if overlap:
             built = torch.cuda.Event()
@@ -402,7 +413,7 @@ def fit_glm_arma11(
                               "cb", "ct", "resid", "resid_w", "pred", "lb", "scale")}
     factors_used = factors
     dchunks = []
-    proj = projector if (projector != "tc" or factors is None or factors.U_hi is not None) else "simt"
+    proj = "tc" if factors is None else _projector(factors)
     if proposal is not None and best_all is None:
         from . import learned
 
@@ -416,8 +427,7 @@ def fit_glm_arma11(
             plan = learned.graph_for(Yb, Xd, grid, layout_l, proposal, recenter=proposal_recenter,
                                      do_scale=not use_double,
                                      gls_kw=dict(want_residuals=want_residuals, want_predicted=want_predicted),
-                                     factor_kw=dict(task_indices=ti, glt=glt,
-                                                    with_tc=projector == "tc" and K <= 256, sets=sets))
+                                     factor_kw=dict(task_indices=ti, glt=glt, with_tc=K <= TC_MAX_K, sets=sets))
             lo, go = plan.run(Yb, Xd)
             factors_used = plan.f
             best, scale = lo.best, lo.scale
@@ -693,8 +703,8 @@ def fit_glm_arma11_grouped(data, designs_by_group: dict, group_indices, tr: floa
     fit_kwargs.setdefault("verbose", False)
     batched_ok = (pre is None and fit_kwargs.get("proposal") is None
                   and not fit_kwargs.get("save_profile_likelihoods", False)
-                  and fit_kwargs.get("projector", "tc") == "tc" and fit_kwargs.get("batch_size") is None
-                  and shape0[1] <= 256 and len(groups) > 1)
+                  and fit_kwargs.get("batch_size") is None and fit_kwargs.get("estimate_per_voxel", True)
+                  and shape0[1] <= TC_MAX_K and len(groups) > 1)
     if batched_ok:
         # one fit over all groups: the designs stacked (D, T, K), each voxel
         # tagged with its design's index

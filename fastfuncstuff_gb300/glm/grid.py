@@ -47,6 +47,45 @@ def get_default_arma_grids(device=None) -> tuple[torch.Tensor, torch.Tensor]:
             torch.linspace(*DEFAULT_ARMA_B_GRID, device=device))
 
 
+def parse_grid_arg(grid_str: str) -> torch.Tensor:
+    """A -a_grid / -b_grid argument as a 1-D float32 tensor, read as
+    fastfuncstuff/cli/reml.py:115-160 reads it:
+
+    * ``start:stop:num``  linspace (num >= 2), e.g. ``-0.9:0.9:65``;
+    * ``start,stop,num``  linspace, when there are exactly three values and the
+      last is a whole number >= 2 (the legacy form);
+    * ``v1,v2,...``       the values themselves.
+
+    A malformed argument prints ``ERROR: ...`` and exits with status 1, as the
+    reference's command line does.
+    """
+    import sys
+
+    def fail(msg: str):
+        print(f"ERROR: {msg}")
+        sys.exit(1)
+
+    s = grid_str.strip()
+    if ":" in s:
+        parts = s.split(":")
+        if len(parts) != 3:
+            fail(f"colon range must be start:stop:num, got '{s}'")
+        try:
+            start, stop, num = float(parts[0]), float(parts[1]), int(parts[2])
+        except ValueError:
+            fail(f"could not parse the range '{s}'")
+        if num < 2:
+            fail(f"num_points must be >= 2 in '{s}'")
+        return torch.linspace(start, stop, num)
+    try:
+        values = [float(p) for p in s.split(",")]
+    except ValueError:
+        fail(f"could not parse grid values '{s}'")
+    if len(values) == 3 and values[2].is_integer() and values[2] >= 2:
+        return torch.linspace(values[0], values[1], int(values[2]))
+    return torch.tensor(values, dtype=torch.float32)
+
+
 def _as_f32_cpu(g) -> torch.Tensor:
     if isinstance(g, torch.Tensor):
         return g.detach().to(device="cpu", dtype=torch.float32).reshape(-1)

@@ -149,7 +149,10 @@ int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int max_ctas, 
  * - Sizes whose ffs_grid_work_bytes(T, K, P) exceeds the limit are rejected
  *   with FFS_ERR_WORKSPACE and a message.
  * - The first call on a device resolves the array's device address (with that
- *   device current); make that first call before any stream capture.
+ *   device current); make that first call before any stream capture. The
+ *   address is cached per device for the life of the process: after a
+ *   cudaDeviceReset the cached address is stale, so a process that resets a
+ *   device must not call this entry point on that device again.
  * - All calls share the one array: calls whose kernels overlap on the GPU
  *   (different streams, or different host threads on one device) race and
  *   must be serialised by the caller. Nothing in the array needs clearing

@@ -12,11 +12,13 @@ host cores is the reference's cost:
      X_w'X_w, Q and the logdets (arma.py:1459-1506);
   3. the hierarchical descent with one subset GEMM per visited pair
      (arma.py:2021-2221), or the exhaustive loop (arma.py:1973-2010);
-  4. the GLS refit per chosen pair with float64 sigma2 accumulation
-     (arma.py:4829-5560).
+  4. the GLS refit per chosen pair: betas, float64 sigma2 accumulation, t,
+     F, R^2 and lambda, unscaled (arma.py:4829-5560, :5827-5862).
 
-It is test infrastructure: the product path never imports it, and
-``tests/test_oracle_golden.py`` checks its selections against the NumPy oracle.
+It is test infrastructure: the product path never imports it.
+``tests/test_cpu_port.py`` pins its selections and GLS outputs to the
+reference's own float32 outputs on the golden fixtures, in both selector
+modes.
 """
 
 from __future__ import annotations
@@ -82,15 +84,19 @@ def _whiten_rows(Y, Linv_p, lens):
     return out
 
 
-def fit(data, design, a_grid, b_grid, run_starts=None, exhaustive=False, threads=None):
-    """The default float32 CPU fit; returns (pair index (V,), betas (V, K))."""
+def fit(data, design, a_grid, b_grid, run_starts=None, exhaustive=False, threads=None, task_indices=None):
+    """The default float32 CPU fit (``exhaustive`` for the reference's
+    force_exhaustive_search). Returns a dict of per-voxel outputs as the
+    reference's ``ARMA11Results`` holds them: ``index`` (pair index),
+    ``arma_params``, ``betas``, ``tstats``, ``sigma2``, ``fstats``, ``r2``,
+    ``arma_lambda`` and ``reml_likelihood``."""
     if threads:
         torch.set_num_threads(int(threads))
     Y = torch.as_tensor(np.asarray(data), dtype=torch.float32)
     X = torch.as_tensor(np.asarray(design), dtype=torch.float32)
     V, T = Y.shape
     K = X.shape[1]
-    starts = sorted(set([0] + list(run_starts or [])))
+    starts = sorted(set([0] + [int(s) for s in np.asarray(run_starts if run_starts is not None else []).reshape(-1)]))
     lens = [e - s for s, e in zip(starts, starts[1:] + [T])]
     scale = Y.std(dim=1).clamp(min=1e-8)
     Ys = Y / scale[:, None]
@@ -157,8 +163,15 @@ def fit(data, design, a_grid, b_grid, run_starts=None, exhaustive=False, threads
                     win = inb & (i >= lo_a) & (i <= hi_a)
                     ev(i, j, torch.nonzero(win).flatten())
     idx = table[ba, bb]
-    # GLS per chosen pair
+    # GLS per chosen pair (arma.py:4853-4905, :5227-5363): betas, float64
+    # sigma2, t, F (task columns when given) and R^2 of the scaled data
     betas = torch.empty(V, K)
+    tstats = torch.empty(V, K)
+    sigma2 = torch.empty(V)
+    fstats = torch.empty(V)
+    r2 = torch.empty(V)
+    dof = max(1, T - K)
+    ti = list(task_indices) if task_indices else None
     for p in torch.unique(idx).tolist():
         rows = torch.nonzero(idx == p).flatten()
         XtX = Xw[p].T @ Xw[p]
@@ -166,6 +179,24 @@ def fit(data, design, a_grid, b_grid, run_starts=None, exhaustive=False, threads
         Yw = _whiten_rows(Ys[rows], Linv[p], lens)
         bp = (Yw @ Xw[p]) @ A.T
         rw = Yw - bp @ Xw[p].T
-        _sigma2 = rw.pow(2).sum(1, dtype=torch.float64) / max(1, T - K)
+        s2 = (rw.pow(2).sum(1, dtype=torch.float64) / dof).float()
+        tstats[rows] = bp / (torch.sqrt(s2[:, None] * torch.diagonal(A)[None, :]) + 1e-10)
+        if ti is not None:
+            M = torch.linalg.inv(A[ti][:, ti] + 1e-8 * torch.eye(len(ti)))
+            bt = bp[:, ti]
+            fstats[rows] = ((bt @ M) * bt).sum(1) / (s2 * len(ti) + 1e-10)
+        else:
+            fstats[rows] = ((bp @ XtX) * bp).sum(1) / (s2 * K + 1e-10)
+        yv = Ys[rows]
+        pred = bp @ X.T
+        ss_res = (yv - pred).pow(2).sum(1)
+        ss_tot = (yv - yv.mean(1, keepdim=True)).pow(2).sum(1)
+        r2[rows] = torch.where(ss_tot <= 1e-10, torch.zeros_like(ss_tot),
+                               torch.clamp(1.0 - ss_res / ss_tot.clamp(min=1e-10), max=1.0))
         betas[rows] = bp * scale[rows, None]
-    return idx.numpy(), betas.numpy()
+        sigma2[rows] = s2 * scale[rows] ** 2
+    pa, pb = a[idx], b[idx]
+    lam_out = (pb + pa) * (1 + pa * pb) / (((1 + (2 * pa) * pb) + pb * pb) + 1e-10)
+    return {"index": idx.numpy(), "arma_params": torch.stack([pa, pb], 1).numpy(), "betas": betas.numpy(),
+            "tstats": tstats.numpy(), "sigma2": sigma2.numpy(), "fstats": fstats.numpy(), "r2": r2.numpy(),
+            "arma_lambda": lam_out.numpy(), "reml_likelihood": best.numpy()}

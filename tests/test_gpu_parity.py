@@ -29,8 +29,6 @@ pytestmark = pytest.mark.gpu
 DEV = torch.device("cuda:0")
 
 # tolerances (see module docstring)
-# projection kernel of the full-fit tests: "tc" (tcgen05, the default) or "simt"
-PROJ = os.environ.get("FFS_TEST_PROJECTOR", "tc")
 ARGMIN_AGREE = 0.999
 CRIT_GAP_REL = 1e-6
 BETA_REL = 1e-4
@@ -140,7 +138,6 @@ def test_tensor_core_projection_matches_simt(K, T, V):
 @pytest.mark.parametrize("case", ["single", "multirun", "censored", "baseline"])
 @pytest.mark.parametrize("exhaustive", [True, False])
 def test_fit_matches_fp64_oracle(case, exhaustive):
-    projector = PROJ
     d = load_golden(case)
     kw = case_kwargs(d)
     ref = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, fp64_scaled=True,
@@ -148,8 +145,7 @@ def test_fit_matches_fp64_oracle(case, exhaustive):
     gkw = dict(kw)
     if "glt_matrices" in gkw:
         gkw["glt_labels"] = ["c0"]
-    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=projector,
-                         force_exhaustive_search=exhaustive, want_r2_partial=True, **gkw)
+    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, force_exhaustive_search=exhaustive, want_r2_partial=True, **gkw)
     grid = G.make_grid(d["a_grid"], d["b_grid"])
     idx = _index(got.arma_params.numpy(), grid)
     check_selection(idx, ref.arma_index, ref.reml_lklhd_surface)
@@ -188,7 +184,7 @@ def test_fit_any_series_length_matches_fp64_oracle(T):
     kw = dict(a_grid=d["a_grid"], b_grid=d["b_grid"], want_residuals=True, want_ljung_box=True)
     ref = o.fit_glm_arma11(Y, X, use_double=True, fp64_scaled=True, force_exhaustive_search=True,
                            save_profile_likelihoods=True, **kw)
-    got = fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, projector=PROJ, force_exhaustive_search=True,
+    got = fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, force_exhaustive_search=True,
                          want_predicted=True, **kw)
     grid = G.make_grid(d["a_grid"], d["b_grid"])
     idx = _index(got.arma_params.numpy(), grid)
@@ -214,15 +210,14 @@ def test_reference_float32_selection_agrees():
         kw = case_kwargs(d)
         if "glt_matrices" in kw:
             kw["glt_labels"] = ["c0"]
-        got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, projector=PROJ, verbose=False, force_exhaustive_search=True, **kw)
+        got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, force_exhaustive_search=True, **kw)
         agree = (got.arma_params.numpy() == d["f32_exh__arma_params"]).all(1).mean()
         assert agree >= 0.98, (case, agree)
 
 
 def test_use_double_semantics_match_fp64_reference():
     d = load_golden("single")
-    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, a_grid=d["a_grid"], b_grid=d["b_grid"], device=DEV, projector=PROJ,
-                         verbose=False, use_double=True, force_exhaustive_search=True)
+    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, a_grid=d["a_grid"], b_grid=d["b_grid"], device=DEV, verbose=False, use_double=True, force_exhaustive_search=True)
     assert got.betas.dtype == torch.float64
     np.testing.assert_array_equal(got.arma_params.numpy(), d["f64_exh__arma_params"])
     np.testing.assert_allclose(got.reml_likelihood.numpy(), d["f64_exh__reml_likelihood"], rtol=1e-5, atol=2e-3)
@@ -233,7 +228,7 @@ def test_grouped_matches_reference():
     d = load_golden("grouped")
     designs = {h: d[f"X{h}"] for h in range(3)}
     got = fit_glm_arma11_grouped(d["Y"], designs, d["gid"], tr=2.0, a_grid=d["a_grid"], b_grid=d["b_grid"],
-                                 device=DEV, projector=PROJ, force_exhaustive_search=True)
+                                 device=DEV, force_exhaustive_search=True)
     grid = G.make_grid(d["a_grid"], d["b_grid"])
     ref_idx = _index(d["f64_exh__arma_params"], grid)
     idx = _index(got.arma_params.numpy(), grid)
@@ -282,8 +277,7 @@ def test_column_sets_match_oracle_and_reference(exhaustive):
     kw = case_kwargs(d)
     ref = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, fp64_scaled=True, force_exhaustive_search=exhaustive,
                            save_profile_likelihoods=True, **kw)
-    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=PROJ,
-                         force_exhaustive_search=exhaustive, **kw)
+    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, force_exhaustive_search=exhaustive, **kw)
     grid = G.make_grid(d["a_grid"], d["b_grid"])
     idx = _index(got.arma_params.numpy(), grid)
     check_selection(idx, ref.arma_index, ref.reml_lklhd_surface)
@@ -370,8 +364,8 @@ def test_precomputed_params_path():
     d = load_golden("multirun")
     kw = case_kwargs(d)
     kw["glt_labels"] = ["c0"]
-    first = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, projector=PROJ, verbose=False, **kw)
-    again = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, projector=PROJ, verbose=False,
+    first = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, **kw)
+    again = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False,
                            precomputed_arma_params=first.arma_params, **kw)
     np.testing.assert_array_equal(again.arma_params.numpy(), first.arma_params.numpy())
     assert rel_maxnorm(again.betas.numpy(), first.betas.numpy()).max() <= 1e-5
@@ -384,7 +378,7 @@ def test_edge_cases_constant_and_pure_signal_voxels():
     Y[0] = 0.0                                 # all-zero voxel
     Y[1] = 7.5                                 # constant voxel
     Y[2] = d["X"] @ np.arange(d["X"].shape[1], dtype=np.float32)  # exactly in the design span
-    got = fit_glm_arma11(Y, d["X"], tr=2.0, a_grid=d["a_grid"], b_grid=d["b_grid"], device=DEV, projector=PROJ, verbose=False)
+    got = fit_glm_arma11(Y, d["X"], tr=2.0, a_grid=d["a_grid"], b_grid=d["b_grid"], device=DEV, verbose=False)
     for name in ("betas", "tstats", "sigma2", "fstats", "r2", "reml_likelihood"):
         assert torch.isfinite(getattr(got, name)).all(), name
     assert float(got.r2[0]) == 0.0
@@ -399,7 +393,7 @@ def test_workload0_subset_parity_exhaustive_and_hierarchical():
     og = o.valid_grid(g.numpy(), g.numpy(), np.float64)
     surf = o.criterion_surface(w.X, w.Y, og, scaled=True)
     for exhaustive in (True, False):
-        got = fit_glm_arma11(w.Y, w.X, tr=2.0, a_grid=g, b_grid=g, device=DEV, projector=PROJ, verbose=False,
+        got = fit_glm_arma11(w.Y, w.X, tr=2.0, a_grid=g, b_grid=g, device=DEV, verbose=False,
                              force_exhaustive_search=exhaustive)
         if exhaustive:
             ref_idx = np.argmin(surf, axis=1)
@@ -419,15 +413,14 @@ def test_rvar_round_trip_reuses_the_fitted_pairs(tmp_path):
     d = load_golden("multirun")
     kw = case_kwargs(d)
     kw["glt_labels"] = ["c0"]
-    first = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=PROJ, **kw)
+    first = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, **kw)
     V = d["Y"].shape[0]
     mask = np.zeros(V + 7, bool)
     mask[3:3 + V] = True
     path = save_arma_rvar(first, tmp_path / "rvar.nii.gz", volume_shape=(V + 7, 1, 1), voxel_mask=mask)
     ab = load_arma_params(path, mask)
     np.testing.assert_array_equal(ab, first.arma_params.numpy())
-    again = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=PROJ,
-                           precomputed_arma_params=ab, **kw)
+    again = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, precomputed_arma_params=ab, **kw)
     np.testing.assert_array_equal(again.arma_params.numpy(), first.arma_params.numpy())
     assert rel_maxnorm(again.betas.numpy(), first.betas.numpy()).max() <= 1e-5
     import gzip
@@ -460,8 +453,7 @@ def test_dsort_matches_oracle_and_reference(tag, exhaustive):
     else:
         kw.update(dsort=d["D"][:, :1], dsort_run_bounds=[0, 64, 128])
     with pytest.warns(UserWarning, match="constant") if tag == "two" else _no_warning():
-        got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, projector=PROJ,
-                             force_exhaustive_search=exhaustive, glt_labels=["t0-t1"], **kw)
+        got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, force_exhaustive_search=exhaustive, glt_labels=["t0-t1"], **kw)
     ref = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, fp64_scaled=True, force_exhaustive_search=exhaustive,
                            save_profile_likelihoods=True, **kw)
     assert got.dof == ref.dof == int(d[f"{tag}_f64_def__dof"])

@@ -279,3 +279,26 @@ def test_dsort_prepare_guard_expansion_and_errors():
     assert exp.shape == (2, 4, T) and not exp[:, 0, 12:].any() and not exp[:, 1, :12].any()
     with pytest.raises(ValueError, match="dsort must be"):
         engine.dsort_prepare(D[:, :, :T - 1], V, T, None, torch.device("cpu"))
+
+
+def test_parse_grid_arg_formats_and_errors(capsys):
+    """The three -a_grid / -b_grid formats of fastfuncstuff/cli/reml.py:115-160."""
+    from fastfuncstuff_gb300 import parse_grid_arg
+
+    g = parse_grid_arg("-0.9:0.9:65")
+    assert g.dtype == torch.float32 and torch.equal(g, torch.linspace(-0.9, 0.9, 65))
+    assert torch.equal(parse_grid_arg(" 0.025:0.9:32 "), torch.linspace(0.025, 0.9, 32))
+    # three comma-separated values whose last is a whole number >= 2: legacy linspace
+    assert torch.equal(parse_grid_arg("-0.8,0.8,33"), torch.linspace(-0.8, 0.8, 33))
+    assert torch.equal(parse_grid_arg("0,0.8,9.0"), torch.linspace(0.0, 0.8, 9))
+    # anything else separated by commas is the list itself
+    assert torch.equal(parse_grid_arg("0.1,0.2,0.3,0.5,0.7,0.9"),
+                       torch.tensor([0.1, 0.2, 0.3, 0.5, 0.7, 0.9], dtype=torch.float32))
+    assert torch.equal(parse_grid_arg("0.1,0.2,0.5"), torch.tensor([0.1, 0.2, 0.5]))  # last not whole
+    assert torch.equal(parse_grid_arg("0.1,0.2,1"), torch.tensor([0.1, 0.2, 1.0]))   # whole but < 2
+    assert torch.equal(parse_grid_arg("0.4"), torch.tensor([0.4]))
+    for bad in ("0:1", "0:1:2:3", "a:1:5", "0:1:1", "0:1:2.5", "0.1,x", ""):
+        with pytest.raises(SystemExit) as e:
+            parse_grid_arg(bad)
+        assert e.value.code == 1
+        assert "ERROR" in capsys.readouterr().out
