@@ -20,7 +20,7 @@ from .glm.arma import (  # noqa: F401
     search_voxels_precomputed_grid,
     set_afni_mode,
 )
-from .glm.rvar import compute_ljung_box_statistic, load_arma_params, save_arma_rvar  # noqa: F401
+from .glm.rvar import compute_ljung_box_statistic, load_arma_params, save_arma_rvar, save_reml_lklhd  # noqa: F401
 from .glm.engine import autotune_projection  # noqa: F401
 
 from . import ops  # noqa: F401,E402  (registers the ffs_gb300:: torch custom operators)

@@ -1,9 +1,12 @@
-"""The -Rvar file of an ARMA(1,1) fit and its reuse (fastfuncstuff/glm/arma.py:6181-6459).
+"""The -Rvar and -Rlklhd files of an ARMA(1,1) fit and the -Rvar reuse
+(fastfuncstuff/glm/arma.py:6181-6459, fastfuncstuff/cli/reml.py:5102-5163).
 
 ``save_arma_rvar`` writes AFNI 3dREMLfit's 6-volume variance-parameter dataset
 (a, b, lam, StDev, -LogLik, LjungBox) as a float32 NIfTI-1 file, ``.nii`` or
 ``.nii.gz``; ``load_arma_params`` reads volumes 0 and 1 back as the
-``precomputed_arma_params`` of a later fit. The NIfTI-1 header is packed here
+``precomputed_arma_params`` of a later fit. ``save_reml_lklhd`` writes the
+REML criterion at every valid (a, b) pair (``save_profile_likelihoods``), one
+volume per pair labelled ``a=X.XX_b=Y.YY``. The NIfTI-1 header is packed here
 from the format's published field layout (no NIfTI library is needed), with
 the sform and qform both set from the affine (code 1, scanner-anatomical, as
 the reference writes a map that names no template) and AFNI's header
@@ -26,7 +29,8 @@ import torch
 
 from .grid import resolve_ljung_box_lag
 
-__all__ = ["save_arma_rvar", "load_arma_params", "compute_ljung_box_statistic", "RVAR_LABELS"]
+__all__ = ["save_arma_rvar", "save_reml_lklhd", "load_arma_params", "compute_ljung_box_statistic",
+           "RVAR_LABELS"]
 
 RVAR_LABELS = ["a", "b", "lam", "StDev", "-LogLik", "LjungBox"]
 
@@ -233,6 +237,56 @@ def save_arma_rvar(results, output_path, volume_shape=None, voxel_mask=None, aff
     blob = _nifti1_bytes(rvar, np.asarray(affine, np.float64),
                          [(_ECODE_AFNI, _afni_extension(RVAR_LABELS, stataux, rvar.shape[-1]))])
     if str(output_path).endswith(".gz"):
+        with gzip.open(output_path, "wb", compresslevel=6) as f:
+            f.write(blob)
+    else:
+        output_path.write_bytes(blob)
+    return output_path
+
+
+def save_reml_lklhd(results, output_path, volume_shape=None, voxel_mask=None, affine=None) -> Path:
+    """Write the fit's -Rlklhd dataset: the REML criterion of every voxel at
+    every valid (a, b) pair, one float32 volume per pair in the fit's pair
+    order, labelled ``a=X.XX_b=Y.YY`` (fastfuncstuff/cli/reml.py:5102-5163).
+
+    Needs a fit with ``save_profile_likelihoods=True`` (ValueError
+    otherwise). With ``volume_shape`` the volumes have that shape
+    (``voxel_mask`` placing the fitted voxels, zero elsewhere), otherwise
+    (V, 1, 1). A path without a NIfTI suffix gets ``.nii.gz``, as the
+    reference names it; ``.gz`` paths are gzip-compressed."""
+    surf = _np(getattr(results, "reml_lklhd_surface", None))
+    params = getattr(results, "reml_surface_params", None)
+    if surf is None or params is None:
+        raise ValueError("save_reml_lklhd needs a fit with save_profile_likelihoods=True "
+                         "(no likelihood surface on these results)")
+    surf = np.asarray(surf, np.float32)
+    V, n_pairs = surf.shape
+    name = str(output_path)
+    if name.endswith(".nii.zst"):
+        raise ValueError(f"{name}: zstd-compressed NIfTI is not written by this build; use .nii or .nii.gz")
+    if not name.endswith((".nii", ".nii.gz")):
+        name += ".nii.gz"
+    output_path = Path(name)
+    output_path.parent.mkdir(parents=True, exist_ok=True)
+    if volume_shape is not None:
+        volume_shape = tuple(int(x) for x in volume_shape)
+        if voxel_mask is not None:
+            mask = _np(voxel_mask).reshape(-1).astype(bool)
+            vol = np.zeros((int(np.prod(volume_shape)), n_pairs), np.float32)
+            vol[mask] = surf
+            vol = vol.reshape(*volume_shape, n_pairs)
+        else:
+            vol = surf.reshape(*volume_shape, n_pairs)
+    else:
+        vol = surf.reshape(V, 1, 1, n_pairs)
+    if affine is None and getattr(results, "affine", None) is not None:
+        affine = results.affine
+    if affine is None:
+        affine = np.eye(4)
+    labels = [f"a={float(a_k):.2f}_b={float(b_k):.2f}" for (a_k, b_k) in params]
+    blob = _nifti1_bytes(vol, np.asarray(affine, np.float64),
+                         [(_ECODE_AFNI, _afni_extension(labels, None, n_pairs))])
+    if name.endswith(".gz"):
         with gzip.open(output_path, "wb", compresslevel=6) as f:
             f.write(blob)
     else:

@@ -145,3 +145,36 @@ def test_load_arma_params_errors(tmp_path):
     bad.write_bytes(b"\x00" * 400)
     with pytest.raises(ValueError):
         load_arma_params(bad)
+
+
+def test_reml_lklhd_surface_file(tmp_path):
+    """-Rlklhd: one float32 volume per valid pair, labelled a=X.XX_b=Y.YY in pair
+    order (fastfuncstuff/cli/reml.py:5102-5163); the suffix defaults to .nii.gz."""
+    from fastfuncstuff_gb300.glm import grid as G
+    from fastfuncstuff_gb300.glm.arma import ARMA11Results
+    from fastfuncstuff_gb300.glm.rvar import _read_nifti1, save_reml_lklhd
+
+    rng = np.random.default_rng(8)
+    grid = G.make_grid(np.linspace(-0.8, 0.8, 5).astype(np.float32), np.linspace(-0.8, 0.8, 5).astype(np.float32))
+    shape = (3, 4, 2)
+    mask = rng.random(shape) < 0.7
+    V = int(mask.sum())
+    res = ARMA11Results()
+    res.reml_lklhd_surface = torch.from_numpy(rng.standard_normal((V, grid.P)).astype(np.float32))
+    res.reml_surface_params = grid.param_list()
+    path = save_reml_lklhd(res, tmp_path / "lk", volume_shape=shape, voxel_mask=mask)
+    assert path.name == "lk.nii.gz"
+    raw = gzip.decompress(path.read_bytes())
+    h = _header(raw)
+    assert h["dim"][:5] == (4, 3, 4, 2, grid.P) and h["datatype"] == (16, 32)
+    xml = raw[360:352 + h["ext"][0]].decode("utf-8")
+    labels = "~".join(f"a={a:.2f}_b={b:.2f}" for a, b in grid.param_list())
+    assert f'"{labels}"' in xml and "BRICK_STATAUX" not in xml
+    vol = _read_nifti1(path)
+    np.testing.assert_array_equal(vol[mask], res.reml_lklhd_surface.numpy())
+    assert not vol[~mask].any()
+    # without a volume shape: (V, 1, 1, P); a fit without the surface is an error
+    flat = _read_nifti1(save_reml_lklhd(res, tmp_path / "flat.nii"))
+    np.testing.assert_array_equal(flat.reshape(V, grid.P), res.reml_lklhd_surface.numpy())
+    with pytest.raises(ValueError):
+        save_reml_lklhd(ARMA11Results(), tmp_path / "none.nii")
