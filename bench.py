@@ -304,6 +304,7 @@ def learned_quality(args, w, Yd, Xd, kw, kw_l, prop, lay, g, tinfo) -> tuple[dic
         "crit_gap_max_of_disagreeing": float(gap.max().item()) if gap.numel() else 0.0,
         "disagreeing_with_gap_gt_1e-6": int((gap > 1e-6).sum().item()),
         "first_window_on_edge": float(ls.stats["edge_first"]), "full_grid_fallback": ls.stats["fallback"],
+        "strip_voxels": int(ls.stats["strip_voxels"].item()) if ls.stats.get("strip_voxels") is not None else 0,
         "recenter_rounds": args.recenter, "window_pair_evals_per_voxel": pair_evals / V,
     }
     if args.fp64_voxels > 0:
@@ -455,8 +456,9 @@ def run_gb300(args) -> None:
         roof = roofline(dom, ms_d, n_d, T, K, P, pk, clk_l["sm_mhz"], work)
 
     method = ("full grid, one design per HRF group (fit_glm_arma11_grouped)" if grouped else
-              f"learned-seeded 5x5 window refine ({args.recenter} re-centred round), full grid on window edges, "
-              f"replayed from CUDA graphs")
+              f"learned-seeded 5x5 window refine, {args.recenter} re-centred round, the strip next to the identity "
+              f"line for voxels within 2 lattice steps of it, full grid for window edges and voxels a strip pair "
+              f"beats; replayed from CUDA graphs")
     line = {
         "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_l, "higher_is_better": True, "scaling": "weak",

@@ -93,7 +93,7 @@ class ProjectArgs(C.Structure):
         ("ld_u", C.c_int), ("yr_hi", C.c_void_p), ("yr_lo", C.c_void_p), ("u_hi", C.c_void_p),
         ("u_lo", C.c_void_p), ("yexp", C.c_void_p), ("uexp", C.c_void_p),
         ("yr_t", C.c_void_p), ("U", C.c_void_p), ("proj", C.c_void_p),
-        ("flag", C.c_void_p),
+        ("flag", C.c_void_p), ("V_dev", C.c_void_p),
     ]
 
 
@@ -178,6 +178,11 @@ SIGNATURES = {
                          C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p, C.c_void_p], C.c_int),
+    "ffs_reml_strip": ([C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                        C.c_void_p], C.c_int),
+    "ffs_reml_near_line": ([C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                            C.c_void_p], C.c_int),
     "ffs_reml_project_tc_list": ([C.POINTER(ProjectArgs), C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                   C.c_void_p], C.c_int),
 }

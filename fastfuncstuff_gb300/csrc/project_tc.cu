@@ -45,6 +45,7 @@ struct TcParams {
   const int* uexp;
   float* proj;
   int* flag;
+  const int* v_dev;    // grid mode: device count of the operand rows to project (or NULL: V)
 };
 
 // One work item: BM operand rows from v0 (nv of them real) against the np
@@ -54,7 +55,7 @@ struct Item {
 };
 
 template <bool LIST>
-__device__ __forceinline__ Item item_at(const TcParams& prm, int item) {
+__device__ __forceinline__ Item item_at(const TcParams& prm, int item, int Vd) {
   Item it;
   if (LIST) {
     const ffs_tc_item w = prm.items[item];
@@ -68,7 +69,7 @@ __device__ __forceinline__ Item item_at(const TcParams& prm, int item) {
   } else {
     const int col = item % prm.n_col_tiles;
     it.v0 = (item / prm.n_col_tiles) * BM;
-    it.nv = min(BM, prm.V - it.v0);
+    it.nv = min(BM, Vd - it.v0);
     it.row_b = col * prm.g * prm.K;
     it.np = min(prm.g, prm.P - col * prm.g);
     it.out0 = it.v0;
@@ -166,7 +167,9 @@ __global__ void __launch_bounds__(192, 1)
   // a CTA that finds an earlier CTA's wait expired does nothing
   if (*reinterpret_cast<volatile int*>(prm.flag) != 0) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n_items = LIST ? *prm.n_items : prm.n_col_tiles * prm.n_vox_tiles;
+  // grid mode: the rows to project (a device count when given)
+  const int Vd = (!LIST && prm.v_dev) ? min(prm.V, max(0, *prm.v_dev)) : prm.V;
+  const int n_items = LIST ? *prm.n_items : prm.n_col_tiles * ((Vd + BM - 1) / BM);
   const int nk = prm.ld / BK;
 
   if (threadIdx.x == 0) {
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(192, 1)
     int kc = 0;
     bool ok = true;
     for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-      const Item it = item_at<LIST>(prm, item);
+      const Item it = item_at<LIST>(prm, item, Vd);
       const int v0 = it.v0, row_b = it.row_b;
       for (int kb = 0; kb < nk; ++kb, ++kc) {
         const int s = kc % STAGES;
@@ -218,7 +221,7 @@ __global__ void __launch_bounds__(192, 1)
     int kc = 0, local = 0;
     bool ok = true;
     for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x, ++local) {
-      const uint32_t idesc = idesc_f16(BM, item_at<LIST>(prm, item).N);
+      const uint32_t idesc = idesc_f16(BM, item_at<LIST>(prm, item, Vd).N);
       const int buf = local & 1;
       const uint32_t acc = tmem + (uint32_t)(buf * 256);
       if (local >= 2 && !mbar_wait(acc_empty + buf, ((local >> 1) - 1) & 1)) {
@@ -270,7 +273,7 @@ __global__ void __launch_bounds__(192, 1)
       // work-list mode differs in where the result goes
       int v, p_first, ncols, nmax, out_row, out_slot = 0;
       if (LIST) {
-        const Item it = item_at<LIST>(prm, item);
+        const Item it = item_at<LIST>(prm, item, Vd);
         v = row < it.nv ? it.v0 + row : prm.V;
         p_first = it.row_b / prm.K;
         ncols = it.np * prm.K;
@@ -279,6 +282,7 @@ __global__ void __launch_bounds__(192, 1)
         out_slot = it.slot0;
       } else {
         v = (item / prm.n_col_tiles) * BM + row;
+        if (v >= Vd) v = prm.V;  // rows past the device count are not written
         p_first = (item % prm.n_col_tiles) * prm.g;
         ncols = prm.g * prm.K;
         nmax = prm.N;
@@ -446,6 +450,7 @@ extern "C" int ffs_reml_project_tc(const ffs_project_args* a, void* stream) {
   prm.uexp = a->uexp;
   prm.proj = a->proj;
   prm.flag = a->flag;
+  prm.v_dev = a->V_dev;
   return launch_tc(a, prm, prm.n_col_tiles * prm.n_vox_tiles, stream);
 }
 
@@ -480,5 +485,6 @@ extern "C" int ffs_reml_project_tc_list(const ffs_project_args* a, const ffs_tc_
   prm.uexp = a->uexp;
   prm.proj = a->proj;
   prm.flag = a->flag;
+  prm.v_dev = nullptr;
   return launch_tc(a, prm, max_items, stream);
 }

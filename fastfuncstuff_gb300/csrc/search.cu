@@ -273,30 +273,6 @@ constexpr int SURF_G2 = SURF_G / 2;
 constexpr int SURF_THREADS = 256;
 constexpr int SURF_TB = 16;  // time steps per prefetch block
 
-__device__ __forceinline__ uint64_t pack2(float lo, float hi) {
-  uint64_t r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void unpack2(uint64_t v, float& lo, float& hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
-  uint64_t d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
-  uint64_t d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
-  uint64_t d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-
 __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_args a) {
   extern __shared__ float4 cf4[];  // [T][SURF_G2] (-m_2k, -m_2k+1, 1/D_2k, 1/D_2k+1)
   float4* cs4 = cf4 + (size_t)a.T * SURF_G2;                        // [T] c_t of the 4 quarters

@@ -389,6 +389,198 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
   w.best_cell[v] = bcell;
 }
 
+// ---------------------------------------------------------------------- strip
+// The strip next to the identity line: pairs of distinct a (each its own AR
+// filter), evaluated for the sorted rows i < min(n, *n_dev) of the voxels
+// idx[i] after the window rounds, to find a second basin of the criterion
+// that the windows could not see. One thread per row, STRIP_TILE rows per
+// CTA and STRIP_G pairs per CTA (blockIdx.y: the group of pairs). Per chunk
+// of WCH steps the pairs' (c_t, -m_t, 1/D_t) are staged in shared memory with
+// per-couple steady flags; each thread keeps its pairs' states as couples in
+// 64-bit registers advanced with packed f32x2 instructions, in the window
+// kernel's operation order (z = y_t - c_t y_{t-1}, v = z - m v, and in a
+// block of 16 steady steps the sum of v^2 scaled by 1/D once), so a strip
+// pair that is also a window pair gets the window's criterion up to the
+// steady/non-steady split of its couple. A voxel whose least strip criterion
+// lies below its window answer dbest[v] by more than 1e-6 of |crit0[v]| is
+// sent to the full grid: fallback[v] = 1, best_cell[v] = -1 (several CTAs may
+// store the same values).
+constexpr int STRIP_TILE = 128;
+constexpr int STRIP_G = 16;
+constexpr int STRIP_G2 = STRIP_G / 2;
+constexpr int STRIP_MAX = 64;  // pairs per call
+
+struct StripArgs {
+  int n, T, K, n_pairs;
+  const int* n_dev;      // device count of real sorted rows (or NULL: n)
+  const int* pairs;      // [n_pairs] pair indices
+  const int* idx;        // [n] voxel of each sorted row
+  const float* rows;     // [V][T] residualised rows (read at idx[i])
+  const float4* coef;    // [P][T] (c, m, 1/D, -)
+  const float* proj;     // [n_pairs][n] ||U'y||^2 of each strip pair and sorted row
+  const float* dcf;      // [P] (logdet_R + logdet_XtX)[p] - that of (0, 0)
+  const float* dbest;    // [V] the window rounds' criterion (relative to (0, 0))
+  const double* crit0;   // [V] the criterion at (0, 0)
+  int* fallback;         // [V]
+  int* best_cell;        // [V]
+};
+
+__global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
+  __shared__ float4 tab[STRIP_G][WCH + 1];  // (-c, -m, 1/D, 0) at steps c0 - 1 .. c0 + WCH - 1
+  __shared__ uint8_t steady[STRIP_G2][WCH];
+  __shared__ uint8_t bsteady[STRIP_G2][WCB];
+  const int m = w.n_dev ? min(w.n, *w.n_dev) : w.n;
+  const int r0 = blockIdx.x * STRIP_TILE;
+  if (r0 >= m) return;  // uniform over the CTA
+  const int q0 = blockIdx.y * STRIP_G;
+  const int nq = min(STRIP_G, w.n_pairs - q0);
+  const int tid = threadIdx.x;
+  const int i = r0 + tid;
+  const bool live = i < m;
+  const int T = w.T;
+  const float* yrow = w.rows + (size_t)w.idx[live ? i : r0] * T;
+  const bool vec = (T & 3) == 0;
+  const uint64_t zero2 = pack2(0.f, 0.f);
+  uint64_t vv[STRIP_G2], st[STRIP_G2];
+#pragma unroll
+  for (int j = 0; j < STRIP_G2; ++j) vv[j] = st[j] = zero2;
+  float yy = 0.f, yp = 0.f;
+  for (int c0 = 0; c0 < T; c0 += WCH) {
+    const int cn = min(WCH, T - c0);
+    __syncthreads();  // the previous chunk's tables are no longer read
+    for (int e = tid; e < STRIP_G * (cn + 1); e += blockDim.x) {
+      const int q = e / (cn + 1), s = e % (cn + 1);
+      const int t = c0 - 1 + s;
+      float4 c = make_float4(0.f, 0.f, 0.f, 0.f);  // an empty slot: nothing summed
+      if (q < nq && t >= 0) {
+        const float4 r = w.coef[(size_t)w.pairs[q0 + q] * T + t];
+        c = make_float4(-r.x, -r.y, r.z, 0.f);
+      }
+      tab[q][s] = c;
+    }
+    __syncthreads();
+    for (int e = tid; e < STRIP_G2 * cn; e += blockDim.x) {
+      const int j = e / cn, s = e % cn;
+      bool same = c0 + s > 0;
+      for (int h = 0; h < 2 && same; ++h) {
+        const float4 x = tab[2 * j + h][s + 1], y = tab[2 * j + h][s];
+        same = x.x == y.x && x.y == y.y && x.z == y.z;
+      }
+      steady[j][s] = same ? 1 : 0;
+    }
+    __syncthreads();
+    for (int e = tid; e < STRIP_G2 * WCB; e += blockDim.x) {
+      const int j = e / WCB, bk = e % WCB;
+      bool all = bk * CRIT_TB + CRIT_TB <= cn;
+      for (int s = bk * CRIT_TB; s < bk * CRIT_TB + CRIT_TB && all; ++s) all = steady[j][s] != 0;
+      bsteady[j][bk] = all ? 1 : 0;
+    }
+    __syncthreads();
+    for (int bs = 0; bs < cn; bs += CRIT_TB) {
+      const int t0 = c0 + bs;
+      float yb[CRIT_TB];
+      if (vec) {
+#pragma unroll
+        for (int k = 0; k < CRIT_TB; k += 4) {
+          const float4 q4 = t0 + k < T ? *reinterpret_cast<const float4*>(yrow + t0 + k)
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+          yb[k] = q4.x;
+          yb[k + 1] = q4.y;
+          yb[k + 2] = q4.z;
+          yb[k + 3] = q4.w;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yrow[t0 + k] : 0.f;
+      }
+      {
+        float yy_b = 0.f;
+#pragma unroll
+        for (int k = 0; k < CRIT_TB; ++k) yy_b = fmaf(yb[k], yb[k], yy_b);
+        yy += yy_b;
+      }
+#pragma unroll
+      for (int j = 0; j < STRIP_G2; ++j) {
+        if (2 * j < nq) {  // uniform over the CTA
+          float4 ca = tab[2 * j][bs + 1], cb = tab[2 * j + 1][bs + 1];
+          uint64_t nc = pack2(ca.x, cb.x), nm = pack2(ca.y, cb.y), id = pack2(ca.z, cb.z);
+          uint64_t v2 = vv[j], sq = zero2;
+          float ypr = yp;
+          if (bsteady[j][bs / CRIT_TB]) {
+#pragma unroll
+            for (int k = 0; k < CRIT_TB; ++k) {
+              const uint64_t z = fma2(nc, pack2(ypr, ypr), pack2(yb[k], yb[k]));
+              ypr = yb[k];
+              v2 = fma2(nm, v2, z);
+              sq = fma2(v2, v2, sq);
+            }
+            st[j] = fma2(sq, id, st[j]);
+          } else {
+#pragma unroll
+            for (int k = 0; k < CRIT_TB; ++k) {
+              if (t0 + k < T) {
+                if (!steady[j][bs + k]) {
+                  ca = tab[2 * j][bs + k + 1];
+                  cb = tab[2 * j + 1][bs + k + 1];
+                  nc = pack2(ca.x, cb.x);
+                  nm = pack2(ca.y, cb.y);
+                  id = pack2(ca.z, cb.z);
+                }
+                const uint64_t z = fma2(nc, pack2(ypr, ypr), pack2(yb[k], yb[k]));
+                ypr = yb[k];
+                v2 = fma2(nm, v2, z);
+                sq = fma2(mul2(v2, id), v2, sq);
+              }
+            }
+            st[j] = add2(st[j], sq);
+          }
+          vv[j] = v2;
+        }
+      }
+      yp = yb[CRIT_TB - 1];
+    }
+  }
+  if (!live) return;
+  const float Tk = (float)(T - w.K);
+  float bd = INFINITY;
+#pragma unroll
+  for (int j = 0; j < STRIP_G2; ++j) {
+    float s2[2];
+    unpack2(st[j], s2[0], s2[1]);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int q = 2 * j + h;
+      if (q < nq) {
+        const float rss = fmaxf(s2[h] - w.proj[(size_t)(q0 + q) * w.n + i], 0.f);
+        bd = fminf(bd, w.dcf[w.pairs[q0 + q]] + Tk * log1pf((rss - yy) / (yy + 1e-10f)));
+      }
+    }
+  }
+  const int v = w.idx[i];
+  if (bd < w.dbest[v] - 1e-6f * fabsf((float)w.crit0[v])) {
+    w.fallback[v] = 1;
+    w.best_cell[v] = -1;
+  }
+}
+
+// The voxels v < V whose pair best[v] lies within k0 lattice steps of an
+// identity pair (dist[p] per pair) and that the full grid does not take
+// anyway (fallback[v] == 0, when given), compacted into ids[0 .. *count) (in
+// no particular order; each voxel's later results depend on it alone).
+__global__ void near_line_kernel(int V, const int* best, const int* dist, int k0, const int* fallback, int* ids,
+                                 int* count) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool take = v < V && dist[best[v]] <= k0 && !(fallback && fallback[v]);
+  const unsigned mk = __ballot_sync(0xffffffffu, take);
+  if (!mk) return;
+  const int lane = threadIdx.x & 31;
+  const int first = __ffs(mk) - 1;
+  int base = 0;
+  if (lane == first) base = atomicAdd(count, __popc(mk));
+  base = __shfl_sync(0xffffffffu, base, first);
+  if (take) ids[base + __popc(mk & ((1u << lane) - 1))] = v;
+}
+
 // fp16 operand rows and exponents in the order idx: a warp per row, 16-byte words
 __global__ void __launch_bounds__(256) gather_rows_kernel(int n, const int* n_dev, int ld_y, const int* __restrict__ idx,
                                                           const uint4* __restrict__ hi, const uint4* __restrict__ lo,
@@ -589,4 +781,33 @@ extern "C" int ffs_reml_centers(int V, const float* prop, const float* a_axis, i
   FFS_REQUIRE(V > 0 && prop && a_axis && b_axis && center && n_a > 0 && n_b > 0, "ffs_reml_centers: bad arguments");
   center_kernel<<<ceil_div(V, 256), 256, 0, (cudaStream_t)stream>>>(V, prop, a_axis, n_a, b_axis, n_b, center);
   return check_launch("center_kernel");
+}
+
+extern "C" int ffs_reml_strip(int n, const int* n_dev, int T, int K, int n_pairs, const int* pairs, const int* idx,
+                              const float* rows, const float* coef, const float* proj, const float* dcf,
+                              const float* dbest, const double* crit0, int* fallback, int* best_cell,
+                              void* stream) {
+  clear_error();
+  FFS_REQUIRE(n > 0 && T > K && K > 0 && n_pairs > 0 && n_pairs <= STRIP_MAX,
+              "ffs_reml_strip: bad sizes (n=%d T=%d K=%d n_pairs=%d, at most %d pairs)", n, T, K, n_pairs,
+              STRIP_MAX);
+  FFS_REQUIRE(pairs && idx && rows && coef && proj && dcf && dbest && crit0 && fallback && best_cell,
+              "ffs_reml_strip: null buffer");
+  FFS_REQUIRE(((uintptr_t)rows & 15) == 0 && ((uintptr_t)coef & 15) == 0,
+              "ffs_reml_strip: rows and coef must be 16-byte aligned");
+  StripArgs w{n, T, K, n_pairs, n_dev, pairs, idx, rows, reinterpret_cast<const float4*>(coef), proj, dcf, dbest,
+              crit0, fallback, best_cell};
+  const dim3 grid(ceil_div(n, STRIP_TILE), ceil_div(n_pairs, STRIP_G));
+  strip_crit_kernel<<<grid, STRIP_TILE, 0, (cudaStream_t)stream>>>(w);
+  return check_launch("strip_crit_kernel");
+}
+
+extern "C" int ffs_reml_near_line(int V, const int* best, const int* dist, int k0, const int* fallback, int* ids,
+                                  int* count, void* stream) {
+  clear_error();
+  FFS_REQUIRE(V > 0 && best && dist && ids && count, "ffs_reml_near_line: bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  FFS_CUDA(cudaMemsetAsync(count, 0, sizeof(int), st));
+  near_line_kernel<<<ceil_div(V, 256), 256, 0, st>>>(V, best, dist, k0, fallback, ids, count);
+  return check_launch("near_line_kernel");
 }

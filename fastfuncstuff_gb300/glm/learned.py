@@ -233,8 +233,67 @@ def _grid_consts(g: RemlGrid, dev):
         c = dict(ident=torch.from_numpy(ident_np.astype(np.uint8)).to(dev), p_id=int(np.nonzero(ident_np)[0][0]),
                  a_ax=torch.from_numpy(g.a_axis).to(dev), b_ax=torch.from_numpy(g.b_axis).to(dev),
                  evals=torch.from_numpy(np.append(evals, 0)).to(dev))  # [ncell + 1]: 0 for a skipped voxel
+        # lattice (Manhattan) distance of every pair to the nearest identity
+        # pair, and the strip next to the identity line (distance 1)
+        ia = np.searchsorted(g.a_axis, g.a)
+        ib = np.searchsorted(g.b_axis, g.b)
+        ida, idb = ia[ident_np], ib[ident_np]
+        dist = (np.abs(ia[:, None] - ida[None, :]) + np.abs(ib[:, None] - idb[None, :])).min(1).astype(np.int32)
+        c["dist_id"] = torch.from_numpy(dist).to(dev)
+        strip = np.nonzero(dist == 1)[0][:STRIP_MAX]
+        c["strip"] = {"n": int(strip.size), "pairs": torch.from_numpy(strip.astype(np.int64)).to(dev),
+                      "pairs32": torch.from_numpy(strip.astype(np.int32)).to(dev)}
         _GRID_CONSTS[key] = c
     return c
+
+
+STRIP_MAX = 64  # most pairs one ffs_reml_strip call takes
+STRIP_K0 = 2  # voxels whose answer lies this close to the identity line get the strip next to it
+
+
+def _strip_round(pre, f, out, *, flag, k0: int):
+    """The pairs next to the identity line (lattice distance 1) for the voxels
+    whose answer lies within k0 lattice steps of it and that the full grid
+    does not take anyway: there the criterion is nearly flat along the line
+    and can have minima at several a, so a window holding one of them proves
+    nothing about the others. The voxels are compacted on the device
+    (ffs_reml_near_line), their rows split to fp16 while gathered, projected
+    against the strip pairs' U rows in one tcgen05 launch (only the device
+    count of rows) and evaluated by ffs_reml_strip, which sends a voxel whose
+    strip pair beats its answer to the full grid."""
+    lib = _lib.load()
+    dev = pre.scale.device
+    c = _window_consts(f)
+    sc = c["strip"]
+    if sc["n"] == 0:
+        return
+    V = out["best"].numel()
+    K, P, T, ld = f.K, f.P, f.T, f.ld
+    st = _st()
+    ids = torch.empty(V, dtype=torch.int32, device=dev)
+    count = torch.empty(1, dtype=torch.int32, device=dev)
+    engine._run("ffs_reml_near_line", lib.ffs_reml_near_line, V, _p(out["best"]), _p(c["dist_id"]), int(k0),
+                _p(out["fb"]), _p(ids), _p(count), st)
+    hi = torch.empty(V, ld, dtype=torch.int16, device=dev)
+    lo = torch.empty(V, ld, dtype=torch.int16, device=dev)
+    yexp = torch.empty(V, dtype=torch.int32, device=dev)
+    engine._run("ffs_reml_gather", lib.ffs_reml_gather, V, _p(count), T, ld, _p(ids), None, None, _p(pre.yexp),
+                _p(pre.rows), _p(hi), _p(lo), _p(yexp), None, st)
+    nq = sc["n"]
+    u_hi = f.U_hi.view(P, K * ld).index_select(0, sc["pairs"])  # [nq][K][ld]: rows nq * K
+    u_lo = f.U_lo.view(P, K * ld).index_select(0, sc["pairs"])
+    uex = f.uexp.index_select(0, sc["pairs"])
+    proj = torch.empty(nq, V, dtype=torch.float32, device=dev)
+    pa = _lib.ProjectArgs(V=V, T=T, K=K, P=nq, ld_y=ld, ld_u=ld, yr_hi=_p(hi), yr_lo=_p(lo), u_hi=_p(u_hi),
+                          u_lo=_p(u_lo), yexp=_p(yexp), uexp=_p(uex), yr_t=None, U=None, proj=_p(proj),
+                          flag=_p(flag), V_dev=_p(count))
+    engine._run("ffs_reml_project_tc", lib.ffs_reml_project_tc, C.byref(pa), st)
+    engine._run("ffs_reml_strip", lib.ffs_reml_strip, V, _p(count), T, K, nq, _p(sc["pairs32"]), _p(ids),
+                _p(pre.rows), _p(f.coef), _p(proj), _p(c["dcf"]), _p(out["dbest"]), _p(out["crit0"]),
+                _p(out["fb"]), _p(out["cell"]), st)
+    out["pair_evals"] = out.get("pair_evals", 0) + nq * count.sum()
+    out["strip_voxels"] = count
+    out.setdefault("_keep", []).append((ids, hi, lo, yexp, u_hi, u_lo, uex, proj))
 
 
 def _window_round(pre, f, cen, out, *, flag, join=None):
@@ -306,13 +365,16 @@ class WindowState:
 
 def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
                     do_scale: bool = True, recenter: int = 0, q0: torch.Tensor | None = None,
-                    join=None) -> WindowState:
+                    join=None, strip_k0: int = STRIP_K0) -> WindowState:
     """The window rounds of the learned-seeded search, with no host round trip
     (so they also run inside a CUDA graph): prep with the proposal features,
-    the MLP, the 5 x 5 window of every voxel and ``recenter`` re-centred rounds
-    for the voxels on a window edge. With ``q0`` (engine.design_basis) the
-    prep does not read the factors; ``join()`` is then called before their
-    first use (they may be built on another stream meanwhile)."""
+    the MLP, the 5 x 5 window of every voxel, ``recenter`` re-centred rounds
+    for the voxels on a window edge, then the strip next to the identity line
+    for the voxels whose answer lies within ``strip_k0`` lattice steps of it
+    (-1: none); a voxel that a strip pair beats takes the full grid. With
+    ``q0`` (engine.design_basis) the prep does not read the factors;
+    ``join()`` is then called before their first use (they may be built on
+    another stream meanwhile)."""
     lib = _lib.load()
     dev = Y.device
     V, T = Y.shape
@@ -346,6 +408,9 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
         again = (out["fb"] != 0) & (out["cell"] >= 0)
         cen = torch.where(again, out["cell"], torch.full_like(out["cell"], ncell)).contiguous()
         counts.append(_window_round(p1, f, cen, out, flag=flag))
+    if strip_k0 >= 0:  # on the last round's answers
+        _strip_round(p1, f, out, flag=flag, k0=strip_k0)
+    stats["strip_voxels"] = out.get("strip_voxels")
     best_crit = (out["crit0"] + out["dbest"].double()).float()
     fb = out["fb"]
     small = torch.stack([fb.sum().to(torch.int32), flag[0]] + [cn[1] for cn in counts])
@@ -385,11 +450,12 @@ def learned_fallback(Y: torch.Tensor, factors: engine.GridFactors, ws: WindowSta
 
 def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
                    do_scale: bool = True, recenter: int = 0, before_fallback=None, q0=None,
-                   join=None) -> LearnedOut:
+                   join=None, strip_k0: int = STRIP_K0) -> LearnedOut:
     """Learned-seeded REML search: the 5 x 5 window around each proposal, the
     full grid for voxels whose best pair sits on the window edge (or whose
     window, holding no identity pair, has nothing below the identity pairs'
-    criterion).
+    criterion), and for voxels near the identity line whose answer a pair of
+    the strip next to that line beats (``strip_k0``, see ``learned_windows``).
 
     ``recenter`` > 0 first re-evaluates such voxels that many times with the
     window centred on their best pair; the full grid then takes those still on
@@ -399,7 +465,8 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
     ``LearnedOut.fallback_idx`` lists the voxels whose pair changed after it.
     """
     Y = Y.float().contiguous()
-    ws = learned_windows(Y, factors, proposal, layout, do_scale=do_scale, recenter=recenter, q0=q0, join=join)
+    ws = learned_windows(Y, factors, proposal, layout, do_scale=do_scale, recenter=recenter, q0=q0, join=join,
+                         strip_k0=strip_k0)
     # copy the few numbers the host needs to pinned memory behind an event,
     # queue the caller's work, and wait for that event only
     host = torch.empty(ws.small.numel(), dtype=torch.int32, pin_memory=True)

@@ -246,6 +246,9 @@ typedef struct {
   float* proj;          /* [P][V]                                                 */
   int* flag;            /* device int, 0 on entry; set non-zero if a bounded
                            device-side wait expired (tc form)                    */
+  const int* V_dev;     /* NULL, or a device count: only the operand rows
+                           v < min(V, *V_dev) are projected (tc grid form; V
+                           stays the row stride of proj)                         */
 } ffs_project_args;
 
 int ffs_reml_project_tc(const ffs_project_args* a, void* stream);
@@ -551,6 +554,32 @@ int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, c
                     const float* winproj, const float* dcf, const unsigned char* ident, int p_id,
                     const double* c_p0, int* best, float* dbest, double* crit0, int* fallback, int* best_cell,
                     void* stream);
+
+/* The strip next to the identity line in the learned-seeded refine (no
+ * reference counterpart: the reference searches every pair). Near lambda = 0
+ * the criterion is nearly flat along the line a = -b and can have minima at
+ * several a, so a window holding one of them proves nothing about the others.
+ * n_pairs <= 64 pairs (pair indices pairs[]) are evaluated for the sorted rows
+ * i < min(n, *n_dev) (n_dev may be NULL) of the voxels idx[i]: the window
+ * kernel's recurrence over rows[idx[i]] (16-byte aligned, T samples each) and
+ * the projections proj[q][i] (row stride n: ffs_reml_project_tc of the
+ * gathered rows against the pairs' U rows), giving each pair's criterion
+ * relative to (0, 0) as ffs_reml_window forms it. A voxel v whose least strip
+ * criterion lies below its window answer dbest[v] by more than
+ * 1e-6 |crit0[v]| gets fallback[v] = 1 and best_cell[v] = -1 (the full grid
+ * decides); nothing else is written. */
+int ffs_reml_strip(int n, const int* n_dev, int T, int K, int n_pairs, const int* pairs, const int* idx,
+                   const float* rows, const float* coef, const float* proj, const float* dcf, const float* dbest,
+                   const double* crit0, int* fallback, int* best_cell, void* stream);
+
+/* The voxels v < V whose pair best[v] lies within k0 lattice steps of an
+ * identity pair (dist[p]: the Manhattan lattice distance of pair p to the
+ * nearest lambda = 0 pair) and, when fallback is given, fallback[v] == 0, into
+ * ids[0 .. *count), in no particular order: the learned-seeded refine
+ * evaluates the strip next to the identity line for these voxels (no
+ * reference counterpart). */
+int ffs_reml_near_line(int V, const int* best, const int* dist, int k0, const int* fallback, int* ids, int* count,
+                       void* stream);
 
 #ifdef __cplusplus
 }

@@ -130,35 +130,107 @@ def test_learned_search_agrees_with_full_grid_and_beats_untrained():
     X = torch.from_numpy(w.X).to(dev)
     gr = torch.linspace(-0.8, 0.8, 33)
     f = engine.build_factors(X, G.make_grid(gr, gr), lay)
-    x, y = learned.training_set(X, f, lay, 1_000_000, seed=5)
-    prop, hist = learned.train(x, y, epochs=15, batch=8192, lr=3e-3, seed=1)
+    x, y = learned.training_set(X, f, lay, 2_000_000, seed=5)  # the benchmark's training size
+    prop, hist = learned.train(x, y, epochs=30, batch=8192, lr=3e-3, seed=1)
     # against the untrained network on the same held-out features
     out0 = learned.ArmaProposal(learned.init_params(1, dev)).forward(x[:50_000])
     loss0 = float(((out0 - y[:50_000]) ** 2).sum(1).mean().item() / 2)
     assert hist[-1]["holdout_loss"] < 0.2 * loss0
-    # held-out voxels
+    # held-out voxels, (a, b) uniform over the valid grid
     a_t = torch.from_numpy(f.grid.a).to(dev)
     b_t = torch.from_numpy(f.grid.b).to(dev)
-    idx = torch.randint(0, f.P, (20_000,), generator=torch.Generator().manual_seed(9)).to(dev)
+    idx = torch.randint(0, f.P, (50_000,), generator=torch.Generator().manual_seed(9)).to(dev)
     Y = learned.simulate(X, lay, a_t[idx], b_t[idx], seed=4242)
     full = engine.search(Y, f, hierarchical=False)
-    seeded = learned.learned_search(Y, f, prop, lay)
-    agree = (seeded.best == full.best).float().mean().item()
+    seeded = learned.learned_search(Y, f, prop, lay, strip_k0=-1)  # the windows alone
     fb = seeded.fallback.float().mean().item()
-    untrained = learned.learned_search(Y, f, learned.ArmaProposal(learned.init_params(1, dev)), lay)
+    untrained = learned.learned_search(Y, f, learned.ArmaProposal(learned.init_params(1, dev)), lay, strip_k0=-1)
     fb0 = untrained.fallback.float().mean().item()
-    print(f"learned: agreement {agree:.5f}, fallback {fb:.4f}; untrained fallback {fb0:.4f}")
-    # voxels that fall back take the full grid's answer; the others take the
-    # window's, so disagreements are second basins the edge test cannot see
-    assert agree >= 0.985
     assert fb < 0.8 * fb0  # the trained network keeps more voxels inside their window
-    # no window beats the full grid's global minimum (criterion to the parity bar)
-    gap = (seeded.best_crit.double() - full.best_crit.double()) / full.best_crit.double().abs().clamp(min=1.0)
-    assert float(gap.min()) >= -1e-6
-    # one re-centred round sends at most half as many voxels to the full grid
+    # the whole search (windows, one re-centred round, the strip next to the
+    # identity line, full-grid fallback)
     rc = learned.learned_search(Y, f, prop, lay, recenter=1)
-    print(f"recentred: fallback {rc.stats['fallback']:.4f}, agreement {(rc.best == full.best).float().mean().item():.5f}")
-    assert rc.stats["fallback"] <= 0.5 * fb
+    agree_u = (rc.best == full.best).float().mean().item()
+    # held-out voxels whose (a, b) follow the benchmark workload's
+    # distribution: a ~ U(0.1, 0.8), b ~ U(-0.5, 0.3)
+    gen = torch.Generator().manual_seed(11)
+    a_w = (0.1 + 0.7 * torch.rand(100_000, generator=gen)).to(dev)
+    b_w = (-0.5 + 0.8 * torch.rand(100_000, generator=gen)).to(dev)
+    Yw = learned.simulate(X, lay, a_w, b_w, seed=777)
+    full_w = engine.search(Yw, f, hierarchical=False)
+    rw = learned.learned_search(Yw, f, prop, lay, recenter=1)
+    same = rw.best == full_w.best
+    agree = same.float().mean().item()
+    gap = (rw.best_crit.double() - full_w.best_crit.double()) / full_w.best_crit.double().abs().clamp(min=1.0)
+    print(f"learned: agreement {agree:.5f} (workload distribution), {agree_u:.5f} (uniform over the grid; "
+          f"windows alone {(seeded.best == full.best).float().mean().item():.5f}); fallback {rw.stats['fallback']:.4f}, "
+          f"strip voxels {int(rw.stats['strip_voxels'].item())}, gap of the disagreeing max "
+          f"{float(gap[~same].max()) if bool((~same).any()) else 0.0:.2e}; untrained fallback {fb0:.4f}")
+    assert agree >= 0.999
+    assert agree_u >= 0.998
+    # a voxel's answer is never below the global minimum (a window can only miss it)
+    assert float(gap.min()) >= -1e-6
+    # the strip only ever moves a voxel to the full grid
+    assert float(rw.stats["fallback"]) >= 0.0
+
+
+@pytest.mark.gpu
+def test_strip_kernel_matches_full_grid_surface():
+    """ffs_reml_strip sends to the full grid exactly the voxels whose least
+    criterion over the strip next to the identity line (the full surface's
+    values) lies below their window answer by more than 1e-6 of |crit0|,
+    up to rounding next to that threshold, and only voxels of the device
+    count compacted by ffs_reml_near_line."""
+    from fastfuncstuff_gb300 import synth
+    from fastfuncstuff_gb300.glm import engine, learned
+    from fastfuncstuff_gb300.glm import grid as G
+
+    dev = torch.device("cuda:0")
+    w = synth.workload(1, V=3000)
+    lay = G.run_layout(w.T, w.run_starts)
+    X = torch.from_numpy(w.X).to(dev)
+    gr = torch.linspace(-0.8, 0.8, 33)
+    g = G.make_grid(gr, gr)
+    f = engine.build_factors(X, g, lay)
+    Y = torch.from_numpy(w.Y).to(dev)
+    V = Y.shape[0]
+    so = engine.search(Y, f, hierarchical=False, keep_surface=True)
+    surf = so.surf.double().cpu().numpy()
+    crit0 = so.crit0.cpu().numpy()
+    n_b = len(g.b_axis)
+    rng = np.random.default_rng(5)
+    cells = rng.integers(0, len(g.a_axis) * n_b, V).astype(np.int32)  # windows anywhere
+    out = dict(best=torch.empty(V, dtype=torch.int32, device=dev), dbest=torch.empty(V, device=dev),
+               crit0=torch.empty(V, dtype=torch.float64, device=dev), fb=torch.zeros(V, dtype=torch.int32, device=dev),
+               cell=torch.empty(V, dtype=torch.int32, device=dev))
+    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    pre = engine.prep(Y, f, want_yr_t=False, want_rows=True, split=False)
+    learned._window_round(pre, f, torch.from_numpy(cells).to(dev), out, flag=flag)
+    torch.cuda.synchronize()
+    fb0 = out["fb"].cpu().numpy().copy()
+    best = out["best"].cpu().numpy()
+    dbest = out["dbest"].cpu().numpy().astype(np.float64)
+    k0 = 6
+    learned._strip_round(pre, f, out, flag=flag, k0=k0)
+    torch.cuda.synchronize()
+    assert int(flag.item()) == 0
+    fb1 = out["fb"].cpu().numpy()
+    cell1 = out["cell"].cpu().numpy()
+    c = learned._window_consts(f)
+    dist = c["dist_id"].cpu().numpy()
+    strip = c["strip"]["pairs"].cpu().numpy()
+    assert strip.size == 32 and (dist[strip] == 1).all()
+    taken = (dist[best] <= k0) & (fb0 == 0)
+    assert int(out["strip_voxels"].item()) == int(taken.sum())
+    smin = surf[strip].min(0)
+    thr = dbest - 1e-6 * np.abs(crit0)
+    want = taken & (smin < thr)
+    near = np.abs(smin - thr) <= 2e-7 * np.abs(crit0) + 1e-4  # rounding of the two kernels' sums
+    assert want.any() and (taken & ~want).any()
+    newly = (fb1 == 1) & (fb0 == 0)
+    assert ((newly == want) | near).all()
+    assert (cell1[newly] == -1).all()
+    assert (fb1[fb0 == 1] == 1).all() and not newly[~taken].any()
 
 
 @pytest.mark.gpu
@@ -285,7 +357,7 @@ def test_fit_with_proposal_matches_full_grid_fit_where_pairs_agree(cuda_graphs):
     again = fit_glm_arma11(Y, X, proposal=prop, proposal_recenter=1, cuda_graphs=cuda_graphs, **kw)
     assert torch.equal(got.betas, again.betas)  # a replay gives the same results
     same = (got.arma_params == full.arma_params).all(1)
-    assert float(same.float().mean()) >= 0.97
+    assert float(same.float().mean()) >= 0.995  # a briefly trained network
     assert 0.0 < float(got.learned_fallback) < 0.5  # some voxels took the fallback path
     for name in ("betas", "tstats", "sigma2", "fstats", "r2", "arma_lambda", "residuals", "residuals_whitened"):
         a, b = getattr(got, name)[same], getattr(full, name)[same]
