@@ -262,8 +262,10 @@ __global__ void __launch_bounds__(GLS_WARPS * 32) gls_kernel(ffs_gls_args a, Gls
 // the tiles of pair g and blocks past the last tile exit. T % 4 == 0.
 //
 // The tile's 32 series sit in shared memory, one voxel per lane (tile.cuh):
-//   b0 = G'y and r = y - X b0, then the refinement d = G'r (b = b0 + d) as
-//   register-blocked passes. The residual statistics use r: the refined
+//   b0 = G'y and r = y - X b0, then the refinement d = G'r (b = b0 + d): the
+//   projections as register-blocked CUDA-core passes (tile_project), the
+//   update r = y - X b0 as warp-level tensor-core MMAs of tf32 hi/lo splits
+//   (tile_subtract_any). The residual statistics use r: the refined
 //   residual r - X d differs from it by X d, which changes the whitened
 //   residual sum of squares only to second order (L^-1 r is orthogonal to
 //   L^-1 X up to d), so the update is not formed. The whitened residual
@@ -428,14 +430,15 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
       m = warp_sum(s) / (float)T;
     }
     float sy = 0.f;
+    const float inv = __frcp_rn(sc);  // one reciprocal per voxel, then products
     if (vec) {  // whole quads: no padding inside the row
       for (int q = lane; q < nq; q += 32) {
         const float4 y = row4[q];
         float4 r;
-        r.x = __fdiv_rn(__fsub_rn(y.x, m), sc);
-        r.y = __fdiv_rn(__fsub_rn(y.y, m), sc);
-        r.z = __fdiv_rn(__fsub_rn(y.z, m), sc);
-        r.w = __fdiv_rn(__fsub_rn(y.w, m), sc);
+        r.x = __fmul_rn(__fsub_rn(y.x, m), inv);
+        r.y = __fmul_rn(__fsub_rn(y.y, m), inv);
+        r.z = __fmul_rn(__fsub_rn(y.z, m), inv);
+        r.w = __fmul_rn(__fsub_rn(y.w, m), inv);
         row4[q] = r;
         sy += ((r.x + r.y) + r.z) + r.w;
       }
@@ -444,10 +447,10 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
         const float4 y = row4[q];
         const int t = 4 * q;
         float4 r;
-        r.x = __fdiv_rn(__fsub_rn(y.x, m), sc);
-        r.y = t + 1 < T ? __fdiv_rn(__fsub_rn(y.y, m), sc) : 0.f;
-        r.z = t + 2 < T ? __fdiv_rn(__fsub_rn(y.z, m), sc) : 0.f;
-        r.w = t + 3 < T ? __fdiv_rn(__fsub_rn(y.w, m), sc) : 0.f;
+        r.x = __fmul_rn(__fsub_rn(y.x, m), inv);
+        r.y = t + 1 < T ? __fmul_rn(__fsub_rn(y.y, m), inv) : 0.f;
+        r.z = t + 2 < T ? __fmul_rn(__fsub_rn(y.z, m), inv) : 0.f;
+        r.w = t + 3 < T ? __fmul_rn(__fsub_rn(y.w, m), inv) : 0.f;
         row4[q] = r;
         sy += ((r.x + r.y) + r.z) + r.w;
       }
@@ -463,8 +466,8 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
 
   const float* Gg = a.G + (size_t)g * K * LT;
   const float* Xt = a.Xt + (size_t)design_of(a, g) * K * LT;
-  // b0 = G'y; SS_tot; r = y - X b0. Warp w owns the rows 4w .. 4w+3 in the
-  // row passes (tile_subtract's layout), lanes over quads.
+  // b0 = G'y; SS_tot; r = y - X b0. Warp w takes the rows 4w .. 4w+3 in the
+  // row passes, lanes over quads.
   tile_project(Gg, LT, Ys, ld, K, C0);
 #pragma unroll
   for (int i = 0; i < TILE_SUB_VB; ++i) {
@@ -487,8 +490,7 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
     sst = warp_sum(sst);
     if (lane == 0) st[4 * TILE_V + l] = sst;
   }
-  tile_subtract(Xt, LT, C0, Ys, ld, K);
-  __syncthreads();
+  tile_subtract_any(Xt, LT, C0, Ys, ld, K);
   // the refinement d = G'r; SS_res and the unwhitened outputs
   tile_project(Gg, LT, Ys, ld, K, C1);
 #pragma unroll

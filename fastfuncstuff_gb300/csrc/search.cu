@@ -174,9 +174,17 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
     }
     const float mean = warp_sum(s) / (float)T;
     float sq = 0.f;
-    for (int t = lane; t < T; t += 32) {
-      const float dlt = row[t] - mean;
-      sq += dlt * dlt;
+    if (vec) {  // whole quads: no padding inside the row
+      for (int q = lane; q < nq; q += 32) {
+        const float4 x = row4[q];
+        const float d0 = x.x - mean, d1 = x.y - mean, d2 = x.z - mean, d3 = x.w - mean;
+        sq += ((d0 * d0 + d1 * d1) + d2 * d2) + d3 * d3;
+      }
+    } else {
+      for (int t = lane; t < T; t += 32) {
+        const float dlt = row[t] - mean;
+        sq += dlt * dlt;
+      }
     }
     sq = warp_sum(sq);
     float sc = 1.0f;
@@ -185,14 +193,23 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
       sc = fmaxf(sc, 1e-8f);
     }
     const float m = centre_on(a) ? mean : 0.f;
-    for (int t = lane; t < T; t += 32) row[t] = __fdiv_rn(__fsub_rn(row[t], m), sc);
+    if (vec) {
+      float4* rw4 = reinterpret_cast<float4*>(row);
+      for (int q = lane; q < nq; q += 32) {
+        const float4 x = rw4[q];
+        rw4[q] = make_float4(__fdiv_rn(__fsub_rn(x.x, m), sc), __fdiv_rn(__fsub_rn(x.y, m), sc),
+                             __fdiv_rn(__fsub_rn(x.z, m), sc), __fdiv_rn(__fsub_rn(x.w, m), sc));
+      }
+    } else {
+      for (int t = lane; t < T; t += 32) row[t] = __fdiv_rn(__fsub_rn(row[t], m), sc);
+    }
     if (lane == 0) a.scale[vs] = sc;
   }
   __syncthreads();
   if (K > 0) {
     const float* Q0 = a.Q0 + (a.tile_design ? (size_t)a.tile_design[blockIdx.x] * K * LT : 0);
     tile_project(Q0, LT, Ys, ld, K, Cq);
-    tile_subtract(Q0, LT, Cq, Ys, ld, K);
+    tile_subtract_any(Q0, LT, Cq, Ys, ld, K);
   }
   __syncthreads();
   if (a.feats) {
@@ -215,11 +232,15 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
       // two samples per lane: 32-bit stores of (hi_t, hi_t+1)
       uint32_t* hi = reinterpret_cast<uint32_t*>(a.yr_hi + (size_t)v * a.ld_y);
       uint32_t* lo = reinterpret_cast<uint32_t*>(a.yr_lo + (size_t)v * a.ld_y);
+      // x * 2^e as one product when 2^e is a normal float (then the same
+      // correctly rounded value as ldexpf)
+      const bool pw = e >= -126 && e <= 127;
+      const float p2 = pw ? __int_as_float((e + 127) << 23) : 0.f;
       for (int t2 = lane; t2 < (a.ld_y >> 1); t2 += 32) {
         uint16_t h0 = 0, l0 = 0, h1 = 0, l1 = 0;
         const int t = 2 * t2;
-        if (t < T) split_fp16(ldexpf(row[t], e), h0, l0);
-        if (t + 1 < T) split_fp16(ldexpf(row[t + 1], e), h1, l1);
+        if (t < T) split_fp16(pw ? __fmul_rn(row[t], p2) : ldexpf(row[t], e), h0, l0);
+        if (t + 1 < T) split_fp16(pw ? __fmul_rn(row[t + 1], p2) : ldexpf(row[t + 1], e), h1, l1);
         hi[t2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
         lo[t2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
       }

@@ -1,7 +1,8 @@
 // Tiles of 32 voxel series in shared memory, worked on by a CTA of 8 warps:
 // the K x T products of the residualisation (prep) and of the GLS refit run
-// as register-blocked passes over the tile instead of one warp reduction per
-// design column.
+// as register-blocked passes over the tile (projections) and as warp-level
+// tensor-core MMAs (updates, tile_subtract_any) instead of one warp reduction
+// per design column.
 //
 // Layout: Ys[l][t] (l < 32 voxels, row stride tile_ld(T)), zero for t >= T;
 // K x T matrices stay in global memory (row stride lm = ld_t(T), a multiple
@@ -189,6 +190,126 @@ __device__ __forceinline__ void tile_subtract(const float* __restrict__ N, int l
       for (int i = 0; i < TILE_SUB_VB; ++i) r4[(size_t)i * ld4 + q] = r[i];
     }
   }
+}
+
+// ------------------------------------------------------------ tensor-core forms
+// The update on the tensor cores, as warp-level tf32 MMAs (m16n8k8, fp32
+// accumulation) of hi/lo splits: x = hi + lo with hi = tf32(x) and
+// lo = tf32(x - hi) (about 22 significant bits, fp32's exponent range, so no
+// per-row scaling), each product formed as hi*hi + (lo*hi + hi*lo) (the lo*lo
+// term is below fp32 rounding). A tile of 32 voxels is two 16-row MMA tiles;
+// time is the MMA's n. The update wins here because every output element is
+// written once with its series value as the accumulator; the projection onto
+// K columns reduces over time instead, and stays on the CUDA cores
+// (tile_project), whose wide loads hide the latency of the matrix reads. Fragment layouts of mma.m16n8k8 with .tf32 operands, lane = 4 g + q:
+// A (16 x 8, row-major): a0 (g, q), a1 (g + 8, q), a2 (g, q + 4), a3 (g + 8, q + 4);
+// B (8 x 8, column-major): b0 (q, g), b1 (q + 4, g);
+// C/D (16 x 8, fp32): c0 (g, 2q), c1 (g, 2q + 1), c2 (g + 8, 2q), c3 (g + 8, 2q + 1).
+
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+  const float r = __fsub_rn(x, __uint_as_float(hi));
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// d += a_hi b_hi and e += a_lo b_hi + a_hi b_lo (a and b as hi/lo splits):
+// two accumulators, so the three products form two short dependency chains
+__device__ __forceinline__ void mma_tf32x3(float (&d)[4], float (&e)[4], const uint32_t (&ah)[4],
+                                           const uint32_t (&al)[4], const uint32_t (&bh)[2], const uint32_t (&bl)[2]) {
+  mma_tf32(e, al[0], al[1], al[2], al[3], bh[0], bh[1]);
+  mma_tf32(d, ah[0], ah[1], ah[2], ah[3], bh[0], bh[1]);
+  mma_tf32(e, ah[0], ah[1], ah[2], ah[3], bl[0], bl[1]);
+}
+
+// Ys[l][t] -= sum_j N[j][t] C[j][l] (N has row stride lm, C is [K][32]) on
+// the tensor cores, for K <= 8 * KS: warp w updates the 16 rows of m tile
+// (w & 1) at the n tiles of 8 samples i = (w >> 1) + 4u, t < lm, each output
+// element once (the series value enters as the accumulator of the hi*hi
+// products, the cross terms are summed apart and added last). Starts
+// with a barrier (other warps may still read the rows); no barrier at the end.
+template <int KS>
+__device__ __forceinline__ void tile_subtract_tc(const float* __restrict__ N, int lm, const float* C, float* Ys,
+                                                 int ld, int K) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  const int mt = w & 1, np = w >> 1;
+  const int r0 = 16 * mt + g, r1 = r0 + 8;
+  // A = -C' (rows: voxels, k: design columns), split once
+  uint32_t ah[KS][4], al[KS][4];
+#pragma unroll
+  for (int k = 0; k < KS; ++k) {
+    const int ja = 8 * k + q, jb = ja + 4;
+    split_tf32(ja < K ? -C[(size_t)ja * TILE_V + r0] : 0.f, ah[k][0], al[k][0]);
+    split_tf32(ja < K ? -C[(size_t)ja * TILE_V + r1] : 0.f, ah[k][1], al[k][1]);
+    split_tf32(jb < K ? -C[(size_t)jb * TILE_V + r0] : 0.f, ah[k][2], al[k][2]);
+    split_tf32(jb < K ? -C[(size_t)jb * TILE_V + r1] : 0.f, ah[k][3], al[k][3]);
+  }
+  __syncthreads();
+  float* y0 = Ys + (size_t)r0 * ld;
+  float* y1 = Ys + (size_t)r1 * ld;
+  const int S = (lm + 7) >> 3;
+  for (int i0 = np; i0 < S; i0 += 8) {  // n tiles i0 and i0 + 4
+    float d[2][4], e[2][4];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int t = 8 * (i0 + 4 * u) + 2 * q;  // this lane's two columns of the n tile
+      d[u][0] = d[u][1] = d[u][2] = d[u][3] = 0.f;
+      e[u][0] = e[u][1] = e[u][2] = e[u][3] = 0.f;
+      if (t < lm) {  // lm % 4 == 0: t and t + 1 both in or both out
+        const float2 a = *reinterpret_cast<const float2*>(y0 + t);
+        const float2 b = *reinterpret_cast<const float2*>(y1 + t);
+        d[u][0] = a.x;
+        d[u][1] = a.y;
+        d[u][2] = b.x;
+        d[u][3] = b.y;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < KS; ++k) {
+      const int ja = 8 * k + q, jb = ja + 4;
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int tb = 8 * (i0 + 4 * u) + g;  // the B column this lane feeds
+        uint32_t bh[2], bl[2];
+        split_tf32((ja < K && tb < lm) ? __ldg(N + (size_t)ja * lm + tb) : 0.f, bh[0], bl[0]);
+        split_tf32((jb < K && tb < lm) ? __ldg(N + (size_t)jb * lm + tb) : 0.f, bh[1], bl[1]);
+        mma_tf32x3(d[u], e[u], ah[k], al[k], bh, bl);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int t = 8 * (i0 + 4 * u) + 2 * q;
+      if (t < lm) {
+        *reinterpret_cast<float2*>(y0 + t) = make_float2(d[u][0] + e[u][0], d[u][1] + e[u][1]);
+        *reinterpret_cast<float2*>(y1 + t) = make_float2(d[u][2] + e[u][2], d[u][3] + e[u][3]);
+      }
+    }
+  }
+}
+
+// Ys -= (N C)' with the tensor cores for K <= 32 and the register-blocked
+// CUDA-core pass otherwise. Starts with a barrier and ends with one.
+__device__ __forceinline__ void tile_subtract_any(const float* __restrict__ N, int lm, const float* C, float* Ys,
+                                                  int ld, int K) {
+  switch ((K + 7) >> 3) {
+    case 1: tile_subtract_tc<1>(N, lm, C, Ys, ld, K); break;
+    case 2: tile_subtract_tc<2>(N, lm, C, Ys, ld, K); break;
+    case 3: tile_subtract_tc<3>(N, lm, C, Ys, ld, K); break;
+    case 4: tile_subtract_tc<4>(N, lm, C, Ys, ld, K); break;
+    default:
+      __syncthreads();
+      tile_subtract(N, lm, C, Ys, ld, K);
+      break;
+  }
+  __syncthreads();
 }
 
 }  // namespace ffsk
