@@ -84,6 +84,7 @@ class PrepArgs(C.Structure):
         ("yr_hi", C.c_void_p), ("yr_lo", C.c_void_p), ("yexp", C.c_void_p),
         ("idx", C.c_void_p), ("feats", C.c_void_p), ("n_runs", C.c_int), ("run_start", C.c_void_p),
         ("yr_rows", C.c_void_p), ("center_dev", C.c_void_p), ("tile_design", C.c_void_p),
+        ("Y_ref", C.c_void_p), ("Y_copy", C.c_void_p),
     ]
 
 
@@ -178,6 +179,7 @@ SIGNATURES = {
                          C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p, C.c_void_p], C.c_int),
+    "ffs_device_view": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
     "ffs_reml_strip": ([C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                         C.c_void_p], C.c_int),

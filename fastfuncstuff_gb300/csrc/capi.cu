@@ -43,3 +43,23 @@ extern "C" const char* ffs_status_string(int status) {
 }
 
 extern "C" const char* ffs_last_error(void) { return ffsk::g_err; }
+
+extern "C" int ffs_device_view(const void* host_ptr, const void** dev_ptr) {
+  ffsk::clear_error();
+  FFS_REQUIRE(host_ptr && dev_ptr, "ffs_device_view: null argument");
+  cudaPointerAttributes at;
+  const cudaError_t e = cudaPointerGetAttributes(&at, host_ptr);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // the failed query leaves no error for later launch checks
+    ffsk::set_error("ffs_device_view: cudaPointerGetAttributes: %s", cudaGetErrorString(e));
+    return FFS_ERR_INVALID;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+    *dev_ptr = at.devicePointer ? at.devicePointer : host_ptr;
+    return FFS_OK;
+  }
+  FFS_REQUIRE(at.type == cudaMemoryTypeHost && at.devicePointer,
+              "ffs_device_view: %p is not pinned host memory mapped into the device's address space", host_ptr);
+  *dev_ptr = at.devicePointer;
+  return FFS_OK;
+}

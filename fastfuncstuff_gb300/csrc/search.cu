@@ -160,7 +160,26 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
     src_row[i] = i >= nv ? -1 : (a.idx ? a.idx[v0 + i] : v0 + i);
   }
   __syncthreads();
-  tile_stage_rows(a.Y, T, nq, src_row, Ys, ld);
+  if (a.Y_ref) {
+    // the input through its address on the device (pinned host memory mapped
+    // into the device's address space, or device memory): plain 16-byte loads,
+    // a warp per row, and the rows as read written out for the later stages
+    const float* Yin = *a.Y_ref;
+    for (int i = wid; i < TILE_V; i += TILE_WARPS) {
+      float4* dst = reinterpret_cast<float4*>(Ys + (size_t)i * ld);
+      const int v = src_row[i];
+      const float4* src = reinterpret_cast<const float4*>(Yin + (size_t)(v < 0 ? 0 : v) * T);
+      float4* cpy = (a.Y_copy && v >= 0) ? reinterpret_cast<float4*>(a.Y_copy + (size_t)v * T) : nullptr;
+      for (int q = lane; q < nq; q += 32) {
+        const float4 x = v >= 0 ? src[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+        dst[q] = x;
+        if (cpy) cpy[q] = x;
+      }
+    }
+    __syncthreads();
+  } else {
+    tile_stage_rows(a.Y, T, nq, src_row, Ys, ld);
+  }
   for (int i = wid; i < nv; i += TILE_WARPS) {
     const int vs = src_row[i];
     if (vs < 0) continue;  // warp-uniform: an empty (padding) row stays zero
@@ -658,13 +677,16 @@ using namespace ffsk;
 extern "C" int ffs_reml_prep(const ffs_prep_args* a, void* stream) {
   clear_error();
   FFS_REQUIRE(a && a->V > 0 && a->T > 1 && a->K >= 0, "ffs_reml_prep: bad sizes");
-  FFS_REQUIRE(a->Y && a->scale && (a->K == 0 || a->Q0), "ffs_reml_prep: null buffer");
+  FFS_REQUIRE((a->Y || a->Y_ref) && a->scale && (a->K == 0 || a->Q0), "ffs_reml_prep: null buffer");
+  FFS_REQUIRE((!a->Y_ref && !a->Y_copy) || (a->T % 4 == 0 && !a->idx && !a->tile_design && a->Y_ref),
+              "ffs_reml_prep: Y_ref / Y_copy need T %% 4 == 0, no idx and no tile_design (T=%d)", a->T);
   FFS_REQUIRE(!a->feats || (a->n_runs > 0 && a->run_start), "ffs_reml_prep: features need the run layout");
   FFS_REQUIRE(!a->yr_hi || (a->yr_lo && a->yexp && a->ld_y >= a->T && a->ld_y % 8 == 0),
               "ffs_reml_prep: ld_y=%d must be >= T and a multiple of 8", a->ld_y);
   {
     const int ld = tile_ld(a->T);
     const size_t smem = sizeof(float) * ((size_t)TILE_V * ld + (size_t)a->K * TILE_V);
+    FFS_REQUIRE(smem <= 200 * 1024 || !a->Y_ref, "ffs_reml_prep: Y_ref needs the tiled prep (T=%d too long)", a->T);
     if (smem <= 200 * 1024) {
       FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(prep_tile_kernel), smem));
       prep_tile_kernel<<<ceil_div(a->V, TILE_V), TILE_WARPS * 32, smem, (cudaStream_t)stream>>>(*a, ld);

@@ -494,6 +494,20 @@ class PrepOut:
 BASIS_MAX_K = 32
 
 
+def device_view(t: torch.Tensor) -> int | None:
+    """The device address of t's data -- device memory, or pinned host
+    memory mapped into the device's address space -- or None when kernels may
+    not read it in place (pageable host memory)."""
+    if t.is_cuda:
+        return t.data_ptr()
+    if not t.is_pinned():
+        return None
+    out = C.c_void_p()
+    if _lib.load().ffs_device_view(C.c_void_p(t.data_ptr()), C.byref(out)) != _lib.FFS_OK:
+        return None
+    return out.value
+
+
 def design_basis(X: torch.Tensor, with_constant: bool = False):
     """Q0 [K][ld_t(T)]: the orthonormal basis of the design's columns (FP64 Cholesky),
     from X alone, so the residualisation need not wait for the grid build.
@@ -518,7 +532,7 @@ def design_basis(X: torch.Tensor, with_constant: bool = False):
 def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core: bool = True,
          idx: torch.Tensor | None = None, want_yr_t: bool = True, layout: RunLayout | None = None,
          scale: torch.Tensor | None = None, want_rows: bool = False, q0: torch.Tensor | None = None,
-         split: bool = True) -> PrepOut:
+         split: bool = True, y_ref: torch.Tensor | None = None, y_copy: torch.Tensor | None = None) -> PrepOut:
     """Per-voxel scaling and residualisation (and the fp16 split for the GEMM).
 
     With ``tensor_core`` and ``split=False`` only the split's exponents
@@ -531,13 +545,19 @@ def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core:
     autocorrelation features of the residualised rows are returned in
     ``PrepOut.feats``; ``want_rows`` adds the residualised rows voxel-major
     (``PrepOut.rows``).
+
+    ``y_ref`` (int64 [1] on the device) holds the address the rows are read
+    from instead of Y's -- device memory or pinned host memory mapped into
+    the device's address space (``device_view``) -- and ``y_copy`` ([V][T])
+    receives the rows as read; Y then only gives the shape.
     """
     lib = _lib.load()
     dev = Y.device
     V, T = Y.shape
     n = V if idx is None else idx.numel()
     K, ld = f.K, f.ld
-    Y = Y.to(dtype=torch.float32).contiguous()
+    if y_ref is None:
+        Y = Y.to(dtype=torch.float32).contiguous()
     if scale is None:
         scale = torch.empty(V, dtype=torch.float32, device=dev)
     yr_t = torch.empty(T, n, dtype=torch.float32, device=dev) if want_yr_t else None
@@ -554,7 +574,10 @@ def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core:
     pa = _lib.PrepArgs(V=n, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=0, ld_y=ld,
                        scale=_p(scale), yr_t=_p(yr_t), yr_hi=_p(yr_hi), yr_lo=_p(yr_lo), yexp=_p(yexp),
                        idx=_p(idx), feats=_p(feats), n_runs=0 if layout is None else layout.n_runs,
-                       run_start=_p(rs), yr_rows=_p(rows), center_dev=_p(f.center_flag))
+                       run_start=_p(rs), yr_rows=_p(rows), center_dev=_p(f.center_flag),
+                       Y_ref=_p(y_ref), Y_copy=_p(y_copy))
+    if y_ref is not None:
+        pa.Y = None
     _run("ffs_reml_prep", lib.ffs_reml_prep, C.byref(pa), _stream())
     out = PrepOut(scale, yr_t, yr_hi, yr_lo, yexp)
     out.feats = feats

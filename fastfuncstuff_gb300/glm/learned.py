@@ -365,7 +365,7 @@ class WindowState:
 
 def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
                     do_scale: bool = True, recenter: int = 0, q0: torch.Tensor | None = None,
-                    join=None, strip_k0: int = STRIP_K0) -> WindowState:
+                    join=None, strip_k0: int = STRIP_K0, y_ref: torch.Tensor | None = None) -> WindowState:
     """The window rounds of the learned-seeded search, with no host round trip
     (so they also run inside a CUDA graph): prep with the proposal features,
     the MLP, the 5 x 5 window of every voxel, ``recenter`` re-centred rounds
@@ -374,7 +374,8 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
     (-1: none); a voxel that a strip pair beats takes the full grid. With
     ``q0`` (engine.design_basis) the prep does not read the factors;
     ``join()`` is then called before their first use (they may be built on
-    another stream meanwhile)."""
+    another stream meanwhile). With ``y_ref`` (engine.prep) the rows are read
+    from the address it holds and written into Y as read."""
     lib = _lib.load()
     dev = Y.device
     V, T = Y.shape
@@ -385,11 +386,12 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
         raise NotImplementedError("the learned search needs T % 4 == 0 (the tiled prep)")
     g = f.grid
     st = _st()
-    Y = Y.float().contiguous()
+    if y_ref is None:
+        Y = Y.float().contiguous()
     c = _grid_consts(g, dev)
     # the windows' rows are split to fp16 while they are gathered (from rows)
     p1 = engine.prep(Y, f, do_scale=do_scale, tensor_core=True, want_yr_t=False, layout=layout, want_rows=True,
-                     q0=q0, split=False)
+                     q0=q0, split=False, y_ref=y_ref, y_copy=Y if y_ref is not None else None)
     scale = p1.scale
     prop = proposal.forward(p1.feats)
     center = torch.empty(V, dtype=torch.int32, device=dev)
@@ -512,19 +514,28 @@ class LearnedFitGraph:
     Graph B is the GLS of every voxel at its window pair. ``run`` replays A,
     records an event, replays B, waits for the event only (B keeps the GPU
     busy meanwhile), then runs the full grid and the GLS of the fallback
-    voxels eagerly. Inputs are copied into the graphs' static buffers; results
-    are returned as new tensors.
+    voxels from graph C beside B. The data are read where they lie (device
+    memory, or pinned host memory streamed by the prep) through an address
+    that each run writes on the device; the design is copied into a static
+    buffer; results are returned as new tensors.
     """
 
     def __init__(self, Y: torch.Tensor, X: torch.Tensor, grid: RemlGrid, layout: RunLayout,
                  proposal: ArmaProposal, *, recenter: int, do_scale: bool, gls_kw: dict, factor_kw: dict):
-        self.Y = Y.float().contiguous().clone()
+        dev = X.device
+        # the data's static buffer: the prep reads each run's rows from the
+        # address in y_ref (device memory, or pinned host memory read in place)
+        # and writes them here for the later stages
+        self.Y = torch.empty(tuple(Y.shape), dtype=torch.float32, device=dev)
+        self.y_ref = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.y_ref_host = torch.zeros(1, dtype=torch.int64, pin_memory=True)
+        self._set_source(Y)
         self.X = X.float().contiguous().clone()
         self.grid, self.layout, self.proposal = grid, layout, proposal
         self.recenter, self.do_scale, self.gls_kw, self.factor_kw = recenter, do_scale, gls_kw, factor_kw
         self.cflag, self.ccoef = engine.constant_flag(self.X)
         self.host = torch.empty(3 + recenter, dtype=torch.int32, pin_memory=True)
-        self.side = torch.cuda.Stream(self.Y.device)  # the grid build runs beside the prep chain
+        self.side = torch.cuda.Stream(dev)  # the grid build runs beside the prep chain
         self.side_fb = torch.cuda.Stream(self.Y.device)  # the fallback runs beside graph B
         self._fb_graphs: dict = {}
         # one eager pass fills the host-side caches (device constants, tensor
@@ -558,17 +569,32 @@ class LearnedFitGraph:
             def join():
                 main.wait_event(built)
         self.ws = learned_windows(self.Y, self.f, self.proposal, self.layout, do_scale=self.do_scale,
-                                  recenter=self.recenter, q0=q0, join=join)
+                                  recenter=self.recenter, q0=q0, join=join, y_ref=self.y_ref)
         self.host.copy_(self.ws.small, non_blocking=True)
 
     def _body_b(self):
         self.best_w = self.ws.best.clone()
         self.go = engine.gls(self.Y, self.ws.scale, self.best_w, self.f, self.X, **self.gls_kw)
 
+    def _set_source(self, Y: torch.Tensor) -> None:
+        """Point y_ref at Y's rows (float32, contiguous, 16-byte aligned; on the
+        device, or pinned host memory that the prep streams in place)."""
+        if tuple(Y.shape) != tuple(self.Y.shape) or Y.dtype != torch.float32 or not Y.is_contiguous():
+            raise ValueError("the learned fit's graph reads float32 contiguous data of its own shape")
+        addr = engine.device_view(Y)
+        if addr is None or addr % 16:
+            raise ValueError("the learned fit's graph reads device memory or pinned host memory (16-byte aligned)")
+        self.y_ref_host[0] = addr
+        self.y_ref.copy_(self.y_ref_host, non_blocking=True)
+        self._src = Y  # kept alive until the run that reads it has finished
+
     def run(self, Y: torch.Tensor, X: torch.Tensor):
-        """(LearnedOut, engine.GlsOut) of data Y (V, T) and design X (T, K)."""
+        """(LearnedOut, engine.GlsOut) of data Y (V, T) and design X (T, K).
+        Y may be a CUDA tensor or a pinned host tensor: the prep reads its rows
+        in place (over the host link for host memory) and the host-to-device
+        transfer overlaps with the grid build and the prep's work."""
         main = torch.cuda.current_stream()
-        self.Y.copy_(Y)
+        self._set_source(Y)
         self.X.copy_(X)
         if self.X.shape[1] > engine.BASIS_MAX_K:  # else graph A runs the centring test
             flag, coef = engine.constant_flag(self.X)
@@ -666,7 +692,7 @@ def graph_for(Y, X, grid, layout, proposal, *, recenter, do_scale, gls_kw, facto
     """The cached LearnedFitGraph of this shape and these options (built on first use)."""
     fk = tuple((k, None if v is None else v.key() if hasattr(v, "key") else np.asarray(v).tobytes())
                for k, v in sorted(factor_kw.items()))
-    key = (tuple(Y.shape), tuple(X.shape), str(Y.device), grid.a.tobytes(), grid.b.tobytes(), grid.lambda_fp32,
+    key = (tuple(Y.shape), tuple(X.shape), str(X.device), grid.a.tobytes(), grid.b.tobytes(), grid.lambda_fp32,
            layout.run_start.tobytes(), layout.tau.tobytes(), id(proposal.params), proposal.params._version,
            recenter, do_scale, tuple(sorted(gls_kw.items())), fk)
     gr = _GRAPHS.get(key)

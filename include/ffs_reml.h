@@ -177,6 +177,13 @@ size_t ffs_design_basis_work_bytes(int T, int K);
 int ffs_design_basis(int T, int K, const float* X, void* work, float* Q0, int* info, int* const_flag,
                      float* const_coef, void* stream);
 
+/* The device address of host_ptr: pinned host memory mapped into the device's
+ * address space (cudaHostAlloc / cudaHostRegister), or device memory (returned
+ * as it is). FFS_ERR_INVALID for pageable or unregistered host memory, which
+ * kernels must not read (no reference counterpart: the reference copies its
+ * batches to the device). */
+int ffs_device_view(const void* host_ptr, const void** dev_ptr);
+
 /* ---------------------------------------------------------------- search data
  * Replaces the per-voxel scaling of fastfuncstuff/glm/arma.py:3952-3954,
  * 4685-4686 and _residualize_reml_search_data (arma.py:1554-1571).
@@ -222,6 +229,18 @@ typedef struct {
    * tile_design[v / 32]; idx[i] < 0 marks an empty (padding) output row,
    * whose outputs are zero and which writes no scale. */
   const int* tile_design;
+  /* End-to-end input without a staging copy (no reference counterpart; the
+   * tiled prep only, T % 4 == 0, idx == NULL, no tile_design):
+   * Y_ref  NULL, or a device pointer to the input's address: the rows are read
+   *        from *Y_ref instead of Y (Y is then ignored; it may be NULL). The
+   *        address may be device memory or pinned host memory mapped into the
+   *        device's address space (ffs_device_view), which the kernel then
+   *        streams over the host link while it works. Being read on the
+   *        device, the address can change between replays of a captured launch.
+   * Y_copy NULL, or [V][T]: the input rows as read, written out (the later
+   *        stages then read device memory). */
+  const float* const* Y_ref;
+  float* Y_copy;
 } ffs_prep_args;
 
 int ffs_reml_prep(const ffs_prep_args* a, void* stream);

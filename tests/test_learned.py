@@ -356,6 +356,11 @@ def test_fit_with_proposal_matches_full_grid_fit_where_pairs_agree(cuda_graphs):
     got = fit_glm_arma11(Y, X, proposal=prop, proposal_recenter=1, cuda_graphs=cuda_graphs, **kw)
     again = fit_glm_arma11(Y, X, proposal=prop, proposal_recenter=1, cuda_graphs=cuda_graphs, **kw)
     assert torch.equal(got.betas, again.betas)  # a replay gives the same results
+    # pinned host data: with graphs the prep streams the rows in place
+    host = fit_glm_arma11(Y.cpu().pin_memory(), X, proposal=prop, proposal_recenter=1, cuda_graphs=cuda_graphs,
+                          **kw)
+    for name in ("betas", "tstats", "sigma2", "arma_params", "reml_likelihood", "residuals"):
+        assert torch.equal(getattr(host, name), getattr(got, name)), name
     same = (got.arma_params == full.arma_params).all(1)
     assert float(same.float().mean()) >= 0.995  # a briefly trained network
     assert 0.0 < float(got.learned_fallback) < 0.5  # some voxels took the fallback path
