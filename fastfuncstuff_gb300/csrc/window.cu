@@ -134,6 +134,7 @@ constexpr int CRIT_TB = 16;  // steps per partial sum and sample prefetch
 // sum by 1/D once; each row keeps its own steady flags, so a pair's
 // arithmetic does not depend on the other rows. y'y is summed on the way.
 constexpr int WCH = 64;  // steps per staged chunk (a multiple of CRIT_TB)
+constexpr int WCP = (WIN + 1) / 2;  // pair couples of a window row
 constexpr int WCB = WCH / CRIT_TB;
 
 __host__ __device__ inline size_t crit_smem_bytes() {
@@ -141,7 +142,7 @@ __host__ __device__ inline size_t crit_smem_bytes() {
          2 * sizeof(float) * WIN * WIN * WTILE + WIN * WCH + WIN * WCB;
 }
 
-__global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const int2* tiles, const int* n_tiles) {
+__global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const int2* tiles, const int* n_tiles) {
   extern __shared__ float2 tab[];  // [WIN rows][WIN pairs][WCH + 1]: steps c0 - 1 .. c0 + WCH - 1
   float* cs = reinterpret_cast<float*>(tab + WIN * WIN * (WCH + 1));  // [WIN][WCH + 1] AR filter c_t
   float* svv = cs + WIN * (WCH + 1);                                   // [WIN * WIN][WTILE] v_{t-1}
@@ -197,6 +198,26 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
 
   float yy = 0.f;  // y'y in the full grid's blocks (the identity chunk of the surface kernel)
   float yp = 0.f;
+  // 16 samples of this thread's series from t0 (zero past T); each block's
+  // samples are requested one block ahead, so the loads overlap the work
+  auto load_block = [&](float (&dst)[CRIT_TB], int t0) {
+    if (vec) {
+#pragma unroll
+      for (int k = 0; k < CRIT_TB; k += 4) {
+        const float4 q = t0 + k < T ? *reinterpret_cast<const float4*>(yrow + t0 + k)
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+        dst[k] = q.x;
+        dst[k + 1] = q.y;
+        dst[k + 2] = q.z;
+        dst[k + 3] = q.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < CRIT_TB; ++k) dst[k] = (t0 + k < T) ? yrow[t0 + k] : 0.f;
+    }
+  };
+  float yb[CRIT_TB];
+  load_block(yb, 0);
   for (int c0 = 0; c0 < T; c0 += WCH) {
     const int cn = min(WCH, T - c0);
     __syncthreads();  // the previous chunk's tables are no longer read
@@ -239,21 +260,8 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
     __syncthreads();
     for (int bs = 0; bs < cn; bs += CRIT_TB) {
       const int t0 = c0 + bs;
-      float yb[CRIT_TB];
-      if (vec) {
-#pragma unroll
-        for (int k = 0; k < CRIT_TB; k += 4) {
-          const float4 q = t0 + k < T ? *reinterpret_cast<const float4*>(yrow + t0 + k)
-                                      : make_float4(0.f, 0.f, 0.f, 0.f);
-          yb[k] = q.x;
-          yb[k + 1] = q.y;
-          yb[k + 2] = q.z;
-          yb[k + 3] = q.w;
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yrow[t0 + k] : 0.f;
-      }
+      float yn[CRIT_TB];
+      load_block(yn, t0 + CRIT_TB);
       {
         float yy_b = 0.f;
 #pragma unroll
@@ -265,19 +273,23 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
         if (npr == 0) continue;  // uniform over the CTA
         const float2* tr = tab + (size_t)r * WIN * (WCH + 1);
         const float* crr = cs + (size_t)r * (WCH + 1);
-        float vv[WIN], st[WIN], sq[WIN], nm[WIN], id[WIN];
+        // the row's pairs as couples (2c, 2c + 1) in 64-bit registers, advanced
+        // with packed f32x2 instructions (two fmaf each, so the same values)
+        uint64_t vv[WCP], st[WCP], sq[WCP], nm[WCP], id[WCP];
         // the coefficients at the block's first step: the table's value there
         // equals what a step-by-step walk holds in its registers
         float cc = crr[bs + 1];
 #pragma unroll
-        for (int g = 0; g < WIN; ++g) {
-          const bool on = g < npr;
-          vv[g] = on ? svv[(r * WIN + g) * WTILE + tid] : 0.f;
-          st[g] = on ? sst[(r * WIN + g) * WTILE + tid] : 0.f;
-          const float2 q = on ? tr[(size_t)g * (WCH + 1) + bs + 1] : make_float2(0.f, 0.f);
-          nm[g] = q.x;
-          id[g] = q.y;
-          sq[g] = 0.f;
+        for (int c = 0; c < WCP; ++c) {
+          const bool on0 = 2 * c < npr, on1 = 2 * c + 1 < npr;
+          const int e0 = (r * WIN + 2 * c) * WTILE + tid, e1 = e0 + WTILE;
+          vv[c] = pack2(on0 ? svv[e0] : 0.f, on1 ? svv[e1] : 0.f);
+          st[c] = pack2(on0 ? sst[e0] : 0.f, on1 ? sst[e1] : 0.f);
+          const float2 q0 = on0 ? tr[(size_t)(2 * c) * (WCH + 1) + bs + 1] : make_float2(0.f, 0.f);
+          const float2 q1 = on1 ? tr[(size_t)(2 * c + 1) * (WCH + 1) + bs + 1] : make_float2(0.f, 0.f);
+          nm[c] = pack2(q0.x, q1.x);
+          id[c] = pack2(q0.y, q1.y);
+          sq[c] = pack2(0.f, 0.f);
         }
         float ypr = yp;
         if (bsteady[r * WCB + bs / CRIT_TB]) {
@@ -286,14 +298,15 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
           for (int k = 0; k < CRIT_TB; ++k) {
             const float z = fmaf(-cc, ypr, yb[k]);
             ypr = yb[k];
+            const uint64_t z2 = pack2(z, z);
 #pragma unroll
-            for (int g = 0; g < WIN; ++g) {
-              vv[g] = fmaf(nm[g], vv[g], z);
-              sq[g] = fmaf(vv[g], vv[g], sq[g]);
+            for (int c = 0; c < WCP; ++c) {
+              vv[c] = fma2(nm[c], vv[c], z2);
+              sq[c] = fma2(vv[c], vv[c], sq[c]);
             }
           }
 #pragma unroll
-          for (int g = 0; g < WIN; ++g) st[g] = fmaf(sq[g], id[g], st[g]);
+          for (int c = 0; c < WCP; ++c) st[c] = fma2(sq[c], id[c], st[c]);
         } else {
           const uint8_t* sr = steady + r * WCH;
 #pragma unroll
@@ -302,35 +315,46 @@ __global__ void __launch_bounds__(WTILE) window_crit_kernel(CritArgs w, const in
               if (!sr[bs + k]) {
                 cc = crr[bs + k + 1];
 #pragma unroll
-                for (int g = 0; g < WIN; ++g) {
-                  if (g < npr) {
-                    const float2 q = tr[(size_t)g * (WCH + 1) + bs + k + 1];
-                    nm[g] = q.x;
-                    id[g] = q.y;
-                  }
+                for (int c = 0; c < WCP; ++c) {
+                  const bool on0 = 2 * c < npr, on1 = 2 * c + 1 < npr;
+                  const float2 q0 = on0 ? tr[(size_t)(2 * c) * (WCH + 1) + bs + k + 1] : make_float2(0.f, 0.f);
+                  const float2 q1 = on1 ? tr[(size_t)(2 * c + 1) * (WCH + 1) + bs + k + 1] : make_float2(0.f, 0.f);
+                  nm[c] = pack2(q0.x, q1.x);
+                  id[c] = pack2(q0.y, q1.y);
                 }
               }
               const float z = fmaf(-cc, ypr, yb[k]);
               ypr = yb[k];
+              const uint64_t z2 = pack2(z, z);
 #pragma unroll
-              for (int g = 0; g < WIN; ++g) {
-                vv[g] = fmaf(nm[g], vv[g], z);
-                sq[g] = fmaf(vv[g] * id[g], vv[g], sq[g]);
+              for (int c = 0; c < WCP; ++c) {
+                vv[c] = fma2(nm[c], vv[c], z2);
+                sq[c] = fma2(mul2(vv[c], id[c]), vv[c], sq[c]);
               }
             }
           }
 #pragma unroll
-          for (int g = 0; g < WIN; ++g) st[g] += sq[g];
+          for (int c = 0; c < WCP; ++c) st[c] = add2(st[c], sq[c]);
         }
 #pragma unroll
-        for (int g = 0; g < WIN; ++g) {
-          if (g < npr) {
-            svv[(r * WIN + g) * WTILE + tid] = vv[g];
-            sst[(r * WIN + g) * WTILE + tid] = st[g];
+        for (int c = 0; c < WCP; ++c) {
+          float v0, v1, s0, s1;
+          unpack2(vv[c], v0, v1);
+          unpack2(st[c], s0, s1);
+          const int e0 = (r * WIN + 2 * c) * WTILE + tid, e1 = e0 + WTILE;
+          if (2 * c < npr) {
+            svv[e0] = v0;
+            sst[e0] = s0;
+          }
+          if (2 * c + 1 < npr) {
+            svv[e1] = v1;
+            sst[e1] = s1;
           }
         }
       }
       yp = yb[CRIT_TB - 1];
+#pragma unroll
+      for (int k = 0; k < CRIT_TB; ++k) yb[k] = yn[k];
     }
   }
 
@@ -445,6 +469,25 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
 #pragma unroll
   for (int j = 0; j < STRIP_G2; ++j) vv[j] = st[j] = zero2;
   float yy = 0.f, yp = 0.f;
+  // 16 samples from t0 (zero past T), requested one block ahead
+  auto load_block = [&](float (&dst)[CRIT_TB], int t0) {
+    if (vec) {
+#pragma unroll
+      for (int k = 0; k < CRIT_TB; k += 4) {
+        const float4 q4 = t0 + k < T ? *reinterpret_cast<const float4*>(yrow + t0 + k)
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+        dst[k] = q4.x;
+        dst[k + 1] = q4.y;
+        dst[k + 2] = q4.z;
+        dst[k + 3] = q4.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < CRIT_TB; ++k) dst[k] = (t0 + k < T) ? yrow[t0 + k] : 0.f;
+    }
+  };
+  float yb[CRIT_TB];
+  load_block(yb, 0);
   for (int c0 = 0; c0 < T; c0 += WCH) {
     const int cn = min(WCH, T - c0);
     __syncthreads();  // the previous chunk's tables are no longer read
@@ -478,21 +521,8 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
     __syncthreads();
     for (int bs = 0; bs < cn; bs += CRIT_TB) {
       const int t0 = c0 + bs;
-      float yb[CRIT_TB];
-      if (vec) {
-#pragma unroll
-        for (int k = 0; k < CRIT_TB; k += 4) {
-          const float4 q4 = t0 + k < T ? *reinterpret_cast<const float4*>(yrow + t0 + k)
-                                       : make_float4(0.f, 0.f, 0.f, 0.f);
-          yb[k] = q4.x;
-          yb[k + 1] = q4.y;
-          yb[k + 2] = q4.z;
-          yb[k + 3] = q4.w;
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yrow[t0 + k] : 0.f;
-      }
+      float yn[CRIT_TB];
+      load_block(yn, t0 + CRIT_TB);
       {
         float yy_b = 0.f;
 #pragma unroll
@@ -538,6 +568,8 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
         }
       }
       yp = yb[CRIT_TB - 1];
+#pragma unroll
+      for (int k = 0; k < CRIT_TB; ++k) yb[k] = yn[k];
     }
   }
   if (!live) return;

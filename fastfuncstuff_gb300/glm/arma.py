@@ -506,11 +506,18 @@ def fit_glm_arma11(
     def cat(name):
         return torch.cat(chunks[name]) if chunks[name] else None
 
+    pending = []  # host copies queued on the stream, waited for once before returning
+
     def out(t, dtype=None):
         if t is None:
             return None
         t = t.to(dtype=dtype or out_dtype)
-        return t if return_device else t.cpu()
+        if return_device:
+            return t
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        pending.append(h)
+        return h
 
     best = cat("best").long()
     a_t = engine.const_dev(grid.a, device)
@@ -578,6 +585,8 @@ def fit_glm_arma11(
         res.voxel_mask = spatial_metadata.get("voxel_mask")
         res.full_shape = spatial_metadata.get("volume_shape")
         res.affine = spatial_metadata.get("affine")
+    if pending:
+        torch.cuda.current_stream(device).synchronize()
     if verbose:
         print(f"ARMA(1,1) REML: {V:,} voxels x {P} pairs, T={T}, K={K} on {torch.cuda.get_device_name(device)}")
     return res
