@@ -469,25 +469,6 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
 #pragma unroll
   for (int j = 0; j < STRIP_G2; ++j) vv[j] = st[j] = zero2;
   float yy = 0.f, yp = 0.f;
-  // 16 samples from t0 (zero past T), requested one block ahead
-  auto load_block = [&](float (&dst)[CRIT_TB], int t0) {
-    if (vec) {
-#pragma unroll
-      for (int k = 0; k < CRIT_TB; k += 4) {
-        const float4 q4 = t0 + k < T ? *reinterpret_cast<const float4*>(yrow + t0 + k)
-                                     : make_float4(0.f, 0.f, 0.f, 0.f);
-        dst[k] = q4.x;
-        dst[k + 1] = q4.y;
-        dst[k + 2] = q4.z;
-        dst[k + 3] = q4.w;
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < CRIT_TB; ++k) dst[k] = (t0 + k < T) ? yrow[t0 + k] : 0.f;
-    }
-  };
-  float yb[CRIT_TB];
-  load_block(yb, 0);
   for (int c0 = 0; c0 < T; c0 += WCH) {
     const int cn = min(WCH, T - c0);
     __syncthreads();  // the previous chunk's tables are no longer read
@@ -521,8 +502,21 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
     __syncthreads();
     for (int bs = 0; bs < cn; bs += CRIT_TB) {
       const int t0 = c0 + bs;
-      float yn[CRIT_TB];
-      load_block(yn, t0 + CRIT_TB);
+      float yb[CRIT_TB];
+      if (vec) {
+#pragma unroll
+        for (int k = 0; k < CRIT_TB; k += 4) {
+          const float4 q4 = t0 + k < T ? *reinterpret_cast<const float4*>(yrow + t0 + k)
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+          yb[k] = q4.x;
+          yb[k + 1] = q4.y;
+          yb[k + 2] = q4.z;
+          yb[k + 3] = q4.w;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < CRIT_TB; ++k) yb[k] = (t0 + k < T) ? yrow[t0 + k] : 0.f;
+      }
       {
         float yy_b = 0.f;
 #pragma unroll
@@ -568,8 +562,6 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
         }
       }
       yp = yb[CRIT_TB - 1];
-#pragma unroll
-      for (int k = 0; k < CRIT_TB; ++k) yb[k] = yn[k];
     }
   }
   if (!live) return;
