@@ -307,6 +307,23 @@ def learned_quality(args, w, Yd, Xd, kw, kw_l, prop, lay, g, tinfo) -> tuple[dic
         "strip_voxels": int(ls.stats["strip_voxels"].item()) if ls.stats.get("strip_voxels") is not None else 0,
         "recenter_rounds": args.recenter, "window_pair_evals_per_voxel": pair_evals / V,
     }
+    if args.transfer:
+        # a proposal trained on a family of four other designs of this
+        # workload's kind (fresh task onsets and motion), used on this design
+        from fastfuncstuff_gb300 import synth
+
+        fam = torch.from_numpy(np.stack([synth.workload1_design(sd) for sd in (101, 102, 103, 104)])).to(Yd.device)
+        prop_fam, info_fam = learned.train_proposal(fam, lay, g, g, n_voxels=args.train_voxels,
+                                                    epochs=args.train_epochs)
+        full_b = engine.search(Yd, f_all, hierarchical=False).best
+        lt = learned.learned_search(Yd, f_all, prop_fam, lay, recenter=args.recenter)
+        q["held_out_design"] = {
+            "proposal": "trained on 4 other designs of this workload's kind (synth.workload1_design seeds 101-104), "
+                        "none of them this fit's design",
+            "agreement_with_full_grid": float((lt.best == full_b).float().mean().item()),
+            "full_grid_fallback": lt.stats["fallback"],
+            "train_s": round(info_fam["label_s"] + info_fam["train_s"], 2),
+        }
     if args.fp64_voxels > 0:
         from oracle import reml as o
 
@@ -550,6 +567,8 @@ def main() -> None:
     ap.add_argument("--fp64-voxels", type=int, default=2000,
                     help="voxels of the learned fit checked against the FP64 oracle (0: skip)")
     ap.add_argument("--recenter", type=int, default=1)
+    ap.add_argument("--no-transfer", dest="transfer", action="store_false",
+                    help="skip the proposal trained on other designs (the held-out-design check)")
     ap.add_argument("--train-voxels", type=int, default=2_000_000)
     ap.add_argument("--train-epochs", type=int, default=30)
     ap.add_argument("--proposal", default=None, help="load a trained proposal (.npz) instead of training one")

@@ -669,7 +669,6 @@ __global__ void __launch_bounds__(256) gather_split_kernel(int n, const int* n_d
   }
 }
 
-// out_t[t][i] = rows[idx[i]][t]: 32 x 32 tiles through shared memory
 // out_t[t][i] = rows[idx[i]][t]: 32 rows x 64 samples per CTA through shared
 // memory (eight loads in flight per thread)
 __global__ void gather_transpose_kernel(int n, const int* n_dev, int T, const int* __restrict__ idx,

@@ -421,7 +421,8 @@ def fit_glm_arma11(
         fallbacks = []
     for v0 in range(0, V, bs):
         v1 = min(V, v0 + bs)
-        if use_graph and not Y.is_cuda and Y.dtype == torch.float32 and Y.is_pinned() and Y.is_contiguous():
+        if (use_graph and T % 4 == 0 and not Y.is_cuda and Y.dtype == torch.float32 and Y.is_pinned()
+                and Y.is_contiguous()):
             # pinned host data: the graph's prep streams the rows in place, so
             # the transfer overlaps with the grid build and the prep
             Yb = Y[v0:v1]

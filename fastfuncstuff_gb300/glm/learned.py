@@ -382,8 +382,6 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
     f = factors
     if f.U_hi is None:
         raise ValueError("the learned search needs the tensor-core operands of the factors")
-    if T % 4:
-        raise NotImplementedError("the learned search needs T % 4 == 0 (the tiled prep)")
     g = f.grid
     st = _st()
     if y_ref is None:
@@ -483,22 +481,32 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
 
 def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxels: int = 2_000_000,
                    epochs: int = 30, batch: int = 8192, lr: float = 3e-3, seed: int = 5):
-    """Train a proposal for design X on the GPU: n_voxels simulated with (a, b)
-    drawn uniformly over the valid pairs, labelled by the full-grid exhaustive
-    argmin, then Adam on the library's forward/backward kernels. Returns
-    (ArmaProposal, info) with the seconds spent."""
+    """Train a proposal on the GPU: n_voxels simulated with (a, b) drawn
+    uniformly over the valid pairs, labelled by the full-grid exhaustive
+    argmin, then Adam on the library's forward/backward kernels. X is one
+    design (T, K), or a family of designs (D, T, K) of one run layout that
+    share the voxels equally (a proposal for designs it was not trained on).
+    Returns (ArmaProposal, info) with the seconds spent."""
     from .grid import make_grid
 
     t0 = time.perf_counter()
-    f = engine.build_factors(X, make_grid(a_grid, b_grid), layout)
-    x, y = training_set(X, f, layout, n_voxels, seed=seed)
+    grid = make_grid(a_grid, b_grid)
+    Xs = X if X.ndim == 3 else X[None]
+    D = Xs.shape[0]
+    parts = []
+    for d in range(D):
+        n_d = n_voxels // D + (1 if d < n_voxels % D else 0)
+        f = engine.build_factors(Xs[d], grid, layout)
+        parts.append(training_set(Xs[d], f, layout, n_d, seed=seed + 7 * d))
+    x = torch.cat([p[0] for p in parts]) if D > 1 else parts[0][0]
+    y = torch.cat([p[1] for p in parts]) if D > 1 else parts[0][1]
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     prop, hist = train(x, y, epochs=epochs, batch=batch, lr=lr, seed=seed)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    info = {"train_voxels": n_voxels, "epochs": epochs, "label_s": t1 - t0, "train_s": t2 - t1,
-            "holdout_loss": hist[-1]["holdout_loss"]}
+    info = {"train_voxels": n_voxels, "epochs": epochs, "train_designs": D, "label_s": t1 - t0,
+            "train_s": t2 - t1, "holdout_loss": hist[-1]["holdout_loss"]}
     prop.meta.update(info)
     return prop, info
 
@@ -527,6 +535,9 @@ class LearnedFitGraph:
         # address in y_ref (device memory, or pinned host memory read in place)
         # and writes them here for the later stages
         self.Y = torch.empty(tuple(Y.shape), dtype=torch.float32, device=dev)
+        # rows read in place need 16-byte rows (T % 4 == 0); otherwise each run
+        # copies the data into the static buffer first
+        self.inplace = Y.shape[1] % 4 == 0
         self.y_ref = torch.zeros(1, dtype=torch.int64, device=dev)
         self.y_ref_host = torch.zeros(1, dtype=torch.int64, pin_memory=True)
         self._set_source(Y)
@@ -569,7 +580,8 @@ class LearnedFitGraph:
             def join():
                 main.wait_event(built)
         self.ws = learned_windows(self.Y, self.f, self.proposal, self.layout, do_scale=self.do_scale,
-                                  recenter=self.recenter, q0=q0, join=join, y_ref=self.y_ref)
+                                  recenter=self.recenter, q0=q0, join=join,
+                                  y_ref=self.y_ref if self.inplace else None)
         self.host.copy_(self.ws.small, non_blocking=True)
 
     def _body_b(self):
@@ -581,6 +593,10 @@ class LearnedFitGraph:
         device, or pinned host memory that the prep streams in place)."""
         if tuple(Y.shape) != tuple(self.Y.shape) or Y.dtype != torch.float32 or not Y.is_contiguous():
             raise ValueError("the learned fit's graph reads float32 contiguous data of its own shape")
+        if not self.inplace:
+            self.Y.copy_(Y, non_blocking=True)
+            self._src = Y
+            return
         addr = engine.device_view(Y)
         if addr is None or addr % 16:
             raise ValueError("the learned fit's graph reads device memory or pinned host memory (16-byte aligned)")

@@ -119,6 +119,20 @@ def _smooth_maps(rng, shape, n_keep, lo_hi_list, sigma=2.0):
     return maps, mask_idx
 
 
+def workload1_design(seed: int) -> np.ndarray:
+    """A fresh design of the 200k-voxel workload's kind, (400, 20) float32:
+    2 runs x 200 TRs, 4 task regressors (20-30 random 1 s events each,
+    double-gamma HRF), a Legendre 0-4 drift per run and 6 motion random walks
+    (step sigma 0.05), from its own seeded generator (a family of such designs
+    trains a proposal that serves designs it has not seen)."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    hrf = double_gamma_hrf()
+    n, lens = 400, [200, 200]
+    task = [event_regressor(n, _random_onsets(rng, n, rng.integers(20, 31)), hrf) for _ in range(4)]
+    motion = np.cumsum(rng.normal(0.0, 0.05, (n, 6)), axis=0)
+    return np.column_stack(task + [block_drift(lens, 4), motion]).astype(np.float32)
+
+
 @dataclass
 class Workload:
     X: np.ndarray                # (T, K) float32 design (one group) or None

@@ -367,3 +367,72 @@ def test_fit_with_proposal_matches_full_grid_fit_where_pairs_agree(cuda_graphs):
     for name in ("betas", "tstats", "sigma2", "fstats", "r2", "arma_lambda", "residuals", "residuals_whitened"):
         a, b = getattr(got, name)[same], getattr(full, name)[same]
         assert torch.equal(a, b), name
+
+
+@pytest.mark.gpu
+def test_proposal_trained_on_a_design_family_serves_a_held_out_design():
+    """A proposal trained on a family of four workload-1-like designs (fresh
+    task onsets and motion) serves a fifth design it never saw: on held-out
+    voxels of that design the whole search agrees with the exhaustive full
+    grid on >= 99.9% of voxels, and it sends at most a little more to the
+    full-grid fallback than a proposal trained on the held-out design itself."""
+    from fastfuncstuff_gb300 import synth
+    from fastfuncstuff_gb300.glm import engine, learned
+    from fastfuncstuff_gb300.glm import grid as G
+
+    dev = torch.device("cuda:0")
+    gr = torch.linspace(-0.8, 0.8, 33)
+    lay = G.run_layout(400, [0, 200])
+    family = torch.from_numpy(np.stack([synth.workload1_design(s) for s in (101, 102, 103, 104)])).to(dev)
+    held = torch.from_numpy(synth.workload1_design(200)).to(dev)
+    prop_fam, info = learned.train_proposal(family, lay, gr, gr)
+    assert info["train_designs"] == 4
+    prop_own, _ = learned.train_proposal(held, lay, gr, gr)
+    f = engine.build_factors(held, G.make_grid(gr, gr), lay)
+    gen = torch.Generator().manual_seed(21)
+    a_w = (0.1 + 0.7 * torch.rand(100_000, generator=gen)).to(dev)
+    b_w = (-0.5 + 0.8 * torch.rand(100_000, generator=gen)).to(dev)
+    Y = learned.simulate(held, lay, a_w, b_w, seed=31)
+    full = engine.search(Y, f, hierarchical=False)
+    res = {}
+    for name, prop in (("family", prop_fam), ("own", prop_own)):
+        lo = learned.learned_search(Y, f, prop, lay, recenter=1)
+        res[name] = ((lo.best == full.best).float().mean().item(), lo.stats["fallback"])
+    print(f"held-out design: family-trained agreement {res['family'][0]:.5f}, fallback {res['family'][1]:.4f}; "
+          f"own-design agreement {res['own'][0]:.5f}, fallback {res['own'][1]:.4f}")
+    assert res["family"][0] >= 0.999
+    assert res["family"][1] <= 1.5 * res["own"][1] + 0.005
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cuda_graphs", [True, False])
+def test_learned_fit_with_t_not_a_multiple_of_four(cuda_graphs):
+    """T = 398 (two runs of 199): the learned path needs no 16-byte rows (the
+    window, strip and gather kernels take their per-sample paths, the graph
+    copies the data into its buffer instead of reading it in place); where the
+    pair agrees with the full-grid fit the GLS outputs are identical."""
+    from fastfuncstuff_gb300 import fit_glm_arma11, synth
+    from fastfuncstuff_gb300.glm import learned
+    from fastfuncstuff_gb300.glm import grid as G
+
+    dev = torch.device("cuda:0")
+    w = synth.workload(1, V=5000)
+    keep = np.ones(400, bool)
+    keep[[199, 399]] = False
+    Yn, Xn = np.ascontiguousarray(w.Y[:, keep]), np.ascontiguousarray(w.X[keep])
+    lay = G.run_layout(398, [0, 199])
+    X = torch.from_numpy(Xn).to(dev)
+    Y = torch.from_numpy(Yn).to(dev)
+    gr = torch.linspace(-0.8, 0.8, 33)
+    prop, _ = learned.train_proposal(X, lay, gr, gr, n_voxels=300_000, epochs=6)
+    kw = dict(tr=2.0, a_grid=gr, b_grid=gr, run_starts=[0, 199], device=dev, verbose=False,
+              force_exhaustive_search=True, return_device=True)
+    full = fit_glm_arma11(Y, X, **kw)
+    got = fit_glm_arma11(Y, X, proposal=prop, proposal_recenter=1, cuda_graphs=cuda_graphs, **kw)
+    host = fit_glm_arma11(Y.cpu().pin_memory(), X, proposal=prop, proposal_recenter=1, cuda_graphs=cuda_graphs,
+                          **kw)
+    assert torch.equal(host.betas, got.betas)
+    same = (got.arma_params == full.arma_params).all(1)
+    assert float(same.float().mean()) >= 0.99
+    for name in ("betas", "tstats", "sigma2", "r2"):
+        assert torch.equal(getattr(got, name)[same], getattr(full, name)[same]), name
