@@ -275,7 +275,8 @@ def fit_glm_arma11(
     ``learned.ArmaProposal``: search each voxel's 5 x 5 window around its
     proposal, the full grid for window-edge voxels) and ``proposal_recenter``
     (re-centred window rounds before that fallback), ``cuda_graphs`` (replay
-    the learned-seeded fit of one voxel batch from CUDA graphs).
+    the learned-seeded fit of one voxel batch, and the grouped fit of
+    fit_glm_arma11_grouped, from CUDA graphs).
     """
     if want_ols or want_ols_residuals or want_ols_predicted or ols_write_callback is not None:
         _unsupported("the OLS side fit (want_ols)")
@@ -377,15 +378,25 @@ def fit_glm_arma11(
     afull = Dd is not None and bool(column_sets)
     q0 = join = None
     slots = None
+    gplan = None
     if _group_designs is not None:
         # grouped fit (fit_glm_arma11_grouped): every design's factors in one
         # grid build, every voxel against its own design in one pass per stage
         Xs, gid = _group_designs
-        factors = engine.build_factors(Xs, grid, layout, task_indices=ti, glt=glt, with_tc=True, sets=sets,
-                                       afull=afull)
-        slots = engine.design_slots(gid, Xs.shape[0], K, P, device)
         bs = V
-    if factors is None and not use_graph:
+        if cuda_graphs and lj is None and Dd is None and sets is None and not save_profile_likelihoods:
+            # the whole grouped fit replayed from one CUDA graph
+            gplan = engine.grouped_graph_for(Y, Xs, grid, layout, gid, hierarchical=not force_exhaustive_search,
+                                             do_scale=not use_double,
+                                             gls_kw=dict(want_residuals=want_residuals,
+                                                         want_predicted=want_predicted),
+                                             factor_kw=dict(task_indices=ti, glt=glt, with_tc=True))
+            slots = gplan.slots
+        else:
+            factors = engine.build_factors(Xs, grid, layout, task_indices=ti, glt=glt, with_tc=True, sets=sets,
+                                           afull=afull)
+            slots = engine.design_slots(gid, Xs.shape[0], K, P, device)
+    if factors is None and not use_graph and gplan is None:
         # the grid build runs on a side stream while the residualisation of the
         # first batch (against the design basis) runs on the main one
         overlap = K <= engine.BASIS_MAX_K
@@ -465,6 +476,12 @@ def fit_glm_arma11(
                     t_all, t_sub = getattr(go, fld), getattr(gs, fld)
                     if t_all is not None:
                         t_all.index_copy_(0, sel, t_sub)
+        elif gplan is not None:
+            so, go = gplan.run(Yb, _group_designs[0])
+            factors_used = gplan.f
+            best, scale = so.best, so.scale
+            chunks["best"].append(best)
+            chunks["crit"].append(so.best_crit)
         elif slots is not None:
             so = engine.search_designs(Yb, factors, slots, hierarchical=not force_exhaustive_search,
                                        do_scale=not use_double)

@@ -972,3 +972,69 @@ def dsort_prepare(dsort, V: int, T: int, run_bounds=None, dev=None) -> torch.Ten
                 out[:, si * n_runs + r, rb[r]:rb[r + 1]] = Dt[:, si, rb[r]:rb[r + 1]]
         Dt = out
     return Dt.contiguous()
+
+
+class GroupedFitGraph:
+    """The grouped full-grid fit of one shape (one design per voxel group) as
+    one CUDA graph: the FP64 grid build of every design, the residualisation
+    of every voxel against its design, the tcgen05 projection work list, the
+    criterion, the selection and the GLS, replayed as one unit. The data and
+    the designs are copied into the graph's static buffers; the centring test
+    of the designs (torch linear algebra) runs before the replay and its
+    result is copied in too. Results are returned as new tensors."""
+
+    def __init__(self, Y: torch.Tensor, Xs: torch.Tensor, grid: RemlGrid, layout: RunLayout, slots: DesignSlots, *,
+                 hierarchical: bool, do_scale: bool, gls_kw: dict, factor_kw: dict):
+        dev = Xs.device
+        self.Y = torch.empty(tuple(Y.shape), dtype=torch.float32, device=dev)
+        self.Xs = Xs.float().contiguous().clone()
+        self.grid, self.layout, self.slots = grid, layout, slots
+        self.hierarchical, self.do_scale, self.gls_kw, self.factor_kw = hierarchical, do_scale, gls_kw, factor_kw
+        self.cflag, self.ccoef = constant_flag(self.Xs)
+        self.Y.copy_(Y, non_blocking=True)
+        self._body()  # fills the host-side caches a capture must not create
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, capture_error_mode="thread_local"):
+            self._body()
+
+    def _body(self):
+        self.f = build_factors(self.Xs, self.grid, self.layout, center=(self.cflag, self.ccoef), **self.factor_kw)
+        self.so = search_designs(self.Y, self.f, self.slots, hierarchical=self.hierarchical, do_scale=self.do_scale)
+        self.go = gls(self.Y, self.so.scale, self.so.best, self.f, self.Xs, design=self.slots.design, **self.gls_kw)
+
+    def run(self, Y: torch.Tensor, Xs: torch.Tensor):
+        """(SearchOut, GlsOut) of data Y (V, T) and designs Xs (D, T, K)."""
+        self.Y.copy_(Y, non_blocking=True)
+        if not torch.equal(Xs, self.Xs):
+            self.Xs.copy_(Xs)
+            flag, coef = constant_flag(self.Xs)
+            self.cflag.copy_(flag)
+            self.ccoef.copy_(coef)
+        self.graph.replay()
+        so = SearchOut(best=self.so.best.clone(), best_crit=self.so.best_crit.clone(), scale=self.so.scale.clone())
+        go = GlsOut(**{k: (None if v is None else v.clone()) for k, v in vars(self.go).items()
+                       if not k.startswith("_")})
+        return so, go
+
+
+_GROUPED_GRAPHS: dict = {}
+
+
+def grouped_graph_for(Y, Xs, grid, layout, gid, *, hierarchical, do_scale, gls_kw, factor_kw) -> GroupedFitGraph:
+    """The cached GroupedFitGraph of this shape, grouping and options (built on first use)."""
+    gid = np.asarray(gid, dtype=np.int32)
+    fk = tuple((k, None if v is None else v.key() if hasattr(v, "key") else np.asarray(v).tobytes())
+               for k, v in sorted(factor_kw.items()))
+    key = (tuple(Y.shape), tuple(Xs.shape), str(Xs.device), grid.a.tobytes(), grid.b.tobytes(), grid.lambda_fp32,
+           layout.run_start.tobytes(), layout.tau.tobytes(), gid.tobytes(), hierarchical, do_scale,
+           tuple(sorted(gls_kw.items())), fk)
+    gr = _GROUPED_GRAPHS.get(key)
+    if gr is None:
+        while len(_GROUPED_GRAPHS) >= 2:  # a plan holds a few GB of static buffers
+            _GROUPED_GRAPHS.pop(next(iter(_GROUPED_GRAPHS)))
+        slots = design_slots(gid, Xs.shape[0], Xs.shape[2], grid.P, Xs.device)
+        gr = GroupedFitGraph(Y, Xs, grid, layout, slots, hierarchical=hierarchical, do_scale=do_scale,
+                             gls_kw=gls_kw, factor_kw=factor_kw)
+        _GROUPED_GRAPHS[key] = gr
+    return gr

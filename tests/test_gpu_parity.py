@@ -363,6 +363,26 @@ def test_grouped_batched_fit_equals_per_group_fits(selector):
             np.testing.assert_array_equal(getattr(got, name).numpy()[m], getattr(ref, name).numpy(), err_msg=name)
 
 
+def test_grouped_fit_graph_equals_eager_fit():
+    """fit_glm_arma11_grouped replays the whole grouped fit (grid build over
+    designs x pairs, residualisation, projection work list, criterion,
+    selection, GLS) from one CUDA graph: bit-identical to the eager fit, and a
+    second replay with new data gives that data's eager results."""
+    w = synth.workload(2, V=5000)
+    keep = np.isin(w.groups, np.arange(5))
+    Y, gid = w.Y[keep], w.groups[keep]
+    designs = {h: w.designs[h] for h in range(5)}
+    kw = dict(a_grid=np.linspace(-0.8, 0.8, 17), b_grid=np.linspace(-0.8, 0.8, 17), run_starts=w.run_starts,
+              tau=w.tau, device=DEV, verbose=False, want_residuals=True, glt_labels=["t0-t1"],
+              glt_matrices=[np.eye(18)[0] - np.eye(18)[1]])
+    for data in (Y, Y[:, ::-1].copy()):  # the second call replays the graph on other data
+        eager = fit_glm_arma11_grouped(data, designs, gid, tr=2.0, cuda_graphs=False, **kw)
+        graph = fit_glm_arma11_grouped(data, designs, gid, tr=2.0, cuda_graphs=True, **kw)
+        for name in ("arma_params", "reml_likelihood", "betas", "tstats", "sigma2", "fstats", "r2", "arma_lambda",
+                     "contrast_betas", "contrast_tstats", "residuals", "residuals_whitened"):
+            np.testing.assert_array_equal(getattr(graph, name).numpy(), getattr(eager, name).numpy(), err_msg=name)
+
+
 def test_precomputed_params_path():
     d = load_golden("multirun")
     kw = case_kwargs(d)
