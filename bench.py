@@ -7,11 +7,12 @@ One step = one complete ``fit_glm_arma11`` of the 200,000-voxel workload
 (a, b) pairs): FP64 grid factors, per-voxel scaling and residualisation, the
 (a, b) search, and the GLS refit with t, F, R^2, sigma2 and lambda.
 ``value`` is the learned-seeded step (each voxel's 5 x 5 window around the
-proposal of the MLP, one re-centred round, the full grid for the voxels still
-on a window edge); ``full_grid`` is the same fit evaluating all 561 pairs
+proposal of the MLP, one re-centred round, the strip next to the identity line
+for voxels near it, the full grid for the voxels still on a window edge or
+beaten by a strip pair); ``full_grid`` is the same fit evaluating all 561 pairs
 (the reference's default hierarchical selector). The proposal is trained on
-the GPU before timing (2M voxels simulated with this design, full-grid
-labels). ``value`` keeps the data resident in HBM; ``e2e`` calls the same
+the GPU before timing (6M voxels simulated with this design, full-grid
+labels, 40 epochs). ``value`` keeps the data resident in HBM; ``e2e`` calls the same
 public API with pinned host buffers (host->device copy of the data and
 device->host copy of the results inside the timed region).
 
@@ -580,8 +581,8 @@ def main() -> None:
     ap.add_argument("--recenter", type=int, default=1)
     ap.add_argument("--no-transfer", dest="transfer", action="store_false",
                     help="skip the proposal trained on other designs (the held-out-design check)")
-    ap.add_argument("--train-voxels", type=int, default=2_000_000)
-    ap.add_argument("--train-epochs", type=int, default=30)
+    ap.add_argument("--train-voxels", type=int, default=6_000_000)
+    ap.add_argument("--train-epochs", type=int, default=40)
     ap.add_argument("--proposal", default=None, help="load a trained proposal (.npz) instead of training one")
     ap.add_argument("--save-proposal", default=None, help="save the proposal trained here (.npz)")
     ap.add_argument("--dsort", type=int, default=0,

@@ -479,8 +479,8 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
     return learned_fallback(Y, factors, ws, host, do_scale=do_scale)
 
 
-def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxels: int = 2_000_000,
-                   epochs: int = 30, batch: int = 8192, lr: float = 3e-3, seed: int = 5):
+def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxels: int = 6_000_000,
+                   epochs: int = 40, batch: int = 8192, lr: float = 3e-3, seed: int = 5):
     """Train a proposal on the GPU: n_voxels simulated with (a, b) drawn
     uniformly over the valid pairs, labelled by the full-grid exhaustive
     argmin, then Adam on the library's forward/backward kernels. X is one

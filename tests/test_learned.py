@@ -130,8 +130,8 @@ def test_learned_search_agrees_with_full_grid_and_beats_untrained():
     X = torch.from_numpy(w.X).to(dev)
     gr = torch.linspace(-0.8, 0.8, 33)
     f = engine.build_factors(X, G.make_grid(gr, gr), lay)
-    x, y = learned.training_set(X, f, lay, 2_000_000, seed=5)  # the benchmark's training size
-    prop, hist = learned.train(x, y, epochs=30, batch=8192, lr=3e-3, seed=1)
+    x, y = learned.training_set(X, f, lay, 6_000_000, seed=5)  # the benchmark's training size
+    prop, hist = learned.train(x, y, epochs=40, batch=8192, lr=3e-3, seed=1)
     # against the untrained network on the same held-out features
     out0 = learned.ArmaProposal(learned.init_params(1, dev)).forward(x[:50_000])
     loss0 = float(((out0 - y[:50_000]) ** 2).sum(1).mean().item() / 2)

@@ -42,6 +42,23 @@ def test_header_declares_the_entry_points():
     assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
 
 
+def declared_arity() -> dict[str, int]:
+    """Number of parameters of every function the header declares."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(ffs_\w+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_take_the_declared_number_of_arguments():
+    arity = declared_arity()
+    for name, (argtypes, _) in _lib.SIGNATURES.items():
+        assert name in arity, name
+        assert len(argtypes) == arity[name], (name, len(argtypes), arity[name])
+
+
 def test_library_builds_loads_and_exports_every_symbol():
     path = B.build()
     assert path.exists()
