@@ -297,7 +297,7 @@ def learned_quality(args, w, Yd, Xd, kw, kw_l, prop, lay, g, tinfo) -> tuple[dic
     c_f = exh.reml_likelihood.double()
     gap = ((c_l - c_f) / c_f.abs().clamp(min=1.0))[~same]
     f_all = engine.build_factors(Xd, G.make_grid(g, g), lay)
-    ls = learned.learned_search(Yd, f_all, prop, lay, recenter=args.recenter)
+    ls = learned.learned_search(Yd, f_all, prop, lay, recenter=args.recenter, count_evals=True)
     pair_evals = float(ls.stats["pair_evals"].item()) if torch.is_tensor(ls.stats["pair_evals"]) else 0.0
     n_fb = int(round(ls.stats["fallback"] * V))
     q = {

@@ -522,7 +522,10 @@ def fit_glm_arma11(
                 chunks[name].append(t)
 
     def cat(name):
-        return torch.cat(chunks[name]) if chunks[name] else None
+        xs = chunks[name]
+        if not xs:
+            return None
+        return xs[0] if len(xs) == 1 else torch.cat(xs)  # one batch: no copy
 
     pending = []  # host copies queued on the stream, waited for once before returning
 

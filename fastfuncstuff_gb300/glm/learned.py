@@ -291,7 +291,8 @@ def _strip_round(pre, f, out, *, flag, k0: int):
     engine._run("ffs_reml_strip", lib.ffs_reml_strip, V, _p(count), T, K, nq, _p(sc["pairs32"]), _p(ids),
                 _p(pre.rows), _p(f.coef), _p(proj), _p(c["dcf"]), _p(out["dbest"]), _p(out["crit0"]),
                 _p(out["fb"]), _p(out["cell"]), st)
-    out["pair_evals"] = out.get("pair_evals", 0) + nq * count.sum()
+    if out.get("count_evals"):
+        out["pair_evals"] = out.get("pair_evals", 0) + nq * count.sum()
     out["strip_voxels"] = count
     out.setdefault("_keep", []).append((ids, hi, lo, yexp, u_hi, u_lo, uex, proj))
 
@@ -346,7 +347,8 @@ def _window_round(pre, f, cen, out, *, flag, join=None):
                 _p(tiles), counts.data_ptr() + 8, max_tiles, _p(pre.rows), _p(f.coef), _p(winproj), _p(c["dcf"]),
                 _p(c["ident"]), c["p_id"], _p(c["c_p0"]),
                 _p(out["best"]), _p(out["dbest"]), _p(out["crit0"]), _p(out["fb"]), _p(out["cell"]), st)
-    out["pair_evals"] = out.get("pair_evals", 0) + c["evals"][cen.long()].sum()
+    if out.get("count_evals"):  # statistics only: (voxel, pair) windows evaluated
+        out["pair_evals"] = out.get("pair_evals", 0) + c["evals"][cen.long()].sum()
     return counts
 
 
@@ -365,7 +367,8 @@ class WindowState:
 
 def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
                     do_scale: bool = True, recenter: int = 0, q0: torch.Tensor | None = None,
-                    join=None, strip_k0: int = STRIP_K0, y_ref: torch.Tensor | None = None) -> WindowState:
+                    join=None, strip_k0: int = STRIP_K0, y_ref: torch.Tensor | None = None,
+                    count_evals: bool = False) -> WindowState:
     """The window rounds of the learned-seeded search, with no host round trip
     (so they also run inside a CUDA graph): prep with the proposal features,
     the MLP, the 5 x 5 window of every voxel, ``recenter`` re-centred rounds
@@ -375,7 +378,8 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
     ``q0`` (engine.design_basis) the prep does not read the factors;
     ``join()`` is then called before their first use (they may be built on
     another stream meanwhile). With ``y_ref`` (engine.prep) the rows are read
-    from the address it holds and written into Y as read."""
+    from the address it holds and written into Y as read. ``count_evals``
+    adds the number of (voxel, pair) criteria evaluated to the statistics."""
     lib = _lib.load()
     dev = Y.device
     V, T = Y.shape
@@ -397,7 +401,7 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
                 len(g.b_axis), _p(center), st)
     out = dict(best=torch.empty(V, dtype=torch.int32, device=dev), dbest=torch.empty(V, dtype=torch.float32, device=dev),
                crit0=torch.empty(V, dtype=torch.float64, device=dev), fb=torch.zeros(V, dtype=torch.int32, device=dev),
-               cell=torch.empty(V, dtype=torch.int32, device=dev))
+               cell=torch.empty(V, dtype=torch.int32, device=dev), count_evals=count_evals)
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
     counts = [_window_round(p1, f, center, out, flag=flag, join=join)]
     stats = {"edge_first": out["fb"].float().mean() if recenter else None}
@@ -414,7 +418,7 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
     best_crit = (out["crit0"] + out["dbest"].double()).float()
     fb = out["fb"]
     small = torch.stack([fb.sum().to(torch.int32), flag[0]] + [cn[1] for cn in counts])
-    stats["pair_evals"] = out["pair_evals"]  # device scalar: (voxel, pair) windows evaluated
+    stats["pair_evals"] = out.get("pair_evals")  # device scalar (with count_evals): (voxel, pair) windows evaluated
     return WindowState(best=out["best"], best_crit=best_crit, scale=scale, fb=fb, proposal=prop, small=small,
                        stats=stats)
 
@@ -450,7 +454,7 @@ def learned_fallback(Y: torch.Tensor, factors: engine.GridFactors, ws: WindowSta
 
 def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
                    do_scale: bool = True, recenter: int = 0, before_fallback=None, q0=None,
-                   join=None, strip_k0: int = STRIP_K0) -> LearnedOut:
+                   join=None, strip_k0: int = STRIP_K0, count_evals: bool = False) -> LearnedOut:
     """Learned-seeded REML search: the 5 x 5 window around each proposal, the
     full grid for voxels whose best pair sits on the window edge (or whose
     window, holding no identity pair, has nothing below the identity pairs'
@@ -466,7 +470,7 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
     """
     Y = Y.float().contiguous()
     ws = learned_windows(Y, factors, proposal, layout, do_scale=do_scale, recenter=recenter, q0=q0, join=join,
-                         strip_k0=strip_k0)
+                         strip_k0=strip_k0, count_evals=count_evals)
     # copy the few numbers the host needs to pinned memory behind an event,
     # queue the caller's work, and wait for that event only
     host = torch.empty(ws.small.numel(), dtype=torch.int32, pin_memory=True)
@@ -585,8 +589,7 @@ class LearnedFitGraph:
         self.host.copy_(self.ws.small, non_blocking=True)
 
     def _body_b(self):
-        self.best_w = self.ws.best.clone()
-        self.go = engine.gls(self.Y, self.ws.scale, self.best_w, self.f, self.X, **self.gls_kw)
+        self.go = engine.gls(self.Y, self.ws.scale, self.ws.best, self.f, self.X, **self.gls_kw)
 
     def _set_source(self, Y: torch.Tensor) -> None:
         """Point y_ref at Y's rows (float32, contiguous, 16-byte aligned; on the
