@@ -133,6 +133,10 @@ class GlsArgs(C.Structure):
     ]
 
 
+class MergeField(C.Structure):
+    _fields_ = [("dst", C.c_void_p), ("src", C.c_void_p), ("src_sub", C.c_void_p), ("row_bytes", C.c_int)]
+
+
 # (symbol, argtypes, restype) of every entry point in include/ffs_reml.h
 SIGNATURES = {
     "ffs_version": ([], C.c_int),
@@ -178,13 +182,17 @@ SIGNATURES = {
     "ffs_reml_window": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                         C.c_void_p, C.c_void_p], C.c_int),
+                         C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "ffs_device_view": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
     "ffs_reml_strip": ([C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                         C.c_void_p], C.c_int),
     "ffs_reml_near_line": ([C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                             C.c_void_p], C.c_int),
+    "ffs_reml_window_finish": ([C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                C.POINTER(C.c_void_p), C.c_void_p], C.c_int),
+    "ffs_reml_compact": ([C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "ffs_merge_rows": ([C.c_int, C.c_void_p, C.c_int, C.POINTER(MergeField), C.c_void_p], C.c_int),
     "ffs_reml_project_tc_list": ([C.POINTER(ProjectArgs), C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                   C.c_void_p], C.c_int),
 }

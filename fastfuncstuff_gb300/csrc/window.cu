@@ -104,7 +104,7 @@ struct CritArgs {
   int n, T, K, n_a, n_b;
   const int* lattice;       // [n_a][n_b]
   const int* idx;           // [n] voxel of each sorted row
-  const int* center;        // [n] cell of each sorted row
+  const int* center;        // [V] window centre cell of each voxel (read at idx[i])
   const float* rows;        // [V][T] residualised rows, voxel-major (read at idx[i])
   const float4* coef;       // [P][T]
   const float* winproj;     // [n][25]
@@ -117,6 +117,7 @@ struct CritArgs {
   double* crit0;
   int* fallback;
   int* best_cell;
+  int* next_center;         // NULL, or [V]: the next round's centre of each voxel taken
 };
 
 constexpr int CRIT_TB = 16;  // steps per partial sum and sample prefetch
@@ -155,7 +156,7 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
   const int tid = threadIdx.x;
   const int i = tl.x + tid;
   const bool live = tid < tl.y;
-  const int c = w.center[tl.x];  // every row of the tile has this centre
+  const int c = w.center[w.idx[tl.x]];  // every row of the tile has this centre
   int a0, wa, b0, wb;
   window_of(c, w.n_a, w.n_b, a0, wa, b0, wb);
   const int T = w.T, Tk = w.T - w.K;
@@ -218,6 +219,10 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
   };
   float yb[CRIT_TB];
   load_block(yb, 0);
+  // a warp holding no row of the tile (a partly filled tile: the re-centred
+  // rounds' tiles often hold a few rows) stages the tables but skips the
+  // recurrences
+  const bool warp_live = (tid & ~31) < tl.y;
   for (int c0 = 0; c0 < T; c0 += WCH) {
     const int cn = min(WCH, T - c0);
     __syncthreads();  // the previous chunk's tables are no longer read
@@ -258,7 +263,7 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
       bsteady[e] = all ? 1 : 0;
     }
     __syncthreads();
-    for (int bs = 0; bs < cn; bs += CRIT_TB) {
+    for (int bs = 0; bs < cn && warp_live; bs += CRIT_TB) {
       const int t0 = c0 + bs;
       float yn[CRIT_TB];
       load_block(yn, t0 + CRIT_TB);
@@ -411,6 +416,9 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
   w.crit0[v] = *w.c_p0 + (double)Tk * log((double)rss0 + 1e-10);
   w.fallback[v] = fb;
   w.best_cell[v] = bcell;
+  // a voxel on its window's edge is re-centred on its best pair; the rest
+  // (and those without a non-identity candidate) skip the next round
+  if (w.next_center) w.next_center[v] = (fb && bcell >= 0) ? bcell : w.n_a * w.n_b;
 }
 
 // ---------------------------------------------------------------------- strip
@@ -781,7 +789,7 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
                                const int* center, const int* tiles, const int* n_tiles, int max_tiles,
                                const float* rows, const float* coef, const float* winproj, const float* dcf,
                                const unsigned char* ident, int p_id, const double* c_p0, int* best, float* dbest,
-                               double* crit0, int* fallback, int* best_cell, void* stream) {
+                               double* crit0, int* fallback, int* best_cell, int* next_center, void* stream) {
   clear_error();
   FFS_REQUIRE(n > 0 && T > K && K > 0 && n_a > 0 && n_b > 0 && p_id >= 0 && max_tiles > 0,
               "ffs_reml_window: bad sizes");
@@ -792,7 +800,7 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(window_crit_kernel), smem));
   FFS_REQUIRE(((uintptr_t)rows & 15) == 0, "ffs_reml_window: rows must be 16-byte aligned");
   CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, rows, reinterpret_cast<const float4*>(coef), winproj, dcf,
-             ident, p_id, c_p0, best, dbest, crit0, fallback, best_cell};
+             ident, p_id, c_p0, best, dbest, crit0, fallback, best_cell, next_center};
   window_crit_kernel<<<max_tiles, WTILE, smem, (cudaStream_t)stream>>>(w, reinterpret_cast<const int2*>(tiles),
                                                                         n_tiles);
   return check_launch("window_crit_kernel");

@@ -429,7 +429,7 @@ def fit_glm_arma11(
         from . import learned
 
         layout_l = layout
-        fallbacks = []
+        fb_voxels = 0.0  # voxels the full grid decided (host numbers the search reads back anyway)
     for v0 in range(0, V, bs):
         v1 = min(V, v0 + bs)
         if (use_graph and T % 4 == 0 and not Y.is_cuda and Y.dtype == torch.float32 and Y.is_pinned()
@@ -450,7 +450,7 @@ def fit_glm_arma11(
             best, scale = lo.best, lo.scale
             chunks["best"].append(best)
             chunks["crit"].append(lo.best_crit)
-            fallbacks.append(lo.fallback)
+            fb_voxels += lo.stats["fallback"] * (v1 - v0)
         elif best_all is None and proposal is not None:
             # the GLS of every voxel at its window's pair is queued before the
             # host waits for the list of fallback voxels; their rows are redone
@@ -465,7 +465,7 @@ def fit_glm_arma11(
             best, scale = lo.best, lo.scale
             chunks["best"].append(best)
             chunks["crit"].append(lo.best_crit)
-            fallbacks.append(lo.fallback)
+            fb_voxels += lo.stats["fallback"] * (v1 - v0)
             go = first["go"]
             sel = lo.fallback_idx
             if sel.numel():
@@ -540,10 +540,9 @@ def fit_glm_arma11(
         pending.append(h)
         return h
 
-    best = cat("best").long()
-    a_t = engine.const_dev(grid.a, device)
-    b_t = engine.const_dev(grid.b, device)
-    res.arma_params = out(torch.stack([a_t[best], b_t[best]], 1))
+    best = cat("best")
+    ab_t = engine.const_dev(np.stack([grid.a, grid.b], 1), device)  # [P][2]
+    res.arma_params = out(ab_t.index_select(0, best))
     if precomputed_arma_params is not None:
         res.arma_params = out(_to_tensor(precomputed_arma_params).reshape(-1, 2).to(device))
         res.reml_likelihood = out(torch.zeros(V, device=device))
@@ -598,10 +597,8 @@ def fit_glm_arma11(
         res.reml_lklhd_surface = out(cat("surf"))
         res.reml_surface_params = grid.param_list()
     if proposal is not None and best_all is None:
-        # fraction of voxels the full grid decided (a device scalar when the
-        # results stay on the device, so the call does not wait for the GPU)
-        fb = torch.cat(fallbacks).float().mean()
-        res.learned_fallback = fb if return_device else float(fb.item())
+        # fraction of voxels the full grid decided
+        res.learned_fallback = fb_voxels / V
     if spatial_metadata:
         res.voxel_mask = spatial_metadata.get("voxel_mask")
         res.full_shape = spatial_metadata.get("volume_shape")

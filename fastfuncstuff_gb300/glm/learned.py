@@ -297,11 +297,13 @@ def _strip_round(pre, f, out, *, flag, k0: int):
     out.setdefault("_keep", []).append((ids, hi, lo, yexp, u_hi, u_lo, uex, proj))
 
 
-def _window_round(pre, f, cen, out, *, flag, join=None):
+def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None):
     """Evaluate the 5 x 5 windows centred at cen (one lattice cell per voxel,
     or ncell = n_a * n_b for a voxel to skip), writing out[...] at the voxel
-    ids. Nothing waits for the host: the number of voxels taken stays on the
-    device. pre is the prep of every voxel (fp16 operands and voxel-major rows)."""
+    ids, and into next_cen (when given) the centre of a re-centred round for
+    each voxel taken (ncell: none). Nothing waits for the host: the number of
+    voxels taken stays on the device. pre is the prep of every voxel (fp16
+    operands and voxel-major rows)."""
     lib = _lib.load()
     dev = pre.scale.device
     g = f.grid
@@ -316,7 +318,6 @@ def _window_round(pre, f, cen, out, *, flag, join=None):
     cell_end = torch.empty(ncell + 2, dtype=torch.int32, device=dev)
     engine._run("ffs_reml_group", lib.ffs_reml_group, n, ncell + 1, _p(cen), _p(cell_end), _p(idx), st)
     n_taken = cell_end[ncell - 1 : ncell]  # device count of the voxels with a window
-    cen_s = cen[idx.long()].contiguous()
     hi = torch.empty(n, ld, dtype=torch.int16, device=dev)
     lo = torch.empty(n, ld, dtype=torch.int16, device=dev)
     yexp = torch.empty(n, dtype=torch.int32, device=dev)
@@ -343,10 +344,11 @@ def _window_round(pre, f, cen, out, *, flag, join=None):
                           proj=_p(winproj), flag=_p(flag))
     engine._run("ffs_reml_project_tc_list", lib.ffs_reml_project_tc_list, C.byref(ja), _p(items), _p(counts),
                 max_items, max_pairs, WIN_SLOTS, st)
-    engine._run("ffs_reml_window", lib.ffs_reml_window, n, T, K, n_a, n_b, _p(f.lattice), _p(idx), _p(cen_s),
+    engine._run("ffs_reml_window", lib.ffs_reml_window, n, T, K, n_a, n_b, _p(f.lattice), _p(idx), _p(cen),
                 _p(tiles), counts.data_ptr() + 8, max_tiles, _p(pre.rows), _p(f.coef), _p(winproj), _p(c["dcf"]),
                 _p(c["ident"]), c["p_id"], _p(c["c_p0"]),
-                _p(out["best"]), _p(out["dbest"]), _p(out["crit0"]), _p(out["fb"]), _p(out["cell"]), st)
+                _p(out["best"]), _p(out["dbest"]), _p(out["crit0"]), _p(out["fb"]), _p(out["cell"]), _p(next_cen),
+                st)
     if out.get("count_evals"):  # statistics only: (voxel, pair) windows evaluated
         out["pair_evals"] = out.get("pair_evals", 0) + c["evals"][cen.long()].sum()
     return counts
@@ -402,22 +404,34 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
     out = dict(best=torch.empty(V, dtype=torch.int32, device=dev), dbest=torch.empty(V, dtype=torch.float32, device=dev),
                crit0=torch.empty(V, dtype=torch.float64, device=dev), fb=torch.zeros(V, dtype=torch.int32, device=dev),
                cell=torch.empty(V, dtype=torch.int32, device=dev), count_evals=count_evals)
+    if not 0 <= recenter <= 6:
+        raise ValueError("recenter: 0 to 6 re-centred rounds")
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
-    counts = [_window_round(p1, f, center, out, flag=flag, join=join)]
-    stats = {"edge_first": out["fb"].float().mean() if recenter else None}
+    # each round writes the next one's centres: the voxels on a window edge
+    # are re-centred on the window's best pair, the rest skipped (ncell)
+    nxt = [torch.empty(V, dtype=torch.int32, device=dev) for _ in range(min(recenter, 2))]
+    counts = [_window_round(p1, f, center, out, flag=flag, join=join, next_cen=nxt[0] if recenter else None)]
+    # the share of voxels on the first window's edge: statistics only
+    stats = {"edge_first": (out["fb"].float().mean() if count_evals else float("nan")) if recenter else None}
     ncell = len(g.a_axis) * len(g.b_axis)
-    for _ in range(recenter):
-        # re-centre the voxels on a window edge on the window's best pair; the
-        # rest (and those whose window held no candidate) are skipped
-        again = (out["fb"] != 0) & (out["cell"] >= 0)
-        cen = torch.where(again, out["cell"], torch.full_like(out["cell"], ncell)).contiguous()
-        counts.append(_window_round(p1, f, cen, out, flag=flag))
+    for r in range(recenter):
+        cen = nxt[r % 2]
+        after = None
+        if r + 1 < recenter:  # a round writes only the voxels it takes
+            after = nxt[(r + 1) % 2]
+            after.fill_(ncell)
+        counts.append(_window_round(p1, f, cen, out, flag=flag, next_cen=after))
     if strip_k0 >= 0:  # on the last round's answers
         _strip_round(p1, f, out, flag=flag, k0=strip_k0)
     stats["strip_voxels"] = out.get("strip_voxels")
-    best_crit = (out["crit0"] + out["dbest"].double()).float()
     fb = out["fb"]
-    small = torch.stack([fb.sum().to(torch.int32), flag[0]] + [cn[1] for cn in counts])
+    # best_crit, and the numbers the host reads back: [fallback count, wait
+    # flag, each round's list overflow]
+    best_crit = torch.empty(V, dtype=torch.float32, device=dev)
+    small = torch.empty(2 + len(counts), dtype=torch.int32, device=dev)
+    extra = (C.c_void_p * (1 + len(counts)))(flag.data_ptr(), *[cn.data_ptr() + 4 for cn in counts])
+    engine._run("ffs_reml_window_finish", lib.ffs_reml_window_finish, V, _p(out["crit0"]), _p(out["dbest"]),
+                _p(fb), _p(best_crit), _p(small), len(extra), extra, st)
     stats["pair_evals"] = out.get("pair_evals")  # device scalar (with count_evals): (voxel, pair) windows evaluated
     return WindowState(best=out["best"], best_crit=best_crit, scale=scale, fb=fb, proposal=prop, small=small,
                        stats=stats)
@@ -645,25 +659,30 @@ class LearnedFitGraph:
         if stats["edge_first"] is None:
             stats["edge_first"] = n_fb / V
         stats["fallback"] = n_fb / V
-        # the graphs' buffers are overwritten by the next run: hand out copies
-        lo = LearnedOut(best=self.ws.best.clone(), best_crit=self.ws.best_crit.clone(), scale=self.ws.scale.clone(),
-                        fallback=self.ws.fb.clone(), proposal=self.ws.proposal.clone(), stats=stats)
-        go = engine.GlsOut(**{k: (None if v is None else v.clone()) for k, v in vars(self.go).items()
-                              if not k.startswith("_")})
-        if fc is None:
-            lo.fallback_idx = torch.empty(0, dtype=torch.long, device=self.Y.device)
-            return lo, go
-        main.wait_event(done)
-        sel = fc.sel[:n_fb]
-        lo.fallback_idx = sel.clone()
-        lo.best.index_copy_(0, sel, fc.so.best[:n_fb])
-        lo.best_crit.index_copy_(0, sel, fc.so.best_crit[:n_fb])
-        for fld in ("betas", "tstats", "sigma2", "fstats", "r2", "lam", "cbeta", "ct", "resid", "resid_w", "pred",
-                    "ljung_box"):
-            t_all, t_sub = getattr(go, fld), getattr(fc.gs, fld)
-            if t_all is not None:
-                t_all.index_copy_(0, sel, t_sub[:n_fb])
-        return lo, go
+        if fc is not None:
+            main.wait_event(done)
+        # the graphs' buffers are overwritten by the next run: the outputs are
+        # new tensors, every voxel's row from graph B (the window answers) or,
+        # for the fallback voxels, from graph C, written by one merge launch
+        ws, go = self.ws, self.go
+        pairs = [(ws.best, fc.so.best if fc else None), (ws.best_crit, fc.so.best_crit if fc else None),
+                 (ws.scale, None), (ws.fb, None), (ws.proposal, None)]
+        names = [k for k, v in vars(go).items() if not k.startswith("_") and v is not None]
+        pairs += [(getattr(go, k), getattr(fc.gs, k) if fc else None) for k in names]
+        outs = [torch.empty_like(src) for src, _ in pairs]
+        fields = (_lib.MergeField * len(pairs))(*[
+            _lib.MergeField(dst.data_ptr(), src.data_ptr(), None if sub is None else sub.data_ptr(),
+                            src[0].numel() * src.element_size()) for dst, (src, sub) in zip(outs, pairs)])
+        lib = _lib.load()
+        engine._run("ffs_merge_rows", lib.ffs_merge_rows, V, _p(fc.pos) if fc else None, len(pairs), fields,
+                    _st())
+        lo = LearnedOut(best=outs[0], best_crit=outs[1], scale=outs[2], fallback=outs[3], proposal=outs[4],
+                        stats=stats)
+        gout = engine.GlsOut(**dict(zip(names, outs[5:])))
+        # the fallback voxels, in no particular order
+        lo.fallback_idx = (fc.ids[:n_fb].long() if fc else
+                           torch.empty(0, dtype=torch.long, device=self.Y.device))
+        return lo, gout
 
     def _fallback_graph(self, n_fb: int):
         """Graph C: the full-grid search and GLS of up to n_pad >= n_fb
@@ -677,19 +696,18 @@ class LearnedFitGraph:
         while len(self._fb_graphs) >= 3:
             self._fb_graphs.pop(next(iter(self._fb_graphs)))
         dev = self.Y.device
-        fc = types.SimpleNamespace(sel=torch.zeros(n_pad + 1, dtype=torch.long, device=dev),
-                                   ids=torch.arange(self.Y.shape[0], device=dev))
-        # the buffers above are filled on the current stream, behind graph B:
-        # the warm-up pass on the fallback stream must not start before them
-        torch.cuda.current_stream().synchronize()
+        V = self.Y.shape[0]
+        fc = types.SimpleNamespace(ids=torch.empty(n_pad, dtype=torch.int32, device=dev),
+                                   pos=torch.empty(V, dtype=torch.int32, device=dev),
+                                   count=torch.empty(1, dtype=torch.int32, device=dev))
+        lib = _lib.load()
 
         def body():
-            fb = self.ws.fb
-            pos = torch.where(fb != 0, torch.cumsum(fb, 0) - 1, torch.full_like(fb, n_pad)).long()
-            fc.sel.zero_()
-            fc.sel.scatter_(0, pos.clamp_(max=n_pad), fc.ids)
-            sel = fc.sel[:n_pad]
-            Yf = self.Y.index_select(0, sel)
+            # the fallback voxels' ids (slots past their count hold voxel 0)
+            # and each voxel's slot, for the merge of the outputs
+            engine._run("ffs_reml_compact", lib.ffs_reml_compact, V, _p(self.ws.fb), n_pad, _p(fc.ids),
+                        _p(fc.pos), _p(fc.count), _st())
+            Yf = self.Y.index_select(0, fc.ids)
             fc.so = engine.search(Yf, self.f, hierarchical=False, projector="tc", do_scale=self.do_scale)
             fc.gs = engine.gls(Yf, fc.so.scale, fc.so.best, self.f, self.X, **self.gls_kw)
 

@@ -554,7 +554,7 @@ int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, cons
 
 /* The windowed refine's criterion over the tiles of ffs_reml_window_items
  * (launched for max_tiles, *n_tiles of them real), one sorted row i < n (voxel
- * idx[i], window centre center[i]): y'R^-1 y of each non-identity window pair by the O(T)
+ * idx[i], window centre center[idx[i]]): y'R^-1 y of each non-identity window pair by the O(T)
  * recurrence of coef over rows[idx[i]] (rows: [V][T] residualised series,
  * voxel-major, 16-byte aligned: ffs_reml_prep's yr_rows), its
  * projection from winproj[i][slot] (ffs_reml_project_tc_list), the criterion
@@ -567,12 +567,14 @@ int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, cons
  * fallback = 1 when the full grid must decide (the best non-identity pair has
  * a valid lattice neighbour outside the window, or the window holds no
  * identity pair and nothing below d = 0), best_cell (the lattice cell of the
- * best non-identity pair, -1 if none). */
+ * best non-identity pair, -1 if none) and, when next_center is given, the
+ * voxel's centre for a re-centred round: best_cell when fallback = 1 and
+ * best_cell >= 0, else n_a * n_b (no window). */
 int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx, const int* center,
                     const int* tiles, const int* n_tiles, int max_tiles, const float* rows, const float* coef,
                     const float* winproj, const float* dcf, const unsigned char* ident, int p_id,
                     const double* c_p0, int* best, float* dbest, double* crit0, int* fallback, int* best_cell,
-                    void* stream);
+                    int* next_center, void* stream);
 
 /* The strip next to the identity line in the learned-seeded refine (no
  * reference counterpart: the reference searches every pair). Near lambda = 0
@@ -599,6 +601,38 @@ int ffs_reml_strip(int n, const int* n_dev, int T, int K, int n_pairs, const int
  * reference counterpart). */
 int ffs_reml_near_line(int V, const int* best, const int* dist, int k0, const int* fallback, int* ids, int* count,
                        void* stream);
+
+/* The end of the learned-seeded refine's window rounds: best_crit[v] =
+ * crit0[v] + dbest[v] (FP64 sum rounded to float) for v < V, small[0] = the
+ * number of voxels with fallback[v] != 0, small[1 + i] = *extra[i] for the
+ * n_extra <= 8 device ints named by the host array extra (the wait flag and
+ * the work lists' overflow flags): the few numbers the host reads back (no
+ * reference counterpart). */
+int ffs_reml_window_finish(int V, const double* crit0, const float* dbest, const int* fallback, float* best_crit,
+                           int* small, int n_extra, const int* const* extra, void* stream);
+
+/* The voxels v < V with flag[v] != 0 into ids[0 .. *count), in no particular
+ * order, with ids[*count .. n_pad) = 0 and pos[v] = the slot of voxel v in ids
+ * or -1: the list of the voxels the full grid takes after the learned-seeded
+ * refine, padded to a captured size (no reference counterpart: the reference
+ * searches every pair). A flagged voxel past n_pad keeps pos -1; size n_pad
+ * from the same flags. */
+int ffs_reml_compact(int V, const int* flag, int n_pad, int* ids, int* pos, int* count, void* stream);
+
+/* One output field of ffs_merge_rows: V rows of row_bytes (a multiple of 4)
+ * each. */
+typedef struct {
+  void* dst;            /* [V] rows written */
+  const void* src;      /* [V] rows: every voxel's value */
+  const void* src_sub;  /* NULL, or [n] rows that replace src's for the voxels with pos[v] >= 0 */
+  int row_bytes;
+} ffs_merge_field;
+
+/* dst[v] = src_sub[pos[v]] if pos (may be NULL) gives pos[v] >= 0 and the
+ * field has src_sub, else src[v], for up to 32 fields in one launch: the fit's
+ * outputs from the windows' answers and the full grid's answers for the
+ * voxels it took (no reference counterpart). */
+int ffs_merge_rows(int V, const int* pos, int n_fields, const ffs_merge_field* fields, void* stream);
 
 #ifdef __cplusplus
 }

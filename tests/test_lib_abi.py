@@ -26,6 +26,7 @@ STRUCTS = {
     "ffs_surface_args": _lib.SurfaceArgs,
     "ffs_select_args": _lib.SelectArgs,
     "ffs_gls_args": _lib.GlsArgs,
+    "ffs_merge_field": _lib.MergeField,
 }
 
 
