@@ -44,8 +44,9 @@ struct MergeFields {
 };
 
 // dst[v] = src_sub[pos[v]] when pos[v] >= 0 and the field has src_sub, else
-// src[v]; blockIdx.y is the field, 16-byte words when the field's rows and
-// pointers allow, 4-byte words otherwise
+// src[v] (a field without src leaves those rows as they are); blockIdx.y is
+// the field, 16-byte words when the field's rows and pointers allow, 4-byte
+// words otherwise
 __global__ void __launch_bounds__(256) merge_kernel(int V, const int* __restrict__ pos, MergeFields m) {
   const ffs_merge_field fd = m.f[blockIdx.y];
   const bool vec = (fd.row_bytes & 15) == 0 && (((uintptr_t)fd.dst | (uintptr_t)fd.src |
@@ -57,6 +58,7 @@ __global__ void __launch_bounds__(256) merge_kernel(int V, const int* __restrict
        e += (long long)gridDim.x * blockDim.x) {
     const int v = (int)(e / nw), k = (int)(e % nw);
     const int p = (pos && fd.src_sub) ? pos[v] : -1;
+    if (p < 0 && !fd.src) continue;
     const char* s = p >= 0 ? static_cast<const char*>(fd.src_sub) + (size_t)p * fd.row_bytes
                            : static_cast<const char*>(fd.src) + (size_t)v * fd.row_bytes;
     char* d = static_cast<char*>(fd.dst) + (size_t)v * fd.row_bytes;
@@ -124,7 +126,7 @@ extern "C" int ffs_merge_rows(int V, const int* pos, int n_fields, const ffs_mer
   long long most = 0;
   for (int i = 0; i < n_fields; ++i) {
     const ffs_merge_field& f = fields[i];
-    FFS_REQUIRE(f.dst && f.src && f.row_bytes > 0 && f.row_bytes % 4 == 0 &&
+    FFS_REQUIRE(f.dst && (f.src || (f.src_sub && pos)) && f.row_bytes > 0 && f.row_bytes % 4 == 0 &&
                     (((uintptr_t)f.dst | (uintptr_t)f.src | (uintptr_t)f.src_sub) & 3) == 0,
                 "ffs_merge_rows: field %d: null buffer, or rows or pointers not 4-byte aligned", i);
     m.f[i] = f;

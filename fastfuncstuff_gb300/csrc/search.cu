@@ -612,6 +612,85 @@ __global__ void group_scan(int P, int* cnt) {
   if (threadIdx.x == 0) cnt[P] = carry;
 }
 
+// Keys up to GROUP_BLOCK_KEYS: each CTA counts a contiguous chunk of the
+// voxels in shared memory (warp-aggregated), then adds each key's count to the
+// global histogram once, so a popular key takes one global atomic per CTA
+// instead of one per warp. Keys lie in [0, P); others are not counted.
+constexpr int GROUP_BLOCK_KEYS = 6144;
+constexpr int GROUP_BLOCK_THREADS = 256;
+
+__device__ __forceinline__ void group_chunk(int V, int& v0, int& v1) {
+  const int chunk = (V + gridDim.x - 1) / gridDim.x;
+  v0 = min(V, (int)blockIdx.x * chunk);
+  v1 = min(V, v0 + chunk);
+}
+
+// the CTA's chunk counted into h[P] (shared memory, zeroed by the caller)
+__device__ __forceinline__ void group_count_chunk(int v0, int v1, const int* best, int P, int* h) {
+  for (int b0 = v0; b0 < v1; b0 += blockDim.x) {  // uniform over the CTA
+    const int v = b0 + threadIdx.x;
+    const bool on = v < v1;
+    const int key = on ? best[v] : -1;
+    const bool ok = on && (unsigned)key < (unsigned)P;
+    const unsigned act = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+      const unsigned same = __match_any_sync(act, key);
+      if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(h + key, __popc(same));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(GROUP_BLOCK_THREADS) group_hist_block(int V, const int* best, int P, int* cnt) {
+  extern __shared__ float sm[];
+  int* h = reinterpret_cast<int*>(sm);  // [P]
+  for (int i = threadIdx.x; i < P; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  int v0, v1;
+  group_chunk(V, v0, v1);
+  group_count_chunk(v0, v1, best, P, h);
+  __syncthreads();
+  for (int i = threadIdx.x; i < P; i += blockDim.x)
+    if (h[i]) atomicAdd(cnt + i, h[i]);
+}
+
+// The CTA reserves each key's slots for its chunk with one global atomic,
+// then every voxel takes the next slot of its key within them (warp leaders
+// claim a run of slots for the lanes of equal key).
+__global__ void __launch_bounds__(GROUP_BLOCK_THREADS) group_scatter_block(int V, const int* best, int P,
+                                                                           int* cursor, int* order) {
+  extern __shared__ float sm[];
+  int* h = reinterpret_cast<int*>(sm);  // [P] the chunk's count, then its running slot
+  int* base = h + P;                    // [P] the chunk's first slot of each key
+  for (int i = threadIdx.x; i < P; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  int v0, v1;
+  group_chunk(V, v0, v1);
+  group_count_chunk(v0, v1, best, P, h);
+  __syncthreads();
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    const int c = h[i];
+    base[i] = c ? atomicAdd(cursor + i, c) : 0;
+    h[i] = 0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (int b0 = v0; b0 < v1; b0 += blockDim.x) {
+    const int v = b0 + threadIdx.x;
+    const bool on = v < v1;
+    const int key = on ? best[v] : -1;
+    const bool ok = on && (unsigned)key < (unsigned)P;
+    const unsigned act = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+      const unsigned same = __match_any_sync(act, key);
+      const int leader = __ffs(same) - 1;
+      int r = 0;
+      if (lane == leader) r = atomicAdd(h + key, __popc(same));
+      r = __shfl_sync(same, r, leader);
+      order[base[key] + r + __popc(same & ((1u << lane) - 1u))] = v;
+    }
+  }
+}
+
 // The leader of each set of equal keys reserves the set's slots with one
 // atomic; every lane takes the slot of its rank within the set.
 __global__ void group_scatter(int V, const int* best, int* cursor, int* order) {
@@ -733,9 +812,17 @@ extern "C" int ffs_reml_group(int V, int P, const int* best, int* work, int* ord
   FFS_REQUIRE(V > 0 && P > 0 && best && work && order, "ffs_reml_group: bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
   FFS_CUDA(cudaMemsetAsync(work, 0, sizeof(int) * (P + 1), st));
-  group_hist<<<ceil_div(V, 256), 256, 0, st>>>(V, best, work);
-  group_scan<<<1, 1024, 0, st>>>(P, work);
-  group_scatter<<<ceil_div(V, 256), 256, 0, st>>>(V, best, work, order);
+  if (P <= GROUP_BLOCK_KEYS) {
+    // a contiguous chunk of the voxels per CTA, counted in shared memory
+    const int grid = std::min(ceil_div(V, GROUP_BLOCK_THREADS), 2 * 152);
+    group_hist_block<<<grid, GROUP_BLOCK_THREADS, sizeof(int) * P, st>>>(V, best, P, work);
+    group_scan<<<1, 1024, 0, st>>>(P, work);
+    group_scatter_block<<<grid, GROUP_BLOCK_THREADS, 2 * sizeof(int) * P, st>>>(V, best, P, work, order);
+  } else {
+    group_hist<<<ceil_div(V, 256), 256, 0, st>>>(V, best, work);
+    group_scan<<<1, 1024, 0, st>>>(P, work);
+    group_scatter<<<ceil_div(V, 256), 256, 0, st>>>(V, best, work, order);
+  }
   return check_launch("group kernels");
 }
 

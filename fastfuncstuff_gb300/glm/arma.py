@@ -375,6 +375,11 @@ def fit_glm_arma11(
     bs = _batch_size(V, T, P, K, batch_size, device)
     use_graph = (best_all is None and proposal is not None and cuda_graphs and lj is None and bs >= V
                  and Dd is None)
+    # results for the host straight from the GLS kernels (pinned memory
+    # written over the host link while they run) when nothing else reads them
+    # on the device
+    host_gls = (use_graph and not return_device and not use_double and not ti and sets is None
+                and not (want_r2_partial or want_r2_semipartial))
     afull = Dd is not None and bool(column_sets)
     q0 = join = None
     slots = None
@@ -445,7 +450,7 @@ def fit_glm_arma11(
                                      do_scale=not use_double,
                                      gls_kw=dict(want_residuals=want_residuals, want_predicted=want_predicted),
                                      factor_kw=dict(task_indices=ti, glt=glt, with_tc=K <= TC_MAX_K, sets=sets))
-            lo, go = plan.run(Yb, Xd)
+            lo, go = plan.run(Yb, Xd, host_out=host_gls)
             factors_used = plan.f
             best, scale = lo.best, lo.scale
             chunks["best"].append(best)
@@ -532,6 +537,9 @@ def fit_glm_arma11(
     def out(t, dtype=None):
         if t is None:
             return None
+        if not t.is_cuda:  # written by the kernels into pinned host memory
+            pending.append(t)
+            return t.to(dtype=dtype or out_dtype)
         t = t.to(dtype=dtype or out_dtype)
         if return_device:
             return t

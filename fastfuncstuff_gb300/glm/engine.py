@@ -495,6 +495,10 @@ class PrepOut:
 BASIS_MAX_K = 32
 
 
+def _view(ptr, t):
+    return None if t is None else ptr(t)
+
+
 def device_view(t: torch.Tensor) -> int | None:
     """The device address of t's data -- device memory, or pinned host
     memory mapped into the device's address space -- or None when kernels may
@@ -775,11 +779,13 @@ class GlsOut:
 
 def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors, X: torch.Tensor, *,
         want_residuals: bool = False, want_predicted: bool = False, lj=None,
-        design: torch.Tensor | None = None) -> GlsOut:
+        design: torch.Tensor | None = None, host_out: bool = False) -> GlsOut:
     """GLS refit of every voxel at its pair ``best`` (indices into ``f``).
 
     Grouped fits pass X as (D, T, K) and ``design`` [V] (each voxel's design):
-    voxels are then grouped by design * P + pair."""
+    voxels are then grouped by design * P + pair. With ``host_out`` the
+    outputs are pinned host tensors that the kernel writes over the host link
+    as it goes (valid once the stream has passed the launch)."""
     lib = _lib.load()
     dev = Y.device
     V, T = Y.shape
@@ -796,7 +802,8 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
     _run("ffs_reml_group", lib.ffs_reml_group, V, P, _p(best), _p(work), _p(order), st)
     X = X.to(device=dev)
     Xt = padded_design_t(X) if X.ndim == 2 else torch.stack([padded_design_t(x) for x in X])
-    f32 = dict(device=dev, dtype=torch.float32)
+    f32 = dict(dtype=torch.float32, pin_memory=True) if host_out else dict(device=dev, dtype=torch.float32)
+    ptr = device_view if host_out else _p
     ng = 0 if f.glt is None else f.glt.shape[0]
     o = GlsOut(betas=torch.empty(V, K, **f32), tstats=torch.empty(V, K, **f32), sigma2=torch.empty(V, **f32),
                fstats=torch.empty(V, **f32), r2=torch.empty(V, **f32), lam=torch.empty(V, **f32),
@@ -810,10 +817,10 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
                       order=_p(order), coef=_p(f.coef), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
                       a=_p(f.a), b=_p(f.b), lambda_fp32=int(f.grid.lambda_fp32), n_task=nt,
                       task_idx=_p(f.task_idx), Ftask=_p(f.Ftask), n_glt=ng, glt=_p(f.glt),
-                      glt_var=_p(f.glt_var), betas=_p(o.betas), tstats=_p(o.tstats), sigma2=_p(o.sigma2),
-                      fstats=_p(o.fstats), r2=_p(o.r2), lam=_p(o.lam), cbeta=_p(o.cbeta), ct=_p(o.ct),
-                      resid=_p(o.resid), resid_w=_p(o.resid_w), pred=_p(o.pred), center_dev=_p(f.center_flag),
-                      n_pairs=n_pairs)
+                      glt_var=_p(f.glt_var), betas=ptr(o.betas), tstats=ptr(o.tstats), sigma2=ptr(o.sigma2),
+                      fstats=ptr(o.fstats), r2=ptr(o.r2), lam=ptr(o.lam), cbeta=_view(ptr, o.cbeta),
+                      ct=_view(ptr, o.ct), resid=_view(ptr, o.resid), resid_w=_view(ptr, o.resid_w),
+                      pred=_view(ptr, o.pred), center_dev=_p(f.center_flag), n_pairs=n_pairs)
     h, ptau_d, w_d = 0, None, None
     if lj is not None and lj[0] > 0:
         h, ptau, w, _ = lj
@@ -821,8 +828,8 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
         w_d = const_dev(w, dev)
         o.ljung_box = torch.empty(V, **f32)
     tiles = torch.empty(P + 1, dtype=torch.int32, device=dev)
-    _run("ffs_reml_gls_grouped", lib.ffs_reml_gls_grouped, C.byref(ga), h, _p(ptau_d), _p(w_d), _p(o.ljung_box),
-         P, _p(work), _p(tiles), st)
+    _run("ffs_reml_gls_grouped", lib.ffs_reml_gls_grouped, C.byref(ga), h, _p(ptau_d), _p(w_d),
+         _view(ptr, o.ljung_box), P, _p(work), _p(tiles), st)
     o._keep = (ptau_d, w_d, tiles)
     o._keep2 = (Y, order, work, Xt, best)
     return o

@@ -530,20 +530,21 @@ def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxe
 
 
 class LearnedFitGraph:
-    """The learned-seeded fit of one shape as two CUDA graphs.
+    """The learned-seeded fit of one shape: two CUDA graphs and one GLS.
 
     Graph A builds the grid factors of X on a side stream while the prep with
     the proposal features (against the design basis of X), the MLP and the
     first window round's grouping and gathers run on the main one; the window
     rounds then join them. It ends by copying the few numbers the host needs
-    (fallback count, wait flag, list overflows) to pinned memory.
-    Graph B is the GLS of every voxel at its window pair. ``run`` replays A,
-    records an event, replays B, waits for the event only (B keeps the GPU
-    busy meanwhile), then runs the full grid and the GLS of the fallback
-    voxels from graph C beside B. The data are read where they lie (device
-    memory, or pinned host memory streamed by the prep) through an address
-    that each run writes on the device; the design is copied into a static
-    buffer; results are returned as new tensors.
+    (fallback count, wait flag, list overflows) to pinned memory. ``run``
+    replays A, records an event, launches the GLS of every voxel at its
+    window pair (into new output tensors: device memory, or pinned host
+    memory written over the host link), waits for the event only (the GLS
+    keeps the GPU busy meanwhile), then runs the full grid and the GLS of the
+    fallback voxels from graph C beside it and merges their rows into the
+    outputs. The data are read where they lie (device memory, or pinned host
+    memory streamed by the prep) through an address that each run writes on
+    the device; the design is copied into a static buffer.
     """
 
     def __init__(self, Y: torch.Tensor, X: torch.Tensor, grid: RemlGrid, layout: RunLayout,
@@ -565,19 +566,15 @@ class LearnedFitGraph:
         self.cflag, self.ccoef = engine.constant_flag(self.X)
         self.host = torch.empty(3 + recenter, dtype=torch.int32, pin_memory=True)
         self.side = torch.cuda.Stream(dev)  # the grid build runs beside the prep chain
-        self.side_fb = torch.cuda.Stream(self.Y.device)  # the fallback runs beside graph B
+        self.side_fb = torch.cuda.Stream(self.Y.device)  # the fallback runs beside the window pairs' GLS
         self._fb_graphs: dict = {}
         # one eager pass fills the host-side caches (device constants, tensor
         # maps, kernel attributes) that a capture must not create
         self._body_a()
-        self._body_b()
         torch.cuda.synchronize()
         self.ga = torch.cuda.CUDAGraph()
-        self.gb = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.ga, capture_error_mode="thread_local"):
             self._body_a()
-        with torch.cuda.graph(self.gb, pool=self.ga.pool(), capture_error_mode="thread_local"):
-            self._body_b()
 
     def _body_a(self):
         main = torch.cuda.current_stream()
@@ -602,9 +599,6 @@ class LearnedFitGraph:
                                   y_ref=self.y_ref if self.inplace else None)
         self.host.copy_(self.ws.small, non_blocking=True)
 
-    def _body_b(self):
-        self.go = engine.gls(self.Y, self.ws.scale, self.ws.best, self.f, self.X, **self.gls_kw)
-
     def _set_source(self, Y: torch.Tensor) -> None:
         """Point y_ref at Y's rows (float32, contiguous, 16-byte aligned; on the
         device, or pinned host memory that the prep streams in place)."""
@@ -621,11 +615,14 @@ class LearnedFitGraph:
         self.y_ref.copy_(self.y_ref_host, non_blocking=True)
         self._src = Y  # kept alive until the run that reads it has finished
 
-    def run(self, Y: torch.Tensor, X: torch.Tensor):
+    def run(self, Y: torch.Tensor, X: torch.Tensor, *, host_out: bool = False):
         """(LearnedOut, engine.GlsOut) of data Y (V, T) and design X (T, K).
         Y may be a CUDA tensor or a pinned host tensor: the prep reads its rows
         in place (over the host link for host memory) and the host-to-device
-        transfer overlaps with the grid build and the prep's work."""
+        transfer overlaps with the grid build and the prep's work. With
+        ``host_out`` the GLS outputs are pinned host tensors written by the
+        kernels over the host link while they run (read them after a
+        synchronisation of the current stream)."""
         main = torch.cuda.current_stream()
         self._set_source(Y)
         self.X.copy_(X)
@@ -636,7 +633,9 @@ class LearnedFitGraph:
         self.ga.replay()
         ready = torch.cuda.Event()
         ready.record()
-        self.gb.replay()
+        # the GLS of every voxel at its window pair, launched while graph A
+        # runs (its outputs are new tensors of this call)
+        go = engine.gls(self.Y, self.ws.scale, self.ws.best, self.f, self.X, host_out=host_out, **self.gls_kw)
         ready.synchronize()
         n_fb, code = int(self.host[0]), int(self.host[1])
         if code != 0:
@@ -644,7 +643,7 @@ class LearnedFitGraph:
         if bool((self.host[2:] != 0).any()):
             raise RuntimeError("ffs_reml_window_items: work list overflow")
         # the fallback voxels' full grid and GLS: graph C (of a padded voxel
-        # count) on a second stream, beside the GLS of graph B (both only read
+        # count) on a second stream, beside the window pairs' GLS (both only read
         # the graphs' buffers)
         fs = self.side_fb
         fc = self._fallback_graph(n_fb) if n_fb else None
@@ -661,28 +660,30 @@ class LearnedFitGraph:
         stats["fallback"] = n_fb / V
         if fc is not None:
             main.wait_event(done)
-        # the graphs' buffers are overwritten by the next run: the outputs are
-        # new tensors, every voxel's row from graph B (the window answers) or,
-        # for the fallback voxels, from graph C, written by one merge launch
-        ws, go = self.ws, self.go
-        pairs = [(ws.best, fc.so.best if fc else None), (ws.best_crit, fc.so.best_crit if fc else None),
-                 (ws.scale, None), (ws.fb, None), (ws.proposal, None)]
-        names = [k for k, v in vars(go).items() if not k.startswith("_") and v is not None]
-        pairs += [(getattr(go, k), getattr(fc.gs, k) if fc else None) for k in names]
-        outs = [torch.empty_like(src) for src, _ in pairs]
-        fields = (_lib.MergeField * len(pairs))(*[
-            _lib.MergeField(dst.data_ptr(), src.data_ptr(), None if sub is None else sub.data_ptr(),
-                            src[0].numel() * src.element_size()) for dst, (src, sub) in zip(outs, pairs)])
+        # graph A's buffers are overwritten by the next run: its answers are
+        # copied into new tensors, with the full grid's rows for the fallback
+        # voxels, and those rows replace the window answers' rows of the GLS
+        # outputs; one merge launch for all of them
+        ws = self.ws
+        keep = [(ws.best, fc.so.best if fc else None), (ws.best_crit, fc.so.best_crit if fc else None),
+                (ws.scale, None), (ws.fb, None), (ws.proposal, None)]
+        outs = [torch.empty_like(src) for src, _ in keep]
+        fields = [(dst.data_ptr(), src.data_ptr(), _p(sub), src[0].numel() * src.element_size())
+                  for dst, (src, sub) in zip(outs, keep)]
+        if fc is not None:
+            for k, v in vars(go).items():
+                if not k.startswith("_") and v is not None:
+                    fields.append((engine.device_view(v), None, getattr(fc.gs, k).data_ptr(),
+                                   v[0].numel() * v.element_size()))
+        arr = (_lib.MergeField * len(fields))(*[_lib.MergeField(*f) for f in fields])
         lib = _lib.load()
-        engine._run("ffs_merge_rows", lib.ffs_merge_rows, V, _p(fc.pos) if fc else None, len(pairs), fields,
-                    _st())
+        engine._run("ffs_merge_rows", lib.ffs_merge_rows, V, _p(fc.pos) if fc else None, len(fields), arr, _st())
         lo = LearnedOut(best=outs[0], best_crit=outs[1], scale=outs[2], fallback=outs[3], proposal=outs[4],
                         stats=stats)
-        gout = engine.GlsOut(**dict(zip(names, outs[5:])))
         # the fallback voxels, in no particular order
         lo.fallback_idx = (fc.ids[:n_fb].long() if fc else
                            torch.empty(0, dtype=torch.long, device=self.Y.device))
-        return lo, gout
+        return lo, go
 
     def _fallback_graph(self, n_fb: int):
         """Graph C: the full-grid search and GLS of up to n_pad >= n_fb
@@ -715,7 +716,7 @@ class LearnedFitGraph:
             body()  # fills the host-side caches a capture must not create
         self.side_fb.synchronize()
         fc.graph = torch.cuda.CUDAGraph()
-        # its own memory pool: graph C runs concurrently with graph B
+        # its own memory pool: graph C runs concurrently with the window pairs' GLS
         with torch.cuda.graph(fc.graph, capture_error_mode="thread_local"):
             body()
         self._fb_graphs[n_pad] = fc

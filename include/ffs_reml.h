@@ -623,15 +623,16 @@ int ffs_reml_compact(int V, const int* flag, int n_pad, int* ids, int* pos, int*
  * each. */
 typedef struct {
   void* dst;            /* [V] rows written */
-  const void* src;      /* [V] rows: every voxel's value */
+  const void* src;      /* [V] rows: every voxel's value, or NULL: dst's other rows stay */
   const void* src_sub;  /* NULL, or [n] rows that replace src's for the voxels with pos[v] >= 0 */
   int row_bytes;
 } ffs_merge_field;
 
 /* dst[v] = src_sub[pos[v]] if pos (may be NULL) gives pos[v] >= 0 and the
- * field has src_sub, else src[v], for up to 32 fields in one launch: the fit's
- * outputs from the windows' answers and the full grid's answers for the
- * voxels it took (no reference counterpart). */
+ * field has src_sub, else src[v] (nothing, for a field without src), for up
+ * to 32 fields in one launch: the fit's outputs from the windows' answers and
+ * the full grid's answers for the voxels it took (no reference counterpart).
+ * dst may be pinned host memory mapped into the device's address space. */
 int ffs_merge_rows(int V, const int* pos, int n_fields, const ffs_merge_field* fields, void* stream);
 
 #ifdef __cplusplus

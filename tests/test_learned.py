@@ -361,6 +361,14 @@ def test_fit_with_proposal_matches_full_grid_fit_where_pairs_agree(cuda_graphs):
                           **kw)
     for name in ("betas", "tstats", "sigma2", "arma_params", "reml_likelihood", "residuals"):
         assert torch.equal(getattr(host, name), getattr(got, name)), name
+    # results on the host (with graphs the GLS kernels write them into pinned
+    # memory as they run, and the fallback voxels' rows are merged there)
+    hout = fit_glm_arma11(Y.cpu().pin_memory(), X, proposal=prop, proposal_recenter=1, cuda_graphs=cuda_graphs,
+                          **dict(kw, return_device=False))
+    for name in ("betas", "tstats", "sigma2", "fstats", "r2", "arma_lambda", "arma_params", "reml_likelihood",
+                 "residuals", "residuals_whitened"):
+        assert not getattr(hout, name).is_cuda, name
+        assert torch.equal(getattr(hout, name), getattr(got, name).cpu()), name
     same = (got.arma_params == full.arma_params).all(1)
     assert float(same.float().mean()) >= 0.995  # a briefly trained network
     assert 0.0 < float(got.learned_fallback) < 0.5  # some voxels took the fallback path
