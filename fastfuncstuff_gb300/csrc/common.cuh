@@ -51,6 +51,20 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// warp_sum of N values at once: the same butterfly per value (so the same
+// sums), the N shuffle chains interleaved
+template <int N>
+__device__ __forceinline__ void warp_sum_n(float (&v)[N]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float t[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) t[k] = __shfl_xor_sync(0xffffffffu, v[k], o);
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] += t[k];
+  }
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -409,57 +409,61 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
   __syncthreads();
   tile_stage_rows(a.Y, T, nq, src_row, Ys, ld);
   const bool centre = a.center_dev ? (*a.center_dev != 0) : (a.center != 0);
-  for (int i = wid; i < TILE_V; i += TILE_WARPS) {
-    float4* row4 = reinterpret_cast<float4*>(Ys + (size_t)i * ld);
-    if (i >= n) {  // warp-uniform
-      if (lane == 0) {
-        st[i] = 0.f;
-        st[TILE_V + i] = 1.f;
-        st[2 * TILE_V + i] = 0.f;
-      }
-      continue;
+  {
+    // the warp's rows wid + 8k together, so their reductions overlap; a row
+    // past the tile's voxels keeps m = 0, sc = 1 and mean 0
+    constexpr int RW = TILE_V / TILE_WARPS;
+    bool on[RW];
+    float sc[RW], m[RW], inv[RW], sy[RW];
+#pragma unroll
+    for (int k = 0; k < RW; ++k) {
+      const int i = wid + TILE_WARPS * k;
+      on[k] = i < n;
+      sc[k] = on[k] ? a.scale[src_row[i]] : 1.f;
+      m[k] = 0.f;
+      sy[k] = 0.f;
+      inv[k] = __frcp_rn(sc[k]);  // one reciprocal per voxel, then products
     }
-    const float sc = a.scale[src_row[i]];
-    float m = 0.f;
     if (centre) {
-      float s = 0.f;
-      for (int q = lane; q < nq; q += 32) {
-        const float4 y = row4[q];
-        s += ((y.x + y.y) + y.z) + y.w;
+#pragma unroll
+      for (int k = 0; k < RW; ++k) {
+        if (!on[k]) continue;  // warp-uniform
+        const float4* row4 = reinterpret_cast<const float4*>(Ys + (size_t)(wid + TILE_WARPS * k) * ld);
+        for (int q = lane; q < nq; q += 32) {
+          const float4 y = row4[q];
+          m[k] += ((y.x + y.y) + y.z) + y.w;
+        }
       }
-      m = warp_sum(s) / (float)T;
+      warp_sum_n(m);
+#pragma unroll
+      for (int k = 0; k < RW; ++k) m[k] = on[k] ? m[k] / (float)T : 0.f;
     }
-    float sy = 0.f;
-    const float inv = __frcp_rn(sc);  // one reciprocal per voxel, then products
-    if (vec) {  // whole quads: no padding inside the row
-      for (int q = lane; q < nq; q += 32) {
-        const float4 y = row4[q];
-        float4 r;
-        r.x = __fmul_rn(__fsub_rn(y.x, m), inv);
-        r.y = __fmul_rn(__fsub_rn(y.y, m), inv);
-        r.z = __fmul_rn(__fsub_rn(y.z, m), inv);
-        r.w = __fmul_rn(__fsub_rn(y.w, m), inv);
-        row4[q] = r;
-        sy += ((r.x + r.y) + r.z) + r.w;
-      }
-    } else {
+#pragma unroll
+    for (int k = 0; k < RW; ++k) {
+      if (!on[k]) continue;
+      float4* row4 = reinterpret_cast<float4*>(Ys + (size_t)(wid + TILE_WARPS * k) * ld);
+      const float mk = m[k], ik = inv[k];
       for (int q = lane; q < nq; q += 32) {
         const float4 y = row4[q];
         const int t = 4 * q;
-        float4 r;
-        r.x = __fmul_rn(__fsub_rn(y.x, m), inv);
-        r.y = t + 1 < T ? __fmul_rn(__fsub_rn(y.y, m), inv) : 0.f;
-        r.z = t + 2 < T ? __fmul_rn(__fsub_rn(y.z, m), inv) : 0.f;
-        r.w = t + 3 < T ? __fmul_rn(__fsub_rn(y.w, m), inv) : 0.f;
+        float4 r;  // whole quads when T % 4 == 0: no padding inside the row
+        r.x = __fmul_rn(__fsub_rn(y.x, mk), ik);
+        r.y = (vec || t + 1 < T) ? __fmul_rn(__fsub_rn(y.y, mk), ik) : 0.f;
+        r.z = (vec || t + 2 < T) ? __fmul_rn(__fsub_rn(y.z, mk), ik) : 0.f;
+        r.w = (vec || t + 3 < T) ? __fmul_rn(__fsub_rn(y.w, mk), ik) : 0.f;
         row4[q] = r;
-        sy += ((r.x + r.y) + r.z) + r.w;
+        sy[k] += ((r.x + r.y) + r.z) + r.w;
       }
     }
-    sy = warp_sum(sy);
+    warp_sum_n(sy);
     if (lane == 0) {
-      st[i] = m;
-      st[TILE_V + i] = sc;
-      st[2 * TILE_V + i] = sy / (float)T;
+#pragma unroll
+      for (int k = 0; k < RW; ++k) {
+        const int i = wid + TILE_WARPS * k;
+        st[i] = m[k];
+        st[TILE_V + i] = sc[k];
+        st[2 * TILE_V + i] = on[k] ? sy[k] / (float)T : 0.f;
+      }
     }
   }
   __syncthreads();
