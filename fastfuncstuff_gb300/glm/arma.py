@@ -437,10 +437,9 @@ def fit_glm_arma11(
         fb_voxels = 0.0  # voxels the full grid decided (host numbers the search reads back anyway)
     for v0 in range(0, V, bs):
         v1 = min(V, v0 + bs)
-        if (use_graph and T % 4 == 0 and not Y.is_cuda and Y.dtype == torch.float32 and Y.is_pinned()
-                and Y.is_contiguous()):
-            # pinned host data: the graph's prep streams the rows in place, so
-            # the transfer overlaps with the grid build and the prep
+        if use_graph and not Y.is_cuda and Y.dtype == torch.float32 and Y.is_pinned() and Y.is_contiguous():
+            # pinned host data: a staged plan copies the rows in by chunks
+            # beside the grid build and preps each chunk as it lands
             Yb = Y[v0:v1]
         else:
             Yb = Y[v0:v1].to(device=device, dtype=torch.float32, non_blocking=True)

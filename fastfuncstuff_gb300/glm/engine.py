@@ -537,7 +537,8 @@ def design_basis(X: torch.Tensor, with_constant: bool = False):
 def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core: bool = True,
          idx: torch.Tensor | None = None, want_yr_t: bool = True, layout: RunLayout | None = None,
          scale: torch.Tensor | None = None, want_rows: bool = False, q0: torch.Tensor | None = None,
-         split: bool = True, y_ref: torch.Tensor | None = None, y_copy: torch.Tensor | None = None) -> PrepOut:
+         split: bool = True, y_ref: torch.Tensor | None = None, y_copy: torch.Tensor | None = None,
+         out: PrepOut | None = None) -> PrepOut:
     """Per-voxel scaling and residualisation (and the fp16 split for the GEMM).
 
     With ``tensor_core`` and ``split=False`` only the split's exponents
@@ -555,6 +556,10 @@ def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core:
     from instead of Y's -- device memory or pinned host memory mapped into
     the device's address space (``device_view``) -- and ``y_copy`` ([V][T])
     receives the rows as read; Y then only gives the shape.
+
+    ``out`` gives the buffers to write (its scale, yexp, feats and rows, of
+    the rows processed; e.g. views of a larger prep's outputs) instead of new
+    ones; the formed outputs it lacks are allocated.
     """
     lib = _lib.load()
     dev = Y.device
@@ -563,17 +568,30 @@ def prep(Y: torch.Tensor, f: GridFactors, *, do_scale: bool = True, tensor_core:
     K, ld = f.K, f.ld
     if y_ref is None:
         Y = Y.to(dtype=torch.float32).contiguous()
+    given = {} if out is None else {k: getattr(out, k, None) for k in ("scale", "yexp", "feats", "rows")}
+    if scale is None:
+        scale = given.get("scale")
     if scale is None:
         scale = torch.empty(V, dtype=torch.float32, device=dev)
     yr_t = torch.empty(T, n, dtype=torch.float32, device=dev) if want_yr_t else None
     yr_hi = torch.empty(n, ld, dtype=torch.int16, device=dev) if tensor_core and split else None
     yr_lo = torch.empty(n, ld, dtype=torch.int16, device=dev) if tensor_core and split else None
-    yexp = torch.empty(n, dtype=torch.int32, device=dev) if tensor_core else None
+    yexp = None
+    if tensor_core:
+        yexp = given.get("yexp")
+        if yexp is None:
+            yexp = torch.empty(n, dtype=torch.int32, device=dev)
     feats = rs = None
     if layout is not None:
-        feats = torch.empty(n, 9, dtype=torch.float32, device=dev)
+        feats = given.get("feats")
+        if feats is None:
+            feats = torch.empty(n, 9, dtype=torch.float32, device=dev)
         rs = const_dev(layout.run_start, dev)
-    rows = torch.empty(n, T, dtype=torch.float32, device=dev) if want_rows else None
+    rows = None
+    if want_rows:
+        rows = given.get("rows")
+        if rows is None:
+            rows = torch.empty(n, T, dtype=torch.float32, device=dev)
     if q0 is None:
         q0 = f.U[f.grid.p0]  # orthonormal basis of the design columns ([K][T]): U of (0, 0)
     pa = _lib.PrepArgs(V=n, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=0, ld_y=ld,

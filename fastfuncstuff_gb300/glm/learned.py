@@ -248,6 +248,7 @@ def _grid_consts(g: RemlGrid, dev):
 
 
 STRIP_MAX = 64  # most pairs one ffs_reml_strip call takes
+STAGE_CHUNKS = 8  # chunks of rows a staged run copies in and preps one after another
 STRIP_K0 = 2  # voxels whose answer lies this close to the identity line get the strip next to it
 
 
@@ -367,10 +368,21 @@ class WindowState:
     stats: dict
 
 
+def learned_prep(Y: torch.Tensor, factors: engine.GridFactors, layout: RunLayout, *, do_scale: bool = True,
+                 q0: torch.Tensor | None = None, y_ref: torch.Tensor | None = None,
+                 out: engine.PrepOut | None = None) -> engine.PrepOut:
+    """The prep of the learned-seeded search: each voxel's scale, its
+    residualised rows (voxel-major), the exponents of their fp16 split and
+    the proposal's features (into ``out``'s buffers when given)."""
+    return engine.prep(Y, factors, do_scale=do_scale, tensor_core=True, want_yr_t=False, layout=layout,
+                       want_rows=True, q0=q0, split=False, y_ref=y_ref, y_copy=Y if y_ref is not None else None,
+                       out=out)
+
+
 def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaProposal, layout: RunLayout, *,
                     do_scale: bool = True, recenter: int = 0, q0: torch.Tensor | None = None,
                     join=None, strip_k0: int = STRIP_K0, y_ref: torch.Tensor | None = None,
-                    count_evals: bool = False) -> WindowState:
+                    count_evals: bool = False, pre: engine.PrepOut | None = None) -> WindowState:
     """The window rounds of the learned-seeded search, with no host round trip
     (so they also run inside a CUDA graph): prep with the proposal features,
     the MLP, the 5 x 5 window of every voxel, ``recenter`` re-centred rounds
@@ -381,7 +393,9 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
     ``join()`` is then called before their first use (they may be built on
     another stream meanwhile). With ``y_ref`` (engine.prep) the rows are read
     from the address it holds and written into Y as read. ``count_evals``
-    adds the number of (voxel, pair) criteria evaluated to the statistics."""
+    adds the number of (voxel, pair) criteria evaluated to the statistics.
+    ``pre`` (learned_prep of every voxel) skips the prep; Y then only gives
+    the shape."""
     lib = _lib.load()
     dev = Y.device
     V, T = Y.shape
@@ -390,12 +404,13 @@ def learned_windows(Y: torch.Tensor, factors: engine.GridFactors, proposal: Arma
         raise ValueError("the learned search needs the tensor-core operands of the factors")
     g = f.grid
     st = _st()
-    if y_ref is None:
-        Y = Y.float().contiguous()
     c = _grid_consts(g, dev)
     # the windows' rows are split to fp16 while they are gathered (from rows)
-    p1 = engine.prep(Y, f, do_scale=do_scale, tensor_core=True, want_yr_t=False, layout=layout, want_rows=True,
-                     q0=q0, split=False, y_ref=y_ref, y_copy=Y if y_ref is not None else None)
+    p1 = pre
+    if p1 is None:
+        if y_ref is None:
+            Y = Y.float().contiguous()
+        p1 = learned_prep(Y, f, layout, do_scale=do_scale, q0=q0, y_ref=y_ref)
     scale = p1.scale
     prop = proposal.forward(p1.feats)
     center = torch.empty(V, dtype=torch.int32, device=dev)
@@ -548,18 +563,21 @@ class LearnedFitGraph:
     """
 
     def __init__(self, Y: torch.Tensor, X: torch.Tensor, grid: RemlGrid, layout: RunLayout,
-                 proposal: ArmaProposal, *, recenter: int, do_scale: bool, gls_kw: dict, factor_kw: dict):
+                 proposal: ArmaProposal, *, recenter: int, do_scale: bool, gls_kw: dict, factor_kw: dict,
+                 staged: bool = False):
         dev = X.device
         # the data's static buffer: the prep reads each run's rows from the
         # address in y_ref (device memory, or pinned host memory read in place)
         # and writes them here for the later stages
         self.Y = torch.empty(tuple(Y.shape), dtype=torch.float32, device=dev)
-        # rows read in place need 16-byte rows (T % 4 == 0); otherwise each run
-        # copies the data into the static buffer first
-        self.inplace = Y.shape[1] % 4 == 0
+        # staged: the data are copied in by the copy engine in chunks (see
+        # run); else rows are read in place when 16-byte rows allow it
+        # (T % 4 == 0), otherwise each run copies the data into the static
+        # buffer first
+        self.staged = staged
+        self.inplace = not staged and Y.shape[1] % 4 == 0
         self.y_ref = torch.zeros(1, dtype=torch.int64, device=dev)
         self.y_ref_host = torch.zeros(1, dtype=torch.int64, pin_memory=True)
-        self._set_source(Y)
         self.X = X.float().contiguous().clone()
         self.grid, self.layout, self.proposal = grid, layout, proposal
         self.recenter, self.do_scale, self.gls_kw, self.factor_kw = recenter, do_scale, gls_kw, factor_kw
@@ -568,6 +586,10 @@ class LearnedFitGraph:
         self.side = torch.cuda.Stream(dev)  # the grid build runs beside the prep chain
         self.side_fb = torch.cuda.Stream(self.Y.device)  # the fallback runs beside the window pairs' GLS
         self._fb_graphs: dict = {}
+        if staged:
+            self._init_staged(Y)
+            return
+        self._set_source(Y)
         # one eager pass fills the host-side caches (device constants, tensor
         # maps, kernel attributes) that a capture must not create
         self._body_a()
@@ -575,6 +597,88 @@ class LearnedFitGraph:
         self.ga = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.ga, capture_error_mode="thread_local"):
             self._body_a()
+
+    def _init_staged(self, Y: torch.Tensor) -> None:
+        """Graphs of a staged run: A0 (the design basis and the grid build),
+        one prep graph per chunk of rows, and A1 (the MLP, the window rounds
+        and the strip), with the prep's outputs in static buffers."""
+        dev = self.Y.device
+        V, T = self.Y.shape
+        step = -(-V // STAGE_CHUNKS)
+        step = -(-step // 32) * 32  # whole 32-voxel tiles of the prep
+        self.bounds = [(c0, min(V, c0 + step)) for c0 in range(0, V, step)]
+        self.copied = [torch.cuda.Event() for _ in self.bounds]
+        self.copy_stream = torch.cuda.Stream(dev)
+        self.prep_stream = torch.cuda.Stream(dev)
+        self.pre = engine.PrepOut(scale=torch.empty(V, dtype=torch.float32, device=dev), yr_t=None, yr_hi=None,
+                                  yr_lo=None, yexp=torch.empty(V, dtype=torch.int32, device=dev))
+        self.pre.feats = torch.empty(V, 9, dtype=torch.float32, device=dev)
+        self.pre.rows = torch.empty(V, T, dtype=torch.float32, device=dev)
+        self.Y.copy_(Y)
+        self._body_a0()
+        for i in range(len(self.bounds)):
+            self._body_prep(i)
+        self._body_a1()
+        torch.cuda.synchronize()
+        self.ga0 = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.ga0, capture_error_mode="thread_local"):
+            self._body_a0()
+        self.gp = []
+        for i in range(len(self.bounds)):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, capture_error_mode="thread_local"):
+                self._body_prep(i)
+            self.gp.append(g)
+        self.ga1 = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.ga1, capture_error_mode="thread_local"):
+            self._body_a1()
+
+    def _body_a0(self):
+        self.q0 = None
+        center = (self.cflag, self.ccoef)
+        if self.X.shape[1] <= engine.BASIS_MAX_K:
+            self.q0, cflag, ccoef = engine.design_basis(self.X, with_constant=True)
+            center = (cflag, ccoef)
+        self.f = engine.build_factors(self.X, self.grid, self.layout, center=center, **self.factor_kw)
+
+    def _body_prep(self, i: int):
+        c0, c1 = self.bounds[i]
+        pr = self.pre
+        view = engine.PrepOut(scale=pr.scale[c0:c1], yr_t=None, yr_hi=None, yr_lo=None, yexp=pr.yexp[c0:c1])
+        view.feats, view.rows = pr.feats[c0:c1], pr.rows[c0:c1]
+        learned_prep(self.Y[c0:c1], self.f, self.layout, do_scale=self.do_scale, q0=self.q0, out=view)
+
+    def _body_a1(self):
+        self.ws = learned_windows(self.Y, self.f, self.proposal, self.layout, do_scale=self.do_scale,
+                                  recenter=self.recenter, q0=self.q0, pre=self.pre)
+        self.host.copy_(self.ws.small, non_blocking=True)
+
+    def _replay_staged(self, Y: torch.Tensor) -> None:
+        """The copy engine brings Y in by chunks while graph A0 builds the
+        grid factors; each chunk's prep runs once both its rows and the
+        factors are there; graph A1 follows the last of them."""
+        if tuple(Y.shape) != tuple(self.Y.shape) or Y.dtype != torch.float32 or not Y.is_contiguous():
+            raise ValueError("the learned fit's graph reads float32 contiguous data of its own shape")
+        main = torch.cuda.current_stream()
+        start = torch.cuda.Event()
+        start.record(main)  # the previous run's readers of the static buffers are behind it
+        cs, ps = self.copy_stream, self.prep_stream
+        cs.wait_event(start)
+        with torch.cuda.stream(cs):
+            for (c0, c1), ev in zip(self.bounds, self.copied):
+                self.Y[c0:c1].copy_(Y[c0:c1], non_blocking=True)
+                ev.record(cs)
+        self._src = Y  # kept alive until the copies have read it
+        self.ga0.replay()
+        built = torch.cuda.Event()
+        built.record(main)
+        ps.wait_event(built)
+        with torch.cuda.stream(ps):
+            for g, ev in zip(self.gp, self.copied):
+                ps.wait_event(ev)
+                g.replay()
+        main.wait_stream(ps)
+        self.ga1.replay()
 
     def _body_a(self):
         main = torch.cuda.current_stream()
@@ -617,20 +721,24 @@ class LearnedFitGraph:
 
     def run(self, Y: torch.Tensor, X: torch.Tensor, *, host_out: bool = False):
         """(LearnedOut, engine.GlsOut) of data Y (V, T) and design X (T, K).
-        Y may be a CUDA tensor or a pinned host tensor: the prep reads its rows
-        in place (over the host link for host memory) and the host-to-device
-        transfer overlaps with the grid build and the prep's work. With
+        Y is a CUDA tensor (the prep reads its rows in place) or, for a staged
+        plan, a pinned host tensor (copied in by chunks beside the grid build,
+        each chunk's prep as soon as its rows are there). With
         ``host_out`` the GLS outputs are pinned host tensors written by the
         kernels over the host link while they run (read them after a
         synchronisation of the current stream)."""
         main = torch.cuda.current_stream()
-        self._set_source(Y)
+        if not self.staged:
+            self._set_source(Y)
         self.X.copy_(X)
         if self.X.shape[1] > engine.BASIS_MAX_K:  # else graph A runs the centring test
             flag, coef = engine.constant_flag(self.X)
             self.cflag.copy_(flag)
             self.ccoef.copy_(coef)
-        self.ga.replay()
+        if self.staged:
+            self._replay_staged(Y)
+        else:
+            self.ga.replay()
         ready = torch.cuda.Event()
         ready.record()
         # the GLS of every voxel at its window pair, launched while graph A
@@ -727,17 +835,18 @@ _GRAPHS: dict = {}
 
 
 def graph_for(Y, X, grid, layout, proposal, *, recenter, do_scale, gls_kw, factor_kw) -> LearnedFitGraph:
-    """The cached LearnedFitGraph of this shape and these options (built on first use)."""
+    """The cached LearnedFitGraph of this shape and these options (built on
+    first use); host data (pinned memory) get a staged plan."""
     fk = tuple((k, None if v is None else v.key() if hasattr(v, "key") else np.asarray(v).tobytes())
                for k, v in sorted(factor_kw.items()))
     key = (tuple(Y.shape), tuple(X.shape), str(X.device), grid.a.tobytes(), grid.b.tobytes(), grid.lambda_fp32,
            layout.run_start.tobytes(), layout.tau.tobytes(), id(proposal.params), proposal.params._version,
-           recenter, do_scale, tuple(sorted(gls_kw.items())), fk)
+           recenter, do_scale, tuple(sorted(gls_kw.items())), fk, not Y.is_cuda)
     gr = _GRAPHS.get(key)
     if gr is None:
         while len(_GRAPHS) >= 2:  # a plan holds a few GB of static buffers
             _GRAPHS.pop(next(iter(_GRAPHS)))
         gr = LearnedFitGraph(Y, X, grid, layout, proposal, recenter=recenter, do_scale=do_scale, gls_kw=gls_kw,
-                             factor_kw=factor_kw)
+                             factor_kw=factor_kw, staged=not Y.is_cuda)
         _GRAPHS[key] = gr
     return gr
