@@ -474,8 +474,9 @@ def run_gb300(args) -> None:
     else:
         ms_l, st_l, l_l, clk_l = timed(kw_l, "learned")
         value = ws * V / (ms_l / 1e3)
-        # the learned step is replayed from CUDA graphs, which the per-call
-        # timer does not see into: its stage breakdown comes from an eager pass
+        # the learned step is mostly replayed from CUDA graphs, which the
+        # per-call timer does not see into: its stage breakdown comes from an
+        # eager pass
         ms_e, st_e, l_e, _ = timed(dict(kw_l, cuda_graphs=False), "learned_eager")
         quality, pair_evals, n_fb = learned_quality(args, w, Yd, Xd, kw, kw_l, prop, lay, g, tinfo)
         # the eager step's GLS launches cover every voxel and, again, the
@@ -487,7 +488,8 @@ def run_gb300(args) -> None:
     method = ("full grid, one design per HRF group (fit_glm_arma11_grouped)" if grouped else
               f"learned-seeded 5x5 window refine, {args.recenter} re-centred round, the strip next to the identity "
               f"line for voxels within 2 lattice steps of it, full grid for window edges and voxels a strip pair "
-              f"beats; replayed from CUDA graphs")
+              f"beats; window rounds and fallback replayed from CUDA graphs, the window pairs' GLS launched "
+              f"beside them")
     line = {
         "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_l, "higher_is_better": True, "scaling": "weak",
