@@ -36,6 +36,36 @@ import numpy as np
 F32 = np.float32
 F64 = np.float64
 
+
+class _AfniMode:
+    """Run-wide AFNI-faithful switch, as the reference keeps it
+    (fastfuncstuff/glm/arma.py:59-92): banded R, near-white pairs dropped from
+    the grid, AFNI's hierarchical ltop."""
+
+    on: bool = False
+    corcut: float = 1e-4
+
+
+AFNI_MODE = _AfniMode()
+
+
+def set_afni_mode(enabled: bool, corcut: float = 1e-4) -> None:
+    """Follows fastfuncstuff/glm/arma.py:85-92."""
+    AFNI_MODE.on = bool(enabled)
+    AFNI_MODE.corcut = float(corcut)
+
+
+def afni_bmax(a: float, lam: float, corcut: float) -> int:
+    """Off-diagonals AFNI keeps in R: the lag at which lam * rho^(k-1) has
+    fallen to corcut, rho = a clamped to [-0.9, 0.9]; 0 (R = I) below corcut,
+    1 for a pure MA(1). Follows fastfuncstuff/glm/arma.py:95-109."""
+    if abs(lam) < corcut:
+        return 0
+    rho = min(0.9, max(-0.9, a))
+    if rho == 0.0:
+        return 1
+    return 1 + int(math.ceil(math.log(corcut / abs(lam)) / math.log(abs(rho))))
+
 _LJ_RUN_SEPARATION = 66666  # fastfuncstuff/glm/arma.py:5968
 
 
@@ -133,6 +163,8 @@ def valid_grid(a_grid, b_grid, dtype=F32) -> Grid:
     ok &= gamma0 > 0
     lam = arma_lambda_f32(a32, b32, dtype)
     ok &= lam >= 0
+    if AFNI_MODE.on:  # near-white pairs fold into (0, 0) (arma.py:1031-1036)
+        ok &= (lam == 0) | (lam >= AFNI_MODE.corcut)
     a, b, lam = a32[ok], b32[ok], lam[ok]
     a_axis = np.array(sorted(set(a.tolist())), dtype=F32)
     b_axis = np.array(sorted(set(b.tolist())), dtype=F32)
@@ -178,12 +210,14 @@ def build_censor_run_info(run_starts, n_total: int, good_list=None):
 # --------------------------------------------------------- correlation / whitener
 
 
-def corr_block(a: float, lam: float, taus: np.ndarray, dtype=F64) -> np.ndarray:
+def corr_block(a: float, lam: float, taus: np.ndarray, dtype=F64, band: int | None = None) -> np.ndarray:
     """Dense ARMA(1,1) correlation of one run block: R_ij = corr[|tau_i - tau_j|].
 
     corr = [1, lam, lam*a, lam*a^2, ...]. Follows
     fastfuncstuff/glm/arma.py:1057-1073 (lambda is the float32 value, the powers
-    of a are taken in ``dtype`` as the reference's type promotion does).
+    of a are taken in ``dtype`` as the reference's type promotion does). With
+    ``band`` the correlations at |tau_i - tau_j| > band are zero (AFNI's banded
+    R, arma.py:1075-1089; band 0 is the identity).
     """
     taus = np.asarray(taus, dtype=np.int64)
     dist = np.abs(taus[:, None] - taus[None, :])
@@ -195,6 +229,8 @@ def corr_block(a: float, lam: float, taus: np.ndarray, dtype=F64) -> np.ndarray:
         if max_lag >= 2:
             ex = np.arange(1, max_lag, dtype=dtype)
             corr[2:] = dtype(lam) * (dtype(a) ** ex)
+    if band is not None:
+        corr[band + 1:] = 0.0
     return corr[dist]
 
 
@@ -256,11 +292,15 @@ def arma11_whiteners(grid: Grid, n: int, run_starts=None, tau=None, dtype=F64):
     bounds = run_bounds(n, run_starts)
     lens = [e - s for s, e in bounds]
     whs, logdet = [], np.zeros(grid.n, dtype=dtype)
+
+    def band(g):
+        return afni_bmax(float(grid.a[g]), float(grid.lam[g]), AFNI_MODE.corcut) if AFNI_MODE.on else None
+
     if tau is None:
         m_max = max(lens)
         taus = np.arange(m_max)
         for g in range(grid.n):
-            R = corr_block(float(grid.a[g]), float(grid.lam[g]), taus, dtype)
+            R = corr_block(float(grid.a[g]), float(grid.lam[g]), taus, dtype, band(g))
             Linv, logdiag = _chol_inv(R)
             cum = np.cumsum(logdiag)
             logdet[g] = 2 * sum(cum[m - 1] for m in lens)
@@ -270,7 +310,7 @@ def arma11_whiteners(grid: Grid, n: int, run_starts=None, tau=None, dtype=F64):
     for g in range(grid.n):
         blocks, ld = [], 0.0
         for s, e in bounds:
-            R = corr_block(float(grid.a[g]), float(grid.lam[g]), tau[s:e], dtype)
+            R = corr_block(float(grid.a[g]), float(grid.lam[g]), tau[s:e], dtype, band(g))
             Linv, logdiag = _chol_inv(R)
             ld = ld + 2 * logdiag.sum()
             blocks.append((s, e, Linv))
@@ -896,6 +936,7 @@ def fit_glm_arma11(data, design, tr=2.0, a_grid=None, b_grid=None, *, use_double
     reference's default CPU run (arma.py:4699-4709).
     """
     dt = F64 if use_double else F32
+    afni_faithful = afni_faithful or AFNI_MODE.on
     Y = np.asarray(data)
     if Y.ndim == 4:
         Y = Y.reshape(-1, Y.shape[-1])

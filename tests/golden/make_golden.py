@@ -17,6 +17,8 @@ Cases (all on ``device=cpu``):
 * ``censored`` two runs with censored TRs (``tau`` from build_censor_run_info)
 * ``grouped``  fit_glm_arma11_grouped with three per-group designs
 * ``afni``     the default AFNI grid (9 x 17), default selector only
+* ``afni_faithful`` ``set_afni_mode(True)``: the banded covariance, AFNI's
+               grid filter and ltop; two runs, and two censored runs
 * ``baseline`` a raw 1000-baseline series (the conditioning test's shape)
 * ``ljung``    the reference test-suite's Ljung-Box series and AFNI golden values
 * ``grid``     logdet(R), logdet(X_w'X_w), X_w and Q of a small precompute
@@ -147,6 +149,26 @@ def main(ref_root: str, only: str | None = None) -> None:
             if r.ljung_box_dof is not None:
                 out[f"{name}__ljung_box_dof"] = np.array(r.ljung_box_dof)
         return out
+
+    # AFNI-faithful mode (banded R, near-white pairs dropped, AFNI's ltop):
+    # two runs, then two censored runs (the band counts tau, not rows)
+    arma.set_afni_mode(True)
+    try:
+        out = {}
+        X, Y, _ = _case(30, [80, 80], V=150)
+        out.update({f"runs_{k}": v for k, v in modes(X, Y, a_grid=g17, b_grid=g17, run_starts=[0, 80]).items()})
+        Xc, Yc, keep = _case(31, [70, 74], V=100, censor=10)
+        starts, tau = build_censor_run_info([0, 70], 144, keep.tolist())
+        out.update({f"cens_{k}": v for k, v in modes(Xc, Yc, a_grid=g17, b_grid=g17, run_starts=starts,
+                                                     tau=tau).items()})
+    finally:
+        arma.set_afni_mode(False)
+    np.savez_compressed(OUT / "afni_faithful.npz", X=X, Y=Y, Xc=Xc, Yc=Yc, a_grid=g17.numpy(),
+                        b_grid=g17.numpy(), run_starts=np.array([0, 80]), cens_run_starts=np.array(starts),
+                        tau=tau.numpy(), keep=keep, corcut=np.array(1e-4), **out)
+    if only == "afni_faithful":
+        print("wrote", OUT / "afni_faithful.npz")
+        return
 
     # global ARMA: (a, b) estimated once from the mean series
     X, Y, _ = _case(22, [60, 60], p_task=2, V=150)

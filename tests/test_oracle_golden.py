@@ -318,3 +318,61 @@ def test_global_arma_matches_reference():
     r = o.fit_glm_arma11(d["Y"], d["X"], use_double=False, **kw)
     np.testing.assert_array_equal(r.arma_params, d["f32__arma_params"])
     _close(r.betas, d["f32__betas"], rtol=2e-3, atol=2e-3)
+
+
+@pytest.fixture
+def afni_mode():
+    o.set_afni_mode(True)
+    yield
+    o.set_afni_mode(False)
+
+
+def afni_faithful_case(d, tag):
+    """(Y, X, fit options) of the two afni_faithful cases (make_golden.py)."""
+    if tag == "runs":
+        return d["Y"], d["X"], dict(a_grid=d["a_grid"], b_grid=d["b_grid"], run_starts=d["run_starts"])
+    return d["Yc"], d["Xc"], dict(a_grid=d["a_grid"], b_grid=d["b_grid"], run_starts=d["cens_run_starts"],
+                                  tau=d["tau"])
+
+
+def test_afni_bmax_known_values():
+    # the band of AFNI's rcmat_arma11: last kept lag where lam * a^(k-1) ~ corcut
+    assert o.afni_bmax(0.5, 5e-5, 1e-4) == 0  # below corcut: R = I
+    assert o.afni_bmax(0.0, 0.3, 1e-4) == 1  # pure MA(1)
+    assert o.afni_bmax(0.5, 0.5, 1e-4) == 1 + int(np.ceil(np.log(2e-4) / np.log(0.5)))
+    assert o.afni_bmax(0.95, 0.9, 1e-4) == o.afni_bmax(0.9, 0.9, 1e-4)  # a clamped to 0.9
+    assert o.afni_bmax(-0.6, 0.2, 1e-4) == o.afni_bmax(0.6, 0.2, 1e-4)
+
+
+@pytest.mark.parametrize("tag", ["runs", "cens"])
+def test_afni_faithful_matches_reference(tag, afni_mode):
+    """set_afni_mode(True): the banded R (fastfuncstuff/glm/arma.py:95-109,
+    :918-926, :1075-1089), the grid filter (:1031-1036) and AFNI's ltop."""
+    d = load_golden("afni_faithful")
+    Y, X, kw = afni_faithful_case(d, tag)
+    r = o.fit_glm_arma11(Y, X, use_double=True, force_exhaustive_search=True, save_profile_likelihoods=True,
+                         **kw)
+    ref = f"{tag}_f64_exh__"
+    np.testing.assert_array_equal(r.arma_params, d[ref + "arma_params"])
+    _close(r.reml_lklhd_surface, d[ref + "reml_lklhd_surface"], rtol=2e-5)
+    _close(r.reml_likelihood, d[ref + "reml_likelihood"], rtol=1e-8, atol=1e-5)
+    for name in ("betas", "tstats", "fstats"):
+        _close(getattr(r, name), d[ref + name], rtol=1e-6, atol=1e-6)
+    _close(r.sigma2, d[ref + "sigma2"], rtol=1e-7)
+    r = o.fit_glm_arma11(Y, X, use_double=True, **kw)
+    ref = f"{tag}_f64_def__"
+    np.testing.assert_array_equal(r.arma_params, d[ref + "arma_params"])
+    _close(r.reml_likelihood, d[ref + "reml_likelihood"], rtol=1e-8, atol=1e-5)
+    _close(r.betas, d[ref + "betas"], rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("tag", ["runs"])
+def test_afni_faithful_band_changes_the_answer(tag, afni_mode):
+    """The banded R is not the dense one: the same fit without AFNI mode gives
+    other likelihoods (and the golden fixture was made in AFNI mode)."""
+    d = load_golden("afni_faithful")
+    Y, X, kw = afni_faithful_case(d, tag)
+    r = o.fit_glm_arma11(Y, X, use_double=True, force_exhaustive_search=True, **kw)
+    o.set_afni_mode(False)
+    dense = o.fit_glm_arma11(Y, X, use_double=True, force_exhaustive_search=True, **kw)
+    assert np.abs(r.reml_likelihood - dense.reml_likelihood).max() > 1e-7
