@@ -21,6 +21,7 @@ _c_u16_p = C.POINTER(C.c_uint16)
 
 FFS_OK, FFS_ERR_INVALID, FFS_ERR_CUDA, FFS_ERR_UNSUPPORTED, FFS_ERR_WORKSPACE, FFS_ERR_TIMEOUT = range(6)
 FFS_DSORT_QMAX = 16  # most voxelwise columns of ffs_reml_gls_dsort
+FFS_BAND_MAX_W = 129  # widest row of the AFNI-faithful banded R (128 off-diagonals)
 
 
 class GridDesc(C.Structure):
@@ -30,6 +31,7 @@ class GridDesc(C.Structure):
         ("X", C.c_void_p), ("lambda_fp32", C.c_int), ("ld_u", C.c_int),
         ("n_task", C.c_int), ("task_idx", C.c_void_p), ("n_glt", C.c_int), ("glt", C.c_void_p),
         ("n_sets", C.c_int), ("set_ptr", C.c_void_p), ("set_idx", C.c_void_p),
+        ("band_w", C.c_int), ("band", C.c_void_p),
     ]
 
 
@@ -40,7 +42,7 @@ class GridOut(C.Structure):
         ("G", C.c_void_p),
         ("Adiag", C.c_void_p), ("XtX", C.c_void_p), ("info", C.c_void_p), ("Ftask", C.c_void_p),
         ("glt_var", C.c_void_p), ("Gsum", C.c_void_p), ("work", C.c_void_p), ("Fsets", C.c_void_p),
-        ("Afull", C.c_void_p),
+        ("Afull", C.c_void_p), ("band_L", C.c_void_p), ("band_coef", C.c_void_p),
     ]
 
 
@@ -105,6 +107,7 @@ class SurfaceArgs(C.Structure):
         ("logdet_XtX", C.c_void_p), ("proj", C.c_void_p), ("chunk_start", C.c_void_p),
         ("n_chunks", C.c_int), ("chunk_pairs", C.c_void_p), ("surf", C.c_void_p),
         ("crit0", C.c_void_p), ("tile_design", C.c_void_p),
+        ("band_coef", C.c_void_p), ("band_w", C.c_int), ("band", C.c_void_p),
     ]
 
 
@@ -130,6 +133,7 @@ class GlsArgs(C.Structure):
         ("fstats", C.c_void_p), ("r2", C.c_void_p), ("lam", C.c_void_p),
         ("cbeta", C.c_void_p), ("ct", C.c_void_p), ("resid", C.c_void_p),
         ("resid_w", C.c_void_p), ("pred", C.c_void_p), ("center_dev", C.c_void_p), ("n_pairs", C.c_int),
+        ("band_coef", C.c_void_p), ("band_w", C.c_int), ("band", C.c_void_p),
     ]
 
 

@@ -40,6 +40,22 @@ __device__ __forceinline__ const float* quad_matrix(const ffs_gls_args& a, int g
   return a.n_task > 0 ? a.Ftask + (size_t)g * a.n_task * a.n_task : a.XtX + (size_t)g * a.K * a.K;
 }
 
+// Whitening against AFNI's banded R: w_t = r_t c[t][0] - sum_j c[t][j] w_{t-j}
+// for j up to the pair's band (rows past a run start or a censoring gap have
+// zero coefficients there), by one thread over the whole series; r and w may
+// be the same array (w_{t-j} is then read where it was written).
+__device__ __forceinline__ void band_whiten(const ffs_gls_args& a, int p, const float* r, float* w, int T) {
+  const int W = a.band_w, bw = a.band[p];
+  const float* cb = a.band_coef + (size_t)p * T * W;
+  for (int t = 0; t < T; ++t) {
+    const float* c = cb + (size_t)t * W;
+    float acc = r[t] * c[0];
+    const int jm = min(bw, t);
+    for (int j = 1; j <= jm; ++j) acc = fmaf(-c[j], w[t - j], acc);
+    w[t] = acc;
+  }
+}
+
 // GLS of one voxel v at pair g, executed by one warp. Gp = G of pair g and Xt
 // (the transposed design) may live in shared or global memory; ys, r, beta and
 // bins are this warp's shared scratch.
@@ -113,7 +129,9 @@ __device__ void gls_voxel(const ffs_gls_args& a, const GlsExtra& x, const int v,
   __syncwarp();
   // whitened residual r_w = L^-1 r (serial recurrence on lane 0), into ys
   const float4* cf = reinterpret_cast<const float4*>(a.coef) + (size_t)pair_of(a, g) * T;
-  if (lane == 0) {
+  if (a.band_coef) {
+    if (lane == 0) band_whiten(a, pair_of(a, g), r, ys, T);
+  } else if (lane == 0) {
     float rp = 0.f, vp = 0.f;
     for (int t = 0; t < T; ++t) {
       const float4 q = cf[t];
@@ -550,6 +568,18 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
   __syncthreads();
   float4* rr = reinterpret_cast<float4*>(Ys + (size_t)lane * ld);
 
+  if (a.band_coef) {
+    // the banded R's whitening: one lane per voxel over the whole series, in
+    // place, and the whitened sum of squares
+    if (wid == 0) {
+      float* row = Ys + (size_t)lane * ld;
+      band_whiten(a, pair_of(a, g), row, row, T);
+      float ssw = 0.f;
+      for (int t = 0; t < T; ++t) ssw = fmaf(row[t], row[t], ssw);
+      st[5 * TILE_V + lane] = ssw;
+    }
+    __syncthreads();
+  } else {
   // whitened residual by segments of the time axis
   const int SQ = (nq + TILE_WARPS - 1) / TILE_WARPS;
   const int s0 = min(T, wid * SQ * 4), s1 = min(T, (wid + 1) * SQ * 4);
@@ -616,6 +646,7 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) gls_tile_kernel(ffs_gls_ar
     st[5 * TILE_V + lane] = s;
   }
   __syncthreads();
+  }
 
   if (x.lj_h > 0 && x.ljung_box) {
     // per-voxel statistics with the Ljung-Box lags: warp w takes voxels w, w + 8, ...

@@ -304,6 +304,95 @@ __device__ __forceinline__ void ldl_of_pair(const ffs_grid_desc& d, const ffs_gr
   __syncthreads();
 }
 
+// Phase 1 of an item with AFNI's banded R (d.band): the Cholesky factor of
+// each run's block of R, where R(t, k) = lam a^(g-1) for 1 <= g = tau_t -
+// tau_k <= band[p] and 0 beyond. One warp per run, rows in order; row t has
+// J_t earlier rows of its run within the band (zero at a run start), and its
+// off-diagonal entries L(t, t - j) solve the triangular system of those rows
+// against R(t, t - j): the lanes hold the right-hand side (lane l the terms
+// j = l + 1 + 32 q), each solved entry is broadcast and taken off the terms
+// not yet solved. The diagonal is sqrt(1 - sum_j L(t, t - j)^2); a pivot that
+// is not positive flags the pair (bad_r) and is replaced by 1. FP64
+// throughout; band_L keeps the factor, band_coef its fp32 whitening
+// coefficients, invdiag and Jrow (shared memory) the reciprocal diagonal and
+// each row's band for phases 2 and 6. logdet_R = 2 sum log(L(t, t) + 1e-10)
+// as the reference takes it from its dense factor; coef is the identity.
+__device__ void band_chol_of_pair(const ffs_grid_desc& d, const ffs_grid_out& o, int p, double* invdiag, int* Jrow,
+                                  double* apow, double* red, int* bad_r) {
+  const int T = d.T, W = d.band_w, bw = d.band[p];
+  const float af = d.a[p], bf = d.b[p];
+  const double a = (double)af;
+  const double lam = d.lambda_fp32 ? (double)lambda_f32(af, bf) : lambda_f64(a, (double)bf);
+  double* Lb = o.band_L + (size_t)p * T * W;
+  float* Cb = o.band_coef + (size_t)p * T * W;
+  if (threadIdx.x == 0) {
+    *bad_r = 0;
+    double x = 1.0;
+    for (int k = 0; k < W; ++k) {  // a^k: corr(g) = lam a^(g - 1), 1 <= g < W
+      apow[k] = x;
+      x *= a;
+    }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int r = warp; r < d.n_runs; r += nw) {
+    const int t0 = d.run_start[r], t1 = d.run_start[r + 1];
+    for (int t = t0; t < t1; ++t) {
+      const int tt = d.tau[t];
+      int J = 0;
+      while (J < t - t0 && J < W - 1 && tt - d.tau[t - J - 1] <= bw) ++J;
+      double rj[4], own = 0.0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = lane + 1 + 32 * q;
+        rj[q] = (j <= J && lam != 0.0) ? lam * apow[tt - d.tau[t - j] - 1] : 0.0;
+      }
+      for (int j = J; j >= 1; --j) {
+        const int q = (j - 1) >> 5, owner = (j - 1) & 31;
+        const double mine = q == 0 ? rj[0] : q == 1 ? rj[1] : q == 2 ? rj[2] : rj[3];
+        const double ell = __shfl_sync(0xffffffffu, mine, owner) * invdiag[t - j];
+        if (lane == owner) {
+          Lb[(size_t)t * W + j] = ell;
+          own = fma(ell, ell, own);
+        }
+#pragma unroll
+        for (int qq = 0; qq < 4; ++qq) {
+          const int jp = lane + 1 + 32 * qq;  // the term of row t - jp, column t - j
+          if (jp < j && j - jp <= Jrow[t - jp]) rj[qq] -= ell * Lb[(size_t)(t - jp) * W + (j - jp)];
+        }
+      }
+      __syncwarp();  // the row's entries, written by their owner lanes, are read below
+      double d2 = 1.0 - warp_sum_d(own);
+      if (!(d2 > 0.0)) {
+        if (lane == 0) *bad_r = 1;
+        d2 = 1.0;
+      }
+      const double ltt = sqrt(d2);
+      const double inv = 1.0 / ltt;
+      for (int j = lane; j < W; j += 32) {
+        const double v = j == 0 ? ltt : (j <= J ? Lb[(size_t)t * W + j] : 0.0);
+        if (j > J) Lb[(size_t)t * W + j] = 0.0;
+        if (j == 0) Lb[(size_t)t * W] = ltt;
+        Cb[(size_t)t * W + j] = (float)(j == 0 ? inv : v * inv);
+      }
+      if (lane == 0) {
+        invdiag[t] = inv;
+        Jrow[t] = J;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  double ld = 0.0;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    ld += 2.0 * log(Lb[(size_t)t * W] + 1e-10);
+    reinterpret_cast<float4*>(o.coef)[(size_t)p * T + t] = make_float4(0.f, 0.f, 1.f, 1.f);
+  }
+  ld = block_sum(ld, red);
+  if (threadIdx.x == 0) o.logdet_R[p] = ld;
+  __syncthreads();
+}
+
 // Phase 1 of every pair once, for the items of all designs (coef and
 // logdet_R depend on the pair only): cm [P][T][4] and bad [P] in the
 // workspace, read back by grid_build_kernel.
@@ -347,13 +436,30 @@ __global__ void __launch_bounds__(GB_THREADS, 4) grid_build_kernel(BuildArgs arg
       for (int i = threadIdx.x; i < 2 * T; i += blockDim.x) reinterpret_cast<double2*>(cms)[i] = src[i];
       if (threadIdx.x == 0) bad_r = pair_bad[p];
       __syncthreads();
+    } else if (d.band) {
+      band_chol_of_pair(d, o, p, cms, reinterpret_cast<int*>(cms + T), cms + T + (T + 1) / 2, red, &bad_r);
     } else {
       ldl_of_pair(d, o, p, cms, red, &bad_r);
     }
 
     // ---- 2. X_w = L^-1 X, one column per thread; the design samples of
-    // GB_PF steps are loaded ahead of the recursion that needs them
-    for (int j = threadIdx.x; j < K; j += blockDim.x) {
+    // GB_PF steps are loaded ahead of the recursion that needs them (with the
+    // banded R: forward substitution against the band of each row)
+    if (d.band) {
+      const int W = d.band_w;
+      const double* Lb = o.band_L + (size_t)p * T * W;
+      const int* Jrow = reinterpret_cast<const int*>(cms + T);
+      for (int j = threadIdx.x; j < K; j += blockDim.x) {
+        double* xw = s.Xw + (size_t)j * T;
+        for (int t = 0; t < T; ++t) {
+          double acc = f2d_exact(__ldg(Xd + (size_t)t * K + j));
+          const double* row = Lb + (size_t)t * W;
+          for (int i = 1; i <= Jrow[t]; ++i) acc = fma(-row[i], xw[t - i], acc);
+          xw[t] = acc * cms[t];
+        }
+      }
+    }
+    for (int j = threadIdx.x; j < K && !d.band; j += blockDim.x) {
       double xp = 0.0, vp = 0.0;
       for (int t0 = 0; t0 < T; t0 += GB_PF) {
         float xb[GB_PF];
@@ -465,7 +571,27 @@ __global__ void __launch_bounds__(GB_THREADS, 4) grid_build_kernel(BuildArgs arg
     // the fp32 coefficients of phase 1
     const float4* cf = reinterpret_cast<const float4*>(o.coef) + (size_t)p * T;
     float umax_local = 0.f;
-    for (int j = threadIdx.x; j < K; j += blockDim.x) {
+    if (d.band) {
+      // back substitution against the band: u_t = (q_t - sum_i L(t + i, t)
+      // u_{t+i}) / L(t, t), the rows t + i of t's run within the band
+      const int W = d.band_w;
+      const double* Lb = o.band_L + (size_t)p * T * W;
+      const int* Jrow = reinterpret_cast<const int*>(cms + T);
+      for (int j = threadIdx.x; j < K; j += blockDim.x) {
+        const float* q = qf + (size_t)j * T;
+        float* u = uf + (size_t)j * T;
+        for (int t = T - 1; t >= 0; --t) {
+          double acc = (double)q[t];
+          for (int i = 1; t + i < T && i <= Jrow[t + i]; ++i) acc = fma(-Lb[(size_t)(t + i) * W + i], (double)u[t + i], acc);
+          const float ut = (float)(acc * cms[t]);
+          u[t] = ut;
+          o.U[((size_t)pd * K + j) * LT + t] = ut;
+          umax_local = fmaxf(umax_local, fabsf(ut));
+        }
+        for (int t = T; t < LT; ++t) o.U[((size_t)pd * K + j) * LT + t] = 0.f;
+      }
+    }
+    for (int j = threadIdx.x; j < K && !d.band; j += blockDim.x) {
       const float* q = qf + (size_t)j * T;
       float* u = uf + (size_t)j * T;
       float xn = 0.f, mn = 0.f, cn = 0.f;  // x_{t+1}, m_{t+1}, c_{t+1}
@@ -838,8 +964,15 @@ extern "C" int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, voi
   FFS_REQUIRE(o->coef && o->logdet_R && o->logdet_XtX && o->U && o->G && o->Adiag && o->XtX &&
                   o->info && o->work,
               "ffs_grid_build: null output");
+  FFS_REQUIRE(!d->band || (d->band_w >= 1 && d->band_w <= FFS_BAND_MAX_W && o->band_L && o->band_coef),
+              "ffs_grid_build: the banded R needs 1 <= band_w=%d <= %d, band_L and band_coef", d->band_w,
+              FFS_BAND_MAX_W);
   BuildArgs args{*d, *o};
-  const size_t smem = sizeof(double) * 4 * (size_t)d->T;
+  // shared memory: [T][4] doubles, or with the band invdiag [T], Jrow [T]
+  // (ints) and the powers of a [band_w]
+  size_t smem = sizeof(double) * 4 * (size_t)d->T;
+  if (d->band)
+    smem = std::max(smem, sizeof(double) * ((size_t)d->T + (d->T + 1) / 2 + (size_t)d->band_w + 1));
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build: T=%d too long", d->T);
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel<false>), smem));
   grid_build_kernel<false><<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, 1, nullptr, nullptr);
@@ -855,6 +988,7 @@ extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int
   FFS_REQUIRE(d->T > 0 && d->K > 0 && d->P > 0 && d->n_runs > 0,
               "ffs_grid_build_designs: T=%d K=%d P=%d n_runs=%d must be positive", d->T, d->K, d->P, d->n_runs);
   FFS_REQUIRE((long long)d->P * n_designs < (1LL << 31), "ffs_grid_build_designs: too many items");
+  FFS_REQUIRE(!d->band, "ffs_grid_build_designs: the banded R is built by ffs_grid_build (one design)");
   FFS_REQUIRE(d->K <= d->T, "ffs_grid_build_designs: K=%d exceeds T=%d", d->K, d->T);
   FFS_REQUIRE(d->n_task >= 0 && d->n_task <= d->K, "ffs_grid_build_designs: bad n_task=%d", d->n_task);
   if (const int rc = check_sets(d, o, "ffs_grid_build_designs")) return rc;
@@ -953,6 +1087,7 @@ extern "C" int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out
   FFS_REQUIRE(d->run_start && d->tau && d->a && d->b && d->X, "ffs_grid_build_noalloc: null input");
   FFS_REQUIRE(o->coef && o->logdet_R && o->logdet_XtX && o->U && o->G && o->Adiag && o->XtX && o->info,
               "ffs_grid_build_noalloc: null output");
+  FFS_REQUIRE(!d->band, "ffs_grid_build_noalloc: the banded R is built by ffs_grid_build");
   const size_t need = sizeof(double) * pair_doubles(d->T, d->K) * (size_t)d->P;
   if (need > kStaticGridScratchBytes) {
     set_error("ffs_grid_build_noalloc: T=%d K=%d P=%d needs %zu bytes of scratch, above the %zu-byte static "

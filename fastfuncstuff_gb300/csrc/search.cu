@@ -498,6 +498,63 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
   if (chunk == 0) a.crit0[v] = (a.logdet_R[a.p0] + ldx[a.p0]) + (double)Tk * log((double)rss0 + 1e-10);
 }
 
+// ------------------------------------------------------------- banded surface
+// AFNI's banded R: one CTA per (pair, tile of SB_THREADS voxels), one thread
+// per voxel. Each step forms w_t = y_t c[t][0] - sum_{j <= band} c[t][j] w_{t-j}
+// against the last band_w - 1 values of w, kept per thread in a ring in
+// shared memory ([slot][thread], so a warp's accesses fall in distinct banks);
+// the coefficients of SB_STEPS steps are staged in shared memory at a time
+// and read by every thread (broadcast). y'R^-1 y = sum w_t^2, and the
+// criterion as the surface kernel forms it.
+constexpr int SB_THREADS = 128;
+constexpr int SB_STEPS = 32;
+
+__global__ void __launch_bounds__(SB_THREADS) surface_band_kernel(ffs_surface_args a) {
+  extern __shared__ float sbm[];
+  const int W = a.band_w, T = a.T;
+  float* ring = sbm;                                  // [W][SB_THREADS]
+  float* cs = ring + (size_t)W * SB_THREADS;          // [SB_STEPS][W]
+  const int p = blockIdx.x, bw = a.band[p];
+  const int tid = threadIdx.x;
+  const int v = blockIdx.y * SB_THREADS + tid;
+  const bool live = v < a.V;
+  const float* cb = a.band_coef + (size_t)p * T * W;
+  for (int i = tid; i < W * SB_THREADS; i += blockDim.x) ring[i] = 0.f;
+  float yy = 0.f, ssw = 0.f;
+  int pos = 0;  // the ring slot of step t
+  for (int c0 = 0; c0 < T; c0 += SB_STEPS) {
+    const int cn = min(SB_STEPS, T - c0);
+    __syncthreads();  // the previous chunk's coefficients are no longer read
+    for (int i = tid; i < cn * W; i += blockDim.x) cs[i] = cb[(size_t)c0 * W + i];
+    __syncthreads();
+    for (int s = 0; s < cn; ++s) {
+      const int t = c0 + s;
+      const float y = live ? a.yr_t[(size_t)t * a.V + v] : 0.f;
+      const float* c = cs + (size_t)s * W;
+      float acc = y * c[0];
+      const int jm = min(bw, t);
+      int q = pos;
+      for (int j = 1; j <= jm; ++j) {
+        q = q == 0 ? W - 1 : q - 1;
+        acc = fmaf(-c[j], ring[(size_t)q * SB_THREADS + tid], acc);
+      }
+      ring[(size_t)pos * SB_THREADS + tid] = acc;
+      pos = pos + 1 == W ? 0 : pos + 1;
+      yy = fmaf(y, y, yy);
+      ssw = fmaf(acc, acc, ssw);
+    }
+  }
+  if (!live) return;
+  const int Tk = a.T - a.K;
+  const double c_p0 = a.logdet_R[a.p0] + a.logdet_XtX[a.p0];
+  const float rss0 = fmaxf(yy - a.proj[(size_t)a.p0 * a.V + v], 0.f);
+  const float den = rss0 + 1e-10f;
+  const float rss = fmaxf(ssw - a.proj[(size_t)p * a.V + v], 0.f);
+  const float dc = (float)((a.logdet_R[p] + a.logdet_XtX[p]) - c_p0);
+  a.surf[(size_t)p * a.V + v] = dc + (float)Tk * log1pf((rss - rss0) / den);
+  if (p == 0) a.crit0[v] = c_p0 + (double)Tk * log((double)rss0 + 1e-10);
+}
+
 // ---------------------------------------------------------------------- select
 __global__ void select_kernel(ffs_select_args a) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -782,6 +839,19 @@ extern "C" int ffs_reml_prep(const ffs_prep_args* a, void* stream) {
 
 extern "C" int ffs_reml_surface(const ffs_surface_args* a, void* stream) {
   clear_error();
+  if (a && a->band_coef) {
+    FFS_REQUIRE(a->V > 0 && a->T > a->K && a->P > 0 && a->band_w >= 1 && a->band_w <= FFS_BAND_MAX_W,
+                "ffs_reml_surface: bad sizes for the banded R");
+    FFS_REQUIRE(a->p0 >= 0 && a->p0 < a->P, "ffs_reml_surface: p0=%d out of range", a->p0);
+    FFS_REQUIRE(a->yr_t && a->band && a->logdet_R && a->logdet_XtX && a->proj && a->surf && a->crit0 &&
+                    !a->tile_design,
+                "ffs_reml_surface: null buffer, or a grouped fit with the banded R");
+    FFS_REQUIRE(ceil_div(a->V, SB_THREADS) <= 65535, "ffs_reml_surface: V=%d exceeds one launch", a->V);
+    const size_t smem = sizeof(float) * (size_t)a->band_w * (SB_THREADS + SB_STEPS);
+    FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(surface_band_kernel), smem));
+    surface_band_kernel<<<dim3(a->P, ceil_div(a->V, SB_THREADS)), SB_THREADS, smem, (cudaStream_t)stream>>>(*a);
+    return check_launch("surface_band_kernel");
+  }
   FFS_REQUIRE(a && a->V > 0 && a->T > 0 && a->P > 0 && a->n_chunks > 0, "ffs_reml_surface: bad sizes");
   FFS_REQUIRE(a->p0 >= 0 && a->p0 < a->P, "ffs_reml_surface: p0=%d out of range", a->p0);
   FFS_REQUIRE(a->yr_t && a->coef && a->logdet_R && a->logdet_XtX && a->proj && a->chunk_start &&

@@ -233,6 +233,10 @@ class GridFactors:
     Fsets: torch.Tensor | None = None  # [n_designs * P][msum] column-set blocks
     sets: "ColumnSets | None" = None
     Afull: torch.Tensor | None = None  # [n_designs * P][K][K] (X_w'X_w)^-1
+    band: torch.Tensor | None = None  # AFNI-faithful banded R: int32 [P] band of each pair
+    band_w: int = 0                   # row stride of band_L / band_coef (max band + 1)
+    band_L: torch.Tensor | None = None  # [P][T][band_w] FP64 Cholesky rows of the banded R
+    band_coef: torch.Tensor | None = None  # [P][T][band_w] fp32 whitening coefficients
 
     @property
     def P(self) -> int:
@@ -433,6 +437,17 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     )
     if afull:
         f.Afull = torch.empty(DP, K, K, **f32)
+    if grid.band is not None:
+        # AFNI-faithful mode: R banded per pair, factored as a band
+        if not single:
+            raise NotImplementedError("the AFNI-faithful banded covariance (set_afni_mode) for grouped designs")
+        f.band_w = int(grid.band.max()) + 1
+        if f.band_w > _lib.FFS_BAND_MAX_W:
+            raise NotImplementedError(f"the AFNI-faithful band of {f.band_w - 1} lags exceeds "
+                                      f"{_lib.FFS_BAND_MAX_W - 1} (a grid with |a| near 1 or a small corcut)")
+        f.band = const_dev(grid.band, dev)
+        f.band_L = torch.empty(P, T, f.band_w, dtype=torch.float64, device=dev)
+        f.band_coef = torch.empty(P, T, f.band_w, **f32)
     if sets is not None and sets.n_sets:
         f.sets = sets
         f.Fsets = torch.empty(DP, sets.msum, **f32)
@@ -443,12 +458,12 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
                       a=_p(a), b=_p(b), X=_p(Xc), lambda_fp32=0, ld_u=ld,
                       n_task=nt, task_idx=_p(task_idx), n_glt=ng, glt=_p(glt_t),
                       n_sets=sets.n_sets if f.Fsets is not None else 0, set_ptr=_p(sets_dev[0]),
-                      set_idx=_p(sets_dev[1]))
+                      set_idx=_p(sets_dev[1]), band_w=f.band_w, band=_p(f.band))
     # no Gsum from the kernel: G'1 is the FP64 coefficient vector of the constant (set below)
     o = _lib.GridOut(coef=_p(f.coef), logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), U=_p(f.U),
                      U_hi=_p(f.U_hi), U_lo=_p(f.U_lo), uexp=_p(f.uexp), G=_p(f.G), Adiag=_p(f.Adiag), XtX=_p(f.XtX),
                      info=_p(f.info), Ftask=_p(f.Ftask), glt_var=_p(f.glt_var), Gsum=None, work=_p(work),
-                     Fsets=_p(f.Fsets), Afull=_p(f.Afull))
+                     Fsets=_p(f.Fsets), Afull=_p(f.Afull), band_L=_p(f.band_L), band_coef=_p(f.band_coef))
     def launch():
         if single:
             _run("ffs_grid_build", lib.ffs_grid_build, C.byref(d), C.byref(o), _stream())
@@ -648,7 +663,8 @@ def search(Y: torch.Tensor, f: GridFactors, *, hierarchical: bool = True, projec
     sa = _lib.SurfaceArgs(V=V, T=T, K=K, P=P, p0=f.grid.p0, yr_t=_p(pr.yr_t), coef=_p(f.coef),
                           logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), proj=_p(proj),
                           chunk_start=_p(f.chunk_start), n_chunks=f.chunk_start.numel() - 1,
-                          chunk_pairs=_p(f.chunk_pairs), surf=_p(surf), crit0=_p(crit0))
+                          chunk_pairs=_p(f.chunk_pairs), surf=_p(surf), crit0=_p(crit0),
+                          band_coef=_p(f.band_coef), band_w=f.band_w, band=_p(f.band))
     _run("ffs_reml_surface", lib.ffs_reml_surface, C.byref(sa), st)
 
     best = torch.empty(V, dtype=torch.int32, device=dev)
@@ -838,7 +854,8 @@ def gls(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridFactors
                       glt_var=_p(f.glt_var), betas=ptr(o.betas), tstats=ptr(o.tstats), sigma2=ptr(o.sigma2),
                       fstats=ptr(o.fstats), r2=ptr(o.r2), lam=ptr(o.lam), cbeta=_view(ptr, o.cbeta),
                       ct=_view(ptr, o.ct), resid=_view(ptr, o.resid), resid_w=_view(ptr, o.resid_w),
-                      pred=_view(ptr, o.pred), center_dev=_p(f.center_flag), n_pairs=n_pairs)
+                      pred=_view(ptr, o.pred), center_dev=_p(f.center_flag), n_pairs=n_pairs,
+                      band_coef=_p(f.band_coef), band_w=f.band_w, band=_p(f.band))
     h, ptau_d, w_d = 0, None, None
     if lj is not None and lj[0] > 0:
         h, ptau, w, _ = lj

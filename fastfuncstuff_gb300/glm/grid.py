@@ -127,6 +127,21 @@ def _valid_mask(a: torch.Tensor, b: torch.Tensor, afni: bool, corcut: float):
     return ok
 
 
+def afni_band(a: float, lam: float, corcut: float) -> int:
+    """The off-diagonals AFNI keeps in R (its rcmat_arma11): the lag at which
+    lam rho^(k-1), rho = a clamped to [-0.9, 0.9], has fallen to corcut; 0
+    (R = I) when |lam| < corcut, 1 for a pure MA(1) (a = 0). Follows
+    fastfuncstuff/glm/arma.py:95-109 in Python floats, as the reference
+    evaluates it."""
+    mag = abs(lam)
+    if mag < corcut:
+        return 0
+    rho = max(-0.9, min(0.9, a))
+    if rho == 0.0:
+        return 1
+    return 1 + int(math.ceil(math.log(corcut / mag) / math.log(abs(rho))))
+
+
 def estimate_valid_grid_pairs(a_grid, b_grid) -> int:
     """Number of valid pairs. Follows fastfuncstuff/glm/arma.py:291-338."""
     a, b = torch.meshgrid(_as_f32_cpu(a_grid), _as_f32_cpu(b_grid), indexing="ij")
@@ -149,6 +164,7 @@ class RemlGrid:
     chunk_start: np.ndarray  # (n_chunks + 1,) int32
     chunk_pairs: np.ndarray  # int32 pair slots of each chunk (-1: empty), one AR filter per quarter
     lambda_fp32: bool
+    band: np.ndarray | None = None  # AFNI-faithful mode: int32 band of R per pair (afni_band)
 
     @property
     def P(self) -> int:
@@ -236,6 +252,12 @@ def make_grid(a_grid, b_grid, use_double: bool = False) -> RemlGrid:
     am, bm = torch.meshgrid(ag.to(dt), bg.to(dt), indexing="ij")
     a, b = am.reshape(-1), bm.reshape(-1)
     ok = _valid_mask(a, b, _REML_MODE.afni_faithful, _REML_MODE.corcut)
+    band = None
+    if _REML_MODE.afni_faithful:
+        # the band from a and lambda in the fit's dtype (arma.py:1077-1084)
+        lam = compute_arma_lambda(a[ok], b[ok])
+        band = np.array([afni_band(float(x), float(y), _REML_MODE.corcut)
+                         for x, y in zip(a[ok].tolist(), lam.tolist())], dtype=np.int32)
     a = a[ok].to(torch.float32).numpy()
     b = b[ok].to(torch.float32).numpy()
     if a.size == 0:
@@ -254,7 +276,7 @@ def make_grid(a_grid, b_grid, use_double: bool = False) -> RemlGrid:
     chunk_start, chunk_pairs = coefficient_chunks(a, b)
     g = RemlGrid(a=a, b=b, a_axis=a_axis, b_axis=b_axis, lattice=lattice, p0=p0, za=za, zb=zb,
                  ltop=hierarchical_ltop(len(a_axis), len(b_axis), _REML_MODE.afni_faithful),
-                 chunk_start=chunk_start, chunk_pairs=chunk_pairs, lambda_fp32=not use_double)
+                 chunk_start=chunk_start, chunk_pairs=chunk_pairs, lambda_fp32=not use_double, band=band)
     if len(_GRID_CACHE) > 64:
         _GRID_CACHE.clear()
     _GRID_CACHE[key] = g

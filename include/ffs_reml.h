@@ -82,6 +82,8 @@ const char* ffs_last_error(void);
  *                  rank deficient at this pair), 2 a pivot of R's factor was
  *                  not positive.
  */
+#define FFS_BAND_MAX_W 129 /* widest band row (128 off-diagonals) of the banded R */
+
 typedef struct {
   int T, K, P, n_runs;
   const int* run_start; /* device [n_runs + 1], run_start[n_runs] == T           */
@@ -99,6 +101,13 @@ typedef struct {
   int n_sets;           /* column sets for Fsets (0: none)                       */
   const int* set_ptr;   /* device [n_sets + 1]: set s is set_idx[set_ptr[s] ..]  */
   const int* set_idx;   /* device [set_ptr[n_sets]] column indices (< K)         */
+  /* AFNI-faithful banded R (fastfuncstuff/glm/arma.py:95-109, :1075-1089):
+   * with band, correlations at |tau_i - tau_j| > band[p] are zero and R is
+   * factored as a band (band_L, band_coef below; coef is then the identity
+   * and unused). band_w = max band[p] + 1 <= FFS_BAND_MAX_W; NULL band: the
+   * exact ARMA(1,1) R. Single-design builds only (ffs_grid_build). */
+  int band_w;
+  const int* band;      /* device [P] or NULL                                    */
 } ffs_grid_desc;
 
 typedef struct {
@@ -119,6 +128,13 @@ typedef struct {
   double* work;         /* scratch, ffs_grid_work_bytes() bytes                   */
   float* Fsets;         /* [P][sum q_S^2] (with n_sets), or NULL                  */
   float* Afull;         /* [P][K][K] (X_w'X_w)^-1 (fp32), or NULL                 */
+  /* with d->band: the Cholesky factor of each run of the banded R, row t of
+   * pair p at [p][t][0 .. band_w): band_L[.][t][j] = L(t, t - j) (FP64, j = 0
+   * the diagonal, zero past the row's band), and band_coef[.][t][0] =
+   * 1 / L(t, t), band_coef[.][t][j] = L(t, t - j) / L(t, t) (fp32): the
+   * whitening w_t = y_t band_coef[t][0] - sum_j band_coef[t][j] w_{t-j}. */
+  double* band_L;
+  float* band_coef;
 } ffs_grid_out;
 
 size_t ffs_grid_work_bytes(int T, int K, int P);
@@ -331,6 +347,13 @@ typedef struct {
   const int* tile_design; /* NULL, or [ceil(V / 256)]: the design of each tile of */
                           /*   256 voxels (grouped fits); logdet_XtX is then      */
                           /*   [n_designs][P] and read at design * P + pair       */
+  /* AFNI-faithful banded R (ffs_grid_desc.band): y'R^-1 y by the band's
+   * forward substitution (band_coef, row stride band_w, band[p] terms per
+   * step) instead of coef's recursion; every pair of the grid is evaluated
+   * and the chunks are not read. NULL band_coef: the exact ARMA(1,1) R. */
+  const float* band_coef;
+  int band_w;
+  const int* band;
 } ffs_surface_args;
 
 int ffs_reml_surface(const ffs_surface_args* a, void* stream);
@@ -393,6 +416,13 @@ typedef struct {
                           /*   pair; G, Adiag, XtX, Gsum, Ftask and glt_var are   */
                           /*   read at the key, coef, a, b at the pair and Xt is  */
                           /*   [n_designs][K][T], read at the design              */
+  /* AFNI-faithful banded R (ffs_grid_desc.band): the whitening of the
+   * residual is w_t = r_t c[t][0] - sum_{1 <= j <= band[p]} c[t][j] w_{t-j}
+   * with c = band_coef of the pair (row stride band_w) instead of coef's
+   * recursion; NULL band_coef: the exact ARMA(1,1) R. */
+  const float* band_coef;
+  int band_w;
+  const int* band;
 } ffs_gls_args;
 
 int ffs_reml_gls(const ffs_gls_args* a, void* stream);

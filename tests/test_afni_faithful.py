@@ -1,0 +1,119 @@
+"""AFNI-faithful mode (``set_afni_mode(True)``) on the GPU: the banded R.
+
+The reference truncates each pair's correlation to AFNI's band
+(fastfuncstuff/glm/arma.py:95-109, :918-926, :1075-1089), drops the near-white
+pairs from the grid (:1031-1036) and uses AFNI's hierarchical ltop. The grid
+build factors the banded R as a band (``band_L``), and the surface and GLS
+kernels whiten against it. Checked against the FP64 oracle (pinned to the
+reference's own outputs in ``tests/golden/afni_faithful.npz``) and against the
+reference's float32 outputs in that fixture.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from fastfuncstuff_gb300.glm import grid as G
+from fastfuncstuff_gb300.glm.arma import fit_glm_arma11, precompute_reml_grid, set_afni_mode
+from oracle import reml as o
+from tests.conftest import load_golden
+from tests.test_gpu_parity import BETA_REL, _index, check_selection, rel_maxnorm
+from tests.test_oracle_golden import afni_faithful_case
+
+pytestmark = pytest.mark.gpu
+
+DEV = torch.device("cuda:0")
+
+
+@pytest.fixture
+def afni_mode():
+    set_afni_mode(True)
+    o.set_afni_mode(True)
+    yield
+    set_afni_mode(False)
+    o.set_afni_mode(False)
+
+
+@pytest.mark.parametrize("tag", ["runs", "cens"])
+def test_banded_factors_match_the_dense_oracle(tag, afni_mode):
+    d = load_golden("afni_faithful")
+    Y, X, kw = afni_faithful_case(d, tag)
+    T = X.shape[0]
+    f = precompute_reml_grid(torch.from_numpy(X), T, d["a_grid"], d["b_grid"], DEV, run_starts=kw["run_starts"],
+                             tau=kw.get("tau"), use_double=True)
+    torch.cuda.synchronize()
+    og = o.valid_grid(d["a_grid"], d["b_grid"], np.float64)
+    np.testing.assert_array_equal(np.stack([f.grid.a, f.grid.b], 1), np.stack([og.a, og.b], 1))
+    band = np.array([o.afni_bmax(float(og.a[p]), float(og.lam[p]), 1e-4) for p in range(og.n)])
+    np.testing.assert_array_equal(f.grid.band, band)
+    assert int(f.info.cpu().abs().sum()) == 0
+    pre = o.precompute_reml_grid(X.astype(np.float64), og, run_starts=kw["run_starts"], tau=kw.get("tau"))
+    np.testing.assert_allclose(f.logdet_R.cpu().numpy(), pre.logdet_R, rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(f.logdet_XtX.cpu().numpy(), pre.logdet_XtX, rtol=1e-9, atol=1e-9)
+    L = f.band_L.cpu().numpy()
+    coef = f.band_coef.cpu().numpy().astype(np.float64)
+    U = f.U[:, :, :T].cpu().numpy()
+    for p in range(0, f.P, 7):
+        # the band rows are the dense Cholesky factor's, zero outside the band
+        Li = pre.whiteners[p].dense()
+        Ld = np.linalg.inv(Li)
+        for t in range(T):
+            for j in range(L.shape[2]):
+                want = Ld[t, t - j] if j <= t else 0.0
+                assert abs(L[p, t, j] - want) <= 1e-9 * max(1.0, abs(want)), (p, t, j)
+        # the fp32 coefficients whiten like L^-1
+        xw = np.zeros_like(X, dtype=np.float64)
+        for t in range(T):
+            acc = X[t].astype(np.float64) * coef[p, t, 0]
+            for j in range(1, min(t, L.shape[2] - 1) + 1):
+                acc -= coef[p, t, j] * xw[t - j]
+            xw[t] = acc
+        np.testing.assert_allclose(xw, pre.X_w[p], rtol=2e-5, atol=2e-5)
+        np.testing.assert_allclose(U[p].T, Li.T @ pre.Q[p], rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("tag", ["runs", "cens"])
+@pytest.mark.parametrize("exhaustive", [True, False])
+def test_afni_faithful_fit_matches_fp64_oracle_and_reference(tag, exhaustive, afni_mode):
+    d = load_golden("afni_faithful")
+    Y, X, kw = afni_faithful_case(d, tag)
+    ref = o.fit_glm_arma11(Y, X, use_double=True, fp64_scaled=True, force_exhaustive_search=exhaustive,
+                           save_profile_likelihoods=True, want_ljung_box=True, want_residuals=True, **kw)
+    got = fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, force_exhaustive_search=exhaustive,
+                         want_ljung_box=True, want_residuals=True, **kw)
+    grid = G.make_grid(d["a_grid"], d["b_grid"])
+    idx = _index(got.arma_params.numpy(), grid)
+    check_selection(idx, ref.arma_index, ref.reml_lklhd_surface)
+    same = idx == ref.arma_index
+    assert rel_maxnorm(got.betas.numpy()[same], ref.betas[same]).max() <= BETA_REL
+    assert rel_maxnorm(got.tstats.numpy()[same], ref.tstats[same]).max() <= BETA_REL
+    np.testing.assert_allclose(got.sigma2.numpy()[same], ref.sigma2[same], rtol=1e-4)
+    np.testing.assert_allclose(got.reml_likelihood.numpy()[same], ref.reml_likelihood[same], rtol=1e-5,
+                               atol=2e-3)
+    np.testing.assert_allclose(got.residuals_whitened.numpy()[same], ref.residuals_whitened[same],
+                               rtol=1e-4, atol=2e-4)
+    np.testing.assert_allclose(got.ljung_box.numpy()[same], ref.ljung_box[same], rtol=2e-3, atol=1e-3)
+    # the reference's own float32 run of the same mode
+    mode = f"{tag}_f32_{'exh' if exhaustive else 'def'}__"
+    agree = (got.arma_params.numpy() == d[mode + "arma_params"]).all(1)
+    assert agree.mean() >= 0.97, agree.mean()
+    assert rel_maxnorm(got.betas.numpy()[agree], d[mode + "betas"][agree]).max() <= 2e-3
+
+
+def test_afni_faithful_surface_differs_from_the_exact_r(afni_mode):
+    """The banded criterion is not the exact one (so the mode is really in use)."""
+    d = load_golden("afni_faithful")
+    Y, X, kw = afni_faithful_case(d, "runs")
+    a = fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, force_exhaustive_search=True, **kw)
+    set_afni_mode(False)
+    b = fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, force_exhaustive_search=True, **kw)
+    assert np.abs(a.reml_likelihood.numpy() - b.reml_likelihood.numpy()).max() > 1e-6
+
+
+def test_afni_faithful_refuses_what_keeps_the_exact_r(afni_mode):
+    d = load_golden("afni_faithful")
+    Y, X, kw = afni_faithful_case(d, "runs")
+    with pytest.raises(NotImplementedError):
+        fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, dsort=Y[:, None, :], **kw)
