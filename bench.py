@@ -510,6 +510,26 @@ def run_gb300(args) -> None:
                       "gpu_launches": l_f, "clocks": clk_f},
     }
 
+    if grouped and args.grouped_learned:
+        # the learned-seeded fit of the grouped workload: a proposal trained on
+        # the family of the groups' designs, each design's voxels searched
+        # against that design's view of one multi-design grid build
+        fam = torch.stack([designs[h] for h in sorted(designs)])
+        lay_g = G.run_layout(T, w.run_starts, w.tau)
+        prop_g, tinfo_g = learned.train_proposal(fam, lay_g, g, g, n_voxels=args.train_voxels,
+                                                 epochs=args.train_epochs)
+        kw_g = dict(kw, proposal=prop_g, proposal_recenter=args.recenter)
+        ms_g, st_g, l_g, clk_g = timed(kw_g, "grouped_learned")
+        r_l = fit(Yd, Xd, return_device=True, **kw_g)
+        r_f = fit(Yd, Xd, return_device=True, **dict(kw, force_exhaustive_search=True))  # the argmin it seeks
+        same = (r_l.arma_params == r_f.arma_params).all(1)
+        line["grouped_learned"] = {
+            "value": ws * V / (ms_g / 1e3), "unit": "voxels/s", "ms_per_step": ms_g,
+            "learned_over_full": ms_f / ms_g, "agreement_with_exhaustive_full_grid": float(same.float().mean()),
+            "full_grid_fallback": float(r_l.learned_fallback), "gpu_launches": l_g, "clocks": clk_g,
+            "stages_ms": {k: round(v["mean_ms"] * v["calls"] / args.steps, 4) for k, v in st_g.items()},
+            "proposal": f"trained on the {fam.shape[0]} group designs", **tinfo_g}
+
     if args.dsort > 0 and not grouped and rank == 0:
         # the full-grid fit with Q voxelwise regressors per voxel (-dsort): the
         # search is unchanged, the final GLS is the extended one
@@ -590,6 +610,8 @@ def main() -> None:
     ap.add_argument("--dsort", type=int, default=0,
                     help="also time the full-grid fit with this many voxelwise regressors (-dsort)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-grouped-learned", dest="grouped_learned", action="store_false",
+                    help="grouped workload: skip the learned-seeded arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

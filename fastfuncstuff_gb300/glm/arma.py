@@ -381,7 +381,7 @@ def fit_glm_arma11(
     P = grid.P
     bs = _batch_size(V, T, P, K, batch_size, device)
     use_graph = (best_all is None and proposal is not None and cuda_graphs and lj is None and bs >= V
-                 and Dd is None)
+                 and Dd is None and _group_designs is None)
     # results for the host straight from the GLS kernels (pinned memory
     # written over the host link while they run) when nothing else reads them
     # on the device
@@ -396,7 +396,8 @@ def fit_glm_arma11(
         # grid build, every voxel against its own design in one pass per stage
         Xs, gid = _group_designs
         bs = V
-        if cuda_graphs and lj is None and Dd is None and sets is None and not save_profile_likelihoods:
+        if (cuda_graphs and lj is None and Dd is None and sets is None and not save_profile_likelihoods
+                and proposal is None):
             # the whole grouped fit replayed from one CUDA graph
             gplan = engine.grouped_graph_for(Y, Xs, grid, layout, gid, hierarchical=not force_exhaustive_search,
                                              do_scale=not use_double,
@@ -462,6 +463,16 @@ def fit_glm_arma11(
             chunks["best"].append(best)
             chunks["crit"].append(lo.best_crit)
             fb_voxels += lo.stats["fallback"] * (v1 - v0)
+        elif best_all is None and proposal is not None and slots is not None:
+            # grouped designs: each design's voxels searched and refit against
+            # that design's view of the one multi-design build
+            best, crit_g, scale, go, nf = learned.grouped_learned_fit(
+                Yb, factors, _group_designs[1][v0:v1], _group_designs[0], proposal, layout_l,
+                do_scale=not use_double, recenter=proposal_recenter,
+                gls_kw=dict(want_residuals=want_residuals, want_predicted=want_predicted), lj=lj)
+            chunks["best"].append(best)
+            chunks["crit"].append(crit_g)
+            fb_voxels += nf
         elif best_all is None and proposal is not None:
             # the GLS of every voxel at its window's pair is queued before the
             # host waits for the list of fallback voxels; their rows are redone
@@ -747,8 +758,7 @@ def fit_glm_arma11_grouped(data, designs_by_group: dict, group_indices, tr: floa
                              "designs must share dims")
     pre = fit_kwargs.pop("precomputed_arma_params", None)
     fit_kwargs.setdefault("verbose", False)
-    batched_ok = (pre is None and fit_kwargs.get("proposal") is None
-                  and not fit_kwargs.get("save_profile_likelihoods", False)
+    batched_ok = (pre is None and not fit_kwargs.get("save_profile_likelihoods", False)
                   and fit_kwargs.get("batch_size") is None and fit_kwargs.get("estimate_per_voxel", True)
                   and shape0[1] <= TC_MAX_K and len(groups) > 1)
     if batched_ok:

@@ -17,6 +17,7 @@ Layouts (V voxels, T time points, K design columns, P pairs):
 
 from __future__ import annotations
 
+import copy
 import ctypes as C
 import math
 from dataclasses import dataclass
@@ -484,6 +485,30 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     f.Gsum = ccoef.reshape(D, 1, K).expand(D, P, K).reshape(DP, K).contiguous()
     f._keep = (Xc, run_start, tau, work, sets_dev)  # inputs must outlive the launch
     return f
+
+
+def design_view(f: GridFactors, d: int, center_flag: torch.Tensor | None = None) -> GridFactors:
+    """The factors of design d of a multi-design build as a single-design
+    GridFactors (views into the build's buffers, no copy): what a fit of that
+    design's voxels alone reads. ``center_flag`` (constant_flag of the
+    design) replaces the build's flag, which holds for every design at once."""
+    if f.n_designs == 1:
+        return f
+    P, K = f.P, f.K
+    sl = slice(d * P, (d + 1) * P)
+    v = copy.copy(f)
+    v.n_designs = 1
+    for name in ("logdet_XtX", "U", "G", "Adiag", "XtX", "info", "Ftask", "glt_var", "Gsum", "uexp", "Fsets",
+                 "Afull"):
+        t = getattr(f, name)
+        setattr(v, name, None if t is None else t[sl])
+    for name in ("U_hi", "U_lo"):
+        t = getattr(f, name)
+        setattr(v, name, None if t is None else t[d * P * K:(d + 1) * P * K])
+    if center_flag is not None:
+        v.center_flag = center_flag
+    v.__dict__.pop("_window_consts", None)  # per-design constants of the learned refine
+    return v
 
 
 @dataclass

@@ -512,6 +512,47 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
     return learned_fallback(Y, factors, ws, host, do_scale=do_scale)
 
 
+def grouped_learned_fit(Y: torch.Tensor, factors: engine.GridFactors, design: np.ndarray, Xs: torch.Tensor,
+                        proposal: ArmaProposal, layout: RunLayout, *, do_scale: bool = True, recenter: int = 0,
+                        gls_kw: dict | None = None, lj=None):
+    """The learned-seeded fit of a grouped fit (one design per voxel group):
+    ``factors`` is the multi-design build of Xs (D, T, K) and ``design`` [V]
+    (host) each voxel's design. Each design's voxels run the single-design
+    search (learned_search) and GLS against that design's view of the factors
+    (engine.design_view); the results are scattered back to voxel order.
+    Returns (best, best_crit, scale, GlsOut, voxels the full grid decided)."""
+    dev = Y.device
+    V = Y.shape[0]
+    design = np.asarray(design).reshape(-1)
+    best = torch.empty(V, dtype=torch.int32, device=dev)
+    best_crit = torch.empty(V, dtype=torch.float32, device=dev)
+    scale = torch.empty(V, dtype=torch.float32, device=dev)
+    out = None
+    n_fb = 0.0
+    for d in range(Xs.shape[0]):
+        idx = np.nonzero(design == d)[0]
+        if idx.size == 0:
+            continue
+        sel = torch.from_numpy(idx).to(dev)
+        Yd = Y.index_select(0, sel)
+        flag, _ = engine.constant_flag(Xs[d])
+        fv = engine.design_view(factors, d, center_flag=flag)
+        lo = learned_search(Yd, fv, proposal, layout, do_scale=do_scale, recenter=recenter)
+        go = engine.gls(Yd, lo.scale, lo.best, fv, Xs[d], lj=lj, **(gls_kw or {}))
+        best.index_copy_(0, sel, lo.best)
+        best_crit.index_copy_(0, sel, lo.best_crit)
+        scale.index_copy_(0, sel, lo.scale)
+        if out is None:
+            out = engine.GlsOut(**{k: None if t is None else torch.empty((V,) + tuple(t.shape[1:]), dtype=t.dtype,
+                                                                          device=dev)
+                                   for k, t in vars(go).items() if not k.startswith("_")})
+        for k, t in vars(go).items():
+            if not k.startswith("_") and t is not None:
+                getattr(out, k).index_copy_(0, sel, t)
+        n_fb += lo.stats["fallback"] * idx.size
+    return best, best_crit, scale, out, n_fb
+
+
 def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxels: int = 6_000_000,
                    epochs: int = 40, batch: int = 8192, lr: float = 3e-3, seed: int = 5):
     """Train a proposal on the GPU: n_voxels simulated with (a, b) drawn

@@ -444,3 +444,43 @@ def test_learned_fit_with_t_not_a_multiple_of_four(cuda_graphs):
     assert float(same.float().mean()) >= 0.99
     for name in ("betas", "tstats", "sigma2", "r2"):
         assert torch.equal(getattr(got, name)[same], getattr(full, name)[same]), name
+
+
+@pytest.mark.gpu
+def test_grouped_learned_fit_equals_per_group_learned_fits():
+    """fit_glm_arma11_grouped with a proposal: one grid build over every
+    design, then each design's voxels through the learned search and GLS
+    against that design's view of it. Each voxel's arithmetic is the
+    single-design learned fit's, so the results are those of fitting every
+    group alone with the same proposal (workload-2 shapes: 4 censored runs,
+    N=855, 6 of the 20 designs), and the pairs agree with the grouped full
+    grid where the windows hold the answer."""
+    from fastfuncstuff_gb300 import fit_glm_arma11, fit_glm_arma11_grouped, synth
+    from fastfuncstuff_gb300.glm import learned
+    from fastfuncstuff_gb300.glm import grid as G
+
+    dev = torch.device("cuda:0")
+    w = synth.workload(2, V=4000)
+    keep = np.isin(w.groups, np.arange(6))
+    Y, gid = w.Y[keep], w.groups[keep]
+    designs = {h: w.designs[h] for h in range(6)}
+    gr = torch.linspace(-0.8, 0.8, 33)
+    lay = G.run_layout(w.Y.shape[1], w.run_starts, w.tau)
+    fam = torch.stack([torch.from_numpy(designs[h]) for h in range(6)]).to(dev)
+    prop, _ = learned.train_proposal(fam, lay, gr, gr, n_voxels=300_000, epochs=6)
+    kw = dict(a_grid=gr, b_grid=gr, run_starts=w.run_starts, tau=w.tau, device=dev, verbose=False,
+              force_exhaustive_search=True, want_residuals=True)
+    got = fit_glm_arma11_grouped(Y, designs, gid, tr=2.0, proposal=prop, proposal_recenter=1, **kw)
+    assert 0.0 <= float(got.learned_fallback) < 0.5
+    for h in range(6):
+        m = gid == h
+        ref = fit_glm_arma11(Y[m], designs[h], tr=2.0, proposal=prop, proposal_recenter=1, cuda_graphs=False,
+                             **kw)
+        np.testing.assert_array_equal(got.arma_params.numpy()[m], ref.arma_params.numpy())
+        for name in ("reml_likelihood", "betas", "tstats", "sigma2", "fstats", "r2", "arma_lambda", "residuals",
+                     "residuals_whitened"):
+            np.testing.assert_array_equal(getattr(got, name).numpy()[m], getattr(ref, name).numpy(), err_msg=name)
+    full = fit_glm_arma11_grouped(Y, designs, gid, tr=2.0, **kw)
+    same = (got.arma_params == full.arma_params).all(1)
+    assert float(same.float().mean()) >= 0.97
+    np.testing.assert_array_equal(got.betas.numpy()[same.numpy()], full.betas.numpy()[same.numpy()])
