@@ -161,22 +161,19 @@ __global__ void __launch_bounds__(TILE_WARPS * 32, 3) prep_tile_kernel(ffs_prep_
   }
   __syncthreads();
   if (a.Y_ref) {
-    // the input through its address on the device (pinned host memory mapped
-    // into the device's address space, or device memory): plain 16-byte loads,
-    // a warp per row, and the rows as read written out for the later stages
-    const float* Yin = *a.Y_ref;
-    for (int i = wid; i < TILE_V; i += TILE_WARPS) {
-      float4* dst = reinterpret_cast<float4*>(Ys + (size_t)i * ld);
-      const int v = src_row[i];
-      const float4* src = reinterpret_cast<const float4*>(Yin + (size_t)(v < 0 ? 0 : v) * T);
-      float4* cpy = (a.Y_copy && v >= 0) ? reinterpret_cast<float4*>(a.Y_copy + (size_t)v * T) : nullptr;
-      for (int q = lane; q < nq; q += 32) {
-        const float4 x = v >= 0 ? src[q] : make_float4(0.f, 0.f, 0.f, 0.f);
-        dst[q] = x;
-        if (cpy) cpy[q] = x;
+    // the input through its address held on the device (device memory): the
+    // tile's rows staged by asynchronous copies, all in flight at once, then
+    // written out from shared memory as read for the later stages (T % 4 == 0)
+    tile_stage_rows(*a.Y_ref, T, nq, src_row, Ys, ld);
+    if (a.Y_copy) {
+      for (int i = wid; i < nv; i += TILE_WARPS) {
+        const int v = src_row[i];
+        if (v < 0) continue;  // warp-uniform
+        const float4* row4 = reinterpret_cast<const float4*>(Ys + (size_t)i * ld);
+        float4* cpy = reinterpret_cast<float4*>(a.Y_copy + (size_t)v * T);
+        for (int q = lane; q < nq; q += 32) cpy[q] = row4[q];
       }
     }
-    __syncthreads();
   } else {
     tile_stage_rows(a.Y, T, nq, src_row, Ys, ld);
   }

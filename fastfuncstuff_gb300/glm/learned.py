@@ -745,17 +745,17 @@ class LearnedFitGraph:
         self.host.copy_(self.ws.small, non_blocking=True)
 
     def _set_source(self, Y: torch.Tensor) -> None:
-        """Point y_ref at Y's rows (float32, contiguous, 16-byte aligned; on the
-        device, or pinned host memory that the prep streams in place)."""
+        """Point y_ref at Y's rows (float32, contiguous, 16-byte aligned device
+        memory; host data take a staged plan)."""
         if tuple(Y.shape) != tuple(self.Y.shape) or Y.dtype != torch.float32 or not Y.is_contiguous():
             raise ValueError("the learned fit's graph reads float32 contiguous data of its own shape")
         if not self.inplace:
             self.Y.copy_(Y, non_blocking=True)
             self._src = Y
             return
-        addr = engine.device_view(Y)
-        if addr is None or addr % 16:
-            raise ValueError("the learned fit's graph reads device memory or pinned host memory (16-byte aligned)")
+        if not Y.is_cuda or Y.data_ptr() % 16:
+            raise ValueError("this plan reads 16-byte aligned device memory in place; host data take a staged plan")
+        addr = Y.data_ptr()
         self.y_ref_host[0] = addr
         self.y_ref.copy_(self.y_ref_host, non_blocking=True)
         self._src = Y  # kept alive until the run that reads it has finished

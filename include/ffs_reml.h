@@ -247,12 +247,11 @@ typedef struct {
   const int* tile_design;
   /* End-to-end input without a staging copy (no reference counterpart; the
    * tiled prep only, T % 4 == 0, idx == NULL, no tile_design):
-   * Y_ref  NULL, or a device pointer to the input's address: the rows are read
-   *        from *Y_ref instead of Y (Y is then ignored; it may be NULL). The
-   *        address may be device memory or pinned host memory mapped into the
-   *        device's address space (ffs_device_view), which the kernel then
-   *        streams over the host link while it works. Being read on the
-   *        device, the address can change between replays of a captured launch.
+   * Y_ref  NULL, or a device pointer to the input's address (device memory):
+   *        the rows are read from *Y_ref instead of Y (Y is then ignored; it
+   *        may be NULL), staged by asynchronous copies. Being read on the
+   *        device, the address can change between replays of a captured
+   *        launch.
    * Y_copy NULL, or [V][T]: the input rows as read, written out (the later
    *        stages then read device memory). */
   const float* const* Y_ref;
