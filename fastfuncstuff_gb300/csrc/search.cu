@@ -621,11 +621,13 @@ __global__ void select_kernel(ffs_select_args a) {
 // Counting with warp-aggregated atomics: the lanes of a warp holding the same
 // key add their count once (neighbouring voxels of a smooth parameter map
 // mostly share a pair, so a popular bin sees one atomic per warp, not 32).
-__global__ void group_hist(int V, const int* best, int* cnt) {
+// Keys outside [0, P) are not counted (nor placed by group_scatter).
+__global__ void group_hist(int V, const int* best, int P, int* cnt) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned act = __ballot_sync(0xffffffffu, v < V);
-  if (v >= V) return;
-  const int key = best[v];
+  const int key = v < V ? best[v] : -1;
+  const bool ok = (unsigned)key < (unsigned)P;
+  const unsigned act = __ballot_sync(0xffffffffu, ok);
+  if (!ok) return;
   const unsigned same = __match_any_sync(act, key);
   if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(cnt + key, __popc(same));
 }
@@ -747,12 +749,13 @@ __global__ void __launch_bounds__(GROUP_BLOCK_THREADS) group_scatter_block(int V
 
 // The leader of each set of equal keys reserves the set's slots with one
 // atomic; every lane takes the slot of its rank within the set.
-__global__ void group_scatter(int V, const int* best, int* cursor, int* order) {
+__global__ void group_scatter(int V, const int* best, int P, int* cursor, int* order) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned act = __ballot_sync(0xffffffffu, v < V);
-  if (v >= V) return;
+  const int key = v < V ? best[v] : -1;
+  const bool ok = (unsigned)key < (unsigned)P;
+  const unsigned act = __ballot_sync(0xffffffffu, ok);
+  if (!ok) return;
   const int lane = threadIdx.x & 31;
-  const int key = best[v];
   const unsigned same = __match_any_sync(act, key);
   const int leader = __ffs(same) - 1;
   int base = 0;
@@ -886,9 +889,9 @@ extern "C" int ffs_reml_group(int V, int P, const int* best, int* work, int* ord
     group_scan<<<1, 1024, 0, st>>>(P, work);
     group_scatter_block<<<grid, GROUP_BLOCK_THREADS, 2 * sizeof(int) * P, st>>>(V, best, P, work, order);
   } else {
-    group_hist<<<ceil_div(V, 256), 256, 0, st>>>(V, best, work);
+    group_hist<<<ceil_div(V, 256), 256, 0, st>>>(V, best, P, work);
     group_scan<<<1, 1024, 0, st>>>(P, work);
-    group_scatter<<<ceil_div(V, 256), 256, 0, st>>>(V, best, work, order);
+    group_scatter<<<ceil_div(V, 256), 256, 0, st>>>(V, best, P, work, order);
   }
   return check_launch("group kernels");
 }

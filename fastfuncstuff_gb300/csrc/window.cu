@@ -39,11 +39,15 @@ __device__ __forceinline__ void window_of(int c, int n_a, int n_b, int& a0, int&
 // [end[c-1], end[c]) (end[-1] = 0)
 __global__ void window_items_kernel(int ncell, const int* end, int n_a, int n_b, const int* lattice, int K,
                                     int max_pairs, ffs_tc_item* items, int* n_items, int max_items, int2* tiles,
-                                    int* n_tiles, int max_tiles, int* overflow) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncell) return;
-  const int s0 = c ? end[c - 1] : 0, n = end[c] - s0;
+                                    int* n_tiles, int max_tiles, int* overflow, int P) {
+  const int key = blockIdx.x * blockDim.x + threadIdx.x;
+  if (key >= ncell) return;
+  const int s0 = key ? end[key - 1] : 0, n = end[key] - s0;
   if (n <= 0) return;
+  // with designs (P > 0) the key is design * n_a n_b + cell, and the U rows
+  // of the design's pairs start at (design * P + pair) * K
+  const int c = P > 0 ? key % (n_a * n_b) : key;
+  const int row0 = P > 0 ? (key / (n_a * n_b)) * P * K : 0;
   int a0, wa, b0, wb;
   window_of(c, n_a, n_b, a0, wa, b0, wb);
   const int ntile = (n + WTILE - 1) / WTILE;
@@ -86,7 +90,7 @@ __global__ void window_items_kernel(int ncell, const int* end, int n_a, int n_b,
       ffs_tc_item it;
       it.v0 = s0 + t * WTILE;
       it.nv = min(WTILE, n - t * WTILE);
-      it.row_b = seg_p[sg] * K;
+      it.row_b = row0 + seg_p[sg] * K;
       it.np = seg_np[sg];
       it.out0 = it.v0;
       it.slot0 = seg_slot[sg];
@@ -118,6 +122,8 @@ struct CritArgs {
   int* fallback;
   int* best_cell;
   int* next_center;         // NULL, or [V]: the next round's centre of each voxel taken
+  const int* design;        // NULL, or [V]: each voxel's design; dcf then [n_designs][P], c_p0 [n_designs]
+  int P;
 };
 
 constexpr int CRIT_TB = 16;  // steps per partial sum and sample prefetch
@@ -157,6 +163,8 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
   const int i = tl.x + tid;
   const bool live = tid < tl.y;
   const int c = w.center[w.idx[tl.x]];  // every row of the tile has this centre
+  const int dsg = w.design ? w.design[w.idx[tl.x]] : 0;  // and this design
+  const float* dcf = w.dcf + (size_t)dsg * w.P;
   int a0, wa, b0, wb;
   window_of(c, w.n_a, w.n_b, a0, wa, b0, wb);
   const int T = w.T, Tk = w.T - w.K;
@@ -372,7 +380,7 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
       const int p = s_pr[ra][g];
       const float stv = sst[(ra * WIN + g) * WTILE + tid];
       const float rss = fmaxf(stv - w.winproj[(size_t)i * WSLOTS + ra * WIN + s_col[ra][g]], 0.f);
-      const float d = w.dcf[p] + (float)Tk * log1pf((rss - yy) / (yy + 1e-10f));
+      const float d = dcf[p] + (float)Tk * log1pf((rss - yy) / (yy + 1e-10f));
       if (d < bd || (d == bd && p < best) || best < 0) {
         bd = d;
         best = p;
@@ -413,7 +421,7 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
   const int v = w.idx[i];
   w.best[v] = best;
   w.dbest[v] = bd;
-  w.crit0[v] = *w.c_p0 + (double)Tk * log((double)rss0 + 1e-10);
+  w.crit0[v] = w.c_p0[dsg] + (double)Tk * log((double)rss0 + 1e-10);
   w.fallback[v] = fb;
   w.best_cell[v] = bcell;
   // a voxel on its window's edge is re-centred on its best pair; the rest
@@ -768,9 +776,10 @@ extern "C" int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const i
 
 extern "C" int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, const int* lattice, int K,
                                      int max_pairs, ffs_tc_item* items, int* n_items, int max_items, int* tiles,
-                                     int* n_tiles, int max_tiles, int* overflow, void* stream) {
+                                     int* n_tiles, int max_tiles, int* overflow, int P, void* stream) {
   clear_error();
-  FFS_REQUIRE(ncell > 0 && n_a > 0 && n_b > 0 && K > 0 && max_pairs > 0 && max_items > 0 && max_tiles > 0,
+  FFS_REQUIRE(ncell > 0 && n_a > 0 && n_b > 0 && K > 0 && max_pairs > 0 && max_items > 0 && max_tiles > 0 &&
+                  P >= 0 && (P == 0 || ncell % (n_a * n_b) == 0),
               "ffs_reml_window_items: bad sizes");
   FFS_REQUIRE(cell_end && lattice && items && n_items && tiles && n_tiles && overflow,
               "ffs_reml_window_items: null buffer");
@@ -780,7 +789,7 @@ extern "C" int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, in
   FFS_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), st));
   window_items_kernel<<<ceil_div(ncell, 128), 128, 0, st>>>(ncell, cell_end, n_a, n_b, lattice, K, max_pairs, items,
                                                              n_items, max_items, reinterpret_cast<int2*>(tiles),
-                                                             n_tiles, max_tiles, overflow);
+                                                             n_tiles, max_tiles, overflow, P);
   clamp_count_kernel<<<1, 1, 0, st>>>(n_items, max_items, n_tiles, max_tiles);
   return check_launch("window_items_kernel");
 }
@@ -789,9 +798,10 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
                                const int* center, const int* tiles, const int* n_tiles, int max_tiles,
                                const float* rows, const float* coef, const float* winproj, const float* dcf,
                                const unsigned char* ident, int p_id, const double* c_p0, int* best, float* dbest,
-                               double* crit0, int* fallback, int* best_cell, int* next_center, void* stream) {
+                               double* crit0, int* fallback, int* best_cell, int* next_center, const int* design,
+                               int P, void* stream) {
   clear_error();
-  FFS_REQUIRE(n > 0 && T > K && K > 0 && n_a > 0 && n_b > 0 && p_id >= 0 && max_tiles > 0,
+  FFS_REQUIRE(n > 0 && T > K && K > 0 && n_a > 0 && n_b > 0 && p_id >= 0 && max_tiles > 0 && (!design || P > 0),
               "ffs_reml_window: bad sizes");
   FFS_REQUIRE(lattice && idx && center && tiles && n_tiles && rows && coef && winproj && dcf && ident && c_p0 &&
                   best && dbest && crit0 && fallback && best_cell,
@@ -800,7 +810,7 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(window_crit_kernel), smem));
   FFS_REQUIRE(((uintptr_t)rows & 15) == 0, "ffs_reml_window: rows must be 16-byte aligned");
   CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, rows, reinterpret_cast<const float4*>(coef), winproj, dcf,
-             ident, p_id, c_p0, best, dbest, crit0, fallback, best_cell, next_center};
+             ident, p_id, c_p0, best, dbest, crit0, fallback, best_cell, next_center, design, P};
   window_crit_kernel<<<max_tiles, WTILE, smem, (cudaStream_t)stream>>>(w, reinterpret_cast<const int2*>(tiles),
                                                                         n_tiles);
   return check_launch("window_crit_kernel");

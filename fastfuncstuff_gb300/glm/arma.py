@@ -469,7 +469,7 @@ def fit_glm_arma11(
             best, crit_g, scale, go, nf = learned.grouped_learned_fit(
                 Yb, factors, _group_designs[1][v0:v1], _group_designs[0], proposal, layout_l,
                 do_scale=not use_double, recenter=proposal_recenter,
-                gls_kw=dict(want_residuals=want_residuals, want_predicted=want_predicted), lj=lj)
+                gls_kw=dict(want_residuals=want_residuals, want_predicted=want_predicted), lj=lj, slots=slots)
             chunks["best"].append(best)
             chunks["crit"].append(crit_g)
             fb_voxels += nf

@@ -748,13 +748,15 @@ def design_slots(gid: np.ndarray, n_designs: int, K: int, P: int, dev) -> Design
         real[vox] = np.arange(start[d], start[d] + counts[d])
     tile_of = np.repeat(np.arange(n_designs, dtype=np.int32), padded // 32)
     g = max(1, min(P, 256 // K))
+    p0 = np.arange(0, P, g, dtype=np.int64)
+    npair = np.minimum(g, P - p0)
     rows = []
-    for d in range(n_designs):
-        for v0 in range(int(start[d]), int(start[d + 1]), 128):
-            for p0 in range(0, P, g):
-                n = min(g, P - p0)
-                rows.append((v0, 128, (d * P + p0) * K, n, v0, p0))
-    items = np.asarray(rows, np.int32).reshape(-1, 6)
+    for d in range(n_designs):  # design-major, then voxel tile, then pair block
+        v0 = np.arange(int(start[d]), int(start[d + 1]), 128, dtype=np.int64)
+        vv, pp = np.meshgrid(v0, p0, indexing="ij")
+        nn = np.broadcast_to(npair, vv.shape)
+        rows.append(np.stack([vv, np.full_like(vv, 128), (d * P + pp) * K, nn, vv, pp], -1).reshape(-1, 6))
+    items = np.concatenate(rows).astype(np.int32) if rows else np.zeros((0, 6), np.int32)
     return DesignSlots(V=V, Vp=Vp, idx=torch.from_numpy(idx).to(dev), real=torch.from_numpy(real).to(dev),
                        design=torch.from_numpy(gid.astype(np.int32)).to(dev),
                        tile32=torch.from_numpy(tile_of).to(dev),

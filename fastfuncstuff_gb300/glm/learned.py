@@ -298,13 +298,16 @@ def _strip_round(pre, f, out, *, flag, k0: int):
     out.setdefault("_keep", []).append((ids, hi, lo, yexp, u_hi, u_lo, uex, proj))
 
 
-def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None):
+def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None, grp=None):
     """Evaluate the 5 x 5 windows centred at cen (one lattice cell per voxel,
     or ncell = n_a * n_b for a voxel to skip), writing out[...] at the voxel
     ids, and into next_cen (when given) the centre of a re-centred round for
     each voxel taken (ncell: none). Nothing waits for the host: the number of
     voxels taken stays on the device. pre is the prep of every voxel (fp16
-    operands and voxel-major rows)."""
+    operands and voxel-major rows). ``grp`` (grouped designs: a multi-design
+    ``f``) gives each row's design and the per-design criterion constants;
+    the rows are then sorted by design and centre, so every tile and work
+    item belongs to one design."""
     lib = _lib.load()
     dev = pre.scale.device
     g = f.grid
@@ -314,11 +317,16 @@ def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None):
     ncell = n_a * n_b
     n = cen.numel()
     c = _grid_consts(g, dev)
-    # voxels sorted by window centre; the skipped ones (bucket ncell) last
+    # voxels sorted by window centre (by design, then centre, for grouped
+    # designs); the skipped ones (the last bucket) last
+    nkey, keys, Pd = ncell, cen, 0
+    if grp is not None:
+        nkey, Pd = grp["D"] * ncell, P
+        keys = torch.where(cen < ncell, grp["design"] * ncell + cen, torch.full_like(cen, nkey)).contiguous()
     idx = torch.empty(n, dtype=torch.int32, device=dev)
-    cell_end = torch.empty(ncell + 2, dtype=torch.int32, device=dev)
-    engine._run("ffs_reml_group", lib.ffs_reml_group, n, ncell + 1, _p(cen), _p(cell_end), _p(idx), st)
-    n_taken = cell_end[ncell - 1 : ncell]  # device count of the voxels with a window
+    cell_end = torch.empty(nkey + 2, dtype=torch.int32, device=dev)
+    engine._run("ffs_reml_group", lib.ffs_reml_group, n, nkey + 1, _p(keys), _p(cell_end), _p(idx), st)
+    n_taken = cell_end[nkey - 1 : nkey]  # device count of the voxels with a window
     hi = torch.empty(n, ld, dtype=torch.int16, device=dev)
     lo = torch.empty(n, ld, dtype=torch.int16, device=dev)
     yexp = torch.empty(n, dtype=torch.int32, device=dev)
@@ -328,19 +336,19 @@ def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None):
                 _p(pre.yexp), _p(pre.rows), _p(hi), _p(lo), _p(yexp), None, st)
     # projections of every window pair on the tensor cores
     max_pairs = max(1, min(5, 256 // K))
-    max_tiles = (n + 127) // 128 + min(n, ncell)
+    max_tiles = (n + 127) // 128 + min(n, nkey)
     max_items = WIN_SLOTS * max_tiles
     items = torch.empty(max_items, 6, dtype=torch.int32, device=dev)
     tiles = torch.empty(max_tiles, 2, dtype=torch.int32, device=dev)
     counts = torch.zeros(3, dtype=torch.int32, device=dev)  # n_items, overflow, n_tiles
-    engine._run("ffs_reml_window_items", lib.ffs_reml_window_items, ncell, _p(cell_end), n_a, n_b, _p(f.lattice),
+    engine._run("ffs_reml_window_items", lib.ffs_reml_window_items, nkey, _p(cell_end), n_a, n_b, _p(f.lattice),
                 K, max_pairs, _p(items), _p(counts), max_items, _p(tiles), counts.data_ptr() + 8, max_tiles,
-                counts.data_ptr() + 4, st)
+                counts.data_ptr() + 4, Pd, st)
     if join is not None:  # the factors may still be in flight on another stream
         join()
-    c = _window_consts(f)
+    c = dict(c, dcf=grp["dcf"], c_p0=grp["c_p0"]) if grp is not None else _window_consts(f)
     winproj = torch.empty(n, WIN_SLOTS, dtype=torch.float32, device=dev)
-    ja = _lib.ProjectArgs(V=n, T=T, K=K, P=P, ld_y=ld, ld_u=ld, yr_hi=_p(hi), yr_lo=_p(lo),
+    ja = _lib.ProjectArgs(V=n, T=T, K=K, P=P * f.n_designs, ld_y=ld, ld_u=ld, yr_hi=_p(hi), yr_lo=_p(lo),
                           u_hi=_p(f.U_hi), u_lo=_p(f.U_lo), yexp=_p(yexp), uexp=_p(f.uexp), yr_t=None, U=None,
                           proj=_p(winproj), flag=_p(flag))
     engine._run("ffs_reml_project_tc_list", lib.ffs_reml_project_tc_list, C.byref(ja), _p(items), _p(counts),
@@ -349,7 +357,7 @@ def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None):
                 _p(tiles), counts.data_ptr() + 8, max_tiles, _p(pre.rows), _p(f.coef), _p(winproj), _p(c["dcf"]),
                 _p(c["ident"]), c["p_id"], _p(c["c_p0"]),
                 _p(out["best"]), _p(out["dbest"]), _p(out["crit0"]), _p(out["fb"]), _p(out["cell"]), _p(next_cen),
-                st)
+                _p(grp["design"]) if grp is not None else None, Pd, st)
     if out.get("count_evals"):  # statistics only: (voxel, pair) windows evaluated
         out["pair_evals"] = out.get("pair_evals", 0) + c["evals"][cen.long()].sum()
     return counts
@@ -514,43 +522,97 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
 
 def grouped_learned_fit(Y: torch.Tensor, factors: engine.GridFactors, design: np.ndarray, Xs: torch.Tensor,
                         proposal: ArmaProposal, layout: RunLayout, *, do_scale: bool = True, recenter: int = 0,
-                        gls_kw: dict | None = None, lj=None):
-    """The learned-seeded fit of a grouped fit (one design per voxel group):
-    ``factors`` is the multi-design build of Xs (D, T, K) and ``design`` [V]
-    (host) each voxel's design. Each design's voxels run the single-design
-    search (learned_search) and GLS against that design's view of the factors
-    (engine.design_view); the results are scattered back to voxel order.
+                        gls_kw: dict | None = None, lj=None, slots: engine.DesignSlots | None = None):
+    """The learned-seeded fit of a grouped fit (one design per voxel group),
+    every design in one pass per stage: ``factors`` is the multi-design build
+    of Xs (D, T, K) and ``design`` [V] (host) each voxel's design. The voxels
+    sit in the design slots of the grouped search (engine.design_slots: each
+    design's voxels padded to whole tiles), the prep residualises each tile
+    against its design's basis and forms the proposal's features, and the
+    window rounds sort the rows by design and window centre, so every work
+    item and criterion tile belongs to one design (its U rows, its criterion
+    constants). The strip next to the identity line is not run here. The
+    voxels a window leaves undecided take the grouped full-grid search; the
+    GLS refits every voxel against its own design. ``slots``: the design
+    slots of ``design`` when the caller has them.
     Returns (best, best_crit, scale, GlsOut, voxels the full grid decided)."""
+    lib = _lib.load()
     dev = Y.device
-    V = Y.shape[0]
-    design = np.asarray(design).reshape(-1)
-    best = torch.empty(V, dtype=torch.int32, device=dev)
-    best_crit = torch.empty(V, dtype=torch.float32, device=dev)
-    scale = torch.empty(V, dtype=torch.float32, device=dev)
-    out = None
-    n_fb = 0.0
-    for d in range(Xs.shape[0]):
-        idx = np.nonzero(design == d)[0]
-        if idx.size == 0:
-            continue
-        sel = torch.from_numpy(idx).to(dev)
-        Yd = Y.index_select(0, sel)
-        flag, _ = engine.constant_flag(Xs[d])
-        fv = engine.design_view(factors, d, center_flag=flag)
-        lo = learned_search(Yd, fv, proposal, layout, do_scale=do_scale, recenter=recenter)
-        go = engine.gls(Yd, lo.scale, lo.best, fv, Xs[d], lj=lj, **(gls_kw or {}))
-        best.index_copy_(0, sel, lo.best)
-        best_crit.index_copy_(0, sel, lo.best_crit)
-        scale.index_copy_(0, sel, lo.scale)
-        if out is None:
-            out = engine.GlsOut(**{k: None if t is None else torch.empty((V,) + tuple(t.shape[1:]), dtype=t.dtype,
-                                                                          device=dev)
-                                   for k, t in vars(go).items() if not k.startswith("_")})
-        for k, t in vars(go).items():
-            if not k.startswith("_") and t is not None:
-                getattr(out, k).index_copy_(0, sel, t)
-        n_fb += lo.stats["fallback"] * idx.size
-    return best, best_crit, scale, out, n_fb
+    Y = Y.float().contiguous()
+    V, T = Y.shape
+    f = factors
+    g = f.grid
+    D, P, K, ld = f.n_designs, f.P, f.K, f.ld
+    st = _st()
+    if slots is None:
+        slots = engine.design_slots(np.asarray(design).reshape(-1), D, K, P, dev)
+    Vp = slots.Vp
+    n_a, n_b = len(g.a_axis), len(g.b_axis)
+    ncell = n_a * n_b
+    c = _grid_consts(g, dev)
+    # the prep of every slot (zero rows in the padding) against its design's
+    # basis, U of (0, 0) per design
+    q0 = f.U.view(D, P, K, -1)[:, g.p0].contiguous()
+    pre = engine.PrepOut(scale=torch.empty(V, dtype=torch.float32, device=dev), yr_t=None, yr_hi=None, yr_lo=None,
+                         yexp=torch.empty(Vp, dtype=torch.int32, device=dev))
+    pre.feats = torch.empty(Vp, 9, dtype=torch.float32, device=dev)
+    pre.rows = torch.empty(Vp, T, dtype=torch.float32, device=dev)
+    rs = engine.const_dev(layout.run_start, dev)
+    pa = _lib.PrepArgs(V=Vp, T=T, K=K, Y=_p(Y), Q0=_p(q0), do_scale=int(do_scale), center=0, ld_y=ld,
+                       scale=_p(pre.scale), yr_t=None, yr_hi=None, yr_lo=None, yexp=_p(pre.yexp),
+                       idx=_p(slots.idx), feats=_p(pre.feats), n_runs=layout.n_runs, run_start=_p(rs),
+                       yr_rows=_p(pre.rows), center_dev=_p(f.center_flag), tile_design=_p(slots.tile32))
+    engine._run("ffs_reml_prep", lib.ffs_reml_prep, C.byref(pa), st)
+    prop = proposal.forward(pre.feats)
+    center = torch.empty(Vp, dtype=torch.int32, device=dev)
+    engine._run("ffs_reml_centers", lib.ffs_reml_centers, Vp, _p(prop), _p(c["a_ax"]), n_a, _p(c["b_ax"]), n_b,
+                _p(center), st)
+    center = torch.where(slots.idx >= 0, center, torch.full_like(center, ncell))  # the padding takes no window
+    # each slot's design and the criterion constants of every design
+    dslot = slots.tile32.repeat_interleave(32).contiguous()
+    ldx = f.logdet_XtX.view(D, P)
+    c_p0 = (f.logdet_R[g.p0] + ldx[:, g.p0]).contiguous()
+    dcf = ((f.logdet_R[None, :] + ldx) - c_p0[:, None]).float().reshape(-1).contiguous()
+    grp = {"design": dslot, "D": D, "dcf": dcf, "c_p0": c_p0}
+    out = dict(best=torch.empty(Vp, dtype=torch.int32, device=dev),
+               dbest=torch.empty(Vp, dtype=torch.float32, device=dev),
+               crit0=torch.empty(Vp, dtype=torch.float64, device=dev), fb=torch.zeros(Vp, dtype=torch.int32, device=dev),
+               cell=torch.empty(Vp, dtype=torch.int32, device=dev))
+    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    # the next round's centres: a round writes those of the rows it takes, so
+    # the padding slots (never taken) keep "no window"
+    nxt = [torch.full((Vp,), ncell, dtype=torch.int32, device=dev) for _ in range(min(recenter, 2))]
+    counts = [_window_round(pre, f, center, out, flag=flag, next_cen=nxt[0] if recenter else None, grp=grp)]
+    for r in range(recenter):
+        after = None
+        if r + 1 < recenter:
+            after = nxt[(r + 1) % 2]
+            after.fill_(ncell)
+        counts.append(_window_round(pre, f, nxt[r % 2], out, flag=flag, next_cen=after, grp=grp))
+    best_crit = torch.empty(Vp, dtype=torch.float32, device=dev)
+    small = torch.empty(2 + len(counts), dtype=torch.int32, device=dev)
+    extra = (C.c_void_p * (1 + len(counts)))(flag.data_ptr(), *[cn.data_ptr() + 4 for cn in counts])
+    engine._run("ffs_reml_window_finish", lib.ffs_reml_window_finish, Vp, _p(out["crit0"]), _p(out["dbest"]),
+                _p(out["fb"]), _p(best_crit), _p(small), len(extra), extra, st)
+    host = small.cpu()
+    if int(host[1]) != 0:
+        raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {int(host[1])})")
+    if bool((host[2:] != 0).any()):
+        raise RuntimeError("ffs_reml_window_items: work list overflow")
+    # back to voxel order; the undecided voxels through the grouped full grid
+    best = out["best"].index_select(0, slots.real)
+    crit = best_crit.index_select(0, slots.real)
+    fbv = out["fb"].index_select(0, slots.real)
+    n_fb = int(host[0])
+    if n_fb:
+        sel = torch.nonzero(fbv).reshape(-1)
+        gid_sub = np.asarray(design).reshape(-1)[sel.cpu().numpy()]
+        sub = engine.design_slots(gid_sub, D, K, P, dev)
+        so = engine.search_designs(Y.index_select(0, sel), f, sub, hierarchical=False, do_scale=do_scale)
+        best.index_copy_(0, sel, so.best)
+        crit.index_copy_(0, sel, so.best_crit)
+    go = engine.gls(Y, pre.scale, best, f, Xs, lj=lj, design=slots.design, **(gls_kw or {}))
+    return best, crit, pre.scale, go, float(n_fb)
 
 
 def train_proposal(X: torch.Tensor, layout: RunLayout, a_grid, b_grid, *, n_voxels: int = 6_000_000,

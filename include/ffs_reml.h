@@ -520,7 +520,8 @@ int ffs_reml_gls_grouped(const ffs_gls_args* a, int lj_h, const int* lj_tau, con
 
 /* Counting sort of voxels by pair: order[] lists voxel ids grouped by best[].
  * Replaces the torch.unique / sort grouping of fastfuncstuff/glm/arma.py:4794-4811.
- * work: int[P + 1]; on return work[g] is the end of pair g's voxels in order. */
+ * work: int[P + 1]; on return work[g] is the end of pair g's voxels in order.
+ * Keys outside [0, P) are left out (order then holds work[P - 1] entries). */
 int ffs_reml_group(int V, int P, const int* best, int* work, int* order, void* stream);
 
 /* --------------------------------------------------------- learned proposal
@@ -576,10 +577,12 @@ int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const int* idx, co
  * slot0 = 5 * window row + window column, and one tile (v0, nv) = tiles[2t],
  * tiles[2t+1] per 128-row tile of a cell for ffs_reml_window. The counts go to
  * *n_items and *n_tiles (clamped to max_items, max_tiles; *overflow = 1 if
- * anything was dropped). */
+ * anything was dropped). With P > 0 (grouped designs) the sort keys are
+ * design * n_a n_b + cell (ncell = n_designs * n_a n_b) and the items' U rows
+ * those of the key's design, (design * P + pair) * K. */
 int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, const int* lattice, int K,
                           int max_pairs, ffs_tc_item* items, int* n_items, int max_items, int* tiles,
-                          int* n_tiles, int max_tiles, int* overflow, void* stream);
+                          int* n_tiles, int max_tiles, int* overflow, int P, void* stream);
 
 /* The windowed refine's criterion over the tiles of ffs_reml_window_items
  * (launched for max_tiles, *n_tiles of them real), one sorted row i < n (voxel
@@ -598,12 +601,15 @@ int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, cons
  * identity pair and nothing below d = 0), best_cell (the lattice cell of the
  * best non-identity pair, -1 if none) and, when next_center is given, the
  * voxel's centre for a re-centred round: best_cell when fallback = 1 and
- * best_cell >= 0, else n_a * n_b (no window). */
+ * best_cell >= 0, else n_a * n_b (no window). With design (grouped designs,
+ * [V] each voxel's design, one design per tile as the design-major sort keys
+ * of ffs_reml_window_items leave them), dcf is [n_designs][P] and c_p0
+ * [n_designs], each read at the tile's design. */
 int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx, const int* center,
                     const int* tiles, const int* n_tiles, int max_tiles, const float* rows, const float* coef,
                     const float* winproj, const float* dcf, const unsigned char* ident, int p_id,
                     const double* c_p0, int* best, float* dbest, double* crit0, int* fallback, int* best_cell,
-                    int* next_center, void* stream);
+                    int* next_center, const int* design, int P, void* stream);
 
 /* The strip next to the identity line in the learned-seeded refine (no
  * reference counterpart: the reference searches every pair). Near lambda = 0

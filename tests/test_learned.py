@@ -449,14 +449,16 @@ def test_learned_fit_with_t_not_a_multiple_of_four(cuda_graphs):
 @pytest.mark.gpu
 def test_grouped_learned_fit_equals_per_group_learned_fits():
     """fit_glm_arma11_grouped with a proposal: one grid build over every
-    design, then each design's voxels through the learned search and GLS
-    against that design's view of it. Each voxel's arithmetic is the
-    single-design learned fit's, so the results are those of fitting every
-    group alone with the same proposal (workload-2 shapes: 4 censored runs,
-    N=855, 6 of the 20 designs), and the pairs agree with the grouped full
-    grid where the windows hold the answer."""
-    from fastfuncstuff_gb300 import fit_glm_arma11, fit_glm_arma11_grouped, synth
-    from fastfuncstuff_gb300.glm import learned
+    design, the voxels in the grouped search's design slots, window rounds
+    whose rows are sorted by design and window centre (every work item and
+    criterion tile of one design). Each voxel's arithmetic is that of the
+    learned search of its group alone against that design's view of the
+    build (the strip next to the identity line off, as the grouped fit runs
+    it): the same pairs and GLS outputs bit for bit (workload-2 shapes: 4
+    censored runs, N=855, 6 of the 20 designs); the pairs agree with the
+    grouped exhaustive full grid where the windows hold the answer."""
+    from fastfuncstuff_gb300 import fit_glm_arma11_grouped, synth
+    from fastfuncstuff_gb300.glm import engine, learned
     from fastfuncstuff_gb300.glm import grid as G
 
     dev = torch.device("cuda:0")
@@ -472,14 +474,20 @@ def test_grouped_learned_fit_equals_per_group_learned_fits():
               force_exhaustive_search=True, want_residuals=True)
     got = fit_glm_arma11_grouped(Y, designs, gid, tr=2.0, proposal=prop, proposal_recenter=1, **kw)
     assert 0.0 <= float(got.learned_fallback) < 0.5
+    grid = G.make_grid(gr, gr)
+    f_all = engine.build_factors(fam, grid, lay)
     for h in range(6):
         m = gid == h
-        ref = fit_glm_arma11(Y[m], designs[h], tr=2.0, proposal=prop, proposal_recenter=1, cuda_graphs=False,
-                             **kw)
-        np.testing.assert_array_equal(got.arma_params.numpy()[m], ref.arma_params.numpy())
-        for name in ("reml_likelihood", "betas", "tstats", "sigma2", "fstats", "r2", "arma_lambda", "residuals",
-                     "residuals_whitened"):
-            np.testing.assert_array_equal(getattr(got, name).numpy()[m], getattr(ref, name).numpy(), err_msg=name)
+        Yh = torch.from_numpy(Y[m]).to(dev)
+        fv = engine.design_view(f_all, h, center_flag=engine.constant_flag(fam[h])[0])
+        lo = learned.learned_search(Yh, fv, prop, lay, recenter=1, strip_k0=-1)
+        go = engine.gls(Yh, lo.scale, lo.best, fv, fam[h], want_residuals=True)
+        best = lo.best.cpu().numpy()
+        np.testing.assert_array_equal(got.arma_params.numpy()[m], np.stack([grid.a[best], grid.b[best]], 1))
+        np.testing.assert_array_equal(got.reml_likelihood.numpy()[m], lo.best_crit.cpu().numpy())
+        for name, ref in (("betas", go.betas), ("tstats", go.tstats), ("sigma2", go.sigma2), ("r2", go.r2),
+                          ("residuals", go.resid), ("residuals_whitened", go.resid_w)):
+            np.testing.assert_array_equal(getattr(got, name).numpy()[m], ref.cpu().numpy(), err_msg=name)
     full = fit_glm_arma11_grouped(Y, designs, gid, tr=2.0, **kw)
     same = (got.arma_params == full.arma_params).all(1)
     assert float(same.float().mean()) >= 0.97
