@@ -42,23 +42,30 @@ __global__ void window_items_kernel(int ncell, const int* end, int n_a, int n_b,
                                     int* n_tiles, int max_tiles, int* overflow, int P) {
   const int key = blockIdx.x * blockDim.x + threadIdx.x;
   if (key >= ncell) return;
+  // with designs (P > 0) the key is cell * n_designs + design: the work items
+  // of a key read its design's U rows, (design * P + pair) * K, and the
+  // criterion tiles of a cell span the rows of all its designs (the window
+  // is the cell's), emitted by the key of the cell's first design
+  const int D = P > 0 ? ncell / (n_a * n_b) : 1;
+  const int c = key / D, dsg = key % D;
+  const int row0 = dsg * P * K;
   const int s0 = key ? end[key - 1] : 0, n = end[key] - s0;
+  if (dsg == 0) {
+    const int cn = end[key + D - 1] - s0;
+    const int ntile = (cn + WTILE - 1) / WTILE;
+    const int tt = ntile > 0 ? atomicAdd(n_tiles, ntile) : 0;
+    for (int t = 0; t < ntile; ++t) {
+      if (tt + t >= max_tiles) {
+        atomicExch(overflow, 1);
+        break;
+      }
+      tiles[tt + t] = make_int2(s0 + t * WTILE, min(WTILE, cn - t * WTILE));
+    }
+  }
   if (n <= 0) return;
-  // with designs (P > 0) the key is design * n_a n_b + cell, and the U rows
-  // of the design's pairs start at (design * P + pair) * K
-  const int c = P > 0 ? key % (n_a * n_b) : key;
-  const int row0 = P > 0 ? (key / (n_a * n_b)) * P * K : 0;
   int a0, wa, b0, wb;
   window_of(c, n_a, n_b, a0, wa, b0, wb);
   const int ntile = (n + WTILE - 1) / WTILE;
-  const int tt = atomicAdd(n_tiles, ntile);
-  for (int t = 0; t < ntile; ++t) {
-    if (tt + t >= max_tiles) {
-      atomicExch(overflow, 1);
-      break;
-    }
-    tiles[tt + t] = make_int2(s0 + t * WTILE, min(WTILE, n - t * WTILE));
-  }
   // the window's runs of consecutive valid pairs (at most one per pair)
   int seg_p[WSLOTS], seg_np[WSLOTS], seg_slot[WSLOTS], nseg = 0;
   for (int ra = 0; ra < wa; ++ra) {
@@ -163,7 +170,9 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
   const int i = tl.x + tid;
   const bool live = tid < tl.y;
   const int c = w.center[w.idx[tl.x]];  // every row of the tile has this centre
-  const int dsg = w.design ? w.design[w.idx[tl.x]] : 0;  // and this design
+  // the row's design (grouped designs: a tile's rows share the cell, not
+  // necessarily the design) and its criterion constants
+  const int dsg = w.design ? w.design[w.idx[live ? i : tl.x]] : 0;
   const float* dcf = w.dcf + (size_t)dsg * w.P;
   int a0, wa, b0, wb;
   window_of(c, w.n_a, w.n_b, a0, wa, b0, wb);

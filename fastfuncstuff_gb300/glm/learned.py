@@ -306,8 +306,8 @@ def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None, grp=None)
     voxels taken stays on the device. pre is the prep of every voxel (fp16
     operands and voxel-major rows). ``grp`` (grouped designs: a multi-design
     ``f``) gives each row's design and the per-design criterion constants;
-    the rows are then sorted by design and centre, so every tile and work
-    item belongs to one design."""
+    the rows are then sorted by centre and design, so every work item reads
+    one design's U rows and every criterion tile one window."""
     lib = _lib.load()
     dev = pre.scale.device
     g = f.grid
@@ -317,12 +317,13 @@ def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None, grp=None)
     ncell = n_a * n_b
     n = cen.numel()
     c = _grid_consts(g, dev)
-    # voxels sorted by window centre (by design, then centre, for grouped
-    # designs); the skipped ones (the last bucket) last
+    # voxels sorted by window centre (for grouped designs by centre, then
+    # design: a criterion tile spans a centre's designs, a work item one
+    # design); the skipped ones (the last bucket) last
     nkey, keys, Pd = ncell, cen, 0
     if grp is not None:
         nkey, Pd = grp["D"] * ncell, P
-        keys = torch.where(cen < ncell, grp["design"] * ncell + cen, torch.full_like(cen, nkey)).contiguous()
+        keys = torch.where(cen < ncell, cen * grp["D"] + grp["design"], torch.full_like(cen, nkey)).contiguous()
     idx = torch.empty(n, dtype=torch.int32, device=dev)
     cell_end = torch.empty(nkey + 2, dtype=torch.int32, device=dev)
     engine._run("ffs_reml_group", lib.ffs_reml_group, n, nkey + 1, _p(keys), _p(cell_end), _p(idx), st)
@@ -529,9 +530,9 @@ def grouped_learned_fit(Y: torch.Tensor, factors: engine.GridFactors, design: np
     sit in the design slots of the grouped search (engine.design_slots: each
     design's voxels padded to whole tiles), the prep residualises each tile
     against its design's basis and forms the proposal's features, and the
-    window rounds sort the rows by design and window centre, so every work
-    item and criterion tile belongs to one design (its U rows, its criterion
-    constants). The strip next to the identity line is not run here. The
+    window rounds sort the rows by window centre and design: every work item
+    reads one design's U rows, every criterion tile holds one window's rows
+    of any design, each row with its design's criterion constants. The strip next to the identity line is not run here. The
     voxels a window leaves undecided take the grouped full-grid search; the
     GLS refits every voxel against its own design. ``slots``: the design
     slots of ``design`` when the caller has them.

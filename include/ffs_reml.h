@@ -578,8 +578,9 @@ int ffs_reml_gather(int n, const int* n_dev, int T, int ld_y, const int* idx, co
  * tiles[2t+1] per 128-row tile of a cell for ffs_reml_window. The counts go to
  * *n_items and *n_tiles (clamped to max_items, max_tiles; *overflow = 1 if
  * anything was dropped). With P > 0 (grouped designs) the sort keys are
- * design * n_a n_b + cell (ncell = n_designs * n_a n_b) and the items' U rows
- * those of the key's design, (design * P + pair) * K. */
+ * cell * n_designs + design (ncell = n_designs * n_a n_b): the items' U rows
+ * are those of the key's design, (design * P + pair) * K, and the tiles span
+ * a cell's rows of every design. */
 int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, const int* lattice, int K,
                           int max_pairs, ffs_tc_item* items, int* n_items, int max_items, int* tiles,
                           int* n_tiles, int max_tiles, int* overflow, int P, void* stream);
@@ -602,9 +603,8 @@ int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, cons
  * best non-identity pair, -1 if none) and, when next_center is given, the
  * voxel's centre for a re-centred round: best_cell when fallback = 1 and
  * best_cell >= 0, else n_a * n_b (no window). With design (grouped designs,
- * [V] each voxel's design, one design per tile as the design-major sort keys
- * of ffs_reml_window_items leave them), dcf is [n_designs][P] and c_p0
- * [n_designs], each read at the tile's design. */
+ * [V] each voxel's design), dcf is [n_designs][P] and c_p0 [n_designs], each
+ * read at the row's design. */
 int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx, const int* center,
                     const int* tiles, const int* n_tiles, int max_tiles, const float* rows, const float* coef,
                     const float* winproj, const float* dcf, const unsigned char* ident, int p_id,
