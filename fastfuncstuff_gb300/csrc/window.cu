@@ -106,6 +106,36 @@ __global__ void window_items_kernel(int ncell, const int* end, int n_a, int n_b,
   }
 }
 
+// one thread per segment s of the sorted rows [end[s-1], end[s]) (end[-1] =
+// 0): an item per 128-row tile and block of at most max_pairs of the
+// segment's n_pairs pairs, U rows from (s * n_pairs + first pair) * K
+__global__ void segment_items_kernel(int n_seg, const int* end, int n_pairs, int K, int max_pairs,
+                                     ffs_tc_item* items, int* n_items, int max_items, int* overflow) {
+  const int sg = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sg >= n_seg) return;
+  const int s0 = sg ? end[sg - 1] : 0, n = end[sg] - s0;
+  if (n <= 0) return;
+  const int ntile = (n + WTILE - 1) / WTILE, nblk = (n_pairs + max_pairs - 1) / max_pairs;
+  const int at = atomicAdd(n_items, ntile * nblk);
+  for (int t = 0; t < ntile; ++t) {
+    for (int bk = 0; bk < nblk; ++bk) {
+      const int k = at + t * nblk + bk;
+      if (k >= max_items) {
+        atomicExch(overflow, 1);
+        return;
+      }
+      ffs_tc_item it;
+      it.v0 = s0 + t * WTILE;
+      it.nv = min(WTILE, n - t * WTILE);
+      it.row_b = (sg * n_pairs + bk * max_pairs) * K;
+      it.np = min(max_pairs, n_pairs - bk * max_pairs);
+      it.out0 = it.v0;
+      it.slot0 = bk * max_pairs;
+      items[k] = it;
+    }
+  }
+}
+
 __global__ void clamp_count_kernel(int* n_items, int max_items, int* n_tiles, int max_tiles) {
   if (*n_items > max_items) *n_items = max_items;
   if (*n_tiles > max_tiles) *n_tiles = max_tiles;
@@ -472,6 +502,8 @@ struct StripArgs {
   const double* crit0;   // [V] the criterion at (0, 0)
   int* fallback;         // [V]
   int* best_cell;        // [V]
+  const int* design;     // [V] each voxel's design (dcf [n_designs][P]), or NULL (dcf [P])
+  int P;                 // pairs per design
 };
 
 __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
@@ -591,6 +623,8 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
   }
   if (!live) return;
   const float Tk = (float)(T - w.K);
+  const int v = w.idx[i];
+  const float* dcf = w.dcf + (w.design ? (size_t)w.design[v] * w.P : 0);
   float bd = INFINITY;
 #pragma unroll
   for (int j = 0; j < STRIP_G2; ++j) {
@@ -601,11 +635,10 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
       const int q = 2 * j + h;
       if (q < nq) {
         const float rss = fmaxf(s2[h] - w.proj[(size_t)(q0 + q) * w.n + i], 0.f);
-        bd = fminf(bd, w.dcf[w.pairs[q0 + q]] + Tk * log1pf((rss - yy) / (yy + 1e-10f)));
+        bd = fminf(bd, dcf[w.pairs[q0 + q]] + Tk * log1pf((rss - yy) / (yy + 1e-10f)));
       }
     }
   }
-  const int v = w.idx[i];
   if (bd < w.dbest[v] - 1e-6f * fabsf((float)w.crit0[v])) {
     w.fallback[v] = 1;
     w.best_cell[v] = -1;
@@ -803,6 +836,21 @@ extern "C" int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, in
   return check_launch("window_items_kernel");
 }
 
+extern "C" int ffs_reml_segment_items(int n_seg, const int* seg_end, int n_pairs, int K, int max_pairs,
+                                      ffs_tc_item* items, int* n_items, int max_items, int* overflow, void* stream) {
+  clear_error();
+  FFS_REQUIRE(n_seg > 0 && n_pairs > 0 && K > 0 && max_pairs > 0 && max_pairs * K <= 256 && max_items > 0,
+              "ffs_reml_segment_items: bad sizes");
+  FFS_REQUIRE(seg_end && items && n_items && overflow, "ffs_reml_segment_items: null buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  FFS_CUDA(cudaMemsetAsync(n_items, 0, sizeof(int), st));
+  FFS_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), st));
+  segment_items_kernel<<<ceil_div(n_seg, 128), 128, 0, st>>>(n_seg, seg_end, n_pairs, K, max_pairs, items, n_items,
+                                                              max_items, overflow);
+  clamp_count_kernel<<<1, 1, 0, st>>>(n_items, max_items, n_items, max_items);
+  return check_launch("segment_items_kernel");
+}
+
 extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx,
                                const int* center, const int* tiles, const int* n_tiles, int max_tiles,
                                const float* rows, const float* coef, const float* winproj, const float* dcf,
@@ -836,8 +884,9 @@ extern "C" int ffs_reml_centers(int V, const float* prop, const float* a_axis, i
 extern "C" int ffs_reml_strip(int n, const int* n_dev, int T, int K, int n_pairs, const int* pairs, const int* idx,
                               const float* rows, const float* coef, const float* proj, const float* dcf,
                               const float* dbest, const double* crit0, int* fallback, int* best_cell,
-                              void* stream) {
+                              const int* design, int P, void* stream) {
   clear_error();
+  FFS_REQUIRE(!design || P > 0, "ffs_reml_strip: designs need P > 0");
   FFS_REQUIRE(n > 0 && T > K && K > 0 && n_pairs > 0 && n_pairs <= STRIP_MAX,
               "ffs_reml_strip: bad sizes (n=%d T=%d K=%d n_pairs=%d, at most %d pairs)", n, T, K, n_pairs,
               STRIP_MAX);
@@ -846,7 +895,7 @@ extern "C" int ffs_reml_strip(int n, const int* n_dev, int T, int K, int n_pairs
   FFS_REQUIRE(((uintptr_t)rows & 15) == 0 && ((uintptr_t)coef & 15) == 0,
               "ffs_reml_strip: rows and coef must be 16-byte aligned");
   StripArgs w{n, T, K, n_pairs, n_dev, pairs, idx, rows, reinterpret_cast<const float4*>(coef), proj, dcf, dbest,
-              crit0, fallback, best_cell};
+              crit0, fallback, best_cell, design, P};
   const dim3 grid(ceil_div(n, STRIP_TILE), ceil_div(n_pairs, STRIP_G));
   strip_crit_kernel<<<grid, STRIP_TILE, 0, (cudaStream_t)stream>>>(w);
   return check_launch("strip_crit_kernel");

@@ -252,6 +252,59 @@ STAGE_CHUNKS = 8  # chunks of rows a staged run copies in and preps one after an
 STRIP_K0 = 2  # voxels whose answer lies this close to the identity line get the strip next to it
 
 
+def _strip_round_grouped(pre, f, out, *, flag, k0: int, grp: dict, pad: torch.Tensor):
+    """_strip_round for grouped designs, every design in one pass: the
+    near-line voxels (padding slots excluded) sorted by design
+    (ffs_reml_group), their rows split to fp16 while gathered, one work-list
+    projection (ffs_reml_segment_items: each design's segment against that
+    design's U rows of the strip pairs) and one ffs_reml_strip launch that
+    reads each row's design constants. Returns the device counts [items,
+    list overflow]."""
+    lib = _lib.load()
+    dev = pre.scale.device
+    c = _grid_consts(f.grid, dev)
+    sc = c["strip"]
+    if sc["n"] == 0:
+        return None
+    V = out["best"].numel()
+    K, P, T, ld, D = f.K, f.P, f.T, f.ld, grp["D"]
+    st = _st()
+    nq = sc["n"]
+    near = (c["dist_id"].index_select(0, out["best"].long()) <= k0) & (out["fb"] == 0) & ~pad
+    keys = torch.where(near, grp["design"], torch.full_like(grp["design"], D)).contiguous()
+    idx = torch.empty(V, dtype=torch.int32, device=dev)
+    seg_end = torch.empty(D + 2, dtype=torch.int32, device=dev)
+    engine._run("ffs_reml_group", lib.ffs_reml_group, V, D + 1, _p(keys), _p(seg_end), _p(idx), st)
+    count = seg_end[D - 1 : D]  # device count of the near-line voxels
+    hi = torch.empty(V, ld, dtype=torch.int16, device=dev)
+    lo = torch.empty(V, ld, dtype=torch.int16, device=dev)
+    yexp = torch.empty(V, dtype=torch.int32, device=dev)
+    engine._run("ffs_reml_gather", lib.ffs_reml_gather, V, _p(count), T, ld, _p(idx), None, None, _p(pre.yexp),
+                _p(pre.rows), _p(hi), _p(lo), _p(yexp), None, st)
+    # the strip pairs' U rows of every design: [D][nq][K][ld]
+    rows = (torch.arange(D, device=dev)[:, None] * P + sc["pairs"][None, :]).reshape(-1)
+    u_hi = f.U_hi.view(D * P, K * ld).index_select(0, rows)
+    u_lo = f.U_lo.view(D * P, K * ld).index_select(0, rows)
+    uex = f.uexp.index_select(0, rows)
+    max_pairs = min(nq, 256 // K)
+    max_items = (-(-V // 128) + D) * -(-nq // max_pairs)
+    items = torch.empty(max_items, 6, dtype=torch.int32, device=dev)
+    counts = torch.zeros(2, dtype=torch.int32, device=dev)  # n_items, overflow
+    engine._run("ffs_reml_segment_items", lib.ffs_reml_segment_items, D, _p(seg_end), nq, K, max_pairs, _p(items),
+                _p(counts), max_items, counts.data_ptr() + 4, st)
+    proj = torch.empty(nq, V, dtype=torch.float32, device=dev)
+    pa = _lib.ProjectArgs(V=V, T=T, K=K, P=D * nq, ld_y=ld, ld_u=ld, yr_hi=_p(hi), yr_lo=_p(lo), u_hi=_p(u_hi),
+                          u_lo=_p(u_lo), yexp=_p(yexp), uexp=_p(uex), yr_t=None, U=None, proj=_p(proj), flag=_p(flag))
+    engine._run("ffs_reml_project_tc_list", lib.ffs_reml_project_tc_list, C.byref(pa), _p(items), _p(counts),
+                max_items, max_pairs, 0, st)
+    engine._run("ffs_reml_strip", lib.ffs_reml_strip, V, _p(count), T, K, nq, _p(sc["pairs32"]), _p(idx),
+                _p(pre.rows), _p(f.coef), _p(proj), _p(grp["dcf"]), _p(out["dbest"]), _p(out["crit0"]),
+                _p(out["fb"]), _p(out["cell"]), _p(grp["design"]), P, st)
+    out["strip_voxels"] = count
+    out.setdefault("_keep", []).append((keys, idx, seg_end, hi, lo, yexp, u_hi, u_lo, uex, items, proj))
+    return counts
+
+
 def _strip_round(pre, f, out, *, flag, k0: int):
     """The pairs next to the identity line (lattice distance 1) for the voxels
     whose answer lies within k0 lattice steps of it and that the full grid
@@ -291,7 +344,7 @@ def _strip_round(pre, f, out, *, flag, k0: int):
     engine._run("ffs_reml_project_tc", lib.ffs_reml_project_tc, C.byref(pa), st)
     engine._run("ffs_reml_strip", lib.ffs_reml_strip, V, _p(count), T, K, nq, _p(sc["pairs32"]), _p(ids),
                 _p(pre.rows), _p(f.coef), _p(proj), _p(c["dcf"]), _p(out["dbest"]), _p(out["crit0"]),
-                _p(out["fb"]), _p(out["cell"]), st)
+                _p(out["fb"]), _p(out["cell"]), None, 0, st)
     if out.get("count_evals"):
         out["pair_evals"] = out.get("pair_evals", 0) + nq * count.sum()
     out["strip_voxels"] = count
@@ -523,7 +576,8 @@ def learned_search(Y: torch.Tensor, factors: engine.GridFactors, proposal: ArmaP
 
 def grouped_learned_fit(Y: torch.Tensor, factors: engine.GridFactors, design: np.ndarray, Xs: torch.Tensor,
                         proposal: ArmaProposal, layout: RunLayout, *, do_scale: bool = True, recenter: int = 0,
-                        gls_kw: dict | None = None, lj=None, slots: engine.DesignSlots | None = None):
+                        gls_kw: dict | None = None, lj=None, slots: engine.DesignSlots | None = None,
+                        strip_k0: int = STRIP_K0):
     """The learned-seeded fit of a grouped fit (one design per voxel group),
     every design in one pass per stage: ``factors`` is the multi-design build
     of Xs (D, T, K) and ``design`` [V] (host) each voxel's design. The voxels
@@ -532,7 +586,10 @@ def grouped_learned_fit(Y: torch.Tensor, factors: engine.GridFactors, design: np
     against its design's basis and forms the proposal's features, and the
     window rounds sort the rows by window centre and design: every work item
     reads one design's U rows, every criterion tile holds one window's rows
-    of any design, each row with its design's criterion constants. The strip next to the identity line is not run here. The
+    of any design, each row with its design's criterion constants. The
+    strip next to the identity line (``strip_k0``, -1: off) evaluates each
+    near-line voxel against its design's strip pairs, all designs in one
+    pass. The
     voxels a window leaves undecided take the grouped full-grid search; the
     GLS refits every voxel against its own design. ``slots``: the design
     slots of ``design`` when the caller has them.
@@ -575,7 +632,7 @@ def grouped_learned_fit(Y: torch.Tensor, factors: engine.GridFactors, design: np
     c_p0 = (f.logdet_R[g.p0] + ldx[:, g.p0]).contiguous()
     dcf = ((f.logdet_R[None, :] + ldx) - c_p0[:, None]).float().reshape(-1).contiguous()
     grp = {"design": dslot, "D": D, "dcf": dcf, "c_p0": c_p0}
-    out = dict(best=torch.empty(Vp, dtype=torch.int32, device=dev),
+    out = dict(best=torch.zeros(Vp, dtype=torch.int32, device=dev),  # a valid pair in the padding slots too
                dbest=torch.empty(Vp, dtype=torch.float32, device=dev),
                crit0=torch.empty(Vp, dtype=torch.float64, device=dev), fb=torch.zeros(Vp, dtype=torch.int32, device=dev),
                cell=torch.empty(Vp, dtype=torch.int32, device=dev))
@@ -590,6 +647,10 @@ def grouped_learned_fit(Y: torch.Tensor, factors: engine.GridFactors, design: np
             after = nxt[(r + 1) % 2]
             after.fill_(ncell)
         counts.append(_window_round(pre, f, nxt[r % 2], out, flag=flag, next_cen=after, grp=grp))
+    if strip_k0 >= 0:  # the strip next to the identity line
+        sc_counts = _strip_round_grouped(pre, f, out, flag=flag, k0=strip_k0, grp=grp, pad=slots.idx < 0)
+        if sc_counts is not None:
+            counts.append(sc_counts)
     best_crit = torch.empty(Vp, dtype=torch.float32, device=dev)
     small = torch.empty(2 + len(counts), dtype=torch.int32, device=dev)
     extra = (C.c_void_p * (1 + len(counts)))(flag.data_ptr(), *[cn.data_ptr() + 4 for cn in counts])
@@ -599,7 +660,7 @@ def grouped_learned_fit(Y: torch.Tensor, factors: engine.GridFactors, design: np
     if int(host[1]) != 0:
         raise RuntimeError(f"ffs_reml_project_tc_list: a bounded wait expired (code {int(host[1])})")
     if bool((host[2:] != 0).any()):
-        raise RuntimeError("ffs_reml_window_items: work list overflow")
+        raise RuntimeError("a projection work list of the window rounds or the strip overflowed")
     # back to voxel order; the undecided voxels through the grouped full grid
     best = out["best"].index_select(0, slots.real)
     crit = best_crit.index_select(0, slots.real)

@@ -623,10 +623,25 @@ int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, c
  * relative to (0, 0) as ffs_reml_window forms it. A voxel v whose least strip
  * criterion lies below its window answer dbest[v] by more than
  * 1e-6 |crit0[v]| gets fallback[v] = 1 and best_cell[v] = -1 (the full grid
- * decides); nothing else is written. */
+ * decides); nothing else is written. With design (grouped designs, [V] each
+ * voxel's design, P pairs per design) dcf is [n_designs][P], read at the
+ * voxel's design; otherwise dcf is [P] and P is ignored. */
 int ffs_reml_strip(int n, const int* n_dev, int T, int K, int n_pairs, const int* pairs, const int* idx,
                    const float* rows, const float* coef, const float* proj, const float* dcf, const float* dbest,
-                   const double* crit0, int* fallback, int* best_cell, void* stream);
+                   const double* crit0, int* fallback, int* best_cell, const int* design, int P, void* stream);
+
+/* Work list of ffs_reml_project_tc_list for rows sorted into n_seg segments
+ * (segment s: sorted rows [seg_end[s-1], seg_end[s]), seg_end[-1] = 0, as
+ * ffs_reml_group leaves them) that each project onto their own n_pairs pairs:
+ * one ffs_tc_item per 128-row tile of a segment and block of at most
+ * max_pairs (max_pairs * K <= 256) of its pairs, U rows from
+ * (s * n_pairs + first pair) * K, output slot = the pair's rank (pair-major,
+ * ld_out = 0). The strip next to the identity line of a grouped fit uses one
+ * segment per design against the strip pairs' U rows of every design
+ * ([n_designs][n_pairs][K][ld]). The count goes to *n_items (clamped to
+ * max_items; *overflow = 1 if items were dropped). No reference counterpart. */
+int ffs_reml_segment_items(int n_seg, const int* seg_end, int n_pairs, int K, int max_pairs, ffs_tc_item* items,
+                           int* n_items, int max_items, int* overflow, void* stream);
 
 /* The voxels v < V whose pair best[v] lies within k0 lattice steps of an
  * identity pair (dist[p]: the Manhattan lattice distance of pair p to the

@@ -453,8 +453,8 @@ def test_grouped_learned_fit_equals_per_group_learned_fits():
     whose rows are sorted by design and window centre (every work item and
     criterion tile of one design). Each voxel's arithmetic is that of the
     learned search of its group alone against that design's view of the
-    build (the strip next to the identity line off, as the grouped fit runs
-    it): the same pairs and GLS outputs bit for bit (workload-2 shapes: 4
+    build, the strip next to the identity line included: the same pairs and
+    GLS outputs bit for bit (workload-2 shapes: 4
     censored runs, N=855, 6 of the 20 designs); the pairs agree with the
     grouped exhaustive full grid where the windows hold the answer."""
     from fastfuncstuff_gb300 import fit_glm_arma11_grouped, synth
@@ -480,7 +480,7 @@ def test_grouped_learned_fit_equals_per_group_learned_fits():
         m = gid == h
         Yh = torch.from_numpy(Y[m]).to(dev)
         fv = engine.design_view(f_all, h, center_flag=engine.constant_flag(fam[h])[0])
-        lo = learned.learned_search(Yh, fv, prop, lay, recenter=1, strip_k0=-1)
+        lo = learned.learned_search(Yh, fv, prop, lay, recenter=1)
         go = engine.gls(Yh, lo.scale, lo.best, fv, fam[h], want_residuals=True)
         best = lo.best.cpu().numpy()
         np.testing.assert_array_equal(got.arma_params.numpy()[m], np.stack([grid.a[best], grid.b[best]], 1))
