@@ -374,7 +374,9 @@ def fit_glm_arma11(
         # (fastfuncstuff/glm/arma.py:5603-5628)
         factors = engine.build_factors(Xd, grid, layout, task_indices=ti, glt=glt, with_tc=K <= TC_MAX_K,
                                        sets=sets, afull=Dd is not None and bool(column_sets))
-        ym = Y.to(device=device, dtype=torch.float32).mean(0, keepdim=True)
+        # the mean in the fit's dtype (the reference's data.mean(0)), searched
+        # in float32 like every series
+        ym = Y.to(device=device, dtype=out_dtype).mean(0, keepdim=True).float()
         so = engine.search(ym, factors, hierarchical=False, projector=_projector(factors), do_scale=False)
         best_all = so.best.expand(V).to(torch.int32).cpu()
         global_crit = so.best_crit[:1].expand(V)

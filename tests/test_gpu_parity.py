@@ -573,6 +573,20 @@ def test_global_arma_matches_oracle_and_reference():
     assert rel_maxnorm(got.betas.numpy(), d["f32__betas"]).max() <= 2e-3
 
 
+def test_global_arma_use_double_matches_fp64_reference():
+    """estimate_per_voxel=False under use_double: the mean series formed in
+    float64 as the reference's data.mean(0) is, the pair and likelihood of the
+    reference's own float64 run."""
+    d = load_golden("global")
+    kw = dict(a_grid=d["a_grid"], b_grid=d["b_grid"], run_starts=d["run_starts"], estimate_per_voxel=False)
+    got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, use_double=True, **kw)
+    assert got.betas.dtype == torch.float64
+    np.testing.assert_array_equal(got.arma_params.numpy(), d["f64__arma_params"])
+    np.testing.assert_allclose(got.reml_likelihood.numpy(), d["f64__reml_likelihood"], rtol=1e-5)
+    assert rel_maxnorm(got.betas.numpy(), d["f64__betas"]).max() <= BETA_REL
+    np.testing.assert_allclose(got.sigma2.numpy(), d["f64__sigma2"], rtol=1e-4)
+
+
 # ------------------------------------------- the benchmark workloads' shapes
 
 
