@@ -395,13 +395,19 @@ __device__ void band_chol_of_pair(const ffs_grid_desc& d, const ffs_grid_out& o,
 
 // Phase 1 of every pair once, for the items of all designs (coef and
 // logdet_R depend on the pair only): cm [P][T][4] and bad [P] in the
-// workspace, read back by grid_build_kernel.
+// workspace, read back by grid_build_kernel. With the banded R the pair's
+// band_L, band_coef, coef and logdet_R are written here, and cm keeps the
+// reciprocal diagonal and each row's band (the first 1.5 T doubles).
 __global__ void __launch_bounds__(GB_THREADS) pair_ldl_kernel(BuildArgs args, double* cm, int* bad) {
   __shared__ double red[32];
   __shared__ int bad_r;
-  extern __shared__ double cms[];  // [T][4]
+  extern __shared__ double cms[];  // [T][4], or with the band as band_chol_of_pair lays it out
   const int T = args.d.T;
-  ldl_of_pair(args.d, args.o, blockIdx.x, cms, red, &bad_r);
+  if (args.d.band)
+    band_chol_of_pair(args.d, args.o, blockIdx.x, cms, reinterpret_cast<int*>(cms + T), cms + T + (T + 1) / 2, red,
+                      &bad_r);
+  else
+    ldl_of_pair(args.d, args.o, blockIdx.x, cms, red, &bad_r);
   double2* dst = reinterpret_cast<double2*>(cm + (size_t)blockIdx.x * 4 * T);
   for (int i = threadIdx.x; i < 2 * T; i += blockDim.x) dst[i] = reinterpret_cast<const double2*>(cms)[i];
   if (threadIdx.x == 0) bad[blockIdx.x] = bad_r;
@@ -988,7 +994,9 @@ extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int
   FFS_REQUIRE(d->T > 0 && d->K > 0 && d->P > 0 && d->n_runs > 0,
               "ffs_grid_build_designs: T=%d K=%d P=%d n_runs=%d must be positive", d->T, d->K, d->P, d->n_runs);
   FFS_REQUIRE((long long)d->P * n_designs < (1LL << 31), "ffs_grid_build_designs: too many items");
-  FFS_REQUIRE(!d->band, "ffs_grid_build_designs: the banded R is built by ffs_grid_build (one design)");
+  FFS_REQUIRE(!d->band || (d->band_w >= 1 && d->band_w <= FFS_BAND_MAX_W && o->band_L && o->band_coef),
+              "ffs_grid_build_designs: the banded R needs 1 <= band_w=%d <= %d, band_L and band_coef", d->band_w,
+              FFS_BAND_MAX_W);
   FFS_REQUIRE(d->K <= d->T, "ffs_grid_build_designs: K=%d exceeds T=%d", d->K, d->T);
   FFS_REQUIRE(d->n_task >= 0 && d->n_task <= d->K, "ffs_grid_build_designs: bad n_task=%d", d->n_task);
   if (const int rc = check_sets(d, o, "ffs_grid_build_designs")) return rc;
@@ -1003,22 +1011,26 @@ extern "C" int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int
   const int grid = (int)(items < cap ? items : cap);
   BuildArgs args{*d, *o};
   const size_t smem = sizeof(double) * 4 * (size_t)d->T;
-  FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build_designs: T=%d too long", d->T);
-  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel<false>), smem));
+  // phase 1 of the banded R also holds the powers of a (band_chol_of_pair)
+  const size_t smem1 = d->band ? std::max(smem, sizeof(double) * ((size_t)d->T + (d->T + 1) / 2 +
+                                                                  (size_t)d->band_w + 1))
+                               : smem;
+  FFS_REQUIRE(smem1 <= 200 * 1024, "ffs_grid_build_designs: T=%d too long", d->T);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel<false>), smem1));
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel<true>), smem));
-  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(pair_ldl_kernel), smem));
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(pair_ldl_kernel), smem1));
   double* pair_cm = nullptr;
   int* pair_bad = nullptr;
   if (n_designs > 1) {
     pair_cm = o->work + designs_slot_doubles(d->T, d->K, d->P, n_designs, max_ctas);
     pair_bad = reinterpret_cast<int*>(pair_cm + (size_t)d->P * 4 * d->T);
-    pair_ldl_kernel<<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, pair_cm, pair_bad);
+    pair_ldl_kernel<<<d->P, GB_THREADS, smem1, (cudaStream_t)stream>>>(args, pair_cm, pair_bad);
     if (const int rc = check_launch("pair_ldl_kernel")) return rc;
   }
   if (pair_cm)
     grid_build_kernel<true><<<grid, GB_THREADS, smem, (cudaStream_t)stream>>>(args, n_designs, pair_cm, pair_bad);
   else
-    grid_build_kernel<false><<<grid, GB_THREADS, smem, (cudaStream_t)stream>>>(args, n_designs, nullptr, nullptr);
+    grid_build_kernel<false><<<grid, GB_THREADS, smem1, (cudaStream_t)stream>>>(args, n_designs, nullptr, nullptr);
   return check_launch("grid_build_kernel (designs)");
 }
 

@@ -504,6 +504,7 @@ __global__ void __launch_bounds__(SURF_THREADS, 2) surface_kernel(ffs_surface_ar
 // and read by every thread (broadcast). y'R^-1 y = sum w_t^2, and the
 // criterion as the surface kernel forms it.
 constexpr int SB_THREADS = 128;
+static_assert(256 % SB_THREADS == 0, "a CTA's voxels lie in one 256-voxel design tile");
 constexpr int SB_STEPS = 32;
 
 __global__ void __launch_bounds__(SB_THREADS) surface_band_kernel(ffs_surface_args a) {
@@ -543,11 +544,13 @@ __global__ void __launch_bounds__(SB_THREADS) surface_band_kernel(ffs_surface_ar
   }
   if (!live) return;
   const int Tk = a.T - a.K;
-  const double c_p0 = a.logdet_R[a.p0] + a.logdet_XtX[a.p0];
+  // grouped fits: the design of this CTA's 256-voxel tile
+  const double* ldx = a.logdet_XtX + (a.tile_design ? (size_t)a.tile_design[blockIdx.y * SB_THREADS / 256] * a.P : 0);
+  const double c_p0 = a.logdet_R[a.p0] + ldx[a.p0];
   const float rss0 = fmaxf(yy - a.proj[(size_t)a.p0 * a.V + v], 0.f);
   const float den = rss0 + 1e-10f;
   const float rss = fmaxf(ssw - a.proj[(size_t)p * a.V + v], 0.f);
-  const float dc = (float)((a.logdet_R[p] + a.logdet_XtX[p]) - c_p0);
+  const float dc = (float)((a.logdet_R[p] + ldx[p]) - c_p0);
   a.surf[(size_t)p * a.V + v] = dc + (float)Tk * log1pf((rss - rss0) / den);
   if (p == 0) a.crit0[v] = c_p0 + (double)Tk * log((double)rss0 + 1e-10);
 }
@@ -843,9 +846,8 @@ extern "C" int ffs_reml_surface(const ffs_surface_args* a, void* stream) {
     FFS_REQUIRE(a->V > 0 && a->T > a->K && a->P > 0 && a->band_w >= 1 && a->band_w <= FFS_BAND_MAX_W,
                 "ffs_reml_surface: bad sizes for the banded R");
     FFS_REQUIRE(a->p0 >= 0 && a->p0 < a->P, "ffs_reml_surface: p0=%d out of range", a->p0);
-    FFS_REQUIRE(a->yr_t && a->band && a->logdet_R && a->logdet_XtX && a->proj && a->surf && a->crit0 &&
-                    !a->tile_design,
-                "ffs_reml_surface: null buffer, or a grouped fit with the banded R");
+    FFS_REQUIRE(a->yr_t && a->band && a->logdet_R && a->logdet_XtX && a->proj && a->surf && a->crit0,
+                "ffs_reml_surface: null buffer");
     FFS_REQUIRE(ceil_div(a->V, SB_THREADS) <= 65535, "ffs_reml_surface: V=%d exceeds one launch", a->V);
     const size_t smem = sizeof(float) * (size_t)a->band_w * (SB_THREADS + SB_STEPS);
     FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(surface_band_kernel), smem));

@@ -439,9 +439,8 @@ def build_factors(X: torch.Tensor, grid: RemlGrid, layout: RunLayout, *, task_in
     if afull:
         f.Afull = torch.empty(DP, K, K, **f32)
     if grid.band is not None:
-        # AFNI-faithful mode: R banded per pair, factored as a band
-        if not single:
-            raise NotImplementedError("the AFNI-faithful banded covariance (set_afni_mode) for grouped designs")
+        # AFNI-faithful mode: R banded per pair, factored as a band (once per
+        # pair for every design)
         f.band_w = int(grid.band.max()) + 1
         if f.band_w > _lib.FFS_BAND_MAX_W:
             raise NotImplementedError(f"the AFNI-faithful band of {f.band_w - 1} lags exceeds "
@@ -806,7 +805,8 @@ def search_designs(Y: torch.Tensor, f: GridFactors, slots: DesignSlots, *, hiera
                           logdet_R=_p(f.logdet_R), logdet_XtX=_p(f.logdet_XtX), proj=_p(proj),
                           chunk_start=_p(f.chunk_start), n_chunks=f.chunk_start.numel() - 1,
                           chunk_pairs=_p(f.chunk_pairs), surf=_p(surf), crit0=_p(crit0),
-                          tile_design=_p(slots.tile256))
+                          tile_design=_p(slots.tile256), band_coef=_p(f.band_coef), band_w=f.band_w,
+                          band=_p(f.band))
     _run("ffs_reml_surface", lib.ffs_reml_surface, C.byref(sa), st)
 
     best = torch.empty(Vp, dtype=torch.int32, device=dev)
@@ -1097,6 +1097,7 @@ def grouped_graph_for(Y, Xs, grid, layout, gid, *, hierarchical, do_scale, gls_k
     fk = tuple((k, None if v is None else v.key() if hasattr(v, "key") else np.asarray(v).tobytes())
                for k, v in sorted(factor_kw.items()))
     key = (tuple(Y.shape), tuple(Xs.shape), str(Xs.device), grid.a.tobytes(), grid.b.tobytes(), grid.lambda_fp32,
+           grid.ltop, None if grid.band is None else grid.band.tobytes(),
            layout.run_start.tobytes(), layout.tau.tobytes(), gid.tobytes(), hierarchical, do_scale,
            tuple(sorted(gls_kw.items())), fk)
     gr = _GROUPED_GRAPHS.get(key)

@@ -105,7 +105,8 @@ typedef struct {
    * with band, correlations at |tau_i - tau_j| > band[p] are zero and R is
    * factored as a band (band_L, band_coef below; coef is then the identity
    * and unused). band_w = max band[p] + 1 <= FFS_BAND_MAX_W; NULL band: the
-   * exact ARMA(1,1) R. Single-design builds only (ffs_grid_build). */
+   * exact ARMA(1,1) R. ffs_grid_build and ffs_grid_build_designs (not the
+   * allocation-free build). */
   int band_w;
   const int* band;      /* device [P] or NULL                                    */
 } ffs_grid_desc;
@@ -150,7 +151,8 @@ int ffs_grid_build(const ffs_grid_desc* d, const ffs_grid_out* o, void* stream);
  * fewer CTAs leave SMs to kernels running beside the build on other streams;
  * work: ffs_grid_work_bytes_designs with the same max_ctas. With more than one
  * design a first launch factors R once per pair (it depends on the pair
- * only) and the items of every design read that factor. */
+ * only) and the items of every design read that factor; with the banded R
+ * (d->band) that launch also writes band_L and band_coef ([P] layout). */
 #define FFS_GRID_MAX_SLOTS 2048
 size_t ffs_grid_work_bytes_designs(int T, int K, int P, int n_designs, int max_ctas);
 int ffs_grid_build_designs(const ffs_grid_desc* d, int n_designs, int max_ctas, const ffs_grid_out* o, void* stream);

@@ -117,3 +117,44 @@ def test_afni_faithful_refuses_what_keeps_the_exact_r(afni_mode):
     Y, X, kw = afni_faithful_case(d, "runs")
     with pytest.raises(NotImplementedError):
         fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, dsort=Y[:, None, :], **kw)
+
+
+def _afni_designs(X):
+    """Three designs of one shape: the case's own, its first column delayed by
+    two samples, its second column with a slow ramp added."""
+    X1 = X.copy()
+    X1[:, 0] = np.roll(X[:, 0], 2)
+    X2 = X.copy()
+    X2[:, 1] = X[:, 1] + np.linspace(-0.5, 0.5, X.shape[0], dtype=X.dtype)
+    return {0: X, 1: X1, 2: X2}
+
+
+@pytest.mark.parametrize("tag", ["runs", "cens"])
+@pytest.mark.parametrize("exhaustive", [True, False])
+def test_afni_faithful_grouped_equals_per_group_fits(tag, exhaustive, afni_mode):
+    """Grouped designs under the banded R: one multi-design build (the band
+    factored once per pair by the pre-pass), the banded criterion per
+    256-voxel design tile, the GLS whitened by the pair's band. Each voxel's
+    arithmetic is the per-group fit's, so the results are those of fitting
+    every group on its own; against the FP64 oracle's grouped fit as the
+    other AFNI-mode fits are."""
+    from fastfuncstuff_gb300 import fit_glm_arma11_grouped
+
+    d = load_golden("afni_faithful")
+    Y, X, kw = afni_faithful_case(d, tag)
+    designs = _afni_designs(X)
+    gid = np.arange(Y.shape[0]) % 3
+    opts = dict(kw, device=DEV, verbose=False, force_exhaustive_search=exhaustive, want_residuals=True)
+    got = fit_glm_arma11_grouped(Y, designs, gid, tr=2.0, **opts)
+    for h in range(3):
+        m = gid == h
+        ref = fit_glm_arma11(Y[m], designs[h], tr=2.0, **opts)
+        for name in ("arma_params", "reml_likelihood", "betas", "tstats", "sigma2", "r2", "residuals_whitened"):
+            np.testing.assert_array_equal(getattr(got, name).numpy()[m], getattr(ref, name).numpy(), err_msg=name)
+    ref = o.fit_glm_arma11_grouped(Y, designs, gid, use_double=True, fp64_scaled=True,
+                                   force_exhaustive_search=exhaustive, save_profile_likelihoods=True, **kw)
+    grid = G.make_grid(d["a_grid"], d["b_grid"])
+    idx = _index(got.arma_params.numpy(), grid)
+    check_selection(idx, ref.arma_index, ref.reml_lklhd_surface)
+    same = idx == ref.arma_index
+    assert rel_maxnorm(got.betas.numpy()[same], ref.betas[same]).max() <= BETA_REL
