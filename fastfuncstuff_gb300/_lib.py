@@ -65,6 +65,7 @@ class DsortArgs(C.Structure):
         ("ljung_box", C.c_void_p),
         ("set_fstats", C.c_void_p), ("set_sd", C.c_void_p), ("set_coef", C.c_void_p),
         ("status", C.c_void_p),
+        ("band_coef", C.c_void_p), ("band_w", C.c_int), ("band", C.c_void_p),
     ]
 
 

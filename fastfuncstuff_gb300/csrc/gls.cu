@@ -44,9 +44,7 @@ __device__ __forceinline__ const float* quad_matrix(const ffs_gls_args& a, int g
 // for j up to the pair's band (rows past a run start or a censoring gap have
 // zero coefficients there), by one thread over the whole series; r and w may
 // be the same array (w_{t-j} is then read where it was written).
-__device__ __forceinline__ void band_whiten(const ffs_gls_args& a, int p, const float* r, float* w, int T) {
-  const int W = a.band_w, bw = a.band[p];
-  const float* cb = a.band_coef + (size_t)p * T * W;
+__device__ __forceinline__ void band_whiten_rows(const float* cb, int W, int bw, const float* r, float* w, int T) {
   for (int t = 0; t < T; ++t) {
     const float* c = cb + (size_t)t * W;
     float acc = r[t] * c[0];
@@ -54,6 +52,10 @@ __device__ __forceinline__ void band_whiten(const ffs_gls_args& a, int p, const 
     for (int j = 1; j <= jm; ++j) acc = fmaf(-c[j], w[t - j], acc);
     w[t] = acc;
   }
+}
+
+__device__ __forceinline__ void band_whiten(const ffs_gls_args& a, int p, const float* r, float* w, int T) {
+  band_whiten_rows(a.band_coef + (size_t)p * T * a.band_w, a.band_w, a.band[p], r, w, T);
 }
 
 // GLS of one voxel v at pair g, executed by one warp. Gp = G of pair g and Xt
@@ -799,6 +801,21 @@ __device__ void whiten_warp(const float4* __restrict__ cf, const float* x, float
   __syncwarp();
 }
 
+// L^-1 x of one series for the dsort GLS: the exact R's recurrence by the
+// whole warp (whiten_warp), or AFNI's banded R by lane 0 (band_whiten_rows).
+// x and out do not overlap.
+__device__ void whiten_dsort(const ffs_dsort_args& a, int p, const float4* __restrict__ cf, const float* x,
+                             float* out, int T) {
+  if (a.band_coef) {
+    __syncwarp();  // x was written by every lane
+    if ((threadIdx.x & 31) == 0)
+      band_whiten_rows(a.band_coef + (size_t)p * T * a.band_w, a.band_w, a.band[p], x, out, T);
+    __syncwarp();
+  } else {
+    whiten_warp(cf, x, out, T);
+  }
+}
+
 // QB: the projection loop's unrolled bound on q (q itself for 1..4, the
 // maximum otherwise), so that small q issues no predicated-off work
 template <int QB>
@@ -871,8 +888,8 @@ __global__ void __launch_bounds__(DS_WARPS * 32) gls_dsort_kernel(ffs_dsort_args
       }
   }
   // whitened y (into w) and D
-  whiten_warp(cf, ys, w, T);
-  for (int k = 0; k < q; ++k) whiten_warp(cf, Ds + k * T, Dw + k * T, T);
+  whiten_dsort(a, p, cf, ys, w, T);
+  for (int k = 0; k < q; ++k) whiten_dsort(a, p, cf, Ds + k * T, Dw + k * T, T);
   // D_w'D_w and D_w'y_w
   for (int k = 0; k < q; ++k) {
     for (int l = 0; l <= k; ++l) {
@@ -943,7 +960,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) gls_dsort_kernel(ffs_dsort_args
   sst = warp_sum(sst);
   __syncwarp();
   // whitened residual and its sum of squares (blocks of 32 terms)
-  whiten_warp(cf, r, w, T);
+  whiten_dsort(a, p, cf, r, w, T);
   double ssw_d = 0.0;
   for (int t0 = 0; t0 < T; t0 += 32) {
     const float x = t0 + lane < T ? w[t0 + lane] : 0.f;
@@ -1221,6 +1238,8 @@ extern "C" int ffs_reml_gls_dsort(const ffs_dsort_args* a, void* stream) {
                                  a->set_sd && a->set_coef),
               "ffs_reml_gls_dsort: column sets need set_ptr, set_idx, set_col, Afull, xmean and outputs");
   FFS_REQUIRE(a->lj_h == 0 || (a->lj_w && a->ljung_box), "ffs_reml_gls_dsort: Ljung-Box buffers");
+  FFS_REQUIRE(!a->band_coef || (a->band && a->band_w >= 1 && a->band_w <= FFS_BAND_MAX_W),
+              "ffs_reml_gls_dsort: the banded R needs band and 1 <= band_w=%d <= %d", a->band_w, FFS_BAND_MAX_W);
   // the set sizes live on the device; a set of distinct columns of [X | D]
   // has at most K + q of them (the caller removes repeats)
   const int ns_max = a->n_sets > 0 ? a->K + a->q : 0;

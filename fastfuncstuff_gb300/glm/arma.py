@@ -286,12 +286,10 @@ def fit_glm_arma11(
         _unsupported("global ARMA estimation (estimate_per_voxel=False) of grouped designs")
     if _REML_MODE.afni_faithful:
         # the banded R runs through the full-grid search and the GLS (one
-        # design or grouped designs); the learned refine and -dsort keep the
-        # exact R only
+        # design or grouped designs, with or without -dsort); the learned
+        # refine keeps the exact R only
         if proposal is not None:
             _unsupported("the learned-seeded refine (proposal) in AFNI-faithful mode (set_afni_mode)")
-        if dsort is not None:
-            _unsupported("-dsort in AFNI-faithful mode (set_afni_mode)")
     out_dtype = torch.float64 if use_double else torch.float32
 
     Y = data if isinstance(data, torch.Tensor) else torch.from_numpy(np.asarray(data))

@@ -997,7 +997,8 @@ def gls_dsort(Y: torch.Tensor, scale: torch.Tensor, best: torch.Tensor, f: GridF
                        dtstats=_p(o.dtstats), sigma2=_p(o.sigma2), fstats=_p(o.fstats), r2=_p(o.r2),
                        cbeta=_p(o.cbeta), ct=_p(o.ct), resid=_p(o.resid), resid_w=_p(o.resid_w), pred=_p(o.pred),
                        ljung_box=_p(o.ljung_box), set_fstats=_p(o.set_fstats), set_sd=_p(o.set_sd),
-                       set_coef=_p(o.set_coef), status=_p(o.status))
+                       set_coef=_p(o.set_coef), status=_p(o.status), band_coef=_p(f.band_coef), band_w=f.band_w,
+                       band=_p(f.band))
     _run("ffs_reml_gls_dsort", lib.ffs_reml_gls_dsort, C.byref(a), st)
     o._keep = (Y, D, key, Xt, xmean, sp, si, sc_, ptau_d, w_d)
     return o

@@ -501,6 +501,12 @@ typedef struct {
   float* set_fstats; float* set_sd; float* set_coef;   /* [V][n_set_out] or NULL  */
   int* status;            /* device int: set to 1 if some voxel's S had a pivot   */
                           /*   <= 0 (D in the span of X); NULL to skip            */
+  /* AFNI-faithful banded R (ffs_grid_desc.band): y, D and the residual are
+   * whitened by the pair's band (band_coef, row stride band_w, band[p] terms)
+   * instead of coef's recursion; NULL band_coef: the exact ARMA(1,1) R. */
+  const float* band_coef;
+  int band_w;
+  const int* band;
 } ffs_dsort_args;
 
 #define FFS_DSORT_QMAX 16

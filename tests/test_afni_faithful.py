@@ -113,10 +113,53 @@ def test_afni_faithful_surface_differs_from_the_exact_r(afni_mode):
 
 
 def test_afni_faithful_refuses_what_keeps_the_exact_r(afni_mode):
+    from fastfuncstuff_gb300.glm import learned
+
     d = load_golden("afni_faithful")
     Y, X, kw = afni_faithful_case(d, "runs")
+    prop = learned.ArmaProposal(learned.init_params(0, DEV))
     with pytest.raises(NotImplementedError):
-        fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, dsort=Y[:, None, :], **kw)
+        fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, proposal=prop, **kw)
+
+
+@pytest.mark.parametrize("tag", ["two", "runs"])
+@pytest.mark.parametrize("exhaustive", [True, False])
+def test_afni_faithful_dsort_matches_fp64_oracle(tag, exhaustive, afni_mode):
+    """-dsort under the banded R: the voxel's regressors, its series and the
+    residual whitened by the pair's band in the dsort GLS (block elimination
+    against the band-built G and U), against the FP64 oracle in the same mode
+    on the dsort fixture's data (two datasets per voxel, and one expanded per
+    run)."""
+    import warnings
+
+    d = load_golden("dsort")
+    kw = dict(a_grid=d["a_grid"], b_grid=d["b_grid"], run_starts=d["run_starts"], task_indices=[0, 1],
+              want_ljung_box=True, want_residuals=True)
+    if tag == "two":
+        kw["dsort"] = d["D"]
+    else:
+        kw.update(dsort=d["D"][:, :1], dsort_run_bounds=[0, 64, 128])
+    with warnings.catch_warnings():
+        warnings.filterwarnings("ignore", message=".*constant.*")
+        got = fit_glm_arma11(d["Y"], d["X"], tr=2.0, device=DEV, verbose=False, force_exhaustive_search=exhaustive,
+                             **kw)
+        ref = o.fit_glm_arma11(d["Y"], d["X"], use_double=True, fp64_scaled=True,
+                               force_exhaustive_search=exhaustive, save_profile_likelihoods=True, **kw)
+    grid = G.make_grid(d["a_grid"], d["b_grid"])
+    idx = _index(got.arma_params.numpy(), grid)
+    check_selection(idx, ref.arma_index, ref.reml_lklhd_surface)
+    same = idx == ref.arma_index
+    full_got = np.concatenate([got.betas.numpy(), got.dsort_betas.numpy()], 1)[same]
+    full_ref = np.concatenate([ref.betas, ref.dsort_betas], 1)[same]
+    assert rel_maxnorm(full_got, full_ref).max() <= BETA_REL
+    t_got = np.concatenate([got.tstats.numpy(), got.dsort_tstats.numpy()], 1)[same]
+    t_ref = np.concatenate([ref.tstats, ref.dsort_tstats], 1)[same]
+    assert rel_maxnorm(t_got, t_ref).max() <= BETA_REL
+    np.testing.assert_allclose(got.sigma2.numpy()[same], ref.sigma2[same], rtol=1e-4)
+    np.testing.assert_allclose(got.ljung_box.numpy()[same], ref.ljung_box[same], rtol=2e-3, atol=1e-3)
+    scale = np.abs(ref.residuals_whitened[same]).max(1, keepdims=True)
+    np.testing.assert_allclose(got.residuals_whitened.numpy()[same] / scale, ref.residuals_whitened[same] / scale,
+                               atol=2e-4)
 
 
 def _afni_designs(X):
