@@ -187,11 +187,14 @@ SIGNATURES = {
     "ffs_reml_window": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int], C.c_int),
+                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
     "ffs_device_view": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
     "ffs_reml_strip": ([C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                        C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+                        C.c_void_p, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
+    "ffs_reml_band_sums": ([C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                            C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                            C.c_void_p, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
     "ffs_reml_segment_items": ([C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                 C.c_void_p, C.c_void_p], C.c_int),
     "ffs_reml_near_line": ([C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -161,6 +161,7 @@ struct CritArgs {
   int* next_center;         // NULL, or [V]: the next round's centre of each voxel taken
   const int* design;        // NULL, or [V]: each voxel's design; dcf then [n_designs][P], c_p0 [n_designs]
   int P;
+  const float* ssw_pre;     // NULL, or [n][WSLOTS]: y'R^-1 y of each row and window slot (the banded R)
 };
 
 constexpr int CRIT_TB = 16;  // steps per partial sum and sample prefetch
@@ -270,7 +271,19 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
   // rounds' tiles often hold a few rows) stages the tables but skips the
   // recurrences
   const bool warp_live = (tid & ~31) < tl.y;
-  for (int c0 = 0; c0 < T; c0 += WCH) {
+  if (w.ssw_pre && live) {
+    // the banded R's sums come from band_sums_kernel: y'y alone here, in the
+    // recurrence path's blocks
+    for (int t0 = 0; t0 < T; t0 += CRIT_TB) {
+      float yq[CRIT_TB];
+      load_block(yq, t0);
+      float yy_b = 0.f;
+#pragma unroll
+      for (int k = 0; k < CRIT_TB; ++k) yy_b = fmaf(yq[k], yq[k], yy_b);
+      yy += yy_b;
+    }
+  }
+  for (int c0 = 0; c0 < T && !w.ssw_pre; c0 += WCH) {
     const int cn = min(WCH, T - c0);
     __syncthreads();  // the previous chunk's tables are no longer read
     for (int e = tid; e < WIN * WIN * (cn + 1); e += blockDim.x) {
@@ -417,7 +430,8 @@ __global__ void __launch_bounds__(WTILE, 4) window_crit_kernel(CritArgs w, const
     for (int g = 0; g < s_np[ra]; ++g) {
       if (!live) break;
       const int p = s_pr[ra][g];
-      const float stv = sst[(ra * WIN + g) * WTILE + tid];
+      const float stv = w.ssw_pre ? w.ssw_pre[(size_t)i * WSLOTS + ra * WIN + s_col[ra][g]]
+                                  : sst[(ra * WIN + g) * WTILE + tid];
       const float rss = fmaxf(stv - w.winproj[(size_t)i * WSLOTS + ra * WIN + s_col[ra][g]], 0.f);
       const float d = dcf[p] + (float)Tk * log1pf((rss - yy) / (yy + 1e-10f));
       if (d < bd || (d == bd && p < best) || best < 0) {
@@ -504,6 +518,7 @@ struct StripArgs {
   int* best_cell;        // [V]
   const int* design;     // [V] each voxel's design (dcf [n_designs][P]), or NULL (dcf [P])
   int P;                 // pairs per design
+  const float* ssw_pre;  // NULL, or [n_pairs][n]: y'R^-1 y of each pair and row (the banded R)
 };
 
 __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
@@ -526,7 +541,18 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
 #pragma unroll
   for (int j = 0; j < STRIP_G2; ++j) vv[j] = st[j] = zero2;
   float yy = 0.f, yp = 0.f;
-  for (int c0 = 0; c0 < T; c0 += WCH) {
+  if (w.ssw_pre && live) {
+    // the banded R's sums come from band_sums_kernel: y'y alone here
+    for (int t0 = 0; t0 < T; t0 += CRIT_TB) {
+      float yy_b = 0.f;
+      for (int k = 0; k < CRIT_TB; ++k) {
+        const float y = t0 + k < T ? yrow[t0 + k] : 0.f;
+        yy_b = fmaf(y, y, yy_b);
+      }
+      yy += yy_b;
+    }
+  }
+  for (int c0 = 0; c0 < T && !w.ssw_pre; c0 += WCH) {
     const int cn = min(WCH, T - c0);
     __syncthreads();  // the previous chunk's tables are no longer read
     for (int e = tid; e < STRIP_G * (cn + 1); e += blockDim.x) {
@@ -634,7 +660,8 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
     for (int h = 0; h < 2; ++h) {
       const int q = 2 * j + h;
       if (q < nq) {
-        const float rss = fmaxf(s2[h] - w.proj[(size_t)(q0 + q) * w.n + i], 0.f);
+        const float ssw = w.ssw_pre ? w.ssw_pre[(size_t)(q0 + q) * w.n + i] : s2[h];
+        const float rss = fmaxf(ssw - w.proj[(size_t)(q0 + q) * w.n + i], 0.f);
         bd = fminf(bd, dcf[w.pairs[q0 + q]] + Tk * log1pf((rss - yy) / (yy + 1e-10f)));
       }
     }
@@ -643,6 +670,96 @@ __global__ void __launch_bounds__(STRIP_TILE) strip_crit_kernel(StripArgs w) {
     w.fallback[v] = 1;
     w.best_cell[v] = -1;
   }
+}
+
+// y'R^-1 y under AFNI's banded R for the learned refine: one CTA per (tile
+// of sorted rows, pair), one thread per row, the band's forward substitution
+// w_t = y_t c[t][0] - sum_{j <= band} c[t][j] w_{t-j} with the last band
+// values of w in a shared-memory ring and the coefficients staged per chunk
+// of BS_STEPS steps (as the full grid's surface_band_kernel forms it). With
+// tiles (the window rounds) CTA (x, s) takes tile x and window slot s of the
+// tile's centre (no work for an empty slot or an identity pair) and writes
+// out[i][s]; without them CTA (x, q) takes rows 128 x .. and pair pairs[q] and
+// writes out[q][i] (row stride n).
+constexpr int BS_STEPS = 32;
+
+struct BandSumArgs {
+  int n;
+  const int* n_dev;        // device count of real rows (strip mode), or NULL
+  int T;
+  const int* idx;          // [n] voxel of each sorted row
+  const float* rows;       // [V][T] residualised rows (read at idx[i])
+  const float* band_coef;  // [P][T][band_w]
+  int band_w;
+  const int* band;         // [P]
+  const int2* tiles;       // window mode: (first row, rows) per tile, *n_tiles of them
+  const int* n_tiles;
+  const int* center;       // [V] window centre cell
+  const int* lattice;
+  int n_a, n_b;
+  const uint8_t* ident;    // [P] lambda == 0
+  const int* pairs;        // strip mode: [n_pairs]
+  float* out;
+};
+
+__global__ void __launch_bounds__(WTILE) band_sums_kernel(BandSumArgs a) {
+  extern __shared__ float bsm[];
+  const int W = a.band_w, T = a.T;
+  int r0, nrow, p;
+  if (a.tiles) {
+    if ((int)blockIdx.x >= *a.n_tiles) return;
+    const int2 tl = a.tiles[blockIdx.x];
+    r0 = tl.x;
+    nrow = tl.y;
+    int a0, wa, b0, wb;
+    window_of(a.center[a.idx[r0]], a.n_a, a.n_b, a0, wa, b0, wb);
+    const int ra = blockIdx.y / WIN, rb = blockIdx.y % WIN;
+    if (ra >= wa || rb >= wb) return;
+    p = a.lattice[(a0 + ra) * a.n_b + b0 + rb];
+    if (p < 0 || a.ident[p]) return;
+  } else {
+    const int m = a.n_dev ? min(a.n, *a.n_dev) : a.n;
+    r0 = blockIdx.x * WTILE;
+    if (r0 >= m) return;
+    nrow = min(WTILE, m - r0);
+    p = a.pairs[blockIdx.y];
+  }
+  float* ring = bsm;                     // [W][WTILE]
+  float* cs = ring + (size_t)W * WTILE;  // [BS_STEPS][W]
+  const int bw = a.band[p];
+  const int tid = threadIdx.x;
+  const bool live = tid < nrow;
+  const int i = r0 + (live ? tid : 0);
+  const float* yrow = a.rows + (size_t)a.idx[i] * T;
+  const float* cb = a.band_coef + (size_t)p * T * W;
+  for (int e = tid; e < W * WTILE; e += blockDim.x) ring[e] = 0.f;
+  float ssw = 0.f;
+  int pos = 0;
+  for (int c0 = 0; c0 < T; c0 += BS_STEPS) {
+    const int cn = min(BS_STEPS, T - c0);
+    __syncthreads();  // the previous chunk's coefficients are no longer read
+    for (int e = tid; e < cn * W; e += blockDim.x) cs[e] = cb[(size_t)c0 * W + e];
+    __syncthreads();
+    for (int s = 0; s < cn; ++s) {
+      const int t = c0 + s;
+      const float* c = cs + (size_t)s * W;
+      float acc = yrow[t] * c[0];
+      const int jm = min(bw, t);
+      int q = pos;
+      for (int j = 1; j <= jm; ++j) {
+        q = q == 0 ? W - 1 : q - 1;
+        acc = fmaf(-c[j], ring[(size_t)q * WTILE + tid], acc);
+      }
+      ring[(size_t)pos * WTILE + tid] = acc;
+      pos = pos + 1 == W ? 0 : pos + 1;
+      ssw = fmaf(acc, acc, ssw);
+    }
+  }
+  if (!live) return;
+  if (a.tiles)
+    a.out[(size_t)i * WSLOTS + blockIdx.y] = ssw;
+  else
+    a.out[(size_t)blockIdx.y * a.n + i] = ssw;
 }
 
 // The voxels v < V whose pair best[v] lies within k0 lattice steps of an
@@ -856,7 +973,7 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
                                const float* rows, const float* coef, const float* winproj, const float* dcf,
                                const unsigned char* ident, int p_id, const double* c_p0, int* best, float* dbest,
                                double* crit0, int* fallback, int* best_cell, int* next_center, const int* design,
-                               int P, void* stream) {
+                               int P, const float* ssw_pre, void* stream) {
   clear_error();
   FFS_REQUIRE(n > 0 && T > K && K > 0 && n_a > 0 && n_b > 0 && p_id >= 0 && max_tiles > 0 && (!design || P > 0),
               "ffs_reml_window: bad sizes");
@@ -867,7 +984,7 @@ extern "C" int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int*
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(window_crit_kernel), smem));
   FFS_REQUIRE(((uintptr_t)rows & 15) == 0, "ffs_reml_window: rows must be 16-byte aligned");
   CritArgs w{n, T, K, n_a, n_b, lattice, idx, center, rows, reinterpret_cast<const float4*>(coef), winproj, dcf,
-             ident, p_id, c_p0, best, dbest, crit0, fallback, best_cell, next_center, design, P};
+             ident, p_id, c_p0, best, dbest, crit0, fallback, best_cell, next_center, design, P, ssw_pre};
   window_crit_kernel<<<max_tiles, WTILE, smem, (cudaStream_t)stream>>>(w, reinterpret_cast<const int2*>(tiles),
                                                                         n_tiles);
   return check_launch("window_crit_kernel");
@@ -884,7 +1001,7 @@ extern "C" int ffs_reml_centers(int V, const float* prop, const float* a_axis, i
 extern "C" int ffs_reml_strip(int n, const int* n_dev, int T, int K, int n_pairs, const int* pairs, const int* idx,
                               const float* rows, const float* coef, const float* proj, const float* dcf,
                               const float* dbest, const double* crit0, int* fallback, int* best_cell,
-                              const int* design, int P, void* stream) {
+                              const int* design, int P, const float* ssw_pre, void* stream) {
   clear_error();
   FFS_REQUIRE(!design || P > 0, "ffs_reml_strip: designs need P > 0");
   FFS_REQUIRE(n > 0 && T > K && K > 0 && n_pairs > 0 && n_pairs <= STRIP_MAX,
@@ -895,10 +1012,30 @@ extern "C" int ffs_reml_strip(int n, const int* n_dev, int T, int K, int n_pairs
   FFS_REQUIRE(((uintptr_t)rows & 15) == 0 && ((uintptr_t)coef & 15) == 0,
               "ffs_reml_strip: rows and coef must be 16-byte aligned");
   StripArgs w{n, T, K, n_pairs, n_dev, pairs, idx, rows, reinterpret_cast<const float4*>(coef), proj, dcf, dbest,
-              crit0, fallback, best_cell, design, P};
+              crit0, fallback, best_cell, design, P, ssw_pre};
   const dim3 grid(ceil_div(n, STRIP_TILE), ceil_div(n_pairs, STRIP_G));
   strip_crit_kernel<<<grid, STRIP_TILE, 0, (cudaStream_t)stream>>>(w);
   return check_launch("strip_crit_kernel");
+}
+
+extern "C" int ffs_reml_band_sums(int n, const int* n_dev, int T, const int* idx, const float* rows,
+                                  const float* band_coef, int band_w, const int* band, const int* tiles,
+                                  const int* n_tiles, int max_tiles, const int* center, const int* lattice, int n_a,
+                                  int n_b, const unsigned char* ident, const int* pairs, int n_pairs, float* out,
+                                  void* stream) {
+  clear_error();
+  FFS_REQUIRE(n > 0 && T > 0 && band_w >= 1 && band_w <= FFS_BAND_MAX_W, "ffs_reml_band_sums: bad sizes");
+  FFS_REQUIRE(idx && rows && band_coef && band && out, "ffs_reml_band_sums: null buffer");
+  FFS_REQUIRE(tiles ? (n_tiles && max_tiles > 0 && center && lattice && ident && n_a > 0 && n_b > 0)
+                    : (pairs && n_pairs > 0 && n_pairs <= 65535),
+              "ffs_reml_band_sums: window mode needs tiles, n_tiles, centre, lattice and ident; strip mode pairs");
+  const size_t smem = sizeof(float) * (size_t)band_w * (WTILE + BS_STEPS);
+  FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(band_sums_kernel), smem));
+  BandSumArgs a{n, n_dev, T, idx, rows, band_coef, band_w, band, reinterpret_cast<const int2*>(tiles), n_tiles,
+                center, lattice, n_a, n_b, ident, pairs, out};
+  const dim3 grid = tiles ? dim3(max_tiles, WSLOTS) : dim3(ceil_div(n, WTILE), n_pairs);
+  band_sums_kernel<<<grid, WTILE, smem, (cudaStream_t)stream>>>(a);
+  return check_launch("band_sums_kernel");
 }
 
 extern "C" int ffs_reml_near_line(int V, const int* best, const int* dist, int k0, const int* fallback, int* ids,

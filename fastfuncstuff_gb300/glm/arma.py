@@ -20,8 +20,9 @@ and lambda in float64, no std scaling: the likelihood is that of the raw data)
 and returns float64 tensors; the arithmetic is this build's (FP64 factors,
 fp32 / split-bf16 voxel work).
 
-Options outside this path (OLS side fits, AFNI-faithful banded covariances)
-raise NotImplementedError.
+Options outside this path (the OLS side fits) raise NotImplementedError;
+AFNI-faithful mode (``set_afni_mode``) runs every fit path with AFNI's banded
+R.
 """
 
 from __future__ import annotations
@@ -37,7 +38,6 @@ import torch
 from . import engine
 from .._lib import FFS_DSORT_QMAX
 from .grid import (
-    _REML_MODE,
     RemlGrid,
     build_censor_run_info,
     compute_arma_lambda,
@@ -284,12 +284,6 @@ def fit_glm_arma11(
         raise ValueError("want_dsort_nods needs dsort")
     if not estimate_per_voxel and _group_designs is not None:
         _unsupported("global ARMA estimation (estimate_per_voxel=False) of grouped designs")
-    if _REML_MODE.afni_faithful:
-        # the banded R runs through the full-grid search and the GLS (one
-        # design or grouped designs, with or without -dsort); the learned
-        # refine keeps the exact R only
-        if proposal is not None:
-            _unsupported("the learned-seeded refine (proposal) in AFNI-faithful mode (set_afni_mode)")
     out_dtype = torch.float64 if use_double else torch.float32
 
     Y = data if isinstance(data, torch.Tensor) else torch.from_numpy(np.asarray(data))

@@ -45,7 +45,8 @@ LAUNCHES = {"ffs_grid_build": 1, "ffs_grid_build_designs": 1, "ffs_reml_prep": 1
             "ffs_reml_gls_ex": 1, "ffs_reml_gls_grouped": 2, "ffs_reml_gather": 1, "ffs_reml_window_items": 2,
             "ffs_reml_window": 1, "ffs_reml_project_tc_list": 1, "ffs_mlp_forward": 1, "ffs_reml_centers": 1,
             "ffs_design_basis": 2, "ffs_reml_strip": 1, "ffs_reml_near_line": 1, "ffs_reml_window_finish": 1,
-            "ffs_reml_compact": 1, "ffs_merge_rows": 1, "ffs_reml_segment_items": 2}
+            "ffs_reml_compact": 1, "ffs_merge_rows": 1, "ffs_reml_segment_items": 2,
+            "ffs_reml_band_sums": 1}
 
 
 class StageTimer:

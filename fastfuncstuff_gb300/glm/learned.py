@@ -252,6 +252,20 @@ STAGE_CHUNKS = 8  # chunks of rows a staged run copies in and preps one after an
 STRIP_K0 = 2  # voxels whose answer lies this close to the identity line get the strip next to it
 
 
+def _band_sums_strip(pre, f, ids, count, pairs32, nq: int, V: int):
+    """AFNI's banded R: y'R^-1 y of the compacted rows ids[i < *count] at the
+    strip pairs, [nq][V] (ffs_reml_band_sums in strip mode); None for the
+    exact R, whose recurrence the strip kernel runs itself."""
+    if f.band_coef is None:
+        return None
+    lib = _lib.load()
+    ssw = torch.empty(nq, V, dtype=torch.float32, device=pre.scale.device)
+    engine._run("ffs_reml_band_sums", lib.ffs_reml_band_sums, V, _p(count), f.T, _p(ids), _p(pre.rows),
+                _p(f.band_coef), f.band_w, _p(f.band), None, None, 0, None, None, 0, 0, None, _p(pairs32), nq,
+                _p(ssw), _st())
+    return ssw
+
+
 def _strip_round_grouped(pre, f, out, *, flag, k0: int, grp: dict, pad: torch.Tensor):
     """_strip_round for grouped designs, every design in one pass: the
     near-line voxels (padding slots excluded) sorted by design
@@ -297,11 +311,12 @@ def _strip_round_grouped(pre, f, out, *, flag, k0: int, grp: dict, pad: torch.Te
                           u_lo=_p(u_lo), yexp=_p(yexp), uexp=_p(uex), yr_t=None, U=None, proj=_p(proj), flag=_p(flag))
     engine._run("ffs_reml_project_tc_list", lib.ffs_reml_project_tc_list, C.byref(pa), _p(items), _p(counts),
                 max_items, max_pairs, 0, st)
+    ssw = _band_sums_strip(pre, f, idx, count, sc["pairs32"], nq, V)
     engine._run("ffs_reml_strip", lib.ffs_reml_strip, V, _p(count), T, K, nq, _p(sc["pairs32"]), _p(idx),
                 _p(pre.rows), _p(f.coef), _p(proj), _p(grp["dcf"]), _p(out["dbest"]), _p(out["crit0"]),
-                _p(out["fb"]), _p(out["cell"]), _p(grp["design"]), P, st)
+                _p(out["fb"]), _p(out["cell"]), _p(grp["design"]), P, _p(ssw), st)
     out["strip_voxels"] = count
-    out.setdefault("_keep", []).append((keys, idx, seg_end, hi, lo, yexp, u_hi, u_lo, uex, items, proj))
+    out.setdefault("_keep", []).append((keys, idx, seg_end, hi, lo, yexp, u_hi, u_lo, uex, items, proj, ssw))
     return counts
 
 
@@ -342,13 +357,14 @@ def _strip_round(pre, f, out, *, flag, k0: int):
                           u_lo=_p(u_lo), yexp=_p(yexp), uexp=_p(uex), yr_t=None, U=None, proj=_p(proj),
                           flag=_p(flag), V_dev=_p(count))
     engine._run("ffs_reml_project_tc", lib.ffs_reml_project_tc, C.byref(pa), st)
+    ssw = _band_sums_strip(pre, f, ids, count, sc["pairs32"], nq, V)
     engine._run("ffs_reml_strip", lib.ffs_reml_strip, V, _p(count), T, K, nq, _p(sc["pairs32"]), _p(ids),
                 _p(pre.rows), _p(f.coef), _p(proj), _p(c["dcf"]), _p(out["dbest"]), _p(out["crit0"]),
-                _p(out["fb"]), _p(out["cell"]), None, 0, st)
+                _p(out["fb"]), _p(out["cell"]), None, 0, _p(ssw), st)
     if out.get("count_evals"):
         out["pair_evals"] = out.get("pair_evals", 0) + nq * count.sum()
     out["strip_voxels"] = count
-    out.setdefault("_keep", []).append((ids, hi, lo, yexp, u_hi, u_lo, uex, proj))
+    out.setdefault("_keep", []).append((ids, hi, lo, yexp, u_hi, u_lo, uex, proj, ssw))
 
 
 def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None, grp=None):
@@ -407,11 +423,20 @@ def _window_round(pre, f, cen, out, *, flag, join=None, next_cen=None, grp=None)
                           proj=_p(winproj), flag=_p(flag))
     engine._run("ffs_reml_project_tc_list", lib.ffs_reml_project_tc_list, C.byref(ja), _p(items), _p(counts),
                 max_items, max_pairs, WIN_SLOTS, st)
+    ssw = None
+    if f.band_coef is not None:
+        # AFNI's banded R: y'R^-1 y of every window slot by the band's forward
+        # substitution, read by the window kernel in place of its recurrence
+        ssw = torch.empty(n, WIN_SLOTS, dtype=torch.float32, device=dev)
+        engine._run("ffs_reml_band_sums", lib.ffs_reml_band_sums, n, None, T, _p(idx), _p(pre.rows),
+                    _p(f.band_coef), f.band_w, _p(f.band), _p(tiles), counts.data_ptr() + 8, max_tiles, _p(cen),
+                    _p(f.lattice), n_a, n_b, _p(c["ident"]), None, 0, _p(ssw), st)
+        out.setdefault("_keep", []).append(ssw)
     engine._run("ffs_reml_window", lib.ffs_reml_window, n, T, K, n_a, n_b, _p(f.lattice), _p(idx), _p(cen),
                 _p(tiles), counts.data_ptr() + 8, max_tiles, _p(pre.rows), _p(f.coef), _p(winproj), _p(c["dcf"]),
                 _p(c["ident"]), c["p_id"], _p(c["c_p0"]),
                 _p(out["best"]), _p(out["dbest"]), _p(out["crit0"]), _p(out["fb"]), _p(out["cell"]), _p(next_cen),
-                _p(grp["design"]) if grp is not None else None, Pd, st)
+                _p(grp["design"]) if grp is not None else None, Pd, _p(ssw), st)
     if out.get("count_evals"):  # statistics only: (voxel, pair) windows evaluated
         out["pair_evals"] = out.get("pair_evals", 0) + c["evals"][cen.long()].sum()
     return counts
@@ -1005,6 +1030,7 @@ def graph_for(Y, X, grid, layout, proposal, *, recenter, do_scale, gls_kw, facto
     fk = tuple((k, None if v is None else v.key() if hasattr(v, "key") else np.asarray(v).tobytes())
                for k, v in sorted(factor_kw.items()))
     key = (tuple(Y.shape), tuple(X.shape), str(X.device), grid.a.tobytes(), grid.b.tobytes(), grid.lambda_fp32,
+           grid.ltop, None if grid.band is None else grid.band.tobytes(),
            layout.run_start.tobytes(), layout.tau.tobytes(), id(proposal.params), proposal.params._version,
            recenter, do_scale, tuple(sorted(gls_kw.items())), fk, not Y.is_cuda)
     gr = _GRAPHS.get(key)

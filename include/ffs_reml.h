@@ -612,12 +612,28 @@ int ffs_reml_window_items(int ncell, const int* cell_end, int n_a, int n_b, cons
  * voxel's centre for a re-centred round: best_cell when fallback = 1 and
  * best_cell >= 0, else n_a * n_b (no window). With design (grouped designs,
  * [V] each voxel's design), dcf is [n_designs][P] and c_p0 [n_designs], each
- * read at the row's design. */
+ * read at the row's design. With ssw_pre ([n][25], AFNI's banded R:
+ * ffs_reml_band_sums) y'R^-1 y of each window slot is read from it instead
+ * of the recurrence of coef. */
 int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, const int* idx, const int* center,
                     const int* tiles, const int* n_tiles, int max_tiles, const float* rows, const float* coef,
                     const float* winproj, const float* dcf, const unsigned char* ident, int p_id,
                     const double* c_p0, int* best, float* dbest, double* crit0, int* fallback, int* best_cell,
-                    int* next_center, const int* design, int P, void* stream);
+                    int* next_center, const int* design, int P, const float* ssw_pre, void* stream);
+
+/* y'R^-1 y of sorted rows under AFNI's banded R (ffs_grid_desc.band) for the
+ * learned-seeded refine, by the band's forward substitution of band_coef
+ * (row stride band_w, band[p] terms) over rows[idx[i]] (T samples, voxel-
+ * major). Window mode (tiles given, as ffs_reml_window_items leaves them):
+ * the rows of tile x, each pair of the 5 x 5 window of the tile's centre
+ * cell center[idx[first row]] that is valid and not an identity pair
+ * (ident), into out[i][slot] (25 slots, 5 * window row + window column).
+ * Strip mode (tiles NULL): the rows i < min(n, *n_dev) against the n_pairs
+ * pairs[q], into out[q][i] (row stride n). No reference counterpart. */
+int ffs_reml_band_sums(int n, const int* n_dev, int T, const int* idx, const float* rows, const float* band_coef,
+                       int band_w, const int* band, const int* tiles, const int* n_tiles, int max_tiles,
+                       const int* center, const int* lattice, int n_a, int n_b, const unsigned char* ident,
+                       const int* pairs, int n_pairs, float* out, void* stream);
 
 /* The strip next to the identity line in the learned-seeded refine (no
  * reference counterpart: the reference searches every pair). Near lambda = 0
@@ -633,10 +649,13 @@ int ffs_reml_window(int n, int T, int K, int n_a, int n_b, const int* lattice, c
  * 1e-6 |crit0[v]| gets fallback[v] = 1 and best_cell[v] = -1 (the full grid
  * decides); nothing else is written. With design (grouped designs, [V] each
  * voxel's design, P pairs per design) dcf is [n_designs][P], read at the
- * voxel's design; otherwise dcf is [P] and P is ignored. */
+ * voxel's design; otherwise dcf is [P] and P is ignored. With ssw_pre
+ * ([n_pairs][n], AFNI's banded R: ffs_reml_band_sums in strip mode) y'R^-1 y
+ * of each pair is read from it instead of the recurrence of coef. */
 int ffs_reml_strip(int n, const int* n_dev, int T, int K, int n_pairs, const int* pairs, const int* idx,
                    const float* rows, const float* coef, const float* proj, const float* dcf, const float* dbest,
-                   const double* crit0, int* fallback, int* best_cell, const int* design, int P, void* stream);
+                   const double* crit0, int* fallback, int* best_cell, const int* design, int P,
+                   const float* ssw_pre, void* stream);
 
 /* Work list of ffs_reml_project_tc_list for rows sorted into n_seg segments
  * (segment s: sorted rows [seg_end[s-1], seg_end[s]), seg_end[-1] = 0, as

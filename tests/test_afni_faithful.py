@@ -112,14 +112,68 @@ def test_afni_faithful_surface_differs_from_the_exact_r(afni_mode):
     assert np.abs(a.reml_likelihood.numpy() - b.reml_likelihood.numpy()).max() > 1e-6
 
 
-def test_afni_faithful_refuses_what_keeps_the_exact_r(afni_mode):
+def test_band_sums_match_the_dense_oracle(afni_mode):
+    """ffs_reml_band_sums (strip mode): y'R^-1 y of residualised rows at a
+    set of pairs by the band's forward substitution, against ||L^-1 y||^2
+    with the FP64 oracle's dense whitener."""
+    from fastfuncstuff_gb300 import _lib
+    from fastfuncstuff_gb300.glm import engine
+
+    d = load_golden("afni_faithful")
+    Y, X, kw = afni_faithful_case(d, "runs")
+    T = X.shape[0]
+    f = precompute_reml_grid(torch.from_numpy(X), T, d["a_grid"], d["b_grid"], DEV, run_starts=kw["run_starts"],
+                             use_double=True)
+    pre = engine.prep(torch.from_numpy(Y).to(DEV), f, want_yr_t=False, want_rows=True)
+    V = Y.shape[0]
+    pairs = np.arange(1, f.P, 7, dtype=np.int32)
+    ids = torch.arange(V, dtype=torch.int32, device=DEV)
+    count = torch.tensor([V], dtype=torch.int32, device=DEV)
+    pairs_d = torch.from_numpy(pairs).to(DEV)
+    out = torch.empty(len(pairs), V, dtype=torch.float32, device=DEV)
+    lib = _lib.load()
+    _lib.check(lib.ffs_reml_band_sums(V, count.data_ptr(), T, ids.data_ptr(), pre.rows.data_ptr(),
+                                      f.band_coef.data_ptr(), f.band_w, f.band.data_ptr(), None, None, 0, None, None,
+                                      0, 0, None, pairs_d.data_ptr(), len(pairs), out.data_ptr(),
+                                      torch.cuda.current_stream().cuda_stream), "ffs_reml_band_sums")
+    torch.cuda.synchronize()
+    og = o.valid_grid(d["a_grid"], d["b_grid"], np.float64)
+    po = o.precompute_reml_grid(X.astype(np.float64), og, run_starts=kw["run_starts"])
+    rows = pre.rows.cpu().numpy().astype(np.float64)
+    got = out.cpu().numpy()
+    for q, p in enumerate(pairs):
+        want = ((po.whiteners[int(p)].dense() @ rows.T) ** 2).sum(0)
+        np.testing.assert_allclose(got[q], want, rtol=2e-5, err_msg=f"pair {p}")
+
+
+def test_afni_faithful_learned_fit(afni_mode):
+    """The learned-seeded refine under the banded R: the window and strip
+    criteria read y'R^-1 y from ffs_reml_band_sums, the fallback and the GLS
+    run the banded full grid. The graph-replayed fit equals the eager one bit
+    for bit; its pairs agree with the exhaustive banded full grid, and where
+    they agree the GLS outputs are the full grid's and the likelihood agrees
+    to float32 rounding."""
     from fastfuncstuff_gb300.glm import learned
 
     d = load_golden("afni_faithful")
     Y, X, kw = afni_faithful_case(d, "runs")
-    prop = learned.ArmaProposal(learned.init_params(0, DEV))
-    with pytest.raises(NotImplementedError):
-        fit_glm_arma11(Y, X, tr=2.0, device=DEV, verbose=False, proposal=prop, **kw)
+    lay = G.run_layout(X.shape[0], kw["run_starts"])
+    prop, _ = learned.train_proposal(torch.from_numpy(X).to(DEV), lay, d["a_grid"], d["b_grid"],
+                                     n_voxels=200_000, epochs=6)
+    opts = dict(kw, device=DEV, verbose=False, want_residuals=True)
+    eager = fit_glm_arma11(Y, X, tr=2.0, proposal=prop, proposal_recenter=1, cuda_graphs=False, **opts)
+    graph = fit_glm_arma11(Y, X, tr=2.0, proposal=prop, proposal_recenter=1, cuda_graphs=True, **opts)
+    for name in ("arma_params", "reml_likelihood", "betas", "tstats", "sigma2", "residuals_whitened"):
+        np.testing.assert_array_equal(getattr(graph, name).numpy(), getattr(eager, name).numpy(), err_msg=name)
+    full = fit_glm_arma11(Y, X, tr=2.0, force_exhaustive_search=True, **opts)
+    same = (eager.arma_params == full.arma_params).all(1).numpy()
+    assert same.mean() >= 0.95, same.mean()
+    np.testing.assert_array_equal(eager.betas.numpy()[same], full.betas.numpy()[same])
+    np.testing.assert_allclose(eager.reml_likelihood.numpy()[same], full.reml_likelihood.numpy()[same], rtol=1e-5)
+    # the voxels the learned fit answers differently lie no lower than the
+    # full grid's optimum (a window holds no pair the full grid does not)
+    assert (eager.reml_likelihood.numpy() >= full.reml_likelihood.numpy() - 1e-5 *
+            np.abs(full.reml_likelihood.numpy())).all()
 
 
 @pytest.mark.parametrize("tag", ["two", "runs"])

@@ -27,6 +27,7 @@ STRUCTS = {
     "ffs_select_args": _lib.SelectArgs,
     "ffs_gls_args": _lib.GlsArgs,
     "ffs_merge_field": _lib.MergeField,
+    "ffs_dsort_args": _lib.DsortArgs,
 }
 
 
@@ -58,6 +59,35 @@ def test_ctypes_signatures_take_the_declared_number_of_arguments():
     for name, (argtypes, _) in _lib.SIGNATURES.items():
         assert name in arity, name
         assert len(argtypes) == arity[name], (name, len(argtypes), arity[name])
+
+
+def _kind_of_param(decl: str) -> str:
+    """pointer / int / size_t / uint64 / float of one declared parameter."""
+    if "*" in decl:
+        return "pointer"
+    words = decl.replace("const", " ").split()
+    ty = " ".join(words[:-1])
+    return {"int": "int", "size_t": "size_t", "uint64_t": "uint64", "float": "float"}.get(ty, ty)
+
+
+def _kind_of_ctype(ct) -> str:
+    import ctypes as C
+
+    if ct is C.c_void_p or ct is C.c_char_p or (isinstance(ct, type) and issubclass(ct, C._Pointer)):
+        return "pointer"
+    return {C.c_int: "int", C.c_size_t: "size_t", C.c_uint64: "uint64", C.c_float: "float"}.get(ct, str(ct))
+
+
+def test_ctypes_signatures_match_the_declared_parameter_types():
+    """Each argument's ctypes type has the kind of the declared parameter
+    (ctypes truncates an int passed where a pointer is declared without a
+    word, so a pointer typed c_int loses its upper half)."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    decls = {m.group(1): m.group(2) for m in re.finditer(r"\b(ffs_\w+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S)}
+    for name, (argtypes, _) in _lib.SIGNATURES.items():
+        params = [x.strip() for x in decls[name].split(",") if x.strip() not in ("", "void")]
+        for i, (decl, ct) in enumerate(zip(params, argtypes)):
+            assert _kind_of_param(decl) == _kind_of_ctype(ct), (name, i, decl, ct)
 
 
 def test_library_builds_loads_and_exports_every_symbol():
