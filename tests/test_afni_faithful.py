@@ -255,3 +255,28 @@ def test_afni_faithful_grouped_equals_per_group_fits(tag, exhaustive, afni_mode)
     check_selection(idx, ref.arma_index, ref.reml_lklhd_surface)
     same = idx == ref.arma_index
     assert rel_maxnorm(got.betas.numpy()[same], ref.betas[same]).max() <= BETA_REL
+
+
+def test_afni_faithful_grouped_learned_fit(afni_mode):
+    """The grouped designs' learned fit under the banded R (window and strip
+    sums from ffs_reml_band_sums, the grouped banded full grid for the
+    fallback): its pairs agree with the grouped exhaustive banded full grid,
+    and where they agree the GLS outputs are the full grid's."""
+    from fastfuncstuff_gb300 import fit_glm_arma11_grouped
+    from fastfuncstuff_gb300.glm import learned
+
+    d = load_golden("afni_faithful")
+    Y, X, kw = afni_faithful_case(d, "runs")
+    designs = _afni_designs(X)
+    gid = np.arange(Y.shape[0]) % 3
+    lay = G.run_layout(X.shape[0], kw["run_starts"])
+    fam = torch.from_numpy(np.stack([designs[h] for h in range(3)])).to(DEV)
+    prop, _ = learned.train_proposal(fam, lay, d["a_grid"], d["b_grid"], n_voxels=200_000, epochs=6)
+    opts = dict(kw, device=DEV, verbose=False)
+    got = fit_glm_arma11_grouped(Y, designs, gid, tr=2.0, proposal=prop, proposal_recenter=1, **opts)
+    full = fit_glm_arma11_grouped(Y, designs, gid, tr=2.0, force_exhaustive_search=True, **opts)
+    same = (got.arma_params == full.arma_params).all(1).numpy()
+    assert same.mean() >= 0.95, same.mean()
+    np.testing.assert_array_equal(got.betas.numpy()[same], full.betas.numpy()[same])
+    assert (got.reml_likelihood.numpy() >= full.reml_likelihood.numpy() - 1e-5 *
+            np.abs(full.reml_likelihood.numpy())).all()
