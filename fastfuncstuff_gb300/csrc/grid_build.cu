@@ -1099,7 +1099,9 @@ extern "C" int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out
   FFS_REQUIRE(d->run_start && d->tau && d->a && d->b && d->X, "ffs_grid_build_noalloc: null input");
   FFS_REQUIRE(o->coef && o->logdet_R && o->logdet_XtX && o->U && o->G && o->Adiag && o->XtX && o->info,
               "ffs_grid_build_noalloc: null output");
-  FFS_REQUIRE(!d->band, "ffs_grid_build_noalloc: the banded R is built by ffs_grid_build");
+  FFS_REQUIRE(!d->band || (d->band_w >= 1 && d->band_w <= FFS_BAND_MAX_W && o->band_L && o->band_coef),
+              "ffs_grid_build_noalloc: the banded R needs 1 <= band_w=%d <= %d, band_L and band_coef", d->band_w,
+              FFS_BAND_MAX_W);
   const size_t need = sizeof(double) * pair_doubles(d->T, d->K) * (size_t)d->P;
   if (need > kStaticGridScratchBytes) {
     set_error("ffs_grid_build_noalloc: T=%d K=%d P=%d needs %zu bytes of scratch, above the %zu-byte static "
@@ -1114,7 +1116,9 @@ extern "C" int ffs_grid_build_noalloc(const ffs_grid_desc* d, const ffs_grid_out
   // the previous call's contents need no clearing
   BuildArgs args{*d, *o};
   args.o.work = scratch;
-  const size_t smem = sizeof(double) * 4 * (size_t)d->T;
+  size_t smem = sizeof(double) * 4 * (size_t)d->T;  // as ffs_grid_build
+  if (d->band)
+    smem = std::max(smem, sizeof(double) * ((size_t)d->T + (d->T + 1) / 2 + (size_t)d->band_w + 1));
   FFS_REQUIRE(smem <= 200 * 1024, "ffs_grid_build_noalloc: T=%d too long", d->T);
   FFS_CUDA(ensure_dyn_smem(reinterpret_cast<const void*>(grid_build_kernel<false>), smem));
   grid_build_kernel<false><<<d->P, GB_THREADS, smem, (cudaStream_t)stream>>>(args, 1, nullptr, nullptr);

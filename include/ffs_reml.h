@@ -105,8 +105,7 @@ typedef struct {
    * with band, correlations at |tau_i - tau_j| > band[p] are zero and R is
    * factored as a band (band_L, band_coef below; coef is then the identity
    * and unused). band_w = max band[p] + 1 <= FFS_BAND_MAX_W; NULL band: the
-   * exact ARMA(1,1) R. ffs_grid_build and ffs_grid_build_designs (not the
-   * allocation-free build). */
+   * exact ARMA(1,1) R. */
   int band_w;
   const int* band;      /* device [P] or NULL                                    */
 } ffs_grid_desc;

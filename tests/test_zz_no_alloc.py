@@ -57,17 +57,24 @@ def _build(entry, g, lay, X, with_work):
         Adiag=torch.full((P, K), np.nan, **f32), XtX=torch.full((P, K, K), np.nan, **f32),
         info=torch.full((P,), -1, dtype=torch.int32, device=DEV), Gsum=torch.full((P, K), np.nan, **f32),
     )
+    band_w = 0
+    if g.band is not None:  # AFNI-faithful mode: R factored as a band
+        band_w = int(g.band.max()) + 1
+        keep["band"] = torch.from_numpy(g.band).to(DEV)
+        out["band_L"] = torch.full((P, T, band_w), np.nan, dtype=torch.float64, device=DEV)
+        out["band_coef"] = torch.full((P, T, band_w), np.nan, **f32)
     work = None
     if with_work:
         work = torch.empty(int(lib.ffs_grid_work_bytes(T, K, P)) // 8 + 1, dtype=torch.float64, device=DEV)
     p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
     d = _lib.GridDesc(T=T, K=K, P=P, n_runs=lay.n_runs, run_start=p(keep["rs"]), tau=p(keep["tau"]), a=p(keep["a"]),
                       b=p(keep["b"]), X=p(keep["X"]), lambda_fp32=0, ld_u=ld, n_task=0, task_idx=None, n_glt=0,
-                      glt=None)
+                      glt=None, band_w=band_w, band=p(keep.get("band")))
     o = _lib.GridOut(coef=p(out["coef"]), logdet_R=p(out["logdet_R"]), logdet_XtX=p(out["logdet_XtX"]), U=p(out["U"]),
                      U_hi=p(out["U_hi"]), U_lo=p(out["U_lo"]), uexp=p(out["uexp"]), G=p(out["G"]),
                      Adiag=p(out["Adiag"]), XtX=p(out["XtX"]), info=p(out["info"]), Ftask=None, glt_var=None,
-                     Gsum=p(out["Gsum"]), work=p(work))
+                     Gsum=p(out["Gsum"]), work=p(work), band_L=p(out.get("band_L")),
+                     band_coef=p(out.get("band_coef")))
     status = getattr(lib, entry)(C.byref(d), C.byref(o), torch.cuda.current_stream().cuda_stream)
     _lib.check(status, entry)
     torch.cuda.synchronize()
@@ -94,6 +101,23 @@ def test_noalloc_grid_build_matches_workspace_build_twice():
         ref = _build("ffs_grid_build", g, lay, X, with_work=True)
         got = _build("ffs_grid_build_noalloc", g, lay, X, with_work=False)
         _compare(ref, got)
+
+
+def test_noalloc_grid_build_matches_workspace_build_with_the_banded_r():
+    """AFNI-faithful mode: the banded R's factor (band_L, band_coef) from the
+    allocation-free build equals the workspace build's."""
+    from fastfuncstuff_gb300.glm import grid as G
+
+    G.set_afni_mode(True)
+    try:
+        g, lay, X = _inputs(160, 8, [0, 80], torch.linspace(-0.8, 0.8, 17), torch.linspace(-0.8, 0.8, 17), 4)
+        assert g.band is not None
+        ref = _build("ffs_grid_build", g, lay, X, with_work=True)
+        got = _build("ffs_grid_build_noalloc", g, lay, X, with_work=False)
+    finally:
+        G.set_afni_mode(False)
+    assert "band_L" in ref
+    _compare(ref, got)
 
 
 def test_noalloc_grid_build_rejects_oversized_problems():
