@@ -111,6 +111,21 @@ def test_argument_validation_needs_no_gpu():
     assert "null" in lib.ffs_last_error().decode()
     with pytest.raises(ValueError, match="ffs_reml_prep"):
         _lib.check(lib.ffs_reml_prep(None, None), "ffs_reml_prep")
+    fake = 256  # a non-null address no check reads
+    # the banded sums: a band wider than the limit; window mode without ident
+    st = lib.ffs_reml_band_sums(8, None, 16, fake, fake, fake, _lib.FFS_BAND_MAX_W + 1, fake, None, None, 0, None,
+                                None, 0, 0, None, fake, 1, fake, None)
+    assert st == _lib.FFS_ERR_INVALID and "ffs_reml_band_sums" in lib.ffs_last_error().decode()
+    st = lib.ffs_reml_band_sums(8, None, 16, fake, fake, fake, 3, fake, fake, fake, 4, fake, fake, 5, 5, None,
+                                None, 0, fake, None)
+    assert st == _lib.FFS_ERR_INVALID and "window mode" in lib.ffs_last_error().decode()
+    # a strip work list whose pair blocks exceed one 256-column MMA tile
+    st = lib.ffs_reml_segment_items(2, fake, 16, 20, 13, fake, fake, 64, fake, None)
+    assert st == _lib.FFS_ERR_INVALID and "ffs_reml_segment_items" in lib.ffs_last_error().decode()
+    # per-row designs need the pairs per design
+    st = lib.ffs_reml_strip(8, None, 16, 2, 4, fake, fake, fake, fake, fake, fake, fake, fake, fake, fake, fake, 0,
+                            None, None)
+    assert st == _lib.FFS_ERR_INVALID and "designs need P" in lib.ffs_last_error().decode()
 
 
 @pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")
