@@ -302,3 +302,30 @@ def test_parse_grid_arg_formats_and_errors(capsys):
             parse_grid_arg(bad)
         assert e.value.code == 1
         assert "ERROR" in capsys.readouterr().out
+
+
+@pytest.mark.parametrize("corcut", [1e-4, 1e-2])
+def test_afni_mode_grid_and_band_match_oracle(corcut):
+    """set_afni_mode(True, corcut): the near-white pairs (0 < lambda < corcut)
+    filtered out of the grid as the oracle filters them, AFNI's ltop, and each
+    pair's band of R
+    (the last lag with lam a^(g-1) above corcut) equal to the oracle's
+    afni_bmax; the exact R's grid comes back when the mode is switched off."""
+    a = b = torch.linspace(-0.8, 0.8, 17)
+    exact = G.make_grid(a, b)
+    G.set_afni_mode(True, corcut)
+    o.set_afni_mode(True, corcut)
+    try:
+        g = G.make_grid(a, b)
+        og = o.valid_grid(a.numpy(), b.numpy(), np.float32)
+        np.testing.assert_array_equal(g.a, og.a)
+        np.testing.assert_array_equal(g.b, og.b)
+        assert g.ltop == o._ltop(len(og.a_axis), len(og.b_axis), True)
+        want = np.array([o.afni_bmax(float(og.a[p]), float(og.lam[p]), corcut) for p in range(og.n)])
+        np.testing.assert_array_equal(g.band, want)
+        assert g.P <= exact.P and (g.band > 0).any()
+    finally:
+        G.set_afni_mode(False)
+        o.set_afni_mode(False)
+    again = G.make_grid(a, b)
+    assert again.band is None and again.P == exact.P
